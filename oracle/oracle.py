@@ -1,0 +1,223 @@
+"""TEST INFRASTRUCTURE -- ctypes front end of the CPU oracle.
+
+Builds ``oracle/_build/libhairfb_oracle.so`` from ``hairfb_oracle.c`` (gcc,
+``-O2 -ffp-contract=off``) and exposes one numpy function per reference pass.
+Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` use this module; the product never does.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "hairfb_oracle.c")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libhairfb_oracle.so")
+LIB_OMP = os.path.join(BUILD, "libhairfb_oracle_omp.so")
+
+_lock = threading.Lock()
+_lib = None
+
+CFLAGS = ["-O2", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+          "-Wall"]
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle (serial build) if the source is newer than the .so."""
+    os.makedirs(BUILD, exist_ok=True)
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
+        tmp = LIB + f".tmp{os.getpid()}"
+        subprocess.check_call(["gcc", *CFLAGS, "-o", tmp, SRC, "-lm"])
+        os.replace(tmp, LIB)
+    return LIB
+
+
+def load():
+    global _lib
+    with _lock:
+        if _lib is None:
+            _lib = ctypes.CDLL(build())
+            _declare(_lib)
+    return _lib
+
+
+def _declare(lib):
+    P = ctypes.c_void_p
+    U = ctypes.c_uint32
+    lib.oracle_sw_raster_test.argtypes = [P, P, P, P, P]
+    lib.oracle_tiles_pass.argtypes = [P, P, P, P, P, P, U, P, P, P]
+    lib.oracle_tile_sort.argtypes = [P, U, U, P, P, P]
+    lib.oracle_fine_pass.argtypes = [P, P, P, P, P, P, P, P, P, P, P]
+    lib.oracle_grid_pre_sim.argtypes = [P, P, P, P, U, P]
+    lib.oracle_sim_integrate.argtypes = [P, P, P, P, P, P, P, P, P, P, U]
+    lib.oracle_grid_post_sim.argtypes = [P, P, P, P, P, P]
+    lib.oracle_shading.argtypes = [P, P, P, P, P, P, P, U, U, P, U, P]
+    lib.oracle_sample_sdf.argtypes = [P, U, P, P, P]
+    lib.oracle_sample_sdf.restype = ctypes.c_float
+    lib.oracle_f32_to_f16.argtypes = [ctypes.c_float]
+    lib.oracle_f32_to_f16.restype = ctypes.c_uint16
+    lib.oracle_f16_to_f32.argtypes = [ctypes.c_uint16]
+    lib.oracle_f16_to_f32.restype = ctypes.c_float
+
+
+def _p(a):
+    if a is None:
+        return None
+    if isinstance(a, (bytes, bytearray)):
+        return ctypes.cast(ctypes.c_char_p(bytes(a)), ctypes.c_void_p)
+    if isinstance(a, ctypes.Structure):
+        return ctypes.cast(ctypes.pointer(a), ctypes.c_void_p)
+    assert a.flags["C_CONTIGUOUS"], "oracle arrays must be contiguous"
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class _Bytes:
+    """Keeps a bytes object alive while a pointer to it is in use."""
+
+    def __init__(self, b: bytes):
+        self.buf = ctypes.create_string_buffer(bytes(b), len(b))
+
+    @property
+    def ptr(self):
+        return ctypes.cast(self.buf, ctypes.c_void_p)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+# --------------------------------------------------------------------------
+# passes
+# --------------------------------------------------------------------------
+
+def sw_raster_test(uniforms: bytes, hair_data: bytes, positions, tangents, width, height):
+    lib = load()
+    out = np.zeros(width * height, np.uint32)
+    u, h = _Bytes(uniforms), _Bytes(hair_data)
+    lib.oracle_sw_raster_test(u.ptr, h.ptr, _p(_f32(positions)), _p(_f32(tangents)), _p(out))
+    return out
+
+
+def tiles_pass(cfg, uniforms: bytes, hair_data: bytes, positions, tangents, depth,
+               strands_to_render, width, height, max_drawn):
+    """Returns (tiles[T*B,4] u32, segments[1 + 2*maxDrawn] u32, seg_count[T] u32)."""
+    lib = load()
+    tx, ty = cfg.tile_count(width, height)
+    T = tx * ty
+    tiles = np.zeros((T * cfg.tile_depth_bins, 4), np.uint32)
+    segs = np.zeros(1 + 2 * max_drawn, np.uint32)
+    cnt = np.zeros(T, np.uint32)
+    c = cfg.to_c()
+    u, h = _Bytes(uniforms), _Bytes(hair_data)
+    lib.oracle_tiles_pass(_p(c), u.ptr, h.ptr, _p(_f32(positions)), _p(_f32(tangents)),
+                          _p(_f32(depth)), strands_to_render, _p(tiles), _p(segs), _p(cnt))
+    return tiles, segs, cnt
+
+
+def tile_sort(cfg, width, height, seg_count):
+    lib = load()
+    tx, ty = cfg.tile_count(width, height)
+    buckets = np.zeros(2 * cfg.sort_buckets, np.uint32)
+    tile_list = np.zeros(4 + tx * ty, np.uint32)
+    c = cfg.to_c()
+    lib.oracle_tile_sort(_p(c), width, height, _p(np.ascontiguousarray(seg_count, np.uint32)),
+                         _p(buckets), _p(tile_list))
+    return buckets, tile_list
+
+
+def fine_pass(cfg, uniforms: bytes, hair_data: bytes, positions, tangents, shading, depth,
+              tiles, segs, tile_list, width, height):
+    lib = load()
+    result = np.zeros(4 + 4 * width * height, np.float32)
+    c = cfg.to_c()
+    u, h = _Bytes(uniforms), _Bytes(hair_data)
+    lib.oracle_fine_pass(_p(c), u.ptr, h.ptr, _p(_f32(positions)), _p(_f32(tangents)),
+                         _p(_f32(shading)), _p(_f32(depth)),
+                         _p(np.ascontiguousarray(tiles, np.uint32)),
+                         _p(np.ascontiguousarray(segs, np.uint32)),
+                         _p(np.ascontiguousarray(tile_list, np.uint32)), _p(result))
+    return result
+
+
+def grid_pre_sim(cfg, sim_uniforms: bytes, dens_vel, sdf, sdf_dims):
+    lib = load()
+    G = cfg.grid_dims
+    out = np.zeros((G * G * G, 4), np.float32)
+    c = cfg.to_c()
+    u = _Bytes(sim_uniforms)
+    lib.oracle_grid_pre_sim(_p(c), u.ptr, _p(np.ascontiguousarray(dens_vel, np.int32)),
+                            _p(_f32(sdf)), sdf_dims, _p(out))
+    return out
+
+
+def sim_integrate(cfg, sim_uniforms: bytes, hair_data: bytes, prev, now, initial, seg_lengths,
+                  dens_vel, grad_wind, sdf, sdf_dims):
+    """Returns the new positions (written into a copy of ``prev``)."""
+    lib = load()
+    out = _f32(prev).copy()
+    c = cfg.to_c()
+    u, h = _Bytes(sim_uniforms), _Bytes(hair_data)
+    lib.oracle_sim_integrate(_p(c), u.ptr, h.ptr, _p(out), _p(_f32(now)), _p(_f32(initial)),
+                             _p(_f32(seg_lengths)), _p(np.ascontiguousarray(dens_vel, np.int32)),
+                             _p(_f32(grad_wind)), _p(_f32(sdf)), sdf_dims)
+    return out
+
+
+def grid_post_sim(cfg, sim_uniforms: bytes, hair_data: bytes, prev, now):
+    lib = load()
+    G = cfg.grid_dims
+    out = np.zeros((G * G * G, 4), np.int32)
+    c = cfg.to_c()
+    u, h = _Bytes(sim_uniforms), _Bytes(hair_data)
+    lib.oracle_grid_post_sim(_p(c), u.ptr, h.ptr, _p(_f32(prev)), _p(_f32(now)), _p(out))
+    return out
+
+
+def shading(cfg, uniforms: bytes, hair_data: bytes, positions, tangents, depth, strands,
+            ao=None, ao_size=(0, 0), shadow_map=None, shadow_size=0):
+    lib = load()
+    out = np.zeros((strands * cfg.shading_points, 4), np.float32)
+    c = cfg.to_c()
+    u, h = _Bytes(uniforms), _Bytes(hair_data)
+    lib.oracle_shading(_p(c), u.ptr, h.ptr, _p(_f32(positions)), _p(_f32(tangents)),
+                       _p(_f32(depth)), _p(None if ao is None else _f32(ao)),
+                       ao_size[0], ao_size[1],
+                       _p(None if shadow_map is None else _f32(shadow_map)), shadow_size, _p(out))
+    return out
+
+
+def sample_sdf(sdf, dims, bmin, bmax, p):
+    lib = load()
+    return lib.oracle_sample_sdf(_p(_f32(sdf)), dims, _p(_f32(bmin)), _p(_f32(bmax)), _p(_f32(p)))
+
+
+# --------------------------------------------------------------------------
+# helpers for comparing the reference-layout list buffers
+# --------------------------------------------------------------------------
+
+INVALID = 0xFFFFFFFF
+
+
+def walk_lists(tiles, segs, max_drawn):
+    """Walk every per-(tile, depth bin) linked list from its head.
+    Returns {tileBinIdx: [encoded (seg << 24 | strand), ...]} in list order."""
+    out = {}
+    data = segs[1:].reshape(-1, 2)
+    heads = tiles[:, 2]
+    for tb in np.nonzero(heads)[0]:
+        ptr = int(heads[tb]) - 1
+        seq = []
+        steps = 0
+        while ptr != INVALID and ptr < max_drawn:
+            seq.append(int(data[ptr, 0]))
+            ptr = int(data[ptr, 1])
+            steps += 1
+            if steps > data.shape[0]:
+                raise RuntimeError("cycle in a tile segment list")
+        out[int(tb)] = seq
+    return out
