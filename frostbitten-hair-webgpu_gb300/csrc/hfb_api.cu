@@ -1,0 +1,391 @@
+// C-ABI of libhairfb.so: context, buffers, validation and the pass entry
+// points declared in include/hairfb.h.  Every entry point converts CUDA and
+// argument errors into HFB_ERR_* codes plus a message; nothing throws across
+// the boundary.
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "hfb_internal.cuh"
+
+namespace {
+
+int fail(HfbCtx* c, int code, const std::string& msg) {
+  if (c) c->lastError = msg;
+  return code;
+}
+
+int cudaFail(HfbCtx* c, cudaError_t e, const char* what) {
+  return fail(c, HFB_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define HFB_CHECK_CTX(c)                                     \
+  do {                                                       \
+    if (!(c)) return HFB_ERR_INVALID_ARGUMENT;               \
+  } while (0)
+
+#define HFB_REQUIRE(c, cond, msg)                                   \
+  do {                                                              \
+    if (!(cond)) return fail((c), HFB_ERR_INVALID_ARGUMENT, (msg)); \
+  } while (0)
+
+#define HFB_LAUNCH(c, expr, what)                       \
+  do {                                                  \
+    cudaError_t e_ = (expr);                            \
+    if (e_ != cudaSuccess) return cudaFail((c), e_, (what)); \
+    return HFB_OK;                                      \
+  } while (0)
+
+bool isPow2(uint32_t v) { return v && !(v & (v - 1u)); }
+
+std::string validateConfig(const HfbConfig& c) {
+  if (c.tileSize != 8 && c.tileSize != 16 && c.tileSize != 32) return "tileSize must be 8, 16 or 32";
+  if (c.tileDepthBins < 1 || c.tileDepthBins > 64) return "tileDepthBins must be in [1, 64]";
+  if (c.slicesPerPixel < 1 || c.slicesPerPixel > 16) return "slicesPerPixel must be in [1, 16]";
+  if (c.tileSize == 32 && c.slicesPerPixel > 8) return "32x32 tiles support at most 8 slices";
+  if (c.shadingPoints < 2 || c.shadingPoints > 1024) return "shadingPoints must be in [2, 1024]";
+  if (c.gridDims < 2 || c.gridDims > 512) return "gridDims must be in [2, 512]";
+  if (c.sortBuckets < 1 || c.sortBuckets > 256) return "sortBuckets must be in [1, 256]";
+  if (c.sortBucketSize < 1) return "sortBucketSize must be >= 1";
+  if (c.avgFragmentsPerSlice < 1) return "avgFragmentsPerSlice must be >= 1";
+  if (!(c.alphaMultiplier == c.alphaMultiplier)) return "alphaMultiplier is NaN";
+  if (!(c.cameraNear > 0.0f) || !(c.cameraFar > c.cameraNear)) return "camera near/far invalid";
+  (void)isPow2;
+  return "";
+}
+
+std::string validateHair(const HfbHairData* h, uint32_t minPoints = 2) {
+  if (!h) return "hair data is NULL";
+  if (h->pointsPerStrand < minPoints || h->pointsPerStrand > 256)
+    return "pointsPerStrand must be in [" + std::to_string(minPoints) + ", 256]";
+  if (h->strandsCount >= (1u << 24)) return "strandsCount must be < 2^24 (segment encoding)";
+  return "";
+}
+
+bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+}  // namespace
+
+namespace hfb {
+
+uint32_t maxDrawnSegments(const HfbConfig& cfg, uint32_t W, uint32_t H) {
+  uint64_t t = (uint64_t)divCeil(W, cfg.tileSize) * divCeil(H, cfg.tileSize);
+  return (uint32_t)(1ull + t * cfg.avgSegmentsPerTile);
+}
+
+static size_t alignUp(size_t v) { return (v + 255u) & ~size_t(255u); }
+
+TilesScratch tilesScratchLayout(void* base, const HfbConfig& cfg, uint32_t W, uint32_t H,
+                                uint32_t maxDrawn) {
+  size_t T = (size_t)divCeil(W, cfg.tileSize) * divCeil(H, cfg.tileSize);
+  size_t TB = T * cfg.tileDepthBins;
+  size_t nBlocks = (TB + 2047) / 2048 + 1;
+  char* p = (char*)base;
+  TilesScratch s;
+  size_t off = 0;
+  s.binCount = (uint32_t*)(p + off); off = alignUp(off + TB * 4);
+  s.binOffset = (uint32_t*)(p + off); off = alignUp(off + TB * 4);
+  s.keys = (uint32_t*)(p + off); off = alignUp(off + (size_t)maxDrawn * 4);
+  s.blockSums = (uint32_t*)(p + off); off = alignUp(off + nBlocks * 4 + 16);
+  s.largeBins = (uint32_t*)(p + off); off = alignUp(off + (TB + 1) * 4);
+  s.bytes = off;
+  return s;
+}
+
+}  // namespace hfb
+
+extern "C" {
+
+int hfb_version(void) { return HFB_VERSION; }
+
+int hfb_ctx_create(const HfbConfig* cfg, int device, HfbCtx** out) {
+  if (!cfg || !out) return HFB_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  std::string err = validateConfig(*cfg);
+  if (!err.empty()) {
+    fprintf(stderr, "hairfb: invalid config: %s\n", err.c_str());
+    return HFB_ERR_INVALID_ARGUMENT;
+  }
+  HfbCtx* c = new (std::nothrow) HfbCtx();
+  if (!c) return HFB_ERR_OUT_OF_MEMORY;
+  c->cfg = *cfg;
+  cudaError_t e;
+  if (device >= 0) {
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) { delete c; return HFB_ERR_CUDA; }
+  }
+  cudaGetDevice(&c->device);
+  cudaDeviceGetAttribute(&c->smCount, cudaDevAttrMultiProcessorCount, c->device);
+  e = cudaStreamCreateWithFlags(&c->ownStream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { delete c; return HFB_ERR_CUDA; }
+  c->stream = c->ownStream;
+  e = cudaMalloc(&c->dCounters, sizeof(hfb::DeviceCounters));
+  if (e != cudaSuccess) { cudaStreamDestroy(c->ownStream); delete c; return HFB_ERR_OUT_OF_MEMORY; }
+  cudaMemsetAsync(c->dCounters, 0, sizeof(hfb::DeviceCounters), c->stream);
+  cudaStreamSynchronize(c->stream);
+  *out = c;
+  return HFB_OK;
+}
+
+int hfb_ctx_destroy(HfbCtx* c) {
+  HFB_CHECK_CTX(c);
+  cudaStreamSynchronize(c->stream);
+  if (c->dCounters) cudaFree(c->dCounters);
+  if (c->ownStream) cudaStreamDestroy(c->ownStream);
+  delete c;
+  return HFB_OK;
+}
+
+const char* hfb_last_error(const HfbCtx* c) { return c ? c->lastError.c_str() : "null context"; }
+
+int hfb_ctx_set_stream(HfbCtx* c, void* stream) {
+  HFB_CHECK_CTX(c);
+  c->stream = stream ? (cudaStream_t)stream : c->ownStream;
+  return HFB_OK;
+}
+
+int hfb_sync(HfbCtx* c) {
+  HFB_CHECK_CTX(c);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cudaFail(c, e, "hfb_sync");
+  return HFB_OK;
+}
+
+int hfb_get_counters(HfbCtx* c, HfbCounters* out) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, out, "out is NULL");
+  hfb::DeviceCounters d;
+  cudaError_t e = cudaMemcpyAsync(&d, c->dCounters, sizeof(d), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cudaFail(c, e, "hfb_get_counters");
+  memset(out, 0, sizeof(*out));
+  out->tileRecords = d.tileRecords;
+  out->tileRecordsDropped = d.tileRecordsDropped;
+  out->finePoolFullBins = d.finePoolFullBins;
+  out->waitTimeouts = d.waitTimeouts;
+  out->launches = c->launches;
+  return HFB_OK;
+}
+
+int hfb_buffer_alloc(HfbCtx* c, size_t bytes, void** out) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, out, "out is NULL");
+  *out = nullptr;
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc(out, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(c, HFB_ERR_OUT_OF_MEMORY, "cudaMalloc failed: " + std::string(cudaGetErrorString(e)));
+  }
+  return HFB_OK;
+}
+
+int hfb_buffer_free(HfbCtx* c, void* ptr) {
+  HFB_CHECK_CTX(c);
+  if (!ptr) return HFB_OK;
+  cudaStreamSynchronize(c->stream);
+  cudaError_t e = cudaFree(ptr);
+  if (e != cudaSuccess) return cudaFail(c, e, "cudaFree");
+  return HFB_OK;
+}
+
+int hfb_buffer_upload(HfbCtx* c, void* dst, const void* src, size_t bytes) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, dst && src, "NULL pointer");
+  HFB_LAUNCH(c, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream), "upload");
+}
+
+int hfb_buffer_download(HfbCtx* c, void* dst, const void* src, size_t bytes) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, dst && src, "NULL pointer");
+  cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cudaFail(c, e, "download");
+  return HFB_OK;
+}
+
+int hfb_buffer_clear(HfbCtx* c, void* dst, size_t bytes) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, dst, "NULL pointer");
+  HFB_LAUNCH(c, cudaMemsetAsync(dst, 0, bytes, c->stream), "clear");
+}
+
+size_t hfb_raster_scratch_bytes(const HfbConfig* cfg, uint32_t width, uint32_t height) {
+  if (!cfg || width == 0 || height == 0) return 0;
+  uint32_t md = hfb::maxDrawnSegments(*cfg, width, height);
+  return hfb::tilesScratchLayout(nullptr, *cfg, width, height, md).bytes;
+}
+
+int hfb_raster_buffers_alloc(HfbCtx* c, uint32_t W, uint32_t H, HfbRasterBuffers* rb) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, rb, "rb is NULL");
+  HFB_REQUIRE(c, W > 0 && H > 0 && W <= 16384 && H <= 16384, "viewport must be 1..16384 px");
+  memset(rb, 0, sizeof(*rb));
+  const HfbConfig& cfg = c->cfg;
+  size_t T = (size_t)hfb::divCeil(W, cfg.tileSize) * hfb::divCeil(H, cfg.tileSize);
+  uint64_t md = 1ull + (uint64_t)T * cfg.avgSegmentsPerTile;
+  HFB_REQUIRE(c, md < 0xFFFFFFF0ull, "maxDrawnHairSegments overflows u32");
+  rb->width = W;
+  rb->height = H;
+  rb->maxDrawnSegments = (uint32_t)md;
+  struct { void** p; size_t bytes; } req[] = {
+      {(void**)&rb->tiles, T * cfg.tileDepthBins * 16},
+      {(void**)&rb->tileSegments, 4 + (size_t)md * 8},
+      {(void**)&rb->segmentCountPerTile, T * 4},
+      {(void**)&rb->sortBuckets, (size_t)cfg.sortBuckets * 8},
+      {(void**)&rb->tileList, (4 + T) * 4},
+      {(void**)&rb->rasterizerResult, 16 + (size_t)W * H * 16},
+  };
+  for (auto& r : req) {
+    if (cudaMalloc(r.p, r.bytes) != cudaSuccess) {
+      cudaGetLastError();
+      hfb_raster_buffers_free(c, rb);
+      return fail(c, HFB_ERR_OUT_OF_MEMORY, "raster buffer allocation failed");
+    }
+  }
+  rb->scratchBytes = hfb_raster_scratch_bytes(&cfg, W, H);
+  if (cudaMalloc(&rb->scratch, rb->scratchBytes) != cudaSuccess) {
+    cudaGetLastError();
+    hfb_raster_buffers_free(c, rb);
+    return fail(c, HFB_ERR_OUT_OF_MEMORY, "raster scratch allocation failed");
+  }
+  cudaMemsetAsync(rb->scratch, 0, rb->scratchBytes, c->stream);
+  return hfb_clear_before_render(c, rb);
+}
+
+int hfb_raster_buffers_free(HfbCtx* c, HfbRasterBuffers* rb) {
+  HFB_CHECK_CTX(c);
+  if (!rb) return HFB_OK;
+  cudaStreamSynchronize(c->stream);
+  void* ps[] = {rb->tiles, rb->tileSegments, rb->segmentCountPerTile, rb->sortBuckets,
+                rb->tileList, rb->rasterizerResult, rb->scratch};
+  for (void* p : ps)
+    if (p) cudaFree(p);
+  memset(rb, 0, sizeof(*rb));
+  return HFB_OK;
+}
+
+static std::string checkRaster(const HfbCtx* c, const HfbRasterBuffers* rb) {
+  if (!rb) return "raster buffers are NULL";
+  if (!rb->tiles || !rb->tileSegments || !rb->segmentCountPerTile || !rb->sortBuckets ||
+      !rb->tileList || !rb->rasterizerResult || !rb->scratch)
+    return "a raster buffer is NULL";
+  if (rb->width == 0 || rb->height == 0) return "raster buffers have an empty viewport";
+  if (rb->scratchBytes < hfb_raster_scratch_bytes(&c->cfg, rb->width, rb->height))
+    return "raster scratch is too small";
+  if (rb->maxDrawnSegments != hfb::maxDrawnSegments(c->cfg, rb->width, rb->height))
+    return "maxDrawnSegments does not match the config";
+  return "";
+}
+
+static std::string checkViewport(const HfbUniforms* u, const HfbRasterBuffers* rb) {
+  if (!u) return "uniforms are NULL";
+  if (!(u->viewport.x == (float)rb->width) || !(u->viewport.y == (float)rb->height))
+    return "Uniforms.viewport does not match the raster buffers";
+  if (u->maxDrawnHairSegments != rb->maxDrawnSegments)
+    return "Uniforms.maxDrawnHairSegments does not match the raster buffers";
+  return "";
+}
+
+int hfb_clear_before_render(HfbCtx* c, HfbRasterBuffers* rb) {
+  HFB_CHECK_CTX(c);
+  std::string err = checkRaster(c, rb);
+  HFB_REQUIRE(c, err.empty(), err);
+  const HfbConfig& cfg = c->cfg;
+  size_t T = (size_t)hfb::divCeil(rb->width, cfg.tileSize) * hfb::divCeil(rb->height, cfg.tileSize);
+  cudaError_t e = cudaSuccess;
+  auto z = [&](void* p, size_t n) { if (e == cudaSuccess) e = cudaMemsetAsync(p, 0, n, c->stream); };
+  z(rb->tiles, T * cfg.tileDepthBins * 16);       // hairTilesPass.ts:48-52
+  z(rb->segmentCountPerTile, T * 4);
+  z(rb->tileSegments, 4);
+  z(rb->rasterizerResult, 16 + (size_t)rb->width * rb->height * 16);  // hairFinePass.ts:50-55
+  z(rb->tileList, 4);                             // hairTileSortPass.ts:63-68
+  z(rb->sortBuckets, (size_t)cfg.sortBuckets * 8);
+  if (e != cudaSuccess) return cudaFail(c, e, "clear_before_render");
+  c->launches += 6;
+  return HFB_OK;
+}
+
+int hfb_grid_pre_sim(HfbCtx* c, const HfbSimUniforms* u, const int32_t* dv, float* gw, const float* sdf,
+                     uint32_t sdfDims) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, u && dv && gw && sdf, "NULL argument");
+  HFB_REQUIRE(c, sdfDims >= 1 && sdfDims <= 1024, "sdfDims must be in [1, 1024]");
+  HFB_REQUIRE(c, aligned16(dv) && aligned16(gw), "grid buffers must be 16-byte aligned");
+  HFB_LAUNCH(c, hfb::launchGridPreSim(c, *u, dv, gw, sdf, sdfDims), "grid_pre_sim");
+}
+
+int hfb_sim_integrate(HfbCtx* c, const HfbSimUniforms* u, const HfbHairData* h, float* prev,
+                      const float* now, const float* initial, const float* segLen, const int32_t* dv,
+                      const float* gw, const float* sdf, uint32_t sdfDims) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, u && prev && now && initial && segLen && dv && gw && sdf, "NULL argument");
+  std::string err = validateHair(h, 4);  // the local shape constraint needs >= 4 points
+  HFB_REQUIRE(c, err.empty(), err);
+  HFB_REQUIRE(c, sdfDims >= 1 && sdfDims <= 1024, "sdfDims must be in [1, 1024]");
+  HFB_REQUIRE(c, u->constraintIterations <= 1024, "constraintIterations must be <= 1024");
+  HFB_REQUIRE(c, aligned16(prev) && aligned16(now) && aligned16(initial) && aligned16(dv) && aligned16(gw),
+              "vec4 buffers must be 16-byte aligned");
+  if (h->strandsCount == 0) return HFB_OK;
+  HFB_LAUNCH(c, hfb::launchSimIntegrate(c, *u, *h, prev, now, initial, segLen, dv, gw, sdf, sdfDims),
+             "sim_integrate");
+}
+
+int hfb_grid_post_sim(HfbCtx* c, const HfbSimUniforms* u, const HfbHairData* h, const float* prev,
+                      const float* now, int32_t* dv) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, u && prev && now && dv, "NULL argument");
+  std::string err = validateHair(h);
+  HFB_REQUIRE(c, err.empty(), err);
+  HFB_REQUIRE(c, aligned16(prev) && aligned16(now) && aligned16(dv), "vec4 buffers must be 16-byte aligned");
+  HFB_LAUNCH(c, hfb::launchGridPostSim(c, *u, *h, prev, now, dv), "grid_post_sim");
+}
+
+int hfb_shading(HfbCtx* c, const HfbUniforms* u, const HfbHairData* h, const float* pos,
+                const float* tan, const float* depth, const float* ao, uint32_t aoW, uint32_t aoH,
+                const float* sm, uint32_t smSize, float* shading) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, u && pos && tan && depth && shading, "NULL argument");
+  std::string err = validateHair(h);
+  HFB_REQUIRE(c, err.empty(), err);
+  HFB_REQUIRE(c, !ao || (aoW > 0 && aoH > 0), "AO texture with an empty size");
+  HFB_REQUIRE(c, !sm || smSize > 0, "shadow map with an empty size");
+  HFB_REQUIRE(c, u->viewport.x >= 1.0f && u->viewport.y >= 1.0f, "viewport is empty");
+  HFB_REQUIRE(c, aligned16(pos) && aligned16(tan) && aligned16(shading), "vec4 buffers must be 16-byte aligned");
+  if (h->strandsCount == 0) return HFB_OK;
+  HFB_LAUNCH(c, hfb::launchShading(c, *u, *h, pos, tan, depth, ao, aoW, aoH, sm, smSize, shading),
+             "shading");
+}
+
+int hfb_tiles_pass(HfbCtx* c, const HfbUniforms* u, const HfbHairData* h, const float* pos,
+                   const float* tan, const float* depth, uint32_t strandsToRender, HfbRasterBuffers* rb) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, pos && tan && depth, "NULL argument");
+  HFB_REQUIRE(c, aligned16(pos) && aligned16(tan), "vec4 buffers must be 16-byte aligned");
+  std::string err = validateHair(h);
+  if (err.empty()) err = checkRaster(c, rb);
+  if (err.empty()) err = checkViewport(u, rb);
+  HFB_REQUIRE(c, err.empty(), err);
+  HFB_LAUNCH(c, hfb::launchTilesPass(c, *u, *h, pos, tan, depth, strandsToRender, *rb), "tiles_pass");
+}
+
+int hfb_tile_sort(HfbCtx* c, HfbRasterBuffers* rb) {
+  HFB_CHECK_CTX(c);
+  std::string err = checkRaster(c, rb);
+  HFB_REQUIRE(c, err.empty(), err);
+  HFB_LAUNCH(c, hfb::launchTileSort(c, *rb), "tile_sort");
+}
+
+int hfb_fine_pass(HfbCtx* c, const HfbUniforms* u, const HfbHairData* h, const float* pos,
+                  const float* tan, const float* shading, const float* depth, HfbRasterBuffers* rb) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, pos && tan && shading && depth, "NULL argument");
+  HFB_REQUIRE(c, aligned16(pos) && aligned16(tan) && aligned16(shading), "vec4 buffers must be 16-byte aligned");
+  std::string err = validateHair(h);
+  if (err.empty()) err = checkRaster(c, rb);
+  if (err.empty()) err = checkViewport(u, rb);
+  HFB_REQUIRE(c, err.empty(), err);
+  HFB_LAUNCH(c, hfb::launchFinePass(c, *u, *h, pos, tan, shading, depth, *rb), "fine_pass");
+}
+
+}  // extern "C"

@@ -1,0 +1,387 @@
+// Simulation passes: GridPreSimPass, HairSimIntegrationPass, GridPostSimPass.
+//
+// Reference WGSL: src/passes/simulation/{gridPreSimPass,hairSimIntegrationPass,
+// gridPostSimPass}.wgsl.ts with shaderImpl/{integration,constraints,
+// collisions}.wgsl.ts and grids/*.wgsl.ts.  All arithmetic follows the fixed
+// fp32 order of hfb_math.cuh, so results are reproducible run to run; the
+// grid splat is integer (i32 fixed point, wrapping adds), hence order-free.
+#include "hfb_internal.cuh"
+#include "hfb_math.cuh"
+
+namespace hfb {
+namespace {
+
+constexpr float GRID_MUL = 1000000.0f;  // GRID_FLOAT_TO_U32_MUL, grids.wgsl.ts:3
+// SDF_SAMPLE_GRAD_OFFSET = SDF_CELL_SIZE * 0.1, collisions.wgsl.ts:23-24
+// (abstract-float constant expression, rounded once to f32)
+constexpr float SDF_GRAD_OFFSET = (float)(0.0033918858971446753 * 0.1);
+constexpr float FLOAT_EPSILON = 1e-7f;
+
+__device__ __forceinline__ int32_t gridEncode(float v) { return f2i(fmul(v, GRID_MUL)); }
+__device__ __forceinline__ float gridDecode(int32_t v) { return (float)v / GRID_MUL; }
+
+__device__ __forceinline__ uint32_t gridIdx(uint32_t G, uint32_t x, uint32_t y, uint32_t z) {
+  return clampu(z, 0u, G - 1u) * G * G + clampu(y, 0u, G - 1u) * G + clampu(x, 0u, G - 1u);
+}
+
+struct GridCo {
+  uint32_t mn[3], mx[3];
+  f3 p;
+};
+
+// _getGridCell, grids.wgsl.ts:43-56
+__device__ __forceinline__ GridCo gridCell(uint32_t G, f3 bmin, f3 bmax, f3 p) {
+  f3 t = sat3(div3(sub3(p, bmin), sub3(bmax, bmin)));
+  float g = (float)(G - 1u);
+  GridCo r;
+  r.p = mul3s(t, g);
+  r.mn[0] = f2u(floorf(r.p.x)); r.mn[1] = f2u(floorf(r.p.y)); r.mn[2] = f2u(floorf(r.p.z));
+  r.mx[0] = f2u(ceilf(r.p.x));  r.mx[1] = f2u(ceilf(r.p.y));  r.mx[2] = f2u(ceilf(r.p.z));
+  return r;
+}
+
+// _getGridCellWeights, grids.wgsl.ts:58-66
+__device__ __forceinline__ f3 cellWeights(uint32_t x, uint32_t y, uint32_t z, f3 p) {
+  return {clampf(fsub(1.0f, fabsf(fsub(p.x, (float)x))), 0.0f, 1.0f),
+          clampf(fsub(1.0f, fabsf(fsub(p.y, (float)y))), 0.0f, 1.0f),
+          clampf(fsub(1.0f, fabsf(fsub(p.z, (float)z))), 0.0f, 1.0f)};
+}
+
+// sampleSDFCollider (sdfCollider.ts:36-44) with the linear / clamp-to-edge
+// sampler of sdfUtils.ts:33-42, as an exact fp32 trilinear filter with texel
+// centres at (i + 0.5) / D.
+__device__ __forceinline__ float sampleSDF(const float* __restrict__ sdf, uint32_t D, f3 bmin, f3 bmax, f3 p) {
+  f3 t = sat3(div3(sub3(p, bmin), sub3(bmax, bmin)));
+  float fD = (float)D;
+  float u = fsub(fmul(t.x, fD), 0.5f), v = fsub(fmul(t.y, fD), 0.5f), w = fsub(fmul(t.z, fD), 0.5f);
+  float fu = floorf(u), fv = floorf(v), fw = floorf(w);
+  float ax = fsub(u, fu), ay = fsub(v, fv), az = fsub(w, fw);
+  int m = (int)D - 1;
+  int x0 = (int)fu, y0 = (int)fv, z0 = (int)fw;
+  int x1 = min(max(x0 + 1, 0), m), y1 = min(max(y0 + 1, 0), m), z1 = min(max(z0 + 1, 0), m);
+  x0 = min(max(x0, 0), m); y0 = min(max(y0, 0), m); z0 = min(max(z0, 0), m);
+  const size_t DD = (size_t)D * D;
+  auto T = [&](int x, int y, int z) { return __ldg(sdf + (size_t)z * DD + (size_t)y * D + x); };
+  float c00 = mixf(T(x0, y0, z0), T(x1, y0, z0), ax);
+  float c10 = mixf(T(x0, y1, z0), T(x1, y1, z0), ax);
+  float c01 = mixf(T(x0, y0, z1), T(x1, y0, z1), ax);
+  float c11 = mixf(T(x0, y1, z1), T(x1, y1, z1), ax);
+  return mixf(mixf(c00, c10, ay), mixf(c01, c11, ay), az);
+}
+
+__device__ __forceinline__ f3 gridMin(const HfbSimUniforms& u) {
+  return mk3(u.gridData.boundsMin.x, u.gridData.boundsMin.y, u.gridData.boundsMin.z);
+}
+__device__ __forceinline__ f3 gridMax(const HfbSimUniforms& u) {
+  return mk3(u.gridData.boundsMax[0], u.gridData.boundsMax[1], u.gridData.boundsMax[2]);
+}
+
+// ---------------------------------------------------------------------------
+// GridPreSimPass.main, gridPreSimPass.wgsl.ts:38-159 (one thread per node)
+// ---------------------------------------------------------------------------
+__global__ void gridPreSimKernel(const HfbSimUniforms u, uint32_t G, const int4* __restrict__ dv,
+                                 float4* __restrict__ gw, const float* __restrict__ sdf, uint32_t D) {
+  uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= G * G * G) return;
+  uint32_t z = id / (G * G);
+  uint32_t idXY = id - z * G * G;
+  uint32_t y = idXY / G, x = idXY % G;
+  f3 gmin = gridMin(u), gmax = gridMax(u);
+  f3 cell = div3s(sub3(gmax, gmin), (float)(G - 1u));
+  f3 pos = add3(gmin, mul3(cell, mk3((float)x, (float)y, (float)z)));
+  f3 smin = mk3(u.sdf.boundsMin.x, u.sdf.boundsMin.y, u.sdf.boundsMin.z);
+  f3 smax = mk3(u.sdf.boundsMax.x, u.sdf.boundsMax.y, u.sdf.boundsMax.z);
+  // getWindStrength, :89-108
+  float wind;
+  float d = sampleSDF(sdf, D, smin, smax, pos);
+  if (d < 0.0f) {
+    wind = 0.0f;
+  } else {
+    f3 nd = norm3(mk3(u.wind.x, u.wind.y, u.wind.z));
+    f3 toward = mk3(-nd.x, -nd.y, -nd.z);
+    f3 rp = add3(pos, mul3s(mul3s(toward, d), u.windColisionTraceOffset));
+    wind = sampleSDF(sdf, D, smin, smax, rp) < 0.0f ? 0.5f : 1.0f;
+  }
+  // getDensityGradient, :111-159
+  uint32_t idx0 = gridIdx(G, x, y, z);
+  float d0 = gridDecode(__ldg(&dv[idx0].w));
+  f3 g = mk3(0.0f, 0.0f, 0.0f);
+  const int off[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    int ox = (int)x + off[k][0], oy = (int)y + off[k][1], oz = (int)z + off[k][2];
+    f3 r = mk3(0.0f, 0.0f, 0.0f);
+    if (!(ox < 0 || oy < 0 || oz < 0)) {
+      uint32_t idxO = gridIdx(G, (uint32_t)ox, (uint32_t)oy, (uint32_t)oz);
+      if (idxO != idx0) {
+        float dO = gridDecode(__ldg(&dv[idxO].w));
+        float m = fmaxf(fsub(d0, dO), 0.0f);
+        r = mul3s(mk3((float)off[k][0], (float)off[k][1], (float)off[k][2]), m);
+      }
+    }
+    g = add3(g, r);
+  }
+  gw[idx0] = make_float4(g.x, g.y, g.z, wind);
+}
+
+// ---------------------------------------------------------------------------
+// HairSimIntegrationPass.main, hairSimIntegrationPass.wgsl.ts:79-273
+//
+// One thread per strand for the Gauss-Seidel constraint chains (length and
+// local shape must stay sequential along the strand).  The strand points
+// live in shared memory laid out [point][strand] (conflict-free).  The
+// Verlet step and the write-back run point-parallel over the whole block so
+// the position buffers are read and written fully coalesced.
+// ---------------------------------------------------------------------------
+constexpr int SIM_STRANDS_PER_BLOCK = 64;
+
+__global__ void __launch_bounds__(SIM_STRANDS_PER_BLOCK)
+simIntegrateKernel(const HfbSimUniforms u, uint32_t S, uint32_t P, uint32_t G,
+                   float4* __restrict__ prev, const float4* __restrict__ now,
+                   const float4* __restrict__ initial, const float* __restrict__ segLen,
+                   const int4* __restrict__ dv, const float4* __restrict__ gw,
+                   const float* __restrict__ sdf, uint32_t D) {
+  extern __shared__ float4 wk[];  // [P][SIM_STRANDS_PER_BLOCK]
+  const uint32_t NB = SIM_STRANDS_PER_BLOCK;
+  const uint32_t s0 = blockIdx.x * NB;
+  const uint32_t nStr = min(NB, S - s0);
+  const uint32_t nPts = nStr * P;
+  const f3 gmin = gridMin(u), gmax = gridMax(u);
+
+  // --- Verlet + forces, point-parallel (:125-162) ---
+  for (uint32_t i = threadIdx.x; i < nPts; i += blockDim.x) {
+    uint32_t ls = i / P, pt = i - ls * P;
+    uint32_t strand = s0 + ls;
+    size_t gi = (size_t)s0 * P + i;
+    f4 posNow = ld4(__ldg(&now[gi]));
+    if (pt == 0) {
+      wk[pt * NB + ls] = make_float4(posNow.x, posNow.y, posNow.z, posNow.w);
+      continue;
+    }
+    f4 posPrev = ld4(prev[gi]);
+    f3 force = mk3(0.0f, -u.gravity, 0.0f);
+    f3 pn = xyz(posNow);
+    // _getGridDensityGradAndWind + _getGridDensityVelocity (same cell, two grids)
+    GridCo co = gridCell(G, gmin, gmax, pn);
+    f3 grad = mk3(0.f, 0.f, 0.f), vel = mk3(0.f, 0.f, 0.f);
+    float windStr = 0.0f, dens = 0.0f;
+    for (uint32_t z = co.mn[2]; z <= co.mx[2]; z++)
+      for (uint32_t y = co.mn[1]; y <= co.mx[1]; y++)
+        for (uint32_t x = co.mn[0]; x <= co.mx[0]; x++) {
+          f3 w = cellWeights(x, y, z, co.p);
+          float wl = len3(w);
+          uint32_t idx = gridIdx(G, x, y, z);
+          float4 a = __ldg(&gw[idx]);
+          grad = add3(grad, mul3(w, mk3(a.x, a.y, a.z)));
+          windStr = fadd(windStr, fmul(wl, a.w));
+          int4 b = __ldg(&dv[idx]);
+          vel = add3(vel, mul3(w, mk3(gridDecode(b.x), gridDecode(b.y), gridDecode(b.z))));
+          dens = fadd(dens, fmul(wl, gridDecode(b.w)));
+        }
+    float timer = fadd(fmul((float)u.frameIdx, 0.73f), fmul(u.windPhaseOffset, (float)strand));
+    float windJitter = fractf(fmul(timer, u.windStrengthFrequency));
+    float jitterDelta = mixf(fmul(-0.5f, u.windStrengthJitter), fmul(0.5f, u.windStrengthJitter), windJitter);
+    float jitterStr = fadd(1.0f, jitterDelta);
+    float windCellStr = sat(mixf(u.windStrengthLull, 1.0f, windStr));
+    force = add3(force, mul3s(mk3(u.wind.x, u.wind.y, u.wind.z),
+                              fabsf(fmul(fmul(u.wind.w, jitterStr), windCellStr))));
+    force = add3(force, mul3s(grad, u.volumePreservation));
+    f3 gridDisp = dens > 0.0f ? div3s(vel, dens) : mk3(0.f, 0.f, 0.f);
+    // verletIntegration, integration.wgsl.ts:8-28
+    float dt = u.deltaTime;
+    f3 pd = sub3(pn, xyz(posPrev));
+    f3 fpd = mix3(pd, gridDisp, u.friction);
+    f3 nxt = add3(add3(pn, fpd), mul3s(mul3s(force, dt), dt));
+    f3 r = mix3(xyz(posPrev), nxt, posNow.w);
+    wk[pt * NB + ls] = make_float4(r.x, r.y, r.z, posNow.w);
+  }
+  __syncthreads();
+
+  const uint32_t ls = threadIdx.x;
+  if (ls < nStr) {
+    const uint32_t strand = s0 + ls;
+    const size_t base = (size_t)strand * P;
+    const uint32_t iters = u.constraintIterations;
+    const f3 smin = mk3(u.sdf.boundsMin.x, u.sdf.boundsMin.y, u.sdf.boundsMin.z);
+    const f3 smax = mk3(u.sdf.boundsMax.x, u.sdf.boundsMax.y, u.sdf.boundsMax.z);
+    const float sdfOffset = u.sdf.boundsMax.w;
+    const f4 sph = mk4(u.collisionSphere.x, u.collisionSphere.y, u.collisionSphere.z, u.collisionSphere.w);
+#define WK(j) wk[(j) * NB + ls]
+    for (uint32_t it = 0; it < iters; it++) {
+      // length constraint (Gauss-Seidel), :176-190, constraints.wgsl.ts:5-28
+      const float kLen = u.stiffnessLengthConstr;
+      float4 a = WK(0);
+      for (uint32_t j = 0; j + 1u < P; j++) {
+        float4 b = WK(j + 1u);
+        float expected = __ldg(&segLen[base + j]);
+        float w0 = a.w, w1 = b.w;
+        f3 tng = mk3(fsub(b.x, a.x), fsub(b.y, a.y), fsub(b.z, a.z));
+        float actual = len3(tng);
+        float corr = fsub(1.0f, expected / actual);
+        float df = fmul(corr, kLen) / fadd(fadd(w0, w1), FLOAT_EPSILON);
+        f3 delta = mul3s(tng, df);
+        a.x = fadd(a.x, fmul(delta.x, w0)); a.y = fadd(a.y, fmul(delta.y, w0)); a.z = fadd(a.z, fmul(delta.z, w0));
+        b.x = fsub(b.x, fmul(w1, delta.x)); b.y = fsub(b.y, fmul(w1, delta.y)); b.z = fsub(b.z, fmul(w1, delta.z));
+        WK(j) = a;
+        WK(j + 1u) = b;
+        a = b;
+      }
+      // global shape, :193-206, constraints.wgsl.ts:31-49
+      const float kGlob = u.stiffnessGlobalConstr / (float)iters;
+      for (uint32_t j = 1; j < P; j++) {
+        float x = (float)j / (float)(P - 1u);
+        float att = fsub(1.0f, sat(fsub(x, u.globalConstrExtent) / u.globalConstrFade));
+        float4 pi = __ldg(&initial[base + j]);
+        float k = fmul(kGlob, att);
+        float4 p = WK(j);
+        f3 dvv = mk3(fsub(pi.x, p.x), fsub(pi.y, p.y), fsub(pi.z, p.z));
+        f3 d = mul3s(mul3s(dvv, p.w), k);
+        p.x = fadd(p.x, d.x); p.y = fadd(p.y, d.y); p.z = fadd(p.z, d.z);
+        WK(j) = p;
+      }
+      // local shape (triangle bending, Gauss-Seidel), :209-232, constraints.wgsl.ts:54-120
+      const float kLoc = u.stiffnessLocalConstr / (float)iters;
+      uint32_t jj = 0;
+      for (; jj + 3u < P; jj++) {
+        float4 i0 = __ldg(&initial[base + jj]), i1 = __ldg(&initial[base + jj + 1u]),
+               i2 = __ldg(&initial[base + jj + 2u]);
+        f3 cI = div3s(add3(add3(mk3(i0.x, i0.y, i0.z), mk3(i1.x, i1.y, i1.z)), mk3(i2.x, i2.y, i2.z)), 3.0f);
+        float h0 = len3(sub3(cI, mk3(i1.x, i1.y, i1.z)));
+        float4 p0 = WK(jj), p1 = WK(jj + 1u), p2 = WK(jj + 2u);
+        f3 c = div3s(add3(add3(mk3(p0.x, p0.y, p0.z), mk3(p1.x, p1.y, p1.z)), mk3(p2.x, p2.y, p2.z)), 3.0f);
+        f3 hv = sub3(mk3(p1.x, p1.y, p1.z), c);
+        float h = len3(hv);
+        float wT = fadd(fadd(i0.w, fmul(2.0f, i1.w)), i2.w);
+        float w0 = fmul(i0.w / wT, 2.0f), w1 = fmul(i1.w / wT, -4.0f), w2 = fmul(i2.w / wT, 2.0f);
+        f3 delta = mul3s(hv, fsub(1.0f, h0 / h));
+        f3 d0 = mul3s(delta, fmul(kLoc, w0)), d1 = mul3s(delta, fmul(kLoc, w1)), d2 = mul3s(delta, fmul(kLoc, w2));
+        p0.x = fadd(p0.x, d0.x); p0.y = fadd(p0.y, d0.y); p0.z = fadd(p0.z, d0.z);
+        p1.x = fadd(p1.x, d1.x); p1.y = fadd(p1.y, d1.y); p1.z = fadd(p1.z, d1.z);
+        p2.x = fadd(p2.x, d2.x); p2.y = fadd(p2.y, d2.y); p2.z = fadd(p2.z, d2.z);
+        WK(jj) = p0;
+        WK(jj + 1u) = p1;
+        WK(jj + 2u) = p2;
+      }
+      for (; jj < P; jj++) {  // applyConstraint_matchInitialTangent
+        float4 i0 = __ldg(&initial[base + jj - 1u]), i1 = __ldg(&initial[base + jj]);
+        f3 tI = mk3(fsub(i1.x, i0.x), fsub(i1.y, i0.y), fsub(i1.z, i0.z));
+        float4 p0 = WK(jj - 1u), p1 = WK(jj);
+        f3 proj = add3(mk3(p0.x, p0.y, p0.z), tI);
+        f3 delta = sub3(proj, mk3(p1.x, p1.y, p1.z));
+        f3 d = mul3s(delta, fmul(kLoc, p1.w));
+        p1.x = fadd(p1.x, d.x); p1.y = fadd(p1.y, d.y); p1.z = fadd(p1.z, d.z);
+        WK(jj) = p1;
+      }
+      // collisions, :236-261, collisions.wgsl.ts:4-61
+      const float kColl = u.stiffnessCollisions / (float)iters;
+      const float kSdf = u.stiffnessSDF / (float)iters;
+      for (uint32_t j = 1; j < P; j++) {
+        float4 pos = WK(j);
+        {
+          f3 v = mk3(fsub(pos.x, sph.x), fsub(pos.y, sph.y), fsub(pos.z, sph.z));
+          float dist = fsub(len3(v), sph.w);
+          float dts = fmaxf(0.0f, -dist);
+          f3 d = mul3s(mul3s(norm3(v), dts), kColl);
+          pos.x = fadd(pos.x, d.x); pos.y = fadd(pos.y, d.y); pos.z = fadd(pos.z, d.z);
+        }
+        if (j > 2u) {
+          f3 p = mk3(pos.x, pos.y, pos.z);
+          float d = sampleSDF(sdf, D, smin, smax, p);
+          float dOff = fadd(d, sdfOffset);
+          if (!(dOff >= 0.0f)) {
+            const float o = SDF_GRAD_OFFSET;
+            f3 cd;
+            cd.x = sampleSDF(sdf, D, smin, smax, add3(p, mk3(fmul(o, 1.0f), fmul(o, 0.0f), fmul(o, 0.0f))));
+            cd.y = sampleSDF(sdf, D, smin, smax, add3(p, mk3(fmul(o, 0.0f), fmul(o, 1.0f), fmul(o, 0.0f))));
+            cd.z = sampleSDF(sdf, D, smin, smax, add3(p, mk3(fmul(o, 0.0f), fmul(o, 0.0f), fmul(o, 1.0f))));
+            cd = sub3(cd, mk3(d, d, d));
+            f3 corr = mul3s(norm3(cd), -dOff);
+            f3 dd = mul3s(corr, kSdf);
+            pos.x = fadd(pos.x, dd.x); pos.y = fadd(pos.y, dd.y); pos.z = fadd(pos.z, dd.z);
+          }
+        }
+        WK(j) = pos;
+      }
+    }
+#undef WK
+  }
+  __syncthreads();
+  // --- write back into the PREV buffer, coalesced (:268-272) ---
+  for (uint32_t i = threadIdx.x; i < nPts; i += blockDim.x) {
+    uint32_t l = i / P, pt = i - l * P;
+    prev[(size_t)s0 * P + i] = wk[pt * NB + l];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// GridPostSimPass.main, gridPostSimPass.wgsl.ts:45-72 with
+// _addGridDensityVelocity, densityVelocityGrid.wgsl.ts:93-124.
+// One thread per point; i32 atomics (wrapping, order-independent).
+// ---------------------------------------------------------------------------
+__global__ void gridPostSimKernel(const HfbSimUniforms u, uint32_t N, uint32_t G,
+                                  const float4* __restrict__ prev, const float4* __restrict__ now,
+                                  int* __restrict__ dv) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  float4 a = __ldg(&prev[i]), b = __ldg(&now[i]);
+  f3 pn = mk3(b.x, b.y, b.z);
+  f3 vel = sub3(pn, mk3(a.x, a.y, a.z));
+  GridCo co = gridCell(G, gridMin(u), gridMax(u), pn);
+  for (uint32_t z = co.mn[2]; z <= co.mx[2]; z++)
+    for (uint32_t y = co.mn[1]; y <= co.mx[1]; y++)
+      for (uint32_t x = co.mn[0]; x <= co.mx[0]; x++) {
+        uint32_t idx = gridIdx(G, x, y, z);
+        f3 w = cellWeights(x, y, z, co.p);
+        f3 cv = mul3(vel, w);
+        int* c = dv + 4u * idx;
+        atomicAdd(c + 0, gridEncode(cv.x));
+        atomicAdd(c + 1, gridEncode(cv.y));
+        atomicAdd(c + 2, gridEncode(cv.z));
+        atomicAdd(c + 3, gridEncode(len3(w)));
+      }
+}
+
+}  // namespace
+
+cudaError_t launchGridPreSim(HfbCtx* c, const HfbSimUniforms& u, const int32_t* dv, float* gw,
+                             const float* sdf, uint32_t sdfDims) {
+  uint32_t G = c->cfg.gridDims;
+  uint32_t n = G * G * G;
+  gridPreSimKernel<<<divCeil(n, 256), 256, 0, c->stream>>>(u, G, (const int4*)dv, (float4*)gw, sdf, sdfDims);
+  c->launches += 1;
+  return cudaGetLastError();
+}
+
+cudaError_t launchSimIntegrate(HfbCtx* c, const HfbSimUniforms& u, const HfbHairData& h, float* prev,
+                               const float* now, const float* initial, const float* segLen,
+                               const int32_t* dv, const float* gw, const float* sdf, uint32_t sdfDims) {
+  uint32_t S = h.strandsCount, P = h.pointsPerStrand;
+  size_t smem = (size_t)P * SIM_STRANDS_PER_BLOCK * sizeof(float4);
+  static bool attrSet = false;
+  if (!attrSet) {
+    cudaFuncSetAttribute(simIntegrateKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 256 * 64 * 16);
+    attrSet = true;
+  }
+  simIntegrateKernel<<<divCeil(S, SIM_STRANDS_PER_BLOCK), SIM_STRANDS_PER_BLOCK, smem, c->stream>>>(
+      u, S, P, c->cfg.gridDims, (float4*)prev, (const float4*)now, (const float4*)initial, segLen,
+      (const int4*)dv, (const float4*)gw, sdf, sdfDims);
+  c->launches += 1;
+  return cudaGetLastError();
+}
+
+cudaError_t launchGridPostSim(HfbCtx* c, const HfbSimUniforms& u, const HfbHairData& h, const float* prev,
+                              const float* now, int32_t* dv) {
+  uint32_t G = c->cfg.gridDims;
+  cudaError_t e = cudaMemsetAsync(dv, 0, (size_t)G * G * G * 16, c->stream);  // clearDensityVelocityBuffer
+  if (e != cudaSuccess) return e;
+  uint32_t N = h.strandsCount * h.pointsPerStrand;
+  if (N) {
+    gridPostSimKernel<<<divCeil(N, 256), 256, 0, c->stream>>>(u, N, G, (const float4*)prev,
+                                                               (const float4*)now, dv);
+    c->launches += 1;
+  }
+  c->launches += 1;
+  return cudaGetLastError();
+}
+
+}  // namespace hfb

@@ -1,0 +1,162 @@
+"""ctypes bindings of libhairfb.so (include/hairfb.h).
+
+The library is the only compute path: if it is missing or does not load,
+every entry point here raises -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from .config import HfbConfig
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libhairfb.so")
+
+HFB_OK = 0
+HFB_ERR_INVALID_ARGUMENT = -1
+HFB_ERR_OUT_OF_MEMORY = -2
+HFB_ERR_CUDA = -3
+HFB_ERR_TIMEOUT = -5
+HFB_ERR_UNSUPPORTED = -6
+
+
+class HfbError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"hairfb error {code}: {msg}")
+        self.code = code
+
+
+class HfbHairData(ctypes.Structure):
+    _fields_ = [("boundingSphere", ctypes.c_float * 4), ("strandsCount", ctypes.c_uint32),
+                ("pointsPerStrand", ctypes.c_uint32), ("padding", ctypes.c_uint32 * 2)]
+
+
+class HfbRasterBuffers(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("maxDrawnSegments", ctypes.c_uint32), ("reserved0", ctypes.c_uint32),
+                ("tiles", ctypes.c_void_p), ("tileSegments", ctypes.c_void_p),
+                ("segmentCountPerTile", ctypes.c_void_p), ("sortBuckets", ctypes.c_void_p),
+                ("tileList", ctypes.c_void_p), ("rasterizerResult", ctypes.c_void_p),
+                ("scratch", ctypes.c_void_p), ("scratchBytes", ctypes.c_size_t)]
+
+
+class HfbCounters(ctypes.Structure):
+    _fields_ = [("tileRecords", ctypes.c_uint64), ("tileRecordsDropped", ctypes.c_uint64),
+                ("finePoolFullBins", ctypes.c_uint64), ("waitTimeouts", ctypes.c_uint64),
+                ("launches", ctypes.c_uint64), ("reserved", ctypes.c_uint64 * 3)]
+
+
+assert ctypes.sizeof(HfbHairData) == 32
+assert ctypes.sizeof(HfbCounters) == 64
+
+# every symbol include/hairfb.h declares: name -> (restype, argtypes)
+P, U32, SZ, I = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_size_t, ctypes.c_int
+SIGNATURES = {
+    "hfb_version": (I, []),
+    "hfb_ctx_create": (I, [P, I, P]),
+    "hfb_ctx_destroy": (I, [P]),
+    "hfb_last_error": (ctypes.c_char_p, [P]),
+    "hfb_ctx_set_stream": (I, [P, P]),
+    "hfb_sync": (I, [P]),
+    "hfb_get_counters": (I, [P, P]),
+    "hfb_buffer_alloc": (I, [P, SZ, P]),
+    "hfb_buffer_free": (I, [P, P]),
+    "hfb_buffer_upload": (I, [P, P, P, SZ]),
+    "hfb_buffer_download": (I, [P, P, P, SZ]),
+    "hfb_buffer_clear": (I, [P, P, SZ]),
+    "hfb_raster_scratch_bytes": (SZ, [P, U32, U32]),
+    "hfb_raster_buffers_alloc": (I, [P, U32, U32, P]),
+    "hfb_raster_buffers_free": (I, [P, P]),
+    "hfb_grid_pre_sim": (I, [P, P, P, P, P, U32]),
+    "hfb_sim_integrate": (I, [P, P, P, P, P, P, P, P, P, P, U32]),
+    "hfb_grid_post_sim": (I, [P, P, P, P, P, P]),
+    "hfb_shading": (I, [P, P, P, P, P, P, P, U32, U32, P, U32, P]),
+    "hfb_clear_before_render": (I, [P, P]),
+    "hfb_tiles_pass": (I, [P, P, P, P, P, P, U32, P]),
+    "hfb_tile_sort": (I, [P, P]),
+    "hfb_fine_pass": (I, [P, P, P, P, P, P, P, P]),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def open_library(path: str):
+    """Opens a libhairfb.so and declares every entry point; raises if it is
+    absent (no fallback path exists)."""
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"{path} is missing: build it with `python -m hairfb.build` (needs nvcc)")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+def load(path: str = LIB_PATH):
+    """The process-wide libhairfb.so."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            _lib = open_library(path)
+    return _lib
+
+
+def ptr(x) -> int | None:
+    """Device address of a torch tensor (or pass-through int / None)."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    return x.data_ptr()
+
+
+def byref(s):
+    return ctypes.cast(ctypes.pointer(s), ctypes.c_void_p)
+
+
+class Context:
+    """Owns one HfbCtx (a CUDA stream + the pass constants)."""
+
+    def __init__(self, cfg: HfbConfig, device: int = -1):
+        self.lib = load()
+        self.cfg = cfg
+        h = ctypes.c_void_p()
+        rc = self.lib.hfb_ctx_create(byref(cfg), device, ctypes.byref(h))
+        if rc != HFB_OK:
+            raise HfbError(rc, "hfb_ctx_create failed (invalid config or CUDA error)")
+        self.handle = h
+
+    def check(self, rc: int) -> None:
+        if rc != HFB_OK:
+            msg = self.lib.hfb_last_error(self.handle)
+            raise HfbError(rc, msg.decode() if msg else "")
+
+    def call(self, name: str, *args) -> None:
+        self.check(getattr(self.lib, name)(self.handle, *args))
+
+    def set_stream(self, stream) -> None:
+        """Run on a torch.cuda.Stream (or raw cudaStream_t int); None = own stream."""
+        s = None if stream is None else (stream if isinstance(stream, int) else stream.cuda_stream)
+        self.call("hfb_ctx_set_stream", s)
+
+    def sync(self) -> None:
+        self.call("hfb_sync")
+
+    def counters(self) -> dict:
+        c = HfbCounters()
+        self.call("hfb_get_counters", byref(c))
+        return {k: getattr(c, k) for k, _ in HfbCounters._fields_ if k != "reserved"}
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.lib.hfb_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,80 @@
+"""Frame orchestration of the hair hot path (src/renderer.ts:145-295).
+
+    simulateHair           GridPreSimPass -> HairSimIntegrationPass (+ swap)
+                           -> GridPostSimPass                  (:212-240)
+    cmdDrawScene           clear -> HairTilesPass -> HairTileSortPass
+                           -> HairFinePass                      (:263-277)
+    updateResources...     HairShadingPass (used by the next frame)  (:285-295)
+
+The mesh pass, hardware hair pass, AO and shadow maps of the reference are
+outside this path: their outputs come in as buffers (the scene depth used
+by the tiles / fine depth tests, the depth-with-hair used by the shading
+attenuation, AO and shadow map textures).
+"""
+from __future__ import annotations
+
+import torch
+
+from . import synthetic, uniforms as UN
+from .config import HairConfig
+from .lib import Context
+from .passes import (GridPostSimPass, GridPreSimPass, HairFinePass, HairObject, HairShadingPass,
+                     HairSimIntegrationPass, HairTileSortPass, HairTilesPass, PhysicsGrids,
+                     RasterBuffers, SdfCollider, clear_before_render)
+
+
+class Renderer:
+    """One hair instance rendered frame by frame through libhairfb.so."""
+
+    def __init__(self, inst: synthetic.Instance, device: int = -1, ctx: Context | None = None):
+        self.inst = inst
+        self.cfg: HairConfig = inst.cfg
+        self.ctx = ctx or Context(inst.cfg.to_c(), device)
+        self.hair = HairObject(inst.hair, inst.cfg.shading_points)
+        self.sdf = SdfCollider(inst.sdf)
+        self.grids = PhysicsGrids(inst.cfg.grid_dims)
+        self.rb = RasterBuffers(self.ctx, inst.width, inst.height)
+        self.scene_depth = torch.as_tensor(inst.scene_depth).cuda()
+        # depth buffer with hair drawn, for the shading attenuation; the
+        # hardware hair pass is outside the path, the scene depth stands in
+        self.shading_depth = self.scene_depth
+        self.grid_pre = GridPreSimPass(self.ctx)
+        self.integrate = HairSimIntegrationPass(self.ctx)
+        self.grid_post = GridPostSimPass(self.ctx)
+        self.shading = HairShadingPass(self.ctx)
+        self.tiles = HairTilesPass(self.ctx)
+        self.sort = HairTileSortPass(self.ctx)
+        self.fine = HairFinePass(self.ctx)
+        self.frame_idx = 0
+        self.uniforms = UN.pack_render_uniforms(inst.scene, inst.cfg)
+
+    def sim_uniforms(self, frame_idx: int) -> bytes:
+        i = self.inst
+        return UN.pack_sim_uniforms(i.sim, i.scene.model_matrix, i.scene.sdf_bounds, i.scene.grid_bounds,
+                                    frame_idx, wind_dir=i.wind_dir, wind_strength=i.wind_strength(frame_idx))
+
+    def before_first_frame(self) -> None:
+        """beforeFirstFrame, renderer.ts:145-169: initial density grid and
+        the first shading."""
+        su = self.sim_uniforms(0)
+        self.grid_post.cmd_update_grids_after_sim(su, self.hair, self.grids)
+        self.shading.cmd_compute_shading_points(self.uniforms, self.hair, self.shading_depth)
+
+    def simulate(self) -> None:
+        su = self.sim_uniforms(self.frame_idx)
+        self.grid_pre.cmd_update_grids_before_sim(su, self.grids, self.sdf)
+        self.integrate.cmd_simulate_hair_positions(su, self.hair, self.grids, self.sdf)
+        self.grid_post.cmd_update_grids_after_sim(su, self.hair, self.grids)
+
+    def draw(self) -> None:
+        clear_before_render(self.ctx, self.rb)
+        self.tiles.cmd_draw_hair_to_tiles(self.uniforms, self.hair, self.scene_depth, self.rb)
+        self.sort.cmd_sort_hair_tiles(self.rb)
+        self.fine.cmd_rasterize_slices_hair(self.uniforms, self.hair, self.scene_depth, self.rb)
+        self.shading.cmd_compute_shading_points(self.uniforms, self.hair, self.shading_depth)
+
+    def frame(self) -> None:
+        """cmdRender, renderer.ts:171-210 (hair passes only)."""
+        self.simulate()
+        self.draw()
+        self.frame_idx += 1

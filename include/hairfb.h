@@ -1,0 +1,280 @@
+/*
+ * hairfb.h -- C-ABI of libhairfb.so, the GB300 (sm_103a) hair hot path.
+ *
+ * One entry point per WGSL compute pass of the reference renderer
+ * (Scthe/frostbitten-hair-webgpu, src/passes/...), with the same inputs and
+ * outputs as the pass's bind group and the same buffer byte layouts, so a
+ * host that drove the WebGPU passes can drive these instead.  The reference's
+ * per-pass interface is ``new XPass(device)`` + ``onViewportResize`` +
+ * ``cmdClearBeforeRender`` + ``cmdX(ctx, hairObject)``
+ * (e.g. src/passes/swHair/hairTilesPass.ts:22-140); here the pass constants
+ * live in the context (HfbConfig), the viewport-sized buffers in
+ * HfbRasterBuffers, and each ``cmdX`` is an ``hfb_*`` call.
+ *
+ * Conventions
+ *   - Every function returns an int status: HFB_OK (0) or a negative
+ *     HFB_ERR_* code; hfb_last_error() returns the message of the last failure
+ *     on that context.  No C++ exception crosses this boundary.
+ *   - Device buffers are plain CUDA device pointers (from hfb_buffer_alloc or
+ *     any other CUDA allocator).  Host pointers are borrowed for the duration
+ *     of the call only.  Uniform blocks are passed as host pointers to their
+ *     raw bytes, as the reference uploads them with queue.writeBuffer.
+ *   - Calls are asynchronous on the context's CUDA stream unless documented
+ *     otherwise (like commands recorded into one WebGPU command encoder).
+ *   - One context is used by one host thread at a time.
+ */
+#ifndef HAIRFB_H
+#define HAIRFB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HFB_VERSION 1
+
+#if defined(__GNUC__)
+#define HFB_API __attribute__((visibility("default")))
+#else
+#define HFB_API
+#endif
+
+#define HFB_OK 0
+#define HFB_ERR_INVALID_ARGUMENT (-1)
+#define HFB_ERR_OUT_OF_MEMORY (-2)
+#define HFB_ERR_CUDA (-3)
+#define HFB_ERR_TIMEOUT (-5)
+#define HFB_ERR_UNSUPPORTED (-6)
+
+/* Pass constants the reference splices into its WGSL at pipeline creation
+ * (CONFIG, src/constants.ts:86-349).  64 bytes. */
+typedef struct HfbConfig {
+  uint32_t tileSize;                        /* hairRender.tileSize: 8, 16 or 32 */
+  uint32_t tileDepthBins;                   /* hairRender.tileDepthBins (<= 64) */
+  uint32_t slicesPerPixel;                  /* hairRender.slicesPerPixel (<= 16; <= 8 with 32 px tiles) */
+  uint32_t shadingPoints;                   /* hairRender.shadingPoints */
+  uint32_t gridDims;                        /* hairSimulation.physicsForcesGrid.dims */
+  uint32_t sortBuckets;                     /* hairRender.sortBuckets (<= 256) */
+  uint32_t sortBucketSize;                  /* hairRender.sortBucketSize */
+  uint32_t avgSegmentsPerTile;              /* hairRender.avgSegmentsPerTile */
+  uint32_t avgFragmentsPerSlice;            /* hairRender.avgFragmentsPerSlice */
+  uint32_t invalidTilesPerSegmentThreshold; /* hairRender.invalidTilesPerSegmentThreshold */
+  uint32_t processorCount;                  /* fine-pass persistent CTAs; 0 = one wave */
+  uint32_t alphaQuadratic;                  /* hairRender.alphaQuadratic (0/1) */
+  float alphaMultiplier;                    /* hairRender.alphaMultipler */
+  float cameraNear, cameraFar;              /* camera.projection (linearizeDepth) */
+  uint32_t reserved;
+} HfbConfig;
+
+/* struct HairData, src/scene/hair/hairDataBuffer.ts:15-19 (padded). */
+typedef struct HfbHairData {
+  float boundingSphere[4]; /* xyz centre, w radius (object space) */
+  uint32_t strandsCount;
+  uint32_t pointsPerStrand; /* 2..256 */
+  uint32_t padding[2];
+} HfbHairData;
+
+typedef struct HfbMat4 { float m[16]; } HfbMat4; /* column-major */
+typedef struct HfbVec4 { float x, y, z, w; } HfbVec4;
+
+/* struct Uniforms, src/passes/renderUniformsBuffer.ts:105-137 (1184 bytes). */
+typedef struct HfbUniforms {
+  HfbMat4 vpMatrix, vpMatrixInv, viewMatrix, projMatrix, projMatrixInv;
+  HfbMat4 modelMatrix, modelViewMat, mvpMatrix, collisionSphereModelMatrix;
+  HfbVec4 viewport;       /* width, height, 0, 0 */
+  HfbVec4 cameraPosition; /* world space */
+  HfbVec4 colorMgmt, lightAmbient;
+  struct { HfbVec4 position, colorAndEnergy; } light0, light1, light2;
+  struct {
+    HfbMat4 sourceModelViewMat, sourceProjMatrix, sourceMVP_Matrix;
+    HfbVec4 sourcePosition;
+    uint32_t usePCSS, PCF_Radius;
+    float bias, strength;
+  } shadows;
+  struct {
+    float radius, directionOffset, falloffStart2, falloffEnd2;
+    uint32_t numDirections, numSteps;
+    float strength, padding0;
+  } ao;
+  struct {
+    float color0[3]; float specular;
+    float color1[3]; float shadows;
+    float weightTT, weightTRT, shift, roughness;
+    float colorRng, lumaRng, attenuation, padding1;
+  } hairMaterial;
+  struct { HfbVec4 boundsMin, boundsMax; } sdf;
+  struct { HfbVec4 boundsMin; float boundsMax[3]; uint32_t debugDisplayValue; } gridData;
+  float fiberRadius, dbgShadowMapPreviewSize;
+  uint32_t maxDrawnHairSegments; /* 1 + tiles * avgSegmentsPerTile */
+  uint32_t displayMode;          /* low 8 bits mode, bits 8..23 extra */
+  float background[8];
+  float collisionSpherePosition[3];
+  uint32_t gizmoActiveState;
+} HfbUniforms;
+
+/* struct SimulationUniforms, src/passes/simulation/simulationUniformsBuffer.ts:19-51 (304 bytes). */
+typedef struct HfbSimUniforms {
+  HfbMat4 modelMatrix, modelMatrixInv;
+  HfbVec4 collisionSphere; /* object space xyz, radius */
+  HfbVec4 wind;            /* object-space direction xyz, strength */
+  struct { HfbVec4 boundsMin, boundsMax; } sdf; /* boundsMax.w = distanceOffset */
+  struct { HfbVec4 boundsMin; float boundsMax[3]; uint32_t debugDisplayValue; } gridData;
+  float deltaTime, gravity;
+  uint32_t constraintIterations, frameIdx;
+  float windStrengthLull, windColisionTraceOffset, stiffnessLengthConstr, stiffnessCollisions;
+  float stiffnessSDF, volumePreservation, friction, stiffnessGlobalConstr;
+  float globalConstrExtent, globalConstrFade, stiffnessLocalConstr, windPhaseOffset;
+  float windStrengthFrequency, windStrengthJitter, padding0, padding1;
+} HfbSimUniforms;
+
+/*
+ * Viewport-sized buffers of the raster passes, in the reference layouts
+ * (created by the passes' onViewportResize in the reference).  T = tile
+ * count, B = tileDepthBins, maxDrawn = Uniforms.maxDrawnHairSegments.
+ */
+typedef struct HfbRasterBuffers {
+  uint32_t width, height;
+  uint32_t maxDrawnSegments;
+  uint32_t reserved0;
+  /* HairTileResult[T*B] {minDepth, maxDepth, tileSegmentPtr, pad}
+   * (src/passes/swHair/shared/hairTilesResultBuffer.ts:77-82) */
+  uint32_t* tiles;
+  /* DrawnHairSegments {u32 drawnSegmentsCount; {strandAndSegmentIdxs, next}[maxDrawn]}
+   * with the array at byte offset 4 (hairTileSegmentsBuffer.ts:60-68) */
+  uint32_t* tileSegments;
+  /* u32[T] (segmentCountPerTileBuffer.ts:10-45) */
+  uint32_t* segmentCountPerTile;
+  /* SortBucket[sortBuckets] {tileCount, writeOffset} (hairTileSortPass.countTiles.wgsl.ts:42-49) */
+  uint32_t* sortBuckets;
+  /* TilesList {u32 drawnTiles; u32 data[T]} (tileListBuffer.ts:15-19), 4 + T words */
+  uint32_t* tileList;
+  /* HairRasterResult {u32 tileQueueAtomicIdx; pad; vec4f data[W*H]} with the
+   * array at byte offset 16 (hairRasterizerResultBuffer.ts:28-34).  Sized
+   * 16 + 16*W*H bytes: one vec4f more than the reference, whose last pixel
+   * falls outside its buffer. */
+  float* rasterizerResult;
+  /* working memory of the tiles pass, hfb_raster_scratch_bytes() bytes */
+  void* scratch;
+  size_t scratchBytes;
+} HfbRasterBuffers;
+
+/* Counters accumulated over the context's lifetime (read with hfb_get_counters). */
+typedef struct HfbCounters {
+  uint64_t tileRecords;        /* (segment, tile) records attempted (sum of drawnSegmentsCount) */
+  uint64_t tileRecordsDropped; /* records lost because the segment pool was full */
+  uint64_t finePoolFullBins;   /* tile depth bins whose fragment pool filled (fine pass break) */
+  uint64_t waitTimeouts;       /* bounded device waits that gave up */
+  uint64_t launches;           /* kernels launched by the library */
+  uint64_t reserved[3];
+} HfbCounters;
+
+typedef struct HfbCtx HfbCtx;
+
+/* ---- context ------------------------------------------------------------ */
+HFB_API int hfb_version(void);
+/* Validates the config (the WGSL constants) and binds the current CUDA
+ * device `device` (-1 = keep current).  Creates the context's stream. */
+HFB_API int hfb_ctx_create(const HfbConfig* cfg, int device, HfbCtx** out);
+HFB_API int hfb_ctx_destroy(HfbCtx* ctx);
+HFB_API const char* hfb_last_error(const HfbCtx* ctx);
+/* Run subsequent calls on `stream` (a cudaStream_t); NULL restores the
+ * context's own stream. */
+HFB_API int hfb_ctx_set_stream(HfbCtx* ctx, void* stream);
+/* Blocks until all work of the context's stream has finished. */
+HFB_API int hfb_sync(HfbCtx* ctx);
+/* Synchronizes, then copies the counters. */
+HFB_API int hfb_get_counters(HfbCtx* ctx, HfbCounters* out);
+
+/* ---- buffers ------------------------------------------------------------ */
+HFB_API int hfb_buffer_alloc(HfbCtx* ctx, size_t bytes, void** out);
+HFB_API int hfb_buffer_free(HfbCtx* ctx, void* ptr);
+HFB_API int hfb_buffer_upload(HfbCtx* ctx, void* dst, const void* src, size_t bytes);
+/* Synchronous device -> host copy. */
+HFB_API int hfb_buffer_download(HfbCtx* ctx, void* dst, const void* src, size_t bytes);
+HFB_API int hfb_buffer_clear(HfbCtx* ctx, void* dst, size_t bytes);
+
+/* Bytes of tiles-pass working memory for a viewport. */
+HFB_API size_t hfb_raster_scratch_bytes(const HfbConfig* cfg, uint32_t width, uint32_t height);
+/* onViewportResize of HairTilesPass / HairTileSortPass / HairFinePass:
+ * allocates every HfbRasterBuffers member for width x height. */
+HFB_API int hfb_raster_buffers_alloc(HfbCtx* ctx, uint32_t width, uint32_t height, HfbRasterBuffers* out);
+HFB_API int hfb_raster_buffers_free(HfbCtx* ctx, HfbRasterBuffers* rb);
+
+/* ---- simulation passes (src/renderer.ts:212-240 order) --------------------- */
+
+/* GridPreSimPass.cmdUpdateGridsBeforeSim (gridPreSimPass.ts:34-62,
+ * gridPreSimPass.wgsl.ts:38-159): densityGradWind[G^3] {vec3f grad, f32 wind}
+ * from the previous frame's densityVelocity[G^3] {i32 vx, vy, vz, density}
+ * and the SDF (sdfDims^3 f32, x fastest). */
+HFB_API int hfb_grid_pre_sim(HfbCtx* ctx, const HfbSimUniforms* u, const int32_t* densityVelocity,
+                     float* densityGradWind, const float* sdf, uint32_t sdfDims);
+
+/* HairSimIntegrationPass.cmdSimulateHairPositions (hairSimIntegrationPass.ts:33-60,
+ * hairSimIntegrationPass.wgsl.ts:79-273): reads positionsPrev and positionsNow
+ * (vec4f, .w = isMovable), writes the new positions into positionsPrev.  The
+ * caller then swaps its "current" buffer (HairObject.swapPositionBuffersAfterSimIntegration). */
+HFB_API int hfb_sim_integrate(HfbCtx* ctx, const HfbSimUniforms* u, const HfbHairData* hair,
+                      float* positionsPrev, const float* positionsNow, const float* positionsInitial,
+                      const float* segmentLengths, const int32_t* densityVelocity,
+                      const float* densityGradWind, const float* sdf, uint32_t sdfDims);
+
+/* GridPostSimPass.cmdUpdateGridsAfterSim (gridPostSimPass.ts:33-59,
+ * gridPostSimPass.wgsl.ts:45-72): clears densityVelocity, then splats
+ * velocity (now - prev) and density of every point into it. */
+HFB_API int hfb_grid_post_sim(HfbCtx* ctx, const HfbSimUniforms* u, const HfbHairData* hair,
+                      const float* positionsPrev, const float* positionsNow, int32_t* densityVelocity);
+
+/* ---- shading (HairShadingPass.cmdComputeShadingPoints, hairShadingPass.ts:41-68) ---- */
+/* depth: width*height f32 (row 0 = top); ao: aoWidth*aoHeight f32 or NULL
+ * (unoccluded); shadowMap: shadowMapSize^2 f32 or NULL (no shadow).
+ * shading: strandsCount*shadingPoints vec4f. */
+HFB_API int hfb_shading(HfbCtx* ctx, const HfbUniforms* u, const HfbHairData* hair, const float* positions,
+                const float* tangents, const float* depth, const float* ao, uint32_t aoWidth,
+                uint32_t aoHeight, const float* shadowMap, uint32_t shadowMapSize, float* shading);
+
+/* ---- software raster (src/renderer.ts:263-277 order) ---------------------- */
+
+/* cmdClearBeforeRender of HairTilesPass, HairFinePass and HairTileSortPass
+ * (hairTilesPass.ts:48-52, hairFinePass.ts:50-55, hairTileSortPass.ts:63-68). */
+HFB_API int hfb_clear_before_render(HfbCtx* ctx, HfbRasterBuffers* rb);
+
+/* HairTilesPass.cmdDrawHairToTiles (hairTilesPass.wgsl.ts:70-246): bins the
+ * segments of the first strandsToRender strands into per-tile depth-bin
+ * lists.  depth: the scene depth buffer, width*height f32, row 0 = top.
+ * The lists come out in a canonical order: within each (tile, depth bin)
+ * the list walks segments in descending (strand, segment) order. */
+HFB_API int hfb_tiles_pass(HfbCtx* ctx, const HfbUniforms* u, const HfbHairData* hair, const float* positions,
+                   const float* tangents, const float* depth, uint32_t strandsToRender,
+                   HfbRasterBuffers* rb);
+
+/* HairTileSortPass.cmdSortHairTiles (count-tiles + sort kernels): tile list,
+ * heaviest bucket first; within a bucket, ascending tile index. */
+HFB_API int hfb_tile_sort(HfbCtx* ctx, HfbRasterBuffers* rb);
+
+/* HairFinePass.cmdRasterizeSlicesHair (hairFinePass.wgsl.ts:126-335):
+ * persistent CTAs take tiles from the queue, blend every depth bin's
+ * segments front to back into rasterizerResult. shading: the strand-space
+ * colours (S*shadingPoints vec4f). */
+HFB_API int hfb_fine_pass(HfbCtx* ctx, const HfbUniforms* u, const HfbHairData* hair, const float* positions,
+                  const float* tangents, const float* shading, const float* depth,
+                  HfbRasterBuffers* rb);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#ifdef __cplusplus
+static_assert(sizeof(HfbConfig) == 64, "HfbConfig layout");
+static_assert(sizeof(HfbHairData) == 32, "HfbHairData layout");
+static_assert(sizeof(HfbUniforms) == 1184, "Uniforms layout");
+static_assert(sizeof(HfbSimUniforms) == 304, "SimulationUniforms layout");
+#else
+_Static_assert(sizeof(HfbConfig) == 64, "HfbConfig layout");
+_Static_assert(sizeof(HfbHairData) == 32, "HfbHairData layout");
+_Static_assert(sizeof(HfbUniforms) == 1184, "Uniforms layout");
+_Static_assert(sizeof(HfbSimUniforms) == 304, "SimulationUniforms layout");
+#endif
+
+#endif /* HAIRFB_H */

@@ -1,0 +1,152 @@
+"""CPU tests: host-side logic, byte layouts, the C-ABI library's exports."""
+import ctypes
+import os
+import re
+import struct
+
+import numpy as np
+import pytest
+
+from hairfb import formats, hair_object as HO, synthetic, uniforms as UN
+from hairfb.config import HairConfig, HfbConfig
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "hairfb.h")
+
+
+def test_uniform_block_sizes_and_offsets():
+    inst = synthetic.plain_small(strands=50)
+    u = UN.pack_render_uniforms(inst.scene, inst.cfg)
+    assert len(u) == 1184  # renderUniformsBuffer.ts BUFFER_SIZE
+    vp = np.frombuffer(u, np.float32, 4, UN.OFF["viewport"])
+    assert tuple(vp) == (640.0, 480.0, 0.0, 0.0)
+    assert struct.unpack_from("<f", u, UN.OFF["fiberRadius"])[0] == np.float32(5e-4)
+    md = struct.unpack_from("<I", u, UN.OFF["maxDrawnHairSegments"])[0]
+    assert md == 1 + 40 * 30 * 128
+    cam = np.frombuffer(u, np.float32, 3, UN.OFF["cameraPosition"])
+    assert np.allclose(cam, inst.scene.camera.eye)
+    # projMatrixInv is the inverse of projMatrix
+    P = np.frombuffer(u, np.float32, 16, UN.OFF["projMatrix"]).reshape(4, 4).T
+    Pi = np.frombuffer(u, np.float32, 16, UN.OFF["projMatrixInv"]).reshape(4, 4).T
+    assert np.allclose(P.astype(np.float64) @ Pi, np.eye(4), atol=1e-4)
+    s = UN.pack_sim_uniforms(inst.sim, inst.scene.model_matrix, inst.scene.sdf_bounds,
+                             inst.scene.grid_bounds, 12)
+    assert len(s) == 304
+    assert struct.unpack_from("<f", s, UN.SIM_OFF["deltaTime"])[0] == np.float32(1 / 60)
+    assert struct.unpack_from("<I", s, UN.SIM_OFF["frameIdx"])[0] == 12
+    assert struct.unpack_from("<I", s, UN.SIM_OFF["constraintIterations"])[0] == 7
+
+
+def test_config_struct_matches_header():
+    assert ctypes.sizeof(HfbConfig) == 64
+    txt = open(HEADER).read()
+    body = re.search(r"typedef struct HfbConfig \{(.*?)\} HfbConfig;", txt, re.S).group(1)
+    names = re.findall(r"(?:uint32_t|float)\s+([\w, ]+);", body)
+    flat = [n.strip() for group in names for n in group.split(",")]
+    assert flat == [f for f, _ in HfbConfig._fields_]
+    c = HairConfig().to_c()  # reference defaults, constants.ts
+    assert (c.tileSize, c.tileDepthBins, c.slicesPerPixel, c.shadingPoints) == (8, 32, 8, 64)
+    assert (c.sortBuckets, c.sortBucketSize, c.processorCount) == (64, 16, 512)
+
+
+def test_max_drawn_segments_formula():
+    # getLengthOfHairTileSegmentsBuffer, hairTileSegmentsBuffer.ts:81-87
+    cfg = HairConfig(tile_size=16, avg_segments_per_tile=128)
+    assert cfg.max_drawn_segments(1920, 1080) == 1 + 120 * 68 * 128
+    assert cfg.slice_data_per_processor() == 16 * 8 * 16 * 16
+
+
+def test_tangents_lengths_bounds():
+    rng = np.random.Generator(np.random.PCG64(3))
+    a = synthetic.grow_hair(rng, 20, 8)
+    t = HO.tangents(a)
+    p = a.positions[:, :3].reshape(20, 8, 3).astype(np.float64)
+    d = p[:, 1:] - p[:, :-1]
+    exp = d / np.linalg.norm(d, axis=-1, keepdims=True)
+    tt = t.reshape(20, 8, 4)
+    assert np.allclose(tt[:, :-1, :3], exp, atol=1e-6)
+    assert np.array_equal(tt[:, -1], tt[:, -2])          # tip copies the previous tangent
+    assert np.all(tt[..., 3] == 0)
+    L = HO.segment_lengths(a).reshape(20, 8)
+    assert np.allclose(L[:, :-1], np.linalg.norm(d, axis=-1), rtol=1e-6)
+    assert np.array_equal(L[:, -1], L[:, -2])
+    bmin, bmax = HO.bounding_box(a.positions)
+    c, r = HO.bounding_sphere(bmin, bmax)
+    assert np.allclose(c, (bmin + bmax) / 2)
+    assert np.isclose(r, np.linalg.norm(bmax - c), rtol=1e-6)
+    gmin, gmax = HO.scale_bounding_box(bmin, bmax, 2.0)
+    assert np.allclose(gmax - gmin, 2 * (bmax - bmin), rtol=1e-5)
+
+
+def test_growth_model():
+    rng = np.random.Generator(np.random.PCG64(0))
+    a = synthetic.grow_hair(rng, 500, 16)
+    p = a.positions.reshape(500, 16, 4)
+    assert np.all(p[:, 0, 3] == 0) and np.all(p[:, 1:, 3] == 1)
+    seg = np.linalg.norm(np.diff(p[..., :3], axis=1), axis=-1)
+    assert np.allclose(seg, 0.01, rtol=1e-4)
+    root_r = np.linalg.norm(p[:, 0, :3], axis=-1)
+    assert np.allclose(root_r, 0.1, rtol=1e-5)
+    assert np.all(p[:, 0, 1] >= 0)                         # upper hemisphere
+
+
+def test_tfx_round_trip_and_errors():
+    rng = np.random.Generator(np.random.PCG64(1))
+    a = synthetic.grow_hair(rng, 30, 16)
+    data = formats.write_tfx(a)
+    assert len(data) == formats.TFX_HEADER_BYTES + 30 * 16 * 16
+    b = formats.parse_tfx(data)
+    assert (b.strands, b.points_per_strand) == (30, 16)
+    assert np.array_equal(a.positions, b.positions)
+    with pytest.raises(ValueError):
+        formats.parse_tfx(data[:200])
+    with pytest.raises(ValueError):
+        formats.parse_tfx(b"\0" * 16)
+
+
+def test_sphere_depth_input():
+    inst = synthetic.plain_small(strands=10)
+    d = inst.scene_depth.reshape(inst.height, inst.width)
+    assert d.min() > 0.0 and d.max() == 1.0
+    # the head sphere covers a disc of the image, the corners are empty
+    assert (d < 1.0).sum() > 5000 and d[0, 0] == 1.0
+
+
+def _declared_symbols():
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"HFB_API\s+[\w\s\*]+?\b(hfb_\w+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol():
+    """The C-ABI library loads without a GPU and exports every entry point
+    include/hairfb.h declares (no compute call is made here)."""
+    from hairfb import build as B
+    from hairfb import lib as L
+    try:
+        path = B.build()
+    except RuntimeError as e:  # no CUDA toolkit on this machine
+        pytest.skip(str(e))
+    so = ctypes.CDLL(path)
+    syms = _declared_symbols()
+    assert len(syms) >= 20
+    missing = [s for s in syms if not hasattr(so, s)]
+    assert not missing, missing
+    assert set(syms) == set(L.SIGNATURES), set(syms) ^ set(L.SIGNATURES)
+    assert so.hfb_version() == 1
+    so.hfb_raster_scratch_bytes.restype = ctypes.c_size_t
+    so.hfb_raster_scratch_bytes.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32]
+    cfg = HairConfig(tile_size=16, tile_depth_bins=8).to_c()
+    n = so.hfb_raster_scratch_bytes(ctypes.byref(cfg), 640, 480)
+    assert n >= 2 * 1200 * 8 * 4 + 4 * (1 + 1200 * 128)
+    # invalid config is rejected before touching CUDA
+    bad = HairConfig(tile_size=12).to_c()
+    h = ctypes.c_void_p()
+    so.hfb_ctx_create.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+    assert so.hfb_ctx_create(ctypes.byref(bad), -1, ctypes.byref(h)) == -1
+
+
+def test_product_has_no_cpu_fallback(tmp_path):
+    """The host package fails loudly when the CUDA library is missing."""
+    from hairfb import lib as L
+    with pytest.raises(FileNotFoundError):
+        L.open_library(str(tmp_path / "libhairfb.so"))

@@ -1,0 +1,383 @@
+"""GPU parity: every pass of libhairfb.so against the CPU oracle, called
+through the C-ABI on the same seeded inputs.
+
+Bars (the reference's own: integer work bit-exact, pixels within 1/255,
+positions within 1e-5 relative after 60 steps):
+- tiles pass: drawnSegmentsCount, segmentCountPerTile, per-bin min/max depth
+  bit-exact; per-bin lists equal as walked sequences (canonical order);
+- tile sort: buckets and tile list bit-exact (stable order on both sides);
+- grids: density/velocity grid bit-exact (integer splat); gradient/wind
+  grid bit-exact;
+- integration: bit-exact after one step (same fp32 op order, no FMA), and
+  within 1e-5 relative after 60 steps of the whole simulation;
+- shading: within 1e-5 (absolute + relative) -- exp/pow are not
+  correctly rounded on either side;
+- fine pass: every pixel channel within 1/255.
+"""
+import numpy as np
+import pytest
+
+from helpers import INVALID, frame_of, small_instance, walk_lists
+from hairfb import uniforms as UN
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+from hairfb.lib import Context  # noqa: E402
+from hairfb.passes import (GridPostSimPass, GridPreSimPass, HairFinePass, HairObject,  # noqa: E402
+                           HairShadingPass, HairSimIntegrationPass, HairTileSortPass, HairTilesPass,
+                           PhysicsGrids, RasterBuffers, SdfCollider, clear_before_render)
+
+
+@pytest.fixture(scope="module")
+def oracle():
+    from oracle import oracle as o
+    o.load()
+    return o
+
+
+def _ctx(inst):
+    return Context(inst.cfg.to_c(), 0)
+
+
+def _raster_gpu(inst, fr, hair=None, depth=None):
+    ctx = _ctx(inst)
+    hair = hair or HairObject(inst.hair, inst.cfg.shading_points)
+    rb = RasterBuffers(ctx, inst.width, inst.height)
+    d = torch.as_tensor(inst.scene_depth if depth is None else depth).cuda()
+    clear_before_render(ctx, rb)
+    HairTilesPass(ctx).cmd_draw_hair_to_tiles(fr.uniforms, hair, d, rb)
+    HairTileSortPass(ctx).cmd_sort_hair_tiles(rb)
+    ctx.sync()
+    return ctx, hair, rb, d
+
+
+def _compare_tiles(o, inst, fr, rb):
+    hb = inst.hair
+    ot, osg, oc = o.tiles_pass(inst.cfg, fr.uniforms, hb.hair_data, hb.asset.positions, hb.tangents,
+                               inst.scene_depth, hb.asset.strands, inst.width, inst.height, fr.max_drawn)
+    gt, gsg, gc = rb.read_tiles(), rb.read_tile_segments(), rb.read_segment_counts()
+    assert int(osg[0]) > 0, "workload draws nothing"
+    assert int(osg[0]) < fr.max_drawn, "parity cases must not overflow the segment pool"
+    assert gsg[0] == osg[0], f"drawnSegmentsCount {gsg[0]} != {osg[0]}"
+    assert np.array_equal(gc, oc), "segmentCountPerTile differs"
+    assert np.array_equal(gt[:, 0], ot[:, 0]), "per-bin minDepth differs"
+    assert np.array_equal(gt[:, 1], ot[:, 1]), "per-bin maxDepth differs"
+    assert np.array_equal(gt[:, 2] != 0, ot[:, 2] != 0), "non-empty bins differ"
+    gl = walk_lists(gt, gsg, fr.max_drawn)
+    ol = walk_lists(ot, osg, fr.max_drawn)
+    assert gl.keys() == ol.keys()
+    bad = [k for k in ol if gl[k] != ol[k]]
+    assert not bad, f"{len(bad)} bins list segments in a different order"
+    assert sum(len(v) for v in gl.values()) == int(gsg[0])
+    return ot, osg, oc
+
+
+@pytest.mark.parametrize("tile,bins", [(16, 8), (8, 32), (32, 4)])
+def test_tiles_pass_bit_exact(oracle, tile, bins):
+    inst = small_instance(tile_size=tile, depth_bins=bins)
+    fr = frame_of(inst)
+    ctx, hair, rb, _ = _raster_gpu(inst, fr)
+    _compare_tiles(oracle, inst, fr, rb)
+
+
+def test_tiles_pass_partial_tiles_and_lod(oracle):
+    # 1000x700 with 16px tiles leaves partial edge tiles; LOD renders 70%
+    inst = small_instance(width=1000, height=700)
+    fr = frame_of(inst)
+    ctx = _ctx(inst)
+    hair = HairObject(inst.hair, inst.cfg.shading_points)
+    hair.lod_render_percent = 70.0
+    rb = RasterBuffers(ctx, inst.width, inst.height)
+    d = torch.as_tensor(inst.scene_depth).cuda()
+    clear_before_render(ctx, rb)
+    HairTilesPass(ctx).cmd_draw_hair_to_tiles(fr.uniforms, hair, d, rb)
+    ctx.sync()
+    hb = inst.hair
+    n = hair.rendered_strand_count()
+    assert n == 1400
+    ot, osg, oc = oracle.tiles_pass(inst.cfg, fr.uniforms, hb.hair_data, hb.asset.positions, hb.tangents,
+                                    inst.scene_depth, n, inst.width, inst.height, fr.max_drawn)
+    assert rb.read_tile_segments()[0] == osg[0]
+    assert np.array_equal(rb.read_segment_counts(), oc)
+    gl = walk_lists(rb.read_tiles(), rb.read_tile_segments(), fr.max_drawn)
+    assert gl == walk_lists(ot, osg, fr.max_drawn)
+
+
+def test_tiles_pass_empty_and_offscreen(oracle):
+    inst = small_instance(strands=50)
+    # move the camera away: nothing on screen
+    inst.scene.camera.eye = inst.scene.camera.eye + np.array([50.0, 0.0, 0.0])
+    fr = frame_of(inst)
+    ctx, hair, rb, _ = _raster_gpu(inst, fr)
+    assert rb.read_tile_segments()[0] == 0
+    assert not rb.read_segment_counts().any()
+    assert rb.read_tile_list()[0] == 0
+
+
+def test_tile_sort_bit_exact(oracle):
+    inst = small_instance()
+    fr = frame_of(inst)
+    ctx, hair, rb, _ = _raster_gpu(inst, fr)
+    ob, otl = oracle.tile_sort(inst.cfg, inst.width, inst.height, rb.read_segment_counts())
+    assert np.array_equal(rb.read_sort_buckets(), ob)
+    assert np.array_equal(rb.read_tile_list(), otl)
+
+
+def test_tile_sort_reference_case():
+    """hairTileSortPass.test.ts:25-128 through the CUDA kernel."""
+    from hairfb.config import HairConfig
+    cfg = HairConfig(tile_size=8, sort_buckets=8)
+    ctx = Context(cfg.to_c(), 0)
+    rb = RasterBuffers(ctx, 16 * 8, 1)
+    seg = np.zeros(16, np.uint32)
+    seg[1], seg[6], seg[2], seg[3], seg[8] = 1, 15, 16, 17, 4096
+    ctx.call("hfb_buffer_upload", rb.rb.segmentCountPerTile, seg.ctypes.data, seg.nbytes)
+    HairTileSortPass(ctx).cmd_sort_hair_tiles(rb)
+    b = rb.read_sort_buckets()
+    tl = rb.read_tile_list()
+    exp = np.zeros(8, np.uint32)
+    for c in seg:
+        if c:
+            exp[min(c // 16, 7)] += 1
+    assert np.array_equal(b[0::2], exp)
+    n = int(tl[0])
+    buckets = [min(int(seg[t]) // 16, 7) for t in tl[1:1 + n]]
+    assert n == 5 and all(buckets[i] <= buckets[i - 1] for i in range(1, n))
+
+
+def _sim_inputs(inst, frame_idx=0):
+    return UN.pack_sim_uniforms(inst.sim, inst.scene.model_matrix, inst.scene.sdf_bounds,
+                                inst.scene.grid_bounds, frame_idx, wind_dir=inst.wind_dir,
+                                wind_strength=inst.wind_strength(frame_idx))
+
+
+@pytest.mark.parametrize("maker", ["small", "curly_wind"])
+def test_grids_and_one_step_bit_exact(oracle, maker):
+    if maker == "small":
+        inst = small_instance()
+    else:
+        inst = small_instance(strands=3000, points=32, curl=True, ellipsoid=True, wind_amplitude=1.0,
+                              iterations=4, sdf_dims=64)
+    hb = inst.hair
+    su = _sim_inputs(inst, 7)
+    ctx = _ctx(inst)
+    hair = HairObject(hb, inst.cfg.shading_points)
+    grids = PhysicsGrids(inst.cfg.grid_dims)
+    sdf = SdfCollider(inst.sdf)
+    # perturb "now" so velocities are non-zero: prev = initial, now = initial + noise
+    rng = np.random.default_rng(1)
+    now = hb.asset.positions.copy()
+    now[:, :3] += rng.normal(0, 2e-3, now[:, :3].shape).astype(np.float32) * (now[:, 3:] > 0)
+    hair.positions.copy_(torch.as_tensor(now))
+    GridPostSimPass(ctx).cmd_update_grids_after_sim(su, hair, grids)
+    ctx.sync()
+    odv = oracle.grid_post_sim(inst.cfg, su, hb.hair_data, hb.asset.positions, now)
+    assert np.array_equal(grids.density_velocity.cpu().numpy(), odv), "density/velocity grid differs"
+    GridPreSimPass(ctx).cmd_update_grids_before_sim(su, grids, sdf)
+    ctx.sync()
+    ogw = oracle.grid_pre_sim(inst.cfg, su, odv, inst.sdf.distances, inst.sdf.dims)
+    assert np.array_equal(grids.density_grad_wind.cpu().numpy().view(np.uint32), ogw.view(np.uint32))
+    HairSimIntegrationPass(ctx).cmd_simulate_hair_positions(su, hair, grids, sdf)
+    ctx.sync()
+    onew = oracle.sim_integrate(inst.cfg, su, hb.hair_data, hb.asset.positions, now, hb.asset.positions,
+                                hb.segment_lengths, odv, ogw, inst.sdf.distances, inst.sdf.dims)
+    g = hair.positions.cpu().numpy()
+    assert np.array_equal(g.view(np.uint32), onew.view(np.uint32)), \
+        f"max abs diff {np.abs(g - onew).max()}"
+
+
+def test_simulation_60_steps(oracle):
+    inst = small_instance(strands=1500, points=24, curl=True, wind_amplitude=1.0, iterations=4)
+    hb = inst.hair
+    ctx = _ctx(inst)
+    hair = HairObject(hb, inst.cfg.shading_points)
+    grids = PhysicsGrids(inst.cfg.grid_dims)
+    sdf = SdfCollider(inst.sdf)
+    pre, integ, post = GridPreSimPass(ctx), HairSimIntegrationPass(ctx), GridPostSimPass(ctx)
+    # oracle state
+    o_prev = hb.asset.positions.copy()
+    o_now = hb.asset.positions.copy()
+    o_dv = oracle.grid_post_sim(inst.cfg, _sim_inputs(inst, 0), hb.hair_data, o_prev, o_now)
+    post.cmd_update_grids_after_sim(_sim_inputs(inst, 0), hair, grids)
+    for f in range(60):
+        su = _sim_inputs(inst, f)
+        pre.cmd_update_grids_before_sim(su, grids, sdf)
+        integ.cmd_simulate_hair_positions(su, hair, grids, sdf)
+        post.cmd_update_grids_after_sim(su, hair, grids)
+        o_gw = oracle.grid_pre_sim(inst.cfg, su, o_dv, inst.sdf.distances, inst.sdf.dims)
+        o_new = oracle.sim_integrate(inst.cfg, su, hb.hair_data, o_prev, o_now, hb.asset.positions,
+                                     hb.segment_lengths, o_dv, o_gw, inst.sdf.distances, inst.sdf.dims)
+        o_prev, o_now = o_now, o_new
+        o_dv = oracle.grid_post_sim(inst.cfg, su, hb.hair_data, o_prev, o_now)
+    ctx.sync()
+    g = hair.positions.cpu().numpy()[:, :3].astype(np.float64)
+    o = o_now[:, :3].astype(np.float64)
+    moved = np.abs(o - hb.asset.positions[:, :3]).max()
+    assert moved > 1e-4, "the simulation did not move the hair"
+    rel = np.abs(g - o).max() / np.abs(o).max()
+    assert rel <= 1e-5, f"relative position error {rel:.3g} after 60 steps"
+
+
+def test_shading_parity(oracle):
+    inst = small_instance()
+    fr = frame_of(inst)
+    hb = inst.hair
+    ctx = _ctx(inst)
+    hair = HairObject(hb, inst.cfg.shading_points)
+    # depth buffer slightly behind the hair so attenuation stays in range
+    depth = np.full(inst.width * inst.height, 0.9995, np.float32)
+    d = torch.as_tensor(depth).cuda()
+    ao = np.linspace(0.2, 1.0, 160 * 120, dtype=np.float32)
+    HairShadingPass(ctx).cmd_compute_shading_points(fr.uniforms, hair, d, torch.as_tensor(ao).cuda(), (160, 120))
+    ctx.sync()
+    o = oracle.shading(inst.cfg, fr.uniforms, hb.hair_data, hb.asset.positions, hb.tangents, depth,
+                       hb.asset.strands, ao=ao, ao_size=(160, 120))
+    g = hair.shading.cpu().numpy()
+    assert np.isfinite(g).all()
+    assert np.abs(o).max() > 1e-3, "shading is all black: bad test input"
+    err = np.abs(g - o)
+    assert (err <= 1e-5 + 1e-5 * np.abs(o)).all(), f"max shading error {err.max():.3g}"
+
+
+def test_shading_parity_with_shadow_map(oracle):
+    inst = small_instance(strands=300)
+    inst.scene.use_pcss = True
+    fr = frame_of(inst)
+    hb = inst.hair
+    ctx = _ctx(inst)
+    hair = HairObject(hb, inst.cfg.shading_points)
+    depth = np.full(inst.width * inst.height, 0.9995, np.float32)
+    rng = np.random.default_rng(3)
+    sm = rng.uniform(0.3, 1.0, 256 * 256).astype(np.float32)
+    HairShadingPass(ctx).cmd_compute_shading_points(fr.uniforms, hair, torch.as_tensor(depth).cuda(),
+                                                    shadow_map=torch.as_tensor(sm).cuda(), shadow_size=256)
+    ctx.sync()
+    o = oracle.shading(inst.cfg, fr.uniforms, hb.hair_data, hb.asset.positions, hb.tangents, depth,
+                       hb.asset.strands, shadow_map=sm, shadow_size=256)
+    g = hair.shading.cpu().numpy()
+    err = np.abs(g - o)
+    assert (err <= 1e-5 + 1e-5 * np.abs(o)).all(), f"max shading error {err.max():.3g}"
+
+
+def _shading_input(inst):
+    """Non-trivial strand colours for the fine pass (shared by both sides)."""
+    rng = np.random.default_rng(5)
+    S, SP = inst.hair.asset.strands, inst.cfg.shading_points
+    c = rng.uniform(0.05, 1.0, (S * SP, 4)).astype(np.float32)
+    c[:, 3] = 1.0
+    c.reshape(S, SP, 4)[:, -1, 3] = 0.0
+    return c
+
+
+@pytest.mark.parametrize("tile,bins,slices", [(16, 8, 4), (8, 16, 8), (32, 4, 4)])
+def test_fine_pass_within_1_255(oracle, tile, bins, slices):
+    inst = small_instance(tile_size=tile, depth_bins=bins, slices=slices)
+    fr = frame_of(inst)
+    ctx, hair, rb, d = _raster_gpu(inst, fr)
+    shade = _shading_input(inst)
+    hair.shading.copy_(torch.as_tensor(shade))
+    HairFinePass(ctx).cmd_rasterize_slices_hair(fr.uniforms, hair, d, rb)
+    ctx.sync()
+    hb = inst.hair
+    ot, osg, oc = oracle.tiles_pass(inst.cfg, fr.uniforms, hb.hair_data, hb.asset.positions, hb.tangents,
+                                    inst.scene_depth, hb.asset.strands, inst.width, inst.height, fr.max_drawn)
+    ob, otl = oracle.tile_sort(inst.cfg, inst.width, inst.height, oc)
+    ores = oracle.fine_pass(inst.cfg, fr.uniforms, hb.hair_data, hb.asset.positions, hb.tangents, shade,
+                            inst.scene_depth, ot, osg, otl, inst.width, inst.height)
+    g = rb.read_result()[4:].reshape(-1, 4)
+    o = ores[4:].reshape(-1, 4)
+    assert (o[:, 3] > 0).sum() > 1000, "too few covered pixels for a meaningful test"
+    err = np.abs(g - o)
+    assert err.max() <= 1.0 / 255.0, f"max pixel error {err.max():.4g} (> 1/255) at {np.argmax(err.max(1))}"
+    assert np.array_equal(g[:, 3] > 0, o[:, 3] > 0), "coverage differs"
+
+
+def test_fine_pass_pool_capacity(oracle):
+    """A tiny fragment pool forces the list walk to stop early, exactly as the
+    reference's PPLL-full break does."""
+    inst = small_instance(strands=4000, tile_size=16, depth_bins=2, slices=2)
+    inst.cfg.avg_fragments_per_slice = 1  # 1 * 2 * 256 = 512 fragments per bin
+    fr = frame_of(inst)
+    ctx, hair, rb, d = _raster_gpu(inst, fr)
+    shade = _shading_input(inst)
+    hair.shading.copy_(torch.as_tensor(shade))
+    HairFinePass(ctx).cmd_rasterize_slices_hair(fr.uniforms, hair, d, rb)
+    ctx.sync()
+    assert ctx.counters()["finePoolFullBins"] > 0, "the pool never filled: the test does not test"
+    hb = inst.hair
+    ot, osg, oc = oracle.tiles_pass(inst.cfg, fr.uniforms, hb.hair_data, hb.asset.positions, hb.tangents,
+                                    inst.scene_depth, hb.asset.strands, inst.width, inst.height, fr.max_drawn)
+    ob, otl = oracle.tile_sort(inst.cfg, inst.width, inst.height, oc)
+    ores = oracle.fine_pass(inst.cfg, fr.uniforms, hb.hair_data, hb.asset.positions, hb.tangents, shade,
+                            inst.scene_depth, ot, osg, otl, inst.width, inst.height)
+    err = np.abs(rb.read_result()[4:] - ores[4:])
+    assert err.max() <= 1.0 / 255.0, f"max pixel error {err.max():.4g}"
+
+
+def test_fine_pass_reads_arbitrary_list_order(oracle):
+    """The fine pass walks whatever list it is given: feed it the oracle's
+    LIFO lists (not the tiles pass's contiguous layout)."""
+    inst = small_instance(strands=1000)
+    fr = frame_of(inst)
+    hb = inst.hair
+    ot, osg, oc = oracle.tiles_pass(inst.cfg, fr.uniforms, hb.hair_data, hb.asset.positions, hb.tangents,
+                                    inst.scene_depth, hb.asset.strands, inst.width, inst.height, fr.max_drawn)
+    ob, otl = oracle.tile_sort(inst.cfg, inst.width, inst.height, oc)
+    shade = _shading_input(inst)
+    ctx = _ctx(inst)
+    hair = HairObject(hb, inst.cfg.shading_points)
+    hair.shading.copy_(torch.as_tensor(shade))
+    rb = RasterBuffers(ctx, inst.width, inst.height)
+    clear_before_render(ctx, rb)
+    for addr, arr in ((rb.rb.tiles, ot), (rb.rb.tileSegments, osg), (rb.rb.tileList, otl)):
+        a = np.ascontiguousarray(arr)
+        ctx.call("hfb_buffer_upload", addr, a.ctypes.data, a.nbytes)
+    d = torch.as_tensor(inst.scene_depth).cuda()
+    HairFinePass(ctx).cmd_rasterize_slices_hair(fr.uniforms, hair, d, rb)
+    ctx.sync()
+    ores = oracle.fine_pass(inst.cfg, fr.uniforms, hb.hair_data, hb.asset.positions, hb.tangents, shade,
+                            inst.scene_depth, ot, osg, otl, inst.width, inst.height)
+    err = np.abs(rb.read_result()[4:] - ores[4:])
+    assert err.max() <= 1.0 / 255.0
+
+
+def test_fine_pass_debug_slices_mode(oracle):
+    """displayMode USED_SLICES: the result counts fragments per pixel."""
+    inst = small_instance(strands=800)
+    inst.scene.display_mode = UN.DISPLAY_MODE_USED_SLICES
+    inst.scene.display_mode_extra = 50
+    fr = frame_of(inst)
+    ctx, hair, rb, d = _raster_gpu(inst, fr)
+    shade = _shading_input(inst)
+    hair.shading.copy_(torch.as_tensor(shade))
+    HairFinePass(ctx).cmd_rasterize_slices_hair(fr.uniforms, hair, d, rb)
+    ctx.sync()
+    hb = inst.hair
+    ot, osg, oc = oracle.tiles_pass(inst.cfg, fr.uniforms, hb.hair_data, hb.asset.positions, hb.tangents,
+                                    inst.scene_depth, hb.asset.strands, inst.width, inst.height, fr.max_drawn)
+    ob, otl = oracle.tile_sort(inst.cfg, inst.width, inst.height, oc)
+    ores = oracle.fine_pass(inst.cfg, fr.uniforms, hb.hair_data, hb.asset.positions, hb.tangents, shade,
+                            inst.scene_depth, ot, osg, otl, inst.width, inst.height)
+    assert np.array_equal(rb.read_result()[4:], ores[4:])
+
+
+def test_invalid_arguments_return_errors():
+    from hairfb.lib import HfbError
+    inst = small_instance(strands=10)
+    fr = frame_of(inst)
+    ctx = _ctx(inst)
+    hair = HairObject(inst.hair, inst.cfg.shading_points)
+    rb = RasterBuffers(ctx, 320, 240)  # viewport does not match the uniforms
+    d = torch.zeros(320 * 240, device="cuda")
+    with pytest.raises(HfbError) as e:
+        HairTilesPass(ctx).cmd_draw_hair_to_tiles(fr.uniforms, hair, d, rb)
+    assert "viewport" in str(e.value)
+    misaligned = torch.zeros(4 * 100 + 1, device="cuda")[1:]
+    with pytest.raises(HfbError):
+        ctx.call("hfb_grid_post_sim", None, None, misaligned.data_ptr(), misaligned.data_ptr(),
+                 misaligned.data_ptr())
+    ctx.sync()  # the context stays usable
