@@ -54,10 +54,10 @@ std::string validateConfig(const HfbConfig& c) {
   return "";
 }
 
-std::string validateHair(const HfbHairData* h, uint32_t minPoints = 2) {
+std::string validateHair(const HfbHairData* h, uint32_t minPoints = 2, uint32_t maxPoints = 256) {
   if (!h) return "hair data is NULL";
-  if (h->pointsPerStrand < minPoints || h->pointsPerStrand > 256)
-    return "pointsPerStrand must be in [" + std::to_string(minPoints) + ", 256]";
+  if (h->pointsPerStrand < minPoints || h->pointsPerStrand > maxPoints)
+    return "pointsPerStrand must be in [" + std::to_string(minPoints) + ", " + std::to_string(maxPoints) + "]";
   if (h->strandsCount >= (1u << 24)) return "strandsCount must be < 2^24 (segment encoding)";
   return "";
 }
@@ -302,7 +302,6 @@ int hfb_clear_before_render(HfbCtx* c, HfbRasterBuffers* rb) {
   z(rb->tileList, 4);                             // hairTileSortPass.ts:63-68
   z(rb->sortBuckets, (size_t)cfg.sortBuckets * 8);
   if (e != cudaSuccess) return cudaFail(c, e, "clear_before_render");
-  c->launches += 6;
   return HFB_OK;
 }
 
@@ -320,7 +319,9 @@ int hfb_sim_integrate(HfbCtx* c, const HfbSimUniforms* u, const HfbHairData* h, 
                       const float* gw, const float* sdf, uint32_t sdfDims) {
   HFB_CHECK_CTX(c);
   HFB_REQUIRE(c, u && prev && now && initial && segLen && dv && gw && sdf, "NULL argument");
-  std::string err = validateHair(h, 4);  // the local shape constraint needs >= 4 points
+  // the local shape constraint needs >= 4 points; a strand must fit the
+  // block's shared-memory staging (128 points x 64 strands x 16 B)
+  std::string err = validateHair(h, 4, 128);
   HFB_REQUIRE(c, err.empty(), err);
   HFB_REQUIRE(c, sdfDims >= 1 && sdfDims <= 1024, "sdfDims must be in [1, 1024]");
   HFB_REQUIRE(c, u->constraintIterations <= 1024, "constraintIterations must be <= 1024");

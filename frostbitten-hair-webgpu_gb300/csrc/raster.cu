@@ -763,14 +763,11 @@ cudaError_t launchTilesPass(HfbCtx* c, const HfbUniforms& u, const HfbHairData& 
                                                           s.blockSums, s.keys, dc);
   binFinalizeKernel<<<min(divCeil(TB, 8), (uint32_t)c->smCount * 16), 256, 0, c->stream>>>(
       TB, s.binCount, s.binOffset, s.blockSums, s.keys, rb.tileSegments, (uint4*)rb.tiles, s.largeBins);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(largeBinsKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, LARGE_SMEM_KEYS * 4);
-    attr = true;
-  }
+  e = cudaFuncSetAttribute(largeBinsKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, LARGE_SMEM_KEYS * 4);
+  if (e != cudaSuccess) return e;
   largeBinsKernel<<<c->smCount, 1024, LARGE_SMEM_KEYS * 4, c->stream>>>(
       s.largeBins, s.binCount, s.binOffset, s.blockSums, s.keys, rb.tileSegments, (uint4*)rb.tiles);
-  c->launches += 8;
+  c->launches += nSeg ? 6 : 5;
   return cudaGetLastError();
 }
 

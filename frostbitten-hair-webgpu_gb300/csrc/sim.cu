@@ -356,12 +356,10 @@ cudaError_t launchSimIntegrate(HfbCtx* c, const HfbSimUniforms& u, const HfbHair
                                const float* now, const float* initial, const float* segLen,
                                const int32_t* dv, const float* gw, const float* sdf, uint32_t sdfDims) {
   uint32_t S = h.strandsCount, P = h.pointsPerStrand;
-  size_t smem = (size_t)P * SIM_STRANDS_PER_BLOCK * sizeof(float4);
-  static bool attrSet = false;
-  if (!attrSet) {
-    cudaFuncSetAttribute(simIntegrateKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 256 * 64 * 16);
-    attrSet = true;
-  }
+  size_t smem = (size_t)P * SIM_STRANDS_PER_BLOCK * sizeof(float4);  // <= 128 KB (P <= 128)
+  cudaError_t e = cudaFuncSetAttribute(simIntegrateKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
   simIntegrateKernel<<<divCeil(S, SIM_STRANDS_PER_BLOCK), SIM_STRANDS_PER_BLOCK, smem, c->stream>>>(
       u, S, P, c->cfg.gridDims, (float4*)prev, (const float4*)now, (const float4*)initial, segLen,
       (const int4*)dv, (const float4*)gw, sdf, sdfDims);
@@ -380,7 +378,6 @@ cudaError_t launchGridPostSim(HfbCtx* c, const HfbSimUniforms& u, const HfbHairD
                                                                (const float4*)now, dv);
     c->launches += 1;
   }
-  c->launches += 1;
   return cudaGetLastError();
 }
 
