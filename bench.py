@@ -1,0 +1,437 @@
+"""Benchmark of the hair hot path (one JSON line on rank 0).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl ours|reference]
+
+A step is one frame of the hot path for the workload: GridPreSim ->
+SimIntegration -> GridPostSim -> clear -> Tiles -> TileSort -> Fine ->
+Shading (src/renderer.ts:171-295 order).  ``value`` is device-timed
+frames/s with every input resident in HBM; the L2 is flushed (a 256 MiB
+write) between timed frames, outside the timed events.  ``e2e`` is the same
+metric through the public API with the per-frame inputs (both uniform blocks
+and the scene depth buffer) copied from pinned host memory and the frame's
+image (the rasterizer result) read back every step.
+
+Under torchrun each rank renders its own instance (replicas, weak scaling):
+value = frames of all ranks / max over ranks of the timed region.
+
+``--impl reference`` times the reference's algorithm on the host cores: the
+reference is TypeScript + WGSL that needs a WebGPU adapter (none exists on
+these machines), so its path runs as the C restatement of its WGSL passes,
+built with OpenMP, on all host threads -- on the same workload and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "frostbitten-hair-webgpu_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+WORKLOADS = {
+    # BASELINE configs[1]: the single full frame
+    "plain_full": "10,000 x 32 curly strands, 1920x1080, 16 px tiles, 16 depth bins, 4 slices, "
+                  "16 shading points, 4 iterations, 64^3 SDF, 32^3 grids, sinusoidal wind",
+    # BASELINE configs[0]
+    "plain_small": "2,000 x 16 strands, 640x480, 16 px tiles, 8 depth bins, 4 slices, 8 shading points",
+    # BASELINE configs[4]
+    "stress": "200,000 x 32 strands (60% ponytail), 3840x2160, 32 depth bins, 8 slices, 32 shading points",
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--workload", default="plain_full", choices=sorted(WORKLOADS))
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="bounded CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def make_instance(name, seed):
+    from hairfb import synthetic
+    return getattr(synthetic, name)(seed=seed)
+
+
+# ----------------------------------------------------------------------------
+# algorithmic bytes per pass (the compulsory traffic of each kernel)
+# ----------------------------------------------------------------------------
+
+def algorithmic_bytes(inst, K):
+    """Compulsory DRAM bytes of one launch of each pass (inputs read once,
+    outputs written once).  K = stored (segment, tile-bin) records."""
+    cfg = inst.cfg
+    S, P = inst.hair.asset.strands, inst.hair.asset.points_per_strand
+    Npt = S * P
+    SP = cfg.shading_points
+    W, H = inst.width, inst.height
+    tx, ty = cfg.tile_count(W, H)
+    T, B = tx * ty, cfg.tile_depth_bins
+    G3 = cfg.grid_dims ** 3
+    D3 = inst.sdf.dims ** 3
+    return {
+        "grid_pre": 16 * G3 + 16 * G3 + 4 * D3,
+        "integrate": Npt * (16 + 16 + 16 + 4 + 16) + 2 * 16 * G3 + 4 * D3,
+        "grid_post": Npt * 32 + 16 * G3,
+        "clear": T * B * 16 + T * 4 + W * H * 16,
+        # positions + tangents, depth, records staged (8 w + 8 r), keys (4 w + 4 r),
+        # lists written (8), heads (16), per-bin counts/offsets (3 x 4), per-tile counts
+        "tiles": Npt * 32 + W * H * 4 + K * (8 + 8 + 4 + 4 + 8) + T * B * (16 + 12) + T * 4,
+        "sort": T * 4 + (4 + T) * 4 + cfg.sort_buckets * 8,
+        # lists read (8), heads (16), shading read, depth read, result write
+        "fine": Npt * 32 + S * SP * 16 + W * H * (4 + 16) + K * 8 + T * B * 16,
+        "shading": Npt * 32 + S * SP * (16 + 8),
+    }
+
+
+# ----------------------------------------------------------------------------
+# clocks sampling (nvidia-smi during the timed region)
+# ----------------------------------------------------------------------------
+
+REASON_BITS = {
+    0x1: "gpu_idle", 0x2: "applications_clocks_setting", 0x4: "sw_power_cap", 0x8: "hw_slowdown",
+    0x10: "sync_boost", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+    0x80: "hw_power_brake_slowdown", 0x100: "display_clock_setting",
+}
+
+
+class ClockSampler:
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 4:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        for s in self.samples:
+            try:
+                sm.append(float(s[0]))
+                mx.append(float(s[1]))
+                bits = int(s[3], 16) if s[3].startswith("0x") else int(s[3])
+                for b, n in REASON_BITS.items():
+                    if bits & b:
+                        reasons.add(n)
+            except ValueError:
+                continue
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["not sampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------
+# CPU leg (the reference algorithm on host cores)
+# ----------------------------------------------------------------------------
+
+def cpu_frame_runner(inst):
+    """One frame of the restated reference passes on the host (OpenMP build)."""
+    from hairfb import uniforms as UN
+    from oracle import oracle as O
+    O.use_threads(True)
+    cfg, hb = inst.cfg, inst.hair
+    u = UN.pack_render_uniforms(inst.scene, cfg)
+    md = cfg.max_drawn_segments(inst.width, inst.height)
+    st = {"prev": hb.asset.positions.copy(), "now": hb.asset.positions.copy(), "f": 0}
+    su0 = UN.pack_sim_uniforms(inst.sim, inst.scene.model_matrix, inst.scene.sdf_bounds,
+                               inst.scene.grid_bounds, 0, wind_dir=inst.wind_dir)
+    st["dv"] = O.grid_post_sim(cfg, su0, hb.hair_data, st["prev"], st["now"])
+    st["shade"] = O.shading(cfg, u, hb.hair_data, st["now"], hb.tangents, inst.scene_depth, hb.asset.strands)
+
+    def frame():
+        f = st["f"]
+        su = UN.pack_sim_uniforms(inst.sim, inst.scene.model_matrix, inst.scene.sdf_bounds,
+                                  inst.scene.grid_bounds, f, wind_dir=inst.wind_dir,
+                                  wind_strength=inst.wind_strength(f))
+        gw = O.grid_pre_sim(cfg, su, st["dv"], inst.sdf.distances, inst.sdf.dims)
+        new = O.sim_integrate(cfg, su, hb.hair_data, st["prev"], st["now"], hb.asset.positions,
+                              hb.segment_lengths, st["dv"], gw, inst.sdf.distances, inst.sdf.dims)
+        st["prev"], st["now"] = st["now"], new
+        st["dv"] = O.grid_post_sim(cfg, su, hb.hair_data, st["prev"], st["now"])
+        tiles, segs, cnt = O.tiles_pass(cfg, u, hb.hair_data, st["now"], hb.tangents, inst.scene_depth,
+                                        hb.asset.strands, inst.width, inst.height, md)
+        _, tl = O.tile_sort(cfg, inst.width, inst.height, cnt)
+        O.fine_pass(cfg, u, hb.hair_data, st["now"], hb.tangents, st["shade"], inst.scene_depth, tiles,
+                    segs, tl, inst.width, inst.height)
+        st["shade"] = O.shading(cfg, u, hb.hair_data, st["now"], hb.tangents, inst.scene_depth,
+                                hb.asset.strands)
+        st["f"] = f + 1
+    return frame
+
+
+def time_cpu(inst, seconds, min_frames=1, max_frames=None):
+    frame = cpu_frame_runner(inst)
+    frame()  # warm-up (page-in, thread pool)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        frame()
+        n += 1
+        el = time.perf_counter() - t0
+        if (el >= seconds and n >= min_frames) or (max_frames and n >= max_frames):
+            break
+    return n, el
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+# ----------------------------------------------------------------------------
+# GPU leg
+# ----------------------------------------------------------------------------
+
+def run_ours(args, rank, world, dist):
+    import torch
+    from hairfb import renderer as R
+    from hairfb.lib import Context
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    inst = make_instance(args.workload, seed=rank)
+    stream = torch.cuda.current_stream()
+    ctx = Context(inst.cfg.to_c(), dev)
+    ctx.set_stream(stream)
+    r = R.Renderer(inst, ctx=ctx)
+    r.before_first_frame()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    names = ["grid_pre", "integrate", "grid_post", "clear", "tiles", "sort", "fine", "shading"]
+
+    def timed_frame(ev):
+        su = r.sim_uniforms(r.frame_idx)
+        ev[0].record(stream)
+        r.grid_pre.cmd_update_grids_before_sim(su, r.grids, r.sdf)
+        ev[1].record(stream)
+        r.integrate.cmd_simulate_hair_positions(su, r.hair, r.grids, r.sdf)
+        ev[2].record(stream)
+        r.grid_post.cmd_update_grids_after_sim(su, r.hair, r.grids)
+        ev[3].record(stream)
+        R.clear_before_render(r.ctx, r.rb)
+        ev[4].record(stream)
+        r.tiles.cmd_draw_hair_to_tiles(r.uniforms, r.hair, r.scene_depth, r.rb)
+        ev[5].record(stream)
+        r.sort.cmd_sort_hair_tiles(r.rb)
+        ev[6].record(stream)
+        r.fine.cmd_rasterize_slices_hair(r.uniforms, r.hair, r.scene_depth, r.rb)
+        ev[7].record(stream)
+        r.shading.cmd_compute_shading_points(r.uniforms, r.hair, r.shading_depth)
+        ev[8].record(stream)
+        r.frame_idx += 1
+
+    for _ in range(args.warmup):
+        r.frame()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    launches0 = ctx.counters()["launches"]
+    rec0 = ctx.counters()["tileRecords"]
+    frame_ms, pass_ms = [], {n: [] for n in names}
+    with ClockSampler(dev) as clk:
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            flush.fill_(1.0)  # L2 flush, outside the timed events
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(9)]
+            timed_frame(ev)
+            torch.cuda.synchronize()
+            frame_ms.append(ev[0].elapsed_time(ev[8]))
+            for i, n in enumerate(names):
+                pass_ms[n].append(ev[i].elapsed_time(ev[i + 1]))
+    launches = ctx.counters()["launches"] - launches0
+    records = (ctx.counters()["tileRecords"] - rec0) / args.steps
+    total_s = sum(frame_ms) / 1000.0
+
+    # ---- e2e through the public API with host buffers ----
+    from hairfb import uniforms as UN
+    depth_h = torch.from_numpy(inst.scene_depth).pin_memory()
+    img_h = torch.empty(4 + 4 * inst.width * inst.height, dtype=torch.float32).pin_memory()
+    depth_d = torch.empty_like(depth_h, device="cuda")
+    e2e_ms = []
+    for k in range(args.warmup + args.steps):
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        u = UN.pack_render_uniforms(inst.scene, inst.cfg)      # host-built uniform blocks
+        su = r.sim_uniforms(r.frame_idx)
+        depth_d.copy_(depth_h, non_blocking=True)               # scene depth H2D
+        r.uniforms = u
+        r.scene_depth = depth_d
+        r.grid_pre.cmd_update_grids_before_sim(su, r.grids, r.sdf)
+        r.integrate.cmd_simulate_hair_positions(su, r.hair, r.grids, r.sdf)
+        r.grid_post.cmd_update_grids_after_sim(su, r.hair, r.grids)
+        R.clear_before_render(r.ctx, r.rb)
+        r.tiles.cmd_draw_hair_to_tiles(u, r.hair, depth_d, r.rb)
+        r.sort.cmd_sort_hair_tiles(r.rb)
+        r.fine.cmd_rasterize_slices_hair(u, r.hair, depth_d, r.rb)
+        r.shading.cmd_compute_shading_points(u, r.hair, r.shading_depth)
+        r.frame_idx += 1
+        ctx.call("hfb_buffer_download", img_h.data_ptr(), r.rb.rb.rasterizerResult, img_h.numel() * 4)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        if k >= args.warmup:
+            e2e_ms.append(t0.elapsed_time(t1))
+    h2d = depth_h.numel() * 4 + UN.RENDER_UNIFORMS_BYTES + UN.SIM_UNIFORMS_BYTES
+    d2h = img_h.numel() * 4
+
+    out = dict(frame_ms=frame_ms, pass_ms=pass_ms, total_s=total_s, launches=launches, records=records,
+               e2e_ms=e2e_ms, h2d=h2d, d2h=d2h, clocks=clk.summary(), inst=inst)
+    ctx.close()
+    return out
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist_
+        dist = dist_
+        if args.impl == "reference":
+            # the host reference runs once, on rank 0
+            if rank != 0:
+                return
+            world = 1
+            dist = None
+        else:
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+            dist.init_process_group("nccl")
+
+    wl = args.workload
+    if args.impl == "reference":
+        inst = make_instance(wl, seed=0)
+        frame = cpu_frame_runner(inst)
+        for _ in range(max(1, min(args.warmup, 3))):
+            frame()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            frame()
+        el = time.perf_counter() - t0
+        n = args.steps
+        fps = n / el
+        cores = host_threads()
+        line = {
+            "impl": "reference", "metric": "frames/s", "value": fps, "unit": "frames/s",
+            "n_gpus": args.gpus, "steps": n, "warmup": max(1, min(args.warmup, 3)), "ms_per_step": 1000.0 * el / n,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": wl, "describe": WORKLOADS[wl],
+                       "implementation": "C restatement of the reference WGSL passes, OpenMP"},
+            "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
+                             "sample": f"{n} full frames of {wl} after warm-up frames"},
+            "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line), flush=True)
+        return
+
+    res = run_ours(args, rank, world, dist)
+    total = res["total_s"]
+    e2e_total = sum(res["e2e_ms"]) / 1000.0
+    if dist:
+        import torch
+        t = torch.tensor([total, e2e_total], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total, e2e_total = float(t[0]), float(t[1])
+        dist.barrier()
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    inst = res["inst"]
+    K = res["records"]
+    alg = algorithmic_bytes(inst, int(K))
+    pass_avg = {n: sum(v) / len(v) for n, v in res["pass_ms"].items()}
+    frame_avg = sum(res["frame_ms"]) / len(res["frame_ms"])
+    dominant = max(pass_avg, key=pass_avg.get)
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peak = json.load(open(peaks_path))["hbm_gbs"]
+        peak_src = "measured"
+    else:
+        peak, peak_src = 6800.0, "fallback"
+    achieved = alg[dominant] / (pass_avg[dominant] / 1000.0) / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        traffic = json.load(open(tp)).get(f"{wl}:{dominant}")
+    fps = world * len(res["frame_ms"]) / total
+    frame_bytes = sum(alg.values())
+    segments = inst.hair.asset.strands * (inst.hair.asset.points_per_strand - 1)
+    srt = sorted(res["frame_ms"])
+    p = lambda q: srt[min(len(srt) - 1, int(round(q * (len(srt) - 1))))]
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        n, el = time_cpu(inst, args.cpu_seconds)
+        cpu = {"value": n / el, "unit": "frames/s", "cores": host_threads(), "kind": "port",
+               "sample": f"{n} full frames of {wl} on the host (C restatement of the reference "
+                         f"WGSL, OpenMP) after 1 warm-up frame, {el:.1f} s"}
+
+    line = {
+        "metric": "frames/s", "value": fps, "unit": "frames/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": frame_avg,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded; no public dataset exists for this path)",
+        "config": {"workload": wl, "describe": WORKLOADS[wl], "l2": "flushed (256 MiB write) between frames",
+                   "p50_ms": p(0.5), "p99_ms": p(0.99), "segments_per_s": world * segments * len(srt) / total,
+                   "tile_records_per_frame": K, "pass_ms": {k: round(v, 4) for k, v in pass_avg.items()},
+                   "frame_algorithmic_bytes": frame_bytes,
+                   "frame_hbm_roofline_frac": frame_bytes * fps / world / (peak * 1e9)},
+        "e2e": {"value": world * len(res["e2e_ms"]) / e2e_total, "unit": "frames/s",
+                "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"]},
+        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
+                     "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                     "algorithmic_bytes": alg[dominant]},
+        "cpu_baseline": cpu,
+        "clocks": res["clocks"],
+        "gpu_launches": res["launches"],
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

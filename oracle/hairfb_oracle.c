@@ -37,6 +37,9 @@
 #include <string.h>
 #include <assert.h>
 #include <stddef.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #define EXPORT __attribute__((visibility("default")))
 
@@ -499,64 +502,98 @@ EXPORT void oracle_tiles_pass(const OracleConfig* cfg, const void* uniforms, con
   v2 depthBoundsVS = V2(bsVS.z - bs.w, bsVS.z + bs.w);
 
   uint32_t nStrands = strandsToRender < S ? strandsToRender : S;
-  for (uint32_t strand = 0; strand < nStrands; strand++) {
-    for (uint32_t seg = 0; seg + 1u < P; seg++) {
-      ProjSeg s = projectHairSegment(U, positions, tangents, P, strand, seg, size, U->fiberRadius);
-      v4 b = getRasterizedHairBounds(&s, size);
-      uint32_t tminx = f2u(b.x) / TS, tminy = f2u(b.y) / TS;
-      uint32_t tmaxx = f2u(b.z) / TS, tmaxy = f2u(b.w) / TS;
-      uint32_t tsx = (tmaxx - tminx) + 1u, tsy = (tmaxy - tminy) + 1u;
-      if (tsx * tsy > cfg->invalidTilesPerSegmentThreshold) continue;
-
-      for (uint32_t ty = tminy; ty <= tmaxy; ty++) {
-        for (uint32_t tx = tminx; tx <= tmaxx; tx++) {
-          /* processTile, hairTilesPass.wgsl.ts:139-238 */
-          TileBounds tb = getTileBoundsPx(W, H, TS, tx, ty);
-          float dmin = 999.0f, dmax = -999.0f;
-          uint32_t dbin = B;
-          for (uint32_t y = tb.y0; y < tb.y1; y++) {
-            for (uint32_t x = tb.x0; x < tb.x1; x++) {
-              v2 p = V2((float)x, (float)y);
-              float C0 = edgeFunction(s.v01, s.v00, p);
-              float C1 = edgeFunction(s.v11, s.v01, p);
-              float C2 = edgeFunction(s.v10, s.v11, p);
-              float C3 = edgeFunction(s.v00, s.v10, p);
-              if (C0 >= 0 && C1 >= 0 && C2 >= 0 && C3 >= 0) {
-                v2 w = interpolateHairQuad(&s, p);
-                float hd = interpolateHairF32(w, s.depthsProj);
-                float zb = loadTex2D(depth, W, H, (int64_t)x, (int64_t)H - (int64_t)y);
-                if (hd > zb) continue;
-                v3 vs = projectVertex(&U->projMatrixInv, V4(p.x, p.y, hd, 1.0f));
-                uint32_t bin = (B - 1u) - getDepthBin(B, depthBoundsVS, vs.z);
-                dmin = fmin_(dmin, hd);
-                dmax = fmax_(dmax, hd);
-                dbin = dbin < bin ? dbin : bin;
+  /* Phase 1 (parallel over strands, static contiguous ranges): every
+   * (segment, tile) that passes becomes a record, appended in canonical
+   * (strand, segment, tileY, tileX) order inside each thread's range. */
+  typedef struct { uint32_t strand, seg, tx, ty, bin; float dmin, dmax; } Rec;
+  int nth = 1;
+#ifdef _OPENMP
+  nth = omp_get_max_threads();
+#endif
+  Rec** recs = (Rec**)calloc((size_t)nth, sizeof(Rec*));
+  size_t* nrec = (size_t*)calloc((size_t)nth, sizeof(size_t));
+  size_t* caprec = (size_t*)calloc((size_t)nth, sizeof(size_t));
+#pragma omp parallel num_threads(nth)
+  {
+    int tid = 0;
+#ifdef _OPENMP
+    tid = omp_get_thread_num();
+#endif
+    uint32_t lo = (uint32_t)(((uint64_t)nStrands * (uint64_t)tid) / (uint64_t)nth);
+    uint32_t hi = (uint32_t)(((uint64_t)nStrands * (uint64_t)(tid + 1)) / (uint64_t)nth);
+    for (uint32_t strand = lo; strand < hi; strand++) {
+      for (uint32_t seg = 0; seg + 1u < P; seg++) {
+        ProjSeg s = projectHairSegment(U, positions, tangents, P, strand, seg, size, U->fiberRadius);
+        v4 b = getRasterizedHairBounds(&s, size);
+        uint32_t tminx = f2u(b.x) / TS, tminy = f2u(b.y) / TS;
+        uint32_t tmaxx = f2u(b.z) / TS, tmaxy = f2u(b.w) / TS;
+        uint32_t tsx = (tmaxx - tminx) + 1u, tsy = (tmaxy - tminy) + 1u;
+        if (tsx * tsy > cfg->invalidTilesPerSegmentThreshold) continue;
+        for (uint32_t ty = tminy; ty <= tmaxy; ty++) {
+          for (uint32_t tx = tminx; tx <= tmaxx; tx++) {
+            /* processTile, hairTilesPass.wgsl.ts:139-238 */
+            TileBounds tb = getTileBoundsPx(W, H, TS, tx, ty);
+            float dmin = 999.0f, dmax = -999.0f;
+            uint32_t dbin = B;
+            for (uint32_t y = tb.y0; y < tb.y1; y++) {
+              for (uint32_t x = tb.x0; x < tb.x1; x++) {
+                v2 p = V2((float)x, (float)y);
+                float C0 = edgeFunction(s.v01, s.v00, p);
+                float C1 = edgeFunction(s.v11, s.v01, p);
+                float C2 = edgeFunction(s.v10, s.v11, p);
+                float C3 = edgeFunction(s.v00, s.v10, p);
+                if (C0 >= 0 && C1 >= 0 && C2 >= 0 && C3 >= 0) {
+                  v2 w = interpolateHairQuad(&s, p);
+                  float hd = interpolateHairF32(w, s.depthsProj);
+                  float zb = loadTex2D(depth, W, H, (int64_t)x, (int64_t)H - (int64_t)y);
+                  if (hd > zb) continue;
+                  v3 vs = projectVertex(&U->projMatrixInv, V4(p.x, p.y, hd, 1.0f));
+                  uint32_t bin = (B - 1u) - getDepthBin(B, depthBoundsVS, vs.z);
+                  dmin = fmin_(dmin, hd);
+                  dmax = fmax_(dmax, hd);
+                  dbin = dbin < bin ? dbin : bin;
+                }
               }
             }
-          }
-          if (dmin > 1.0f) continue;
-          uint32_t nextPtr = segBuf[0]++;
-          if (nextPtr < maxDrawn) {
-            /* _storeTileHead, hairTilesResultBuffer.ts:14-42 */
-            uint32_t ti = ty * tilesX * B + tx * B + dbin;
-            uint32_t dmaxU = f2u(dmax * fMAX_U32);
-            uint32_t dminU = f2u((1.0f - dmin) * fMAX_U32);
-            uint32_t* head = tilesBuf + 4u * (size_t)ti;
-            if (dminU > head[0]) head[0] = dminU;
-            if (dmaxU > head[1]) head[1] = dmaxU;
-            uint32_t last = head[2];
-            head[2] = nextPtr + 1u;
-            uint32_t prevPtr = last == 0u ? INVALID_PTR : last - 1u;
-            /* _storeTileSegment, hairTileSegmentsBuffer.ts:22-29 */
-            segBuf[1u + 2u * (size_t)nextPtr] = (seg << 24) | strand;
-            segBuf[2u + 2u * (size_t)nextPtr] = prevPtr;
-            /* _incTileSegmentCount, segmentCountPerTileBuffer.ts:21-26 */
-            segCount[ty * tilesX + tx] += 1u;
+            if (dmin > 1.0f) continue;
+            if (nrec[tid] == caprec[tid]) {
+              caprec[tid] = caprec[tid] ? 2 * caprec[tid] : 1024;
+              recs[tid] = (Rec*)realloc(recs[tid], caprec[tid] * sizeof(Rec));
+            }
+            Rec r = {strand, seg, tx, ty, dbin, dmin, dmax};
+            recs[tid][nrec[tid]++] = r;
           }
         }
       }
     }
   }
+  /* Phase 2 (serial): allocate pointers and link the lists in canonical
+   * order, as one serial dispatch of the WGSL would. */
+  for (int t = 0; t < nth; t++) {
+    for (size_t i = 0; i < nrec[t]; i++) {
+      const Rec* r = &recs[t][i];
+      uint32_t nextPtr = segBuf[0]++;
+      if (nextPtr < maxDrawn) {
+        /* _storeTileHead, hairTilesResultBuffer.ts:14-42 */
+        uint32_t ti = r->ty * tilesX * B + r->tx * B + r->bin;
+        uint32_t dmaxU = f2u(r->dmax * fMAX_U32);
+        uint32_t dminU = f2u((1.0f - r->dmin) * fMAX_U32);
+        uint32_t* head = tilesBuf + 4u * (size_t)ti;
+        if (dminU > head[0]) head[0] = dminU;
+        if (dmaxU > head[1]) head[1] = dmaxU;
+        uint32_t last = head[2];
+        head[2] = nextPtr + 1u;
+        uint32_t prevPtr = last == 0u ? INVALID_PTR : last - 1u;
+        /* _storeTileSegment, hairTileSegmentsBuffer.ts:22-29 */
+        segBuf[1u + 2u * (size_t)nextPtr] = (r->seg << 24) | r->strand;
+        segBuf[2u + 2u * (size_t)nextPtr] = prevPtr;
+        /* _incTileSegmentCount, segmentCountPerTileBuffer.ts:21-26 */
+        segCount[r->ty * tilesX + r->tx] += 1u;
+      }
+    }
+    free(recs[t]);
+  }
+  free(recs); free(nrec); free(caprec);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -644,12 +681,16 @@ EXPORT void oracle_fine_pass(const OracleConfig* cfg, const void* uniforms, cons
   uint32_t dbgMax = dispMode == 4u ? ((U->displayMode >> 8) & 0xffffu) : 0u;
   int isDbg = dbgMax != 0u;
 
+  float* res = result + 4;
+  uint32_t drawnTiles = tileList[0];
+  /* tiles are independent (each writes only its own pixels): any order and
+   * any number of processors give the same result */
+#pragma omp parallel
+  {
   SliceEntry* pool = (SliceEntry*)malloc(sizeof(SliceEntry) * (size_t)CAP);
   uint32_t* heads = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)NPX * L);
   uint8_t* done = (uint8_t*)malloc(NPX);
-  float* res = result + 4;
-
-  uint32_t drawnTiles = tileList[0];
+#pragma omp for schedule(dynamic, 1)
   for (uint32_t q = 0; q < drawnTiles; q++) {
     uint32_t tileIdx = tileList[1u + q];
     if (tileIdx >= tileCount) continue;
@@ -754,8 +795,9 @@ EXPORT void oracle_fine_pass(const OracleConfig* cfg, const void* uniforms, cons
       if (all) break;
     }
   }
-  result[0] = 0.0f; /* queue counter is not modelled: processors are serial */
   free(pool); free(heads); free(done);
+  }
+  result[0] = 0.0f; /* the tile queue counter is not modelled */
 }
 
 /* ------------------------------------------------------------------------ */
@@ -870,6 +912,7 @@ EXPORT void oracle_grid_pre_sim(const OracleConfig* cfg, const void* simUniforms
   v3 gmax = V3(U->gridData.boundsMax[0], U->gridData.boundsMax[1], U->gridData.boundsMax[2]);
   v3 smin = xyz(U->sdf.boundsMin), smax = xyz(U->sdf.boundsMax);
   v3 cell = div3s(sub3(gmax, gmin), (float)(G - 1u));
+#pragma omp parallel for schedule(static)
   for (uint32_t id = 0; id < G * G * G; id++) {
     uint32_t z = id / (G * G);
     uint32_t idXY = id - z * G * G;
@@ -945,8 +988,10 @@ EXPORT void oracle_sim_integrate(const OracleConfig* cfg, const void* simUniform
   float sdfOffset = U->sdf.boundsMax.w; /* getSDF_Offset */
   v3 gravityForce = V3(0.0f, -U->gravity, 0.0f);
   v4 wind = U->wind;
+#pragma omp parallel
+  {
   v4* wk = (v4*)malloc(sizeof(v4) * P);
-
+#pragma omp for schedule(static)
   for (uint32_t strand = 0; strand < S; strand++) {
     const float* pn = positionsNow + 4u * (size_t)strand * P;
     const float* pp = positionsPrev + 4u * (size_t)strand * P;
@@ -1065,6 +1110,7 @@ EXPORT void oracle_sim_integrate(const OracleConfig* cfg, const void* simUniform
 #undef LD
   }
   free(wk);
+  }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1083,6 +1129,7 @@ EXPORT void oracle_grid_post_sim(const OracleConfig* cfg, const void* simUniform
   v3 gmax = V3(U->gridData.boundsMax[0], U->gridData.boundsMax[1], U->gridData.boundsMax[2]);
   uint32_t N = HD->strandsCount * HD->pointsPerStrand;
   uint32_t* g = (uint32_t*)densVel;
+#pragma omp parallel for schedule(static)
   for (uint32_t i = 0; i < N; i++) {
     v3 pp = V3(positionsPrev[4u * i], positionsPrev[4u * i + 1u], positionsPrev[4u * i + 2u]);
     v3 pn = V3(positionsNow[4u * i], positionsNow[4u * i + 1u], positionsNow[4u * i + 2u]);
@@ -1094,9 +1141,13 @@ EXPORT void oracle_grid_post_sim(const OracleConfig* cfg, const void* simUniform
           uint32_t idx = gridIdx(G, x, y, z);
           v3 w = cellWeights(x, y, z, co.pInGrid);
           v3 cv = mul3(vel, w);
+#pragma omp atomic
           g[4u * idx + 0u] += (uint32_t)gridEncode(cv.x);
+#pragma omp atomic
           g[4u * idx + 1u] += (uint32_t)gridEncode(cv.y);
+#pragma omp atomic
           g[4u * idx + 2u] += (uint32_t)gridEncode(cv.z);
+#pragma omp atomic
           g[4u * idx + 3u] += (uint32_t)gridEncode(len3(w));
         }
   }
@@ -1252,6 +1303,7 @@ EXPORT void oracle_shading(const OracleConfig* cfg, const void* uniforms, const 
   v2 vp = V2(U->viewport.x, U->viewport.y);
   uint32_t W = f2u(vp.x), H = f2u(vp.y);
   const OHairMaterial* m = &U->hairMaterial;
+#pragma omp parallel for schedule(static)
   for (uint32_t strand = 0; strand < HD->strandsCount; strand++) {
     for (uint32_t sp = 0; sp < SP; sp++) {
       float t = (float)sp / (float)SP;

@@ -21,29 +21,44 @@ LIB = os.path.join(BUILD, "libhairfb_oracle.so")
 LIB_OMP = os.path.join(BUILD, "libhairfb_oracle_omp.so")
 
 _lock = threading.Lock()
-_lib = None
+_libs = {}
+_threaded = False
 
 CFLAGS = ["-O2", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
-          "-Wall"]
+          "-Wall", "-Wno-unknown-pragmas"]
+
+
+def _build_one(out: str, extra, force: bool) -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    if force or not os.path.exists(out) or os.path.getmtime(out) < os.path.getmtime(SRC):
+        tmp = out + f".tmp{os.getpid()}"
+        subprocess.check_call(["gcc", *CFLAGS, *extra, "-o", tmp, SRC, "-lm"])
+        os.replace(tmp, out)
+    return out
 
 
 def build(force: bool = False) -> str:
-    """Compile the oracle (serial build) if the source is newer than the .so."""
-    os.makedirs(BUILD, exist_ok=True)
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
-        tmp = LIB + f".tmp{os.getpid()}"
-        subprocess.check_call(["gcc", *CFLAGS, "-o", tmp, SRC, "-lm"])
-        os.replace(tmp, LIB)
-    return LIB
+    """Compile both builds of the oracle: serial (the canonical checker) and
+    OpenMP (the same arithmetic on every host core, for the CPU baseline)."""
+    _build_one(LIB_OMP, ["-fopenmp"], force)
+    return _build_one(LIB, [], force)
 
 
-def load():
-    global _lib
+def use_threads(on: bool) -> None:
+    """Route subsequent calls to the OpenMP build (True) or the serial one."""
+    global _threaded
+    _threaded = bool(on)
+
+
+def load(threaded: bool | None = None):
+    t = _threaded if threaded is None else threaded
     with _lock:
-        if _lib is None:
-            _lib = ctypes.CDLL(build())
-            _declare(_lib)
-    return _lib
+        if t not in _libs:
+            build()
+            lib = ctypes.CDLL(LIB_OMP if t else LIB)
+            _declare(lib)
+            _libs[t] = lib
+    return _libs[t]
 
 
 def _declare(lib):

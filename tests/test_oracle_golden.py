@@ -96,3 +96,34 @@ def test_sdf_binary_rejects_bad_size():
     import pytest
     with pytest.raises(ValueError):
         formats.parse_sdf(data[:-4])
+
+
+def test_threaded_oracle_matches_serial(oracle):
+    """The OpenMP build of the oracle (CPU baseline) computes exactly what the
+    serial build does: the canonical list order survives the parallel raster."""
+    import helpers
+    inst = helpers.small_instance(strands=600)
+    fr = helpers.frame_of(inst)
+    hb = inst.hair
+    out = {}
+    for t in (False, True):
+        oracle.use_threads(t)
+        try:
+            tl = oracle.tiles_pass(inst.cfg, fr.uniforms, hb.hair_data, hb.asset.positions, hb.tangents,
+                                   inst.scene_depth, hb.asset.strands, inst.width, inst.height, fr.max_drawn)
+            b, lst = oracle.tile_sort(inst.cfg, inst.width, inst.height, tl[2])
+            sh = oracle.shading(inst.cfg, fr.uniforms, hb.hair_data, hb.asset.positions, hb.tangents,
+                                inst.scene_depth, hb.asset.strands)
+            fine = oracle.fine_pass(inst.cfg, fr.uniforms, hb.hair_data, hb.asset.positions, hb.tangents,
+                                    sh + 0.25, inst.scene_depth, tl[0], tl[1], lst, inst.width, inst.height)
+            dv = oracle.grid_post_sim(inst.cfg, fr.uniforms[:304], hb.hair_data, hb.asset.positions,
+                                      hb.asset.positions * 1.001)
+        finally:
+            oracle.use_threads(False)
+        out[t] = (tl, lst, sh, fine, dv)
+    for a, b in zip(out[False], out[True]):
+        if isinstance(a, tuple):
+            for x, y in zip(a, b):
+                assert np.array_equal(x, y)
+        else:
+            assert np.array_equal(a, b)
