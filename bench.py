@@ -230,7 +230,8 @@ def run_ours(args, rank, world, dist):
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     inst = make_instance(args.workload, seed=rank)
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()  # the library, the events and torch all run on it
+    torch.cuda.set_stream(stream)
     ctx = Context(inst.cfg.to_c(), dev)
     ctx.set_stream(stream)
     r = R.Renderer(inst, ctx=ctx)

@@ -138,9 +138,14 @@ class Context:
         self.check(getattr(self.lib, name)(self.handle, *args))
 
     def set_stream(self, stream) -> None:
-        """Run on a torch.cuda.Stream (or raw cudaStream_t int); None = own stream."""
-        s = None if stream is None else (stream if isinstance(stream, int) else stream.cuda_stream)
-        self.call("hfb_ctx_set_stream", s)
+        """Run on a torch.cuda.Stream (or raw cudaStream_t int); None = the
+        context's own stream.  Handle 0 (torch's default stream) is the
+        legacy default stream, passed as cudaStreamLegacy."""
+        if stream is None:
+            self.call("hfb_ctx_set_stream", None)
+            return
+        h = stream if isinstance(stream, int) else stream.cuda_stream
+        self.call("hfb_ctx_set_stream", h if h else 1)  # 1 == cudaStreamLegacy
 
     def sync(self) -> None:
         self.call("hfb_sync")

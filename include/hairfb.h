@@ -179,7 +179,8 @@ HFB_API int hfb_version(void);
 HFB_API int hfb_ctx_create(const HfbConfig* cfg, int device, HfbCtx** out);
 HFB_API int hfb_ctx_destroy(HfbCtx* ctx);
 HFB_API const char* hfb_last_error(const HfbCtx* ctx);
-/* Run subsequent calls on `stream` (a cudaStream_t); NULL restores the
+/* Run subsequent calls on `stream` (a cudaStream_t, including the special
+ * handles cudaStreamLegacy / cudaStreamPerThread); NULL restores the
  * context's own stream. */
 HFB_API int hfb_ctx_set_stream(HfbCtx* ctx, void* stream);
 /* Blocks until all work of the context's stream has finished. */
