@@ -76,6 +76,7 @@ SIGNATURES = {
     "hfb_tiles_pass": (I, [P, P, P, P, P, P, U32, P]),
     "hfb_tile_sort": (I, [P, P]),
     "hfb_fine_pass": (I, [P, P, P, P, P, P, P, P]),
+    "hfb_tiles_pass_noalloc": (I, [P, P, P, P, P, P, U32, P]),
 }
 
 _lock = threading.Lock()

@@ -262,6 +262,23 @@ HFB_API int hfb_fine_pass(HfbCtx* ctx, const HfbUniforms* u, const HfbHairData* 
                   const float* tangents, const float* shading, const float* depth,
                   HfbRasterBuffers* rb);
 
+/* No counterpart in the reference.  hfb_tiles_pass for callers that cannot
+ * allocate device memory (a render thread that must not take cudaMalloc's
+ * device-wide synchronisation, a host whose allocator owns every device
+ * byte, code about to record a stream capture).  Same inputs, outputs and
+ * results as hfb_tiles_pass, but the pass's working memory comes from one
+ * fixed array of HFB_NOALLOC_SCRATCH_BYTES compiled into the library, held
+ * by every GPU that loads it until exit; rb->scratch is ignored and may be
+ * NULL.  Viewports needing more (hfb_raster_scratch_bytes) are rejected with
+ * HFB_ERR_INVALID_ARGUMENT.  Calls share the array: calls whose work
+ * overlaps on the GPU race.  The first call on a device looks the array up
+ * (cudaGetSymbolAddress) and should come before any stream capture.  The
+ * call allocates nothing. */
+#define HFB_NOALLOC_SCRATCH_BYTES (16u << 20)
+HFB_API int hfb_tiles_pass_noalloc(HfbCtx* ctx, const HfbUniforms* u, const HfbHairData* hair,
+                                   const float* positions, const float* tangents, const float* depth,
+                                   uint32_t strandsToRender, HfbRasterBuffers* rb);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif
