@@ -41,7 +41,7 @@ import numpy as np  # noqa: E402
 WORKLOADS = {
     # BASELINE configs[1]: the single full frame
     "plain_full": "10,000 x 32 curly strands, 1920x1080, 16 px tiles, 16 depth bins, 4 slices, "
-                  "16 shading points, 4 iterations, 64^3 SDF, 32^3 grids, sinusoidal wind",
+                  "16 shading points, 4 iterations, 64^3 SDF, 64^3 grids, sinusoidal wind",
     # BASELINE configs[0]
     "plain_small": "2,000 x 16 strands, 640x480, 16 px tiles, 8 depth bins, 4 slices, 8 shading points",
     # BASELINE configs[4]

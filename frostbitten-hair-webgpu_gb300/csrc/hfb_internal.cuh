@@ -18,6 +18,10 @@ struct HfbCtx {
   // device-side counters: HfbDeviceCounters
   unsigned long long* dCounters = nullptr;
   uint64_t launches = 0;
+  // per-context launch set-up done once (kernel attributes, occupancy)
+  size_t simSmemSet = 0;
+  bool largeBinsAttrSet = false;
+  int fineBlocksPerSM[3][3] = {};  // [tile 8/16/32][slices 4/8/16]
 };
 
 namespace hfb {

@@ -145,6 +145,46 @@ __device__ __forceinline__ f2 interpolateHairQuad(const ProjSeg& s, f2 c) {
   return {sat(d0), sat(d1)};
 }
 
+// The pixel-independent parts of interpolateHairQuad, computed once per
+// segment with exactly the operations interpolateHairQuad performs, so the
+// per-pixel remainder (interpolateHairQuadPre) returns identical values.
+struct QuadConst {
+  f2 sm, ab;          // start-edge midpoint; end midpoint - start midpoint
+  float d2, lse;      // dot(ab, ab); length(sm - em)
+  float wS, wE;       // widthStart, widthEnd
+  f2 ab2;             // v10 - v00
+  float d22, pad;     // dot(ab2, ab2)
+};
+
+__device__ __forceinline__ QuadConst quadConst(const ProjSeg& s) {
+  QuadConst q;
+  q.sm = div2s(add2(s.v00, s.v01), 2.0f);
+  f2 em = div2s(add2(s.v10, s.v11), 2.0f);
+  q.ab = sub2(em, q.sm);
+  q.d2 = dot2(q.ab, q.ab);
+  q.lse = len2(sub2(q.sm, em));
+  q.wS = len2(sub2(s.v00, s.v01));
+  q.wE = fmul(q.wS, dot2(norm2(sub2(s.v00, s.v01)), norm2(sub2(s.v10, s.v11))));
+  q.ab2 = sub2(s.v10, s.v00);
+  q.d22 = dot2(q.ab2, q.ab2);
+  q.pad = 0.0f;
+  return q;
+}
+
+// interpolateHairQuad with the per-segment constants precomputed
+__device__ __forceinline__ f2 interpolateHairQuadPre(const QuadConst& q, f2 v00, f2 c) {
+  // cp = projectPointToLine(sm, em, c)
+  f2 ac = sub2(c, q.sm);
+  f2 cp = add2(q.sm, div2s(mul2s(q.ab, dot2(q.ab, ac)), q.d2));
+  float d1 = len2(sub2(cp, q.sm)) / q.lse;
+  float expectedWidth = mixf(q.wS, q.wE, d1);
+  // e1 = projectPointToLine(v00, v10, c)
+  f2 ac2 = sub2(c, v00);
+  f2 e1 = add2(v00, div2s(mul2s(q.ab2, dot2(q.ab2, ac2)), q.d22));
+  float d0 = len2(sub2(c, e1)) / expectedWidth;
+  return {sat(d0), sat(d1)};
+}
+
 // interpolateHairF32, swRasterizeHair.wgsl.ts:198-202
 __device__ __forceinline__ float interpolateHairF32(f2 w, f4 v) {
   return mixf(mixf(v.x, v.y, w.x), mixf(v.z, v.w, w.x), w.y);

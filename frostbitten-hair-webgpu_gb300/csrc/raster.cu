@@ -65,6 +65,55 @@ __device__ __forceinline__ bool insideQuad(const ProjSeg& s, f2 p) {
   return C0 >= 0.0f && C1 >= 0.0f && C2 >= 0.0f && C3 >= 0.0f;
 }
 
+// Candidate pixels of one row of a projected segment quad.  The four edge
+// functions are linear in x along a row, so the covered interval follows
+// from the edge equations: x = a.x + (y - a.y) * slope per edge.  Edges with
+// |slope| > 64 (nearly horizontal, ill conditioned) are skipped, which bounds
+// the fp32 error of the solved x by ~0.03 px at 4096 px; a 2-pixel margin
+// keeps every pixel the exact fp32 edge test accepts inside the candidate
+// range -- the exact test still decides each pixel.
+struct RowSpan {
+  float ax[4], ay[4], slope[4];
+  uint32_t lower;  // bit i: edge i bounds x from below (A > 0), else from above
+  uint32_t use;    // bit i: edge i is used
+  __device__ __forceinline__ void candidates(float y, uint32_t& x0, uint32_t& x1) const {
+    float lo = -1e30f, hi = 1e30f;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      if (!((use >> i) & 1u)) continue;
+      float b = ax[i] + (y - ay[i]) * slope[i];
+      if ((lower >> i) & 1u) lo = fmaxf(lo, b); else hi = fminf(hi, b);
+    }
+    if (!(lo <= hi + 4.0f)) { x1 = x0; return; }  // empty row (NaN-safe)
+    float l = floorf(lo) - 2.0f, h = ceilf(hi) + 3.0f;
+    if (l > (float)x0) x0 = (uint32_t)fminf(l, 4294967040.0f);
+    if (h < (float)x1) x1 = h < 0.0f ? 0u : (uint32_t)h;
+    if (x1 < x0) x1 = x0;
+  }
+};
+
+__device__ __forceinline__ RowSpan makeRowSpan(const ProjSeg& s) {
+  // edges in the order the test uses: v01->v00, v11->v01, v10->v11, v00->v10
+  const f2 a[4] = {s.v01, s.v11, s.v10, s.v00};
+  const f2 b[4] = {s.v00, s.v01, s.v11, s.v10};
+  RowSpan r;
+  r.lower = 0u;
+  r.use = 0u;
+  bool finite = true;
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const float A = b[i].y - a[i].y, Bx = b[i].x - a[i].x;
+    r.ax[i] = a[i].x;
+    r.ay[i] = a[i].y;
+    r.slope[i] = Bx / A;
+    if (fabsf(A) * 64.0f >= fabsf(Bx) + 1.0f) r.use |= 1u << i;
+    if (A > 0.0f) r.lower |= 1u << i;
+    finite = finite && isfinite(a[i].x) && isfinite(a[i].y);
+  }
+  if (!finite) r.use = 0u;
+  return r;
+}
+
 // ---------------------------------------------------------------------------
 // 1. tilesRaster: HairTilesPass.main + processTile, hairTilesPass.wgsl.ts:70-238
 // ---------------------------------------------------------------------------
@@ -99,17 +148,21 @@ tilesRasterKernel(const HfbUniforms U, uint32_t P, uint32_t nStrands, uint32_t T
   const float dv0 = fsub(bsVS.z, bsphere.w), dv1 = fadd(bsVS.z, bsphere.w);
   const uint32_t key = (strand << 8) | seg;
 
+  const RowSpan span = makeRowSpan(s);
   for (uint32_t ty = tminy; ty <= tmaxy; ty++) {
     for (uint32_t tx = tminx; tx <= tmaxx; tx++) {
       TileB tb = tileBoundsPx(W, H, TS, tx, ty);
       // Only pixel corners inside the segment's bounding rectangle can pass
-      // the four edge tests, so the walk is restricted to tile x rect.
+      // the four edge tests, so the walk is restricted to tile x rect, and
+      // per row to the candidate span around the covered interval.
       const uint32_t xa = max(tb.x0, ux0), xb = min(tb.x1, ux1 + 1u);
       const uint32_t ya = max(tb.y0, uy0), yb = min(tb.y1, uy1 + 1u);
       float dmin = 999.0f, dmax = -999.0f;
       uint32_t dbin = B;
       for (uint32_t y = ya; y < yb; y++) {
-        for (uint32_t x = xa; x < xb; x++) {
+        uint32_t x0r = xa, x1r = xb;
+        span.candidates((float)y, x0r, x1r);
+        for (uint32_t x = x0r; x < x1r; x++) {
           f2 p = mk2((float)x, (float)y);
           if (!insideQuad(s, p)) continue;
           f2 w = interpolateHairQuad(s, p);
@@ -237,7 +290,10 @@ __device__ __forceinline__ void writeList(uint32_t* __restrict__ segBuf, uint4* 
   uint32_t p = start + i;
   segBuf[1u + 2u * p] = ((key & 0xffu) << 24) | (key >> 8);
   segBuf[2u + 2u * p] = i == 0 ? INVALID_PTR : p - 1u;
-  if (i == n - 1u) tiles[ti].z = p + 1u;  // head pointer (+1, 0 = empty)
+  if (i == n - 1u) {
+    tiles[ti].z = p + 1u;  // head pointer (+1, 0 = empty)
+    tiles[ti].w = n;       // padding0: list length, a hint the fine pass verifies
+  }
 }
 
 __global__ void __launch_bounds__(256)
@@ -445,49 +501,28 @@ tileSortKernel(uint32_t T, uint32_t NB, uint32_t bucketSize, const uint32_t* __r
 // exactly: slots are counted per segment in pixel order and the list walk
 // stops after the segment that fills the pool.
 // ---------------------------------------------------------------------------
-constexpr uint32_t CHUNK = 32;
+constexpr uint32_t CHUNK = 32;     // segments per exact-path sub-chunk (32-bit masks)
+constexpr uint32_t STAGE = 256;    // segments staged in shared memory per round
+constexpr uint32_t NSHADE = 4;     // shading entries staged per segment
 
 struct FineShared {
-  ProjSeg seg[CHUNK];
-  uint32_t strand[CHUNK];
-  uint32_t segIdx[CHUNK];
-  uint32_t cnt[32][CHUNK];  // per-warp passing counts per segment (exact path)
-  uint32_t n, nextPtr, queueIdx;
+  ProjSeg seg[STAGE];
+  float4 shade[STAGE][NSHADE];  // the shading entries each segment can sample
+  uint32_t strand[STAGE];
+  uint32_t segIdx[STAGE];
+  uint32_t box[STAGE];       // tile-local pixel-corner bbox x0|y0<<8|x1<<16|y1<<24 (x0 > x1: empty)
+  uint32_t area[STAGE];      // pixels of the bbox (upper bound of the segment's fragments)
+  uint32_t shadeBase[STAGE]; // first staged shading index | count << 16
+  uint4 head[64];            // the tile's HairTileResult per depth bin
+  uint32_t binOff[65];       // whole-tile staging: first staged segment of each bin
+  uint32_t cnt[32][CHUNK];   // per-warp passing counts per segment (exact path)
+  uint32_t red[32];
+  uint32_t n, nextPtr, queueIdx, bad, tileMode, total;
   uint32_t cutSeg, cutSlots, chunkTotal;
 };
 
-// Colour of one fragment (processHairSegment.wgsl.ts:43-53), rounded through
-// f16 like pack2x16float (hairSlicesDataBuffer.ts:50-63), blended in front of
-// the slice's accumulated colour.
-template <int MAXL>
-__device__ __forceinline__ void addFragment(f4 (&acc)[MAXL], const ProjSeg& s, f2 w, float hd, uint32_t segIdx,
-                                            uint32_t strand, uint32_t P, uint32_t SP, uint32_t L, float td0,
-                                            float td1, uint32_t alphaQuadratic, float alphaMul,
-                                            const float4* __restrict__ shading) {
-  // getAlphaCoverage, processHairSegment.wgsl.ts:60-69
-  float alpha = fsub(1.0f, fabsf(fsub(fmul(w.x, 2.0f), 1.0f)));
-  if (alphaQuadratic) alpha = sqrtf(alpha);
-  alpha = sat(fmul(alpha, alphaMul));
-  float tFull = fadd((float)segIdx, w.y) / (float)(P - 1u);
-  // _sampleShading, hairShadingBuffer.ts:28-38
-  uint32_t i0, i1;
-  float fr = remapToIndices(SP, tFull, i0, i1);
-  const size_t sb = (size_t)strand * SP;
-  f4 c = mix4(ld4(__ldg(&shading[sb + i0])), ld4(__ldg(&shading[sb + i1])), fr);
-  c.w = fmul(c.w, alpha);
-  uint32_t sl = getDepthBin(L, td0, td1, hd);  // getSliceIdx
-  f4 q = mk4(__half2float(__float2half_rn(c.x)), __half2float(__float2half_rn(c.y)),
-             __half2float(__float2half_rn(c.z)), __half2float(__float2half_rn(c.w)));
-  float k = fsub(1.0f, q.w);
-#pragma unroll
-  for (int si = 0; si < MAXL; si++) {
-    if ((uint32_t)si == sl) {
-      acc[si].x = fadd(q.x, fmul(k, acc[si].x));
-      acc[si].y = fadd(q.y, fmul(k, acc[si].y));
-      acc[si].z = fadd(q.z, fmul(k, acc[si].z));
-      acc[si].w = fadd(q.w, fmul(k, acc[si].w));
-    }
-  }
+__device__ __forceinline__ bool inBox(uint32_t box, uint32_t lx, uint32_t ly) {
+  return lx >= (box & 0xffu) && ly >= ((box >> 8) & 0xffu) && lx <= ((box >> 16) & 0xffu) && ly <= (box >> 24);
 }
 
 // edge + depth test of processHairSegment (:5-31); fills w / hd when it passes
@@ -498,17 +533,223 @@ __device__ __forceinline__ bool fragmentPasses(const ProjSeg& s, f2 pp, float zb
   return hd < zbuf;  // depth test with GL_LESS (skip when >=)
 }
 
+// Colour of one fragment (processHairSegment.wgsl.ts:43-53), rounded through
+// f16 like pack2x16float (hairSlicesDataBuffer.ts:50-63), blended in front of
+// the slice's accumulated colour.  The two shading entries come from the
+// segment's staged copy (or global memory when outside it).
+template <int MAXL>
+__device__ __forceinline__ void addFragment(f4 (&acc)[MAXL], const FineShared& sh, uint32_t k, f2 w, float hd,
+                                            uint32_t P, uint32_t SP, uint32_t L, float td0, float td1,
+                                            uint32_t alphaQuadratic, float alphaMul,
+                                            const float4* __restrict__ shading) {
+  // getAlphaCoverage, processHairSegment.wgsl.ts:60-69
+  float alpha = fsub(1.0f, fabsf(fsub(fmul(w.x, 2.0f), 1.0f)));
+  if (alphaQuadratic) alpha = sqrtf(alpha);
+  alpha = sat(fmul(alpha, alphaMul));
+  float tFull = fadd((float)sh.segIdx[k], w.y) / (float)(P - 1u);
+  // _sampleShading, hairShadingBuffer.ts:28-38
+  uint32_t i0, i1;
+  float fr = remapToIndices(SP, tFull, i0, i1);
+  const uint32_t e0 = sh.shadeBase[k] & 0xffffu, ne = sh.shadeBase[k] >> 16;
+  float4 c0, c1;
+  if (i0 - e0 < ne && i1 - e0 < ne) {
+    c0 = sh.shade[k][i0 - e0];
+    c1 = sh.shade[k][i1 - e0];
+  } else {
+    const size_t sb = (size_t)sh.strand[k] * SP;
+    c0 = __ldg(&shading[sb + i0]);
+    c1 = __ldg(&shading[sb + i1]);
+  }
+  f4 c = mix4(ld4(c0), ld4(c1), fr);
+  c.w = fmul(c.w, alpha);
+  uint32_t sl = getDepthBin(L, td0, td1, hd);  // getSliceIdx
+  f4 q = mk4(__half2float(__float2half_rn(c.x)), __half2float(__float2half_rn(c.y)),
+             __half2float(__float2half_rn(c.z)), __half2float(__float2half_rn(c.w)));
+  float kk = fsub(1.0f, q.w);
+#pragma unroll
+  for (int si = 0; si < MAXL; si++) {
+    if ((uint32_t)si == sl) {
+      acc[si].x = fadd(q.x, fmul(kk, acc[si].x));
+      acc[si].y = fadd(q.y, fmul(kk, acc[si].y));
+      acc[si].z = fadd(q.z, fmul(kk, acc[si].z));
+      acc[si].w = fadd(q.w, fmul(kk, acc[si].w));
+    }
+  }
+}
+
+// Projects staged segment k, its tile-local bounding box, and stages the
+// shading entries its fragments can sample (tFull is monotonic in the
+// segment coordinate, so they are [i0(t = 0), i1(t = 1)]).
+template <int TS>
+__device__ __forceinline__ void projectStaged(const HfbUniforms& U, const float4* __restrict__ pos,
+                                              const float4* __restrict__ tan, const float4* __restrict__ shading,
+                                              uint32_t S, uint32_t P, uint32_t SP, f2 size, uint32_t x0,
+                                              uint32_t y0, FineShared& sh, uint32_t k) {
+  const uint32_t st = sh.strand[k], sg = sh.segIdx[k];
+  ProjSeg s;
+  uint32_t box = 0x00ff00ffu, area = 0, shadeBase = 0;  // empty
+  if (st < S && sg + 1u < P) {
+    s = projectSegment(U, pos, tan, P, st, sg, size);
+    // pixel corners that can pass the edge tests: [floor(min), ceil(max)]
+    float mnx = floorf(fminf(fminf(s.v00.x, s.v01.x), fminf(s.v10.x, s.v11.x))) - (float)x0;
+    float mny = floorf(fminf(fminf(s.v00.y, s.v01.y), fminf(s.v10.y, s.v11.y))) - (float)y0;
+    float mxx = ceilf(fmaxf(fmaxf(s.v00.x, s.v01.x), fmaxf(s.v10.x, s.v11.x))) - (float)x0;
+    float mxy = ceilf(fmaxf(fmaxf(s.v00.y, s.v01.y), fmaxf(s.v10.y, s.v11.y))) - (float)y0;
+    if (mnx <= mxx && mny <= mxy && mxx >= 0.0f && mxy >= 0.0f && mnx <= (float)(TS - 1) && mny <= (float)(TS - 1)) {
+      uint32_t bx0 = (uint32_t)fmaxf(mnx, 0.0f), by0 = (uint32_t)fmaxf(mny, 0.0f);
+      uint32_t bx1 = (uint32_t)fminf(mxx, (float)(TS - 1)), by1 = (uint32_t)fminf(mxy, (float)(TS - 1));
+      box = bx0 | (by0 << 8) | (bx1 << 16) | (by1 << 24);
+      area = (bx1 - bx0 + 1u) * (by1 - by0 + 1u);
+      uint32_t a0, a1, b0, b1;
+      remapToIndices(SP, fadd((float)sg, 0.0f) / (float)(P - 1u), a0, a1);
+      remapToIndices(SP, fadd((float)sg, 1.0f) / (float)(P - 1u), b0, b1);
+      const uint32_t ne = min(b1 - a0 + 1u, NSHADE);
+      const size_t sb = (size_t)st * SP;
+      for (uint32_t e = 0; e < ne; e++) sh.shade[k][e] = __ldg(&shading[sb + a0 + e]);
+      shadeBase = a0 | (ne << 16);
+    }
+  } else {  // not a segment of this hair: covers no pixel
+    const float nan = __int_as_float(0x7fffffff);
+    s.v00 = s.v01 = s.v10 = s.v11 = mk2(nan, nan);
+    s.depthsProj = mk4(nan, nan, nan, nan);
+  }
+  sh.seg[k] = s;
+  sh.box[k] = box;
+  sh.area[k] = area;
+  sh.shadeBase[k] = shadeBase;
+}
+
+// Block-wide sum (all threads call; every thread gets the total).
+template <int NW>
+__device__ __forceinline__ uint32_t blockSum(uint32_t v, FineShared& sh, uint32_t lane, uint32_t warp) {
+  const uint32_t w = __reduce_add_sync(0xffffffffu, v);
+  if (lane == 0) sh.red[warp] = w;
+  __syncthreads();
+  uint32_t t = 0;
+#pragma unroll
+  for (int i = 0; i < NW; i++) t += sh.red[i];
+  __syncthreads();
+  return t;
+}
+
+// Per-bin state of one pixel and of the whole tile (uniform members).
+template <int MAXL>
+struct BinState {
+  f4 acc[MAXL];
+  uint32_t nFrag, pending;            // per pixel
+  uint32_t running, runningUB;        // uniform: slots allocated (exact / upper bound)
+  bool stop;                          // uniform: the pool filled
+};
+
+// Rasterizes staged segments [s0, s0 + n) of the current bin in list order
+// (processHairSegment for every pixel), keeping the reference's fragment
+// pool accounting exact.  Called by every thread of the CTA.
 template <int TS, int MAXL>
-__global__ void __launch_bounds__(TS * TS)
+__device__ __forceinline__ void rasterRange(BinState<MAXL>& st, FineShared& sh, uint32_t s0, uint32_t n,
+                                            uint32_t active, uint32_t CAP, bool done, f2 pp, float zbuf,
+                                            uint32_t lx, uint32_t ly, uint32_t lane, uint32_t warp, uint32_t tid,
+                                            uint32_t P, uint32_t SP, uint32_t L, float td0, float td1,
+                                            uint32_t alphaQuadratic, float alphaMul,
+                                            const float4* __restrict__ shading,
+                                            DeviceCounters* __restrict__ counters) {
+  constexpr int NW = TS * TS / 32;
+  for (uint32_t c0 = s0; c0 < s0 + n && !st.stop; c0 += CHUNK) {
+    const uint32_t cn = min(CHUNK, s0 + n - c0);
+    uint32_t bound = 0;
+    for (uint32_t j = 0; j < cn; j++) bound += min(sh.area[c0 + j], active);
+    if (st.runningUB + bound > CAP) {  // tighten: exact count of what was added so far
+      st.running += blockSum<NW>(st.pending, sh, lane, warp);
+      st.pending = 0;
+      st.runningUB = st.running;
+    }
+    if (st.runningUB + bound <= CAP) {
+      // ---- fast path: the pool cannot fill inside this sub-chunk ----
+      if (!done) {
+        for (uint32_t j = c0; j < c0 + cn; j++) {
+          if (!inBox(sh.box[j], lx, ly)) continue;
+          f2 w; float hd;
+          if (!fragmentPasses(sh.seg[j], pp, zbuf, w, hd)) continue;
+          st.pending++;
+          st.nFrag++;
+          addFragment<MAXL>(st.acc, sh, j, w, hd, P, SP, L, td0, td1, alphaQuadratic, alphaMul, shading);
+        }
+      }
+      st.runningUB += bound;
+    } else {
+      // ---- exact path: slots in pixel order, stop at the filling segment ----
+      uint32_t mask = 0;
+      if (!done) {
+        for (uint32_t j = 0; j < cn; j++) {
+          if (!inBox(sh.box[c0 + j], lx, ly)) continue;
+          f2 w; float hd;
+          if (fragmentPasses(sh.seg[c0 + j], pp, zbuf, w, hd)) mask |= 1u << j;
+        }
+      }
+      for (uint32_t j = 0; j < cn; j++) {
+        const uint32_t bal = __ballot_sync(0xffffffffu, (mask >> j) & 1u);
+        if (lane == 0) sh.cnt[warp][j] = __popc(bal);
+      }
+      __syncthreads();
+      if (warp == 0) {
+        uint32_t c = 0;
+        if (lane < cn)
+          for (int w2 = 0; w2 < NW; w2++) c += sh.cnt[w2][lane];
+        uint32_t incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= (uint32_t)o) incl += y;
+        }
+        const uint32_t fb = __ballot_sync(0xffffffffu, lane < cn && st.running + incl >= CAP);
+        const uint32_t j = fb ? (uint32_t)(__ffs(fb) - 1) : 0u;
+        const uint32_t exclJ = __shfl_sync(0xffffffffu, incl - c, j);
+        const uint32_t total = __shfl_sync(0xffffffffu, incl, cn - 1u);
+        if (lane == 0) {
+          sh.cutSeg = fb ? j : CHUNK;
+          sh.cutSlots = fb ? CAP - (st.running + exclJ) : 0u;
+          sh.chunkTotal = total;
+        }
+      }
+      __syncthreads();
+      const uint32_t cutSeg = sh.cutSeg, cutSlots = sh.cutSlots;
+      uint32_t m = mask;
+      if (cutSeg < CHUNK) {
+        uint32_t rank = 0;  // slots taken in the cut segment by lower pixels
+        for (uint32_t w2 = 0; w2 < warp; w2++) rank += sh.cnt[w2][cutSeg];
+        rank += __popc(__ballot_sync(0xffffffffu, (mask >> cutSeg) & 1u) & ((1u << lane) - 1u));
+        m &= cutSeg == 31u ? 0xffffffffu : ((2u << cutSeg) - 1u);  // segments <= cut
+        if (rank >= cutSlots) m &= ~(1u << cutSeg);
+      }
+      while (m) {
+        const uint32_t j = __ffs(m) - 1u;
+        m &= m - 1u;
+        f2 w; float hd;
+        fragmentPasses(sh.seg[c0 + j], pp, zbuf, w, hd);
+        addFragment<MAXL>(st.acc, sh, c0 + j, w, hd, P, SP, L, td0, td1, alphaQuadratic, alphaMul, shading);
+        st.nFrag++;
+      }
+      st.running = cutSeg < CHUNK ? CAP : st.running + sh.chunkTotal;
+      st.runningUB = st.running;
+      if (st.running >= CAP) {
+        if (tid == 0) atomicAdd(&counters->finePoolFullBins, 1ull);
+        st.stop = true;  // the reference breaks after the filling segment
+      }
+      __syncthreads();  // sh.cnt / cut words are reused
+    }
+  }
+}
+
+template <int TS, int MAXL>
+__global__ void __launch_bounds__(TS * TS, TS == 16 ? (MAXL <= 4 ? 3 : 2) : 1)
 fineKernel(const HfbUniforms U, uint32_t S, uint32_t P, uint32_t B, uint32_t L, uint32_t SP, uint32_t CAP,
            uint32_t alphaQuadratic, float alphaMul, const float4* __restrict__ pos, const float4* __restrict__ tan,
            const float4* __restrict__ shading, const float* __restrict__ depth, const uint4* __restrict__ tiles,
            const uint32_t* __restrict__ segBuf, const uint32_t* __restrict__ tileList,
            float* __restrict__ result, DeviceCounters* __restrict__ counters) {
   constexpr uint32_t NPX = TS * TS;
-  constexpr uint32_t NW = NPX / 32;
   __shared__ FineShared sh;
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const uint32_t lx = tid % TS, ly = tid / TS;
   const f2 size = mk2(U.viewport.x, U.viewport.y);
   const uint32_t W = f2u(size.x), H = f2u(size.y);
   const uint32_t tilesX = divCeil(W, TS), tileCount = tilesX * divCeil(H, TS);
@@ -527,184 +768,182 @@ fineKernel(const HfbUniforms U, uint32_t S, uint32_t P, uint32_t B, uint32_t L, 
     if (tid == 0) sh.queueIdx = atomicAdd(queue, 1u);  // getNextTileIdx, :294-303
     __syncthreads();
     const uint32_t q = sh.queueIdx;
-    __syncthreads();
     if (q >= drawnTiles) break;
     const uint32_t tileIdx = tileList[1u + q];
-    if (tileIdx >= tileCount) continue;
+    if (tileIdx >= tileCount) { __syncthreads(); continue; }
     const uint32_t tx = tileIdx % tilesX, ty = tileIdx / tilesX;
     const TileB tbp = tileBoundsPx(W, H, TS, tx, ty);
-    const uint32_t px = tbp.x0 + tid % TS, py = tbp.y0 + tid / TS;
+    const uint32_t px = tbp.x0 + lx, py = tbp.y0 + ly;
     // Pixels of a partial edge tile outside the viewport take no part.
     const bool inView = px < W && py < H;
     const f2 pp = mk2((float)px, (float)py);
     const float zbuf = inView ? loadTex2DClamp(depth, W, H, f2i(pp.x), f2i(fsub(size.y, pp.y))) : 0.0f;
     bool done = !inView;
     f4 fin = mk4(0.f, 0.f, 0.f, 0.f);  // rasterizerResult was cleared before the pass
+    if (tid < B) sh.head[tid] = tiles[ty * tilesX * B + tx * B + tid];
+    __syncthreads();
+
+    // ---- whole-tile staging: every bin's list at once when the lists carry
+    // a length hint (padding0, written by the tiles pass) that checks out ----
+    if (warp == 0) {
+      uint32_t ok = 1, sum = 0;
+      for (uint32_t b0 = 0; b0 < B; b0 += 32) {
+        const uint32_t bb = b0 + lane;
+        uint32_t nb = 0;
+        if (bb < B) {
+          const uint4 h = sh.head[bb];
+          const bool nonEmpty = (float)h.y / F_MAX_U32 != 0.0f && h.z != 0u;
+          if (nonEmpty) {
+            if (h.w != 0u && h.w <= h.z && h.z <= maxDrawn) nb = h.w; else ok = 0;
+          }
+        }
+        uint32_t incl = nb;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= (uint32_t)o) incl += y;
+        }
+        if (bb < B) sh.binOff[bb] = sum + incl - nb;
+        sum += __shfl_sync(0xffffffffu, incl, 31);
+      }
+      ok = __all_sync(0xffffffffu, ok);
+      if (lane == 0) {
+        sh.binOff[B] = sum;
+        sh.total = sum;
+        sh.tileMode = ok && sum <= STAGE && sum <= maxProcessed;
+        sh.bad = 0;
+      }
+    }
+    __syncthreads();
+    bool tileMode = sh.tileMode != 0u;
+    if (tileMode) {
+      const uint32_t total = sh.total;
+      for (uint32_t k = tid; k < total; k += NPX) {
+        uint32_t lo = 0, hi = B;  // bin of k: binOff[lo] <= k < binOff[lo + 1]
+        while (hi - lo > 1u) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if (sh.binOff[mid] <= k) lo = mid; else hi = mid;
+        }
+        const uint4 h = sh.head[lo];
+        const uint32_t j = k - sh.binOff[lo];
+        const uint32_t idx = h.z - 1u - j;
+        const uint32_t enc = __ldg(&segBuf[1u + 2u * idx]);
+        const uint32_t nxt = __ldg(&segBuf[2u + 2u * idx]);
+        if (nxt != ((j + 1u == h.w) ? INVALID_PTR : idx - 1u)) sh.bad = 1;
+        sh.strand[k] = enc & 0x00ffffffu;
+        sh.segIdx[k] = enc >> 24;
+      }
+      __syncthreads();
+      tileMode = sh.bad == 0u;
+      if (tileMode) {
+        for (uint32_t k = tid; k < total; k += NPX)
+          projectStaged<TS>(U, pos, tan, shading, S, P, SP, size, tbp.x0, tbp.y0, sh, k);
+      }
+      __syncthreads();
+    }
 
     for (uint32_t bin = 0; bin < B; bin++) {
-      const uint4 head = tiles[ty * tilesX * B + tx * B + bin];
+      const uint4 head = sh.head[bin];
       // _getTileDepth, hairTilesResultBuffer.ts:47-54
       const float td0 = (float)(0xffffffffu - head.x) / F_MAX_U32;
       const float td1 = (float)head.y / F_MAX_U32;
       if (td1 != 0.0f) {  // processTile, :205-288
-        f4 acc[MAXL];
+        BinState<MAXL> st;
 #pragma unroll
-        for (int si = 0; si < MAXL; si++) acc[si] = mk4(0.f, 0.f, 0.f, 0.f);
-        uint32_t nFrag = 0;
+        for (int si = 0; si < MAXL; si++) st.acc[si] = mk4(0.f, 0.f, 0.f, 0.f);
+        st.nFrag = 0; st.pending = 0; st.running = 0; st.runningUB = 0; st.stop = false;
         const uint32_t active = __syncthreads_count(!done);
-        uint32_t running = 0;  // slots allocated so far (sliceDataOffset)
-        uint32_t ptr = head.z == 0u ? INVALID_PTR : head.z - 1u;
-        uint32_t processed = 0;
-        while (true) {
-          // ---- next chunk of the list, read by warp 0 ----
-          if (warp == 0) {
-            uint32_t p = ptr, n = 0;
-            while (n < CHUNK && p != INVALID_PTR && p < maxDrawn && processed + n < maxProcessed) {
-              const uint32_t want = min(CHUNK - n, maxProcessed - processed - n);
-              // speculate that the list runs p, p-1, p-2, ... (the layout the
-              // tiles pass writes); the first entry that does not chain on
-              // ends the run and its `next` is followed
-              const uint32_t cand = p - lane;
-              const bool inRange = lane < want && lane <= p;
-              uint2 e = make_uint2(0u, INVALID_PTR);
-              if (inRange) {
-                e.x = __ldg(&segBuf[1u + 2u * cand]);
-                e.y = __ldg(&segBuf[2u + 2u * cand]);
+        if (tileMode) {
+          const uint32_t s0 = sh.binOff[bin], n = sh.binOff[bin + 1] - s0;
+          rasterRange<TS, MAXL>(st, sh, s0, n, active, CAP, done, pp, zbuf, lx, ly, lane, warp, tid, P, SP, L,
+                                td0, td1, alphaQuadratic, alphaMul, shading, counters);
+        } else {
+          // ---- per-bin staging: runs of the list (hinted contiguous runs in
+          // parallel, otherwise a warp walks it) ----
+          uint32_t ptr = head.z == 0u ? INVALID_PTR : head.z - 1u;
+          uint32_t hint = (head.w != 0u && head.w <= head.z && head.z <= maxDrawn) ? head.w : 0u;
+          uint32_t processed = 0;
+          while (!st.stop && ptr != INVALID_PTR && ptr < maxDrawn && processed < maxProcessed) {
+            uint32_t n = 0;
+            if (hint) {
+              n = min(min(hint, STAGE), maxProcessed - processed);
+              if (tid == 0) sh.bad = 0;
+              __syncthreads();
+              for (uint32_t k = tid; k < n; k += NPX) {
+                const uint32_t idx = ptr - k;
+                const uint32_t enc = __ldg(&segBuf[1u + 2u * idx]);
+                const uint32_t nxt = __ldg(&segBuf[2u + 2u * idx]);
+                if (nxt != ((k + 1u == hint) ? INVALID_PTR : idx - 1u)) sh.bad = 1;
+                sh.strand[k] = enc & 0x00ffffffu;
+                sh.segIdx[k] = enc >> 24;
               }
-              const bool chain = inRange && e.y == cand - 1u;
-              const uint32_t brk = __ballot_sync(0xffffffffu, !chain);
-              const uint32_t first = brk ? (uint32_t)(__ffs(brk) - 1) : 32u;
-              bool firstIn = false;
-              uint32_t firstNext = 0u;
-              if (first < 32u) {
-                firstIn = __shfl_sync(0xffffffffu, inRange, first);
-                firstNext = __shfl_sync(0xffffffffu, e.y, first);
+              __syncthreads();
+              if (sh.bad) {
+                hint = 0;  // not the contiguous layout: walk it
+                continue;
               }
-              const uint32_t cnt = firstIn ? first + 1u : first;
-              if (lane < cnt) {
-                sh.strand[n + lane] = e.x & 0x00ffffffu;
-                sh.segIdx[n + lane] = e.x >> 24;
+              if (tid == 0) sh.nextPtr = (n == hint) ? INVALID_PTR : ptr - n;
+              hint -= n;
+            } else {
+              if (warp == 0) {  // speculative contiguous runs, else pointer chasing
+                uint32_t p = ptr, m = 0;
+                while (m < CHUNK && p != INVALID_PTR && p < maxDrawn && processed + m < maxProcessed) {
+                  const uint32_t want = min(CHUNK - m, maxProcessed - processed - m);
+                  const uint32_t cand = p - lane;
+                  const bool inRange = lane < want && lane <= p;
+                  uint2 e = make_uint2(0u, INVALID_PTR);
+                  if (inRange) {
+                    e.x = __ldg(&segBuf[1u + 2u * cand]);
+                    e.y = __ldg(&segBuf[2u + 2u * cand]);
+                  }
+                  const bool chain = inRange && e.y == cand - 1u;
+                  const uint32_t brk = __ballot_sync(0xffffffffu, !chain);
+                  const uint32_t first = brk ? (uint32_t)(__ffs(brk) - 1) : 32u;
+                  bool firstIn = false;
+                  uint32_t firstNext = 0u;
+                  if (first < 32u) {
+                    firstIn = __shfl_sync(0xffffffffu, inRange, first);
+                    firstNext = __shfl_sync(0xffffffffu, e.y, first);
+                  }
+                  const uint32_t cnt = firstIn ? first + 1u : first;
+                  if (lane < cnt) {
+                    sh.strand[m + lane] = e.x & 0x00ffffffu;
+                    sh.segIdx[m + lane] = e.x >> 24;
+                  }
+                  m += cnt;
+                  p = firstIn ? firstNext : p - cnt;
+                }
+                if (lane == 0) { sh.n = m; sh.nextPtr = p; }
               }
-              n += cnt;
-              p = firstIn ? firstNext : p - cnt;
+              __syncthreads();
+              n = sh.n;
             }
-            if (lane == 0) { sh.n = n; sh.nextPtr = p; }
-          }
-          __syncthreads();
-          const uint32_t n = sh.n;
-          if (n == 0) break;
-          // ---- project the chunk, one thread per segment ----
-          if (tid < n) {
-            const uint32_t st = sh.strand[tid], sg = sh.segIdx[tid];
-            if (st < S && sg + 1u < P) {
-              sh.seg[tid] = projectSegment(U, pos, tan, P, st, sg, size);
-            } else {  // not a segment of this hair: covers no pixel
-              const float nan = __int_as_float(0x7fffffff);
-              sh.seg[tid].v00 = sh.seg[tid].v01 = sh.seg[tid].v10 = sh.seg[tid].v11 = mk2(nan, nan);
-              sh.seg[tid].depthsProj = mk4(nan, nan, nan, nan);
-            }
-          }
-          __syncthreads();
-
-          if (running + active * n <= CAP) {
-            // ---- fast path: the pool cannot fill inside this chunk ----
-            uint32_t myCount = 0;
-            if (!done) {
-              for (uint32_t j = 0; j < n; j++) {
-                f2 w; float hd;
-                if (!fragmentPasses(sh.seg[j], pp, zbuf, w, hd)) continue;
-                myCount++;
-                addFragment<MAXL>(acc, sh.seg[j], w, hd, sh.segIdx[j], sh.strand[j], P, SP, L, td0, td1,
-                                  alphaQuadratic, alphaMul, shading);
-              }
-            }
-            nFrag += myCount;
-            const uint32_t wsum = __reduce_add_sync(0xffffffffu, myCount);
-            if (lane == 0) sh.cnt[warp][0] = wsum;
+            if (n == 0) break;
+            for (uint32_t k = tid; k < n; k += NPX)
+              projectStaged<TS>(U, pos, tan, shading, S, P, SP, size, tbp.x0, tbp.y0, sh, k);
             __syncthreads();
-            uint32_t tot = 0;
-#pragma unroll
-            for (uint32_t w2 = 0; w2 < NW; w2++) tot += sh.cnt[w2][0];
-            running += tot;
-          } else {
-            // ---- exact path: slots in pixel order, stop at the filling segment ----
-            uint32_t mask = 0;
-            if (!done) {
-              for (uint32_t j = 0; j < n; j++) {
-                f2 w; float hd;
-                if (fragmentPasses(sh.seg[j], pp, zbuf, w, hd)) mask |= 1u << j;
-              }
-            }
-            for (uint32_t j = 0; j < n; j++) {
-              const uint32_t bal = __ballot_sync(0xffffffffu, (mask >> j) & 1u);
-              if (lane == 0) sh.cnt[warp][j] = __popc(bal);
-            }
-            __syncthreads();
-            if (warp == 0) {
-              uint32_t c = 0;
-              if (lane < n)
-                for (uint32_t w2 = 0; w2 < NW; w2++) c += sh.cnt[w2][lane];
-              uint32_t incl = c;
-#pragma unroll
-              for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= (uint32_t)o) incl += y;
-              }
-              const uint32_t fb = __ballot_sync(0xffffffffu, lane < n && running + incl >= CAP);
-              const uint32_t j = fb ? (uint32_t)(__ffs(fb) - 1) : 0u;
-              const uint32_t exclJ = __shfl_sync(0xffffffffu, incl - c, j);
-              const uint32_t total = __shfl_sync(0xffffffffu, incl, n - 1u);
-              if (lane == 0) {
-                sh.cutSeg = fb ? j : CHUNK;
-                sh.cutSlots = fb ? CAP - (running + exclJ) : 0u;
-                sh.chunkTotal = total;
-              }
-            }
-            __syncthreads();
-            const uint32_t cutSeg = sh.cutSeg, cutSlots = sh.cutSlots;
-            uint32_t m = mask;
-            if (cutSeg < CHUNK) {
-              uint32_t rank = 0;  // slots taken in the cut segment by lower pixels
-              for (uint32_t w2 = 0; w2 < warp; w2++) rank += sh.cnt[w2][cutSeg];
-              rank += __popc(__ballot_sync(0xffffffffu, (mask >> cutSeg) & 1u) & ((1u << lane) - 1u));
-              m &= cutSeg == 31u ? 0xffffffffu : ((2u << cutSeg) - 1u);  // segments <= cut
-              if (rank >= cutSlots) m &= ~(1u << cutSeg);
-            }
-            while (m) {
-              const uint32_t j = __ffs(m) - 1u;
-              m &= m - 1u;
-              f2 w; float hd;
-              fragmentPasses(sh.seg[j], pp, zbuf, w, hd);
-              addFragment<MAXL>(acc, sh.seg[j], w, hd, sh.segIdx[j], sh.strand[j], P, SP, L, td0, td1,
-                                alphaQuadratic, alphaMul, shading);
-              nFrag++;
-            }
-            running = cutSeg < CHUNK ? CAP : running + sh.chunkTotal;
+            const uint32_t nextPtr = sh.nextPtr;
+            rasterRange<TS, MAXL>(st, sh, 0, n, active, CAP, done, pp, zbuf, lx, ly, lane, warp, tid, P, SP, L,
+                                  td0, td1, alphaQuadratic, alphaMul, shading, counters);
+            processed += n;
+            __syncthreads();  // the staged run is refilled next iteration
+            ptr = nextPtr;
           }
-          processed += n;
-          const uint32_t nextPtr = sh.nextPtr;
-          __syncthreads();  // the chunk buffers are refilled next iteration
-          if (running >= CAP) {
-            if (tid == 0) atomicAdd(&counters->finePoolFullBins, 1ull);
-            break;
-          }
-          ptr = nextPtr;
-          if (ptr == INVALID_PTR || ptr >= maxDrawn || processed >= maxProcessed) break;
         }
         // reduceHairSlices (runs for every non-empty bin, as in the reference)
         if (!done) {
           if (isDbg) {
-            const uint32_t cntAll = f2u(fmul(fin.x, (float)dbgMax)) + nFrag;
+            const uint32_t cntAll = f2u(fmul(fin.x, (float)dbgMax)) + st.nFrag;
             fin = mk4(sat((float)cntAll / (float)dbgMax), 0.0f, 0.0f, 1.0f);
           } else {
 #pragma unroll
             for (int si = 0; si < MAXL; si++) {
               if ((uint32_t)si < L && fin.w < 0.999f) {
                 const float k = fsub(1.0f, fin.w);
-                fin.x = fadd(fin.x, fmul(acc[si].x, k));
-                fin.y = fadd(fin.y, fmul(acc[si].y, k));
-                fin.z = fadd(fin.z, fmul(acc[si].z, k));
-                fin.w = fadd(fin.w, fmul(acc[si].w, k));
+                fin.x = fadd(fin.x, fmul(st.acc[si].x, k));
+                fin.y = fadd(fin.y, fmul(st.acc[si].y, k));
+                fin.z = fadd(fin.z, fmul(st.acc[si].z, k));
+                fin.w = fadd(fin.w, fmul(st.acc[si].w, k));
               }
             }
             done = fin.w >= 0.999f;  // isPixelDone with ALPHA_CUTOFF
@@ -715,6 +954,7 @@ fineKernel(const HfbUniforms U, uint32_t S, uint32_t P, uint32_t B, uint32_t L, 
       if (__syncthreads_and(done)) break;
     }
     if (inView) res[(size_t)py * W + px] = make_float4(fin.x, fin.y, fin.z, fin.w);
+    __syncthreads();  // the tile's shared state is rewritten for the next tile
   }
 }
 
@@ -722,8 +962,8 @@ template <int TS, int MAXL>
 cudaError_t launchFineT(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, const float* pos,
                         const float* tan, const float* shading, const float* depth, HfbRasterBuffers& rb) {
   const HfbConfig& cfg = c->cfg;
-  int perSM = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, fineKernel<TS, MAXL>, TS * TS, 0);
+  int& perSM = c->fineBlocksPerSM[TS == 8 ? 0 : TS == 16 ? 1 : 2][MAXL == 4 ? 0 : MAXL == 8 ? 1 : 2];
+  if (perSM == 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, fineKernel<TS, MAXL>, TS * TS, 0);
   uint32_t grid = cfg.processorCount ? cfg.processorCount : (uint32_t)(max(perSM, 1) * c->smCount);
   uint32_t CAP = cfg.avgFragmentsPerSlice * cfg.slicesPerPixel * cfg.tileSize * cfg.tileSize;
   fineKernel<TS, MAXL><<<grid, TS * TS, 0, c->stream>>>(
@@ -763,8 +1003,11 @@ cudaError_t launchTilesPass(HfbCtx* c, const HfbUniforms& u, const HfbHairData& 
                                                           s.blockSums, s.keys, dc);
   binFinalizeKernel<<<min(divCeil(TB, 8), (uint32_t)c->smCount * 16), 256, 0, c->stream>>>(
       TB, s.binCount, s.binOffset, s.blockSums, s.keys, rb.tileSegments, (uint4*)rb.tiles, s.largeBins);
-  e = cudaFuncSetAttribute(largeBinsKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, LARGE_SMEM_KEYS * 4);
-  if (e != cudaSuccess) return e;
+  if (!c->largeBinsAttrSet) {
+    e = cudaFuncSetAttribute(largeBinsKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, LARGE_SMEM_KEYS * 4);
+    if (e != cudaSuccess) return e;
+    c->largeBinsAttrSet = true;
+  }
   largeBinsKernel<<<c->smCount, 1024, LARGE_SMEM_KEYS * 4, c->stream>>>(
       s.largeBins, s.binCount, s.binOffset, s.blockSums, s.keys, rb.tileSegments, (uint4*)rb.tiles);
   c->launches += nSeg ? 6 : 5;

@@ -5,8 +5,13 @@
 // collisions}.wgsl.ts and grids/*.wgsl.ts.  All arithmetic follows the fixed
 // fp32 order of hfb_math.cuh, so results are reproducible run to run; the
 // grid splat is integer (i32 fixed point, wrapping adds), hence order-free.
+#include <cooperative_groups.h>
+#include <cooperative_groups/reduce.h>
+
 #include "hfb_internal.cuh"
 #include "hfb_math.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace hfb {
 namespace {
@@ -314,31 +319,240 @@ simIntegrateKernel(const HfbSimUniforms u, uint32_t S, uint32_t P, uint32_t G,
 }
 
 // ---------------------------------------------------------------------------
+// HairSimIntegrationPass, one warp per strand (lane j = point j, P <= 32).
+//
+// The same arithmetic in the same order as simIntegrateKernel: the
+// Gauss-Seidel length and local-shape chains are walked step by step with
+// every lane computing the step's correction from the two / three current
+// points (shuffled from their owners) and the owners applying it, so each
+// step sees the points the previous step left -- exactly the reference's
+// sequential loop.  The per-point work (Verlet, grid gathers, global shape,
+// sphere and SDF collisions) runs on all lanes at once.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float4 shfl4(float4 v, int src) {
+  return make_float4(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src),
+                     __shfl_sync(0xffffffffu, v.z, src), __shfl_sync(0xffffffffu, v.w, src));
+}
+
+__global__ void __launch_bounds__(128)
+simIntegrateWarpKernel(const HfbSimUniforms u, uint32_t S, uint32_t P, uint32_t G,
+                       float4* __restrict__ prev, const float4* __restrict__ now,
+                       const float4* __restrict__ initial, const float* __restrict__ segLen,
+                       const int4* __restrict__ dv, const float4* __restrict__ gw,
+                       const float* __restrict__ sdf, uint32_t D) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t strand = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (strand >= S) return;  // whole warps only
+  const bool has = lane < P;
+  const size_t gi = (size_t)strand * P + lane;
+  const f3 gmin = gridMin(u), gmax = gridMax(u);
+
+  // --- Verlet + forces (:125-162), one lane per point ---
+  float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (has) {
+    const f4 posNow = ld4(__ldg(&now[gi]));
+    if (lane == 0) {
+      p = make_float4(posNow.x, posNow.y, posNow.z, posNow.w);
+    } else {
+      const f4 posPrev = ld4(prev[gi]);
+      f3 force = mk3(0.0f, -u.gravity, 0.0f);
+      const f3 pn = xyz(posNow);
+      GridCo co = gridCell(G, gmin, gmax, pn);
+      f3 grad = mk3(0.f, 0.f, 0.f), vel = mk3(0.f, 0.f, 0.f);
+      float windStr = 0.0f, dens = 0.0f;
+      for (uint32_t z = co.mn[2]; z <= co.mx[2]; z++)
+        for (uint32_t y = co.mn[1]; y <= co.mx[1]; y++)
+          for (uint32_t x = co.mn[0]; x <= co.mx[0]; x++) {
+            f3 w = cellWeights(x, y, z, co.p);
+            float wl = len3(w);
+            uint32_t idx = gridIdx(G, x, y, z);
+            float4 a = __ldg(&gw[idx]);
+            grad = add3(grad, mul3(w, mk3(a.x, a.y, a.z)));
+            windStr = fadd(windStr, fmul(wl, a.w));
+            int4 b = __ldg(&dv[idx]);
+            vel = add3(vel, mul3(w, mk3(gridDecode(b.x), gridDecode(b.y), gridDecode(b.z))));
+            dens = fadd(dens, fmul(wl, gridDecode(b.w)));
+          }
+      float timer = fadd(fmul((float)u.frameIdx, 0.73f), fmul(u.windPhaseOffset, (float)strand));
+      float windJitter = fractf(fmul(timer, u.windStrengthFrequency));
+      float jitterDelta = mixf(fmul(-0.5f, u.windStrengthJitter), fmul(0.5f, u.windStrengthJitter), windJitter);
+      float jitterStr = fadd(1.0f, jitterDelta);
+      float windCellStr = sat(mixf(u.windStrengthLull, 1.0f, windStr));
+      force = add3(force, mul3s(mk3(u.wind.x, u.wind.y, u.wind.z),
+                                fabsf(fmul(fmul(u.wind.w, jitterStr), windCellStr))));
+      force = add3(force, mul3s(grad, u.volumePreservation));
+      f3 gridDisp = dens > 0.0f ? div3s(vel, dens) : mk3(0.f, 0.f, 0.f);
+      float dt = u.deltaTime;
+      f3 pd = sub3(pn, xyz(posPrev));
+      f3 fpd = mix3(pd, gridDisp, u.friction);
+      f3 nxt = add3(add3(pn, fpd), mul3s(mul3s(force, dt), dt));
+      f3 r = mix3(xyz(posPrev), nxt, posNow.w);
+      p = make_float4(r.x, r.y, r.z, posNow.w);
+    }
+  }
+
+  // --- per-lane constants of the constraints (from the initial positions) ---
+  const float4 pi = has ? __ldg(&initial[gi]) : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float L0 = has ? __ldg(&segLen[gi]) : 0.0f;
+  // triangle-bending constants of the triplet that starts at this lane
+  const float4 i1 = shfl4(pi, min(lane + 1u, 31u)), i2 = shfl4(pi, min(lane + 2u, 31u));
+  float h0, tw0, tw1, tw2;
+  {
+    f3 cI = div3s(add3(add3(mk3(pi.x, pi.y, pi.z), mk3(i1.x, i1.y, i1.z)), mk3(i2.x, i2.y, i2.z)), 3.0f);
+    h0 = len3(sub3(cI, mk3(i1.x, i1.y, i1.z)));
+    float wT = fadd(fadd(pi.w, fmul(2.0f, i1.w)), i2.w);
+    tw0 = fmul(pi.w / wT, 2.0f);
+    tw1 = fmul(i1.w / wT, -4.0f);
+    tw2 = fmul(i2.w / wT, 2.0f);
+  }
+  // initial tangent towards this point (matchInitialTangent)
+  const float4 im1 = shfl4(pi, lane ? lane - 1u : 0u);
+  const f3 tInit = mk3(fsub(pi.x, im1.x), fsub(pi.y, im1.y), fsub(pi.z, im1.z));
+
+  const uint32_t iters = u.constraintIterations;
+  const f3 smin = mk3(u.sdf.boundsMin.x, u.sdf.boundsMin.y, u.sdf.boundsMin.z);
+  const f3 smax = mk3(u.sdf.boundsMax.x, u.sdf.boundsMax.y, u.sdf.boundsMax.z);
+  const float sdfOffset = u.sdf.boundsMax.w;
+  const f4 sph = mk4(u.collisionSphere.x, u.collisionSphere.y, u.collisionSphere.z, u.collisionSphere.w);
+  for (uint32_t it = 0; it < iters; it++) {
+    // length constraint, sequential along the strand
+    const float kLen = u.stiffnessLengthConstr;
+    for (uint32_t j = 0; j + 1u < P; j++) {
+      const float4 a = shfl4(p, j), b = shfl4(p, j + 1u);
+      const float expected = __shfl_sync(0xffffffffu, L0, j);
+      const float w0 = a.w, w1 = b.w;
+      f3 tng = mk3(fsub(b.x, a.x), fsub(b.y, a.y), fsub(b.z, a.z));
+      float actual = len3(tng);
+      float corr = fsub(1.0f, expected / actual);
+      float df = fmul(corr, kLen) / fadd(fadd(w0, w1), FLOAT_EPSILON);
+      f3 delta = mul3s(tng, df);
+      if (lane == j) {
+        p.x = fadd(a.x, fmul(delta.x, w0)); p.y = fadd(a.y, fmul(delta.y, w0)); p.z = fadd(a.z, fmul(delta.z, w0));
+      } else if (lane == j + 1u) {
+        p.x = fsub(b.x, fmul(w1, delta.x)); p.y = fsub(b.y, fmul(w1, delta.y)); p.z = fsub(b.z, fmul(w1, delta.z));
+      }
+    }
+    // global shape, every point at once
+    const float kGlob = u.stiffnessGlobalConstr / (float)iters;
+    if (has && lane >= 1u) {
+      float x = (float)lane / (float)(P - 1u);
+      float att = fsub(1.0f, sat(fsub(x, u.globalConstrExtent) / u.globalConstrFade));
+      float k = fmul(kGlob, att);
+      f3 dvv = mk3(fsub(pi.x, p.x), fsub(pi.y, p.y), fsub(pi.z, p.z));
+      f3 d = mul3s(mul3s(dvv, p.w), k);
+      p.x = fadd(p.x, d.x); p.y = fadd(p.y, d.y); p.z = fadd(p.z, d.z);
+    }
+    // local shape, sequential over the triplets
+    const float kLoc = u.stiffnessLocalConstr / (float)iters;
+    uint32_t jj = 0;
+    for (; jj + 3u < P; jj++) {
+      const float4 p0 = shfl4(p, jj), p1 = shfl4(p, jj + 1u), p2 = shfl4(p, jj + 2u);
+      const float hh0 = __shfl_sync(0xffffffffu, h0, jj);
+      const float w0 = __shfl_sync(0xffffffffu, tw0, jj), w1 = __shfl_sync(0xffffffffu, tw1, jj),
+                  w2 = __shfl_sync(0xffffffffu, tw2, jj);
+      f3 c = div3s(add3(add3(mk3(p0.x, p0.y, p0.z), mk3(p1.x, p1.y, p1.z)), mk3(p2.x, p2.y, p2.z)), 3.0f);
+      f3 hv = sub3(mk3(p1.x, p1.y, p1.z), c);
+      float h = len3(hv);
+      f3 delta = mul3s(hv, fsub(1.0f, hh0 / h));
+      if (lane == jj) {
+        f3 d = mul3s(delta, fmul(kLoc, w0));
+        p.x = fadd(p0.x, d.x); p.y = fadd(p0.y, d.y); p.z = fadd(p0.z, d.z);
+      } else if (lane == jj + 1u) {
+        f3 d = mul3s(delta, fmul(kLoc, w1));
+        p.x = fadd(p1.x, d.x); p.y = fadd(p1.y, d.y); p.z = fadd(p1.z, d.z);
+      } else if (lane == jj + 2u) {
+        f3 d = mul3s(delta, fmul(kLoc, w2));
+        p.x = fadd(p2.x, d.x); p.y = fadd(p2.y, d.y); p.z = fadd(p2.z, d.z);
+      }
+    }
+    for (; jj < P; jj++) {  // applyConstraint_matchInitialTangent, sequential
+      const float4 p0 = shfl4(p, jj - 1u);
+      if (lane == jj) {
+        f3 proj = add3(mk3(p0.x, p0.y, p0.z), tInit);
+        f3 delta = sub3(proj, mk3(p.x, p.y, p.z));
+        f3 d = mul3s(delta, fmul(kLoc, p.w));
+        p.x = fadd(p.x, d.x); p.y = fadd(p.y, d.y); p.z = fadd(p.z, d.z);
+      }
+    }
+    // collisions, every point at once
+    const float kColl = u.stiffnessCollisions / (float)iters;
+    const float kSdf = u.stiffnessSDF / (float)iters;
+    if (has && lane >= 1u) {
+      {
+        f3 v = mk3(fsub(p.x, sph.x), fsub(p.y, sph.y), fsub(p.z, sph.z));
+        float dist = fsub(len3(v), sph.w);
+        float dts = fmaxf(0.0f, -dist);
+        f3 d = mul3s(mul3s(norm3(v), dts), kColl);
+        p.x = fadd(p.x, d.x); p.y = fadd(p.y, d.y); p.z = fadd(p.z, d.z);
+      }
+      if (lane > 2u) {
+        f3 q = mk3(p.x, p.y, p.z);
+        float d = sampleSDF(sdf, D, smin, smax, q);
+        float dOff = fadd(d, sdfOffset);
+        if (!(dOff >= 0.0f)) {
+          const float o = SDF_GRAD_OFFSET;
+          f3 cd;
+          cd.x = sampleSDF(sdf, D, smin, smax, add3(q, mk3(fmul(o, 1.0f), fmul(o, 0.0f), fmul(o, 0.0f))));
+          cd.y = sampleSDF(sdf, D, smin, smax, add3(q, mk3(fmul(o, 0.0f), fmul(o, 1.0f), fmul(o, 0.0f))));
+          cd.z = sampleSDF(sdf, D, smin, smax, add3(q, mk3(fmul(o, 0.0f), fmul(o, 0.0f), fmul(o, 1.0f))));
+          cd = sub3(cd, mk3(d, d, d));
+          f3 corr = mul3s(norm3(cd), -dOff);
+          f3 dd = mul3s(corr, kSdf);
+          p.x = fadd(p.x, dd.x); p.y = fadd(p.y, dd.y); p.z = fadd(p.z, dd.z);
+        }
+      }
+    }
+  }
+  if (has) prev[gi] = p;  // write into the PREV buffer (:268-272)
+}
+
+// ---------------------------------------------------------------------------
 // GridPostSimPass.main, gridPostSimPass.wgsl.ts:45-72 with
 // _addGridDensityVelocity, densityVelocityGrid.wgsl.ts:93-124.
 // One thread per point; i32 atomics (wrapping, order-independent).
 // ---------------------------------------------------------------------------
-__global__ void gridPostSimKernel(const HfbSimUniforms u, uint32_t N, uint32_t G,
-                                  const float4* __restrict__ prev, const float4* __restrict__ now,
-                                  int* __restrict__ dv) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= N) return;
-  float4 a = __ldg(&prev[i]), b = __ldg(&now[i]);
-  f3 pn = mk3(b.x, b.y, b.z);
-  f3 vel = sub3(pn, mk3(a.x, a.y, a.z));
-  GridCo co = gridCell(G, gridMin(u), gridMax(u), pn);
-  for (uint32_t z = co.mn[2]; z <= co.mx[2]; z++)
-    for (uint32_t y = co.mn[1]; y <= co.mx[1]; y++)
-      for (uint32_t x = co.mn[0]; x <= co.mx[0]; x++) {
-        uint32_t idx = gridIdx(G, x, y, z);
-        f3 w = cellWeights(x, y, z, co.p);
-        f3 cv = mul3(vel, w);
-        int* c = dv + 4u * idx;
-        atomicAdd(c + 0, gridEncode(cv.x));
-        atomicAdd(c + 1, gridEncode(cv.y));
-        atomicAdd(c + 2, gridEncode(cv.z));
-        atomicAdd(c + 3, gridEncode(len3(w)));
-      }
+__global__ void __launch_bounds__(256)
+gridPostSimKernel(const HfbSimUniforms u, uint32_t N, uint32_t G, const float4* __restrict__ prev,
+                  const float4* __restrict__ now, unsigned* __restrict__ dv) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = i < N;
+  float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+  if (valid) { a = __ldg(&prev[i]); b = __ldg(&now[i]); }
+  const f3 pn = mk3(b.x, b.y, b.z);
+  const f3 vel = sub3(pn, mk3(a.x, a.y, a.z));
+  const GridCo co = gridCell(G, gridMin(u), gridMax(u), pn);
+  // Consecutive points of a strand mostly share their cell: the lanes that
+  // add to the same node sum their (wrapping, order-free) i32 values first
+  // and one lane issues the atomics.
+  const cg::thread_block_tile<32> warp = cg::tiled_partition<32>(cg::this_thread_block());
+#pragma unroll 1
+  for (uint32_t k = 0; k < 8u; k++) {
+    const uint32_t x = co.mn[0] + (k & 1u), y = co.mn[1] + ((k >> 1) & 1u), z = co.mn[2] + (k >> 2);
+    const bool on = valid && x <= co.mx[0] && y <= co.mx[1] && z <= co.mx[2];
+    unsigned v0 = 0, v1 = 0, v2 = 0, v3 = 0;
+    uint32_t idx = 0xffffffffu;
+    if (on) {
+      idx = gridIdx(G, x, y, z);
+      const f3 w = cellWeights(x, y, z, co.p);
+      const f3 cv = mul3(vel, w);
+      v0 = (unsigned)gridEncode(cv.x);
+      v1 = (unsigned)gridEncode(cv.y);
+      v2 = (unsigned)gridEncode(cv.z);
+      v3 = (unsigned)gridEncode(len3(w));
+    }
+    const cg::coalesced_group g = cg::labeled_partition(warp, idx);
+    v0 = cg::reduce(g, v0, cg::plus<unsigned>());
+    v1 = cg::reduce(g, v1, cg::plus<unsigned>());
+    v2 = cg::reduce(g, v2, cg::plus<unsigned>());
+    v3 = cg::reduce(g, v3, cg::plus<unsigned>());
+    if (on && g.thread_rank() == 0) {
+      unsigned* c = dv + 4u * idx;
+      atomicAdd(c + 0, v0);
+      atomicAdd(c + 1, v1);
+      atomicAdd(c + 2, v2);
+      atomicAdd(c + 3, v3);
+    }
+  }
 }
 
 }  // namespace
@@ -356,10 +570,22 @@ cudaError_t launchSimIntegrate(HfbCtx* c, const HfbSimUniforms& u, const HfbHair
                                const float* now, const float* initial, const float* segLen,
                                const int32_t* dv, const float* gw, const float* sdf, uint32_t sdfDims) {
   uint32_t S = h.strandsCount, P = h.pointsPerStrand;
+  // warp per strand while the strands fill at most a couple of waves of the
+  // GPU; beyond that one thread per strand keeps every lane busy
+  if (P <= 32u && (uint64_t)S * 32u <= (uint64_t)c->smCount * 2048u * 2u) {
+    simIntegrateWarpKernel<<<divCeil(S, 4), 128, 0, c->stream>>>(
+        u, S, P, c->cfg.gridDims, (float4*)prev, (const float4*)now, (const float4*)initial, segLen,
+        (const int4*)dv, (const float4*)gw, sdf, sdfDims);
+    c->launches += 1;
+    return cudaGetLastError();
+  }
   size_t smem = (size_t)P * SIM_STRANDS_PER_BLOCK * sizeof(float4);  // <= 128 KB (P <= 128)
-  cudaError_t e = cudaFuncSetAttribute(simIntegrateKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
-  if (e != cudaSuccess) return e;
+  if (smem > c->simSmemSet) {
+    cudaError_t e = cudaFuncSetAttribute(simIntegrateKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    c->simSmemSet = smem;
+  }
   simIntegrateKernel<<<divCeil(S, SIM_STRANDS_PER_BLOCK), SIM_STRANDS_PER_BLOCK, smem, c->stream>>>(
       u, S, P, c->cfg.gridDims, (float4*)prev, (const float4*)now, (const float4*)initial, segLen,
       (const int4*)dv, (const float4*)gw, sdf, sdfDims);
@@ -375,7 +601,7 @@ cudaError_t launchGridPostSim(HfbCtx* c, const HfbSimUniforms& u, const HfbHairD
   uint32_t N = h.strandsCount * h.pointsPerStrand;
   if (N) {
     gridPostSimKernel<<<divCeil(N, 256), 256, 0, c->stream>>>(u, N, G, (const float4*)prev,
-                                                               (const float4*)now, dv);
+                                                               (const float4*)now, (unsigned*)dv);
     c->launches += 1;
   }
   return cudaGetLastError();

@@ -155,10 +155,14 @@ def _sim_inputs(inst, frame_idx=0):
                                 wind_strength=inst.wind_strength(frame_idx))
 
 
-@pytest.mark.parametrize("maker", ["small", "curly_wind"])
+@pytest.mark.parametrize("maker", ["small", "curly_wind", "many_strands"])
 def test_grids_and_one_step_bit_exact(oracle, maker):
+    """Both integration kernels: warp per strand (moderate strand counts)
+    and thread per strand (many strands)."""
     if maker == "small":
         inst = small_instance()
+    elif maker == "many_strands":
+        inst = small_instance(strands=24000, points=16, iterations=3)
     else:
         inst = small_instance(strands=3000, points=32, curl=True, ellipsoid=True, wind_amplitude=1.0,
                               iterations=4, sdf_dims=64)
@@ -188,6 +192,24 @@ def test_grids_and_one_step_bit_exact(oracle, maker):
     g = hair.positions.cpu().numpy()
     assert np.array_equal(g.view(np.uint32), onew.view(np.uint32)), \
         f"max abs diff {np.abs(g - onew).max()}"
+
+
+def test_density_grid_wraps_like_the_reference(oracle):
+    """10,000 x 32 strands on a 32^3 grid overflow the reference's i32
+    fixed-point density (atomicAdd<i32> of i32(w * 1e6) wraps): the CUDA splat
+    wraps identically (two's complement), node for node."""
+    from hairfb import synthetic
+    inst = synthetic.plain_full(grid_dims=32)
+    hb = inst.hair
+    su = _sim_inputs(inst, 0)
+    ctx = _ctx(inst)
+    hair = HairObject(hb, inst.cfg.shading_points)
+    grids = PhysicsGrids(inst.cfg.grid_dims)
+    GridPostSimPass(ctx).cmd_update_grids_after_sim(su, hair, grids)
+    ctx.sync()
+    o = oracle.grid_post_sim(inst.cfg, su, hb.hair_data, hb.asset.positions, hb.asset.positions)
+    assert (o[:, 3] < 0).sum() > 0, "no node wrapped: the case does not test the overflow"
+    assert np.array_equal(grids.density_velocity.cpu().numpy(), o)
 
 
 def test_simulation_60_steps(oracle):
