@@ -39,12 +39,12 @@ for _p in (ROOT, PKG):
 import numpy as np  # noqa: E402
 
 WORKLOADS = {
-    # BASELINE configs[1]: the single full frame
+    # one full frame: 10k strands at 1080p
     "plain_full": "10,000 x 32 curly strands, 1920x1080, 16 px tiles, 16 depth bins, 4 slices, "
                   "16 shading points, 4 iterations, 64^3 SDF, 64^3 grids, sinusoidal wind",
-    # BASELINE configs[0]
+    # the small case the reference also runs on a CPU adapter
     "plain_small": "2,000 x 16 strands, 640x480, 16 px tiles, 8 depth bins, 4 slices, 8 shading points",
-    # BASELINE configs[4]
+    # the 4K stress frame: 200k strands
     "stress": "200,000 x 32 strands (60% ponytail), 3840x2160, 32 depth bins, 8 slices, 32 shading points",
 }
 

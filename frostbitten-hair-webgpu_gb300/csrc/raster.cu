@@ -486,71 +486,185 @@ tileSortKernel(uint32_t T, uint32_t NB, uint32_t bucketSize, const uint32_t* __r
 }
 
 // ---------------------------------------------------------------------------
-// HairFinePass: persistent CTAs, one thread per tile pixel.
+// HairFinePass: persistent CTAs of TS x TS threads, one tile at a time.
 //
-// Per depth bin, the bin's list is walked in chunks of 32 segments (a warp
-// reads the list speculatively as a contiguous run and falls back to pointer
-// chasing where it is not), the chunk is projected in parallel into shared
-// memory, and every pixel tests the chunk in list order.  Each slice of a
-// pixel keeps the closed form of its front-to-back blend in registers:
-// fragments arrive back to front (descending key) and acc = f + (1 - f.a) *
-// acc, which equals the reference's per-slice linked list reduced front to
-// back (reduceHairSlices.wgsl.ts:9-73) -- no fragment pool in memory.  The
-// fragment-pool capacity of the reference (SLICE_DATA_PER_PROCESSOR_COUNT,
-// processHairSegment.wgsl.ts:33-40, hairFinePass.wgsl.ts:258-264) is kept
-// exactly: slots are counted per segment in pixel order and the list walk
-// stops after the segment that fills the pool.
+// The tile's depth bins are processed in order (processTile per bin,
+// hairFinePass.wgsl.ts:205-288).  Their lists are staged in rounds of up to
+// STAGE segments -- short bins share a round, a long bin spans several -- and
+// each round runs in three phases:
+//   A1  one thread per (segment, pixel of the segment's tile-local bounding
+//       box) pair: the four edge tests of processHairSegment (:5-20); the
+//       passing pairs are appended to a list;
+//   A2  one thread per passing pair: segment-space interpolation, the depth
+//       test and the fragment colour (:21-53), rounded through f16 like
+//       pack2x16float (hairSlicesDataBuffer.ts:50-63);
+//   B   one thread per pixel: the pixel's fragments in list order, found
+//       through a per-pixel bit mask over the round's segments.
+// A pixel covers ~4 of the ~25 pixels of a segment's box at 1080p, so the
+// pair phases keep the lanes busy where a pixel-per-thread walk of the list
+// would idle most of them.  Each slice of a pixel keeps the closed form of
+// its front-to-back blend in registers: fragments arrive back to front
+// (descending key) and acc = f + (1 - f.a) * acc, which equals the
+// reference's per-slice linked list reduced front to back
+// (reduceHairSlices.wgsl.ts:9-73) -- no fragment pool in memory.
+//
+// The reference's fragment-pool capacity per bin (SLICE_DATA_PER_PROCESSOR_
+// COUNT, processHairSegment.wgsl.ts:33-40, hairFinePass.wgsl.ts:258-264) is
+// kept exactly: while an upper bound (edge-test passes) shows that a bin
+// cannot fill its pool inside a round, nothing is counted; otherwise the
+// round is restricted to that bin, fragments are counted per segment, and the
+// segment that fills the pool keeps its first slots in pixel order, after
+// which the bin stops.
 // ---------------------------------------------------------------------------
-constexpr uint32_t CHUNK = 32;     // segments per exact-path sub-chunk (32-bit masks)
-constexpr uint32_t STAGE = 256;    // segments staged in shared memory per round
-constexpr uint32_t NSHADE = 4;     // shading entries staged per segment
+constexpr uint32_t NSHADE = 4;              // shading entries staged per segment
+constexpr uint32_t MAX_RUNS = 66;           // runs of one round: at most one per depth bin (+1)
+constexpr uint32_t PAIR_NONE = 0xffffffffu; // pair without a fragment
+constexpr uint32_t EMPTY_BOX = 0x0000ffffu; // x0 = y0 = 255 > x1 = y1 = 0
+constexpr uint32_t RUN_ENDS = 1u << 31;
 
-struct FineShared {
-  ProjSeg seg[STAGE];
-  float4 shade[STAGE][NSHADE];  // the shading entries each segment can sample
-  uint32_t strand[STAGE];
-  uint32_t segIdx[STAGE];
-  uint32_t box[STAGE];       // tile-local pixel-corner bbox x0|y0<<8|x1<<16|y1<<24 (x0 > x1: empty)
-  uint32_t area[STAGE];      // pixels of the bbox (upper bound of the segment's fragments)
-  uint32_t shadeBase[STAGE]; // first staged shading index | count << 16
-  uint4 head[64];            // the tile's HairTileResult per depth bin
-  uint32_t binOff[65];       // whole-tile staging: first staged segment of each bin
-  uint32_t cnt[32][CHUNK];   // per-warp passing counts per segment (exact path)
+template <int TS> struct FineDims;
+template <> struct FineDims<8> { static constexpr uint32_t STAGE = 64, PAIRS = 1024; };
+template <> struct FineDims<16> { static constexpr uint32_t STAGE = 128, PAIRS = 3072; };
+template <> struct FineDims<32> { static constexpr uint32_t STAGE = 256, PAIRS = 4096; };
+
+template <int TS>
+struct FineSmem {
+  static constexpr uint32_t NT = TS * TS, STAGE = FineDims<TS>::STAGE, PAIRS = FineDims<TS>::PAIRS;
+  static_assert(PAIRS >= NT, "a segment box covers up to TS*TS pairs");
+  float4 shade[STAGE][NSHADE];   // the shading entries each staged segment can sample
+  uint2 frag[PAIRS];             // A1: pixel | segment << 16 of a passing pair; A2: its colour as 4 x f16
+  uint32_t pairInfo[PAIRS];      // per pair: fragment index | slice << 16, or PAIR_NONE
+  // staged segments, one array per quantity (consecutive segments in consecutive banks)
+  float ox[4][STAGE], oy[4][STAGE];  // first vertex of the four edge tests: v01, v11, v10, v00
+  float ex[4][STAGE], ey[4][STAGE];  // second - first vertex of each edge test
+  float dp[4][STAGE];                // depthsProj
+  float qsx[STAGE], qsy[STAGE], qax[STAGE], qay[STAGE], qd2[STAGE], qlse[STAGE], qws[STAGE], qwe[STAGE],
+      qd22[STAGE];                   // QuadConst
+  uint32_t strand[STAGE], segIdx[STAGE], listIdx[STAGE];
+  uint32_t box[STAGE];               // tile-local pixel box x0 | y0 << 8 | x1 << 16 | y1 << 24
+  uint32_t shadeBase[STAGE];         // first staged shading index | count << 16 | depth bin << 24
+  uint32_t pairBase[STAGE + 1];      // exclusive prefix of the box areas
+  uint32_t cntEdge[STAGE], cntFrag[STAGE];
+  uint32_t pixMask[STAGE / 32][NT];  // bit k of pixel p: staged segment k left a fragment at p
+  // the tile
+  uint4 head[64];                    // HairTileResult per depth bin
+  uint32_t binOff[65];               // tile mode: first entry of each bin in the tile's sequence
+  float zbuf[NT];
+  uint32_t doneMask[NT / 32];
+  // the round
+  uint32_t runBin[MAX_RUNS], runK0[MAX_RUNS], runK1[MAX_RUNS], runOff[MAX_RUNS];
   uint32_t red[32];
-  uint32_t n, nextPtr, queueIdx, bad, tileMode, total;
-  uint32_t cutSeg, cutSlots, chunkTotal;
+  uint32_t nRuns, nStaged, nSeg, passCount, queueIdx, bad, tileMode, total, walkNext;
+  uint32_t mode, cutSeg, cutSlots, roundFrags, e0, eLast;
 };
 
 __device__ __forceinline__ bool inBox(uint32_t box, uint32_t lx, uint32_t ly) {
   return lx >= (box & 0xffu) && ly >= ((box >> 8) & 0xffu) && lx <= ((box >> 16) & 0xffu) && ly <= (box >> 24);
 }
 
-// edge + depth test of processHairSegment (:5-31); fills w / hd when it passes
-__device__ __forceinline__ bool fragmentPasses(const ProjSeg& s, f2 pp, float zbuf, f2& w, float& hd) {
-  if (!insideQuad(s, pp)) return false;
-  w = interpolateHairQuad(s, pp);
-  hd = interpolateHairF32(w, s.depthsProj);
-  return hd < zbuf;  // depth test with GL_LESS (skip when >=)
+// Block-wide sum (all threads call; every thread gets the total).
+template <int NW>
+__device__ __forceinline__ uint32_t blockSum(uint32_t v, uint32_t* red, uint32_t lane, uint32_t warp) {
+  const uint32_t w = __reduce_add_sync(0xffffffffu, v);
+  if (lane == 0) red[warp] = w;
+  __syncthreads();
+  uint32_t t = 0;
+#pragma unroll
+  for (int i = 0; i < NW; i++) t += red[i];
+  __syncthreads();
+  return t;
 }
 
-// Colour of one fragment (processHairSegment.wgsl.ts:43-53), rounded through
-// f16 like pack2x16float (hairSlicesDataBuffer.ts:50-63), blended in front of
-// the slice's accumulated colour.  The two shading entries come from the
-// segment's staged copy (or global memory when outside it).
-template <int MAXL>
-__device__ __forceinline__ void addFragment(f4 (&acc)[MAXL], const FineShared& sh, uint32_t k, f2 w, float hd,
-                                            uint32_t P, uint32_t SP, uint32_t L, float td0, float td1,
-                                            uint32_t alphaQuadratic, float alphaMul,
-                                            const float4* __restrict__ shading) {
-  // getAlphaCoverage, processHairSegment.wgsl.ts:60-69
+// Block-wide exclusive prefix in thread order (all threads call).
+template <int NW>
+__device__ __forceinline__ uint32_t blockExclusive(uint32_t v, uint32_t* red, uint32_t lane, uint32_t warp) {
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= (uint32_t)o) x += y;
+  }
+  if (lane == 31) red[warp] = x;
+  __syncthreads();
+  uint32_t pre = 0;
+  for (uint32_t i = 0; i < warp; i++) pre += red[i];
+  __syncthreads();
+  return pre + x - v;
+}
+
+// Projects staged segment k: edge-test constants, depths, the pixel-
+// independent part of interpolateHairQuad, the tile-local box of the pixels
+// that can pass the edge tests ([floor(min), ceil(max)] of the vertices), and
+// the shading entries its fragments can sample (tFull is monotonic in the
+// segment coordinate, so they are [i0(t = 0), i1(t = 1)]).  Returns the
+// box area.
+template <int TS>
+__device__ __forceinline__ uint32_t stageSegment(FineSmem<TS>& sh, uint32_t k, uint32_t bin, const HfbUniforms& U,
+                                                 const float4* __restrict__ pos, const float4* __restrict__ tan,
+                                                 const float4* __restrict__ shading, uint32_t S, uint32_t P,
+                                                 uint32_t SP, f2 size, uint32_t x0, uint32_t y0) {
+  const uint32_t st = sh.strand[k], sg = sh.segIdx[k];
+  uint32_t box = EMPTY_BOX, area = 0, shadeBase = bin << 24;
+  if (st < S && sg + 1u < P) {  // otherwise not a segment of this hair: covers no pixel
+    const ProjSeg s = projectSegment(U, pos, tan, P, st, sg, size);
+    float mnx = floorf(fminf(fminf(s.v00.x, s.v01.x), fminf(s.v10.x, s.v11.x))) - (float)x0;
+    float mny = floorf(fminf(fminf(s.v00.y, s.v01.y), fminf(s.v10.y, s.v11.y))) - (float)y0;
+    float mxx = ceilf(fmaxf(fmaxf(s.v00.x, s.v01.x), fmaxf(s.v10.x, s.v11.x))) - (float)x0;
+    float mxy = ceilf(fmaxf(fmaxf(s.v00.y, s.v01.y), fmaxf(s.v10.y, s.v11.y))) - (float)y0;
+    if (mnx <= mxx && mny <= mxy && mxx >= 0.0f && mxy >= 0.0f && mnx <= (float)(TS - 1) && mny <= (float)(TS - 1)) {
+      const uint32_t bx0 = (uint32_t)fmaxf(mnx, 0.0f), by0 = (uint32_t)fmaxf(mny, 0.0f);
+      const uint32_t bx1 = (uint32_t)fminf(mxx, (float)(TS - 1)), by1 = (uint32_t)fminf(mxy, (float)(TS - 1));
+      box = bx0 | (by0 << 8) | (bx1 << 16) | (by1 << 24);
+      area = (bx1 - bx0 + 1u) * (by1 - by0 + 1u);
+      // edge tests in the order insideQuad evaluates them
+      const f2 o[4] = {s.v01, s.v11, s.v10, s.v00};
+      const f2 e[4] = {s.v00, s.v01, s.v11, s.v10};
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        sh.ox[i][k] = o[i].x;
+        sh.oy[i][k] = o[i].y;
+        sh.ex[i][k] = fsub(e[i].x, o[i].x);
+        sh.ey[i][k] = fsub(e[i].y, o[i].y);
+      }
+      sh.dp[0][k] = s.depthsProj.x;
+      sh.dp[1][k] = s.depthsProj.y;
+      sh.dp[2][k] = s.depthsProj.z;
+      sh.dp[3][k] = s.depthsProj.w;
+      const QuadConst q = quadConst(s);
+      sh.qsx[k] = q.sm.x; sh.qsy[k] = q.sm.y; sh.qax[k] = q.ab.x; sh.qay[k] = q.ab.y;
+      sh.qd2[k] = q.d2; sh.qlse[k] = q.lse; sh.qws[k] = q.wS; sh.qwe[k] = q.wE; sh.qd22[k] = q.d22;
+      uint32_t a0, a1, b0, b1;
+      remapToIndices(SP, fadd((float)sg, 0.0f) / (float)(P - 1u), a0, a1);
+      remapToIndices(SP, fadd((float)sg, 1.0f) / (float)(P - 1u), b0, b1);
+      const uint32_t ne = min(b1 - a0 + 1u, NSHADE);
+      const size_t sb = (size_t)st * SP;
+      for (uint32_t j = 0; j < ne; j++) sh.shade[k][j] = __ldg(&shading[sb + a0 + j]);
+      shadeBase |= a0 | (ne << 16);
+    }
+  }
+  sh.box[k] = box;
+  sh.shadeBase[k] = shadeBase;
+  sh.cntEdge[k] = 0;
+  sh.cntFrag[k] = 0;
+  return area;
+}
+
+// Fragment colour of staged segment k at segment coordinates w and depth hd
+// (processHairSegment.wgsl.ts:43-53 with getAlphaCoverage :60-69 and
+// _sampleShading, hairShadingBuffer.ts:28-38), as 4 x f16, and its slice.
+template <int TS>
+__device__ __forceinline__ uint2 fragmentColour(const FineSmem<TS>& sh, uint32_t k, f2 w, float hd, uint32_t P,
+                                                uint32_t SP, uint32_t L, float td0, float td1,
+                                                uint32_t alphaQuadratic, float alphaMul,
+                                                const float4* __restrict__ shading, uint32_t& slice) {
   float alpha = fsub(1.0f, fabsf(fsub(fmul(w.x, 2.0f), 1.0f)));
   if (alphaQuadratic) alpha = sqrtf(alpha);
   alpha = sat(fmul(alpha, alphaMul));
-  float tFull = fadd((float)sh.segIdx[k], w.y) / (float)(P - 1u);
-  // _sampleShading, hairShadingBuffer.ts:28-38
+  const float tFull = fadd((float)sh.segIdx[k], w.y) / (float)(P - 1u);
   uint32_t i0, i1;
-  float fr = remapToIndices(SP, tFull, i0, i1);
-  const uint32_t e0 = sh.shadeBase[k] & 0xffffu, ne = sh.shadeBase[k] >> 16;
+  const float fr = remapToIndices(SP, tFull, i0, i1);
+  const uint32_t sbase = sh.shadeBase[k];
+  const uint32_t e0 = sbase & 0xffffu, ne = (sbase >> 16) & 0xffu;
   float4 c0, c1;
   if (i0 - e0 < ne && i1 - e0 < ne) {
     c0 = sh.shade[k][i0 - e0];
@@ -562,10 +676,20 @@ __device__ __forceinline__ void addFragment(f4 (&acc)[MAXL], const FineShared& s
   }
   f4 c = mix4(ld4(c0), ld4(c1), fr);
   c.w = fmul(c.w, alpha);
-  uint32_t sl = getDepthBin(L, td0, td1, hd);  // getSliceIdx
-  f4 q = mk4(__half2float(__float2half_rn(c.x)), __half2float(__float2half_rn(c.y)),
-             __half2float(__float2half_rn(c.z)), __half2float(__float2half_rn(c.w)));
-  float kk = fsub(1.0f, q.w);
+  slice = getDepthBin(L, td0, td1, hd);  // getSliceIdx
+  const uint32_t hx = __half_as_ushort(__float2half_rn(c.x)), hy = __half_as_ushort(__float2half_rn(c.y));
+  const uint32_t hz = __half_as_ushort(__float2half_rn(c.z)), hw = __half_as_ushort(__float2half_rn(c.w));
+  return make_uint2(hx | (hy << 16), hz | (hw << 16));
+}
+
+__device__ __forceinline__ float halfLo(uint32_t v) { return __half2float(__ushort_as_half((unsigned short)(v & 0xffffu))); }
+__device__ __forceinline__ float halfHi(uint32_t v) { return __half2float(__ushort_as_half((unsigned short)(v >> 16))); }
+
+// acc[slice] = f + (1 - f.a) * acc[slice]
+template <int MAXL>
+__device__ __forceinline__ void blendFragment(f4 (&acc)[MAXL], uint32_t sl, uint2 h) {
+  const f4 q = mk4(halfLo(h.x), halfHi(h.x), halfLo(h.y), halfHi(h.y));
+  const float kk = fsub(1.0f, q.w);
 #pragma unroll
   for (int si = 0; si < MAXL; si++) {
     if ((uint32_t)si == sl) {
@@ -577,177 +701,46 @@ __device__ __forceinline__ void addFragment(f4 (&acc)[MAXL], const FineShared& s
   }
 }
 
-// Projects staged segment k, its tile-local bounding box, and stages the
-// shading entries its fragments can sample (tFull is monotonic in the
-// segment coordinate, so they are [i0(t = 0), i1(t = 1)]).
+// Tile mode: the runs of the next round, from bin `bin`, entry `off` of its
+// list, up to `cap` segments.  Bins without depth (td1 == 0) are skipped as
+// the reference skips them; a depth bin with an empty list is a run of zero
+// segments (its reduce still runs).  Called by one thread.
 template <int TS>
-__device__ __forceinline__ void projectStaged(const HfbUniforms& U, const float4* __restrict__ pos,
-                                              const float4* __restrict__ tan, const float4* __restrict__ shading,
-                                              uint32_t S, uint32_t P, uint32_t SP, f2 size, uint32_t x0,
-                                              uint32_t y0, FineShared& sh, uint32_t k) {
-  const uint32_t st = sh.strand[k], sg = sh.segIdx[k];
-  ProjSeg s;
-  uint32_t box = 0x00ff00ffu, area = 0, shadeBase = 0;  // empty
-  if (st < S && sg + 1u < P) {
-    s = projectSegment(U, pos, tan, P, st, sg, size);
-    // pixel corners that can pass the edge tests: [floor(min), ceil(max)]
-    float mnx = floorf(fminf(fminf(s.v00.x, s.v01.x), fminf(s.v10.x, s.v11.x))) - (float)x0;
-    float mny = floorf(fminf(fminf(s.v00.y, s.v01.y), fminf(s.v10.y, s.v11.y))) - (float)y0;
-    float mxx = ceilf(fmaxf(fmaxf(s.v00.x, s.v01.x), fmaxf(s.v10.x, s.v11.x))) - (float)x0;
-    float mxy = ceilf(fmaxf(fmaxf(s.v00.y, s.v01.y), fmaxf(s.v10.y, s.v11.y))) - (float)y0;
-    if (mnx <= mxx && mny <= mxy && mxx >= 0.0f && mxy >= 0.0f && mnx <= (float)(TS - 1) && mny <= (float)(TS - 1)) {
-      uint32_t bx0 = (uint32_t)fmaxf(mnx, 0.0f), by0 = (uint32_t)fmaxf(mny, 0.0f);
-      uint32_t bx1 = (uint32_t)fminf(mxx, (float)(TS - 1)), by1 = (uint32_t)fminf(mxy, (float)(TS - 1));
-      box = bx0 | (by0 << 8) | (bx1 << 16) | (by1 << 24);
-      area = (bx1 - bx0 + 1u) * (by1 - by0 + 1u);
-      uint32_t a0, a1, b0, b1;
-      remapToIndices(SP, fadd((float)sg, 0.0f) / (float)(P - 1u), a0, a1);
-      remapToIndices(SP, fadd((float)sg, 1.0f) / (float)(P - 1u), b0, b1);
-      const uint32_t ne = min(b1 - a0 + 1u, NSHADE);
-      const size_t sb = (size_t)st * SP;
-      for (uint32_t e = 0; e < ne; e++) sh.shade[k][e] = __ldg(&shading[sb + a0 + e]);
-      shadeBase = a0 | (ne << 16);
-    }
-  } else {  // not a segment of this hair: covers no pixel
-    const float nan = __int_as_float(0x7fffffff);
-    s.v00 = s.v01 = s.v10 = s.v11 = mk2(nan, nan);
-    s.depthsProj = mk4(nan, nan, nan, nan);
+__device__ __forceinline__ uint32_t buildRuns(FineSmem<TS>& sh, uint32_t B, uint32_t bin, uint32_t off,
+                                              uint32_t cap, uint32_t& used) {
+  uint32_t n = 0;
+  used = 0;
+  while (bin < B && n < MAX_RUNS) {
+    if (sh.head[bin].y == 0u) { bin++; off = 0; continue; }
+    const uint32_t rem = sh.binOff[bin + 1] - sh.binOff[bin] - off;
+    if (rem > 0u && used == cap) break;
+    const uint32_t take = min(rem, cap - used);
+    const bool ends = take == rem;
+    sh.runBin[n] = bin | (ends ? RUN_ENDS : 0u);
+    sh.runK0[n] = used;
+    sh.runK1[n] = used + take;
+    sh.runOff[n] = off;
+    n++;
+    used += take;
+    if (!ends) break;
+    bin++;
+    off = 0;
   }
-  sh.seg[k] = s;
-  sh.box[k] = box;
-  sh.area[k] = area;
-  sh.shadeBase[k] = shadeBase;
-}
-
-// Block-wide sum (all threads call; every thread gets the total).
-template <int NW>
-__device__ __forceinline__ uint32_t blockSum(uint32_t v, FineShared& sh, uint32_t lane, uint32_t warp) {
-  const uint32_t w = __reduce_add_sync(0xffffffffu, v);
-  if (lane == 0) sh.red[warp] = w;
-  __syncthreads();
-  uint32_t t = 0;
-#pragma unroll
-  for (int i = 0; i < NW; i++) t += sh.red[i];
-  __syncthreads();
-  return t;
-}
-
-// Per-bin state of one pixel and of the whole tile (uniform members).
-template <int MAXL>
-struct BinState {
-  f4 acc[MAXL];
-  uint32_t nFrag, pending;            // per pixel
-  uint32_t running, runningUB;        // uniform: slots allocated (exact / upper bound)
-  bool stop;                          // uniform: the pool filled
-};
-
-// Rasterizes staged segments [s0, s0 + n) of the current bin in list order
-// (processHairSegment for every pixel), keeping the reference's fragment
-// pool accounting exact.  Called by every thread of the CTA.
-template <int TS, int MAXL>
-__device__ __forceinline__ void rasterRange(BinState<MAXL>& st, FineShared& sh, uint32_t s0, uint32_t n,
-                                            uint32_t active, uint32_t CAP, bool done, f2 pp, float zbuf,
-                                            uint32_t lx, uint32_t ly, uint32_t lane, uint32_t warp, uint32_t tid,
-                                            uint32_t P, uint32_t SP, uint32_t L, float td0, float td1,
-                                            uint32_t alphaQuadratic, float alphaMul,
-                                            const float4* __restrict__ shading,
-                                            DeviceCounters* __restrict__ counters) {
-  constexpr int NW = TS * TS / 32;
-  for (uint32_t c0 = s0; c0 < s0 + n && !st.stop; c0 += CHUNK) {
-    const uint32_t cn = min(CHUNK, s0 + n - c0);
-    uint32_t bound = 0;
-    for (uint32_t j = 0; j < cn; j++) bound += min(sh.area[c0 + j], active);
-    if (st.runningUB + bound > CAP) {  // tighten: exact count of what was added so far
-      st.running += blockSum<NW>(st.pending, sh, lane, warp);
-      st.pending = 0;
-      st.runningUB = st.running;
-    }
-    if (st.runningUB + bound <= CAP) {
-      // ---- fast path: the pool cannot fill inside this sub-chunk ----
-      if (!done) {
-        for (uint32_t j = c0; j < c0 + cn; j++) {
-          if (!inBox(sh.box[j], lx, ly)) continue;
-          f2 w; float hd;
-          if (!fragmentPasses(sh.seg[j], pp, zbuf, w, hd)) continue;
-          st.pending++;
-          st.nFrag++;
-          addFragment<MAXL>(st.acc, sh, j, w, hd, P, SP, L, td0, td1, alphaQuadratic, alphaMul, shading);
-        }
-      }
-      st.runningUB += bound;
-    } else {
-      // ---- exact path: slots in pixel order, stop at the filling segment ----
-      uint32_t mask = 0;
-      if (!done) {
-        for (uint32_t j = 0; j < cn; j++) {
-          if (!inBox(sh.box[c0 + j], lx, ly)) continue;
-          f2 w; float hd;
-          if (fragmentPasses(sh.seg[c0 + j], pp, zbuf, w, hd)) mask |= 1u << j;
-        }
-      }
-      for (uint32_t j = 0; j < cn; j++) {
-        const uint32_t bal = __ballot_sync(0xffffffffu, (mask >> j) & 1u);
-        if (lane == 0) sh.cnt[warp][j] = __popc(bal);
-      }
-      __syncthreads();
-      if (warp == 0) {
-        uint32_t c = 0;
-        if (lane < cn)
-          for (int w2 = 0; w2 < NW; w2++) c += sh.cnt[w2][lane];
-        uint32_t incl = c;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-          if (lane >= (uint32_t)o) incl += y;
-        }
-        const uint32_t fb = __ballot_sync(0xffffffffu, lane < cn && st.running + incl >= CAP);
-        const uint32_t j = fb ? (uint32_t)(__ffs(fb) - 1) : 0u;
-        const uint32_t exclJ = __shfl_sync(0xffffffffu, incl - c, j);
-        const uint32_t total = __shfl_sync(0xffffffffu, incl, cn - 1u);
-        if (lane == 0) {
-          sh.cutSeg = fb ? j : CHUNK;
-          sh.cutSlots = fb ? CAP - (st.running + exclJ) : 0u;
-          sh.chunkTotal = total;
-        }
-      }
-      __syncthreads();
-      const uint32_t cutSeg = sh.cutSeg, cutSlots = sh.cutSlots;
-      uint32_t m = mask;
-      if (cutSeg < CHUNK) {
-        uint32_t rank = 0;  // slots taken in the cut segment by lower pixels
-        for (uint32_t w2 = 0; w2 < warp; w2++) rank += sh.cnt[w2][cutSeg];
-        rank += __popc(__ballot_sync(0xffffffffu, (mask >> cutSeg) & 1u) & ((1u << lane) - 1u));
-        m &= cutSeg == 31u ? 0xffffffffu : ((2u << cutSeg) - 1u);  // segments <= cut
-        if (rank >= cutSlots) m &= ~(1u << cutSeg);
-      }
-      while (m) {
-        const uint32_t j = __ffs(m) - 1u;
-        m &= m - 1u;
-        f2 w; float hd;
-        fragmentPasses(sh.seg[c0 + j], pp, zbuf, w, hd);
-        addFragment<MAXL>(st.acc, sh, c0 + j, w, hd, P, SP, L, td0, td1, alphaQuadratic, alphaMul, shading);
-        st.nFrag++;
-      }
-      st.running = cutSeg < CHUNK ? CAP : st.running + sh.chunkTotal;
-      st.runningUB = st.running;
-      if (st.running >= CAP) {
-        if (tid == 0) atomicAdd(&counters->finePoolFullBins, 1ull);
-        st.stop = true;  // the reference breaks after the filling segment
-      }
-      __syncthreads();  // sh.cnt / cut words are reused
-    }
-  }
+  return n;
 }
 
 template <int TS, int MAXL>
-__global__ void __launch_bounds__(TS * TS, TS == 16 ? (MAXL <= 4 ? 3 : 2) : 1)
+__global__ void __launch_bounds__(TS * TS, TS == 8 ? 6 : TS == 16 ? (MAXL <= 4 ? 3 : 2) : 1)
 fineKernel(const HfbUniforms U, uint32_t S, uint32_t P, uint32_t B, uint32_t L, uint32_t SP, uint32_t CAP,
            uint32_t alphaQuadratic, float alphaMul, const float4* __restrict__ pos, const float4* __restrict__ tan,
            const float4* __restrict__ shading, const float* __restrict__ depth, const uint4* __restrict__ tiles,
            const uint32_t* __restrict__ segBuf, const uint32_t* __restrict__ tileList,
            float* __restrict__ result, DeviceCounters* __restrict__ counters) {
-  constexpr uint32_t NPX = TS * TS;
-  __shared__ FineShared sh;
+  using SM = FineSmem<TS>;
+  constexpr uint32_t NT = SM::NT, STAGE = SM::STAGE, PAIRS = SM::PAIRS, NW = NT / 32u;
+  constexpr uint32_t MODE_FAST = 0, MODE_TIGHTEN = 1;
+  extern __shared__ __align__(16) unsigned char fineSmemRaw[];
+  SM& sh = *reinterpret_cast<SM*>(fineSmemRaw);
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const uint32_t lx = tid % TS, ly = tid / TS;
   const f2 size = mk2(U.viewport.x, U.viewport.y);
@@ -776,15 +769,19 @@ fineKernel(const HfbUniforms U, uint32_t S, uint32_t P, uint32_t B, uint32_t L, 
     const uint32_t px = tbp.x0 + lx, py = tbp.y0 + ly;
     // Pixels of a partial edge tile outside the viewport take no part.
     const bool inView = px < W && py < H;
-    const f2 pp = mk2((float)px, (float)py);
-    const float zbuf = inView ? loadTex2DClamp(depth, W, H, f2i(pp.x), f2i(fsub(size.y, pp.y))) : 0.0f;
+    sh.zbuf[tid] = inView ? loadTex2DClamp(depth, W, H, f2i((float)px), f2i(fsub(size.y, (float)py))) : 0.0f;
     bool done = !inView;
+    {
+      const uint32_t dm = __ballot_sync(0xffffffffu, done);
+      if (lane == 0) sh.doneMask[warp] = dm;
+    }
     f4 fin = mk4(0.f, 0.f, 0.f, 0.f);  // rasterizerResult was cleared before the pass
     if (tid < B) sh.head[tid] = tiles[ty * tilesX * B + tx * B + tid];
     __syncthreads();
 
-    // ---- whole-tile staging: every bin's list at once when the lists carry
-    // a length hint (padding0, written by the tiles pass) that checks out ----
+    // ---- tile mode: every depth bin's list carries a length hint (padding0,
+    // written by the tiles pass) and the lists are the contiguous runs the
+    // tiles pass writes; otherwise each list is walked ----
     if (warp == 0) {
       uint32_t ok = 1, sum = 0;
       for (uint32_t b0 = 0; b0 < B; b0 += 32) {
@@ -792,9 +789,8 @@ fineKernel(const HfbUniforms U, uint32_t S, uint32_t P, uint32_t B, uint32_t L, 
         uint32_t nb = 0;
         if (bb < B) {
           const uint4 h = sh.head[bb];
-          const bool nonEmpty = (float)h.y / F_MAX_U32 != 0.0f && h.z != 0u;
-          if (nonEmpty) {
-            if (h.w != 0u && h.w <= h.z && h.z <= maxDrawn) nb = h.w; else ok = 0;
+          if (h.y != 0u && h.z != 0u) {
+            if (h.w != 0u && h.w <= h.z && h.z <= maxDrawn && h.w <= maxProcessed) nb = h.w; else ok = 0;
           }
         }
         uint32_t incl = nb;
@@ -810,15 +806,15 @@ fineKernel(const HfbUniforms U, uint32_t S, uint32_t P, uint32_t B, uint32_t L, 
       if (lane == 0) {
         sh.binOff[B] = sum;
         sh.total = sum;
-        sh.tileMode = ok && sum <= STAGE && sum <= maxProcessed;
+        sh.tileMode = ok;
         sh.bad = 0;
       }
     }
     __syncthreads();
     bool tileMode = sh.tileMode != 0u;
-    if (tileMode) {
+    if (tileMode) {  // check every link of the contiguous layout
       const uint32_t total = sh.total;
-      for (uint32_t k = tid; k < total; k += NPX) {
+      for (uint32_t k = tid; k < total; k += NT) {
         uint32_t lo = 0, hi = B;  // bin of k: binOff[lo] <= k < binOff[lo + 1]
         while (hi - lo > 1u) {
           const uint32_t mid = (lo + hi) >> 1;
@@ -827,131 +823,428 @@ fineKernel(const HfbUniforms U, uint32_t S, uint32_t P, uint32_t B, uint32_t L, 
         const uint4 h = sh.head[lo];
         const uint32_t j = k - sh.binOff[lo];
         const uint32_t idx = h.z - 1u - j;
-        const uint32_t enc = __ldg(&segBuf[1u + 2u * idx]);
         const uint32_t nxt = __ldg(&segBuf[2u + 2u * idx]);
         if (nxt != ((j + 1u == h.w) ? INVALID_PTR : idx - 1u)) sh.bad = 1;
-        sh.strand[k] = enc & 0x00ffffffu;
-        sh.segIdx[k] = enc >> 24;
       }
       __syncthreads();
       tileMode = sh.bad == 0u;
-      if (tileMode) {
-        for (uint32_t k = tid; k < total; k += NPX)
-          projectStaged<TS>(U, pos, tan, shading, S, P, SP, size, tbp.x0, tbp.y0, sh, k);
-      }
-      __syncthreads();
     }
 
-    for (uint32_t bin = 0; bin < B; bin++) {
-      const uint4 head = sh.head[bin];
-      // _getTileDepth, hairTilesResultBuffer.ts:47-54
-      const float td0 = (float)(0xffffffffu - head.x) / F_MAX_U32;
-      const float td1 = (float)head.y / F_MAX_U32;
-      if (td1 != 0.0f) {  // processTile, :205-288
-        BinState<MAXL> st;
+    // per-pixel state of the current bin
+    f4 acc[MAXL];
 #pragma unroll
-        for (int si = 0; si < MAXL; si++) st.acc[si] = mk4(0.f, 0.f, 0.f, 0.f);
-        st.nFrag = 0; st.pending = 0; st.running = 0; st.runningUB = 0; st.stop = false;
-        const uint32_t active = __syncthreads_count(!done);
-        if (tileMode) {
-          const uint32_t s0 = sh.binOff[bin], n = sh.binOff[bin + 1] - s0;
-          rasterRange<TS, MAXL>(st, sh, s0, n, active, CAP, done, pp, zbuf, lx, ly, lane, warp, tid, P, SP, L,
-                                td0, td1, alphaQuadratic, alphaMul, shading, counters);
-        } else {
-          // ---- per-bin staging: runs of the list (hinted contiguous runs in
-          // parallel, otherwise a warp walks it) ----
-          uint32_t ptr = head.z == 0u ? INVALID_PTR : head.z - 1u;
-          uint32_t hint = (head.w != 0u && head.w <= head.z && head.z <= maxDrawn) ? head.w : 0u;
-          uint32_t processed = 0;
-          while (!st.stop && ptr != INVALID_PTR && ptr < maxDrawn && processed < maxProcessed) {
-            uint32_t n = 0;
-            if (hint) {
-              n = min(min(hint, STAGE), maxProcessed - processed);
-              if (tid == 0) sh.bad = 0;
-              __syncthreads();
-              for (uint32_t k = tid; k < n; k += NPX) {
-                const uint32_t idx = ptr - k;
-                const uint32_t enc = __ldg(&segBuf[1u + 2u * idx]);
-                const uint32_t nxt = __ldg(&segBuf[2u + 2u * idx]);
-                if (nxt != ((k + 1u == hint) ? INVALID_PTR : idx - 1u)) sh.bad = 1;
-                sh.strand[k] = enc & 0x00ffffffu;
-                sh.segIdx[k] = enc >> 24;
-              }
-              __syncthreads();
-              if (sh.bad) {
-                hint = 0;  // not the contiguous layout: walk it
-                continue;
-              }
-              if (tid == 0) sh.nextPtr = (n == hint) ? INVALID_PTR : ptr - n;
-              hint -= n;
-            } else {
-              if (warp == 0) {  // speculative contiguous runs, else pointer chasing
-                uint32_t p = ptr, m = 0;
-                while (m < CHUNK && p != INVALID_PTR && p < maxDrawn && processed + m < maxProcessed) {
-                  const uint32_t want = min(CHUNK - m, maxProcessed - processed - m);
-                  const uint32_t cand = p - lane;
-                  const bool inRange = lane < want && lane <= p;
-                  uint2 e = make_uint2(0u, INVALID_PTR);
-                  if (inRange) {
-                    e.x = __ldg(&segBuf[1u + 2u * cand]);
-                    e.y = __ldg(&segBuf[2u + 2u * cand]);
-                  }
-                  const bool chain = inRange && e.y == cand - 1u;
-                  const uint32_t brk = __ballot_sync(0xffffffffu, !chain);
-                  const uint32_t first = brk ? (uint32_t)(__ffs(brk) - 1) : 32u;
-                  bool firstIn = false;
-                  uint32_t firstNext = 0u;
-                  if (first < 32u) {
-                    firstIn = __shfl_sync(0xffffffffu, inRange, first);
-                    firstNext = __shfl_sync(0xffffffffu, e.y, first);
-                  }
-                  const uint32_t cnt = firstIn ? first + 1u : first;
-                  if (lane < cnt) {
-                    sh.strand[m + lane] = e.x & 0x00ffffffu;
-                    sh.segIdx[m + lane] = e.x >> 24;
-                  }
-                  m += cnt;
-                  p = firstIn ? firstNext : p - cnt;
-                }
-                if (lane == 0) { sh.n = m; sh.nextPtr = p; }
-              }
-              __syncthreads();
-              n = sh.n;
-            }
-            if (n == 0) break;
-            for (uint32_t k = tid; k < n; k += NPX)
-              projectStaged<TS>(U, pos, tan, shading, S, P, SP, size, tbp.x0, tbp.y0, sh, k);
-            __syncthreads();
-            const uint32_t nextPtr = sh.nextPtr;
-            rasterRange<TS, MAXL>(st, sh, 0, n, active, CAP, done, pp, zbuf, lx, ly, lane, warp, tid, P, SP, L,
-                                  td0, td1, alphaQuadratic, alphaMul, shading, counters);
-            processed += n;
-            __syncthreads();  // the staged run is refilled next iteration
-            ptr = nextPtr;
-          }
+    for (int si = 0; si < MAXL; si++) acc[si] = mk4(0.f, 0.f, 0.f, 0.f);
+    uint32_t nFrag = 0, pending = 0;
+    // uniform state: cursor and the pool accounting of the bin at the cursor
+    uint32_t bin = 0, off = 0;                     // tile mode: bin, entry of its list
+    uint32_t walkPtr = INVALID_PTR, processed = 0;  // walk mode: list pointer, entries processed
+    uint32_t running = 0, runningUB = 0;            // slots taken (exact / upper bound)
+
+    while (true) {
+      // ---------------- stage the round ----------------
+      if (tileMode) {
+        if (tid == 0) {
+          uint32_t used;
+          sh.nRuns = buildRuns<TS>(sh, B, bin, off, STAGE, used);
+          sh.nStaged = used;
         }
-        // reduceHairSlices (runs for every non-empty bin, as in the reference)
-        if (!done) {
-          if (isDbg) {
-            const uint32_t cntAll = f2u(fmul(fin.x, (float)dbgMax)) + st.nFrag;
-            fin = mk4(sat((float)cntAll / (float)dbgMax), 0.0f, 0.0f, 1.0f);
-          } else {
-#pragma unroll
-            for (int si = 0; si < MAXL; si++) {
-              if ((uint32_t)si < L && fin.w < 0.999f) {
-                const float k = fsub(1.0f, fin.w);
-                fin.x = fadd(fin.x, fmul(st.acc[si].x, k));
-                fin.y = fadd(fin.y, fmul(st.acc[si].y, k));
-                fin.z = fadd(fin.z, fmul(st.acc[si].z, k));
-                fin.w = fadd(fin.w, fmul(st.acc[si].w, k));
-              }
+        __syncthreads();
+        const uint32_t nStaged = sh.nStaged, nRuns = sh.nRuns;
+        for (uint32_t k = tid; k < nStaged; k += NT) {
+          uint32_t r = 0;
+          while (r + 1u < nRuns && sh.runK0[r + 1u] <= k) r++;
+          const uint32_t b = sh.runBin[r] & 0xffu;
+          const uint32_t idx = sh.head[b].z - 1u - (sh.runOff[r] + k - sh.runK0[r]);
+          const uint32_t enc = __ldg(&segBuf[1u + 2u * idx]);
+          sh.strand[k] = enc & 0x00ffffffu;
+          sh.segIdx[k] = enc >> 24;
+          sh.listIdx[k] = idx;
+        }
+      } else {
+        while (bin < B && sh.head[bin].y == 0u) bin++;  // bins without depth are skipped
+        if (bin >= B) break;
+        if (processed == 0u) {
+          const uint32_t hz = sh.head[bin].z;
+          walkPtr = hz == 0u ? INVALID_PTR : hz - 1u;
+        }
+        if (warp == 0) {  // speculative contiguous runs, else pointer chasing
+          uint32_t p = walkPtr, m = 0;
+          while (m < STAGE && p != INVALID_PTR && p < maxDrawn && processed + m < maxProcessed) {
+            const uint32_t want = min(min(32u, STAGE - m), maxProcessed - processed - m);
+            const uint32_t cand = p - lane;
+            const bool inRange = lane < want && lane <= p;
+            uint2 e = make_uint2(0u, INVALID_PTR);
+            if (inRange) {
+              e.x = __ldg(&segBuf[1u + 2u * cand]);
+              e.y = __ldg(&segBuf[2u + 2u * cand]);
             }
-            done = fin.w >= 0.999f;  // isPixelDone with ALPHA_CUTOFF
+            const bool chain = inRange && e.y == cand - 1u;
+            const uint32_t brk = __ballot_sync(0xffffffffu, !chain);
+            const uint32_t first = brk ? (uint32_t)(__ffs(brk) - 1) : 32u;
+            bool firstIn = false;
+            uint32_t firstNext = 0u;
+            if (first < 32u) {
+              firstIn = __shfl_sync(0xffffffffu, inRange, first);
+              firstNext = __shfl_sync(0xffffffffu, e.y, first);
+            }
+            const uint32_t cnt = firstIn ? first + 1u : first;
+            if (lane < cnt) {
+              sh.strand[m + lane] = e.x & 0x00ffffffu;
+              sh.segIdx[m + lane] = e.x >> 24;
+              sh.listIdx[m + lane] = cand;
+            }
+            m += cnt;
+            p = firstIn ? firstNext : p - cnt;
+          }
+          if (lane == 0) {
+            const bool ends = !(p != INVALID_PTR && p < maxDrawn && processed + m < maxProcessed);
+            sh.nStaged = m;
+            sh.walkNext = p;
+            sh.nRuns = 1;
+            sh.runBin[0] = bin | (ends ? RUN_ENDS : 0u);
+            sh.runK0[0] = 0;
+            sh.runK1[0] = m;
+            sh.runOff[0] = processed;
           }
         }
       }
-      // checkAllPixelsInWkgrpDone, :305-327
+      __syncthreads();
+      uint32_t nRuns = sh.nRuns;
+      if (nRuns == 0u) break;  // tile mode: no depth bin left
+      const bool fresh = sh.runOff[0] == 0u;  // run 0 starts its bin
+      if (fresh) { running = 0; runningUB = 0; }
+
+      // ---------------- project ----------------
+      {
+        const uint32_t nStaged = sh.nStaged;
+#pragma unroll
+        for (uint32_t w = 0; w < STAGE / 32; w++) sh.pixMask[w][tid] = 0u;
+        for (uint32_t k = tid; k < nStaged; k += NT) {
+          uint32_t r = 0;
+          while (r + 1u < nRuns && sh.runK0[r + 1u] <= k) r++;
+          sh.pairBase[k] = stageSegment<TS>(sh, k, sh.runBin[r] & 0xffu, U, pos, tan, shading, S, P, SP, size,
+                                            tbp.x0, tbp.y0);
+        }
+        __syncthreads();
+        // exclusive prefix of the areas; the round keeps the longest prefix
+        // of segments whose pairs fit
+        if (warp == 0) {
+          uint32_t carry = 0, nSeg = nStaged;
+          for (uint32_t k0 = 0; k0 < nStaged; k0 += 32) {
+            const uint32_t k = k0 + lane;
+            const uint32_t a = k < nStaged ? sh.pairBase[k] : 0u;
+            uint32_t incl = a;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+              const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+              if (lane >= (uint32_t)o) incl += y;
+            }
+            if (k < nStaged) sh.pairBase[k] = carry + incl - a;
+            const uint32_t over = __ballot_sync(0xffffffffu, k < nStaged && carry + incl > PAIRS);
+            if (over && nSeg == nStaged) nSeg = k0 + (uint32_t)(__ffs(over) - 1);
+            carry += __shfl_sync(0xffffffffu, incl, 31);
+          }
+          if (lane == 0) {
+            sh.pairBase[nStaged] = carry;
+            sh.passCount = 0;
+            if (nSeg < nStaged) {  // drop the segments from nSeg on
+              if (tileMode) {
+                uint32_t used;
+                sh.nRuns = buildRuns<TS>(sh, B, bin, off, nSeg, used);
+              } else {
+                sh.runK1[0] = nSeg;
+                sh.runBin[0] &= ~RUN_ENDS;
+              }
+            }
+            sh.nSeg = nSeg;
+          }
+        }
+        __syncthreads();
+      }
+      uint32_t nSeg = sh.nSeg;
+      nRuns = sh.nRuns;
+      const uint32_t nPairs = sh.pairBase[nSeg];
+
+      // ---------------- A1: edge tests, one thread per pair ----------------
+      {
+        const uint32_t per = divCeil(nPairs, NT);
+        uint32_t p = tid * per;
+        const uint32_t pEnd = min(p + per, nPairs);
+        uint32_t k = 0, rx = 0, ry = 0, bw = 1, bh = 1, bx0 = 0, by0 = 0, myCnt = 0;
+        float eox[4], eoy[4], eex[4], eey[4];
+        auto loadSeg = [&](uint32_t kk) {
+          const uint32_t bx = sh.box[kk];
+          bx0 = bx & 0xffu;
+          by0 = (bx >> 8) & 0xffu;
+          bw = ((bx >> 16) & 0xffu) - bx0 + 1u;
+          bh = (bx >> 24) - by0 + 1u;
+#pragma unroll
+          for (int i = 0; i < 4; i++) {
+            eox[i] = sh.ox[i][kk]; eoy[i] = sh.oy[i][kk]; eex[i] = sh.ex[i][kk]; eey[i] = sh.ey[i][kk];
+          }
+        };
+        if (p < pEnd) {
+          uint32_t lo = 0, hi = nSeg;  // last k with pairBase[k] <= p
+          while (hi - lo > 1u) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (sh.pairBase[mid] <= p) lo = mid; else hi = mid;
+          }
+          k = lo;
+          loadSeg(k);
+          const uint32_t r = p - sh.pairBase[k];
+          ry = r / bw;
+          rx = r - ry * bw;
+        }
+        for (uint32_t it = 0; it < per; it++) {
+          const bool valid = p < pEnd;
+          bool pass = false;
+          uint32_t pix = 0;
+          if (valid) {
+            const uint32_t qx = bx0 + rx, qy = by0 + ry;
+            pix = qy * TS + qx;
+            if (!((sh.doneMask[pix >> 5] >> (pix & 31u)) & 1u)) {
+              const f2 pf = mk2((float)(tbp.x0 + qx), (float)(tbp.y0 + qy));
+              pass = true;
+#pragma unroll
+              for (int i = 0; i < 4; i++) {  // edgeFunction, swRasterizeHair.wgsl.ts:128-130
+                const float C = fsub(fmul(fsub(pf.x, eox[i]), eey[i]), fmul(fsub(pf.y, eoy[i]), eex[i]));
+                pass = pass && C >= 0.0f;
+              }
+            }
+            sh.pairInfo[p] = PAIR_NONE;
+          }
+          const uint32_t bal = __ballot_sync(0xffffffffu, pass);
+          if (bal) {
+            const uint32_t leader = (uint32_t)(__ffs(bal) - 1);
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(&sh.passCount, (uint32_t)__popc(bal));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (pass) sh.frag[base + __popc(bal & ((1u << lane) - 1u))].x = pix | (k << 16);
+          }
+          myCnt += pass ? 1u : 0u;
+          if (valid) {
+            p++;
+            if (++rx == bw) {
+              rx = 0;
+              if (++ry == bh) {  // segment done
+                if (myCnt) atomicAdd(&sh.cntEdge[k], myCnt);
+                myCnt = 0;
+                if (p < pEnd) {
+                  while (sh.pairBase[k + 1u] <= p) k++;  // next segment with pairs
+                  loadSeg(k);
+                  ry = 0;
+                }
+              }
+            }
+          }
+        }
+        if (myCnt) atomicAdd(&sh.cntEdge[k], myCnt);
+      }
+      __syncthreads();
+
+      // ---------------- can a bin fill its pool in this round? ----------------
+      if (warp == 0) {
+        uint32_t mode = MODE_FAST, keep = nRuns, e0 = 0, eLast = 0;
+        for (uint32_t r = 0; r < nRuns; r++) {
+          uint32_t e = 0;
+          for (uint32_t k = sh.runK0[r] + lane; k < sh.runK1[r]; k += 32) e += sh.cntEdge[k];
+          e = __reduce_add_sync(0xffffffffu, e);
+          const uint32_t base = r == 0u ? runningUB : 0u;
+          if (r == 0u) e0 = e;
+          if (base + e > CAP) {
+            if (r == 0u) { mode = MODE_TIGHTEN; keep = 1; } else { keep = r; }
+            break;
+          }
+          eLast = e;
+        }
+        if (lane == 0) {
+          sh.mode = mode;
+          sh.e0 = e0;
+          sh.eLast = eLast;
+          if (keep < nRuns) {  // the round ends where that bin's run starts
+            sh.nRuns = keep;
+            sh.nSeg = sh.runK1[keep - 1u];
+          }
+          sh.roundFrags = 0;
+        }
+      }
+      __syncthreads();
+      nRuns = sh.nRuns;
+      nSeg = sh.nSeg;
+      bool exact = false;
+      if (sh.mode == MODE_TIGHTEN) {
+        running += blockSum<NW>(pending, sh.red, lane, warp);
+        pending = 0;
+        runningUB = running;
+        exact = runningUB + sh.e0 > CAP;
+      }
+
+      // ---------------- A2: fragments, one thread per passing pair ----------------
+      {
+        const uint32_t nPass = sh.passCount;
+        for (uint32_t i = tid; i < nPass; i += NT) {
+          const uint32_t e = sh.frag[i].x;
+          const uint32_t pix = e & 0xffffu, k = e >> 16;
+          if (k >= nSeg) continue;  // dropped from the round
+          const uint32_t qx = pix % TS, qy = pix / TS;
+          const f2 pf = mk2((float)(tbp.x0 + qx), (float)(tbp.y0 + qy));
+          QuadConst qc;
+          qc.sm = mk2(sh.qsx[k], sh.qsy[k]);
+          qc.ab = mk2(sh.qax[k], sh.qay[k]);
+          qc.d2 = sh.qd2[k]; qc.lse = sh.qlse[k]; qc.wS = sh.qws[k]; qc.wE = sh.qwe[k];
+          qc.ab2 = mk2(sh.ex[3][k], sh.ey[3][k]);
+          qc.d22 = sh.qd22[k];
+          const f2 w = interpolateHairQuadPre(qc, mk2(sh.ox[3][k], sh.oy[3][k]), pf);
+          const float hd = interpolateHairF32(w, mk4(sh.dp[0][k], sh.dp[1][k], sh.dp[2][k], sh.dp[3][k]));
+          if (!(hd < sh.zbuf[pix])) continue;  // depth test with GL_LESS (skip when >=)
+          const uint4 h = sh.head[sh.shadeBase[k] >> 24];
+          const float td0 = (float)(0xffffffffu - h.x) / F_MAX_U32;  // _getTileDepth
+          const float td1 = (float)h.y / F_MAX_U32;
+          uint32_t slice;
+          const uint2 col = fragmentColour<TS>(sh, k, w, hd, P, SP, L, td0, td1, alphaQuadratic, alphaMul,
+                                               shading, slice);
+          sh.frag[i] = col;
+          const uint32_t bx = sh.box[k];
+          sh.pairInfo[sh.pairBase[k] + (qy - ((bx >> 8) & 0xffu)) * (((bx >> 16) & 0xffu) - (bx & 0xffu) + 1u) +
+                      (qx - (bx & 0xffu))] = i | (slice << 16);
+          atomicOr(&sh.pixMask[k >> 5][pix], 1u << (k & 31u));
+          if (exact) atomicAdd(&sh.cntFrag[k], 1u);
+        }
+      }
+      __syncthreads();
+
+      // ---------------- exact accounting: the segment that fills the pool ----------------
+      if (exact) {
+        if (warp == 0) {  // one run (this bin) in the round
+          uint32_t carry = 0, cut = INVALID_PTR, cutSlots = 0;
+          for (uint32_t k0 = 0; k0 < nSeg; k0 += 32) {
+            const uint32_t k = k0 + lane;
+            const uint32_t c = k < nSeg ? sh.cntFrag[k] : 0u;
+            uint32_t incl = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+              const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+              if (lane >= (uint32_t)o) incl += y;
+            }
+            const uint32_t fb = __ballot_sync(0xffffffffu, k < nSeg && running + carry + incl >= CAP);
+            if (fb) {
+              const uint32_t j = (uint32_t)(__ffs(fb) - 1);
+              cut = k0 + j;
+              cutSlots = CAP - (running + carry + __shfl_sync(0xffffffffu, incl - c, j));
+              break;
+            }
+            carry += __shfl_sync(0xffffffffu, incl, 31);
+          }
+          if (lane == 0) {
+            sh.cutSeg = cut;
+            sh.cutSlots = cutSlots;
+            sh.roundFrags = carry;
+            if (cut != INVALID_PTR) {
+              sh.nSeg = cut + 1u;
+              sh.runK1[0] = cut + 1u;
+              sh.runBin[0] |= RUN_ENDS;  // the reference breaks after the filling segment
+              atomicAdd(&counters->finePoolFullBins, 1ull);
+            }
+          }
+        }
+        __syncthreads();
+        const uint32_t cut = sh.cutSeg;
+        if (cut != INVALID_PTR) {  // slots of the filling segment in pixel order
+          const uint32_t base = sh.pairBase[cut], area = sh.pairBase[cut + 1u] - base;
+          const bool has = tid < area && sh.pairInfo[base + tid] != PAIR_NONE;
+          const uint32_t rank = blockExclusive<NW>(has ? 1u : 0u, sh.red, lane, warp);
+          if (has && rank >= sh.cutSlots) sh.pairInfo[base + tid] = PAIR_NONE;
+          __syncthreads();
+        }
+        nSeg = sh.nSeg;
+      }
+
+      // ---------------- B: every pixel blends its fragments in list order ----------------
+      for (uint32_t r = 0; r < nRuns; r++) {
+        const uint32_t rb = sh.runBin[r], k0 = sh.runK0[r], k1 = sh.runK1[r];
+        if (!done && k0 < k1) {
+          for (uint32_t w = k0 >> 5; w <= (k1 - 1u) >> 5; w++) {
+            const uint32_t lo = max(k0, w * 32u) - w * 32u, hi = min(k1, w * 32u + 32u) - w * 32u;
+            uint32_t bits = sh.pixMask[w][tid] & (hi == 32u ? 0xffffffffu : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
+            while (bits) {
+              const uint32_t j = w * 32u + (uint32_t)(__ffs(bits) - 1);
+              bits &= bits - 1u;
+              const uint32_t b = sh.box[j];
+              const uint32_t bx0 = b & 0xffu, by0 = (b >> 8) & 0xffu;
+              const uint32_t info =
+                  sh.pairInfo[sh.pairBase[j] + (ly - by0) * (((b >> 16) & 0xffu) - bx0 + 1u) + (lx - bx0)];
+              if (info != PAIR_NONE) {  // not dropped by a full pool
+                blendFragment<MAXL>(acc, info >> 16, sh.frag[info & 0xffffu]);
+                nFrag++;
+                pending++;
+              }
+            }
+          }
+        }
+        if (rb & RUN_ENDS) {
+          // reduceHairSlices (runs for every bin with depth, as in the reference)
+          if (!done) {
+            if (isDbg) {
+              const uint32_t cntAll = f2u(fmul(fin.x, (float)dbgMax)) + nFrag;
+              fin = mk4(sat((float)cntAll / (float)dbgMax), 0.0f, 0.0f, 1.0f);
+            } else {
+#pragma unroll
+              for (int si = 0; si < MAXL; si++) {
+                if ((uint32_t)si < L && fin.w < 0.999f) {
+                  const float kk = fsub(1.0f, fin.w);
+                  fin.x = fadd(fin.x, fmul(acc[si].x, kk));
+                  fin.y = fadd(fin.y, fmul(acc[si].y, kk));
+                  fin.z = fadd(fin.z, fmul(acc[si].z, kk));
+                  fin.w = fadd(fin.w, fmul(acc[si].w, kk));
+                }
+              }
+              done = fin.w >= 0.999f;  // isPixelDone with ALPHA_CUTOFF
+            }
+          }
+#pragma unroll
+          for (int si = 0; si < MAXL; si++) acc[si] = mk4(0.f, 0.f, 0.f, 0.f);
+          nFrag = 0;
+          pending = 0;
+        }
+      }
+
+      // ---------------- carry the pool state and advance the cursor ----------------
+      const uint32_t lastBin = sh.runBin[nRuns - 1u];
+      const bool lastEnds = (lastBin & RUN_ENDS) != 0u;
+      if (lastEnds) {
+        running = 0;
+        runningUB = 0;
+      } else if (nRuns == 1u) {
+        if (exact) {
+          running += sh.roundFrags;
+          runningUB = running;
+          pending = 0;
+        } else {
+          runningUB += sh.e0;
+        }
+      } else {
+        running = 0;
+        runningUB = sh.eLast;
+      }
+      if (tileMode) {
+        const uint32_t lb = lastBin & 0xffu;
+        if (lastEnds) { bin = lb + 1u; off = 0; }
+        else { off = sh.runOff[nRuns - 1u] + sh.runK1[nRuns - 1u] - sh.runK0[nRuns - 1u]; bin = lb; }
+      } else {
+        if (lastEnds) { bin++; processed = 0; }
+        else {
+          walkPtr = nSeg < sh.nStaged ? sh.listIdx[nSeg] : sh.walkNext;
+          processed += nSeg;
+        }
+      }
+      {
+        const uint32_t dm = __ballot_sync(0xffffffffu, done);
+        if (lane == 0) sh.doneMask[warp] = dm;
+      }
+      // checkAllPixelsInWkgrpDone, :305-327 (also the barrier before the
+      // next round rewrites the staged state)
       if (__syncthreads_and(done)) break;
+      if (bin >= B) break;
     }
     if (inView) res[(size_t)py * W + px] = make_float4(fin.x, fin.y, fin.z, fin.w);
     __syncthreads();  // the tile's shared state is rewritten for the next tile
@@ -962,11 +1255,18 @@ template <int TS, int MAXL>
 cudaError_t launchFineT(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, const float* pos,
                         const float* tan, const float* shading, const float* depth, HfbRasterBuffers& rb) {
   const HfbConfig& cfg = c->cfg;
+  constexpr size_t SMEM = sizeof(FineSmem<TS>);
   int& perSM = c->fineBlocksPerSM[TS == 8 ? 0 : TS == 16 ? 1 : 2][MAXL == 4 ? 0 : MAXL == 8 ? 1 : 2];
-  if (perSM == 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, fineKernel<TS, MAXL>, TS * TS, 0);
-  uint32_t grid = cfg.processorCount ? cfg.processorCount : (uint32_t)(max(perSM, 1) * c->smCount);
+  if (perSM == 0) {
+    cudaError_t e = cudaFuncSetAttribute(fineKernel<TS, MAXL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, fineKernel<TS, MAXL>, TS * TS, SMEM);
+    if (e != cudaSuccess) return e;
+    if (perSM < 1) return cudaErrorInvalidConfiguration;
+  }
+  uint32_t grid = cfg.processorCount ? cfg.processorCount : (uint32_t)(perSM * c->smCount);
   uint32_t CAP = cfg.avgFragmentsPerSlice * cfg.slicesPerPixel * cfg.tileSize * cfg.tileSize;
-  fineKernel<TS, MAXL><<<grid, TS * TS, 0, c->stream>>>(
+  fineKernel<TS, MAXL><<<grid, TS * TS, SMEM, c->stream>>>(
       u, h.strandsCount, h.pointsPerStrand, cfg.tileDepthBins, cfg.slicesPerPixel, cfg.shadingPoints, CAP,
       cfg.alphaQuadratic, cfg.alphaMultiplier, (const float4*)pos, (const float4*)tan, (const float4*)shading,
       depth, (const uint4*)rb.tiles, rb.tileSegments, rb.tileList, rb.rasterizerResult,
