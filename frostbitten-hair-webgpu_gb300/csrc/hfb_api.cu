@@ -2,6 +2,7 @@
 // points declared in include/hairfb.h.  Every entry point converts CUDA and
 // argument errors into HFB_ERR_* codes plus a message; nothing throws across
 // the boundary.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -92,6 +93,23 @@ TilesScratch tilesScratchLayout(void* base, const HfbConfig& cfg, uint32_t W, ui
   return s;
 }
 
+FineScratch fineScratchLayout(void* base, const HfbConfig& cfg, uint32_t W, uint32_t H) {
+  const size_t T = (size_t)divCeil(W, cfg.tileSize) * divCeil(H, cfg.tileSize);
+  const size_t groupBytes = (size_t)cfg.tileSize * cfg.tileSize * 16;
+  FineScratch s;
+  // split groups: at most 1024, and at most 4 MiB of composites
+  s.maxGroups = (uint32_t)std::min<size_t>(1024, (4u << 20) / groupBytes);
+  s.maxItems = (uint32_t)(T + s.maxGroups);
+  char* p = (char*)base;
+  size_t off = 0;
+  s.hdr = (uint32_t*)(p + off); off = alignUp(off + 16);
+  s.items = (uint4*)(p + off); off = alignUp(off + (size_t)s.maxItems * 16);
+  s.arrivals = (uint32_t*)(p + off); off = alignUp(off + (size_t)s.maxGroups * 4);
+  s.groups = (float4*)(p + off); off = alignUp(off + (size_t)s.maxGroups * groupBytes);
+  s.bytes = off;
+  return s;
+}
+
 }  // namespace hfb
 
 extern "C" {
@@ -164,6 +182,8 @@ int hfb_get_counters(HfbCtx* c, HfbCounters* out) {
   out->finePoolFullBins = d.finePoolFullBins;
   out->waitTimeouts = d.waitTimeouts;
   out->launches = c->launches;
+  out->fineSplitTiles = d.fineSplitTiles;
+  out->fineSplitRedone = d.fineSplitRedone;
   return HFB_OK;
 }
 
@@ -213,7 +233,8 @@ int hfb_buffer_clear(HfbCtx* c, void* dst, size_t bytes) {
 size_t hfb_raster_scratch_bytes(const HfbConfig* cfg, uint32_t width, uint32_t height) {
   if (!cfg || width == 0 || height == 0) return 0;
   uint32_t md = hfb::maxDrawnSegments(*cfg, width, height);
-  return hfb::tilesScratchLayout(nullptr, *cfg, width, height, md).bytes;
+  return std::max(hfb::tilesScratchLayout(nullptr, *cfg, width, height, md).bytes,
+                  hfb::fineScratchLayout(nullptr, *cfg, width, height).bytes);
 }
 
 int hfb_raster_buffers_alloc(HfbCtx* c, uint32_t W, uint32_t H, HfbRasterBuffers* rb) {

@@ -32,6 +32,8 @@ struct DeviceCounters {
   unsigned long long tileRecordsDropped;
   unsigned long long finePoolFullBins;
   unsigned long long waitTimeouts;
+  unsigned long long fineSplitTiles;
+  unsigned long long fineSplitRedone;
 };
 
 // Layout of the tiles-pass scratch area (all offsets 256-byte aligned).
@@ -45,6 +47,18 @@ struct TilesScratch {
 };
 TilesScratch tilesScratchLayout(void* base, const HfbConfig& cfg, uint32_t W, uint32_t H,
                                 uint32_t maxDrawn);
+
+// Layout of the fine-pass scratch area (the same memory as the tiles pass's,
+// which is dead by then; all offsets 256-byte aligned).
+struct FineScratch {
+  uint32_t* hdr;       // [0] = work items
+  uint4* items;        // tile list index, b0 | b1 << 8 | group << 16 | groups << 24, first group slot
+  uint32_t* arrivals;  // per split tile (at its first group slot): groups done | 1 << 31 if one gave up
+  float4* groups;      // per group slot: the TS*TS composites of the group's depth bins
+  uint32_t maxItems, maxGroups;
+  size_t bytes;
+};
+FineScratch fineScratchLayout(void* base, const HfbConfig& cfg, uint32_t W, uint32_t H);
 uint32_t maxDrawnSegments(const HfbConfig& cfg, uint32_t W, uint32_t H);
 
 // Launchers. Each returns cudaSuccess or the launch error.

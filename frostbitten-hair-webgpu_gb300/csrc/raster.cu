@@ -521,6 +521,7 @@ constexpr uint32_t MAX_RUNS = 66;           // runs of one round: at most one pe
 constexpr uint32_t PAIR_NONE = 0xffffffffu; // pair without a fragment
 constexpr uint32_t EMPTY_BOX = 0x0000ffffu; // x0 = y0 = 255 > x1 = y1 = 0
 constexpr uint32_t RUN_ENDS = 1u << 31;
+constexpr uint32_t FINE_SPLIT_MIN = 256;  // records: tiles below this are never split
 
 template <int TS> struct FineDims;
 template <> struct FineDims<8> { static constexpr uint32_t STAGE = 64, PAIRS = 1024; };
@@ -555,12 +556,8 @@ struct FineSmem {
   uint32_t runBin[MAX_RUNS], runK0[MAX_RUNS], runK1[MAX_RUNS], runOff[MAX_RUNS];
   uint32_t red[32];
   uint32_t nRuns, nStaged, nSeg, passCount, queueIdx, bad, tileMode, total, walkNext;
-  uint32_t mode, cutSeg, cutSlots, roundFrags, e0, eLast;
+  uint32_t mode, cutSeg, cutSlots, roundFrags, e0, eLast, arrive;
 };
-
-__device__ __forceinline__ bool inBox(uint32_t box, uint32_t lx, uint32_t ly) {
-  return lx >= (box & 0xffu) && ly >= ((box >> 8) & 0xffu) && lx <= ((box >> 16) & 0xffu) && ly <= (box >> 24);
-}
 
 // Block-wide sum (all threads call; every thread gets the total).
 template <int NW>
@@ -729,525 +726,693 @@ __device__ __forceinline__ uint32_t buildRuns(FineSmem<TS>& sh, uint32_t B, uint
   return n;
 }
 
+// Shared inputs of the fine pass.
+struct FineArgs {
+  uint32_t S, P, B, L, SP, CAP, alphaQuadratic;
+  float alphaMul;
+  const float4* __restrict__ pos;
+  const float4* __restrict__ tan;
+  const float4* __restrict__ shading;
+  const float* __restrict__ depth;
+  const uint4* __restrict__ tiles;
+  const uint32_t* __restrict__ segBuf;
+  DeviceCounters* counters;
+};
+
+// Rasterizes depth bins [b0, b1) of tile tileIdx in order, every pixel
+// starting from an empty colour (processTile per bin + reduceHairSlices,
+// hairFinePass.wgsl.ts:205-288), and leaves each pixel's colour in fin.
+// With `independent`, the bins are a later part of a split tile: every pixel
+// in view takes part, and the call gives up (returns false) as soon as a bin
+// could fill its fragment pool, whose cut would depend on which pixels the
+// earlier bins finished.
 template <int TS, int MAXL>
-__global__ void __launch_bounds__(TS * TS, TS == 8 ? 6 : TS == 16 ? (MAXL <= 4 ? 3 : 2) : 1)
-fineKernel(const HfbUniforms U, uint32_t S, uint32_t P, uint32_t B, uint32_t L, uint32_t SP, uint32_t CAP,
-           uint32_t alphaQuadratic, float alphaMul, const float4* __restrict__ pos, const float4* __restrict__ tan,
-           const float4* __restrict__ shading, const float* __restrict__ depth, const uint4* __restrict__ tiles,
-           const uint32_t* __restrict__ segBuf, const uint32_t* __restrict__ tileList,
-           float* __restrict__ result, DeviceCounters* __restrict__ counters) {
+__device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U, const FineArgs& a,
+                                         uint32_t tileIdx, uint32_t b0, uint32_t b1, bool independent, f4& fin) {
   using SM = FineSmem<TS>;
   constexpr uint32_t NT = SM::NT, STAGE = SM::STAGE, PAIRS = SM::PAIRS, NW = NT / 32u;
-  constexpr uint32_t MODE_FAST = 0, MODE_TIGHTEN = 1;
-  extern __shared__ __align__(16) unsigned char fineSmemRaw[];
-  SM& sh = *reinterpret_cast<SM*>(fineSmemRaw);
+  constexpr uint32_t MODE_FAST = 0, MODE_TIGHTEN = 1, MODE_ABORT = 2;
+  const uint32_t S = a.S, P = a.P, B = a.B, L = a.L, SP = a.SP, CAP = a.CAP, alphaQuadratic = a.alphaQuadratic;
+  const float alphaMul = a.alphaMul;
+  const float4* __restrict__ pos = a.pos;
+  const float4* __restrict__ tan = a.tan;
+  const float4* __restrict__ shading = a.shading;
+  const uint32_t* __restrict__ segBuf = a.segBuf;
+  DeviceCounters* __restrict__ counters = a.counters;
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const uint32_t lx = tid % TS, ly = tid / TS;
   const f2 size = mk2(U.viewport.x, U.viewport.y);
   const uint32_t W = f2u(size.x), H = f2u(size.y);
-  const uint32_t tilesX = divCeil(W, TS), tileCount = tilesX * divCeil(H, TS);
+  const uint32_t tilesX = divCeil(W, TS);
   const uint32_t maxDrawn = U.maxDrawnHairSegments;
   const uint32_t maxProcessed = S * P;  // MAX_PROCESSED_SEGMENTS, hairFinePass.wgsl.ts:212
   const uint32_t dispMode = U.displayMode & 0xffu;
   const uint32_t dbgMax = dispMode == 4u ? ((U.displayMode >> 8) & 0xffffu) : 0u;  // getDbgSlicesModeMaxSlices
   const bool isDbg = dbgMax != 0u;
-  const uint32_t drawnTiles = tileList[0];
-  // the list array sits at byte offset 4 (hairTileSegmentsBuffer.ts:60-68):
-  // only 4-byte loads are aligned there
-  uint32_t* queue = reinterpret_cast<uint32_t*>(result);  // tileQueueAtomicIdx
-  float4* res = reinterpret_cast<float4*>(result + 4);
+  const uint32_t tx = tileIdx % tilesX, ty = tileIdx / tilesX;
+  const TileB tbp = tileBoundsPx(W, H, TS, tx, ty);
+  const uint32_t px = tbp.x0 + lx, py = tbp.y0 + ly;
+  // Pixels of a partial edge tile outside the viewport take no part.
+  const bool inView = px < W && py < H;
+  sh.zbuf[tid] = inView ? loadTex2DClamp(a.depth, W, H, f2i((float)px), f2i(fsub(size.y, (float)py))) : 0.0f;
+  bool done = !inView;
+  {
+    const uint32_t dm = __ballot_sync(0xffffffffu, done);
+    if (lane == 0) sh.doneMask[warp] = dm;
+  }
+  fin = mk4(0.f, 0.f, 0.f, 0.f);  // rasterizerResult was cleared before the pass
+  if (tid < B) sh.head[tid] = a.tiles[ty * tilesX * B + tx * B + tid];
+  __syncthreads();
+
+  // ---- tile mode: every depth bin's list carries a length hint (padding0,
+  // written by the tiles pass) and the lists are the contiguous runs the
+  // tiles pass writes; otherwise each list is walked ----
+  if (warp == 0) {
+    uint32_t ok = 1, sum = 0;
+    for (uint32_t c0 = 0; c0 < B; c0 += 32) {
+      const uint32_t bb = c0 + lane;
+      uint32_t nb = 0;
+      if (bb >= b0 && bb < b1) {
+        const uint4 h = sh.head[bb];
+        if (h.y != 0u && h.z != 0u) {
+          if (h.w != 0u && h.w <= h.z && h.z <= maxDrawn && h.w <= maxProcessed) nb = h.w; else ok = 0;
+        }
+      }
+      uint32_t incl = nb;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+      }
+      if (bb < B) sh.binOff[bb] = sum + incl - nb;
+      sum += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    ok = __all_sync(0xffffffffu, ok);
+    if (lane == 0) {
+      sh.binOff[B] = sum;
+      sh.total = sum;
+      sh.tileMode = ok;
+      sh.bad = 0;
+    }
+  }
+  __syncthreads();
+  bool tileMode = sh.tileMode != 0u;
+  if (tileMode) {  // check every link of the contiguous layout
+    const uint32_t total = sh.total;
+    for (uint32_t k = tid; k < total; k += NT) {
+      uint32_t lo = 0, hi = B;  // bin of k: binOff[lo] <= k < binOff[lo + 1]
+      while (hi - lo > 1u) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (sh.binOff[mid] <= k) lo = mid; else hi = mid;
+      }
+      const uint4 h = sh.head[lo];
+      const uint32_t j = k - sh.binOff[lo];
+      const uint32_t idx = h.z - 1u - j;
+      const uint32_t nxt = __ldg(&segBuf[2u + 2u * idx]);
+      if (nxt != ((j + 1u == h.w) ? INVALID_PTR : idx - 1u)) sh.bad = 1;
+    }
+    __syncthreads();
+    tileMode = sh.bad == 0u;
+  }
+
+  // per-pixel state of the current bin
+  f4 acc[MAXL];
+#pragma unroll
+  for (int si = 0; si < MAXL; si++) acc[si] = mk4(0.f, 0.f, 0.f, 0.f);
+  uint32_t nFrag = 0, pending = 0;
+  // uniform state: cursor and the pool accounting of the bin at the cursor
+  uint32_t bin = b0, off = 0;                    // tile mode: bin, entry of its list
+  uint32_t walkPtr = INVALID_PTR, processed = 0;  // walk mode: list pointer, entries processed
+  uint32_t running = 0, runningUB = 0;            // slots taken (exact / upper bound)
 
   while (true) {
-    if (tid == 0) sh.queueIdx = atomicAdd(queue, 1u);  // getNextTileIdx, :294-303
+    // ---------------- stage the round ----------------
+    if (tileMode) {
+      if (tid == 0) {
+        uint32_t used;
+        sh.nRuns = buildRuns<TS>(sh, b1, bin, off, STAGE, used);
+        sh.nStaged = used;
+      }
+      __syncthreads();
+      const uint32_t nStaged = sh.nStaged, nRuns = sh.nRuns;
+      for (uint32_t k = tid; k < nStaged; k += NT) {
+        uint32_t r = 0;
+        while (r + 1u < nRuns && sh.runK0[r + 1u] <= k) r++;
+        const uint32_t b = sh.runBin[r] & 0xffu;
+        const uint32_t idx = sh.head[b].z - 1u - (sh.runOff[r] + k - sh.runK0[r]);
+        const uint32_t enc = __ldg(&segBuf[1u + 2u * idx]);
+        sh.strand[k] = enc & 0x00ffffffu;
+        sh.segIdx[k] = enc >> 24;
+        sh.listIdx[k] = idx;
+      }
+    } else {
+      while (bin < b1 && sh.head[bin].y == 0u) bin++;  // bins without depth are skipped
+      if (bin >= b1) break;
+      if (processed == 0u) {
+        const uint32_t hz = sh.head[bin].z;
+        walkPtr = hz == 0u ? INVALID_PTR : hz - 1u;
+      }
+      if (warp == 0) {  // speculative contiguous runs, else pointer chasing
+        uint32_t p = walkPtr, m = 0;
+        while (m < STAGE && p != INVALID_PTR && p < maxDrawn && processed + m < maxProcessed) {
+          const uint32_t want = min(min(32u, STAGE - m), maxProcessed - processed - m);
+          const uint32_t cand = p - lane;
+          const bool inRange = lane < want && lane <= p;
+          uint2 e = make_uint2(0u, INVALID_PTR);
+          if (inRange) {
+            e.x = __ldg(&segBuf[1u + 2u * cand]);
+            e.y = __ldg(&segBuf[2u + 2u * cand]);
+          }
+          const bool chain = inRange && e.y == cand - 1u;
+          const uint32_t brk = __ballot_sync(0xffffffffu, !chain);
+          const uint32_t first = brk ? (uint32_t)(__ffs(brk) - 1) : 32u;
+          bool firstIn = false;
+          uint32_t firstNext = 0u;
+          if (first < 32u) {
+            firstIn = __shfl_sync(0xffffffffu, inRange, first);
+            firstNext = __shfl_sync(0xffffffffu, e.y, first);
+          }
+          const uint32_t cnt = firstIn ? first + 1u : first;
+          if (lane < cnt) {
+            sh.strand[m + lane] = e.x & 0x00ffffffu;
+            sh.segIdx[m + lane] = e.x >> 24;
+            sh.listIdx[m + lane] = cand;
+          }
+          m += cnt;
+          p = firstIn ? firstNext : p - cnt;
+        }
+        if (lane == 0) {
+          const bool ends = !(p != INVALID_PTR && p < maxDrawn && processed + m < maxProcessed);
+          sh.nStaged = m;
+          sh.walkNext = p;
+          sh.nRuns = 1;
+          sh.runBin[0] = bin | (ends ? RUN_ENDS : 0u);
+          sh.runK0[0] = 0;
+          sh.runK1[0] = m;
+          sh.runOff[0] = processed;
+        }
+      }
+    }
     __syncthreads();
-    const uint32_t q = sh.queueIdx;
-    if (q >= drawnTiles) break;
-    const uint32_t tileIdx = tileList[1u + q];
-    if (tileIdx >= tileCount) { __syncthreads(); continue; }
-    const uint32_t tx = tileIdx % tilesX, ty = tileIdx / tilesX;
-    const TileB tbp = tileBoundsPx(W, H, TS, tx, ty);
-    const uint32_t px = tbp.x0 + lx, py = tbp.y0 + ly;
-    // Pixels of a partial edge tile outside the viewport take no part.
-    const bool inView = px < W && py < H;
-    sh.zbuf[tid] = inView ? loadTex2DClamp(depth, W, H, f2i((float)px), f2i(fsub(size.y, (float)py))) : 0.0f;
-    bool done = !inView;
+    uint32_t nRuns = sh.nRuns;
+    if (nRuns == 0u) break;  // tile mode: no depth bin left
+    const bool fresh = sh.runOff[0] == 0u;  // run 0 starts its bin
+    if (fresh) { running = 0; runningUB = 0; }
+
+    // ---------------- project ----------------
+    {
+      const uint32_t nStaged = sh.nStaged;
+#pragma unroll
+      for (uint32_t w = 0; w < STAGE / 32; w++) sh.pixMask[w][tid] = 0u;
+      for (uint32_t k = tid; k < nStaged; k += NT) {
+        uint32_t r = 0;
+        while (r + 1u < nRuns && sh.runK0[r + 1u] <= k) r++;
+        sh.pairBase[k] = stageSegment<TS>(sh, k, sh.runBin[r] & 0xffu, U, pos, tan, shading, S, P, SP, size,
+                                          tbp.x0, tbp.y0);
+      }
+      __syncthreads();
+      // exclusive prefix of the areas; the round keeps the longest prefix
+      // of segments whose pairs fit
+      if (warp == 0) {
+        uint32_t carry = 0, nSeg = nStaged;
+        for (uint32_t k0 = 0; k0 < nStaged; k0 += 32) {
+          const uint32_t k = k0 + lane;
+          const uint32_t a = k < nStaged ? sh.pairBase[k] : 0u;
+          uint32_t incl = a;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+          }
+          if (k < nStaged) sh.pairBase[k] = carry + incl - a;
+          const uint32_t over = __ballot_sync(0xffffffffu, k < nStaged && carry + incl > PAIRS);
+          if (over && nSeg == nStaged) nSeg = k0 + (uint32_t)(__ffs(over) - 1);
+          carry += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        if (lane == 0) {
+          sh.pairBase[nStaged] = carry;
+          sh.passCount = 0;
+          if (nSeg < nStaged) {  // drop the segments from nSeg on
+            if (tileMode) {
+              uint32_t used;
+              sh.nRuns = buildRuns<TS>(sh, b1, bin, off, nSeg, used);
+            } else {
+              sh.runK1[0] = nSeg;
+              sh.runBin[0] &= ~RUN_ENDS;
+            }
+          }
+          sh.nSeg = nSeg;
+        }
+      }
+      __syncthreads();
+    }
+    uint32_t nSeg = sh.nSeg;
+    nRuns = sh.nRuns;
+    const uint32_t nPairs = sh.pairBase[nSeg];
+
+    // ---------------- A1: edge tests, one thread per pair ----------------
+    {
+      const uint32_t per = divCeil(nPairs, NT);
+      uint32_t p = tid * per;
+      const uint32_t pEnd = min(p + per, nPairs);
+      uint32_t k = 0, rx = 0, ry = 0, bw = 1, bh = 1, bx0 = 0, by0 = 0, myCnt = 0;
+      float eox[4], eoy[4], eex[4], eey[4];
+      auto loadSeg = [&](uint32_t kk) {
+        const uint32_t bx = sh.box[kk];
+        bx0 = bx & 0xffu;
+        by0 = (bx >> 8) & 0xffu;
+        bw = ((bx >> 16) & 0xffu) - bx0 + 1u;
+        bh = (bx >> 24) - by0 + 1u;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          eox[i] = sh.ox[i][kk]; eoy[i] = sh.oy[i][kk]; eex[i] = sh.ex[i][kk]; eey[i] = sh.ey[i][kk];
+        }
+      };
+      if (p < pEnd) {
+        uint32_t lo = 0, hi = nSeg;  // last k with pairBase[k] <= p
+        while (hi - lo > 1u) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if (sh.pairBase[mid] <= p) lo = mid; else hi = mid;
+        }
+        k = lo;
+        loadSeg(k);
+        const uint32_t r = p - sh.pairBase[k];
+        ry = r / bw;
+        rx = r - ry * bw;
+      }
+      for (uint32_t it = 0; it < per; it++) {
+        const bool valid = p < pEnd;
+        bool pass = false;
+        uint32_t pix = 0;
+        if (valid) {
+          const uint32_t qx = bx0 + rx, qy = by0 + ry;
+          pix = qy * TS + qx;
+          if (!((sh.doneMask[pix >> 5] >> (pix & 31u)) & 1u)) {
+            const f2 pf = mk2((float)(tbp.x0 + qx), (float)(tbp.y0 + qy));
+            pass = true;
+#pragma unroll
+            for (int i = 0; i < 4; i++) {  // edgeFunction, swRasterizeHair.wgsl.ts:128-130
+              const float C = fsub(fmul(fsub(pf.x, eox[i]), eey[i]), fmul(fsub(pf.y, eoy[i]), eex[i]));
+              pass = pass && C >= 0.0f;
+            }
+          }
+          sh.pairInfo[p] = PAIR_NONE;
+        }
+        const uint32_t bal = __ballot_sync(0xffffffffu, pass);
+        if (bal) {
+          const uint32_t leader = (uint32_t)(__ffs(bal) - 1);
+          uint32_t base = 0;
+          if (lane == leader) base = atomicAdd(&sh.passCount, (uint32_t)__popc(bal));
+          base = __shfl_sync(0xffffffffu, base, leader);
+          if (pass) sh.frag[base + __popc(bal & ((1u << lane) - 1u))].x = pix | (k << 16);
+        }
+        myCnt += pass ? 1u : 0u;
+        if (valid) {
+          p++;
+          if (++rx == bw) {
+            rx = 0;
+            if (++ry == bh) {  // segment done
+              if (myCnt) atomicAdd(&sh.cntEdge[k], myCnt);
+              myCnt = 0;
+              if (p < pEnd) {
+                while (sh.pairBase[k + 1u] <= p) k++;  // next segment with pairs
+                loadSeg(k);
+                ry = 0;
+              }
+            }
+          }
+        }
+      }
+      if (myCnt) atomicAdd(&sh.cntEdge[k], myCnt);
+    }
+    __syncthreads();
+
+    // ---------------- can a bin fill its pool in this round? ----------------
+    if (warp == 0) {
+      uint32_t mode = MODE_FAST, keep = nRuns, e0 = 0, eLast = 0;
+      for (uint32_t r = 0; r < nRuns; r++) {
+        uint32_t e = 0;
+        for (uint32_t k = sh.runK0[r] + lane; k < sh.runK1[r]; k += 32) e += sh.cntEdge[k];
+        e = __reduce_add_sync(0xffffffffu, e);
+        const uint32_t base = r == 0u ? runningUB : 0u;
+        if (r == 0u) e0 = e;
+        if (base + e > CAP) {
+          if (r == 0u) { mode = MODE_TIGHTEN; keep = 1; } else { keep = r; }
+          break;
+        }
+        eLast = e;
+      }
+      if (independent && (mode == MODE_TIGHTEN || keep < nRuns)) mode = MODE_ABORT;
+      if (lane == 0) {
+        sh.mode = mode;
+        sh.e0 = e0;
+        sh.eLast = eLast;
+        if (keep < nRuns) {  // the round ends where that bin's run starts
+          sh.nRuns = keep;
+          sh.nSeg = sh.runK1[keep - 1u];
+        }
+        sh.roundFrags = 0;
+      }
+    }
+    __syncthreads();
+    if (sh.mode == MODE_ABORT) return false;  // a pool could fill: this group cannot stand alone
+    nRuns = sh.nRuns;
+    nSeg = sh.nSeg;
+    bool exact = false;
+    if (sh.mode == MODE_TIGHTEN) {
+      running += blockSum<NW>(pending, sh.red, lane, warp);
+      pending = 0;
+      runningUB = running;
+      exact = runningUB + sh.e0 > CAP;
+    }
+
+    // ---------------- A2: fragments, one thread per passing pair ----------------
+    {
+      const uint32_t nPass = sh.passCount;
+      for (uint32_t i = tid; i < nPass; i += NT) {
+        const uint32_t e = sh.frag[i].x;
+        const uint32_t pix = e & 0xffffu, k = e >> 16;
+        if (k >= nSeg) continue;  // dropped from the round
+        const uint32_t qx = pix % TS, qy = pix / TS;
+        const f2 pf = mk2((float)(tbp.x0 + qx), (float)(tbp.y0 + qy));
+        QuadConst qc;
+        qc.sm = mk2(sh.qsx[k], sh.qsy[k]);
+        qc.ab = mk2(sh.qax[k], sh.qay[k]);
+        qc.d2 = sh.qd2[k]; qc.lse = sh.qlse[k]; qc.wS = sh.qws[k]; qc.wE = sh.qwe[k];
+        qc.ab2 = mk2(sh.ex[3][k], sh.ey[3][k]);
+        qc.d22 = sh.qd22[k];
+        const f2 w = interpolateHairQuadPre(qc, mk2(sh.ox[3][k], sh.oy[3][k]), pf);
+        const float hd = interpolateHairF32(w, mk4(sh.dp[0][k], sh.dp[1][k], sh.dp[2][k], sh.dp[3][k]));
+        if (!(hd < sh.zbuf[pix])) continue;  // depth test with GL_LESS (skip when >=)
+        const uint4 h = sh.head[sh.shadeBase[k] >> 24];
+        const float td0 = (float)(0xffffffffu - h.x) / F_MAX_U32;  // _getTileDepth
+        const float td1 = (float)h.y / F_MAX_U32;
+        uint32_t slice;
+        const uint2 col = fragmentColour<TS>(sh, k, w, hd, P, SP, L, td0, td1, alphaQuadratic, alphaMul,
+                                             shading, slice);
+        sh.frag[i] = col;
+        const uint32_t bx = sh.box[k];
+        sh.pairInfo[sh.pairBase[k] + (qy - ((bx >> 8) & 0xffu)) * (((bx >> 16) & 0xffu) - (bx & 0xffu) + 1u) +
+                    (qx - (bx & 0xffu))] = i | (slice << 16);
+        atomicOr(&sh.pixMask[k >> 5][pix], 1u << (k & 31u));
+        if (exact) atomicAdd(&sh.cntFrag[k], 1u);
+      }
+    }
+    __syncthreads();
+
+    // ---------------- exact accounting: the segment that fills the pool ----------------
+    if (exact) {
+      if (warp == 0) {  // one run (this bin) in the round
+        uint32_t carry = 0, cut = INVALID_PTR, cutSlots = 0;
+        for (uint32_t k0 = 0; k0 < nSeg; k0 += 32) {
+          const uint32_t k = k0 + lane;
+          const uint32_t c = k < nSeg ? sh.cntFrag[k] : 0u;
+          uint32_t incl = c;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+          }
+          const uint32_t fb = __ballot_sync(0xffffffffu, k < nSeg && running + carry + incl >= CAP);
+          if (fb) {
+            const uint32_t j = (uint32_t)(__ffs(fb) - 1);
+            cut = k0 + j;
+            cutSlots = CAP - (running + carry + __shfl_sync(0xffffffffu, incl - c, j));
+            break;
+          }
+          carry += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        if (lane == 0) {
+          sh.cutSeg = cut;
+          sh.cutSlots = cutSlots;
+          sh.roundFrags = carry;
+          if (cut != INVALID_PTR) {
+            sh.nSeg = cut + 1u;
+            sh.runK1[0] = cut + 1u;
+            sh.runBin[0] |= RUN_ENDS;  // the reference breaks after the filling segment
+            atomicAdd(&counters->finePoolFullBins, 1ull);
+          }
+        }
+      }
+      __syncthreads();
+      const uint32_t cut = sh.cutSeg;
+      if (cut != INVALID_PTR) {  // slots of the filling segment in pixel order
+        const uint32_t base = sh.pairBase[cut], area = sh.pairBase[cut + 1u] - base;
+        const bool has = tid < area && sh.pairInfo[base + tid] != PAIR_NONE;
+        const uint32_t rank = blockExclusive<NW>(has ? 1u : 0u, sh.red, lane, warp);
+        if (has && rank >= sh.cutSlots) sh.pairInfo[base + tid] = PAIR_NONE;
+        __syncthreads();
+      }
+      nSeg = sh.nSeg;
+    }
+
+    // ---------------- B: every pixel blends its fragments in list order ----------------
+    for (uint32_t r = 0; r < nRuns; r++) {
+      const uint32_t rb = sh.runBin[r], k0 = sh.runK0[r], k1 = sh.runK1[r];
+      if (!done && k0 < k1) {
+        for (uint32_t w = k0 >> 5; w <= (k1 - 1u) >> 5; w++) {
+          const uint32_t lo = max(k0, w * 32u) - w * 32u, hi = min(k1, w * 32u + 32u) - w * 32u;
+          uint32_t bits = sh.pixMask[w][tid] & (hi == 32u ? 0xffffffffu : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
+          while (bits) {
+            const uint32_t j = w * 32u + (uint32_t)(__ffs(bits) - 1);
+            bits &= bits - 1u;
+            const uint32_t b = sh.box[j];
+            const uint32_t bx0 = b & 0xffu, by0 = (b >> 8) & 0xffu;
+            const uint32_t info =
+                sh.pairInfo[sh.pairBase[j] + (ly - by0) * (((b >> 16) & 0xffu) - bx0 + 1u) + (lx - bx0)];
+            if (info != PAIR_NONE) {  // not dropped by a full pool
+              blendFragment<MAXL>(acc, info >> 16, sh.frag[info & 0xffffu]);
+              nFrag++;
+              pending++;
+            }
+          }
+        }
+      }
+      if (rb & RUN_ENDS) {
+        // reduceHairSlices (runs for every bin with depth, as in the reference)
+        if (!done) {
+          if (isDbg) {
+            const uint32_t cntAll = f2u(fmul(fin.x, (float)dbgMax)) + nFrag;
+            fin = mk4(sat((float)cntAll / (float)dbgMax), 0.0f, 0.0f, 1.0f);
+          } else {
+#pragma unroll
+            for (int si = 0; si < MAXL; si++) {
+              if ((uint32_t)si < L && fin.w < 0.999f) {
+                const float kk = fsub(1.0f, fin.w);
+                fin.x = fadd(fin.x, fmul(acc[si].x, kk));
+                fin.y = fadd(fin.y, fmul(acc[si].y, kk));
+                fin.z = fadd(fin.z, fmul(acc[si].z, kk));
+                fin.w = fadd(fin.w, fmul(acc[si].w, kk));
+              }
+            }
+            done = fin.w >= 0.999f;  // isPixelDone with ALPHA_CUTOFF
+          }
+        }
+#pragma unroll
+        for (int si = 0; si < MAXL; si++) acc[si] = mk4(0.f, 0.f, 0.f, 0.f);
+        nFrag = 0;
+        pending = 0;
+      }
+    }
+
+    // ---------------- carry the pool state and advance the cursor ----------------
+    const uint32_t lastBin = sh.runBin[nRuns - 1u];
+    const bool lastEnds = (lastBin & RUN_ENDS) != 0u;
+    if (lastEnds) {
+      running = 0;
+      runningUB = 0;
+    } else if (nRuns == 1u) {
+      if (exact) {
+        running += sh.roundFrags;
+        runningUB = running;
+        pending = 0;
+      } else {
+        runningUB += sh.e0;
+      }
+    } else {
+      running = 0;
+      runningUB = sh.eLast;
+    }
+    if (tileMode) {
+      const uint32_t lb = lastBin & 0xffu;
+      if (lastEnds) { bin = lb + 1u; off = 0; }
+      else { off = sh.runOff[nRuns - 1u] + sh.runK1[nRuns - 1u] - sh.runK0[nRuns - 1u]; bin = lb; }
+    } else {
+      if (lastEnds) { bin++; processed = 0; }
+      else {
+        walkPtr = nSeg < sh.nStaged ? sh.listIdx[nSeg] : sh.walkNext;
+        processed += nSeg;
+      }
+    }
     {
       const uint32_t dm = __ballot_sync(0xffffffffu, done);
       if (lane == 0) sh.doneMask[warp] = dm;
     }
-    f4 fin = mk4(0.f, 0.f, 0.f, 0.f);  // rasterizerResult was cleared before the pass
-    if (tid < B) sh.head[tid] = tiles[ty * tilesX * B + tx * B + tid];
-    __syncthreads();
+    // checkAllPixelsInWkgrpDone, :305-327 (also the barrier before the
+    // next round rewrites the staged state)
+    if (__syncthreads_and(done)) break;
+    if (bin >= b1) break;
+  }
+  return true;
+}
 
-    // ---- tile mode: every depth bin's list carries a length hint (padding0,
-    // written by the tiles pass) and the lists are the contiguous runs the
-    // tiles pass writes; otherwise each list is walked ----
-    if (warp == 0) {
-      uint32_t ok = 1, sum = 0;
-      for (uint32_t b0 = 0; b0 < B; b0 += 32) {
-        const uint32_t bb = b0 + lane;
-        uint32_t nb = 0;
-        if (bb < B) {
-          const uint4 h = sh.head[bb];
+// Builds the work list of the fine pass: one item per drawn tile, in the
+// tile list's order (most records first), except that a tile with more
+// records than a CTA's average share is split into groups of whole depth
+// bins, so that no single CTA carries the frame's tail.  Group sizes come
+// from the list-length hints; a tile without valid hints is not split.
+// One CTA.
+__global__ void __launch_bounds__(1024)
+fineScheduleKernel(const uint32_t* __restrict__ tileList, const uint32_t* __restrict__ segCount,
+                   const uint4* __restrict__ tiles, uint32_t T, uint32_t B, uint32_t grid, uint32_t maxDrawn,
+                   uint32_t maxProcessed, uint32_t allowSplit, FineScratch fs,
+                   DeviceCounters* __restrict__ counters) {
+  __shared__ uint32_t warpSums[32];
+  __shared__ uint32_t total;
+  const uint32_t tid = threadIdx.x;
+  const uint32_t drawn = min(tileList[0], T);
+  if (tid == 0) total = 0;
+  __syncthreads();
+  uint32_t mine = 0;
+  for (uint32_t q = tid; q < drawn; q += blockDim.x) {
+    const uint32_t t = tileList[1u + q];
+    if (t < T) mine += segCount[t];
+  }
+  atomicAdd(&total, mine);
+  __syncthreads();
+  const uint32_t thr = max(FINE_SPLIT_MIN, total / max(grid, 1u));
+  uint32_t carryItems = 0, carrySlots = 0;
+  for (uint32_t q0 = 0; q0 < drawn; q0 += blockDim.x) {
+    const uint32_t q = q0 + tid;
+    uint32_t nG = 1, t = T;
+    if (q < drawn) {
+      t = tileList[1u + q];
+      if (allowSplit && t < T && segCount[t] > thr) {  // count the groups of the split
+        uint32_t g = 0, acc = 0;
+        bool ok = true;
+        for (uint32_t b = 0; b < B; b++) {
+          const uint4 h = tiles[(size_t)t * B + b];
+          uint32_t nb = 0;
           if (h.y != 0u && h.z != 0u) {
-            if (h.w != 0u && h.w <= h.z && h.z <= maxDrawn && h.w <= maxProcessed) nb = h.w; else ok = 0;
+            if (h.w != 0u && h.w <= h.z && h.z <= maxDrawn && h.w <= maxProcessed) nb = h.w; else ok = false;
           }
+          if (nb == 0u) continue;
+          if (acc > 0u && acc + nb > thr) { g++; acc = 0; }
+          acc += nb;
         }
-        uint32_t incl = nb;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-          if (lane >= (uint32_t)o) incl += y;
-        }
-        if (bb < B) sh.binOff[bb] = sum + incl - nb;
-        sum += __shfl_sync(0xffffffffu, incl, 31);
-      }
-      ok = __all_sync(0xffffffffu, ok);
-      if (lane == 0) {
-        sh.binOff[B] = sum;
-        sh.total = sum;
-        sh.tileMode = ok;
-        sh.bad = 0;
+        if (acc > 0u) g++;
+        if (ok && g > 1u) nG = g;
       }
     }
+    uint32_t chunkSlots;
+    const uint32_t mySlots = nG > 1u ? nG : 0u;
+    const uint32_t slotEnd = carrySlots + blockExclusiveScan(mySlots, warpSums, chunkSlots) + mySlots;
+    const bool split = nG > 1u && slotEnd <= fs.maxGroups;
+    if (!split) nG = 1;
+    uint32_t chunkItems;
+    const uint32_t itemBase = carryItems + blockExclusiveScan(nG, warpSums, chunkItems);
+    if (q < drawn) {
+      if (split) {
+        const uint32_t slot = slotEnd - nG;
+        fs.arrivals[slot] = 0;
+        atomicAdd(&counters->fineSplitTiles, 1ull);
+        uint32_t g = 0, acc = 0, start = 0;
+        for (uint32_t b = 0; b < B; b++) {
+          const uint4 h = tiles[(size_t)t * B + b];
+          const uint32_t nb = (h.y != 0u && h.z != 0u) ? h.w : 0u;
+          if (nb == 0u) continue;
+          if (acc > 0u && acc + nb > thr) {
+            fs.items[itemBase + g] = make_uint4(q, start | (b << 8) | (g << 16) | (nG << 24), slot, 0u);
+            g++;
+            acc = 0;
+            start = b;
+          }
+          acc += nb;
+        }
+        fs.items[itemBase + g] = make_uint4(q, start | (B << 8) | (g << 16) | (nG << 24), slot, 0u);
+      } else {
+        fs.items[itemBase] = make_uint4(q, 0u | (B << 8) | (1u << 24), 0u, 0u);
+      }
+    }
+    carryItems += chunkItems;
+    carrySlots += chunkSlots;
+  }
+  if (tid == 0) fs.hdr[0] = carryItems;
+}
+
+template <int TS, int MAXL>
+__global__ void __launch_bounds__(TS * TS, TS == 8 ? 6 : TS == 16 ? (MAXL <= 4 ? 3 : 2) : 1)
+fineKernel(const HfbUniforms U, const FineArgs a, const uint32_t* __restrict__ tileList, float* __restrict__ result,
+           FineScratch fs) {
+  using SM = FineSmem<TS>;
+  constexpr uint32_t NT = SM::NT;
+  constexpr uint32_t UNSAFE = 1u << 31;
+  extern __shared__ __align__(16) unsigned char fineSmemRaw[];
+  SM& sh = *reinterpret_cast<SM*>(fineSmemRaw);
+  const uint32_t tid = threadIdx.x;
+  const uint32_t lx = tid % TS, ly = tid / TS;
+  const uint32_t W = f2u(U.viewport.x), H = f2u(U.viewport.y);
+  const uint32_t tilesX = divCeil(W, TS), tileCount = tilesX * divCeil(H, TS);
+  const uint32_t nItems = fs.hdr[0];
+  uint32_t* queue = reinterpret_cast<uint32_t*>(result);  // tileQueueAtomicIdx, getNextTileIdx :294-303
+  float4* res = reinterpret_cast<float4*>(result + 4);
+
+  while (true) {
+    if (tid == 0) sh.queueIdx = atomicAdd(queue, 1u);
     __syncthreads();
-    bool tileMode = sh.tileMode != 0u;
-    if (tileMode) {  // check every link of the contiguous layout
-      const uint32_t total = sh.total;
-      for (uint32_t k = tid; k < total; k += NT) {
-        uint32_t lo = 0, hi = B;  // bin of k: binOff[lo] <= k < binOff[lo + 1]
-        while (hi - lo > 1u) {
-          const uint32_t mid = (lo + hi) >> 1;
-          if (sh.binOff[mid] <= k) lo = mid; else hi = mid;
-        }
-        const uint4 h = sh.head[lo];
-        const uint32_t j = k - sh.binOff[lo];
-        const uint32_t idx = h.z - 1u - j;
-        const uint32_t nxt = __ldg(&segBuf[2u + 2u * idx]);
-        if (nxt != ((j + 1u == h.w) ? INVALID_PTR : idx - 1u)) sh.bad = 1;
-      }
-      __syncthreads();
-      tileMode = sh.bad == 0u;
-    }
-
-    // per-pixel state of the current bin
-    f4 acc[MAXL];
-#pragma unroll
-    for (int si = 0; si < MAXL; si++) acc[si] = mk4(0.f, 0.f, 0.f, 0.f);
-    uint32_t nFrag = 0, pending = 0;
-    // uniform state: cursor and the pool accounting of the bin at the cursor
-    uint32_t bin = 0, off = 0;                     // tile mode: bin, entry of its list
-    uint32_t walkPtr = INVALID_PTR, processed = 0;  // walk mode: list pointer, entries processed
-    uint32_t running = 0, runningUB = 0;            // slots taken (exact / upper bound)
-
+    const uint32_t it = sh.queueIdx;
+    if (it >= nItems) break;
+    const uint4 item = fs.items[it];
+    const uint32_t tileIdx = tileList[1u + item.x];
+    uint32_t b0 = item.y & 0xffu, b1 = (item.y >> 8) & 0xffu;
+    const uint32_t g = (item.y >> 16) & 0xffu, nG = item.y >> 24;
+    if (tileIdx >= tileCount || b1 > a.B || b0 >= b1) { __syncthreads(); continue; }
+    bool split = nG > 1u, write = true;
+    f4 fin;
     while (true) {
-      // ---------------- stage the round ----------------
-      if (tileMode) {
-        if (tid == 0) {
-          uint32_t used;
-          sh.nRuns = buildRuns<TS>(sh, B, bin, off, STAGE, used);
-          sh.nStaged = used;
-        }
-        __syncthreads();
-        const uint32_t nStaged = sh.nStaged, nRuns = sh.nRuns;
-        for (uint32_t k = tid; k < nStaged; k += NT) {
-          uint32_t r = 0;
-          while (r + 1u < nRuns && sh.runK0[r + 1u] <= k) r++;
-          const uint32_t b = sh.runBin[r] & 0xffu;
-          const uint32_t idx = sh.head[b].z - 1u - (sh.runOff[r] + k - sh.runK0[r]);
-          const uint32_t enc = __ldg(&segBuf[1u + 2u * idx]);
-          sh.strand[k] = enc & 0x00ffffffu;
-          sh.segIdx[k] = enc >> 24;
-          sh.listIdx[k] = idx;
-        }
-      } else {
-        while (bin < B && sh.head[bin].y == 0u) bin++;  // bins without depth are skipped
-        if (bin >= B) break;
-        if (processed == 0u) {
-          const uint32_t hz = sh.head[bin].z;
-          walkPtr = hz == 0u ? INVALID_PTR : hz - 1u;
-        }
-        if (warp == 0) {  // speculative contiguous runs, else pointer chasing
-          uint32_t p = walkPtr, m = 0;
-          while (m < STAGE && p != INVALID_PTR && p < maxDrawn && processed + m < maxProcessed) {
-            const uint32_t want = min(min(32u, STAGE - m), maxProcessed - processed - m);
-            const uint32_t cand = p - lane;
-            const bool inRange = lane < want && lane <= p;
-            uint2 e = make_uint2(0u, INVALID_PTR);
-            if (inRange) {
-              e.x = __ldg(&segBuf[1u + 2u * cand]);
-              e.y = __ldg(&segBuf[2u + 2u * cand]);
-            }
-            const bool chain = inRange && e.y == cand - 1u;
-            const uint32_t brk = __ballot_sync(0xffffffffu, !chain);
-            const uint32_t first = brk ? (uint32_t)(__ffs(brk) - 1) : 32u;
-            bool firstIn = false;
-            uint32_t firstNext = 0u;
-            if (first < 32u) {
-              firstIn = __shfl_sync(0xffffffffu, inRange, first);
-              firstNext = __shfl_sync(0xffffffffu, e.y, first);
-            }
-            const uint32_t cnt = firstIn ? first + 1u : first;
-            if (lane < cnt) {
-              sh.strand[m + lane] = e.x & 0x00ffffffu;
-              sh.segIdx[m + lane] = e.x >> 24;
-              sh.listIdx[m + lane] = cand;
-            }
-            m += cnt;
-            p = firstIn ? firstNext : p - cnt;
-          }
-          if (lane == 0) {
-            const bool ends = !(p != INVALID_PTR && p < maxDrawn && processed + m < maxProcessed);
-            sh.nStaged = m;
-            sh.walkNext = p;
-            sh.nRuns = 1;
-            sh.runBin[0] = bin | (ends ? RUN_ENDS : 0u);
-            sh.runK0[0] = 0;
-            sh.runK1[0] = m;
-            sh.runOff[0] = processed;
-          }
-        }
+      const bool ok = fineTile<TS, MAXL>(sh, U, a, tileIdx, b0, b1, split && g > 0u, fin);
+      if (!split) break;
+      // a group of a split tile: publish its composite; the last to arrive merges
+      fs.groups[(size_t)(item.z + g) * NT + tid] = make_float4(fin.x, fin.y, fin.z, fin.w);
+      __threadfence();
+      __syncthreads();
+      if (tid == 0) {
+        if (!ok) atomicOr(&fs.arrivals[item.z], UNSAFE);
+        const uint32_t old = atomicAdd(&fs.arrivals[item.z], 1u);
+        sh.arrive = (old & 0xffffu) + 1u == nG ? ((old & UNSAFE) ? 2u : 1u) : 0u;
+        if (sh.arrive == 2u) atomicAdd(&a.counters->fineSplitRedone, 1ull);
       }
       __syncthreads();
-      uint32_t nRuns = sh.nRuns;
-      if (nRuns == 0u) break;  // tile mode: no depth bin left
-      const bool fresh = sh.runOff[0] == 0u;  // run 0 starts its bin
-      if (fresh) { running = 0; runningUB = 0; }
-
-      // ---------------- project ----------------
-      {
-        const uint32_t nStaged = sh.nStaged;
-#pragma unroll
-        for (uint32_t w = 0; w < STAGE / 32; w++) sh.pixMask[w][tid] = 0u;
-        for (uint32_t k = tid; k < nStaged; k += NT) {
-          uint32_t r = 0;
-          while (r + 1u < nRuns && sh.runK0[r + 1u] <= k) r++;
-          sh.pairBase[k] = stageSegment<TS>(sh, k, sh.runBin[r] & 0xffu, U, pos, tan, shading, S, P, SP, size,
-                                            tbp.x0, tbp.y0);
-        }
-        __syncthreads();
-        // exclusive prefix of the areas; the round keeps the longest prefix
-        // of segments whose pairs fit
-        if (warp == 0) {
-          uint32_t carry = 0, nSeg = nStaged;
-          for (uint32_t k0 = 0; k0 < nStaged; k0 += 32) {
-            const uint32_t k = k0 + lane;
-            const uint32_t a = k < nStaged ? sh.pairBase[k] : 0u;
-            uint32_t incl = a;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-              const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-              if (lane >= (uint32_t)o) incl += y;
-            }
-            if (k < nStaged) sh.pairBase[k] = carry + incl - a;
-            const uint32_t over = __ballot_sync(0xffffffffu, k < nStaged && carry + incl > PAIRS);
-            if (over && nSeg == nStaged) nSeg = k0 + (uint32_t)(__ffs(over) - 1);
-            carry += __shfl_sync(0xffffffffu, incl, 31);
-          }
-          if (lane == 0) {
-            sh.pairBase[nStaged] = carry;
-            sh.passCount = 0;
-            if (nSeg < nStaged) {  // drop the segments from nSeg on
-              if (tileMode) {
-                uint32_t used;
-                sh.nRuns = buildRuns<TS>(sh, B, bin, off, nSeg, used);
-              } else {
-                sh.runK1[0] = nSeg;
-                sh.runBin[0] &= ~RUN_ENDS;
-              }
-            }
-            sh.nSeg = nSeg;
-          }
-        }
-        __syncthreads();
+      const uint32_t m = sh.arrive;
+      if (m == 0u) { write = false; break; }
+      if (m == 2u) {  // a later group could fill a pool: the whole tile in order
+        b0 = 0;
+        b1 = a.B;
+        split = false;
+        continue;
       }
-      uint32_t nSeg = sh.nSeg;
-      nRuns = sh.nRuns;
-      const uint32_t nPairs = sh.pairBase[nSeg];
-
-      // ---------------- A1: edge tests, one thread per pair ----------------
-      {
-        const uint32_t per = divCeil(nPairs, NT);
-        uint32_t p = tid * per;
-        const uint32_t pEnd = min(p + per, nPairs);
-        uint32_t k = 0, rx = 0, ry = 0, bw = 1, bh = 1, bx0 = 0, by0 = 0, myCnt = 0;
-        float eox[4], eoy[4], eex[4], eey[4];
-        auto loadSeg = [&](uint32_t kk) {
-          const uint32_t bx = sh.box[kk];
-          bx0 = bx & 0xffu;
-          by0 = (bx >> 8) & 0xffu;
-          bw = ((bx >> 16) & 0xffu) - bx0 + 1u;
-          bh = (bx >> 24) - by0 + 1u;
-#pragma unroll
-          for (int i = 0; i < 4; i++) {
-            eox[i] = sh.ox[i][kk]; eoy[i] = sh.oy[i][kk]; eex[i] = sh.ex[i][kk]; eey[i] = sh.ey[i][kk];
-          }
-        };
-        if (p < pEnd) {
-          uint32_t lo = 0, hi = nSeg;  // last k with pairBase[k] <= p
-          while (hi - lo > 1u) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (sh.pairBase[mid] <= p) lo = mid; else hi = mid;
-          }
-          k = lo;
-          loadSeg(k);
-          const uint32_t r = p - sh.pairBase[k];
-          ry = r / bw;
-          rx = r - ry * bw;
-        }
-        for (uint32_t it = 0; it < per; it++) {
-          const bool valid = p < pEnd;
-          bool pass = false;
-          uint32_t pix = 0;
-          if (valid) {
-            const uint32_t qx = bx0 + rx, qy = by0 + ry;
-            pix = qy * TS + qx;
-            if (!((sh.doneMask[pix >> 5] >> (pix & 31u)) & 1u)) {
-              const f2 pf = mk2((float)(tbp.x0 + qx), (float)(tbp.y0 + qy));
-              pass = true;
-#pragma unroll
-              for (int i = 0; i < 4; i++) {  // edgeFunction, swRasterizeHair.wgsl.ts:128-130
-                const float C = fsub(fmul(fsub(pf.x, eox[i]), eey[i]), fmul(fsub(pf.y, eoy[i]), eex[i]));
-                pass = pass && C >= 0.0f;
-              }
-            }
-            sh.pairInfo[p] = PAIR_NONE;
-          }
-          const uint32_t bal = __ballot_sync(0xffffffffu, pass);
-          if (bal) {
-            const uint32_t leader = (uint32_t)(__ffs(bal) - 1);
-            uint32_t base = 0;
-            if (lane == leader) base = atomicAdd(&sh.passCount, (uint32_t)__popc(bal));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            if (pass) sh.frag[base + __popc(bal & ((1u << lane) - 1u))].x = pix | (k << 16);
-          }
-          myCnt += pass ? 1u : 0u;
-          if (valid) {
-            p++;
-            if (++rx == bw) {
-              rx = 0;
-              if (++ry == bh) {  // segment done
-                if (myCnt) atomicAdd(&sh.cntEdge[k], myCnt);
-                myCnt = 0;
-                if (p < pEnd) {
-                  while (sh.pairBase[k + 1u] <= p) k++;  // next segment with pairs
-                  loadSeg(k);
-                  ry = 0;
-                }
-              }
-            }
-          }
-        }
-        if (myCnt) atomicAdd(&sh.cntEdge[k], myCnt);
-      }
-      __syncthreads();
-
-      // ---------------- can a bin fill its pool in this round? ----------------
-      if (warp == 0) {
-        uint32_t mode = MODE_FAST, keep = nRuns, e0 = 0, eLast = 0;
-        for (uint32_t r = 0; r < nRuns; r++) {
-          uint32_t e = 0;
-          for (uint32_t k = sh.runK0[r] + lane; k < sh.runK1[r]; k += 32) e += sh.cntEdge[k];
-          e = __reduce_add_sync(0xffffffffu, e);
-          const uint32_t base = r == 0u ? runningUB : 0u;
-          if (r == 0u) e0 = e;
-          if (base + e > CAP) {
-            if (r == 0u) { mode = MODE_TIGHTEN; keep = 1; } else { keep = r; }
-            break;
-          }
-          eLast = e;
-        }
-        if (lane == 0) {
-          sh.mode = mode;
-          sh.e0 = e0;
-          sh.eLast = eLast;
-          if (keep < nRuns) {  // the round ends where that bin's run starts
-            sh.nRuns = keep;
-            sh.nSeg = sh.runK1[keep - 1u];
-          }
-          sh.roundFrags = 0;
+      __threadfence();
+      // front-to-back "over" of the groups' composites, each pixel stopping
+      // where the reference stops (isPixelDone, alpha >= 0.999)
+      const float4 f0 = __ldcg(&fs.groups[(size_t)item.z * NT + tid]);
+      fin = mk4(f0.x, f0.y, f0.z, f0.w);
+      for (uint32_t g2 = 1; g2 < nG; g2++) {
+        const float4 c = __ldcg(&fs.groups[(size_t)(item.z + g2) * NT + tid]);
+        if (fin.w < 0.999f) {
+          const float k = fsub(1.0f, fin.w);
+          fin.x = fadd(fin.x, fmul(c.x, k));
+          fin.y = fadd(fin.y, fmul(c.y, k));
+          fin.z = fadd(fin.z, fmul(c.z, k));
+          fin.w = fadd(fin.w, fmul(c.w, k));
         }
       }
-      __syncthreads();
-      nRuns = sh.nRuns;
-      nSeg = sh.nSeg;
-      bool exact = false;
-      if (sh.mode == MODE_TIGHTEN) {
-        running += blockSum<NW>(pending, sh.red, lane, warp);
-        pending = 0;
-        runningUB = running;
-        exact = runningUB + sh.e0 > CAP;
-      }
-
-      // ---------------- A2: fragments, one thread per passing pair ----------------
-      {
-        const uint32_t nPass = sh.passCount;
-        for (uint32_t i = tid; i < nPass; i += NT) {
-          const uint32_t e = sh.frag[i].x;
-          const uint32_t pix = e & 0xffffu, k = e >> 16;
-          if (k >= nSeg) continue;  // dropped from the round
-          const uint32_t qx = pix % TS, qy = pix / TS;
-          const f2 pf = mk2((float)(tbp.x0 + qx), (float)(tbp.y0 + qy));
-          QuadConst qc;
-          qc.sm = mk2(sh.qsx[k], sh.qsy[k]);
-          qc.ab = mk2(sh.qax[k], sh.qay[k]);
-          qc.d2 = sh.qd2[k]; qc.lse = sh.qlse[k]; qc.wS = sh.qws[k]; qc.wE = sh.qwe[k];
-          qc.ab2 = mk2(sh.ex[3][k], sh.ey[3][k]);
-          qc.d22 = sh.qd22[k];
-          const f2 w = interpolateHairQuadPre(qc, mk2(sh.ox[3][k], sh.oy[3][k]), pf);
-          const float hd = interpolateHairF32(w, mk4(sh.dp[0][k], sh.dp[1][k], sh.dp[2][k], sh.dp[3][k]));
-          if (!(hd < sh.zbuf[pix])) continue;  // depth test with GL_LESS (skip when >=)
-          const uint4 h = sh.head[sh.shadeBase[k] >> 24];
-          const float td0 = (float)(0xffffffffu - h.x) / F_MAX_U32;  // _getTileDepth
-          const float td1 = (float)h.y / F_MAX_U32;
-          uint32_t slice;
-          const uint2 col = fragmentColour<TS>(sh, k, w, hd, P, SP, L, td0, td1, alphaQuadratic, alphaMul,
-                                               shading, slice);
-          sh.frag[i] = col;
-          const uint32_t bx = sh.box[k];
-          sh.pairInfo[sh.pairBase[k] + (qy - ((bx >> 8) & 0xffu)) * (((bx >> 16) & 0xffu) - (bx & 0xffu) + 1u) +
-                      (qx - (bx & 0xffu))] = i | (slice << 16);
-          atomicOr(&sh.pixMask[k >> 5][pix], 1u << (k & 31u));
-          if (exact) atomicAdd(&sh.cntFrag[k], 1u);
-        }
-      }
-      __syncthreads();
-
-      // ---------------- exact accounting: the segment that fills the pool ----------------
-      if (exact) {
-        if (warp == 0) {  // one run (this bin) in the round
-          uint32_t carry = 0, cut = INVALID_PTR, cutSlots = 0;
-          for (uint32_t k0 = 0; k0 < nSeg; k0 += 32) {
-            const uint32_t k = k0 + lane;
-            const uint32_t c = k < nSeg ? sh.cntFrag[k] : 0u;
-            uint32_t incl = c;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-              const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-              if (lane >= (uint32_t)o) incl += y;
-            }
-            const uint32_t fb = __ballot_sync(0xffffffffu, k < nSeg && running + carry + incl >= CAP);
-            if (fb) {
-              const uint32_t j = (uint32_t)(__ffs(fb) - 1);
-              cut = k0 + j;
-              cutSlots = CAP - (running + carry + __shfl_sync(0xffffffffu, incl - c, j));
-              break;
-            }
-            carry += __shfl_sync(0xffffffffu, incl, 31);
-          }
-          if (lane == 0) {
-            sh.cutSeg = cut;
-            sh.cutSlots = cutSlots;
-            sh.roundFrags = carry;
-            if (cut != INVALID_PTR) {
-              sh.nSeg = cut + 1u;
-              sh.runK1[0] = cut + 1u;
-              sh.runBin[0] |= RUN_ENDS;  // the reference breaks after the filling segment
-              atomicAdd(&counters->finePoolFullBins, 1ull);
-            }
-          }
-        }
-        __syncthreads();
-        const uint32_t cut = sh.cutSeg;
-        if (cut != INVALID_PTR) {  // slots of the filling segment in pixel order
-          const uint32_t base = sh.pairBase[cut], area = sh.pairBase[cut + 1u] - base;
-          const bool has = tid < area && sh.pairInfo[base + tid] != PAIR_NONE;
-          const uint32_t rank = blockExclusive<NW>(has ? 1u : 0u, sh.red, lane, warp);
-          if (has && rank >= sh.cutSlots) sh.pairInfo[base + tid] = PAIR_NONE;
-          __syncthreads();
-        }
-        nSeg = sh.nSeg;
-      }
-
-      // ---------------- B: every pixel blends its fragments in list order ----------------
-      for (uint32_t r = 0; r < nRuns; r++) {
-        const uint32_t rb = sh.runBin[r], k0 = sh.runK0[r], k1 = sh.runK1[r];
-        if (!done && k0 < k1) {
-          for (uint32_t w = k0 >> 5; w <= (k1 - 1u) >> 5; w++) {
-            const uint32_t lo = max(k0, w * 32u) - w * 32u, hi = min(k1, w * 32u + 32u) - w * 32u;
-            uint32_t bits = sh.pixMask[w][tid] & (hi == 32u ? 0xffffffffu : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
-            while (bits) {
-              const uint32_t j = w * 32u + (uint32_t)(__ffs(bits) - 1);
-              bits &= bits - 1u;
-              const uint32_t b = sh.box[j];
-              const uint32_t bx0 = b & 0xffu, by0 = (b >> 8) & 0xffu;
-              const uint32_t info =
-                  sh.pairInfo[sh.pairBase[j] + (ly - by0) * (((b >> 16) & 0xffu) - bx0 + 1u) + (lx - bx0)];
-              if (info != PAIR_NONE) {  // not dropped by a full pool
-                blendFragment<MAXL>(acc, info >> 16, sh.frag[info & 0xffffu]);
-                nFrag++;
-                pending++;
-              }
-            }
-          }
-        }
-        if (rb & RUN_ENDS) {
-          // reduceHairSlices (runs for every bin with depth, as in the reference)
-          if (!done) {
-            if (isDbg) {
-              const uint32_t cntAll = f2u(fmul(fin.x, (float)dbgMax)) + nFrag;
-              fin = mk4(sat((float)cntAll / (float)dbgMax), 0.0f, 0.0f, 1.0f);
-            } else {
-#pragma unroll
-              for (int si = 0; si < MAXL; si++) {
-                if ((uint32_t)si < L && fin.w < 0.999f) {
-                  const float kk = fsub(1.0f, fin.w);
-                  fin.x = fadd(fin.x, fmul(acc[si].x, kk));
-                  fin.y = fadd(fin.y, fmul(acc[si].y, kk));
-                  fin.z = fadd(fin.z, fmul(acc[si].z, kk));
-                  fin.w = fadd(fin.w, fmul(acc[si].w, kk));
-                }
-              }
-              done = fin.w >= 0.999f;  // isPixelDone with ALPHA_CUTOFF
-            }
-          }
-#pragma unroll
-          for (int si = 0; si < MAXL; si++) acc[si] = mk4(0.f, 0.f, 0.f, 0.f);
-          nFrag = 0;
-          pending = 0;
-        }
-      }
-
-      // ---------------- carry the pool state and advance the cursor ----------------
-      const uint32_t lastBin = sh.runBin[nRuns - 1u];
-      const bool lastEnds = (lastBin & RUN_ENDS) != 0u;
-      if (lastEnds) {
-        running = 0;
-        runningUB = 0;
-      } else if (nRuns == 1u) {
-        if (exact) {
-          running += sh.roundFrags;
-          runningUB = running;
-          pending = 0;
-        } else {
-          runningUB += sh.e0;
-        }
-      } else {
-        running = 0;
-        runningUB = sh.eLast;
-      }
-      if (tileMode) {
-        const uint32_t lb = lastBin & 0xffu;
-        if (lastEnds) { bin = lb + 1u; off = 0; }
-        else { off = sh.runOff[nRuns - 1u] + sh.runK1[nRuns - 1u] - sh.runK0[nRuns - 1u]; bin = lb; }
-      } else {
-        if (lastEnds) { bin++; processed = 0; }
-        else {
-          walkPtr = nSeg < sh.nStaged ? sh.listIdx[nSeg] : sh.walkNext;
-          processed += nSeg;
-        }
-      }
-      {
-        const uint32_t dm = __ballot_sync(0xffffffffu, done);
-        if (lane == 0) sh.doneMask[warp] = dm;
-      }
-      // checkAllPixelsInWkgrpDone, :305-327 (also the barrier before the
-      // next round rewrites the staged state)
-      if (__syncthreads_and(done)) break;
-      if (bin >= B) break;
+      break;
     }
-    if (inView) res[(size_t)py * W + px] = make_float4(fin.x, fin.y, fin.z, fin.w);
-    __syncthreads();  // the tile's shared state is rewritten for the next tile
+    const uint32_t tx = tileIdx % tilesX, ty = tileIdx / tilesX;
+    const TileB tbp = tileBoundsPx(W, H, TS, tx, ty);
+    const uint32_t px = tbp.x0 + lx, py = tbp.y0 + ly;
+    if (write && px < W && py < H) res[(size_t)py * W + px] = make_float4(fin.x, fin.y, fin.z, fin.w);
+    __syncthreads();  // the tile's shared state is rewritten for the next item
   }
 }
 
@@ -1264,14 +1429,33 @@ cudaError_t launchFineT(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, c
     if (e != cudaSuccess) return e;
     if (perSM < 1) return cudaErrorInvalidConfiguration;
   }
-  uint32_t grid = cfg.processorCount ? cfg.processorCount : (uint32_t)(perSM * c->smCount);
-  uint32_t CAP = cfg.avgFragmentsPerSlice * cfg.slicesPerPixel * cfg.tileSize * cfg.tileSize;
-  fineKernel<TS, MAXL><<<grid, TS * TS, SMEM, c->stream>>>(
-      u, h.strandsCount, h.pointsPerStrand, cfg.tileDepthBins, cfg.slicesPerPixel, cfg.shadingPoints, CAP,
-      cfg.alphaQuadratic, cfg.alphaMultiplier, (const float4*)pos, (const float4*)tan, (const float4*)shading,
-      depth, (const uint4*)rb.tiles, rb.tileSegments, rb.tileList, rb.rasterizerResult,
-      (DeviceCounters*)c->dCounters);
-  c->launches += 1;
+  const uint32_t grid = cfg.processorCount ? cfg.processorCount : (uint32_t)(perSM * c->smCount);
+  const uint32_t T = divCeil(rb.width, TS) * divCeil(rb.height, TS);
+  const uint32_t dispMode = u.displayMode & 0xffu;
+  const bool dbg = dispMode == 4u && ((u.displayMode >> 8) & 0xffffu) != 0u;
+  FineScratch fs = fineScratchLayout(rb.scratch, cfg, rb.width, rb.height);
+  fineScheduleKernel<<<1, 1024, 0, c->stream>>>(rb.tileList, rb.segmentCountPerTile, (const uint4*)rb.tiles, T,
+                                                cfg.tileDepthBins, grid, rb.maxDrawnSegments,
+                                                h.strandsCount * h.pointsPerStrand, dbg ? 0u : 1u, fs,
+                                                (DeviceCounters*)c->dCounters);
+  FineArgs a;
+  a.S = h.strandsCount;
+  a.P = h.pointsPerStrand;
+  a.B = cfg.tileDepthBins;
+  a.L = cfg.slicesPerPixel;
+  a.SP = cfg.shadingPoints;
+  a.CAP = cfg.avgFragmentsPerSlice * cfg.slicesPerPixel * cfg.tileSize * cfg.tileSize;
+  a.alphaQuadratic = cfg.alphaQuadratic;
+  a.alphaMul = cfg.alphaMultiplier;
+  a.pos = (const float4*)pos;
+  a.tan = (const float4*)tan;
+  a.shading = (const float4*)shading;
+  a.depth = depth;
+  a.tiles = (const uint4*)rb.tiles;
+  a.segBuf = rb.tileSegments;
+  a.counters = (DeviceCounters*)c->dCounters;
+  fineKernel<TS, MAXL><<<grid, TS * TS, SMEM, c->stream>>>(u, a, rb.tileList, rb.rasterizerResult, fs);
+  c->launches += 2;
   return cudaGetLastError();
 }
 

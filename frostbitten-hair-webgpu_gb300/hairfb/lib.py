@@ -44,7 +44,8 @@ class HfbRasterBuffers(ctypes.Structure):
 class HfbCounters(ctypes.Structure):
     _fields_ = [("tileRecords", ctypes.c_uint64), ("tileRecordsDropped", ctypes.c_uint64),
                 ("finePoolFullBins", ctypes.c_uint64), ("waitTimeouts", ctypes.c_uint64),
-                ("launches", ctypes.c_uint64), ("reserved", ctypes.c_uint64 * 3)]
+                ("launches", ctypes.c_uint64), ("fineSplitTiles", ctypes.c_uint64),
+                ("fineSplitRedone", ctypes.c_uint64), ("reserved", ctypes.c_uint64 * 1)]
 
 
 assert ctypes.sizeof(HfbHairData) == 32

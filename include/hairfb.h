@@ -167,7 +167,9 @@ typedef struct HfbCounters {
   uint64_t finePoolFullBins;   /* tile depth bins whose fragment pool filled (fine pass break) */
   uint64_t waitTimeouts;       /* bounded device waits that gave up */
   uint64_t launches;           /* kernels launched by the library */
-  uint64_t reserved[3];
+  uint64_t fineSplitTiles;     /* fine pass: tiles split into groups of depth bins across CTAs */
+  uint64_t fineSplitRedone;    /* fine pass: split tiles redone in order (a later group could fill a pool) */
+  uint64_t reserved[1];
 } HfbCounters;
 
 typedef struct HfbCtx HfbCtx;

@@ -340,6 +340,48 @@ def test_fine_pass_pool_capacity(oracle):
     assert err.max() <= 1.0 / 255.0, f"max pixel error {err.max():.4g}"
 
 
+def _fine_vs_oracle(oracle, inst):
+    fr = frame_of(inst)
+    ctx, hair, rb, d = _raster_gpu(inst, fr)
+    shade = _shading_input(inst)
+    hair.shading.copy_(torch.as_tensor(shade))
+    HairFinePass(ctx).cmd_rasterize_slices_hair(fr.uniforms, hair, d, rb)
+    ctx.sync()
+    hb = inst.hair
+    ot, osg, oc = oracle.tiles_pass(inst.cfg, fr.uniforms, hb.hair_data, hb.asset.positions, hb.tangents,
+                                    inst.scene_depth, hb.asset.strands, inst.width, inst.height, fr.max_drawn)
+    ob, otl = oracle.tile_sort(inst.cfg, inst.width, inst.height, oc)
+    ores = oracle.fine_pass(inst.cfg, fr.uniforms, hb.hair_data, hb.asset.positions, hb.tangents, shade,
+                            inst.scene_depth, ot, osg, otl, inst.width, inst.height)
+    g = rb.read_result()[4:].reshape(-1, 4)
+    o = ores[4:].reshape(-1, 4)
+    return ctx.counters(), g, o
+
+
+def test_fine_pass_split_tiles(oracle):
+    """Dense tiles (far more records than a CTA's share) are split into
+    groups of depth bins on several CTAs and merged front to back."""
+    inst = small_instance(strands=6000, points=32, width=320, height=240, depth_bins=16, slices=4)
+    cnt, g, o = _fine_vs_oracle(oracle, inst)
+    assert cnt["fineSplitTiles"] > 0, "no tile was split: the test does not test"
+    assert cnt["fineSplitRedone"] == 0
+    err = np.abs(g - o)
+    assert err.max() <= 1.0 / 255.0, f"max pixel error {err.max():.4g} (> 1/255)"
+    assert np.array_equal(g[:, 3] > 0, o[:, 3] > 0), "coverage differs"
+
+
+def test_fine_pass_split_tiles_with_full_pools(oracle):
+    """A split tile whose later group could fill a fragment pool is redone in
+    order by one CTA, so the pool's cut stays the reference's."""
+    inst = small_instance(strands=6000, points=32, width=320, height=240, depth_bins=4, slices=2)
+    inst.cfg.avg_fragments_per_slice = 1  # 1 * 2 * 256 = 512 fragments per bin
+    cnt, g, o = _fine_vs_oracle(oracle, inst)
+    assert cnt["fineSplitTiles"] > 0 and cnt["fineSplitRedone"] > 0, cnt
+    assert cnt["finePoolFullBins"] > 0, cnt
+    err = np.abs(g - o)
+    assert err.max() <= 1.0 / 255.0, f"max pixel error {err.max():.4g} (> 1/255)"
+
+
 def test_fine_pass_reads_arbitrary_list_order(oracle):
     """The fine pass walks whatever list it is given: feed it the oracle's
     LIFO lists (not the tiles pass's contiguous layout)."""
