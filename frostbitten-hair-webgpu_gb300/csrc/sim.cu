@@ -132,94 +132,131 @@ __global__ void gridPreSimKernel(const HfbSimUniforms u, uint32_t G, const int4*
 // ---------------------------------------------------------------------------
 // HairSimIntegrationPass.main, hairSimIntegrationPass.wgsl.ts:79-273
 //
-// One thread per strand for the Gauss-Seidel constraint chains (length and
-// local shape must stay sequential along the strand).  The strand points
-// live in shared memory laid out [point][strand] (conflict-free).  The
-// Verlet step and the write-back run point-parallel over the whole block so
-// the position buffers are read and written fully coalesced.
+// A block holds NB strands in shared memory, laid out [strand][point + 1]:
+// one thread per strand walks the Gauss-Seidel chains (length and local
+// shape must stay sequential along the strand, as in the reference), and
+// the whole block runs the per-point phases (Verlet and forces, global
+// shape, sphere and SDF collisions) and the coalesced loads and stores.
+// The padding makes both access patterns conflict-free.  Everything the
+// chains need from the initial pose (segment lengths, the triangle-bending
+// constants, the initial tangents) is staged beside the points, so a chain
+// step touches shared memory only.
 // ---------------------------------------------------------------------------
-constexpr int SIM_STRANDS_PER_BLOCK = 64;
+constexpr uint32_t SIM_THREADS = 256;
 
-__global__ void __launch_bounds__(SIM_STRANDS_PER_BLOCK)
+// Strands per block for P points per strand: one chain warp per block for
+// P <= 32, fewer strands for longer strands (shared memory ~38 KB).
+__host__ __device__ inline uint32_t simStrandsPerBlock(uint32_t P) {
+  return P <= 32u ? 32u : max(8u, 1024u / P);
+}
+__host__ __device__ inline size_t simSmemBytes(uint32_t P) {
+  return (size_t)simStrandsPerBlock(P) * (P + 1u) * (2u * sizeof(float4) + sizeof(float));
+}
+
+// Verlet step of one point with the grid forces (:125-162, integration.wgsl.ts:8-28)
+__device__ __forceinline__ float4 verletPoint(const HfbSimUniforms& u, uint32_t G, f3 gmin, f3 gmax,
+                                              uint32_t strand, f4 posNow, f4 posPrev,
+                                              const int4* __restrict__ dv, const float4* __restrict__ gw) {
+  f3 force = mk3(0.0f, -u.gravity, 0.0f);
+  const f3 pn = xyz(posNow);
+  // _getGridDensityGradAndWind + _getGridDensityVelocity (same cell, two grids)
+  GridCo co = gridCell(G, gmin, gmax, pn);
+  f3 grad = mk3(0.f, 0.f, 0.f), vel = mk3(0.f, 0.f, 0.f);
+  float windStr = 0.0f, dens = 0.0f;
+  for (uint32_t z = co.mn[2]; z <= co.mx[2]; z++)
+    for (uint32_t y = co.mn[1]; y <= co.mx[1]; y++)
+      for (uint32_t x = co.mn[0]; x <= co.mx[0]; x++) {
+        f3 w = cellWeights(x, y, z, co.p);
+        float wl = len3(w);
+        uint32_t idx = gridIdx(G, x, y, z);
+        float4 a = __ldg(&gw[idx]);
+        grad = add3(grad, mul3(w, mk3(a.x, a.y, a.z)));
+        windStr = fadd(windStr, fmul(wl, a.w));
+        int4 b = __ldg(&dv[idx]);
+        vel = add3(vel, mul3(w, mk3(gridDecode(b.x), gridDecode(b.y), gridDecode(b.z))));
+        dens = fadd(dens, fmul(wl, gridDecode(b.w)));
+      }
+  float timer = fadd(fmul((float)u.frameIdx, 0.73f), fmul(u.windPhaseOffset, (float)strand));
+  float windJitter = fractf(fmul(timer, u.windStrengthFrequency));
+  float jitterDelta = mixf(fmul(-0.5f, u.windStrengthJitter), fmul(0.5f, u.windStrengthJitter), windJitter);
+  float jitterStr = fadd(1.0f, jitterDelta);
+  float windCellStr = sat(mixf(u.windStrengthLull, 1.0f, windStr));
+  force = add3(force, mul3s(mk3(u.wind.x, u.wind.y, u.wind.z),
+                            fabsf(fmul(fmul(u.wind.w, jitterStr), windCellStr))));
+  force = add3(force, mul3s(grad, u.volumePreservation));
+  f3 gridDisp = dens > 0.0f ? div3s(vel, dens) : mk3(0.f, 0.f, 0.f);
+  float dt = u.deltaTime;
+  f3 pd = sub3(pn, xyz(posPrev));
+  f3 fpd = mix3(pd, gridDisp, u.friction);
+  f3 nxt = add3(add3(pn, fpd), mul3s(mul3s(force, dt), dt));
+  f3 r = mix3(xyz(posPrev), nxt, posNow.w);
+  return make_float4(r.x, r.y, r.z, posNow.w);
+}
+
+__global__ void __launch_bounds__(SIM_THREADS)
 simIntegrateKernel(const HfbSimUniforms u, uint32_t S, uint32_t P, uint32_t G,
                    float4* __restrict__ prev, const float4* __restrict__ now,
                    const float4* __restrict__ initial, const float* __restrict__ segLen,
                    const int4* __restrict__ dv, const float4* __restrict__ gw,
                    const float* __restrict__ sdf, uint32_t D) {
-  extern __shared__ float4 wk[];  // [P][SIM_STRANDS_PER_BLOCK]
-  const uint32_t NB = SIM_STRANDS_PER_BLOCK;
+  extern __shared__ float4 simSmem[];
+  const uint32_t NB = simStrandsPerBlock(P), R = P + 1u;  // row stride (padded)
+  float4* wk = simSmem;                                   // [NB][R] positions
+  float4* lc = wk + NB * R;  // [NB][R] triangle-bending constants (h0, w0, w1, w2) of the triplet at j,
+                             // or the initial tangent into j for the points matchInitialTangent moves
+  float* sl = reinterpret_cast<float*>(lc + NB * R);  // [NB][R] segment lengths
+  const uint32_t tid = threadIdx.x;
   const uint32_t s0 = blockIdx.x * NB;
   const uint32_t nStr = min(NB, S - s0);
   const uint32_t nPts = nStr * P;
   const f3 gmin = gridMin(u), gmax = gridMax(u);
+  // first point matchInitialTangent moves: the triplet loop ends at P - 3
+  const uint32_t jTan = P >= 3u ? P - 3u : 0u;
 
-  // --- Verlet + forces, point-parallel (:125-162) ---
-  for (uint32_t i = threadIdx.x; i < nPts; i += blockDim.x) {
-    uint32_t ls = i / P, pt = i - ls * P;
-    uint32_t strand = s0 + ls;
-    size_t gi = (size_t)s0 * P + i;
-    f4 posNow = ld4(__ldg(&now[gi]));
-    if (pt == 0) {
-      wk[pt * NB + ls] = make_float4(posNow.x, posNow.y, posNow.z, posNow.w);
-      continue;
+  // --- Verlet + forces and the chain constants, point-parallel ---
+  for (uint32_t i = tid; i < nPts; i += SIM_THREADS) {
+    const uint32_t ls = i / P, pt = i - ls * P;
+    const size_t gi = (size_t)s0 * P + i;
+    const f4 posNow = ld4(__ldg(&now[gi]));
+    wk[ls * R + pt] = pt == 0u ? make_float4(posNow.x, posNow.y, posNow.z, posNow.w)
+                               : verletPoint(u, G, gmin, gmax, s0 + ls, posNow, ld4(prev[gi]), dv, gw);
+    sl[ls * R + pt] = __ldg(&segLen[gi]);
+    const float4 i0 = __ldg(&initial[gi]);
+    float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (pt + 3u < P) {  // applyConstraint_localShape constants (constraints.wgsl.ts:54-99)
+      const float4 i1 = __ldg(&initial[gi + 1u]), i2 = __ldg(&initial[gi + 2u]);
+      f3 cI = div3s(add3(add3(mk3(i0.x, i0.y, i0.z), mk3(i1.x, i1.y, i1.z)), mk3(i2.x, i2.y, i2.z)), 3.0f);
+      const float h0 = len3(sub3(cI, mk3(i1.x, i1.y, i1.z)));
+      const float wT = fadd(fadd(i0.w, fmul(2.0f, i1.w)), i2.w);
+      c = make_float4(h0, fmul(i0.w / wT, 2.0f), fmul(i1.w / wT, -4.0f), fmul(i2.w / wT, 2.0f));
+    } else if (pt >= jTan && pt >= 1u) {  // applyConstraint_matchInitialTangent (:100-120)
+      const float4 im = __ldg(&initial[gi - 1u]);
+      c = make_float4(fsub(i0.x, im.x), fsub(i0.y, im.y), fsub(i0.z, im.z), 0.0f);
     }
-    f4 posPrev = ld4(prev[gi]);
-    f3 force = mk3(0.0f, -u.gravity, 0.0f);
-    f3 pn = xyz(posNow);
-    // _getGridDensityGradAndWind + _getGridDensityVelocity (same cell, two grids)
-    GridCo co = gridCell(G, gmin, gmax, pn);
-    f3 grad = mk3(0.f, 0.f, 0.f), vel = mk3(0.f, 0.f, 0.f);
-    float windStr = 0.0f, dens = 0.0f;
-    for (uint32_t z = co.mn[2]; z <= co.mx[2]; z++)
-      for (uint32_t y = co.mn[1]; y <= co.mx[1]; y++)
-        for (uint32_t x = co.mn[0]; x <= co.mx[0]; x++) {
-          f3 w = cellWeights(x, y, z, co.p);
-          float wl = len3(w);
-          uint32_t idx = gridIdx(G, x, y, z);
-          float4 a = __ldg(&gw[idx]);
-          grad = add3(grad, mul3(w, mk3(a.x, a.y, a.z)));
-          windStr = fadd(windStr, fmul(wl, a.w));
-          int4 b = __ldg(&dv[idx]);
-          vel = add3(vel, mul3(w, mk3(gridDecode(b.x), gridDecode(b.y), gridDecode(b.z))));
-          dens = fadd(dens, fmul(wl, gridDecode(b.w)));
-        }
-    float timer = fadd(fmul((float)u.frameIdx, 0.73f), fmul(u.windPhaseOffset, (float)strand));
-    float windJitter = fractf(fmul(timer, u.windStrengthFrequency));
-    float jitterDelta = mixf(fmul(-0.5f, u.windStrengthJitter), fmul(0.5f, u.windStrengthJitter), windJitter);
-    float jitterStr = fadd(1.0f, jitterDelta);
-    float windCellStr = sat(mixf(u.windStrengthLull, 1.0f, windStr));
-    force = add3(force, mul3s(mk3(u.wind.x, u.wind.y, u.wind.z),
-                              fabsf(fmul(fmul(u.wind.w, jitterStr), windCellStr))));
-    force = add3(force, mul3s(grad, u.volumePreservation));
-    f3 gridDisp = dens > 0.0f ? div3s(vel, dens) : mk3(0.f, 0.f, 0.f);
-    // verletIntegration, integration.wgsl.ts:8-28
-    float dt = u.deltaTime;
-    f3 pd = sub3(pn, xyz(posPrev));
-    f3 fpd = mix3(pd, gridDisp, u.friction);
-    f3 nxt = add3(add3(pn, fpd), mul3s(mul3s(force, dt), dt));
-    f3 r = mix3(xyz(posPrev), nxt, posNow.w);
-    wk[pt * NB + ls] = make_float4(r.x, r.y, r.z, posNow.w);
+    lc[ls * R + pt] = c;
   }
   __syncthreads();
 
-  const uint32_t ls = threadIdx.x;
-  if (ls < nStr) {
-    const uint32_t strand = s0 + ls;
-    const size_t base = (size_t)strand * P;
-    const uint32_t iters = u.constraintIterations;
-    const f3 smin = mk3(u.sdf.boundsMin.x, u.sdf.boundsMin.y, u.sdf.boundsMin.z);
-    const f3 smax = mk3(u.sdf.boundsMax.x, u.sdf.boundsMax.y, u.sdf.boundsMax.z);
-    const float sdfOffset = u.sdf.boundsMax.w;
-    const f4 sph = mk4(u.collisionSphere.x, u.collisionSphere.y, u.collisionSphere.z, u.collisionSphere.w);
-#define WK(j) wk[(j) * NB + ls]
-    for (uint32_t it = 0; it < iters; it++) {
-      // length constraint (Gauss-Seidel), :176-190, constraints.wgsl.ts:5-28
-      const float kLen = u.stiffnessLengthConstr;
-      float4 a = WK(0);
+  const uint32_t iters = u.constraintIterations;
+  const f3 smin = mk3(u.sdf.boundsMin.x, u.sdf.boundsMin.y, u.sdf.boundsMin.z);
+  const f3 smax = mk3(u.sdf.boundsMax.x, u.sdf.boundsMax.y, u.sdf.boundsMax.z);
+  const float sdfOffset = u.sdf.boundsMax.w;
+  const f4 sph = mk4(u.collisionSphere.x, u.collisionSphere.y, u.collisionSphere.z, u.collisionSphere.w);
+  const float kLen = u.stiffnessLengthConstr;
+  const float kGlob = u.stiffnessGlobalConstr / (float)iters;
+  const float kLoc = u.stiffnessLocalConstr / (float)iters;
+  const float kColl = u.stiffnessCollisions / (float)iters;
+  const float kSdf = u.stiffnessSDF / (float)iters;
+  for (uint32_t it = 0; it < iters; it++) {
+    // length constraint (Gauss-Seidel), :176-190, constraints.wgsl.ts:5-28
+    if (tid < nStr) {
+      float4* w = wk + tid * R;
+      const float* L = sl + tid * R;
+      float4 a = w[0];
       for (uint32_t j = 0; j + 1u < P; j++) {
-        float4 b = WK(j + 1u);
-        float expected = __ldg(&segLen[base + j]);
-        float w0 = a.w, w1 = b.w;
+        float4 b = w[j + 1u];
+        const float expected = L[j];
+        const float w0 = a.w, w1 = b.w;
         f3 tng = mk3(fsub(b.x, a.x), fsub(b.y, a.y), fsub(b.z, a.z));
         float actual = len3(tng);
         float corr = fsub(1.0f, expected / actual);
@@ -227,266 +264,80 @@ simIntegrateKernel(const HfbSimUniforms u, uint32_t S, uint32_t P, uint32_t G,
         f3 delta = mul3s(tng, df);
         a.x = fadd(a.x, fmul(delta.x, w0)); a.y = fadd(a.y, fmul(delta.y, w0)); a.z = fadd(a.z, fmul(delta.z, w0));
         b.x = fsub(b.x, fmul(w1, delta.x)); b.y = fsub(b.y, fmul(w1, delta.y)); b.z = fsub(b.z, fmul(w1, delta.z));
-        WK(j) = a;
-        WK(j + 1u) = b;
+        w[j] = a;
         a = b;
       }
-      // global shape, :193-206, constraints.wgsl.ts:31-49
-      const float kGlob = u.stiffnessGlobalConstr / (float)iters;
-      for (uint32_t j = 1; j < P; j++) {
-        float x = (float)j / (float)(P - 1u);
-        float att = fsub(1.0f, sat(fsub(x, u.globalConstrExtent) / u.globalConstrFade));
-        float4 pi = __ldg(&initial[base + j]);
-        float k = fmul(kGlob, att);
-        float4 p = WK(j);
-        f3 dvv = mk3(fsub(pi.x, p.x), fsub(pi.y, p.y), fsub(pi.z, p.z));
-        f3 d = mul3s(mul3s(dvv, p.w), k);
-        p.x = fadd(p.x, d.x); p.y = fadd(p.y, d.y); p.z = fadd(p.z, d.z);
-        WK(j) = p;
-      }
-      // local shape (triangle bending, Gauss-Seidel), :209-232, constraints.wgsl.ts:54-120
-      const float kLoc = u.stiffnessLocalConstr / (float)iters;
-      uint32_t jj = 0;
-      for (; jj + 3u < P; jj++) {
-        float4 i0 = __ldg(&initial[base + jj]), i1 = __ldg(&initial[base + jj + 1u]),
-               i2 = __ldg(&initial[base + jj + 2u]);
-        f3 cI = div3s(add3(add3(mk3(i0.x, i0.y, i0.z), mk3(i1.x, i1.y, i1.z)), mk3(i2.x, i2.y, i2.z)), 3.0f);
-        float h0 = len3(sub3(cI, mk3(i1.x, i1.y, i1.z)));
-        float4 p0 = WK(jj), p1 = WK(jj + 1u), p2 = WK(jj + 2u);
-        f3 c = div3s(add3(add3(mk3(p0.x, p0.y, p0.z), mk3(p1.x, p1.y, p1.z)), mk3(p2.x, p2.y, p2.z)), 3.0f);
-        f3 hv = sub3(mk3(p1.x, p1.y, p1.z), c);
-        float h = len3(hv);
-        float wT = fadd(fadd(i0.w, fmul(2.0f, i1.w)), i2.w);
-        float w0 = fmul(i0.w / wT, 2.0f), w1 = fmul(i1.w / wT, -4.0f), w2 = fmul(i2.w / wT, 2.0f);
-        f3 delta = mul3s(hv, fsub(1.0f, h0 / h));
-        f3 d0 = mul3s(delta, fmul(kLoc, w0)), d1 = mul3s(delta, fmul(kLoc, w1)), d2 = mul3s(delta, fmul(kLoc, w2));
-        p0.x = fadd(p0.x, d0.x); p0.y = fadd(p0.y, d0.y); p0.z = fadd(p0.z, d0.z);
-        p1.x = fadd(p1.x, d1.x); p1.y = fadd(p1.y, d1.y); p1.z = fadd(p1.z, d1.z);
-        p2.x = fadd(p2.x, d2.x); p2.y = fadd(p2.y, d2.y); p2.z = fadd(p2.z, d2.z);
-        WK(jj) = p0;
-        WK(jj + 1u) = p1;
-        WK(jj + 2u) = p2;
-      }
-      for (; jj < P; jj++) {  // applyConstraint_matchInitialTangent
-        float4 i0 = __ldg(&initial[base + jj - 1u]), i1 = __ldg(&initial[base + jj]);
-        f3 tI = mk3(fsub(i1.x, i0.x), fsub(i1.y, i0.y), fsub(i1.z, i0.z));
-        float4 p0 = WK(jj - 1u), p1 = WK(jj);
-        f3 proj = add3(mk3(p0.x, p0.y, p0.z), tI);
-        f3 delta = sub3(proj, mk3(p1.x, p1.y, p1.z));
-        f3 d = mul3s(delta, fmul(kLoc, p1.w));
-        p1.x = fadd(p1.x, d.x); p1.y = fadd(p1.y, d.y); p1.z = fadd(p1.z, d.z);
-        WK(jj) = p1;
-      }
-      // collisions, :236-261, collisions.wgsl.ts:4-61
-      const float kColl = u.stiffnessCollisions / (float)iters;
-      const float kSdf = u.stiffnessSDF / (float)iters;
-      for (uint32_t j = 1; j < P; j++) {
-        float4 pos = WK(j);
-        {
-          f3 v = mk3(fsub(pos.x, sph.x), fsub(pos.y, sph.y), fsub(pos.z, sph.z));
-          float dist = fsub(len3(v), sph.w);
-          float dts = fmaxf(0.0f, -dist);
-          f3 d = mul3s(mul3s(norm3(v), dts), kColl);
-          pos.x = fadd(pos.x, d.x); pos.y = fadd(pos.y, d.y); pos.z = fadd(pos.z, d.z);
-        }
-        if (j > 2u) {
-          f3 p = mk3(pos.x, pos.y, pos.z);
-          float d = sampleSDF(sdf, D, smin, smax, p);
-          float dOff = fadd(d, sdfOffset);
-          if (!(dOff >= 0.0f)) {
-            const float o = SDF_GRAD_OFFSET;
-            f3 cd;
-            cd.x = sampleSDF(sdf, D, smin, smax, add3(p, mk3(fmul(o, 1.0f), fmul(o, 0.0f), fmul(o, 0.0f))));
-            cd.y = sampleSDF(sdf, D, smin, smax, add3(p, mk3(fmul(o, 0.0f), fmul(o, 1.0f), fmul(o, 0.0f))));
-            cd.z = sampleSDF(sdf, D, smin, smax, add3(p, mk3(fmul(o, 0.0f), fmul(o, 0.0f), fmul(o, 1.0f))));
-            cd = sub3(cd, mk3(d, d, d));
-            f3 corr = mul3s(norm3(cd), -dOff);
-            f3 dd = mul3s(corr, kSdf);
-            pos.x = fadd(pos.x, dd.x); pos.y = fadd(pos.y, dd.y); pos.z = fadd(pos.z, dd.z);
-          }
-        }
-        WK(j) = pos;
-      }
+      w[P - 1u] = a;
     }
-#undef WK
-  }
-  __syncthreads();
-  // --- write back into the PREV buffer, coalesced (:268-272) ---
-  for (uint32_t i = threadIdx.x; i < nPts; i += blockDim.x) {
-    uint32_t l = i / P, pt = i - l * P;
-    prev[(size_t)s0 * P + i] = wk[pt * NB + l];
-  }
-}
-
-// ---------------------------------------------------------------------------
-// HairSimIntegrationPass, one warp per strand (lane j = point j, P <= 32).
-//
-// The same arithmetic in the same order as simIntegrateKernel: the
-// Gauss-Seidel length and local-shape chains are walked step by step with
-// every lane computing the step's correction from the two / three current
-// points (shuffled from their owners) and the owners applying it, so each
-// step sees the points the previous step left -- exactly the reference's
-// sequential loop.  The per-point work (Verlet, grid gathers, global shape,
-// sphere and SDF collisions) runs on all lanes at once.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ float4 shfl4(float4 v, int src) {
-  return make_float4(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src),
-                     __shfl_sync(0xffffffffu, v.z, src), __shfl_sync(0xffffffffu, v.w, src));
-}
-
-__global__ void __launch_bounds__(128)
-simIntegrateWarpKernel(const HfbSimUniforms u, uint32_t S, uint32_t P, uint32_t G,
-                       float4* __restrict__ prev, const float4* __restrict__ now,
-                       const float4* __restrict__ initial, const float* __restrict__ segLen,
-                       const int4* __restrict__ dv, const float4* __restrict__ gw,
-                       const float* __restrict__ sdf, uint32_t D) {
-  const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t strand = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (strand >= S) return;  // whole warps only
-  const bool has = lane < P;
-  const size_t gi = (size_t)strand * P + lane;
-  const f3 gmin = gridMin(u), gmax = gridMax(u);
-
-  // --- Verlet + forces (:125-162), one lane per point ---
-  float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (has) {
-    const f4 posNow = ld4(__ldg(&now[gi]));
-    if (lane == 0) {
-      p = make_float4(posNow.x, posNow.y, posNow.z, posNow.w);
-    } else {
-      const f4 posPrev = ld4(prev[gi]);
-      f3 force = mk3(0.0f, -u.gravity, 0.0f);
-      const f3 pn = xyz(posNow);
-      GridCo co = gridCell(G, gmin, gmax, pn);
-      f3 grad = mk3(0.f, 0.f, 0.f), vel = mk3(0.f, 0.f, 0.f);
-      float windStr = 0.0f, dens = 0.0f;
-      for (uint32_t z = co.mn[2]; z <= co.mx[2]; z++)
-        for (uint32_t y = co.mn[1]; y <= co.mx[1]; y++)
-          for (uint32_t x = co.mn[0]; x <= co.mx[0]; x++) {
-            f3 w = cellWeights(x, y, z, co.p);
-            float wl = len3(w);
-            uint32_t idx = gridIdx(G, x, y, z);
-            float4 a = __ldg(&gw[idx]);
-            grad = add3(grad, mul3(w, mk3(a.x, a.y, a.z)));
-            windStr = fadd(windStr, fmul(wl, a.w));
-            int4 b = __ldg(&dv[idx]);
-            vel = add3(vel, mul3(w, mk3(gridDecode(b.x), gridDecode(b.y), gridDecode(b.z))));
-            dens = fadd(dens, fmul(wl, gridDecode(b.w)));
-          }
-      float timer = fadd(fmul((float)u.frameIdx, 0.73f), fmul(u.windPhaseOffset, (float)strand));
-      float windJitter = fractf(fmul(timer, u.windStrengthFrequency));
-      float jitterDelta = mixf(fmul(-0.5f, u.windStrengthJitter), fmul(0.5f, u.windStrengthJitter), windJitter);
-      float jitterStr = fadd(1.0f, jitterDelta);
-      float windCellStr = sat(mixf(u.windStrengthLull, 1.0f, windStr));
-      force = add3(force, mul3s(mk3(u.wind.x, u.wind.y, u.wind.z),
-                                fabsf(fmul(fmul(u.wind.w, jitterStr), windCellStr))));
-      force = add3(force, mul3s(grad, u.volumePreservation));
-      f3 gridDisp = dens > 0.0f ? div3s(vel, dens) : mk3(0.f, 0.f, 0.f);
-      float dt = u.deltaTime;
-      f3 pd = sub3(pn, xyz(posPrev));
-      f3 fpd = mix3(pd, gridDisp, u.friction);
-      f3 nxt = add3(add3(pn, fpd), mul3s(mul3s(force, dt), dt));
-      f3 r = mix3(xyz(posPrev), nxt, posNow.w);
-      p = make_float4(r.x, r.y, r.z, posNow.w);
-    }
-  }
-
-  // --- per-lane constants of the constraints (from the initial positions) ---
-  const float4 pi = has ? __ldg(&initial[gi]) : make_float4(0.f, 0.f, 0.f, 0.f);
-  const float L0 = has ? __ldg(&segLen[gi]) : 0.0f;
-  // triangle-bending constants of the triplet that starts at this lane
-  const float4 i1 = shfl4(pi, min(lane + 1u, 31u)), i2 = shfl4(pi, min(lane + 2u, 31u));
-  float h0, tw0, tw1, tw2;
-  {
-    f3 cI = div3s(add3(add3(mk3(pi.x, pi.y, pi.z), mk3(i1.x, i1.y, i1.z)), mk3(i2.x, i2.y, i2.z)), 3.0f);
-    h0 = len3(sub3(cI, mk3(i1.x, i1.y, i1.z)));
-    float wT = fadd(fadd(pi.w, fmul(2.0f, i1.w)), i2.w);
-    tw0 = fmul(pi.w / wT, 2.0f);
-    tw1 = fmul(i1.w / wT, -4.0f);
-    tw2 = fmul(i2.w / wT, 2.0f);
-  }
-  // initial tangent towards this point (matchInitialTangent)
-  const float4 im1 = shfl4(pi, lane ? lane - 1u : 0u);
-  const f3 tInit = mk3(fsub(pi.x, im1.x), fsub(pi.y, im1.y), fsub(pi.z, im1.z));
-
-  const uint32_t iters = u.constraintIterations;
-  const f3 smin = mk3(u.sdf.boundsMin.x, u.sdf.boundsMin.y, u.sdf.boundsMin.z);
-  const f3 smax = mk3(u.sdf.boundsMax.x, u.sdf.boundsMax.y, u.sdf.boundsMax.z);
-  const float sdfOffset = u.sdf.boundsMax.w;
-  const f4 sph = mk4(u.collisionSphere.x, u.collisionSphere.y, u.collisionSphere.z, u.collisionSphere.w);
-  for (uint32_t it = 0; it < iters; it++) {
-    // length constraint, sequential along the strand
-    const float kLen = u.stiffnessLengthConstr;
-    for (uint32_t j = 0; j + 1u < P; j++) {
-      const float4 a = shfl4(p, j), b = shfl4(p, j + 1u);
-      const float expected = __shfl_sync(0xffffffffu, L0, j);
-      const float w0 = a.w, w1 = b.w;
-      f3 tng = mk3(fsub(b.x, a.x), fsub(b.y, a.y), fsub(b.z, a.z));
-      float actual = len3(tng);
-      float corr = fsub(1.0f, expected / actual);
-      float df = fmul(corr, kLen) / fadd(fadd(w0, w1), FLOAT_EPSILON);
-      f3 delta = mul3s(tng, df);
-      if (lane == j) {
-        p.x = fadd(a.x, fmul(delta.x, w0)); p.y = fadd(a.y, fmul(delta.y, w0)); p.z = fadd(a.z, fmul(delta.z, w0));
-      } else if (lane == j + 1u) {
-        p.x = fsub(b.x, fmul(w1, delta.x)); p.y = fsub(b.y, fmul(w1, delta.y)); p.z = fsub(b.z, fmul(w1, delta.z));
-      }
-    }
-    // global shape, every point at once
-    const float kGlob = u.stiffnessGlobalConstr / (float)iters;
-    if (has && lane >= 1u) {
-      float x = (float)lane / (float)(P - 1u);
-      float att = fsub(1.0f, sat(fsub(x, u.globalConstrExtent) / u.globalConstrFade));
-      float k = fmul(kGlob, att);
+    __syncthreads();
+    // global shape, :193-206, constraints.wgsl.ts:31-49 (point-parallel)
+    for (uint32_t i = tid; i < nPts; i += SIM_THREADS) {
+      const uint32_t ls = i / P, j = i - ls * P;
+      if (j == 0u) continue;
+      const float x = (float)j / (float)(P - 1u);
+      const float att = fsub(1.0f, sat(fsub(x, u.globalConstrExtent) / u.globalConstrFade));
+      const float4 pi = __ldg(&initial[(size_t)s0 * P + i]);
+      const float k = fmul(kGlob, att);
+      float4 p = wk[ls * R + j];
       f3 dvv = mk3(fsub(pi.x, p.x), fsub(pi.y, p.y), fsub(pi.z, p.z));
       f3 d = mul3s(mul3s(dvv, p.w), k);
       p.x = fadd(p.x, d.x); p.y = fadd(p.y, d.y); p.z = fadd(p.z, d.z);
+      wk[ls * R + j] = p;
     }
-    // local shape, sequential over the triplets
-    const float kLoc = u.stiffnessLocalConstr / (float)iters;
-    uint32_t jj = 0;
-    for (; jj + 3u < P; jj++) {
-      const float4 p0 = shfl4(p, jj), p1 = shfl4(p, jj + 1u), p2 = shfl4(p, jj + 2u);
-      const float hh0 = __shfl_sync(0xffffffffu, h0, jj);
-      const float w0 = __shfl_sync(0xffffffffu, tw0, jj), w1 = __shfl_sync(0xffffffffu, tw1, jj),
-                  w2 = __shfl_sync(0xffffffffu, tw2, jj);
-      f3 c = div3s(add3(add3(mk3(p0.x, p0.y, p0.z), mk3(p1.x, p1.y, p1.z)), mk3(p2.x, p2.y, p2.z)), 3.0f);
-      f3 hv = sub3(mk3(p1.x, p1.y, p1.z), c);
-      float h = len3(hv);
-      f3 delta = mul3s(hv, fsub(1.0f, hh0 / h));
-      if (lane == jj) {
-        f3 d = mul3s(delta, fmul(kLoc, w0));
-        p.x = fadd(p0.x, d.x); p.y = fadd(p0.y, d.y); p.z = fadd(p0.z, d.z);
-      } else if (lane == jj + 1u) {
-        f3 d = mul3s(delta, fmul(kLoc, w1));
-        p.x = fadd(p1.x, d.x); p.y = fadd(p1.y, d.y); p.z = fadd(p1.z, d.z);
-      } else if (lane == jj + 2u) {
-        f3 d = mul3s(delta, fmul(kLoc, w2));
-        p.x = fadd(p2.x, d.x); p.y = fadd(p2.y, d.y); p.z = fadd(p2.z, d.z);
+    __syncthreads();
+    // local shape (triangle bending, Gauss-Seidel), :209-232, constraints.wgsl.ts:54-120
+    if (tid < nStr) {
+      float4* w = wk + tid * R;
+      const float4* C = lc + tid * R;
+      uint32_t jj = 0;
+      if (P >= 3u) {
+        float4 p0 = w[0], p1 = w[1];
+        for (; jj + 3u < P; jj++) {
+          float4 p2 = w[jj + 2u];
+          const float4 cc = C[jj];
+          f3 c = div3s(add3(add3(mk3(p0.x, p0.y, p0.z), mk3(p1.x, p1.y, p1.z)), mk3(p2.x, p2.y, p2.z)), 3.0f);
+          f3 hv = sub3(mk3(p1.x, p1.y, p1.z), c);
+          float h = len3(hv);
+          f3 delta = mul3s(hv, fsub(1.0f, cc.x / h));
+          f3 d0 = mul3s(delta, fmul(kLoc, cc.y)), d1 = mul3s(delta, fmul(kLoc, cc.z)),
+             d2 = mul3s(delta, fmul(kLoc, cc.w));
+          p0.x = fadd(p0.x, d0.x); p0.y = fadd(p0.y, d0.y); p0.z = fadd(p0.z, d0.z);
+          p1.x = fadd(p1.x, d1.x); p1.y = fadd(p1.y, d1.y); p1.z = fadd(p1.z, d1.z);
+          p2.x = fadd(p2.x, d2.x); p2.y = fadd(p2.y, d2.y); p2.z = fadd(p2.z, d2.z);
+          w[jj] = p0;
+          p0 = p1;
+          p1 = p2;
+        }
+        w[jj] = p0;
+        w[jj + 1u] = p1;
+      }
+      for (; jj < P; jj++) {  // applyConstraint_matchInitialTangent
+        if (jj == 0u) continue;
+        const float4 p0 = w[jj - 1u];
+        float4 p1 = w[jj];
+        const float4 t = C[jj];
+        f3 proj = add3(mk3(p0.x, p0.y, p0.z), mk3(t.x, t.y, t.z));
+        f3 delta = sub3(proj, mk3(p1.x, p1.y, p1.z));
+        f3 d = mul3s(delta, fmul(kLoc, p1.w));
+        p1.x = fadd(p1.x, d.x); p1.y = fadd(p1.y, d.y); p1.z = fadd(p1.z, d.z);
+        w[jj] = p1;
       }
     }
-    for (; jj < P; jj++) {  // applyConstraint_matchInitialTangent, sequential
-      const float4 p0 = shfl4(p, jj - 1u);
-      if (lane == jj) {
-        f3 proj = add3(mk3(p0.x, p0.y, p0.z), tInit);
-        f3 delta = sub3(proj, mk3(p.x, p.y, p.z));
-        f3 d = mul3s(delta, fmul(kLoc, p.w));
-        p.x = fadd(p.x, d.x); p.y = fadd(p.y, d.y); p.z = fadd(p.z, d.z);
-      }
-    }
-    // collisions, every point at once
-    const float kColl = u.stiffnessCollisions / (float)iters;
-    const float kSdf = u.stiffnessSDF / (float)iters;
-    if (has && lane >= 1u) {
+    __syncthreads();
+    // collisions, :236-261, collisions.wgsl.ts:4-61 (point-parallel)
+    for (uint32_t i = tid; i < nPts; i += SIM_THREADS) {
+      const uint32_t ls = i / P, j = i - ls * P;
+      if (j == 0u) continue;
+      float4 pos = wk[ls * R + j];
       {
-        f3 v = mk3(fsub(p.x, sph.x), fsub(p.y, sph.y), fsub(p.z, sph.z));
+        f3 v = mk3(fsub(pos.x, sph.x), fsub(pos.y, sph.y), fsub(pos.z, sph.z));
         float dist = fsub(len3(v), sph.w);
         float dts = fmaxf(0.0f, -dist);
         f3 d = mul3s(mul3s(norm3(v), dts), kColl);
-        p.x = fadd(p.x, d.x); p.y = fadd(p.y, d.y); p.z = fadd(p.z, d.z);
+        pos.x = fadd(pos.x, d.x); pos.y = fadd(pos.y, d.y); pos.z = fadd(pos.z, d.z);
       }
-      if (lane > 2u) {
-        f3 q = mk3(p.x, p.y, p.z);
+      if (j > 2u) {
+        f3 q = mk3(pos.x, pos.y, pos.z);
         float d = sampleSDF(sdf, D, smin, smax, q);
         float dOff = fadd(d, sdfOffset);
         if (!(dOff >= 0.0f)) {
@@ -498,12 +349,18 @@ simIntegrateWarpKernel(const HfbSimUniforms u, uint32_t S, uint32_t P, uint32_t 
           cd = sub3(cd, mk3(d, d, d));
           f3 corr = mul3s(norm3(cd), -dOff);
           f3 dd = mul3s(corr, kSdf);
-          p.x = fadd(p.x, dd.x); p.y = fadd(p.y, dd.y); p.z = fadd(p.z, dd.z);
+          pos.x = fadd(pos.x, dd.x); pos.y = fadd(pos.y, dd.y); pos.z = fadd(pos.z, dd.z);
         }
       }
+      wk[ls * R + j] = pos;
     }
+    __syncthreads();
   }
-  if (has) prev[gi] = p;  // write into the PREV buffer (:268-272)
+  // --- write back into the PREV buffer, coalesced (:268-272) ---
+  for (uint32_t i = tid; i < nPts; i += SIM_THREADS) {
+    const uint32_t ls = i / P, pt = i - ls * P;
+    prev[(size_t)s0 * P + i] = wk[ls * R + pt];
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -569,24 +426,15 @@ cudaError_t launchGridPreSim(HfbCtx* c, const HfbSimUniforms& u, const int32_t* 
 cudaError_t launchSimIntegrate(HfbCtx* c, const HfbSimUniforms& u, const HfbHairData& h, float* prev,
                                const float* now, const float* initial, const float* segLen,
                                const int32_t* dv, const float* gw, const float* sdf, uint32_t sdfDims) {
-  uint32_t S = h.strandsCount, P = h.pointsPerStrand;
-  // warp per strand while the strands fill at most a couple of waves of the
-  // GPU; beyond that one thread per strand keeps every lane busy
-  if (P <= 32u && (uint64_t)S * 32u <= (uint64_t)c->smCount * 2048u * 2u) {
-    simIntegrateWarpKernel<<<divCeil(S, 4), 128, 0, c->stream>>>(
-        u, S, P, c->cfg.gridDims, (float4*)prev, (const float4*)now, (const float4*)initial, segLen,
-        (const int4*)dv, (const float4*)gw, sdf, sdfDims);
-    c->launches += 1;
-    return cudaGetLastError();
-  }
-  size_t smem = (size_t)P * SIM_STRANDS_PER_BLOCK * sizeof(float4);  // <= 128 KB (P <= 128)
+  const uint32_t S = h.strandsCount, P = h.pointsPerStrand;
+  const size_t smem = simSmemBytes(P);
   if (smem > c->simSmemSet) {
     cudaError_t e = cudaFuncSetAttribute(simIntegrateKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
     c->simSmemSet = smem;
   }
-  simIntegrateKernel<<<divCeil(S, SIM_STRANDS_PER_BLOCK), SIM_STRANDS_PER_BLOCK, smem, c->stream>>>(
+  simIntegrateKernel<<<divCeil(S, simStrandsPerBlock(P)), SIM_THREADS, smem, c->stream>>>(
       u, S, P, c->cfg.gridDims, (float4*)prev, (const float4*)now, (const float4*)initial, segLen,
       (const int4*)dv, (const float4*)gw, sdf, sdfDims);
   c->launches += 1;
