@@ -114,95 +114,7 @@ __device__ __forceinline__ RowSpan makeRowSpan(const ProjSeg& s) {
   return r;
 }
 
-// ---------------------------------------------------------------------------
-// 1. tilesRaster: HairTilesPass.main + processTile, hairTilesPass.wgsl.ts:70-238
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128)
-tilesRasterKernel(const HfbUniforms U, uint32_t P, uint32_t nStrands, uint32_t TS, uint32_t B,
-                  uint32_t threshold, float4 bsphere, const float4* __restrict__ pos,
-                  const float4* __restrict__ tan, const float* __restrict__ depth, uint4* __restrict__ tiles,
-                  uint32_t* __restrict__ segBuf, uint32_t* __restrict__ segCount,
-                  uint32_t* __restrict__ binCount, DeviceCounters* __restrict__ counters) {
-  const uint32_t segsPerStrand = P - 1u;
-  const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (gid >= nStrands * segsPerStrand) return;
-  const uint32_t strand = gid / segsPerStrand, seg = gid - strand * segsPerStrand;
-  const f2 size = mk2(U.viewport.x, U.viewport.y);
-  const uint32_t W = f2u(size.x), H = f2u(size.y);
-  const uint32_t tilesX = divCeil(W, TS);
-  const uint32_t maxDrawn = U.maxDrawnHairSegments;
-
-  ProjSeg s = projectSegment(U, pos, tan, P, strand, seg, size);
-  // getRasterizedHairBounds, swRasterizeHair.wgsl.ts:111-124
-  float bx1 = fminf(ceilf(fmaxf(fmaxf(s.v00.x, s.v01.x), fmaxf(s.v10.x, s.v11.x))), size.x);
-  float by1 = fminf(ceilf(fmaxf(fmaxf(s.v00.y, s.v01.y), fmaxf(s.v10.y, s.v11.y))), size.y);
-  float bx0 = fmaxf(floorf(fminf(fminf(s.v00.x, s.v01.x), fminf(s.v10.x, s.v11.x))), 0.0f);
-  float by0 = fmaxf(floorf(fminf(fminf(s.v00.y, s.v01.y), fminf(s.v10.y, s.v11.y))), 0.0f);
-  const uint32_t ux0 = f2u(bx0), uy0 = f2u(by0), ux1 = f2u(bx1), uy1 = f2u(by1);
-  const uint32_t tminx = ux0 / TS, tminy = uy0 / TS, tmaxx = ux1 / TS, tmaxy = uy1 / TS;
-  const uint32_t tsx = (tmaxx - tminx) + 1u, tsy = (tmaxy - tminy) + 1u;
-  if (tsx * tsy > threshold) return;  // degenerate segment rejection, :111-117
-
-  // getHairDepthBoundsVS, :242-246
-  f4 bsVS = m4v(U.modelViewMat.m, mk4(bsphere.x, bsphere.y, bsphere.z, 1.0f));
-  const float dv0 = fsub(bsVS.z, bsphere.w), dv1 = fadd(bsVS.z, bsphere.w);
-  const uint32_t key = (strand << 8) | seg;
-
-  const RowSpan span = makeRowSpan(s);
-  for (uint32_t ty = tminy; ty <= tmaxy; ty++) {
-    for (uint32_t tx = tminx; tx <= tmaxx; tx++) {
-      TileB tb = tileBoundsPx(W, H, TS, tx, ty);
-      // Only pixel corners inside the segment's bounding rectangle can pass
-      // the four edge tests, so the walk is restricted to tile x rect, and
-      // per row to the candidate span around the covered interval.
-      const uint32_t xa = max(tb.x0, ux0), xb = min(tb.x1, ux1 + 1u);
-      const uint32_t ya = max(tb.y0, uy0), yb = min(tb.y1, uy1 + 1u);
-      float dmin = 999.0f, dmax = -999.0f;
-      uint32_t dbin = B;
-      for (uint32_t y = ya; y < yb; y++) {
-        uint32_t x0r = xa, x1r = xb;
-        span.candidates((float)y, x0r, x1r);
-        for (uint32_t x = x0r; x < x1r; x++) {
-          f2 p = mk2((float)x, (float)y);
-          if (!insideQuad(s, p)) continue;
-          f2 w = interpolateHairQuad(s, p);
-          float hd = interpolateHairF32(w, s.depthsProj);
-          float zb = loadTex2DClamp(depth, W, H, (int)x, (int)H - (int)y);
-          if (hd > zb) continue;  // depth test, :193-195
-          f3 vs = projectVertex(U.projMatrixInv.m, mk4(p.x, p.y, hd, 1.0f));
-          uint32_t bin = (B - 1u) - getDepthBin(B, dv0, dv1, vs.z);
-          dmin = fminf(dmin, hd);
-          dmax = fmaxf(dmax, hd);
-          dbin = min(dbin, bin);
-        }
-      }
-      if (dmin > 1.0f) continue;
-      // store the result, :220-237 (warp-aggregated pointer allocation)
-      cg::coalesced_group g = cg::coalesced_threads();
-      uint32_t base = 0;
-      if (g.thread_rank() == 0) base = atomicAdd(&segBuf[0], g.size());
-      base = g.shfl(base, 0);
-      uint32_t ptr = base + g.thread_rank();
-      if (ptr < maxDrawn) {
-        uint32_t ti = ty * tilesX * B + tx * B + dbin;
-        // _storeTileHead: min / max depth as u32 maxima (order independent)
-        atomicMax(&tiles[ti].x, f2u(fmul(fsub(1.0f, dmin), F_MAX_U32)));
-        atomicMax(&tiles[ti].y, f2u(fmul(dmax, F_MAX_U32)));
-        atomicAdd(&segCount[ty * tilesX + tx], 1u);  // _incTileSegmentCount
-        atomicAdd(&binCount[ti], 1u);
-        // staging record in the list slot; binFinalize rewrites it
-        segBuf[1u + 2u * ptr] = ti;
-        segBuf[2u + 2u * ptr] = key;
-      } else {
-        atomicAdd(&counters->tileRecordsDropped, 1ull);
-      }
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// 2. binScan: exclusive prefix over T*B counts (block-local + block sums)
-// ---------------------------------------------------------------------------
+// Block-wide exclusive prefix (all threads call; total = block sum).
 __device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* warpSums, uint32_t& total) {
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   uint32_t x = v;
@@ -230,6 +142,329 @@ __device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* war
   return warpPrefix + x - v;
 }
 
+// ---------------------------------------------------------------------------
+// 1. tilesRaster: HairTilesPass.main + processTile, hairTilesPass.wgsl.ts:70-238
+//
+// A block takes TR_SEGS consecutive segments.  The candidate pixels of a
+// segment are its bounding rectangle clipped to the pixels the tiles cover
+// ([0, W - 1) x [0, H - 1): getTileBoundsPx clamps the tile ends to W - 1 /
+// H - 1), each belonging to tile (x / TS, y / TS).  The block then runs:
+//   A1  one thread per (segment, candidate pixel) pair: the edge tests;
+//       passing pairs are appended to a list;
+//   A2  one thread per passing pixel: interpolated depth, the depth test
+//       against the scene, the view-space depth bin, folded into the
+//       (segment, tile) accumulators with shared-memory atomics (min / max
+//       over an order-preserving u32 image of the depth, min of the bin):
+//       the result does not depend on the order;
+//   E   one thread per (segment, tile): the record, as processTile stores
+//       it (:220-237).
+// A segment whose tiles do not fit the block's accumulators is walked by its
+// own thread, tile by tile (rasterSegmentSerial).
+// ---------------------------------------------------------------------------
+constexpr uint32_t TR_SEGS = 128;   // segments (and threads) per block
+constexpr uint32_t TR_SLOTS = 1024; // (segment, tile) accumulators per block
+constexpr uint32_t TR_CHUNK = 4096; // pairs per A1 / A2 round
+
+struct TrShared {
+  float ox[4][TR_SEGS], oy[4][TR_SEGS], ex[4][TR_SEGS], ey[4][TR_SEGS];  // edge tests (insideQuad order)
+  float dp[4][TR_SEGS];                                                 // depthsProj
+  float qsx[TR_SEGS], qsy[TR_SEGS], qax[TR_SEGS], qay[TR_SEGS], qd2[TR_SEGS], qlse[TR_SEGS], qws[TR_SEGS],
+      qwe[TR_SEGS], qd22[TR_SEGS];                                      // QuadConst
+  uint32_t cx0[TR_SEGS], cy0[TR_SEGS], cw[TR_SEGS];  // candidate rectangle origin and width
+  uint32_t tminx[TR_SEGS], tminy[TR_SEGS], tsx[TR_SEGS];
+  uint32_t pairBase[TR_SEGS + 1], slotBase[TR_SEGS + 1];
+  uint32_t accMin[TR_SLOTS], accMax[TR_SLOTS], accBin[TR_SLOTS];
+  uint32_t pass[TR_CHUNK];  // segment | pair offset << 7
+  uint32_t warpSums[32];
+  uint32_t passCount;
+};
+
+// order-preserving u32 image of a float (NaN excluded by the caller)
+__device__ __forceinline__ uint32_t orderedBits(float f) {
+  const uint32_t b = __float_as_uint(f);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float orderedFloat(uint32_t u) {
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+// view-space depth bin of a passing pixel (:196-203, getHairDepthBoundsVS :242-246)
+__device__ __forceinline__ uint32_t viewDepthBin(const HfbUniforms& U, uint32_t B, float dv0, float dv1, f2 p,
+                                                 float hd) {
+  const f3 vs = projectVertex(U.projMatrixInv.m, mk4(p.x, p.y, hd, 1.0f));
+  return (B - 1u) - getDepthBin(B, dv0, dv1, vs.z);
+}
+
+// Stores one (segment, tile) record, :220-237 (warp-aggregated pointer
+// allocation; min / max depth as u32 maxima, order independent).
+__device__ __forceinline__ void storeTileRecord(uint4* __restrict__ tiles, uint32_t* __restrict__ segBuf,
+                                               uint32_t* __restrict__ segCount, uint32_t* __restrict__ binCount,
+                                               DeviceCounters* __restrict__ counters, uint32_t maxDrawn,
+                                               uint32_t tilesX, uint32_t B, uint32_t tx, uint32_t ty,
+                                               uint32_t dbin, float dmin, float dmax, uint32_t key) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  uint32_t base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(&segBuf[0], g.size());
+  base = g.shfl(base, 0);
+  const uint32_t ptr = base + g.thread_rank();
+  if (ptr < maxDrawn) {
+    const uint32_t ti = ty * tilesX * B + tx * B + dbin;
+    atomicMax(&tiles[ti].x, f2u(fmul(fsub(1.0f, dmin), F_MAX_U32)));  // _storeTileHead
+    atomicMax(&tiles[ti].y, f2u(fmul(dmax, F_MAX_U32)));
+    atomicAdd(&segCount[ty * tilesX + tx], 1u);  // _incTileSegmentCount
+    atomicAdd(&binCount[ti], 1u);
+    // staging record in the list slot; binFinalize rewrites it
+    segBuf[1u + 2u * ptr] = ti;
+    segBuf[2u + 2u * ptr] = key;
+  } else {
+    atomicAdd(&counters->tileRecordsDropped, 1ull);
+  }
+}
+
+// processTile for every tile of one segment's tile range, by one thread.
+__device__ void rasterSegmentSerial(const HfbUniforms& U, const ProjSeg& s, uint32_t W, uint32_t H, uint32_t TS,
+                                    uint32_t B, uint32_t tilesX, uint32_t maxDrawn, float dv0, float dv1,
+                                    uint32_t key, uint32_t ux0, uint32_t uy0, uint32_t ux1, uint32_t uy1,
+                                    const float* __restrict__ depth, uint4* __restrict__ tiles,
+                                    uint32_t* __restrict__ segBuf, uint32_t* __restrict__ segCount,
+                                    uint32_t* __restrict__ binCount, DeviceCounters* __restrict__ counters) {
+  const uint32_t tminx = ux0 / TS, tminy = uy0 / TS, tmaxx = ux1 / TS, tmaxy = uy1 / TS;
+  const RowSpan span = makeRowSpan(s);
+  for (uint32_t ty = tminy; ty <= tmaxy; ty++) {
+    for (uint32_t tx = tminx; tx <= tmaxx; tx++) {
+      TileB tb = tileBoundsPx(W, H, TS, tx, ty);
+      // Only pixel corners inside the segment's bounding rectangle can pass
+      // the four edge tests, so the walk is restricted to tile x rect, and
+      // per row to the candidate span around the covered interval.
+      const uint32_t xa = max(tb.x0, ux0), xb = min(tb.x1, ux1 + 1u);
+      const uint32_t ya = max(tb.y0, uy0), yb = min(tb.y1, uy1 + 1u);
+      float dmin = 999.0f, dmax = -999.0f;
+      uint32_t dbin = B;
+      for (uint32_t y = ya; y < yb; y++) {
+        uint32_t x0r = xa, x1r = xb;
+        span.candidates((float)y, x0r, x1r);
+        for (uint32_t x = x0r; x < x1r; x++) {
+          f2 p = mk2((float)x, (float)y);
+          if (!insideQuad(s, p)) continue;
+          f2 w = interpolateHairQuad(s, p);
+          float hd = interpolateHairF32(w, s.depthsProj);
+          float zb = loadTex2DClamp(depth, W, H, (int)x, (int)H - (int)y);
+          if (hd > zb) continue;  // depth test, :193-195
+          dmin = fminf(dmin, hd);
+          dmax = fmaxf(dmax, hd);
+          dbin = min(dbin, viewDepthBin(U, B, dv0, dv1, p, hd));
+        }
+      }
+      if (dmin > 1.0f) continue;
+      storeTileRecord(tiles, segBuf, segCount, binCount, counters, maxDrawn, tilesX, B, tx, ty, dbin, dmin, dmax,
+                      key);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(TR_SEGS)
+tilesRasterKernel(const HfbUniforms U, uint32_t P, uint32_t nStrands, uint32_t TS, uint32_t B,
+                  uint32_t threshold, float4 bsphere, const float4* __restrict__ pos,
+                  const float4* __restrict__ tan, const float* __restrict__ depth, uint4* __restrict__ tiles,
+                  uint32_t* __restrict__ segBuf, uint32_t* __restrict__ segCount,
+                  uint32_t* __restrict__ binCount, DeviceCounters* __restrict__ counters) {
+  __shared__ TrShared sh;
+  const uint32_t tid = threadIdx.x, lane = tid & 31u;
+  const uint32_t segsPerStrand = P - 1u;
+  const uint32_t nSeg = nStrands * segsPerStrand;
+  const uint32_t gid = blockIdx.x * TR_SEGS + tid;
+  const f2 size = mk2(U.viewport.x, U.viewport.y);
+  const uint32_t W = f2u(size.x), H = f2u(size.y);
+  const uint32_t tilesX = divCeil(W, TS);
+  const uint32_t maxDrawn = U.maxDrawnHairSegments;
+  // getHairDepthBoundsVS, :242-246
+  const f4 bsVS = m4v(U.modelViewMat.m, mk4(bsphere.x, bsphere.y, bsphere.z, 1.0f));
+  const float dv0 = fsub(bsVS.z, bsphere.w), dv1 = fadd(bsVS.z, bsphere.w);
+
+  // ---- project this thread's segment ----
+  uint32_t pairs = 0, slots = 0, key = 0;
+  bool serial = false;
+  ProjSeg s;
+  uint32_t ux0 = 0, uy0 = 0, ux1 = 0, uy1 = 0;
+  if (gid < nSeg) {
+    const uint32_t strand = gid / segsPerStrand, seg = gid - strand * segsPerStrand;
+    key = (strand << 8) | seg;
+    s = projectSegment(U, pos, tan, P, strand, seg, size);
+    // getRasterizedHairBounds, swRasterizeHair.wgsl.ts:111-124
+    const float bx1 = fminf(ceilf(fmaxf(fmaxf(s.v00.x, s.v01.x), fmaxf(s.v10.x, s.v11.x))), size.x);
+    const float by1 = fminf(ceilf(fmaxf(fmaxf(s.v00.y, s.v01.y), fmaxf(s.v10.y, s.v11.y))), size.y);
+    const float bx0 = fmaxf(floorf(fminf(fminf(s.v00.x, s.v01.x), fminf(s.v10.x, s.v11.x))), 0.0f);
+    const float by0 = fmaxf(floorf(fminf(fminf(s.v00.y, s.v01.y), fminf(s.v10.y, s.v11.y))), 0.0f);
+    ux0 = f2u(bx0); uy0 = f2u(by0); ux1 = f2u(bx1); uy1 = f2u(by1);
+    const uint32_t tminx = ux0 / TS, tminy = uy0 / TS, tmaxx = ux1 / TS, tmaxy = uy1 / TS;
+    const uint32_t tsx = (tmaxx - tminx) + 1u, tsy = (tmaxy - tminy) + 1u;
+    if (tsx * tsy <= threshold) {  // degenerate segment rejection, :111-117
+      const uint32_t cx1 = min(ux1 + 1u, W - 1u), cy1 = min(uy1 + 1u, H - 1u);
+      const uint32_t cwid = cx1 > ux0 ? cx1 - ux0 : 0u, chei = cy1 > uy0 ? cy1 - uy0 : 0u;
+      if (cwid && chei) {
+        if ((uint64_t)cwid * chei >= (1ull << 24)) {
+          serial = true;  // beyond the pair encoding: its own walk
+        } else {
+          pairs = cwid * chei;
+          slots = tsx * tsy;
+        }
+      }
+      sh.cx0[tid] = ux0; sh.cy0[tid] = uy0; sh.cw[tid] = max(cwid, 1u);
+      sh.tminx[tid] = tminx; sh.tminy[tid] = tminy; sh.tsx[tid] = tsx;
+      const f2 o[4] = {s.v01, s.v11, s.v10, s.v00};  // the edge tests in insideQuad's order
+      const f2 e[4] = {s.v00, s.v01, s.v11, s.v10};
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        sh.ox[i][tid] = o[i].x;
+        sh.oy[i][tid] = o[i].y;
+        sh.ex[i][tid] = fsub(e[i].x, o[i].x);
+        sh.ey[i][tid] = fsub(e[i].y, o[i].y);
+      }
+      sh.dp[0][tid] = s.depthsProj.x; sh.dp[1][tid] = s.depthsProj.y;
+      sh.dp[2][tid] = s.depthsProj.z; sh.dp[3][tid] = s.depthsProj.w;
+      const QuadConst q = quadConst(s);
+      sh.qsx[tid] = q.sm.x; sh.qsy[tid] = q.sm.y; sh.qax[tid] = q.ab.x; sh.qay[tid] = q.ab.y;
+      sh.qd2[tid] = q.d2; sh.qlse[tid] = q.lse; sh.qws[tid] = q.wS; sh.qwe[tid] = q.wE; sh.qd22[tid] = q.d22;
+    }
+  }
+  // accumulators of the block's (segment, tile) pairs; segments beyond them walk alone
+  uint32_t slotTotal;
+  const uint32_t slotEx = blockExclusiveScan(slots, sh.warpSums, slotTotal);
+  if (slots && slotEx + slots > TR_SLOTS) {
+    serial = true;
+    pairs = 0;
+    slots = 0;
+  }
+  sh.slotBase[tid] = slotEx;
+  uint32_t pairTotal;
+  sh.pairBase[tid] = blockExclusiveScan(pairs, sh.warpSums, pairTotal);
+  if (tid == 0) sh.pairBase[TR_SEGS] = pairTotal;
+  for (uint32_t i = tid; i < TR_SLOTS; i += TR_SEGS) {
+    sh.accMin[i] = 0xffffffffu;
+    sh.accMax[i] = 0u;
+    sh.accBin[i] = B;
+  }
+  __syncthreads();
+
+  for (uint32_t c0 = 0; c0 < pairTotal; c0 += TR_CHUNK) {
+    const uint32_t n = min(TR_CHUNK, pairTotal - c0);
+    if (tid == 0) sh.passCount = 0;
+    __syncthreads();
+    // ---- A1: edge tests, contiguous pairs per thread ----
+    {
+      const uint32_t per = divCeil(n, TR_SEGS);
+      uint32_t p = c0 + tid * per;
+      const uint32_t pEnd = min(p + per, c0 + n);
+      uint32_t k = 0, rx = 0, ry = 0, w = 1, x0 = 0, y0 = 0;
+      float eox[4], eoy[4], eex[4], eey[4];
+      auto loadSeg = [&](uint32_t kk) {
+        x0 = sh.cx0[kk]; y0 = sh.cy0[kk]; w = sh.cw[kk];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          eox[i] = sh.ox[i][kk]; eoy[i] = sh.oy[i][kk]; eex[i] = sh.ex[i][kk]; eey[i] = sh.ey[i][kk];
+        }
+      };
+      if (p < pEnd) {
+        uint32_t lo = 0, hi = TR_SEGS;  // last k with pairBase[k] <= p
+        while (hi - lo > 1u) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if (sh.pairBase[mid] <= p) lo = mid; else hi = mid;
+        }
+        k = lo;
+        loadSeg(k);
+        const uint32_t r = p - sh.pairBase[k];
+        ry = r / w;
+        rx = r - ry * w;
+      }
+      for (uint32_t it = 0; it < per; it++) {
+        const bool valid = p < pEnd;
+        bool pass = false;
+        if (valid) {
+          const f2 pf = mk2((float)(x0 + rx), (float)(y0 + ry));
+          pass = true;
+#pragma unroll
+          for (int i = 0; i < 4; i++) {  // edgeFunction, swRasterizeHair.wgsl.ts:128-130
+            const float C = fsub(fmul(fsub(pf.x, eox[i]), eey[i]), fmul(fsub(pf.y, eoy[i]), eex[i]));
+            pass = pass && C >= 0.0f;
+          }
+        }
+        const uint32_t bal = __ballot_sync(0xffffffffu, pass);
+        if (bal) {
+          const uint32_t leader = (uint32_t)(__ffs(bal) - 1);
+          uint32_t base = 0;
+          if (lane == leader) base = atomicAdd(&sh.passCount, (uint32_t)__popc(bal));
+          base = __shfl_sync(0xffffffffu, base, leader);
+          if (pass) sh.pass[base + __popc(bal & ((1u << lane) - 1u))] = k | ((p - sh.pairBase[k]) << 7);
+        }
+        if (valid) {
+          p++;
+          if (++rx == w) {
+            rx = 0;
+            ry++;
+            if (p < pEnd && p >= sh.pairBase[k + 1u]) {  // next segment with pairs
+              while (sh.pairBase[k + 1u] <= p) k++;
+              loadSeg(k);
+              ry = 0;
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // ---- A2: depth, depth test and bin of every passing pixel ----
+    const uint32_t nPass = sh.passCount;
+    for (uint32_t i = tid; i < nPass; i += TR_SEGS) {
+      const uint32_t e = sh.pass[i];
+      const uint32_t k = e & 0x7fu, r = e >> 7;
+      const uint32_t w = sh.cw[k];
+      const uint32_t ry = r / w, rx = r - ry * w;
+      const uint32_t x = sh.cx0[k] + rx, y = sh.cy0[k] + ry;
+      const f2 p = mk2((float)x, (float)y);
+      QuadConst qc;
+      qc.sm = mk2(sh.qsx[k], sh.qsy[k]);
+      qc.ab = mk2(sh.qax[k], sh.qay[k]);
+      qc.d2 = sh.qd2[k]; qc.lse = sh.qlse[k]; qc.wS = sh.qws[k]; qc.wE = sh.qwe[k];
+      qc.ab2 = mk2(sh.ex[3][k], sh.ey[3][k]);
+      qc.d22 = sh.qd22[k];
+      const f2 wq = interpolateHairQuadPre(qc, mk2(sh.ox[3][k], sh.oy[3][k]), p);
+      const float hd = interpolateHairF32(wq, mk4(sh.dp[0][k], sh.dp[1][k], sh.dp[2][k], sh.dp[3][k]));
+      const float zb = loadTex2DClamp(depth, W, H, (int)x, (int)H - (int)y);
+      if (hd > zb) continue;  // depth test, :193-195
+      const uint32_t slot = sh.slotBase[k] + (y / TS - sh.tminy[k]) * sh.tsx[k] + (x / TS - sh.tminx[k]);
+      atomicMin(&sh.accBin[slot], viewDepthBin(U, B, dv0, dv1, p, hd));
+      if (!isnan(hd)) {  // fminf / fmaxf ignore a NaN depth
+        atomicMin(&sh.accMin[slot], orderedBits(hd));
+        atomicMax(&sh.accMax[slot], orderedBits(hd));
+      }
+    }
+    __syncthreads();
+  }
+
+  // ---- E: one record per (segment, tile) that took a pixel ----
+  for (uint32_t i = tid; i < slotTotal && i < TR_SLOTS; i += TR_SEGS) {
+    if (sh.accMin[i] == 0xffffffffu) continue;  // no pixel with a depth
+    const float dmin = orderedFloat(sh.accMin[i]);
+    if (dmin > 1.0f) continue;
+    uint32_t lo = 0, hi = TR_SEGS;  // segment of the slot: last k with slotBase[k] <= i
+    while (hi - lo > 1u) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (sh.slotBase[mid] <= i) lo = mid; else hi = mid;
+    }
+    const uint32_t k = lo, l = i - sh.slotBase[k];
+    const uint32_t ty = sh.tminy[k] + l / sh.tsx[k], tx = sh.tminx[k] + l % sh.tsx[k];
+    const uint32_t g = blockIdx.x * TR_SEGS + k;
+    const uint32_t strand = g / segsPerStrand, seg = g - strand * segsPerStrand;
+    storeTileRecord(tiles, segBuf, segCount, binCount, counters, maxDrawn, tilesX, B, tx, ty, sh.accBin[i], dmin,
+                    orderedFloat(sh.accMax[i]), (strand << 8) | seg);
+  }
+  if (serial)
+    rasterSegmentSerial(U, s, W, H, TS, B, tilesX, maxDrawn, dv0, dv1, key, ux0, uy0, ux1, uy1, depth, tiles,
+                        segBuf, segCount, binCount, counters);
+}
+
+// ---------------------------------------------------------------------------
+// 2. binScan: exclusive prefix over T*B counts (block-local + block sums)
+// ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(512) binScanBlocks(const uint32_t* __restrict__ cnt, uint32_t* __restrict__ off,
                                                      uint32_t* __restrict__ blockSums, uint32_t n) {
   __shared__ uint32_t warpSums[32];
@@ -1476,7 +1711,7 @@ cudaError_t launchTilesPass(HfbCtx* c, const HfbUniforms& u, const HfbHairData& 
   DeviceCounters* dc = (DeviceCounters*)c->dCounters;
   if (nSeg) {
     float4 bs = make_float4(h.boundingSphere[0], h.boundingSphere[1], h.boundingSphere[2], h.boundingSphere[3]);
-    tilesRasterKernel<<<divCeil(nSeg, 128), 128, 0, c->stream>>>(
+    tilesRasterKernel<<<divCeil(nSeg, TR_SEGS), TR_SEGS, 0, c->stream>>>(
         u, h.pointsPerStrand, nStrands, TS, B, cfg.invalidTilesPerSegmentThreshold, bs, (const float4*)pos,
         (const float4*)tan, depth, (uint4*)rb.tiles, rb.tileSegments, rb.segmentCountPerTile, s.binCount, dc);
   }
