@@ -5,13 +5,8 @@
 // collisions}.wgsl.ts and grids/*.wgsl.ts.  All arithmetic follows the fixed
 // fp32 order of hfb_math.cuh, so results are reproducible run to run; the
 // grid splat is integer (i32 fixed point, wrapping adds), hence order-free.
-#include <cooperative_groups.h>
-#include <cooperative_groups/reduce.h>
-
 #include "hfb_internal.cuh"
 #include "hfb_math.cuh"
-
-namespace cg = cooperative_groups;
 
 namespace hfb {
 namespace {
@@ -378,37 +373,21 @@ gridPostSimKernel(const HfbSimUniforms u, uint32_t N, uint32_t G, const float4* 
   const f3 pn = mk3(b.x, b.y, b.z);
   const f3 vel = sub3(pn, mk3(a.x, a.y, a.z));
   const GridCo co = gridCell(G, gridMin(u), gridMax(u), pn);
-  // Consecutive points of a strand mostly share their cell: the lanes that
-  // add to the same node sum their (wrapping, order-free) i32 values first
-  // and one lane issues the atomics.
-  const cg::thread_block_tile<32> warp = cg::tiled_partition<32>(cg::this_thread_block());
-#pragma unroll 1
+  // Eight corners, four wrapping i32 adds each (fire-and-forget reductions
+  // in L2; the sums do not depend on their order).
+  if (!valid) return;
+#pragma unroll
   for (uint32_t k = 0; k < 8u; k++) {
     const uint32_t x = co.mn[0] + (k & 1u), y = co.mn[1] + ((k >> 1) & 1u), z = co.mn[2] + (k >> 2);
-    const bool on = valid && x <= co.mx[0] && y <= co.mx[1] && z <= co.mx[2];
-    unsigned v0 = 0, v1 = 0, v2 = 0, v3 = 0;
-    uint32_t idx = 0xffffffffu;
-    if (on) {
-      idx = gridIdx(G, x, y, z);
-      const f3 w = cellWeights(x, y, z, co.p);
-      const f3 cv = mul3(vel, w);
-      v0 = (unsigned)gridEncode(cv.x);
-      v1 = (unsigned)gridEncode(cv.y);
-      v2 = (unsigned)gridEncode(cv.z);
-      v3 = (unsigned)gridEncode(len3(w));
-    }
-    const cg::coalesced_group g = cg::labeled_partition(warp, idx);
-    v0 = cg::reduce(g, v0, cg::plus<unsigned>());
-    v1 = cg::reduce(g, v1, cg::plus<unsigned>());
-    v2 = cg::reduce(g, v2, cg::plus<unsigned>());
-    v3 = cg::reduce(g, v3, cg::plus<unsigned>());
-    if (on && g.thread_rank() == 0) {
-      unsigned* c = dv + 4u * idx;
-      atomicAdd(c + 0, v0);
-      atomicAdd(c + 1, v1);
-      atomicAdd(c + 2, v2);
-      atomicAdd(c + 3, v3);
-    }
+    if (x > co.mx[0] || y > co.mx[1] || z > co.mx[2]) continue;
+    const uint32_t idx = gridIdx(G, x, y, z);
+    const f3 w = cellWeights(x, y, z, co.p);
+    const f3 cv = mul3(vel, w);
+    unsigned* c = dv + 4u * idx;
+    atomicAdd(c + 0, (unsigned)gridEncode(cv.x));
+    atomicAdd(c + 1, (unsigned)gridEncode(cv.y));
+    atomicAdd(c + 2, (unsigned)gridEncode(cv.z));
+    atomicAdd(c + 3, (unsigned)gridEncode(len3(w)));
   }
 }
 
