@@ -74,42 +74,6 @@ uint32_t maxDrawnSegments(const HfbConfig& cfg, uint32_t W, uint32_t H) {
   return (uint32_t)(1ull + t * cfg.avgSegmentsPerTile);
 }
 
-static size_t alignUp(size_t v) { return (v + 255u) & ~size_t(255u); }
-
-TilesScratch tilesScratchLayout(void* base, const HfbConfig& cfg, uint32_t W, uint32_t H,
-                                uint32_t maxDrawn) {
-  size_t T = (size_t)divCeil(W, cfg.tileSize) * divCeil(H, cfg.tileSize);
-  size_t TB = T * cfg.tileDepthBins;
-  size_t nBlocks = (TB + 2047) / 2048 + 1;
-  char* p = (char*)base;
-  TilesScratch s;
-  size_t off = 0;
-  s.binCount = (uint32_t*)(p + off); off = alignUp(off + TB * 4);
-  s.binOffset = (uint32_t*)(p + off); off = alignUp(off + TB * 4);
-  s.keys = (uint32_t*)(p + off); off = alignUp(off + (size_t)maxDrawn * 4);
-  s.blockSums = (uint32_t*)(p + off); off = alignUp(off + nBlocks * 4 + 16);
-  s.largeBins = (uint32_t*)(p + off); off = alignUp(off + (TB + 1) * 4);
-  s.bytes = off;
-  return s;
-}
-
-FineScratch fineScratchLayout(void* base, const HfbConfig& cfg, uint32_t W, uint32_t H) {
-  const size_t T = (size_t)divCeil(W, cfg.tileSize) * divCeil(H, cfg.tileSize);
-  const size_t groupBytes = (size_t)cfg.tileSize * cfg.tileSize * 16;
-  FineScratch s;
-  // split groups: at most 1024, and at most 4 MiB of composites
-  s.maxGroups = (uint32_t)std::min<size_t>(1024, (4u << 20) / groupBytes);
-  s.maxItems = (uint32_t)(T + s.maxGroups);
-  char* p = (char*)base;
-  size_t off = 0;
-  s.hdr = (uint32_t*)(p + off); off = alignUp(off + 16);
-  s.items = (uint4*)(p + off); off = alignUp(off + (size_t)s.maxItems * 16);
-  s.arrivals = (uint32_t*)(p + off); off = alignUp(off + (size_t)s.maxGroups * 4);
-  s.groups = (float4*)(p + off); off = alignUp(off + (size_t)s.maxGroups * groupBytes);
-  s.bytes = off;
-  return s;
-}
-
 }  // namespace hfb
 
 extern "C" {
@@ -148,6 +112,7 @@ int hfb_ctx_create(const HfbConfig* cfg, int device, HfbCtx** out) {
 int hfb_ctx_destroy(HfbCtx* c) {
   HFB_CHECK_CTX(c);
   cudaStreamSynchronize(c->stream);
+  hfb::frameBatchRelease(c);
   if (c->dCounters) cudaFree(c->dCounters);
   if (c->ownStream) cudaStreamDestroy(c->ownStream);
   delete c;
@@ -184,6 +149,7 @@ int hfb_get_counters(HfbCtx* c, HfbCounters* out) {
   out->launches = c->launches;
   out->fineSplitTiles = d.fineSplitTiles;
   out->fineSplitRedone = d.fineSplitRedone;
+  out->badWorkItems = d.badWorkItems;
   return HFB_OK;
 }
 
@@ -308,10 +274,7 @@ static std::string checkViewport(const HfbUniforms* u, const HfbRasterBuffers* r
   return "";
 }
 
-int hfb_clear_before_render(HfbCtx* c, HfbRasterBuffers* rb) {
-  HFB_CHECK_CTX(c);
-  std::string err = checkRaster(c, rb);
-  HFB_REQUIRE(c, err.empty(), err);
+static cudaError_t clearRaster(HfbCtx* c, HfbRasterBuffers* rb) {
   const HfbConfig& cfg = c->cfg;
   size_t T = (size_t)hfb::divCeil(rb->width, cfg.tileSize) * hfb::divCeil(rb->height, cfg.tileSize);
   cudaError_t e = cudaSuccess;
@@ -322,6 +285,14 @@ int hfb_clear_before_render(HfbCtx* c, HfbRasterBuffers* rb) {
   z(rb->rasterizerResult, 16 + (size_t)rb->width * rb->height * 16);  // hairFinePass.ts:50-55
   z(rb->tileList, 4);                             // hairTileSortPass.ts:63-68
   z(rb->sortBuckets, (size_t)cfg.sortBuckets * 8);
+  return e;
+}
+
+int hfb_clear_before_render(HfbCtx* c, HfbRasterBuffers* rb) {
+  HFB_CHECK_CTX(c);
+  std::string err = checkRaster(c, rb);
+  HFB_REQUIRE(c, err.empty(), err);
+  cudaError_t e = clearRaster(c, rb);
   if (e != cudaSuccess) return cudaFail(c, e, "clear_before_render");
   return HFB_OK;
 }
@@ -408,6 +379,75 @@ int hfb_fine_pass(HfbCtx* c, const HfbUniforms* u, const HfbHairData* h, const f
   if (err.empty()) err = checkViewport(u, rb);
   HFB_REQUIRE(c, err.empty(), err);
   HFB_LAUNCH(c, hfb::launchFinePass(c, *u, *h, pos, tan, shading, depth, *rb), "fine_pass");
+}
+
+// Checks one instance of a frame (the union of the per-pass checks).
+static std::string checkInstance(const HfbCtx* c, const HfbInstance* in) {
+  if (!in) return "instance is NULL";
+  if (!in->uniforms || !in->simUniforms) return "instance uniforms are NULL";
+  std::string err = validateHair(&in->hair, 4, 128);
+  if (!err.empty()) return err;
+  if (!in->positions[0] || !in->positions[1] || !in->positionsInitial || !in->tangents || !in->segmentLengths ||
+      !in->densityVelocity || !in->densityGradWind || !in->sdf || !in->shading || !in->sceneDepth)
+    return "an instance buffer is NULL";
+  if (in->positions[0] == in->positions[1]) return "the two position buffers are the same";
+  if (in->current > 1u) return "current must be 0 or 1";
+  if (!aligned16(in->positions[0]) || !aligned16(in->positions[1]) || !aligned16(in->positionsInitial) ||
+      !aligned16(in->tangents) || !aligned16(in->densityVelocity) || !aligned16(in->densityGradWind) ||
+      !aligned16(in->shading))
+    return "vec4 buffers must be 16-byte aligned";
+  if (in->sdfDims < 1 || in->sdfDims > 1024) return "sdfDims must be in [1, 1024]";
+  if (in->simUniforms->constraintIterations > 1024) return "constraintIterations must be <= 1024";
+  if (in->ao && (in->aoWidth == 0 || in->aoHeight == 0)) return "AO texture with an empty size";
+  if (in->shadowMap && in->shadowMapSize == 0) return "shadow map with an empty size";
+  err = checkRaster(c, &in->raster);
+  if (err.empty()) err = checkViewport(in->uniforms, &in->raster);
+  return err;
+}
+
+int hfb_frame(HfbCtx* c, HfbInstance* in) {
+  HFB_CHECK_CTX(c);
+  std::string err = checkInstance(c, in);
+  HFB_REQUIRE(c, err.empty(), err);
+  const HfbSimUniforms& su = *in->simUniforms;
+  const HfbUniforms& u = *in->uniforms;
+  const HfbHairData& h = in->hair;
+  const uint32_t cur = in->current;
+  float* prev = in->positions[1u - cur];
+  float* now = in->positions[cur];
+  HfbRasterBuffers& rb = in->raster;
+  cudaError_t e = hfb::launchGridPreSim(c, su, in->densityVelocity, in->densityGradWind, in->sdf, in->sdfDims);
+  if (e == cudaSuccess && h.strandsCount)
+    e = hfb::launchSimIntegrate(c, su, h, prev, now, in->positionsInitial, in->segmentLengths, in->densityVelocity,
+                                in->densityGradWind, in->sdf, in->sdfDims);
+  // HairObject.swapPositionBuffersAfterSimIntegration: the new positions are "now"
+  if (e == cudaSuccess) e = hfb::launchGridPostSim(c, su, h, now, prev, in->densityVelocity);
+  if (e == cudaSuccess) e = clearRaster(c, &rb);
+  if (e == cudaSuccess)
+    e = hfb::launchTilesPass(c, u, h, prev, in->tangents, in->sceneDepth, in->strandsToRender, rb);
+  if (e == cudaSuccess) e = hfb::launchTileSort(c, rb);
+  if (e == cudaSuccess) e = hfb::launchFinePass(c, u, h, prev, in->tangents, in->shading, in->sceneDepth, rb);
+  if (e == cudaSuccess && h.strandsCount)
+    e = hfb::launchShading(c, u, h, prev, in->tangents, in->shadingDepth ? in->shadingDepth : in->sceneDepth,
+                           in->ao, in->ao ? in->aoWidth : 0u, in->ao ? in->aoHeight : 0u, in->shadowMap,
+                           in->shadowMap ? in->shadowMapSize : 0u, in->shading);
+  if (e != cudaSuccess) return cudaFail(c, e, "frame");
+  in->current = 1u - cur;
+  return HFB_OK;
+}
+
+int hfb_frame_batch(HfbCtx* c, HfbInstance* insts, uint32_t n) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, insts || n == 0, "instances are NULL");
+  HFB_REQUIRE(c, n <= hfb::BATCH_MAX, "at most 1024 instances per batch");
+  if (n == 0) return HFB_OK;
+  for (uint32_t i = 0; i < n; i++) {
+    std::string err = checkInstance(c, &insts[i]);
+    HFB_REQUIRE(c, err.empty(), "instance " + std::to_string(i) + ": " + err);
+  }
+  cudaError_t e = hfb::frameBatch(c, insts, n);
+  if (e != cudaSuccess) return cudaFail(c, e, "frame_batch");
+  return HFB_OK;
 }
 
 }  // extern "C"

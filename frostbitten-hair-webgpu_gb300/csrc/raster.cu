@@ -161,7 +161,7 @@ __device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* war
 // A segment whose tiles do not fit the block's accumulators is walked by its
 // own thread, tile by tile (rasterSegmentSerial).
 // ---------------------------------------------------------------------------
-constexpr uint32_t TR_SEGS = 128;   // segments (and threads) per block
+constexpr uint32_t TR_SEGS = TILES_RASTER_SEGS;  // segments (and threads) per block
 constexpr uint32_t TR_SLOTS = 1024; // (segment, tile) accumulators per block
 constexpr uint32_t TR_CHUNK = 4096; // pairs per A1 / A2 round
 
@@ -262,17 +262,17 @@ __device__ void rasterSegmentSerial(const HfbUniforms& U, const ProjSeg& s, uint
   }
 }
 
-__global__ void __launch_bounds__(TR_SEGS)
-tilesRasterKernel(const HfbUniforms U, uint32_t P, uint32_t nStrands, uint32_t TS, uint32_t B,
-                  uint32_t threshold, float4 bsphere, const float4* __restrict__ pos,
-                  const float4* __restrict__ tan, const float* __restrict__ depth, uint4* __restrict__ tiles,
-                  uint32_t* __restrict__ segBuf, uint32_t* __restrict__ segCount,
-                  uint32_t* __restrict__ binCount, DeviceCounters* __restrict__ counters) {
-  __shared__ TrShared sh;
+__device__ __forceinline__ void tilesRasterBody(const HfbUniforms& U, uint32_t P, uint32_t nStrands, uint32_t TS,
+                                                uint32_t B, uint32_t threshold, float4 bsphere,
+                                                const float4* __restrict__ pos, const float4* __restrict__ tan,
+                                                const float* __restrict__ depth, uint4* __restrict__ tiles,
+                                                uint32_t* __restrict__ segBuf, uint32_t* __restrict__ segCount,
+                                                uint32_t* __restrict__ binCount,
+                                                DeviceCounters* __restrict__ counters, TrShared& sh, uint32_t blk) {
   const uint32_t tid = threadIdx.x, lane = tid & 31u;
   const uint32_t segsPerStrand = P - 1u;
   const uint32_t nSeg = nStrands * segsPerStrand;
-  const uint32_t gid = blockIdx.x * TR_SEGS + tid;
+  const uint32_t gid = blk * TR_SEGS + tid;
   const f2 size = mk2(U.viewport.x, U.viewport.y);
   const uint32_t W = f2u(size.x), H = f2u(size.y);
   const uint32_t tilesX = divCeil(W, TS);
@@ -452,7 +452,7 @@ tilesRasterKernel(const HfbUniforms U, uint32_t P, uint32_t nStrands, uint32_t T
     }
     const uint32_t k = lo, l = i - sh.slotBase[k];
     const uint32_t ty = sh.tminy[k] + l / sh.tsx[k], tx = sh.tminx[k] + l % sh.tsx[k];
-    const uint32_t g = blockIdx.x * TR_SEGS + k;
+    const uint32_t g = blk * TR_SEGS + k;
     const uint32_t strand = g / segsPerStrand, seg = g - strand * segsPerStrand;
     storeTileRecord(tiles, segBuf, segCount, binCount, counters, maxDrawn, tilesX, B, tx, ty, sh.accBin[i], dmin,
                     orderedFloat(sh.accMax[i]), (strand << 8) | seg);
@@ -460,15 +460,27 @@ tilesRasterKernel(const HfbUniforms U, uint32_t P, uint32_t nStrands, uint32_t T
   if (serial)
     rasterSegmentSerial(U, s, W, H, TS, B, tilesX, maxDrawn, dv0, dv1, key, ux0, uy0, ux1, uy1, depth, tiles,
                         segBuf, segCount, binCount, counters);
+  __syncthreads();  // the block's staging is reused by its next segments
+}
+
+__global__ void __launch_bounds__(TR_SEGS)
+tilesRasterKernel(const HfbUniforms U, uint32_t P, uint32_t nStrands, uint32_t TS, uint32_t B,
+                  uint32_t threshold, float4 bsphere, const float4* __restrict__ pos,
+                  const float4* __restrict__ tan, const float* __restrict__ depth, uint4* __restrict__ tiles,
+                  uint32_t* __restrict__ segBuf, uint32_t* __restrict__ segCount,
+                  uint32_t* __restrict__ binCount, DeviceCounters* __restrict__ counters) {
+  __shared__ TrShared sh;
+  tilesRasterBody(U, P, nStrands, TS, B, threshold, bsphere, pos, tan, depth, tiles, segBuf, segCount, binCount,
+                  counters, sh, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
 // 2. binScan: exclusive prefix over T*B counts (block-local + block sums)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(512) binScanBlocks(const uint32_t* __restrict__ cnt, uint32_t* __restrict__ off,
-                                                     uint32_t* __restrict__ blockSums, uint32_t n) {
-  __shared__ uint32_t warpSums[32];
-  const uint32_t base = blockIdx.x * SCAN_PER_BLOCK + threadIdx.x * 4u;
+__device__ __forceinline__ void binScanBlocksBody(const uint32_t* __restrict__ cnt, uint32_t* __restrict__ off,
+                                                  uint32_t* __restrict__ blockSums, uint32_t n, uint32_t* warpSums,
+                                                  uint32_t blk) {
+  const uint32_t base = blk * SCAN_PER_BLOCK + threadIdx.x * 4u;
   uint32_t v[4], s = 0;
 #pragma unroll
   for (int k = 0; k < 4; k++) {
@@ -482,11 +494,17 @@ __global__ void __launch_bounds__(512) binScanBlocks(const uint32_t* __restrict_
     if (base + k < n) off[base + k] = ex;
     ex += v[k];
   }
-  if (threadIdx.x == 0) blockSums[blockIdx.x] = total;
+  if (threadIdx.x == 0) blockSums[blk] = total;
 }
 
-__global__ void __launch_bounds__(1024) binScanSums(uint32_t* __restrict__ blockSums, uint32_t nBlocks) {
+__global__ void __launch_bounds__(512) binScanBlocks(const uint32_t* __restrict__ cnt, uint32_t* __restrict__ off,
+                                                     uint32_t* __restrict__ blockSums, uint32_t n) {
   __shared__ uint32_t warpSums[32];
+  binScanBlocksBody(cnt, off, blockSums, n, warpSums, blockIdx.x);
+}
+
+__device__ __forceinline__ void binScanSumsBody(uint32_t* __restrict__ blockSums, uint32_t nBlocks,
+                                                uint32_t* warpSums) {
   uint32_t carry = 0;
   for (uint32_t b0 = 0; b0 < nBlocks; b0 += blockDim.x) {
     uint32_t i = b0 + threadIdx.x;
@@ -498,21 +516,34 @@ __global__ void __launch_bounds__(1024) binScanSums(uint32_t* __restrict__ block
   }
 }
 
+__global__ void __launch_bounds__(1024) binScanSums(uint32_t* __restrict__ blockSums, uint32_t nBlocks) {
+  __shared__ uint32_t warpSums[32];
+  binScanSumsBody(blockSums, nBlocks, warpSums);
+}
+
 // ---------------------------------------------------------------------------
 // 3. binScatter: keys into CSR order (order inside a bin fixed by step 4)
 // ---------------------------------------------------------------------------
-__global__ void binScatterKernel(const uint32_t* __restrict__ segBuf, uint32_t maxDrawn,
-                                 uint32_t* __restrict__ binOffset, const uint32_t* __restrict__ blockSums,
-                                 uint32_t* __restrict__ keys, DeviceCounters* __restrict__ counters) {
+__device__ __forceinline__ void binScatterBody(const uint32_t* __restrict__ segBuf, uint32_t maxDrawn,
+                                               uint32_t* __restrict__ binOffset,
+                                               const uint32_t* __restrict__ blockSums, uint32_t* __restrict__ keys,
+                                               DeviceCounters* __restrict__ counters, uint32_t blk, uint32_t nblk) {
   const uint32_t total = segBuf[0];
   const uint32_t n = min(total, maxDrawn);
-  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&counters->tileRecords, (unsigned long long)total);
-  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+  if (blk == 0 && threadIdx.x == 0) atomicAdd(&counters->tileRecords, (unsigned long long)total);
+  for (uint32_t r = blk * blockDim.x + threadIdx.x; r < n; r += nblk * blockDim.x) {
     uint32_t ti = segBuf[1u + 2u * r];
     uint32_t key = segBuf[2u + 2u * r];
     uint32_t pos = blockSums[ti / SCAN_PER_BLOCK] + atomicAdd(&binOffset[ti], 1u);
     keys[pos] = key;
   }
+}
+
+__global__ void __launch_bounds__(256)
+binScatterKernel(const uint32_t* __restrict__ segBuf, uint32_t maxDrawn, uint32_t* __restrict__ binOffset,
+                 const uint32_t* __restrict__ blockSums, uint32_t* __restrict__ keys,
+                 DeviceCounters* __restrict__ counters) {
+  binScatterBody(segBuf, maxDrawn, binOffset, blockSums, keys, counters, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -531,14 +562,15 @@ __device__ __forceinline__ void writeList(uint32_t* __restrict__ segBuf, uint4* 
   }
 }
 
-__global__ void __launch_bounds__(256)
-binFinalizeKernel(uint32_t TB, const uint32_t* __restrict__ binCount, const uint32_t* __restrict__ binOffset,
-                  const uint32_t* __restrict__ blockSums, uint32_t* __restrict__ keys,
-                  uint32_t* __restrict__ segBuf, uint4* __restrict__ tiles, uint32_t* __restrict__ largeBins) {
-  __shared__ uint32_t smem[8][MEDIUM_BIN];
+__device__ __forceinline__ void binFinalizeBody(uint32_t TB, const uint32_t* __restrict__ binCount,
+                                                const uint32_t* __restrict__ binOffset,
+                                                const uint32_t* __restrict__ blockSums, uint32_t* __restrict__ keys,
+                                                uint32_t* __restrict__ segBuf, uint4* __restrict__ tiles,
+                                                uint32_t* __restrict__ largeBins, uint32_t (*smem)[MEDIUM_BIN],
+                                                uint32_t blk, uint32_t nblk) {
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t gw = (blk * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nw = (nblk * blockDim.x) >> 5;
   uint32_t* s = smem[warp];
   for (uint32_t ti = gw; ti < TB; ti += nw) {
     const uint32_t n = binCount[ti];
@@ -583,19 +615,28 @@ binFinalizeKernel(uint32_t TB, const uint32_t* __restrict__ binCount, const uint
   }
 }
 
+__global__ void __launch_bounds__(256)
+binFinalizeKernel(uint32_t TB, const uint32_t* __restrict__ binCount, const uint32_t* __restrict__ binOffset,
+                  const uint32_t* __restrict__ blockSums, uint32_t* __restrict__ keys,
+                  uint32_t* __restrict__ segBuf, uint4* __restrict__ tiles, uint32_t* __restrict__ largeBins) {
+  __shared__ uint32_t smem[8][MEDIUM_BIN];
+  binFinalizeBody(TB, binCount, binOffset, blockSums, keys, segBuf, tiles, largeBins, smem, blockIdx.x, gridDim.x);
+}
+
 // ---------------------------------------------------------------------------
 // 5. largeBins: one CTA per bin with > MEDIUM_BIN records.  Runs of
 //    LARGE_SMEM_KEYS are bitonic-sorted in shared memory, then merged pairwise
 //    through the bin's own list slots (free until the final write) by rank
 //    search (keys are unique).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(1024)
-largeBinsKernel(const uint32_t* __restrict__ largeBins, const uint32_t* __restrict__ binCount,
-                const uint32_t* __restrict__ binOffset, const uint32_t* __restrict__ blockSums,
-                uint32_t* __restrict__ keys, uint32_t* __restrict__ segBuf, uint4* __restrict__ tiles) {
-  extern __shared__ uint32_t sk[];
+__device__ __forceinline__ void largeBinsBody(const uint32_t* __restrict__ largeBins,
+                                              const uint32_t* __restrict__ binCount,
+                                              const uint32_t* __restrict__ binOffset,
+                                              const uint32_t* __restrict__ blockSums, uint32_t* __restrict__ keys,
+                                              uint32_t* __restrict__ segBuf, uint4* __restrict__ tiles, uint32_t* sk,
+                                              uint32_t vblk, uint32_t nvblk) {
   const uint32_t nLarge = largeBins[0];
-  for (uint32_t li = blockIdx.x; li < nLarge; li += gridDim.x) {
+  for (uint32_t li = vblk; li < nLarge; li += nvblk) {
     const uint32_t ti = largeBins[1u + li];
     const uint32_t n = binCount[ti];
     const uint32_t start = blockSums[ti / SCAN_PER_BLOCK] + binOffset[ti] - n;
@@ -652,17 +693,33 @@ largeBinsKernel(const uint32_t* __restrict__ largeBins, const uint32_t* __restri
   }
 }
 
+__global__ void __launch_bounds__(1024)
+largeBinsKernel(const uint32_t* __restrict__ largeBins, const uint32_t* __restrict__ binCount,
+                const uint32_t* __restrict__ binOffset, const uint32_t* __restrict__ blockSums,
+                uint32_t* __restrict__ keys, uint32_t* __restrict__ segBuf, uint4* __restrict__ tiles) {
+  extern __shared__ uint32_t sk[];
+  largeBinsBody(largeBins, binCount, binOffset, blockSums, keys, segBuf, tiles, sk, blockIdx.x, gridDim.x);
+}
+
 // ---------------------------------------------------------------------------
 // HairTileSortPass (count-tiles + sort) in one CTA, stable inside a bucket.
 // ---------------------------------------------------------------------------
 constexpr uint32_t SORT_MAX_BUCKETS = 256;
 
-__global__ void __launch_bounds__(1024)
-tileSortKernel(uint32_t T, uint32_t NB, uint32_t bucketSize, const uint32_t* __restrict__ segCount,
-               uint32_t* __restrict__ buckets, uint32_t* __restrict__ tileList) {
-  __shared__ uint32_t hist[SORT_MAX_BUCKETS], offs[SORT_MAX_BUCKETS], run[SORT_MAX_BUCKETS];
-  __shared__ uint32_t wcnt[32][SORT_MAX_BUCKETS];
-  __shared__ uint32_t drawn;
+struct SortShared {
+  uint32_t hist[SORT_MAX_BUCKETS], offs[SORT_MAX_BUCKETS], run[SORT_MAX_BUCKETS];
+  uint32_t wcnt[32][SORT_MAX_BUCKETS];
+  uint32_t drawn;
+};
+
+__device__ __forceinline__ void tileSortBody(uint32_t T, uint32_t NB, uint32_t bucketSize,
+                                             const uint32_t* __restrict__ segCount, uint32_t* __restrict__ buckets,
+                                             uint32_t* __restrict__ tileList, SortShared& ss) {
+  uint32_t* hist = ss.hist;
+  uint32_t* offs = ss.offs;
+  uint32_t* run = ss.run;
+  uint32_t (*wcnt)[SORT_MAX_BUCKETS] = ss.wcnt;
+  uint32_t& drawn = ss.drawn;
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   for (uint32_t b = tid; b < NB; b += blockDim.x) { hist[b] = 0; run[b] = 0; }
   if (tid == 0) drawn = 0;
@@ -718,6 +775,13 @@ tileSortKernel(uint32_t T, uint32_t NB, uint32_t bucketSize, const uint32_t* __r
     if (valid) tileList[1u + offs[b] + wcnt[warp][b] + rank] = t;
     __syncthreads();
   }
+}
+
+__global__ void __launch_bounds__(1024)
+tileSortKernel(uint32_t T, uint32_t NB, uint32_t bucketSize, const uint32_t* __restrict__ segCount,
+               uint32_t* __restrict__ buckets, uint32_t* __restrict__ tileList) {
+  __shared__ SortShared ss;
+  tileSortBody(T, NB, bucketSize, segCount, buckets, tileList, ss);
 }
 
 // ---------------------------------------------------------------------------
@@ -1497,13 +1561,13 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
 // bins, so that no single CTA carries the frame's tail.  Group sizes come
 // from the list-length hints; a tile without valid hints is not split.
 // One CTA.
-__global__ void __launch_bounds__(1024)
-fineScheduleKernel(const uint32_t* __restrict__ tileList, const uint32_t* __restrict__ segCount,
-                   const uint4* __restrict__ tiles, uint32_t T, uint32_t B, uint32_t grid, uint32_t maxDrawn,
-                   uint32_t maxProcessed, uint32_t allowSplit, FineScratch fs,
-                   DeviceCounters* __restrict__ counters) {
-  __shared__ uint32_t warpSums[32];
-  __shared__ uint32_t total;
+__device__ __forceinline__ void fineScheduleBody(const uint32_t* __restrict__ tileList,
+                                                 const uint32_t* __restrict__ segCount,
+                                                 const uint4* __restrict__ tiles, uint32_t T, uint32_t B,
+                                                 uint32_t grid, uint32_t maxDrawn, uint32_t maxProcessed,
+                                                 uint32_t allowSplit, const FineScratch& fs,
+                                                 DeviceCounters* __restrict__ counters, uint32_t* warpSums,
+                                                 uint32_t& total) {
   const uint32_t tid = threadIdx.x;
   const uint32_t drawn = min(tileList[0], T);
   if (tid == 0) total = 0;
@@ -1573,36 +1637,45 @@ fineScheduleKernel(const uint32_t* __restrict__ tileList, const uint32_t* __rest
     carrySlots += chunkSlots;
   }
   if (tid == 0) fs.hdr[0] = carryItems;
+  __syncthreads();  // total and warpSums are reused by the block's next instance
 }
 
+__global__ void __launch_bounds__(1024)
+fineScheduleKernel(const uint32_t* __restrict__ tileList, const uint32_t* __restrict__ segCount,
+                   const uint4* __restrict__ tiles, uint32_t T, uint32_t B, uint32_t grid, uint32_t maxDrawn,
+                   uint32_t maxProcessed, uint32_t allowSplit, FineScratch fs,
+                   DeviceCounters* __restrict__ counters) {
+  __shared__ uint32_t warpSums[32];
+  __shared__ uint32_t total;
+  fineScheduleBody(tileList, segCount, tiles, T, B, grid, maxDrawn, maxProcessed, allowSplit, fs, counters,
+                   warpSums, total);
+}
+
+// One work item of the fine pass: a tile, or one group of depth bins of a
+// split tile (then the last group to finish merges the tile).
 template <int TS, int MAXL>
-__global__ void __launch_bounds__(TS * TS, TS == 8 ? 6 : TS == 16 ? (MAXL <= 4 ? 3 : 2) : 1)
-fineKernel(const HfbUniforms U, const FineArgs a, const uint32_t* __restrict__ tileList, float* __restrict__ result,
-           FineScratch fs) {
+__device__ __forceinline__ void fineItem(FineSmem<TS>& sh, const HfbUniforms& U, const FineArgs a,
+                                         const uint32_t* __restrict__ tileList, float* __restrict__ result,
+                                         const FineScratch fs, const uint4 item) {
   using SM = FineSmem<TS>;
   constexpr uint32_t NT = SM::NT;
   constexpr uint32_t UNSAFE = 1u << 31;
-  extern __shared__ __align__(16) unsigned char fineSmemRaw[];
-  SM& sh = *reinterpret_cast<SM*>(fineSmemRaw);
   const uint32_t tid = threadIdx.x;
   const uint32_t lx = tid % TS, ly = tid / TS;
   const uint32_t W = f2u(U.viewport.x), H = f2u(U.viewport.y);
   const uint32_t tilesX = divCeil(W, TS), tileCount = tilesX * divCeil(H, TS);
-  const uint32_t nItems = fs.hdr[0];
-  uint32_t* queue = reinterpret_cast<uint32_t*>(result);  // tileQueueAtomicIdx, getNextTileIdx :294-303
   float4* res = reinterpret_cast<float4*>(result + 4);
-
-  while (true) {
-    if (tid == 0) sh.queueIdx = atomicAdd(queue, 1u);
-    __syncthreads();
-    const uint32_t it = sh.queueIdx;
-    if (it >= nItems) break;
-    const uint4 item = fs.items[it];
+  {
     const uint32_t tileIdx = tileList[1u + item.x];
     uint32_t b0 = item.y & 0xffu, b1 = (item.y >> 8) & 0xffu;
     const uint32_t g = (item.y >> 16) & 0xffu, nG = item.y >> 24;
-    if (tileIdx >= tileCount || b1 > a.B || b0 >= b1) { __syncthreads(); continue; }
+    if (tileIdx >= tileCount || b1 > a.B || b0 >= b1) return;
     bool split = nG > 1u, write = true;
+    if (split && (g >= nG || item.z >= fs.maxGroups || nG > fs.maxGroups - item.z)) {
+      // not an item the schedule writes: count it and leave the tile alone
+      if (tid == 0) atomicAdd(&a.counters->badWorkItems, 1ull);
+      return;
+    }
     f4 fin;
     while (true) {
       const bool ok = fineTile<TS, MAXL>(sh, U, a, tileIdx, b0, b1, split && g > 0u, fin);
@@ -1647,7 +1720,58 @@ fineKernel(const HfbUniforms U, const FineArgs a, const uint32_t* __restrict__ t
     const TileB tbp = tileBoundsPx(W, H, TS, tx, ty);
     const uint32_t px = tbp.x0 + lx, py = tbp.y0 + ly;
     if (write && px < W && py < H) res[(size_t)py * W + px] = make_float4(fin.x, fin.y, fin.z, fin.w);
+  }
+}
+
+template <int TS, int MAXL>
+__global__ void __launch_bounds__(TS * TS, TS == 8 ? 6 : TS == 16 ? (MAXL <= 4 ? 3 : 2) : 1)
+fineKernel(const HfbUniforms U, const FineArgs a, const uint32_t* __restrict__ tileList, float* __restrict__ result,
+           FineScratch fs) {
+  using SM = FineSmem<TS>;
+  extern __shared__ __align__(16) unsigned char fineSmemRaw[];
+  SM& sh = *reinterpret_cast<SM*>(fineSmemRaw);
+  const uint32_t nItems = min(fs.hdr[0], fs.maxItems);
+  uint32_t* queue = reinterpret_cast<uint32_t*>(result);  // tileQueueAtomicIdx, getNextTileIdx :294-303
+  while (true) {
+    if (threadIdx.x == 0) sh.queueIdx = atomicAdd(queue, 1u);
+    __syncthreads();
+    const uint32_t it = sh.queueIdx;
+    if (it >= nItems) break;
+    fineItem<TS, MAXL>(sh, U, a, tileList, result, fs, fs.items[it]);
     __syncthreads();  // the tile's shared state is rewritten for the next item
+  }
+}
+
+// batched: one queue over the work items of every instance
+template <int TS, int MAXL>
+__global__ void __launch_bounds__(TS * TS, TS == 8 ? 6 : TS == 16 ? (MAXL <= 4 ? 3 : 2) : 1)
+fineBatch(BatchView b, FineArgs base, HfbConfig cfgParam) {
+  using SM = FineSmem<TS>;
+  const HfbConfig cfg = cfgParam;
+  extern __shared__ __align__(16) unsigned char fineSmemRaw[];
+  SM& sh = *reinterpret_cast<SM*>(fineSmemRaw);
+  const uint32_t n = b.hdr->n;
+  const uint32_t total = b.itemPrefix[n];
+  while (true) {
+    if (threadIdx.x == 0) sh.queueIdx = atomicAdd(&b.hdr->fineQueue, 1u);
+    __syncthreads();
+    const uint32_t gi = sh.queueIdx;
+    if (gi >= total) break;
+    const uint32_t i = batchFind(b.itemPrefix, n, gi);
+    const BatchInst& I = b.insts[i];
+    FineArgs a = base;
+    a.S = I.S;
+    a.P = I.P;
+    a.pos = I.posNew;
+    a.tan = I.tan;
+    a.shading = I.shading;
+    a.depth = I.depth;
+    a.tiles = I.tiles;
+    a.segBuf = I.segBuf;
+    const FineScratch fs = fineScratchLayout(I.scratch, cfg, I.W, I.H);
+    const uint32_t li = gi - b.itemPrefix[i];
+    if (li < fs.maxItems) fineItem<TS, MAXL>(sh, I.U, a, I.tileList, I.result, fs, fs.items[li]);
+    __syncthreads();
   }
 }
 
@@ -1691,6 +1815,155 @@ cudaError_t launchFineT(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, c
   a.counters = (DeviceCounters*)c->dCounters;
   fineKernel<TS, MAXL><<<grid, TS * TS, SMEM, c->stream>>>(u, a, rb.tileList, rb.rasterizerResult, fs);
   c->launches += 2;
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Batched tiles pass, tile sort and fine pass: persistent over the virtual
+// blocks of every instance (hfb_frame_batch).
+// ---------------------------------------------------------------------------
+#define BATCH_LOOP(KIND)                                              \
+  const uint32_t n = b.hdr->n;                                        \
+  const uint32_t* row = b.prefix + (KIND) * (BATCH_MAX + 1);          \
+  const uint32_t totalVb = row[n];                                    \
+  for (uint32_t v = blockIdx.x; v < totalVb; v += gridDim.x) {        \
+    const uint32_t i = batchFind(row, n, v);                          \
+    const BatchInst& I = b.insts[i];                                  \
+    const uint32_t local = v - row[i], nLocal = row[i + 1] - row[i];  \
+    (void)nLocal; (void)local;                                        \
+    const TilesScratch ts = tilesScratchLayout(I.scratch, cfg, I.W, I.H, I.maxDrawn); \
+    (void)ts;
+
+__global__ void __launch_bounds__(TR_SEGS) tilesRasterBatch(BatchView b, HfbConfig cfgParam,
+                                                             DeviceCounters* __restrict__ counters) {
+  const HfbConfig cfg = cfgParam;
+  __shared__ TrShared sh;
+  BATCH_LOOP(BK_RASTER)
+    tilesRasterBody(I.U, I.P, min(I.strandsToRender, I.S), cfg.tileSize, cfg.tileDepthBins,
+                    cfg.invalidTilesPerSegmentThreshold, I.bsphere, I.posNew, I.tan, I.depth, I.tiles, I.segBuf,
+                    I.segCount, ts.binCount, counters, sh, local);
+  }
+}
+
+__global__ void __launch_bounds__(512) binScanBatch(BatchView b, HfbConfig cfgParam) {
+  const HfbConfig cfg = cfgParam;
+  __shared__ uint32_t warpSums[32];
+  BATCH_LOOP(BK_SCAN)
+    binScanBlocksBody(ts.binCount, ts.binOffset, ts.blockSums, I.T * cfg.tileDepthBins, warpSums, local);
+  }
+}
+
+__global__ void __launch_bounds__(1024) binScanSumsBatch(BatchView b, HfbConfig cfgParam) {
+  const HfbConfig cfg = cfgParam;
+  __shared__ uint32_t warpSums[32];
+  BATCH_LOOP(BK_SCAN_SUMS)
+    binScanSumsBody(ts.blockSums, divCeil(I.T * cfg.tileDepthBins, SCAN_PER_BLOCK), warpSums);
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(256) binScatterBatch(BatchView b, HfbConfig cfgParam,
+                                                        DeviceCounters* __restrict__ counters) {
+  const HfbConfig cfg = cfgParam;
+  BATCH_LOOP(BK_SCATTER)
+    binScatterBody(I.segBuf, I.maxDrawn, ts.binOffset, ts.blockSums, ts.keys, counters, local, nLocal);
+  }
+}
+
+__global__ void __launch_bounds__(256) binFinalizeBatch(BatchView b, HfbConfig cfgParam) {
+  const HfbConfig cfg = cfgParam;
+  __shared__ uint32_t smem[8][MEDIUM_BIN];
+  BATCH_LOOP(BK_FINALIZE)
+    binFinalizeBody(I.T * cfg.tileDepthBins, ts.binCount, ts.binOffset, ts.blockSums, ts.keys, I.segBuf, I.tiles,
+                    ts.largeBins, smem, local, nLocal);
+  }
+}
+
+__global__ void __launch_bounds__(1024) largeBinsBatch(BatchView b, HfbConfig cfgParam) {
+  const HfbConfig cfg = cfgParam;
+  extern __shared__ uint32_t sk[];
+  BATCH_LOOP(BK_LARGE)
+    largeBinsBody(ts.largeBins, ts.binCount, ts.binOffset, ts.blockSums, ts.keys, I.segBuf, I.tiles, sk, local,
+                  nLocal);
+  }
+}
+
+__global__ void __launch_bounds__(1024) tileSortBatch(BatchView b, HfbConfig cfgParam) {
+  const HfbConfig cfg = cfgParam;
+  __shared__ SortShared ss;
+  BATCH_LOOP(BK_SORT)
+    tileSortBody(I.T, cfg.sortBuckets, cfg.sortBucketSize, I.segCount, I.sortBuckets, I.tileList, ss);
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(1024) fineScheduleBatch(BatchView b, HfbConfig cfgParam, uint32_t grid,
+                                                          DeviceCounters* __restrict__ counters) {
+  const HfbConfig cfg = cfgParam;
+  __shared__ uint32_t warpSums[32];
+  __shared__ uint32_t totalRecords;
+  BATCH_LOOP(BK_SCHEDULE)
+    const FineScratch fs = fineScratchLayout(I.scratch, cfg, I.W, I.H);
+    const uint32_t dispMode = I.U.displayMode & 0xffu;
+    const bool dbg = dispMode == 4u && ((I.U.displayMode >> 8) & 0xffffu) != 0u;
+    fineScheduleBody(I.tileList, I.segCount, I.tiles, I.T, cfg.tileDepthBins, grid, I.maxDrawn, I.S * I.P,
+                     dbg ? 0u : 1u, fs, counters, warpSums, totalRecords);
+  }
+}
+
+// Exclusive prefix of the instances' work items; resets the batch queue.
+__global__ void __launch_bounds__(1024) fineItemPrefixBatch(BatchView b, HfbConfig cfgParam) {
+  const HfbConfig cfg = cfgParam;
+  __shared__ uint32_t warpSums[32];
+  const uint32_t n = b.hdr->n;
+  uint32_t carry = 0;
+  for (uint32_t i0 = 0; i0 < n; i0 += blockDim.x) {
+    const uint32_t i = i0 + threadIdx.x;
+    uint32_t items = 0;
+    if (i < n) {
+      const BatchInst& I = b.insts[i];
+      items = fineScratchLayout(I.scratch, cfg, I.W, I.H).hdr[0];
+    }
+    uint32_t chunk;
+    const uint32_t ex = blockExclusiveScan(items, warpSums, chunk);
+    if (i < n) b.itemPrefix[i] = carry + ex;
+    carry += chunk;
+  }
+  if (threadIdx.x == 0) {
+    b.itemPrefix[n] = carry;
+    b.hdr->fineQueue = 0;
+  }
+}
+#undef BATCH_LOOP
+
+template <int TS, int MAXL>
+cudaError_t launchFineBatchT(HfbCtx* c, const BatchView& b) {
+  const HfbConfig& cfg = c->cfg;
+  constexpr size_t SMEM = sizeof(FineSmem<TS>);
+  uint32_t& grid = c->batchGrid[BK_COUNT];  // the fine kernel's persistent grid
+  if (!grid) {
+    cudaError_t e = cudaFuncSetAttribute(fineBatch<TS, MAXL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);
+    int per = 0;
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fineBatch<TS, MAXL>, TS * TS, SMEM);
+    if (e != cudaSuccess) return e;
+    if (per < 1) return cudaErrorInvalidConfiguration;
+    grid = cfg.processorCount ? cfg.processorCount : (uint32_t)per * c->smCount;
+  }
+  DeviceCounters* dc = (DeviceCounters*)c->dCounters;
+  uint32_t& sgrid = c->batchGrid[BK_SCHEDULE];
+  if (!sgrid) sgrid = c->smCount;
+  fineScheduleBatch<<<sgrid, 1024, 0, c->stream>>>(b, cfg, grid, dc);
+  fineItemPrefixBatch<<<1, 1024, 0, c->stream>>>(b, cfg);
+  FineArgs a{};
+  a.B = cfg.tileDepthBins;
+  a.L = cfg.slicesPerPixel;
+  a.SP = cfg.shadingPoints;
+  a.CAP = cfg.avgFragmentsPerSlice * cfg.slicesPerPixel * cfg.tileSize * cfg.tileSize;
+  a.alphaQuadratic = cfg.alphaQuadratic;
+  a.alphaMul = cfg.alphaMultiplier;
+  a.counters = dc;
+  fineBatch<TS, MAXL><<<grid, TS * TS, SMEM, c->stream>>>(b, a, cfg);
+  c->launches += 3;
   return cudaGetLastError();
 }
 
@@ -1759,6 +2032,63 @@ cudaError_t launchFinePass(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h
   if (L <= 4) return launchFineT<32, 4>(c, u, h, pos, tan, shading, depth, rb);
   if (L <= 8) return launchFineT<32, 8>(c, u, h, pos, tan, shading, depth, rb);
   return cudaErrorInvalidValue;  // 32x32 tiles with more than 8 slices: too many registers per pixel
+}
+
+}  // namespace hfb
+
+namespace hfb {
+
+cudaError_t launchBatchTiles(HfbCtx* c, const BatchView& b) {
+  const HfbConfig& cfg = c->cfg;
+  DeviceCounters* dc = (DeviceCounters*)c->dCounters;
+  uint32_t* g = c->batchGrid;
+  if (!g[BK_RASTER]) {
+    int per = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, tilesRasterBatch, TR_SEGS, 0);
+    if (e != cudaSuccess) return e;
+    g[BK_RASTER] = (uint32_t)(per > 0 ? per : 1) * c->smCount;
+    g[BK_SCAN] = c->smCount * 4u;
+    g[BK_SCAN_SUMS] = c->smCount;
+    g[BK_SCATTER] = c->smCount * 8u;
+    g[BK_FINALIZE] = c->smCount * 8u;
+    g[BK_LARGE] = c->smCount;
+    e = cudaFuncSetAttribute(largeBinsBatch, cudaFuncAttributeMaxDynamicSharedMemorySize, LARGE_SMEM_KEYS * 4);
+    if (e != cudaSuccess) return e;
+  }
+  tilesRasterBatch<<<g[BK_RASTER], TR_SEGS, 0, c->stream>>>(b, cfg, dc);
+  binScanBatch<<<g[BK_SCAN], 512, 0, c->stream>>>(b, cfg);
+  binScanSumsBatch<<<g[BK_SCAN_SUMS], 1024, 0, c->stream>>>(b, cfg);
+  binScatterBatch<<<g[BK_SCATTER], 256, 0, c->stream>>>(b, cfg, dc);
+  binFinalizeBatch<<<g[BK_FINALIZE], 256, 0, c->stream>>>(b, cfg);
+  largeBinsBatch<<<g[BK_LARGE], 1024, LARGE_SMEM_KEYS * 4, c->stream>>>(b, cfg);
+  c->launches += 6;
+  return cudaGetLastError();
+}
+
+cudaError_t launchBatchSort(HfbCtx* c, const BatchView& b) {
+  if (c->cfg.sortBuckets > SORT_MAX_BUCKETS) return cudaErrorInvalidValue;
+  uint32_t& grid = c->batchGrid[BK_SORT];
+  if (!grid) grid = c->smCount;
+  tileSortBatch<<<grid, 1024, 0, c->stream>>>(b, c->cfg);
+  c->launches += 1;
+  return cudaGetLastError();
+}
+
+cudaError_t launchBatchFine(HfbCtx* c, const BatchView& b) {
+  const uint32_t TS = c->cfg.tileSize, L = c->cfg.slicesPerPixel;
+  if (TS == 8) {
+    if (L <= 4) return launchFineBatchT<8, 4>(c, b);
+    if (L <= 8) return launchFineBatchT<8, 8>(c, b);
+    return launchFineBatchT<8, 16>(c, b);
+  }
+  if (TS == 16) {
+    if (L <= 4) return launchFineBatchT<16, 4>(c, b);
+    if (L <= 8) return launchFineBatchT<16, 8>(c, b);
+    return launchFineBatchT<16, 16>(c, b);
+  }
+  if (L <= 4) return launchFineBatchT<32, 4>(c, b);
+  if (L <= 8) return launchFineBatchT<32, 8>(c, b);
+  return cudaErrorInvalidValue;
 }
 
 }  // namespace hfb

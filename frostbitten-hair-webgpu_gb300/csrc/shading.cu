@@ -139,12 +139,12 @@ __device__ __forceinline__ float linearizeDepth(float n, float f, float d) {
   return fmul(n, f) / fadd(f, fmul(fsub(n, f), d));
 }
 
-__global__ void shadingKernel(const HfbUniforms U, uint32_t S, uint32_t P, uint32_t SP, float zNear, float zFar,
-                              const float4* __restrict__ pos, const float4* __restrict__ tan,
-                              const float* __restrict__ depth, const float* __restrict__ ao, uint32_t aoW,
-                              uint32_t aoH, const float* __restrict__ sm, uint32_t smSize,
-                              float4* __restrict__ shading) {
-  uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void shadingBody(const HfbUniforms& U, uint32_t S, uint32_t P, uint32_t SP, float zNear,
+                                            float zFar, const float4* __restrict__ pos,
+                                            const float4* __restrict__ tan, const float* __restrict__ depth,
+                                            const float* __restrict__ ao, uint32_t aoW, uint32_t aoH,
+                                            const float* __restrict__ sm, uint32_t smSize,
+                                            float4* __restrict__ shading, uint32_t gid) {
   if (gid >= S * SP) return;
   uint32_t strand = gid / SP, sp = gid - strand * SP;
   f2 vp = mk2(U.viewport.x, U.viewport.y);
@@ -211,6 +211,28 @@ __global__ void shadingKernel(const HfbUniforms U, uint32_t S, uint32_t P, uint3
   shading[gid] = make_float4(sum.x, sum.y, sum.z, alpha);  // _setShadingPoint
 }
 
+__global__ void __launch_bounds__(128)
+shadingKernel(const HfbUniforms U, uint32_t S, uint32_t P, uint32_t SP, float zNear, float zFar,
+              const float4* __restrict__ pos, const float4* __restrict__ tan, const float* __restrict__ depth,
+              const float* __restrict__ ao, uint32_t aoW, uint32_t aoH, const float* __restrict__ sm,
+              uint32_t smSize, float4* __restrict__ shading) {
+  shadingBody(U, S, P, SP, zNear, zFar, pos, tan, depth, ao, aoW, aoH, sm, smSize, shading,
+              blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// batched: persistent over the virtual blocks of every instance
+__global__ void __launch_bounds__(128) shadingBatch(BatchView b, uint32_t SP, float zNear, float zFar) {
+  const uint32_t n = b.hdr->n;
+  const uint32_t* row = b.prefix + BK_SHADING * (BATCH_MAX + 1);
+  const uint32_t total = row[n];
+  for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
+    const uint32_t i = batchFind(row, n, v);
+    const BatchInst& I = b.insts[i];
+    shadingBody(I.U, I.S, I.P, SP, zNear, zFar, I.posNew, I.tan, I.shadingDepth, I.ao, I.aoW, I.aoH, I.sm,
+                I.smSize, I.shading, (v - row[i]) * 128u + threadIdx.x);
+  }
+}
+
 }  // namespace
 
 cudaError_t launchShading(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, const float* pos,
@@ -226,4 +248,14 @@ cudaError_t launchShading(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h,
   return cudaGetLastError();
 }
 
+}  // namespace hfb
+
+namespace hfb {
+cudaError_t launchBatchShading(HfbCtx* c, const BatchView& b) {
+  uint32_t& grid = c->batchGrid[BK_SHADING];
+  if (!grid) grid = c->smCount * 16u;
+  shadingBatch<<<grid, 128, 0, c->stream>>>(b, c->cfg.shadingPoints, c->cfg.cameraNear, c->cfg.cameraFar);
+  c->launches += 1;
+  return cudaGetLastError();
+}
 }  // namespace hfb

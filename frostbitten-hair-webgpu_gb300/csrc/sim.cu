@@ -79,9 +79,9 @@ __device__ __forceinline__ f3 gridMax(const HfbSimUniforms& u) {
 // ---------------------------------------------------------------------------
 // GridPreSimPass.main, gridPreSimPass.wgsl.ts:38-159 (one thread per node)
 // ---------------------------------------------------------------------------
-__global__ void gridPreSimKernel(const HfbSimUniforms u, uint32_t G, const int4* __restrict__ dv,
-                                 float4* __restrict__ gw, const float* __restrict__ sdf, uint32_t D) {
-  uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void gridPreSimBody(const HfbSimUniforms& u, uint32_t G, const int4* __restrict__ dv,
+                                               float4* __restrict__ gw, const float* __restrict__ sdf, uint32_t D,
+                                               uint32_t id) {
   if (id >= G * G * G) return;
   uint32_t z = id / (G * G);
   uint32_t idXY = id - z * G * G;
@@ -124,6 +124,12 @@ __global__ void gridPreSimKernel(const HfbSimUniforms u, uint32_t G, const int4*
   gw[idx0] = make_float4(g.x, g.y, g.z, wind);
 }
 
+__global__ void __launch_bounds__(256) gridPreSimKernel(const HfbSimUniforms u, uint32_t G, const int4* __restrict__ dv,
+                                                        float4* __restrict__ gw, const float* __restrict__ sdf,
+                                                        uint32_t D) {
+  gridPreSimBody(u, G, dv, gw, sdf, D, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 // ---------------------------------------------------------------------------
 // HairSimIntegrationPass.main, hairSimIntegrationPass.wgsl.ts:79-273
 //
@@ -139,14 +145,6 @@ __global__ void gridPreSimKernel(const HfbSimUniforms u, uint32_t G, const int4*
 // ---------------------------------------------------------------------------
 constexpr uint32_t SIM_THREADS = 256;
 
-// Strands per block for P points per strand: one chain warp per block for
-// P <= 32, fewer strands for longer strands (shared memory ~38 KB).
-__host__ __device__ inline uint32_t simStrandsPerBlock(uint32_t P) {
-  return P <= 32u ? 32u : max(8u, 1024u / P);
-}
-__host__ __device__ inline size_t simSmemBytes(uint32_t P) {
-  return (size_t)simStrandsPerBlock(P) * (P + 1u) * (2u * sizeof(float4) + sizeof(float));
-}
 
 // Verlet step of one point with the grid forces (:125-162, integration.wgsl.ts:8-28)
 __device__ __forceinline__ float4 verletPoint(const HfbSimUniforms& u, uint32_t G, f3 gmin, f3 gmax,
@@ -188,20 +186,19 @@ __device__ __forceinline__ float4 verletPoint(const HfbSimUniforms& u, uint32_t 
   return make_float4(r.x, r.y, r.z, posNow.w);
 }
 
-__global__ void __launch_bounds__(SIM_THREADS)
-simIntegrateKernel(const HfbSimUniforms u, uint32_t S, uint32_t P, uint32_t G,
-                   float4* __restrict__ prev, const float4* __restrict__ now,
-                   const float4* __restrict__ initial, const float* __restrict__ segLen,
-                   const int4* __restrict__ dv, const float4* __restrict__ gw,
-                   const float* __restrict__ sdf, uint32_t D) {
-  extern __shared__ float4 simSmem[];
+__device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32_t S, uint32_t P, uint32_t G,
+                                                 float4* __restrict__ prev, const float4* __restrict__ now,
+                                                 const float4* __restrict__ initial, const float* __restrict__ segLen,
+                                                 const int4* __restrict__ dv, const float4* __restrict__ gw,
+                                                 const float* __restrict__ sdf, uint32_t D, float4* simSmem,
+                                                 uint32_t blk) {
   const uint32_t NB = simStrandsPerBlock(P), R = P + 1u;  // row stride (padded)
   float4* wk = simSmem;                                   // [NB][R] positions
   float4* lc = wk + NB * R;  // [NB][R] triangle-bending constants (h0, w0, w1, w2) of the triplet at j,
                              // or the initial tangent into j for the points matchInitialTangent moves
   float* sl = reinterpret_cast<float*>(lc + NB * R);  // [NB][R] segment lengths
   const uint32_t tid = threadIdx.x;
-  const uint32_t s0 = blockIdx.x * NB;
+  const uint32_t s0 = blk * NB;
   const uint32_t nStr = min(NB, S - s0);
   const uint32_t nPts = nStr * P;
   const f3 gmin = gridMin(u), gmax = gridMax(u);
@@ -356,6 +353,17 @@ simIntegrateKernel(const HfbSimUniforms u, uint32_t S, uint32_t P, uint32_t G,
     const uint32_t ls = i / P, pt = i - ls * P;
     prev[(size_t)s0 * P + i] = wk[ls * R + pt];
   }
+  __syncthreads();  // the block's staging is reused by its next strands
+}
+
+__global__ void __launch_bounds__(SIM_THREADS)
+simIntegrateKernel(const HfbSimUniforms u, uint32_t S, uint32_t P, uint32_t G,
+                   float4* __restrict__ prev, const float4* __restrict__ now,
+                   const float4* __restrict__ initial, const float* __restrict__ segLen,
+                   const int4* __restrict__ dv, const float4* __restrict__ gw,
+                   const float* __restrict__ sdf, uint32_t D) {
+  extern __shared__ float4 simSmem[];
+  simIntegrateBody(u, S, P, G, prev, now, initial, segLen, dv, gw, sdf, D, simSmem, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -363,10 +371,9 @@ simIntegrateKernel(const HfbSimUniforms u, uint32_t S, uint32_t P, uint32_t G,
 // _addGridDensityVelocity, densityVelocityGrid.wgsl.ts:93-124.
 // One thread per point; i32 atomics (wrapping, order-independent).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256)
-gridPostSimKernel(const HfbSimUniforms u, uint32_t N, uint32_t G, const float4* __restrict__ prev,
-                  const float4* __restrict__ now, unsigned* __restrict__ dv) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void gridPostSimBody(const HfbSimUniforms& u, uint32_t N, uint32_t G,
+                                                const float4* __restrict__ prev, const float4* __restrict__ now,
+                                                unsigned* __restrict__ dv, uint32_t i) {
   const bool valid = i < N;
   float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
   if (valid) { a = __ldg(&prev[i]); b = __ldg(&now[i]); }
@@ -389,6 +396,56 @@ gridPostSimKernel(const HfbSimUniforms u, uint32_t N, uint32_t G, const float4* 
     atomicAdd(c + 2, (unsigned)gridEncode(cv.z));
     atomicAdd(c + 3, (unsigned)gridEncode(len3(w)));
   }
+}
+
+__global__ void __launch_bounds__(256)
+gridPostSimKernel(const HfbSimUniforms u, uint32_t N, uint32_t G, const float4* __restrict__ prev,
+                  const float4* __restrict__ now, unsigned* __restrict__ dv) {
+  gridPostSimBody(u, N, G, prev, now, dv, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// ---- batched: persistent over the virtual blocks of every instance ----
+__global__ void __launch_bounds__(256) gridPreSimBatch(BatchView b, uint32_t G) {
+  const uint32_t n = b.hdr->n;
+  const uint32_t* row = b.prefix + BK_GRID_PRE * (BATCH_MAX + 1);
+  const uint32_t total = row[n];
+  for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
+    const uint32_t i = batchFind(row, n, v);
+    const BatchInst& I = b.insts[i];
+    gridPreSimBody(I.SU, G, I.dv, I.gw, I.sdf, I.sdfDims, (v - row[i]) * 256u + threadIdx.x);
+  }
+}
+
+__global__ void __launch_bounds__(SIM_THREADS) simIntegrateBatch(BatchView b, uint32_t G) {
+  extern __shared__ float4 simSmem[];
+  const uint32_t n = b.hdr->n;
+  const uint32_t* row = b.prefix + BK_INTEGRATE * (BATCH_MAX + 1);
+  const uint32_t total = row[n];
+  for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
+    const uint32_t i = batchFind(row, n, v);
+    const BatchInst& I = b.insts[i];
+    // integration reads positions[1 - current] (prev) and [current] (now), writes the former
+    simIntegrateBody(I.SU, I.S, I.P, G, I.posNew, I.posOld, I.initial, I.segLen, I.dv, I.gw, I.sdf, I.sdfDims,
+                     simSmem, v - row[i]);
+  }
+}
+
+__global__ void __launch_bounds__(256) gridPostSimBatch(BatchView b, uint32_t G) {
+  const uint32_t n = b.hdr->n;
+  const uint32_t* row = b.prefix + BK_GRID_POST * (BATCH_MAX + 1);
+  const uint32_t total = row[n];
+  for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
+    const uint32_t i = batchFind(row, n, v);
+    const BatchInst& I = b.insts[i];
+    // after the swap: prev = the old current positions, now = the new ones
+    gridPostSimBody(I.SU, I.S * I.P, G, I.posOld, I.posNew, (unsigned*)I.dv, (v - row[i]) * 256u + threadIdx.x);
+  }
+}
+
+size_t simSmemMax() {
+  size_t m = 0;
+  for (uint32_t P = 4; P <= 128; P++) m = m > simSmemBytes(P) ? m : simSmemBytes(P);
+  return m;
 }
 
 }  // namespace
@@ -416,6 +473,33 @@ cudaError_t launchSimIntegrate(HfbCtx* c, const HfbSimUniforms& u, const HfbHair
   simIntegrateKernel<<<divCeil(S, simStrandsPerBlock(P)), SIM_THREADS, smem, c->stream>>>(
       u, S, P, c->cfg.gridDims, (float4*)prev, (const float4*)now, (const float4*)initial, segLen,
       (const int4*)dv, (const float4*)gw, sdf, sdfDims);
+  c->launches += 1;
+  return cudaGetLastError();
+}
+
+cudaError_t launchBatchSim(HfbCtx* c, const BatchView& b, BatchKind k) {
+  const uint32_t G = c->cfg.gridDims;
+  uint32_t& grid = c->batchGrid[k];
+  if (k == BK_GRID_PRE) {
+    if (!grid) grid = c->smCount * 8u;
+    gridPreSimBatch<<<grid, 256, 0, c->stream>>>(b, G);
+  } else if (k == BK_INTEGRATE) {
+    const size_t smem = simSmemMax();
+    if (!grid) {
+      cudaError_t e = cudaFuncSetAttribute(simIntegrateBatch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      int perSM = 0;
+      if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, simIntegrateBatch, SIM_THREADS, smem);
+      if (e != cudaSuccess) return e;
+      grid = (uint32_t)(perSM > 0 ? perSM : 1) * c->smCount;
+    }
+    simIntegrateBatch<<<grid, SIM_THREADS, smem, c->stream>>>(b, G);
+  } else if (k == BK_GRID_POST) {
+    if (!grid) grid = c->smCount * 8u;
+    gridPostSimBatch<<<grid, 256, 0, c->stream>>>(b, G);
+  } else {
+    return cudaErrorInvalidValue;
+  }
   c->launches += 1;
   return cudaGetLastError();
 }

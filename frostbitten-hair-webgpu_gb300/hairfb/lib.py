@@ -41,15 +41,29 @@ class HfbRasterBuffers(ctypes.Structure):
                 ("scratch", ctypes.c_void_p), ("scratchBytes", ctypes.c_size_t)]
 
 
+class HfbInstance(ctypes.Structure):
+    """One hair instance of a frame (hfb_frame / hfb_frame_batch)."""
+    _fields_ = [("uniforms", ctypes.c_void_p), ("simUniforms", ctypes.c_void_p), ("hair", HfbHairData),
+                ("positions", ctypes.c_void_p * 2), ("current", ctypes.c_uint32),
+                ("strandsToRender", ctypes.c_uint32), ("positionsInitial", ctypes.c_void_p),
+                ("tangents", ctypes.c_void_p), ("segmentLengths", ctypes.c_void_p),
+                ("densityVelocity", ctypes.c_void_p), ("densityGradWind", ctypes.c_void_p),
+                ("sdf", ctypes.c_void_p), ("sdfDims", ctypes.c_uint32), ("shadowMapSize", ctypes.c_uint32),
+                ("shading", ctypes.c_void_p), ("sceneDepth", ctypes.c_void_p), ("shadingDepth", ctypes.c_void_p),
+                ("ao", ctypes.c_void_p), ("aoWidth", ctypes.c_uint32), ("aoHeight", ctypes.c_uint32),
+                ("shadowMap", ctypes.c_void_p), ("raster", HfbRasterBuffers)]
+
+
 class HfbCounters(ctypes.Structure):
     _fields_ = [("tileRecords", ctypes.c_uint64), ("tileRecordsDropped", ctypes.c_uint64),
                 ("finePoolFullBins", ctypes.c_uint64), ("waitTimeouts", ctypes.c_uint64),
                 ("launches", ctypes.c_uint64), ("fineSplitTiles", ctypes.c_uint64),
-                ("fineSplitRedone", ctypes.c_uint64), ("reserved", ctypes.c_uint64 * 1)]
+                ("fineSplitRedone", ctypes.c_uint64), ("badWorkItems", ctypes.c_uint64)]
 
 
 assert ctypes.sizeof(HfbHairData) == 32
 assert ctypes.sizeof(HfbCounters) == 64
+assert ctypes.sizeof(HfbInstance) == 256
 
 # every symbol include/hairfb.h declares: name -> (restype, argtypes)
 P, U32, SZ, I = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_size_t, ctypes.c_int
@@ -78,6 +92,8 @@ SIGNATURES = {
     "hfb_tile_sort": (I, [P, P]),
     "hfb_fine_pass": (I, [P, P, P, P, P, P, P, P]),
     "hfb_tiles_pass_noalloc": (I, [P, P, P, P, P, P, U32, P]),
+    "hfb_frame": (I, [P, P]),
+    "hfb_frame_batch": (I, [P, P, U32]),
 }
 
 _lock = threading.Lock()

@@ -13,11 +13,13 @@ attenuation, AO and shadow map textures).
 """
 from __future__ import annotations
 
+import ctypes
+
 import torch
 
 from . import synthetic, uniforms as UN
 from .config import HairConfig
-from .lib import Context
+from .lib import Context, HfbInstance, ptr
 from .passes import (GridPostSimPass, GridPreSimPass, HairFinePass, HairObject, HairShadingPass,
                      HairSimIntegrationPass, HairTileSortPass, HairTilesPass, PhysicsGrids,
                      RasterBuffers, SdfCollider, clear_before_render)
@@ -74,7 +76,68 @@ class Renderer:
         self.shading.cmd_compute_shading_points(self.uniforms, self.hair, self.shading_depth)
 
     def frame(self) -> None:
-        """cmdRender, renderer.ts:171-210 (hair passes only)."""
+        """cmdRender, renderer.ts:171-210 (hair passes only), pass by pass."""
         self.simulate()
         self.draw()
         self.frame_idx += 1
+
+    # ---- whole frames through hfb_frame / hfb_frame_batch ----
+    def instance(self) -> HfbInstance:
+        """This frame's HfbInstance; the uniform bytes it points to stay
+        alive on the renderer until the next call."""
+        self._u_buf = ctypes.create_string_buffer(self.uniforms, len(self.uniforms))
+        su = self.sim_uniforms(self.frame_idx)
+        self._su_buf = ctypes.create_string_buffer(su, len(su))
+        h = self.hair
+        inst = HfbInstance()
+        inst.uniforms = ctypes.addressof(self._u_buf)
+        inst.simUniforms = ctypes.addressof(self._su_buf)
+        inst.hair = h.hair_data
+        inst.positions[0] = ptr(h.positions_0)
+        inst.positions[1] = ptr(h.positions_1)
+        inst.current = h._current
+        inst.strandsToRender = h.rendered_strand_count()
+        inst.positionsInitial = ptr(h.initial)
+        inst.tangents = ptr(h.tangents)
+        inst.segmentLengths = ptr(h.segment_lengths)
+        inst.densityVelocity = ptr(self.grids.density_velocity)
+        inst.densityGradWind = ptr(self.grids.density_grad_wind)
+        inst.sdf = ptr(self.sdf.texture)
+        inst.sdfDims = self.sdf.dims
+        inst.shading = ptr(h.shading)
+        inst.sceneDepth = ptr(self.scene_depth)
+        inst.shadingDepth = ptr(self.shading_depth)
+        inst.raster = self.rb.rb
+        return inst
+
+    def after_native_frame(self, inst: HfbInstance) -> None:
+        self.hair._current = inst.current
+        self.frame_idx += 1
+
+    def frame_native(self) -> None:
+        """One frame through hfb_frame (the same passes, one C call)."""
+        inst = self.instance()
+        self.ctx.call("hfb_frame", ctypes.byref(inst))
+        self.after_native_frame(inst)
+
+
+class BatchRenderer:
+    """Many hair instances, one hfb_frame_batch call per frame.  Every
+    renderer must share the batch's context (its config applies to all)."""
+
+    def __init__(self, renderers: list[Renderer]):
+        assert renderers, "empty batch"
+        self.ctx = renderers[0].ctx
+        assert all(r.ctx is self.ctx for r in renderers), "a batch shares one context"
+        self.renderers = renderers
+
+    def before_first_frame(self) -> None:
+        for r in self.renderers:
+            r.before_first_frame()
+
+    def frame(self) -> None:
+        n = len(self.renderers)
+        arr = (HfbInstance * n)(*[r.instance() for r in self.renderers])
+        self.ctx.call("hfb_frame_batch", arr, n)
+        for r, inst in zip(self.renderers, arr):
+            r.after_native_frame(inst)

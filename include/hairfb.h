@@ -169,7 +169,7 @@ typedef struct HfbCounters {
   uint64_t launches;           /* kernels launched by the library */
   uint64_t fineSplitTiles;     /* fine pass: tiles split into groups of depth bins across CTAs */
   uint64_t fineSplitRedone;    /* fine pass: split tiles redone in order (a later group could fill a pool) */
-  uint64_t reserved[1];
+  uint64_t badWorkItems;       /* fine-pass work items that failed their bounds checks (0 expected) */
 } HfbCounters;
 
 typedef struct HfbCtx HfbCtx;
@@ -264,6 +264,55 @@ HFB_API int hfb_fine_pass(HfbCtx* ctx, const HfbUniforms* u, const HfbHairData* 
                   const float* tangents, const float* shading, const float* depth,
                   HfbRasterBuffers* rb);
 
+/* ---- whole frames (src/renderer.ts:171-295 order) -------------------------- */
+
+/* One hair instance of a frame: its resident buffers and this frame's
+ * uniforms.  A frame runs, in the reference's order, GridPreSimPass,
+ * HairSimIntegrationPass (then the position swap), GridPostSimPass, the
+ * raster clears, HairTilesPass, HairTileSortPass, HairFinePass and
+ * HairShadingPass (whose result the next frame samples). */
+typedef struct HfbInstance {
+  const HfbUniforms* uniforms;        /* host, read during the call */
+  const HfbSimUniforms* simUniforms;  /* host, read during the call */
+  HfbHairData hair;
+  /* tick-tock positions (vec4f, .w = isMovable): positions[current] is
+   * "now", the other "prev" (hairPointsPositionsBuffer.ts).  Integration
+   * writes the new positions over "prev" and the frame flips `current`
+   * (HairObject.swapPositionBuffersAfterSimIntegration). */
+  float* positions[2];
+  uint32_t current;
+  uint32_t strandsToRender;           /* LOD: strands drawn by the tiles pass */
+  const float* positionsInitial;
+  const float* tangents;
+  const float* segmentLengths;
+  int32_t* densityVelocity;           /* G^3 {i32 vx, vy, vz, density} */
+  float* densityGradWind;             /* G^3 {vec3f grad, f32 wind} */
+  const float* sdf;
+  uint32_t sdfDims;
+  uint32_t shadowMapSize;
+  float* shading;                     /* S*SP vec4f */
+  const float* sceneDepth;            /* W*H f32: tiles / fine depth tests */
+  const float* shadingDepth;          /* W*H f32: shading attenuation; NULL = sceneDepth */
+  const float* ao;                    /* NULL = unoccluded */
+  uint32_t aoWidth, aoHeight;
+  const float* shadowMap;             /* NULL = unshadowed */
+  HfbRasterBuffers raster;            /* from hfb_raster_buffers_alloc */
+} HfbInstance;
+
+/* One frame of one instance (the per-pass entries above, in order). */
+HFB_API int hfb_frame(HfbCtx* ctx, HfbInstance* instance);
+
+/* No single counterpart in the reference, which renders one hair object per
+ * frame.  One frame of n instances of uneven strand counts, points per
+ * strand and viewports: every pass runs as one persistent launch over all
+ * instances (instance-offset tables in device memory), the launch sequence
+ * is a CUDA graph captured once per context, and the fine pass pulls the
+ * tiles of all instances from one queue.  The context's config (tile size,
+ * depth bins, slices, grid size) applies to every instance.  Results are
+ * those of hfb_frame on each instance alone.  The call flips every
+ * instance's `current`.  n <= 1024. */
+HFB_API int hfb_frame_batch(HfbCtx* ctx, HfbInstance* instances, uint32_t n);
+
 /* No counterpart in the reference.  hfb_tiles_pass for callers that cannot
  * allocate device memory (a render thread that must not take cudaMalloc's
  * device-wide synchronisation, a host whose allocator owns every device
@@ -290,11 +339,13 @@ static_assert(sizeof(HfbConfig) == 64, "HfbConfig layout");
 static_assert(sizeof(HfbHairData) == 32, "HfbHairData layout");
 static_assert(sizeof(HfbUniforms) == 1184, "Uniforms layout");
 static_assert(sizeof(HfbSimUniforms) == 304, "SimulationUniforms layout");
+static_assert(sizeof(HfbInstance) == 256, "HfbInstance layout");
 #else
 _Static_assert(sizeof(HfbConfig) == 64, "HfbConfig layout");
 _Static_assert(sizeof(HfbHairData) == 32, "HfbHairData layout");
 _Static_assert(sizeof(HfbUniforms) == 1184, "Uniforms layout");
 _Static_assert(sizeof(HfbSimUniforms) == 304, "SimulationUniforms layout");
+_Static_assert(sizeof(HfbInstance) == 256, "HfbInstance layout");
 #endif
 
 #endif /* HAIRFB_H */

@@ -1,0 +1,112 @@
+"""Whole frames: hfb_frame (one instance, one call) and hfb_frame_batch (many
+instances, one persistent launch per pass, replayed as a captured CUDA
+graph) against the pass-by-pass path on the same instances.
+
+Bars: positions, density grid, tile counts, per-bin depth bounds, lists and
+the tile list bit-exact (the batched kernels run the same arithmetic);
+shading within 1e-6; pixels within 1/255 (the fine pass may split a heavy
+tile differently when its CTA count differs).
+"""
+
+import numpy as np
+import pytest
+
+from helpers import walk_lists
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+from hairfb import synthetic  # noqa: E402
+from hairfb.lib import Context, HfbInstance  # noqa: E402
+from hairfb.renderer import BatchRenderer, Renderer  # noqa: E402
+
+
+def _instances(seed=3):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    common = dict(tile_size=16, depth_bins=8, slices=4, shading_points=8, grid_dims=32, iterations=4,
+                  wind_amplitude=1.0)
+    return [synthetic.make_instance(rng, strands=1500, points=16, width=320, height=240, **common),
+            synthetic.make_instance(rng, strands=600, points=24, width=256, height=256, curl=True, **common),
+            synthetic.make_instance(rng, strands=2500, points=32, width=512, height=384, **common)]
+
+
+def _state(r: Renderer):
+    rb = r.rb
+    return dict(pos=r.hair.positions.cpu().numpy(), dv=r.grids.density_velocity.cpu().numpy(),
+                shading=r.hair.shading.cpu().numpy(), tiles=rb.read_tiles(),
+                counts=rb.read_segment_counts(), segs=rb.read_tile_segments(), tl=rb.read_tile_list(),
+                px=rb.read_result()[4:].reshape(-1, 4))
+
+
+def _compare(a, b, r: Renderer, frame):
+    tag = f"frame {frame}"
+    assert np.array_equal(a["pos"], b["pos"]), f"{tag}: positions differ"
+    assert np.array_equal(a["dv"], b["dv"]), f"{tag}: density grid differs"
+    assert np.array_equal(a["counts"], b["counts"]), f"{tag}: segment counts differ"
+    ta, tb = a["tiles"].reshape(-1, 4), b["tiles"].reshape(-1, 4)
+    assert np.array_equal(ta[:, :2], tb[:, :2]), f"{tag}: depth bounds differ"
+    md = r.rb.max_drawn_segments
+    assert a["segs"][0] == b["segs"][0], f"{tag}: drawnSegmentsCount differs"
+    assert walk_lists(ta, a["segs"], md) == walk_lists(tb, b["segs"], md), f"{tag}: lists differ"
+    n = int(a["tl"][0])
+    assert n == int(b["tl"][0]) and np.array_equal(a["tl"][1:1 + n], b["tl"][1:1 + n]), f"{tag}: tile list"
+    assert np.abs(a["shading"] - b["shading"]).max() <= 1e-6, f"{tag}: shading differs"
+    err = np.abs(a["px"] - b["px"]).max()
+    assert err <= 1.0 / 255.0, f"{tag}: pixel error {err:.4g}"
+
+
+def test_frame_matches_pass_by_pass():
+    insts = _instances()
+    for inst in insts:
+        ref = Renderer(inst, 0)
+        nat = Renderer(inst, 0)
+        ref.before_first_frame()
+        nat.before_first_frame()
+        for f in range(3):
+            ref.frame()
+            nat.frame_native()
+            torch.cuda.synchronize()
+            _compare(_state(ref), _state(nat), ref, f)
+
+
+def test_frame_batch_matches_each_instance_alone():
+    insts = _instances()
+    alone = [Renderer(inst, 0) for inst in insts]
+    ctx = Context(insts[0].cfg.to_c(), 0)
+    batch = BatchRenderer([Renderer(inst, 0, ctx=ctx) for inst in insts])
+    for r in alone:
+        r.before_first_frame()
+    batch.before_first_frame()
+    l0 = ctx.counters()["launches"]
+    for f in range(4):  # the first batch runs plain launches, the later ones replay the graph
+        for r in alone:
+            r.frame()
+        batch.frame()
+        torch.cuda.synchronize()
+        for ra, rb in zip(alone, batch.renderers):
+            _compare(_state(ra), _state(rb), ra, f)
+            assert ra.hair._current == rb.hair._current
+    # one persistent launch per pass kind for the whole batch, every frame
+    per_frame = (ctx.counters()["launches"] - l0) / 4
+    assert per_frame <= 20, per_frame
+
+
+def test_frame_batch_rejects_bad_instances():
+    insts = _instances()[:2]
+    ctx = Context(insts[0].cfg.to_c(), 0)
+    rs = [Renderer(inst, 0, ctx=ctx) for inst in insts]
+    arr = (HfbInstance * 2)(*[r.instance() for r in rs])
+    arr[1].current = 2
+    with pytest.raises(Exception, match="instance 1: current"):
+        ctx.call("hfb_frame_batch", arr, 2)
+    arr[1].current = 0
+    arr[0].positions[1] = arr[0].positions[0]
+    with pytest.raises(Exception, match="instance 0"):
+        ctx.call("hfb_frame_batch", arr, 2)
+    with pytest.raises(Exception, match="1024"):
+        ctx.call("hfb_frame_batch", arr, 5000)
+    assert ctx.lib.hfb_frame_batch(ctx.handle, None, 0) == 0
+
