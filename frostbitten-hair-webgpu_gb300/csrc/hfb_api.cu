@@ -7,6 +7,7 @@
 #include <cstring>
 #include <new>
 
+#define HFB_TU 4
 #include "hfb_internal.cuh"
 
 namespace {
@@ -113,6 +114,7 @@ int hfb_ctx_destroy(HfbCtx* c) {
   HFB_CHECK_CTX(c);
   cudaStreamSynchronize(c->stream);
   hfb::frameBatchRelease(c);
+  if (c->checkDev) cudaFree(c->checkDev);
   if (c->dCounters) cudaFree(c->dCounters);
   if (c->ownStream) cudaStreamDestroy(c->ownStream);
   delete c;
@@ -274,25 +276,11 @@ static std::string checkViewport(const HfbUniforms* u, const HfbRasterBuffers* r
   return "";
 }
 
-static cudaError_t clearRaster(HfbCtx* c, HfbRasterBuffers* rb) {
-  const HfbConfig& cfg = c->cfg;
-  size_t T = (size_t)hfb::divCeil(rb->width, cfg.tileSize) * hfb::divCeil(rb->height, cfg.tileSize);
-  cudaError_t e = cudaSuccess;
-  auto z = [&](void* p, size_t n) { if (e == cudaSuccess) e = cudaMemsetAsync(p, 0, n, c->stream); };
-  z(rb->tiles, T * cfg.tileDepthBins * 16);       // hairTilesPass.ts:48-52
-  z(rb->segmentCountPerTile, T * 4);
-  z(rb->tileSegments, 4);
-  z(rb->rasterizerResult, 16 + (size_t)rb->width * rb->height * 16);  // hairFinePass.ts:50-55
-  z(rb->tileList, 4);                             // hairTileSortPass.ts:63-68
-  z(rb->sortBuckets, (size_t)cfg.sortBuckets * 8);
-  return e;
-}
-
 int hfb_clear_before_render(HfbCtx* c, HfbRasterBuffers* rb) {
   HFB_CHECK_CTX(c);
   std::string err = checkRaster(c, rb);
   HFB_REQUIRE(c, err.empty(), err);
-  cudaError_t e = clearRaster(c, rb);
+  cudaError_t e = hfb::clearRaster(c, *rb);
   if (e != cudaSuccess) return cudaFail(c, e, "clear_before_render");
   return HFB_OK;
 }
@@ -409,30 +397,10 @@ int hfb_frame(HfbCtx* c, HfbInstance* in) {
   HFB_CHECK_CTX(c);
   std::string err = checkInstance(c, in);
   HFB_REQUIRE(c, err.empty(), err);
-  const HfbSimUniforms& su = *in->simUniforms;
-  const HfbUniforms& u = *in->uniforms;
-  const HfbHairData& h = in->hair;
-  const uint32_t cur = in->current;
-  float* prev = in->positions[1u - cur];
-  float* now = in->positions[cur];
-  HfbRasterBuffers& rb = in->raster;
-  cudaError_t e = hfb::launchGridPreSim(c, su, in->densityVelocity, in->densityGradWind, in->sdf, in->sdfDims);
-  if (e == cudaSuccess && h.strandsCount)
-    e = hfb::launchSimIntegrate(c, su, h, prev, now, in->positionsInitial, in->segmentLengths, in->densityVelocity,
-                                in->densityGradWind, in->sdf, in->sdfDims);
-  // HairObject.swapPositionBuffersAfterSimIntegration: the new positions are "now"
-  if (e == cudaSuccess) e = hfb::launchGridPostSim(c, su, h, now, prev, in->densityVelocity);
-  if (e == cudaSuccess) e = clearRaster(c, &rb);
-  if (e == cudaSuccess)
-    e = hfb::launchTilesPass(c, u, h, prev, in->tangents, in->sceneDepth, in->strandsToRender, rb);
-  if (e == cudaSuccess) e = hfb::launchTileSort(c, rb);
-  if (e == cudaSuccess) e = hfb::launchFinePass(c, u, h, prev, in->tangents, in->shading, in->sceneDepth, rb);
-  if (e == cudaSuccess && h.strandsCount)
-    e = hfb::launchShading(c, u, h, prev, in->tangents, in->shadingDepth ? in->shadingDepth : in->sceneDepth,
-                           in->ao, in->ao ? in->aoWidth : 0u, in->ao ? in->aoHeight : 0u, in->shadowMap,
-                           in->shadowMap ? in->shadowMapSize : 0u, in->shading);
+  cudaError_t e = cudaSuccess;
+  for (uint32_t p = 0; p < hfb::FP_COUNT && e == cudaSuccess; p++) e = hfb::framePass(c, in, (hfb::FramePass)p);
   if (e != cudaSuccess) return cudaFail(c, e, "frame");
-  in->current = 1u - cur;
+  in->current ^= 1u;
   return HFB_OK;
 }
 
@@ -449,5 +417,60 @@ int hfb_frame_batch(HfbCtx* c, HfbInstance* insts, uint32_t n) {
   if (e != cudaSuccess) return cudaFail(c, e, "frame_batch");
   return HFB_OK;
 }
+
+int hfb_frame_batch_profile(HfbCtx* c, HfbInstance* insts, uint32_t n, float* passMs) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, insts && n > 0 && passMs, "NULL argument or empty batch");
+  HFB_REQUIRE(c, n <= hfb::BATCH_MAX, "at most 1024 instances per batch");
+  for (uint32_t i = 0; i < n; i++) {
+    std::string err = checkInstance(c, &insts[i]);
+    HFB_REQUIRE(c, err.empty(), "instance " + std::to_string(i) + ": " + err);
+  }
+  cudaError_t e = hfb::frameBatch(c, insts, n, passMs);
+  if (e != cudaSuccess) return cudaFail(c, e, "frame_batch_profile");
+  return HFB_OK;
+}
+
+#ifdef HFB_DEVICE_CHECKS
+// Self-checking build only (not part of include/hairfb.h): registers the
+// byte ranges [lo, hi) that the kernels may touch (pairs in lohi; the
+// context's own device counters are added), and resets the failure record.
+HFB_API int hfb_debug_check_ranges(HfbCtx* c, const unsigned long long* lohi, uint32_t n) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, lohi || n == 0, "NULL ranges");
+  HFB_REQUIRE(c, n + 1 <= hfb::CHECK_MAX_RANGES, "too many ranges");
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess && !c->checkDev) e = cudaMalloc(&c->checkDev, sizeof(hfb::CheckState));
+  if (e != cudaSuccess) return cudaFail(c, e, "debug_check_ranges");
+  hfb::CheckState* h = new hfb::CheckState();
+  for (uint32_t i = 0; i < n; i++) {
+    h->lo[i] = lohi[2 * i];
+    h->hi[i] = lohi[2 * i + 1];
+  }
+  h->lo[n] = (unsigned long long)c->dCounters;
+  h->hi[n] = h->lo[n] + sizeof(hfb::DeviceCounters);
+  h->nRanges = n + 1;
+  e = cudaMemcpy(c->checkDev, h, sizeof(*h), cudaMemcpyHostToDevice);
+  delete h;
+  if (e != cudaSuccess) return cudaFail(c, e, "debug_check_ranges");
+  return HFB_OK;
+}
+
+// out[0] = failed checks, out[1] = translation unit << 16 | line of the
+// first, out[2] = its address (0 for a failed condition), out[3] = its bytes.
+HFB_API int hfb_debug_check_read(HfbCtx* c, unsigned long long* out) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, out && c->checkDev, "NULL output or no ranges registered");
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  hfb::CheckState h;
+  if (e == cudaSuccess) e = cudaMemcpy(&h, c->checkDev, sizeof(h), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cudaFail(c, e, "debug_check_read");
+  out[0] = h.fails;
+  out[1] = h.firstWhere;
+  out[2] = h.firstAddr;
+  out[3] = h.firstBytes;
+  return HFB_OK;
+}
+#endif
 
 }  // extern "C"

@@ -211,7 +211,7 @@ __device__ __forceinline__ void projectHairPoint(const float* modelMatrix, const
 __device__ __forceinline__ float loadTex2DClamp(const float* tex, uint32_t w, uint32_t h, int x, int y) {
   x = min(max(x, 0), (int)w - 1);
   y = min(max(y, 0), (int)h - 1);
-  return __ldg(tex + (size_t)y * w + x);
+  return __ldg(HFB_G(tex + (size_t)y * w + x));
 }
 
 }  // namespace hfb

@@ -29,6 +29,7 @@
 #include <mutex>
 #include <string>
 
+#define HFB_TU 6
 #include "hfb_internal.cuh"
 
 namespace {

@@ -21,6 +21,7 @@
 #include <cooperative_groups.h>
 #include <cuda_fp16.h>
 
+#define HFB_TU 3
 #include "hfb_internal.cuh"
 #include "hfb_math.cuh"
 
@@ -50,9 +51,9 @@ __device__ __forceinline__ ProjSeg projectSegment(const HfbUniforms& U, const fl
   ProjSeg r;
   f3 cam = mk3(U.cameraPosition.x, U.cameraPosition.y, U.cameraPosition.z);
   size_t i = (size_t)strand * P + seg;
-  projectHairPoint(U.modelMatrix.m, U.vpMatrix.m, cam, ld4(__ldg(&pos[i])), ld4(__ldg(&tan[i])), size,
+  projectHairPoint(U.modelMatrix.m, U.vpMatrix.m, cam, ld4(__ldg(HFB_G(&pos[i]))), ld4(__ldg(HFB_G(&tan[i]))), size,
                    U.fiberRadius, r.v00, r.v01, r.depthsProj.x, r.depthsProj.y);
-  projectHairPoint(U.modelMatrix.m, U.vpMatrix.m, cam, ld4(__ldg(&pos[i + 1])), ld4(__ldg(&tan[i + 1])), size,
+  projectHairPoint(U.modelMatrix.m, U.vpMatrix.m, cam, ld4(__ldg(HFB_G(&pos[i + 1]))), ld4(__ldg(HFB_G(&tan[i + 1]))), size,
                    U.fiberRadius, r.v10, r.v11, r.depthsProj.z, r.depthsProj.w);
   return r;
 }
@@ -201,23 +202,24 @@ __device__ __forceinline__ void storeTileRecord(uint4* __restrict__ tiles, uint3
                                                uint32_t* __restrict__ segCount, uint32_t* __restrict__ binCount,
                                                DeviceCounters* __restrict__ counters, uint32_t maxDrawn,
                                                uint32_t tilesX, uint32_t B, uint32_t tx, uint32_t ty,
-                                               uint32_t dbin, float dmin, float dmax, uint32_t key) {
+                                               uint32_t dbin, float dmin, float dmax, uint32_t key, uint32_t T) {
+  if (!HFB_EXPECT(tx < tilesX && ty * tilesX + tx < T && dbin < B)) return;
   cg::coalesced_group g = cg::coalesced_threads();
   uint32_t base = 0;
-  if (g.thread_rank() == 0) base = atomicAdd(&segBuf[0], g.size());
+  if (g.thread_rank() == 0) base = atomicAdd(HFB_G(&segBuf[0]), g.size());
   base = g.shfl(base, 0);
   const uint32_t ptr = base + g.thread_rank();
   if (ptr < maxDrawn) {
     const uint32_t ti = ty * tilesX * B + tx * B + dbin;
-    atomicMax(&tiles[ti].x, f2u(fmul(fsub(1.0f, dmin), F_MAX_U32)));  // _storeTileHead
-    atomicMax(&tiles[ti].y, f2u(fmul(dmax, F_MAX_U32)));
-    atomicAdd(&segCount[ty * tilesX + tx], 1u);  // _incTileSegmentCount
-    atomicAdd(&binCount[ti], 1u);
+    atomicMax(HFB_G(&tiles[ti].x), f2u(fmul(fsub(1.0f, dmin), F_MAX_U32)));  // _storeTileHead
+    atomicMax(HFB_G(&tiles[ti].y), f2u(fmul(dmax, F_MAX_U32)));
+    atomicAdd(HFB_G(&segCount[ty * tilesX + tx]), 1u);  // _incTileSegmentCount
+    atomicAdd(HFB_G(&binCount[ti]), 1u);
     // staging record in the list slot; binFinalize rewrites it
-    segBuf[1u + 2u * ptr] = ti;
-    segBuf[2u + 2u * ptr] = key;
+    (*HFB_G(&segBuf[1u + 2u * ptr])) = ti;
+    (*HFB_G(&segBuf[2u + 2u * ptr])) = key;
   } else {
-    atomicAdd(&counters->tileRecordsDropped, 1ull);
+    atomicAdd(HFB_G(&counters->tileRecordsDropped), 1ull);
   }
 }
 
@@ -257,7 +259,7 @@ __device__ void rasterSegmentSerial(const HfbUniforms& U, const ProjSeg& s, uint
       }
       if (dmin > 1.0f) continue;
       storeTileRecord(tiles, segBuf, segCount, binCount, counters, maxDrawn, tilesX, B, tx, ty, dbin, dmin, dmax,
-                      key);
+                      key, tilesX * divCeil(H, TS));
     }
   }
 }
@@ -394,7 +396,8 @@ __device__ __forceinline__ void tilesRasterBody(const HfbUniforms& U, uint32_t P
           uint32_t base = 0;
           if (lane == leader) base = atomicAdd(&sh.passCount, (uint32_t)__popc(bal));
           base = __shfl_sync(0xffffffffu, base, leader);
-          if (pass) sh.pass[base + __popc(bal & ((1u << lane) - 1u))] = k | ((p - sh.pairBase[k]) << 7);
+          const uint32_t at = base + __popc(bal & ((1u << lane) - 1u));
+          if (pass && HFB_EXPECT(at < TR_CHUNK && k < TR_SEGS)) sh.pass[at] = k | ((p - sh.pairBase[k]) << 7);
         }
         if (valid) {
           p++;
@@ -431,6 +434,7 @@ __device__ __forceinline__ void tilesRasterBody(const HfbUniforms& U, uint32_t P
       const float zb = loadTex2DClamp(depth, W, H, (int)x, (int)H - (int)y);
       if (hd > zb) continue;  // depth test, :193-195
       const uint32_t slot = sh.slotBase[k] + (y / TS - sh.tminy[k]) * sh.tsx[k] + (x / TS - sh.tminx[k]);
+      if (!HFB_EXPECT(slot < TR_SLOTS)) continue;
       atomicMin(&sh.accBin[slot], viewDepthBin(U, B, dv0, dv1, p, hd));
       if (!isnan(hd)) {  // fminf / fmaxf ignore a NaN depth
         atomicMin(&sh.accMin[slot], orderedBits(hd));
@@ -455,7 +459,7 @@ __device__ __forceinline__ void tilesRasterBody(const HfbUniforms& U, uint32_t P
     const uint32_t g = blk * TR_SEGS + k;
     const uint32_t strand = g / segsPerStrand, seg = g - strand * segsPerStrand;
     storeTileRecord(tiles, segBuf, segCount, binCount, counters, maxDrawn, tilesX, B, tx, ty, sh.accBin[i], dmin,
-                    orderedFloat(sh.accMax[i]), (strand << 8) | seg);
+                    orderedFloat(sh.accMax[i]), (strand << 8) | seg, tilesX * divCeil(H, TS));
   }
   if (serial)
     rasterSegmentSerial(U, s, W, H, TS, B, tilesX, maxDrawn, dv0, dv1, key, ux0, uy0, ux1, uy1, depth, tiles,
@@ -484,17 +488,17 @@ __device__ __forceinline__ void binScanBlocksBody(const uint32_t* __restrict__ c
   uint32_t v[4], s = 0;
 #pragma unroll
   for (int k = 0; k < 4; k++) {
-    v[k] = base + k < n ? cnt[base + k] : 0u;
+    v[k] = base + k < n ? (*HFB_G(&cnt[base + k])) : 0u;
     s += v[k];
   }
   uint32_t total;
   uint32_t ex = blockExclusiveScan(s, warpSums, total);
 #pragma unroll
   for (int k = 0; k < 4; k++) {
-    if (base + k < n) off[base + k] = ex;
+    if (base + k < n) (*HFB_G(&off[base + k])) = ex;
     ex += v[k];
   }
-  if (threadIdx.x == 0) blockSums[blk] = total;
+  if (threadIdx.x == 0) (*HFB_G(&blockSums[blk])) = total;
 }
 
 __global__ void __launch_bounds__(512) binScanBlocks(const uint32_t* __restrict__ cnt, uint32_t* __restrict__ off,
@@ -508,10 +512,10 @@ __device__ __forceinline__ void binScanSumsBody(uint32_t* __restrict__ blockSums
   uint32_t carry = 0;
   for (uint32_t b0 = 0; b0 < nBlocks; b0 += blockDim.x) {
     uint32_t i = b0 + threadIdx.x;
-    uint32_t v = i < nBlocks ? blockSums[i] : 0u;
+    uint32_t v = i < nBlocks ? (*HFB_G(&blockSums[i])) : 0u;
     uint32_t total;
     uint32_t ex = blockExclusiveScan(v, warpSums, total);
-    if (i < nBlocks) blockSums[i] = carry + ex;
+    if (i < nBlocks) (*HFB_G(&blockSums[i])) = carry + ex;
     carry += total;
   }
 }
@@ -527,23 +531,25 @@ __global__ void __launch_bounds__(1024) binScanSums(uint32_t* __restrict__ block
 __device__ __forceinline__ void binScatterBody(const uint32_t* __restrict__ segBuf, uint32_t maxDrawn,
                                                uint32_t* __restrict__ binOffset,
                                                const uint32_t* __restrict__ blockSums, uint32_t* __restrict__ keys,
-                                               DeviceCounters* __restrict__ counters, uint32_t blk, uint32_t nblk) {
-  const uint32_t total = segBuf[0];
+                                               DeviceCounters* __restrict__ counters, uint32_t blk, uint32_t nblk,
+                                               uint32_t TB) {
+  const uint32_t total = (*HFB_G(&segBuf[0]));
   const uint32_t n = min(total, maxDrawn);
-  if (blk == 0 && threadIdx.x == 0) atomicAdd(&counters->tileRecords, (unsigned long long)total);
+  if (blk == 0 && threadIdx.x == 0) atomicAdd(HFB_G(&counters->tileRecords), (unsigned long long)total);
   for (uint32_t r = blk * blockDim.x + threadIdx.x; r < n; r += nblk * blockDim.x) {
-    uint32_t ti = segBuf[1u + 2u * r];
-    uint32_t key = segBuf[2u + 2u * r];
-    uint32_t pos = blockSums[ti / SCAN_PER_BLOCK] + atomicAdd(&binOffset[ti], 1u);
-    keys[pos] = key;
+    uint32_t ti = (*HFB_G(&segBuf[1u + 2u * r]));
+    uint32_t key = (*HFB_G(&segBuf[2u + 2u * r]));
+    if (!HFB_EXPECT(ti < TB)) continue;
+    uint32_t pos = (*HFB_G(&blockSums[ti / SCAN_PER_BLOCK])) + atomicAdd(HFB_G(&binOffset[ti]), 1u);
+    if (HFB_EXPECT(pos < maxDrawn)) (*HFB_G(&keys[pos])) = key;
   }
 }
 
 __global__ void __launch_bounds__(256)
 binScatterKernel(const uint32_t* __restrict__ segBuf, uint32_t maxDrawn, uint32_t* __restrict__ binOffset,
                  const uint32_t* __restrict__ blockSums, uint32_t* __restrict__ keys,
-                 DeviceCounters* __restrict__ counters) {
-  binScatterBody(segBuf, maxDrawn, binOffset, blockSums, keys, counters, blockIdx.x, gridDim.x);
+                 DeviceCounters* __restrict__ counters, uint32_t TB) {
+  binScatterBody(segBuf, maxDrawn, binOffset, blockSums, keys, counters, blockIdx.x, gridDim.x, TB);
 }
 
 // ---------------------------------------------------------------------------
@@ -554,11 +560,11 @@ __device__ __forceinline__ void writeList(uint32_t* __restrict__ segBuf, uint4* 
   // _storeTileSegment encoding: (segment << 24) | strand; next = previous
   // (smaller) key, so the walk from the head visits keys in descending order.
   uint32_t p = start + i;
-  segBuf[1u + 2u * p] = ((key & 0xffu) << 24) | (key >> 8);
-  segBuf[2u + 2u * p] = i == 0 ? INVALID_PTR : p - 1u;
+  (*HFB_G(&segBuf[1u + 2u * p])) = ((key & 0xffu) << 24) | (key >> 8);
+  (*HFB_G(&segBuf[2u + 2u * p])) = i == 0 ? INVALID_PTR : p - 1u;
   if (i == n - 1u) {
-    tiles[ti].z = p + 1u;  // head pointer (+1, 0 = empty)
-    tiles[ti].w = n;       // padding0: list length, a hint the fine pass verifies
+    (*HFB_G(&tiles[ti])).z = p + 1u;  // head pointer (+1, 0 = empty)
+    (*HFB_G(&tiles[ti])).w = n;       // padding0: list length, a hint the fine pass verifies
   }
 }
 
@@ -573,12 +579,13 @@ __device__ __forceinline__ void binFinalizeBody(uint32_t TB, const uint32_t* __r
   const uint32_t nw = (nblk * blockDim.x) >> 5;
   uint32_t* s = smem[warp];
   for (uint32_t ti = gw; ti < TB; ti += nw) {
-    const uint32_t n = binCount[ti];
+    const uint32_t n = (*HFB_G(&binCount[ti]));
     if (n == 0) continue;
-    const uint32_t end = blockSums[ti / SCAN_PER_BLOCK] + binOffset[ti];  // cursor ended at bin end
+    const uint32_t end = (*HFB_G(&blockSums[ti / SCAN_PER_BLOCK])) + (*HFB_G(&binOffset[ti]));  // cursor ended at bin end
     const uint32_t start = end - n;
+    if (!HFB_EXPECT(n <= end && end <= (*HFB_G(&segBuf[0])))) continue;
     if (n <= SMALL_BIN) {
-      uint32_t v = lane < n ? keys[start + lane] : 0xffffffffu;
+      uint32_t v = lane < n ? (*HFB_G(&keys[start + lane])) : 0xffffffffu;
       // bitonic sort across the warp, ascending
 #pragma unroll
       for (uint32_t k = 2; k <= 32; k <<= 1) {
@@ -593,7 +600,7 @@ __device__ __forceinline__ void binFinalizeBody(uint32_t TB, const uint32_t* __r
     } else if (n <= MEDIUM_BIN) {
       uint32_t N = 64;
       while (N < n) N <<= 1;
-      for (uint32_t i = lane; i < N; i += 32) s[i] = i < n ? keys[start + i] : 0xffffffffu;
+      for (uint32_t i = lane; i < N; i += 32) s[i] = i < n ? (*HFB_G(&keys[start + i])) : 0xffffffffu;
       __syncwarp();
       for (uint32_t k = 2; k <= N; k <<= 1) {
         for (uint32_t j = k >> 1; j > 0; j >>= 1) {
@@ -609,8 +616,8 @@ __device__ __forceinline__ void binFinalizeBody(uint32_t TB, const uint32_t* __r
       for (uint32_t i = lane; i < n; i += 32) writeList(segBuf, tiles, ti, start, i, n, s[i]);
       __syncwarp();
     } else if (lane == 0) {
-      uint32_t slot = atomicAdd(&largeBins[0], 1u);
-      largeBins[1u + slot] = ti;
+      uint32_t slot = atomicAdd(HFB_G(&largeBins[0]), 1u);
+      (*HFB_G(&largeBins[1u + slot])) = ti;
     }
   }
 }
@@ -635,11 +642,12 @@ __device__ __forceinline__ void largeBinsBody(const uint32_t* __restrict__ large
                                               const uint32_t* __restrict__ blockSums, uint32_t* __restrict__ keys,
                                               uint32_t* __restrict__ segBuf, uint4* __restrict__ tiles, uint32_t* sk,
                                               uint32_t vblk, uint32_t nvblk) {
-  const uint32_t nLarge = largeBins[0];
+  const uint32_t nLarge = (*HFB_G(&largeBins[0]));
   for (uint32_t li = vblk; li < nLarge; li += nvblk) {
-    const uint32_t ti = largeBins[1u + li];
-    const uint32_t n = binCount[ti];
-    const uint32_t start = blockSums[ti / SCAN_PER_BLOCK] + binOffset[ti] - n;
+    const uint32_t ti = (*HFB_G(&largeBins[1u + li]));
+    const uint32_t n = (*HFB_G(&binCount[ti]));
+    const uint32_t start = (*HFB_G(&blockSums[ti / SCAN_PER_BLOCK])) + (*HFB_G(&binOffset[ti])) - n;
+    if (!HFB_EXPECT(start + n <= (*HFB_G(&segBuf[0])) && n > MEDIUM_BIN)) continue;
     uint32_t* a = keys + start;
     uint32_t* tmp = segBuf + 1u + 2u * start;  // 2n free words
     // sort runs in shared memory
@@ -647,7 +655,7 @@ __device__ __forceinline__ void largeBinsBody(const uint32_t* __restrict__ large
       uint32_t m = min(LARGE_SMEM_KEYS, n - r0);
       uint32_t N = 2;
       while (N < m) N <<= 1;
-      for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) sk[i] = i < m ? a[r0 + i] : 0xffffffffu;
+      for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) sk[i] = i < m ? (*HFB_G(&a[r0 + i])) : 0xffffffffu;
       __syncthreads();
       for (uint32_t k = 2; k <= N; k <<= 1)
         for (uint32_t j = k >> 1; j > 0; j >>= 1) {
@@ -659,7 +667,7 @@ __device__ __forceinline__ void largeBinsBody(const uint32_t* __restrict__ large
           }
           __syncthreads();
         }
-      for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) a[r0 + i] = sk[i];
+      for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) (*HFB_G(&a[r0 + i])) = sk[i];
       __syncthreads();
     }
     // merge passes (ping-pong between a and tmp)
@@ -669,26 +677,26 @@ __device__ __forceinline__ void largeBinsBody(const uint32_t* __restrict__ large
       for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
         uint32_t blk = i / (2u * run);
         uint32_t l0 = blk * 2u * run, l1 = min(l0 + run, n), r1 = min(l0 + 2u * run, n);
-        uint32_t v = src[i];
+        uint32_t v = (*HFB_G(&src[i]));
         bool left = i < l1;
         uint32_t o0 = left ? l1 : l0, o1 = left ? r1 : l1;  // the other run
         uint32_t lo = o0, hi = o1;                           // count of other < v
         while (lo < hi) {
           uint32_t mid = (lo + hi) >> 1;
-          if (src[mid] < v) lo = mid + 1; else hi = mid;
+          if ((*HFB_G(&src[mid])) < v) lo = mid + 1; else hi = mid;
         }
         uint32_t rankOther = lo - o0;
         uint32_t rankSelf = i - (left ? l0 : l1);
-        dst[l0 + rankSelf + rankOther] = v;
+        (*HFB_G(&dst[l0 + rankSelf + rankOther])) = v;
       }
       __syncthreads();
       uint32_t* t = src; src = dst; dst = t;
     }
     if (src != a) {
-      for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) a[i] = src[i];
+      for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) (*HFB_G(&a[i])) = (*HFB_G(&src[i]));
       __syncthreads();
     }
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) writeList(segBuf, tiles, ti, start, i, n, a[i]);
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) writeList(segBuf, tiles, ti, start, i, n, (*HFB_G(&a[i])));
     __syncthreads();
   }
 }
@@ -727,7 +735,7 @@ __device__ __forceinline__ void tileSortBody(uint32_t T, uint32_t NB, uint32_t b
   // count-tiles: calcTileSortBucket, hairTileSortPass.countTiles.wgsl.ts:37-40
   uint32_t local = 0;
   for (uint32_t t = tid; t < T; t += blockDim.x) {
-    uint32_t c = segCount[t];
+    uint32_t c = (*HFB_G(&segCount[t]));
     if (c > 0u) {
       atomicAdd(&hist[clampu(c / bucketSize, 0u, NB - 1u)], 1u);
       local++;
@@ -745,17 +753,17 @@ __device__ __forceinline__ void tileSortBody(uint32_t T, uint32_t NB, uint32_t b
     }
   }
   for (uint32_t b = tid; b < NB; b += blockDim.x) {
-    buckets[2u * b] = hist[b];
-    buckets[2u * b + 1u] = hist[b];  // the in-bucket write counter ends at tileCount
+    (*HFB_G(&buckets[2u * b])) = hist[b];
+    (*HFB_G(&buckets[2u * b + 1u])) = hist[b];  // the in-bucket write counter ends at tileCount
   }
-  if (tid == 0) tileList[0] = drawn;
+  if (tid == 0) (*HFB_G(&tileList[0])) = drawn;
   __syncthreads();
   // stable scatter, one 1024-tile chunk at a time
   for (uint32_t c0 = 0; c0 < T; c0 += blockDim.x) {
     for (uint32_t i = tid; i < 32u * NB; i += blockDim.x) wcnt[i / NB][i % NB] = 0;
     __syncthreads();
     uint32_t t = c0 + tid;
-    uint32_t c = t < T ? segCount[t] : 0u;
+    uint32_t c = t < T ? (*HFB_G(&segCount[t])) : 0u;
     bool valid = c > 0u;
     uint32_t b = valid ? clampu(c / bucketSize, 0u, NB - 1u) : SORT_MAX_BUCKETS;
     uint32_t peers = __match_any_sync(0xffffffffu, b);
@@ -772,7 +780,7 @@ __device__ __forceinline__ void tileSortBody(uint32_t T, uint32_t NB, uint32_t b
       run[bb] = s;
     }
     __syncthreads();
-    if (valid) tileList[1u + offs[b] + wcnt[warp][b] + rank] = t;
+    if (valid && HFB_EXPECT(offs[b] + wcnt[warp][b] + rank < T)) (*HFB_G(&tileList[1u + offs[b] + wcnt[warp][b] + rank])) = t;
     __syncthreads();
   }
 }
@@ -934,7 +942,7 @@ __device__ __forceinline__ uint32_t stageSegment(FineSmem<TS>& sh, uint32_t k, u
       remapToIndices(SP, fadd((float)sg, 1.0f) / (float)(P - 1u), b0, b1);
       const uint32_t ne = min(b1 - a0 + 1u, NSHADE);
       const size_t sb = (size_t)st * SP;
-      for (uint32_t j = 0; j < ne; j++) sh.shade[k][j] = __ldg(&shading[sb + a0 + j]);
+      for (uint32_t j = 0; j < ne; j++) sh.shade[k][j] = __ldg(HFB_G(&shading[sb + a0 + j]));
       shadeBase |= a0 | (ne << 16);
     }
   }
@@ -967,8 +975,8 @@ __device__ __forceinline__ uint2 fragmentColour(const FineSmem<TS>& sh, uint32_t
     c1 = sh.shade[k][i1 - e0];
   } else {
     const size_t sb = (size_t)sh.strand[k] * SP;
-    c0 = __ldg(&shading[sb + i0]);
-    c1 = __ldg(&shading[sb + i1]);
+    c0 = __ldg(HFB_G(&shading[sb + i0]));
+    c1 = __ldg(HFB_G(&shading[sb + i1]));
   }
   f4 c = mix4(ld4(c0), ld4(c1), fr);
   c.w = fmul(c.w, alpha);
@@ -1080,7 +1088,7 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
     if (lane == 0) sh.doneMask[warp] = dm;
   }
   fin = mk4(0.f, 0.f, 0.f, 0.f);  // rasterizerResult was cleared before the pass
-  if (tid < B) sh.head[tid] = a.tiles[ty * tilesX * B + tx * B + tid];
+  if (tid < B) sh.head[tid] = (*HFB_G(&a.tiles[ty * tilesX * B + tx * B + tid]));
   __syncthreads();
 
   // ---- tile mode: every depth bin's list carries a length hint (padding0,
@@ -1127,7 +1135,8 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
       const uint4 h = sh.head[lo];
       const uint32_t j = k - sh.binOff[lo];
       const uint32_t idx = h.z - 1u - j;
-      const uint32_t nxt = __ldg(&segBuf[2u + 2u * idx]);
+      if (!HFB_EXPECT(idx < maxDrawn)) { sh.bad = 1; continue; }
+      const uint32_t nxt = __ldg(HFB_G(&segBuf[2u + 2u * idx]));
       if (nxt != ((j + 1u == h.w) ? INVALID_PTR : idx - 1u)) sh.bad = 1;
     }
     __syncthreads();
@@ -1159,7 +1168,7 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
         while (r + 1u < nRuns && sh.runK0[r + 1u] <= k) r++;
         const uint32_t b = sh.runBin[r] & 0xffu;
         const uint32_t idx = sh.head[b].z - 1u - (sh.runOff[r] + k - sh.runK0[r]);
-        const uint32_t enc = __ldg(&segBuf[1u + 2u * idx]);
+        const uint32_t enc = HFB_EXPECT(idx < maxDrawn) ? __ldg(HFB_G(&segBuf[1u + 2u * idx])) : 0xffffffffu;
         sh.strand[k] = enc & 0x00ffffffu;
         sh.segIdx[k] = enc >> 24;
         sh.listIdx[k] = idx;
@@ -1179,8 +1188,8 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
           const bool inRange = lane < want && lane <= p;
           uint2 e = make_uint2(0u, INVALID_PTR);
           if (inRange) {
-            e.x = __ldg(&segBuf[1u + 2u * cand]);
-            e.y = __ldg(&segBuf[2u + 2u * cand]);
+            e.x = __ldg(HFB_G(&segBuf[1u + 2u * cand]));
+            e.y = __ldg(HFB_G(&segBuf[2u + 2u * cand]));
           }
           const bool chain = inRange && e.y == cand - 1u;
           const uint32_t brk = __ballot_sync(0xffffffffu, !chain);
@@ -1392,6 +1401,7 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
         const uint32_t e = sh.frag[i].x;
         const uint32_t pix = e & 0xffffu, k = e >> 16;
         if (k >= nSeg) continue;  // dropped from the round
+        if (!HFB_EXPECT(i < PAIRS && k < STAGE && pix < NT)) continue;
         const uint32_t qx = pix % TS, qy = pix / TS;
         const f2 pf = mk2((float)(tbp.x0 + qx), (float)(tbp.y0 + qy));
         QuadConst qc;
@@ -1449,7 +1459,7 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
             sh.nSeg = cut + 1u;
             sh.runK1[0] = cut + 1u;
             sh.runBin[0] |= RUN_ENDS;  // the reference breaks after the filling segment
-            atomicAdd(&counters->finePoolFullBins, 1ull);
+            atomicAdd(HFB_G(&counters->finePoolFullBins), 1ull);
           }
         }
       }
@@ -1479,7 +1489,7 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
             const uint32_t bx0 = b & 0xffu, by0 = (b >> 8) & 0xffu;
             const uint32_t info =
                 sh.pairInfo[sh.pairBase[j] + (ly - by0) * (((b >> 16) & 0xffu) - bx0 + 1u) + (lx - bx0)];
-            if (info != PAIR_NONE) {  // not dropped by a full pool
+            if (info != PAIR_NONE && HFB_EXPECT((info & 0xffffu) < PAIRS)) {  // not dropped by a full pool
               blendFragment<MAXL>(acc, info >> 16, sh.frag[info & 0xffffu]);
               nFrag++;
               pending++;
@@ -1569,13 +1579,13 @@ __device__ __forceinline__ void fineScheduleBody(const uint32_t* __restrict__ ti
                                                  DeviceCounters* __restrict__ counters, uint32_t* warpSums,
                                                  uint32_t& total) {
   const uint32_t tid = threadIdx.x;
-  const uint32_t drawn = min(tileList[0], T);
+  const uint32_t drawn = min((*HFB_G(&tileList[0])), T);
   if (tid == 0) total = 0;
   __syncthreads();
   uint32_t mine = 0;
   for (uint32_t q = tid; q < drawn; q += blockDim.x) {
-    const uint32_t t = tileList[1u + q];
-    if (t < T) mine += segCount[t];
+    const uint32_t t = (*HFB_G(&tileList[1u + q]));
+    if (t < T) mine += (*HFB_G(&segCount[t]));
   }
   atomicAdd(&total, mine);
   __syncthreads();
@@ -1583,14 +1593,15 @@ __device__ __forceinline__ void fineScheduleBody(const uint32_t* __restrict__ ti
   uint32_t carryItems = 0, carrySlots = 0;
   for (uint32_t q0 = 0; q0 < drawn; q0 += blockDim.x) {
     const uint32_t q = q0 + tid;
-    uint32_t nG = 1, t = T;
+    uint32_t nG = 0, t = T;  // items of this tile-list entry: none past the list's end
     if (q < drawn) {
-      t = tileList[1u + q];
-      if (allowSplit && t < T && segCount[t] > thr) {  // count the groups of the split
+      nG = 1;
+      t = (*HFB_G(&tileList[1u + q]));
+      if (allowSplit && t < T && (*HFB_G(&segCount[t])) > thr) {  // count the groups of the split
         uint32_t g = 0, acc = 0;
         bool ok = true;
         for (uint32_t b = 0; b < B; b++) {
-          const uint4 h = tiles[(size_t)t * B + b];
+          const uint4 h = (*HFB_G(&tiles[(size_t)t * B + b]));
           uint32_t nb = 0;
           if (h.y != 0u && h.z != 0u) {
             if (h.w != 0u && h.w <= h.z && h.z <= maxDrawn && h.w <= maxProcessed) nb = h.w; else ok = false;
@@ -1607,37 +1618,37 @@ __device__ __forceinline__ void fineScheduleBody(const uint32_t* __restrict__ ti
     const uint32_t mySlots = nG > 1u ? nG : 0u;
     const uint32_t slotEnd = carrySlots + blockExclusiveScan(mySlots, warpSums, chunkSlots) + mySlots;
     const bool split = nG > 1u && slotEnd <= fs.maxGroups;
-    if (!split) nG = 1;
+    if (nG > 1u && !split) nG = 1;
     uint32_t chunkItems;
     const uint32_t itemBase = carryItems + blockExclusiveScan(nG, warpSums, chunkItems);
     if (q < drawn) {
       if (split) {
         const uint32_t slot = slotEnd - nG;
-        fs.arrivals[slot] = 0;
-        atomicAdd(&counters->fineSplitTiles, 1ull);
+        (*HFB_G(&fs.arrivals[slot])) = 0;
+        atomicAdd(HFB_G(&counters->fineSplitTiles), 1ull);
         uint32_t g = 0, acc = 0, start = 0;
         for (uint32_t b = 0; b < B; b++) {
-          const uint4 h = tiles[(size_t)t * B + b];
+          const uint4 h = (*HFB_G(&tiles[(size_t)t * B + b]));
           const uint32_t nb = (h.y != 0u && h.z != 0u) ? h.w : 0u;
           if (nb == 0u) continue;
           if (acc > 0u && acc + nb > thr) {
-            fs.items[itemBase + g] = make_uint4(q, start | (b << 8) | (g << 16) | (nG << 24), slot, 0u);
+            (*HFB_G(&fs.items[itemBase + g])) = make_uint4(q, start | (b << 8) | (g << 16) | (nG << 24), slot, 0u);
             g++;
             acc = 0;
             start = b;
           }
           acc += nb;
         }
-        fs.items[itemBase + g] = make_uint4(q, start | (B << 8) | (g << 16) | (nG << 24), slot, 0u);
+        (*HFB_G(&fs.items[itemBase + g])) = make_uint4(q, start | (B << 8) | (g << 16) | (nG << 24), slot, 0u);
       } else {
-        fs.items[itemBase] = make_uint4(q, 0u | (B << 8) | (1u << 24), 0u, 0u);
+        (*HFB_G(&fs.items[itemBase])) = make_uint4(q, 0u | (B << 8) | (1u << 24), 0u, 0u);
       }
     }
     carryItems += chunkItems;
     carrySlots += chunkSlots;
   }
-  if (tid == 0) fs.hdr[0] = carryItems;
-  __syncthreads();  // total and warpSums are reused by the block's next instance
+  if (tid == 0) (*HFB_G(&fs.hdr[0])) = carryItems;
+  __syncthreads();
 }
 
 __global__ void __launch_bounds__(1024)
@@ -1666,14 +1677,18 @@ __device__ __forceinline__ void fineItem(FineSmem<TS>& sh, const HfbUniforms& U,
   const uint32_t tilesX = divCeil(W, TS), tileCount = tilesX * divCeil(H, TS);
   float4* res = reinterpret_cast<float4*>(result + 4);
   {
-    const uint32_t tileIdx = tileList[1u + item.x];
+    if (item.x >= tileCount) {  // not an entry of the tile list: count it and skip
+      if (tid == 0) atomicAdd(HFB_G(&a.counters->badWorkItems), 1ull);
+      return;
+    }
+    const uint32_t tileIdx = (*HFB_G(&tileList[1u + item.x]));
     uint32_t b0 = item.y & 0xffu, b1 = (item.y >> 8) & 0xffu;
     const uint32_t g = (item.y >> 16) & 0xffu, nG = item.y >> 24;
     if (tileIdx >= tileCount || b1 > a.B || b0 >= b1) return;
     bool split = nG > 1u, write = true;
     if (split && (g >= nG || item.z >= fs.maxGroups || nG > fs.maxGroups - item.z)) {
       // not an item the schedule writes: count it and leave the tile alone
-      if (tid == 0) atomicAdd(&a.counters->badWorkItems, 1ull);
+      if (tid == 0) atomicAdd(HFB_G(&a.counters->badWorkItems), 1ull);
       return;
     }
     f4 fin;
@@ -1681,14 +1696,14 @@ __device__ __forceinline__ void fineItem(FineSmem<TS>& sh, const HfbUniforms& U,
       const bool ok = fineTile<TS, MAXL>(sh, U, a, tileIdx, b0, b1, split && g > 0u, fin);
       if (!split) break;
       // a group of a split tile: publish its composite; the last to arrive merges
-      fs.groups[(size_t)(item.z + g) * NT + tid] = make_float4(fin.x, fin.y, fin.z, fin.w);
+      (*HFB_G(&fs.groups[(size_t)(item.z + g) * NT + tid])) = make_float4(fin.x, fin.y, fin.z, fin.w);
       __threadfence();
       __syncthreads();
       if (tid == 0) {
-        if (!ok) atomicOr(&fs.arrivals[item.z], UNSAFE);
-        const uint32_t old = atomicAdd(&fs.arrivals[item.z], 1u);
+        if (!ok) atomicOr(HFB_G(&fs.arrivals[item.z]), UNSAFE);
+        const uint32_t old = atomicAdd(HFB_G(&fs.arrivals[item.z]), 1u);
         sh.arrive = (old & 0xffffu) + 1u == nG ? ((old & UNSAFE) ? 2u : 1u) : 0u;
-        if (sh.arrive == 2u) atomicAdd(&a.counters->fineSplitRedone, 1ull);
+        if (sh.arrive == 2u) atomicAdd(HFB_G(&a.counters->fineSplitRedone), 1ull);
       }
       __syncthreads();
       const uint32_t m = sh.arrive;
@@ -1702,10 +1717,10 @@ __device__ __forceinline__ void fineItem(FineSmem<TS>& sh, const HfbUniforms& U,
       __threadfence();
       // front-to-back "over" of the groups' composites, each pixel stopping
       // where the reference stops (isPixelDone, alpha >= 0.999)
-      const float4 f0 = __ldcg(&fs.groups[(size_t)item.z * NT + tid]);
+      const float4 f0 = __ldcg(HFB_G(&fs.groups[(size_t)item.z * NT + tid]));
       fin = mk4(f0.x, f0.y, f0.z, f0.w);
       for (uint32_t g2 = 1; g2 < nG; g2++) {
-        const float4 c = __ldcg(&fs.groups[(size_t)(item.z + g2) * NT + tid]);
+        const float4 c = __ldcg(HFB_G(&fs.groups[(size_t)(item.z + g2) * NT + tid]));
         if (fin.w < 0.999f) {
           const float k = fsub(1.0f, fin.w);
           fin.x = fadd(fin.x, fmul(c.x, k));
@@ -1719,7 +1734,7 @@ __device__ __forceinline__ void fineItem(FineSmem<TS>& sh, const HfbUniforms& U,
     const uint32_t tx = tileIdx % tilesX, ty = tileIdx / tilesX;
     const TileB tbp = tileBoundsPx(W, H, TS, tx, ty);
     const uint32_t px = tbp.x0 + lx, py = tbp.y0 + ly;
-    if (write && px < W && py < H) res[(size_t)py * W + px] = make_float4(fin.x, fin.y, fin.z, fin.w);
+    if (write && px < W && py < H) (*HFB_G(&res[(size_t)py * W + px])) = make_float4(fin.x, fin.y, fin.z, fin.w);
   }
 }
 
@@ -1730,54 +1745,22 @@ fineKernel(const HfbUniforms U, const FineArgs a, const uint32_t* __restrict__ t
   using SM = FineSmem<TS>;
   extern __shared__ __align__(16) unsigned char fineSmemRaw[];
   SM& sh = *reinterpret_cast<SM*>(fineSmemRaw);
-  const uint32_t nItems = min(fs.hdr[0], fs.maxItems);
+  const uint32_t nItems = min((*HFB_G(&fs.hdr[0])), fs.maxItems);
   uint32_t* queue = reinterpret_cast<uint32_t*>(result);  // tileQueueAtomicIdx, getNextTileIdx :294-303
   while (true) {
-    if (threadIdx.x == 0) sh.queueIdx = atomicAdd(queue, 1u);
+    if (threadIdx.x == 0) sh.queueIdx = atomicAdd(HFB_G(queue), 1u);
     __syncthreads();
     const uint32_t it = sh.queueIdx;
     if (it >= nItems) break;
-    fineItem<TS, MAXL>(sh, U, a, tileList, result, fs, fs.items[it]);
+    fineItem<TS, MAXL>(sh, U, a, tileList, result, fs, (*HFB_G(&fs.items[it])));
     __syncthreads();  // the tile's shared state is rewritten for the next item
-  }
-}
-
-// batched: one queue over the work items of every instance
-template <int TS, int MAXL>
-__global__ void __launch_bounds__(TS * TS, TS == 8 ? 6 : TS == 16 ? (MAXL <= 4 ? 3 : 2) : 1)
-fineBatch(BatchView b, FineArgs base, HfbConfig cfgParam) {
-  using SM = FineSmem<TS>;
-  const HfbConfig cfg = cfgParam;
-  extern __shared__ __align__(16) unsigned char fineSmemRaw[];
-  SM& sh = *reinterpret_cast<SM*>(fineSmemRaw);
-  const uint32_t n = b.hdr->n;
-  const uint32_t total = b.itemPrefix[n];
-  while (true) {
-    if (threadIdx.x == 0) sh.queueIdx = atomicAdd(&b.hdr->fineQueue, 1u);
-    __syncthreads();
-    const uint32_t gi = sh.queueIdx;
-    if (gi >= total) break;
-    const uint32_t i = batchFind(b.itemPrefix, n, gi);
-    const BatchInst& I = b.insts[i];
-    FineArgs a = base;
-    a.S = I.S;
-    a.P = I.P;
-    a.pos = I.posNew;
-    a.tan = I.tan;
-    a.shading = I.shading;
-    a.depth = I.depth;
-    a.tiles = I.tiles;
-    a.segBuf = I.segBuf;
-    const FineScratch fs = fineScratchLayout(I.scratch, cfg, I.W, I.H);
-    const uint32_t li = gi - b.itemPrefix[i];
-    if (li < fs.maxItems) fineItem<TS, MAXL>(sh, I.U, a, I.tileList, I.result, fs, fs.items[li]);
-    __syncthreads();
   }
 }
 
 template <int TS, int MAXL>
 cudaError_t launchFineT(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, const float* pos,
                         const float* tan, const float* shading, const float* depth, HfbRasterBuffers& rb) {
+  HFB_CHECK_BIND(c);
   const HfbConfig& cfg = c->cfg;
   constexpr size_t SMEM = sizeof(FineSmem<TS>);
   int& perSM = c->fineBlocksPerSM[TS == 8 ? 0 : TS == 16 ? 1 : 2][MAXL == 4 ? 0 : MAXL == 8 ? 1 : 2];
@@ -1797,6 +1780,7 @@ cudaError_t launchFineT(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, c
                                                 cfg.tileDepthBins, grid, rb.maxDrawnSegments,
                                                 h.strandsCount * h.pointsPerStrand, dbg ? 0u : 1u, fs,
                                                 (DeviceCounters*)c->dCounters);
+  HFB_AFTER_LAUNCH(c, "fineScheduleKernel");
   FineArgs a;
   a.S = h.strandsCount;
   a.P = h.pointsPerStrand;
@@ -1814,163 +1798,17 @@ cudaError_t launchFineT(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, c
   a.segBuf = rb.tileSegments;
   a.counters = (DeviceCounters*)c->dCounters;
   fineKernel<TS, MAXL><<<grid, TS * TS, SMEM, c->stream>>>(u, a, rb.tileList, rb.rasterizerResult, fs);
+  HFB_AFTER_LAUNCH(c, "fineKernel");
   c->launches += 2;
   return cudaGetLastError();
 }
 
-// ---------------------------------------------------------------------------
-// Batched tiles pass, tile sort and fine pass: persistent over the virtual
-// blocks of every instance (hfb_frame_batch).
-// ---------------------------------------------------------------------------
-#define BATCH_LOOP(KIND)                                              \
-  const uint32_t n = b.hdr->n;                                        \
-  const uint32_t* row = b.prefix + (KIND) * (BATCH_MAX + 1);          \
-  const uint32_t totalVb = row[n];                                    \
-  for (uint32_t v = blockIdx.x; v < totalVb; v += gridDim.x) {        \
-    const uint32_t i = batchFind(row, n, v);                          \
-    const BatchInst& I = b.insts[i];                                  \
-    const uint32_t local = v - row[i], nLocal = row[i + 1] - row[i];  \
-    (void)nLocal; (void)local;                                        \
-    const TilesScratch ts = tilesScratchLayout(I.scratch, cfg, I.W, I.H, I.maxDrawn); \
-    (void)ts;
-
-__global__ void __launch_bounds__(TR_SEGS) tilesRasterBatch(BatchView b, HfbConfig cfgParam,
-                                                             DeviceCounters* __restrict__ counters) {
-  const HfbConfig cfg = cfgParam;
-  __shared__ TrShared sh;
-  BATCH_LOOP(BK_RASTER)
-    tilesRasterBody(I.U, I.P, min(I.strandsToRender, I.S), cfg.tileSize, cfg.tileDepthBins,
-                    cfg.invalidTilesPerSegmentThreshold, I.bsphere, I.posNew, I.tan, I.depth, I.tiles, I.segBuf,
-                    I.segCount, ts.binCount, counters, sh, local);
-  }
-}
-
-__global__ void __launch_bounds__(512) binScanBatch(BatchView b, HfbConfig cfgParam) {
-  const HfbConfig cfg = cfgParam;
-  __shared__ uint32_t warpSums[32];
-  BATCH_LOOP(BK_SCAN)
-    binScanBlocksBody(ts.binCount, ts.binOffset, ts.blockSums, I.T * cfg.tileDepthBins, warpSums, local);
-  }
-}
-
-__global__ void __launch_bounds__(1024) binScanSumsBatch(BatchView b, HfbConfig cfgParam) {
-  const HfbConfig cfg = cfgParam;
-  __shared__ uint32_t warpSums[32];
-  BATCH_LOOP(BK_SCAN_SUMS)
-    binScanSumsBody(ts.blockSums, divCeil(I.T * cfg.tileDepthBins, SCAN_PER_BLOCK), warpSums);
-    __syncthreads();
-  }
-}
-
-__global__ void __launch_bounds__(256) binScatterBatch(BatchView b, HfbConfig cfgParam,
-                                                        DeviceCounters* __restrict__ counters) {
-  const HfbConfig cfg = cfgParam;
-  BATCH_LOOP(BK_SCATTER)
-    binScatterBody(I.segBuf, I.maxDrawn, ts.binOffset, ts.blockSums, ts.keys, counters, local, nLocal);
-  }
-}
-
-__global__ void __launch_bounds__(256) binFinalizeBatch(BatchView b, HfbConfig cfgParam) {
-  const HfbConfig cfg = cfgParam;
-  __shared__ uint32_t smem[8][MEDIUM_BIN];
-  BATCH_LOOP(BK_FINALIZE)
-    binFinalizeBody(I.T * cfg.tileDepthBins, ts.binCount, ts.binOffset, ts.blockSums, ts.keys, I.segBuf, I.tiles,
-                    ts.largeBins, smem, local, nLocal);
-  }
-}
-
-__global__ void __launch_bounds__(1024) largeBinsBatch(BatchView b, HfbConfig cfgParam) {
-  const HfbConfig cfg = cfgParam;
-  extern __shared__ uint32_t sk[];
-  BATCH_LOOP(BK_LARGE)
-    largeBinsBody(ts.largeBins, ts.binCount, ts.binOffset, ts.blockSums, ts.keys, I.segBuf, I.tiles, sk, local,
-                  nLocal);
-  }
-}
-
-__global__ void __launch_bounds__(1024) tileSortBatch(BatchView b, HfbConfig cfgParam) {
-  const HfbConfig cfg = cfgParam;
-  __shared__ SortShared ss;
-  BATCH_LOOP(BK_SORT)
-    tileSortBody(I.T, cfg.sortBuckets, cfg.sortBucketSize, I.segCount, I.sortBuckets, I.tileList, ss);
-    __syncthreads();
-  }
-}
-
-__global__ void __launch_bounds__(1024) fineScheduleBatch(BatchView b, HfbConfig cfgParam, uint32_t grid,
-                                                          DeviceCounters* __restrict__ counters) {
-  const HfbConfig cfg = cfgParam;
-  __shared__ uint32_t warpSums[32];
-  __shared__ uint32_t totalRecords;
-  BATCH_LOOP(BK_SCHEDULE)
-    const FineScratch fs = fineScratchLayout(I.scratch, cfg, I.W, I.H);
-    const uint32_t dispMode = I.U.displayMode & 0xffu;
-    const bool dbg = dispMode == 4u && ((I.U.displayMode >> 8) & 0xffffu) != 0u;
-    fineScheduleBody(I.tileList, I.segCount, I.tiles, I.T, cfg.tileDepthBins, grid, I.maxDrawn, I.S * I.P,
-                     dbg ? 0u : 1u, fs, counters, warpSums, totalRecords);
-  }
-}
-
-// Exclusive prefix of the instances' work items; resets the batch queue.
-__global__ void __launch_bounds__(1024) fineItemPrefixBatch(BatchView b, HfbConfig cfgParam) {
-  const HfbConfig cfg = cfgParam;
-  __shared__ uint32_t warpSums[32];
-  const uint32_t n = b.hdr->n;
-  uint32_t carry = 0;
-  for (uint32_t i0 = 0; i0 < n; i0 += blockDim.x) {
-    const uint32_t i = i0 + threadIdx.x;
-    uint32_t items = 0;
-    if (i < n) {
-      const BatchInst& I = b.insts[i];
-      items = fineScratchLayout(I.scratch, cfg, I.W, I.H).hdr[0];
-    }
-    uint32_t chunk;
-    const uint32_t ex = blockExclusiveScan(items, warpSums, chunk);
-    if (i < n) b.itemPrefix[i] = carry + ex;
-    carry += chunk;
-  }
-  if (threadIdx.x == 0) {
-    b.itemPrefix[n] = carry;
-    b.hdr->fineQueue = 0;
-  }
-}
-#undef BATCH_LOOP
-
-template <int TS, int MAXL>
-cudaError_t launchFineBatchT(HfbCtx* c, const BatchView& b) {
-  const HfbConfig& cfg = c->cfg;
-  constexpr size_t SMEM = sizeof(FineSmem<TS>);
-  uint32_t& grid = c->batchGrid[BK_COUNT];  // the fine kernel's persistent grid
-  if (!grid) {
-    cudaError_t e = cudaFuncSetAttribute(fineBatch<TS, MAXL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);
-    int per = 0;
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fineBatch<TS, MAXL>, TS * TS, SMEM);
-    if (e != cudaSuccess) return e;
-    if (per < 1) return cudaErrorInvalidConfiguration;
-    grid = cfg.processorCount ? cfg.processorCount : (uint32_t)per * c->smCount;
-  }
-  DeviceCounters* dc = (DeviceCounters*)c->dCounters;
-  uint32_t& sgrid = c->batchGrid[BK_SCHEDULE];
-  if (!sgrid) sgrid = c->smCount;
-  fineScheduleBatch<<<sgrid, 1024, 0, c->stream>>>(b, cfg, grid, dc);
-  fineItemPrefixBatch<<<1, 1024, 0, c->stream>>>(b, cfg);
-  FineArgs a{};
-  a.B = cfg.tileDepthBins;
-  a.L = cfg.slicesPerPixel;
-  a.SP = cfg.shadingPoints;
-  a.CAP = cfg.avgFragmentsPerSlice * cfg.slicesPerPixel * cfg.tileSize * cfg.tileSize;
-  a.alphaQuadratic = cfg.alphaQuadratic;
-  a.alphaMul = cfg.alphaMultiplier;
-  a.counters = dc;
-  fineBatch<TS, MAXL><<<grid, TS * TS, SMEM, c->stream>>>(b, a, cfg);
-  c->launches += 3;
-  return cudaGetLastError();
-}
 
 }  // namespace
 
 cudaError_t launchTilesPass(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, const float* pos,
                             const float* tan, const float* depth, uint32_t strandsToRender, HfbRasterBuffers& rb) {
+  HFB_CHECK_BIND(c);
   const HfbConfig& cfg = c->cfg;
   const uint32_t W = rb.width, H = rb.height, TS = cfg.tileSize, B = cfg.tileDepthBins;
   const uint32_t T = divCeil(W, TS) * divCeil(H, TS);
@@ -1987,14 +1825,19 @@ cudaError_t launchTilesPass(HfbCtx* c, const HfbUniforms& u, const HfbHairData& 
     tilesRasterKernel<<<divCeil(nSeg, TR_SEGS), TR_SEGS, 0, c->stream>>>(
         u, h.pointsPerStrand, nStrands, TS, B, cfg.invalidTilesPerSegmentThreshold, bs, (const float4*)pos,
         (const float4*)tan, depth, (uint4*)rb.tiles, rb.tileSegments, rb.segmentCountPerTile, s.binCount, dc);
+    HFB_AFTER_LAUNCH(c, "tilesRasterKernel");
   }
   const uint32_t nBlocks = divCeil(TB, SCAN_PER_BLOCK);
   binScanBlocks<<<nBlocks, 512, 0, c->stream>>>(s.binCount, s.binOffset, s.blockSums, TB);
+  HFB_AFTER_LAUNCH(c, "binScanBlocks");
   binScanSums<<<1, 1024, 0, c->stream>>>(s.blockSums, nBlocks);
+  HFB_AFTER_LAUNCH(c, "binScanSums");
   binScatterKernel<<<c->smCount * 4, 256, 0, c->stream>>>(rb.tileSegments, rb.maxDrawnSegments, s.binOffset,
-                                                          s.blockSums, s.keys, dc);
+                                                          s.blockSums, s.keys, dc, TB);
+  HFB_AFTER_LAUNCH(c, "binScatterKernel");
   binFinalizeKernel<<<min(divCeil(TB, 8), (uint32_t)c->smCount * 16), 256, 0, c->stream>>>(
       TB, s.binCount, s.binOffset, s.blockSums, s.keys, rb.tileSegments, (uint4*)rb.tiles, s.largeBins);
+  HFB_AFTER_LAUNCH(c, "binFinalizeKernel");
   if (!c->largeBinsAttrSet) {
     e = cudaFuncSetAttribute(largeBinsKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, LARGE_SMEM_KEYS * 4);
     if (e != cudaSuccess) return e;
@@ -2002,16 +1845,19 @@ cudaError_t launchTilesPass(HfbCtx* c, const HfbUniforms& u, const HfbHairData& 
   }
   largeBinsKernel<<<c->smCount, 1024, LARGE_SMEM_KEYS * 4, c->stream>>>(
       s.largeBins, s.binCount, s.binOffset, s.blockSums, s.keys, rb.tileSegments, (uint4*)rb.tiles);
+  HFB_AFTER_LAUNCH(c, "largeBinsKernel");
   c->launches += nSeg ? 6 : 5;
   return cudaGetLastError();
 }
 
 cudaError_t launchTileSort(HfbCtx* c, HfbRasterBuffers& rb) {
+  HFB_CHECK_BIND(c);
   const HfbConfig& cfg = c->cfg;
   const uint32_t T = divCeil(rb.width, cfg.tileSize) * divCeil(rb.height, cfg.tileSize);
   if (cfg.sortBuckets > SORT_MAX_BUCKETS) return cudaErrorInvalidValue;
   tileSortKernel<<<1, 1024, 0, c->stream>>>(T, cfg.sortBuckets, cfg.sortBucketSize, rb.segmentCountPerTile,
                                             rb.sortBuckets, rb.tileList);
+  HFB_AFTER_LAUNCH(c, "tileSortKernel");
   c->launches += 1;
   return cudaGetLastError();
 }
@@ -2032,63 +1878,6 @@ cudaError_t launchFinePass(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h
   if (L <= 4) return launchFineT<32, 4>(c, u, h, pos, tan, shading, depth, rb);
   if (L <= 8) return launchFineT<32, 8>(c, u, h, pos, tan, shading, depth, rb);
   return cudaErrorInvalidValue;  // 32x32 tiles with more than 8 slices: too many registers per pixel
-}
-
-}  // namespace hfb
-
-namespace hfb {
-
-cudaError_t launchBatchTiles(HfbCtx* c, const BatchView& b) {
-  const HfbConfig& cfg = c->cfg;
-  DeviceCounters* dc = (DeviceCounters*)c->dCounters;
-  uint32_t* g = c->batchGrid;
-  if (!g[BK_RASTER]) {
-    int per = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, tilesRasterBatch, TR_SEGS, 0);
-    if (e != cudaSuccess) return e;
-    g[BK_RASTER] = (uint32_t)(per > 0 ? per : 1) * c->smCount;
-    g[BK_SCAN] = c->smCount * 4u;
-    g[BK_SCAN_SUMS] = c->smCount;
-    g[BK_SCATTER] = c->smCount * 8u;
-    g[BK_FINALIZE] = c->smCount * 8u;
-    g[BK_LARGE] = c->smCount;
-    e = cudaFuncSetAttribute(largeBinsBatch, cudaFuncAttributeMaxDynamicSharedMemorySize, LARGE_SMEM_KEYS * 4);
-    if (e != cudaSuccess) return e;
-  }
-  tilesRasterBatch<<<g[BK_RASTER], TR_SEGS, 0, c->stream>>>(b, cfg, dc);
-  binScanBatch<<<g[BK_SCAN], 512, 0, c->stream>>>(b, cfg);
-  binScanSumsBatch<<<g[BK_SCAN_SUMS], 1024, 0, c->stream>>>(b, cfg);
-  binScatterBatch<<<g[BK_SCATTER], 256, 0, c->stream>>>(b, cfg, dc);
-  binFinalizeBatch<<<g[BK_FINALIZE], 256, 0, c->stream>>>(b, cfg);
-  largeBinsBatch<<<g[BK_LARGE], 1024, LARGE_SMEM_KEYS * 4, c->stream>>>(b, cfg);
-  c->launches += 6;
-  return cudaGetLastError();
-}
-
-cudaError_t launchBatchSort(HfbCtx* c, const BatchView& b) {
-  if (c->cfg.sortBuckets > SORT_MAX_BUCKETS) return cudaErrorInvalidValue;
-  uint32_t& grid = c->batchGrid[BK_SORT];
-  if (!grid) grid = c->smCount;
-  tileSortBatch<<<grid, 1024, 0, c->stream>>>(b, c->cfg);
-  c->launches += 1;
-  return cudaGetLastError();
-}
-
-cudaError_t launchBatchFine(HfbCtx* c, const BatchView& b) {
-  const uint32_t TS = c->cfg.tileSize, L = c->cfg.slicesPerPixel;
-  if (TS == 8) {
-    if (L <= 4) return launchFineBatchT<8, 4>(c, b);
-    if (L <= 8) return launchFineBatchT<8, 8>(c, b);
-    return launchFineBatchT<8, 16>(c, b);
-  }
-  if (TS == 16) {
-    if (L <= 4) return launchFineBatchT<16, 4>(c, b);
-    if (L <= 8) return launchFineBatchT<16, 8>(c, b);
-    return launchFineBatchT<16, 16>(c, b);
-  }
-  if (L <= 4) return launchFineBatchT<32, 4>(c, b);
-  if (L <= 8) return launchFineBatchT<32, 8>(c, b);
-  return cudaErrorInvalidValue;
 }
 
 }  // namespace hfb

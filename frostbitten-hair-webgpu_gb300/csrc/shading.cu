@@ -5,6 +5,7 @@
 // src/passes/shadowMapPass/shared/sampleShadows.wgsl.ts:21-150, AO lookup
 // src/passes/aoPass/shared/textureAo.wgsl.ts:7-12, linearizeDepth
 // src/passes/_shaderSnippets/linearDepth.wgsl.ts:9-22.
+#define HFB_TU 2
 #include "hfb_internal.cuh"
 #include "hfb_math.cuh"
 
@@ -154,9 +155,9 @@ __device__ __forceinline__ void shadingBody(const HfbUniforms& U, uint32_t S, ui
   float t = (float)sp / (float)SP;
   uint32_t i0, i1;
   float ts = remapToIndices(P, t, i0, i1);
-  float4 a = __ldg(&pos[(size_t)strand * P + i0]);
-  float4 b = __ldg(&pos[(size_t)strand * P + i1]);
-  float4 tg = __ldg(&tan[(size_t)strand * P + i1]);
+  float4 a = __ldg(HFB_G(&pos[(size_t)strand * P + i0]));
+  float4 b = __ldg(HFB_G(&pos[(size_t)strand * P + i1]));
+  float4 tg = __ldg(HFB_G(&tan[(size_t)strand * P + i1]));
   f3 s0 = mk3(a.x, a.y, a.z), s1 = mk3(b.x, b.y, b.z);
   f3 t0 = norm3(sub3(s1, s0));
   f3 posO = mix3(s0, s1, ts);
@@ -208,7 +209,7 @@ __device__ __forceinline__ void shadingBody(const HfbUniforms& U, uint32_t S, ui
                               ld4(make_float4(U.light2.colorAndEnergy.x, U.light2.colorAndEnergy.y, U.light2.colorAndEnergy.z, U.light2.colorAndEnergy.w)),
                               toCam, xyz(tanWS), xyz(posWS), shadow, aoT));
   float alpha = sp >= SP - 1u ? 0.0f : 1.0f;
-  shading[gid] = make_float4(sum.x, sum.y, sum.z, alpha);  // _setShadingPoint
+  *HFB_G(&shading[gid]) = make_float4(sum.x, sum.y, sum.z, alpha);  // _setShadingPoint
 }
 
 __global__ void __launch_bounds__(128)
@@ -220,42 +221,21 @@ shadingKernel(const HfbUniforms U, uint32_t S, uint32_t P, uint32_t SP, float zN
               blockIdx.x * blockDim.x + threadIdx.x);
 }
 
-// batched: persistent over the virtual blocks of every instance
-__global__ void __launch_bounds__(128) shadingBatch(BatchView b, uint32_t SP, float zNear, float zFar) {
-  const uint32_t n = b.hdr->n;
-  const uint32_t* row = b.prefix + BK_SHADING * (BATCH_MAX + 1);
-  const uint32_t total = row[n];
-  for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
-    const uint32_t i = batchFind(row, n, v);
-    const BatchInst& I = b.insts[i];
-    shadingBody(I.U, I.S, I.P, SP, zNear, zFar, I.posNew, I.tan, I.shadingDepth, I.ao, I.aoW, I.aoH, I.sm,
-                I.smSize, I.shading, (v - row[i]) * 128u + threadIdx.x);
-  }
-}
-
 }  // namespace
 
 cudaError_t launchShading(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, const float* pos,
                           const float* tan, const float* depth, const float* ao, uint32_t aoW, uint32_t aoH,
                           const float* sm, uint32_t smSize, float* shading) {
+  HFB_CHECK_BIND(c);
   uint32_t SP = c->cfg.shadingPoints;
   uint32_t n = h.strandsCount * SP;
   shadingKernel<<<divCeil(n, 128), 128, 0, c->stream>>>(u, h.strandsCount, h.pointsPerStrand, SP,
                                                           c->cfg.cameraNear, c->cfg.cameraFar,
                                                           (const float4*)pos, (const float4*)tan, depth, ao,
                                                           aoW, aoH, sm, smSize, (float4*)shading);
+  HFB_AFTER_LAUNCH(c, "shadingKernel");
   c->launches += 1;
   return cudaGetLastError();
 }
 
-}  // namespace hfb
-
-namespace hfb {
-cudaError_t launchBatchShading(HfbCtx* c, const BatchView& b) {
-  uint32_t& grid = c->batchGrid[BK_SHADING];
-  if (!grid) grid = c->smCount * 16u;
-  shadingBatch<<<grid, 128, 0, c->stream>>>(b, c->cfg.shadingPoints, c->cfg.cameraNear, c->cfg.cameraFar);
-  c->launches += 1;
-  return cudaGetLastError();
-}
 }  // namespace hfb

@@ -5,6 +5,7 @@
 // collisions}.wgsl.ts and grids/*.wgsl.ts.  All arithmetic follows the fixed
 // fp32 order of hfb_math.cuh, so results are reproducible run to run; the
 // grid splat is integer (i32 fixed point, wrapping adds), hence order-free.
+#define HFB_TU 1
 #include "hfb_internal.cuh"
 #include "hfb_math.cuh"
 
@@ -61,7 +62,7 @@ __device__ __forceinline__ float sampleSDF(const float* __restrict__ sdf, uint32
   int x1 = min(max(x0 + 1, 0), m), y1 = min(max(y0 + 1, 0), m), z1 = min(max(z0 + 1, 0), m);
   x0 = min(max(x0, 0), m); y0 = min(max(y0, 0), m); z0 = min(max(z0, 0), m);
   const size_t DD = (size_t)D * D;
-  auto T = [&](int x, int y, int z) { return __ldg(sdf + (size_t)z * DD + (size_t)y * D + x); };
+  auto T = [&](int x, int y, int z) { return __ldg(HFB_G(sdf + (size_t)z * DD + (size_t)y * D + x)); };
   float c00 = mixf(T(x0, y0, z0), T(x1, y0, z0), ax);
   float c10 = mixf(T(x0, y1, z0), T(x1, y1, z0), ax);
   float c01 = mixf(T(x0, y0, z1), T(x1, y0, z1), ax);
@@ -104,7 +105,7 @@ __device__ __forceinline__ void gridPreSimBody(const HfbSimUniforms& u, uint32_t
   }
   // getDensityGradient, :111-159
   uint32_t idx0 = gridIdx(G, x, y, z);
-  float d0 = gridDecode(__ldg(&dv[idx0].w));
+  float d0 = gridDecode(__ldg(HFB_G(&dv[idx0].w)));
   f3 g = mk3(0.0f, 0.0f, 0.0f);
   const int off[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
 #pragma unroll
@@ -114,14 +115,14 @@ __device__ __forceinline__ void gridPreSimBody(const HfbSimUniforms& u, uint32_t
     if (!(ox < 0 || oy < 0 || oz < 0)) {
       uint32_t idxO = gridIdx(G, (uint32_t)ox, (uint32_t)oy, (uint32_t)oz);
       if (idxO != idx0) {
-        float dO = gridDecode(__ldg(&dv[idxO].w));
+        float dO = gridDecode(__ldg(HFB_G(&dv[idxO].w)));
         float m = fmaxf(fsub(d0, dO), 0.0f);
         r = mul3s(mk3((float)off[k][0], (float)off[k][1], (float)off[k][2]), m);
       }
     }
     g = add3(g, r);
   }
-  gw[idx0] = make_float4(g.x, g.y, g.z, wind);
+  *HFB_G(&gw[idx0]) = make_float4(g.x, g.y, g.z, wind);
 }
 
 __global__ void __launch_bounds__(256) gridPreSimKernel(const HfbSimUniforms u, uint32_t G, const int4* __restrict__ dv,
@@ -162,10 +163,10 @@ __device__ __forceinline__ float4 verletPoint(const HfbSimUniforms& u, uint32_t 
         f3 w = cellWeights(x, y, z, co.p);
         float wl = len3(w);
         uint32_t idx = gridIdx(G, x, y, z);
-        float4 a = __ldg(&gw[idx]);
+        float4 a = __ldg(HFB_G(&gw[idx]));
         grad = add3(grad, mul3(w, mk3(a.x, a.y, a.z)));
         windStr = fadd(windStr, fmul(wl, a.w));
-        int4 b = __ldg(&dv[idx]);
+        int4 b = __ldg(HFB_G(&dv[idx]));
         vel = add3(vel, mul3(w, mk3(gridDecode(b.x), gridDecode(b.y), gridDecode(b.z))));
         dens = fadd(dens, fmul(wl, gridDecode(b.w)));
       }
@@ -209,20 +210,20 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
   for (uint32_t i = tid; i < nPts; i += SIM_THREADS) {
     const uint32_t ls = i / P, pt = i - ls * P;
     const size_t gi = (size_t)s0 * P + i;
-    const f4 posNow = ld4(__ldg(&now[gi]));
+    const f4 posNow = ld4(__ldg(HFB_G(&now[gi])));
     wk[ls * R + pt] = pt == 0u ? make_float4(posNow.x, posNow.y, posNow.z, posNow.w)
-                               : verletPoint(u, G, gmin, gmax, s0 + ls, posNow, ld4(prev[gi]), dv, gw);
-    sl[ls * R + pt] = __ldg(&segLen[gi]);
-    const float4 i0 = __ldg(&initial[gi]);
+                               : verletPoint(u, G, gmin, gmax, s0 + ls, posNow, ld4(*HFB_G(&prev[gi])), dv, gw);
+    sl[ls * R + pt] = __ldg(HFB_G(&segLen[gi]));
+    const float4 i0 = __ldg(HFB_G(&initial[gi]));
     float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
     if (pt + 3u < P) {  // applyConstraint_localShape constants (constraints.wgsl.ts:54-99)
-      const float4 i1 = __ldg(&initial[gi + 1u]), i2 = __ldg(&initial[gi + 2u]);
+      const float4 i1 = __ldg(HFB_G(&initial[gi + 1u])), i2 = __ldg(HFB_G(&initial[gi + 2u]));
       f3 cI = div3s(add3(add3(mk3(i0.x, i0.y, i0.z), mk3(i1.x, i1.y, i1.z)), mk3(i2.x, i2.y, i2.z)), 3.0f);
       const float h0 = len3(sub3(cI, mk3(i1.x, i1.y, i1.z)));
       const float wT = fadd(fadd(i0.w, fmul(2.0f, i1.w)), i2.w);
       c = make_float4(h0, fmul(i0.w / wT, 2.0f), fmul(i1.w / wT, -4.0f), fmul(i2.w / wT, 2.0f));
     } else if (pt >= jTan && pt >= 1u) {  // applyConstraint_matchInitialTangent (:100-120)
-      const float4 im = __ldg(&initial[gi - 1u]);
+      const float4 im = __ldg(HFB_G(&initial[gi - 1u]));
       c = make_float4(fsub(i0.x, im.x), fsub(i0.y, im.y), fsub(i0.z, im.z), 0.0f);
     }
     lc[ls * R + pt] = c;
@@ -268,7 +269,7 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
       if (j == 0u) continue;
       const float x = (float)j / (float)(P - 1u);
       const float att = fsub(1.0f, sat(fsub(x, u.globalConstrExtent) / u.globalConstrFade));
-      const float4 pi = __ldg(&initial[(size_t)s0 * P + i]);
+      const float4 pi = __ldg(HFB_G(&initial[(size_t)s0 * P + i]));
       const float k = fmul(kGlob, att);
       float4 p = wk[ls * R + j];
       f3 dvv = mk3(fsub(pi.x, p.x), fsub(pi.y, p.y), fsub(pi.z, p.z));
@@ -351,7 +352,7 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
   // --- write back into the PREV buffer, coalesced (:268-272) ---
   for (uint32_t i = tid; i < nPts; i += SIM_THREADS) {
     const uint32_t ls = i / P, pt = i - ls * P;
-    prev[(size_t)s0 * P + i] = wk[ls * R + pt];
+    *HFB_G(&prev[(size_t)s0 * P + i]) = wk[ls * R + pt];
   }
   __syncthreads();  // the block's staging is reused by its next strands
 }
@@ -376,7 +377,7 @@ __device__ __forceinline__ void gridPostSimBody(const HfbSimUniforms& u, uint32_
                                                 unsigned* __restrict__ dv, uint32_t i) {
   const bool valid = i < N;
   float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
-  if (valid) { a = __ldg(&prev[i]); b = __ldg(&now[i]); }
+  if (valid) { a = __ldg(HFB_G(&prev[i])); b = __ldg(HFB_G(&now[i])); }
   const f3 pn = mk3(b.x, b.y, b.z);
   const f3 vel = sub3(pn, mk3(a.x, a.y, a.z));
   const GridCo co = gridCell(G, gridMin(u), gridMax(u), pn);
@@ -390,7 +391,7 @@ __device__ __forceinline__ void gridPostSimBody(const HfbSimUniforms& u, uint32_
     const uint32_t idx = gridIdx(G, x, y, z);
     const f3 w = cellWeights(x, y, z, co.p);
     const f3 cv = mul3(vel, w);
-    unsigned* c = dv + 4u * idx;
+    unsigned* c = reinterpret_cast<unsigned*>(HFB_G(reinterpret_cast<uint4*>(dv + 4u * idx)));
     atomicAdd(c + 0, (unsigned)gridEncode(cv.x));
     atomicAdd(c + 1, (unsigned)gridEncode(cv.y));
     atomicAdd(c + 2, (unsigned)gridEncode(cv.z));
@@ -404,57 +405,15 @@ gridPostSimKernel(const HfbSimUniforms u, uint32_t N, uint32_t G, const float4* 
   gridPostSimBody(u, N, G, prev, now, dv, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
-// ---- batched: persistent over the virtual blocks of every instance ----
-__global__ void __launch_bounds__(256) gridPreSimBatch(BatchView b, uint32_t G) {
-  const uint32_t n = b.hdr->n;
-  const uint32_t* row = b.prefix + BK_GRID_PRE * (BATCH_MAX + 1);
-  const uint32_t total = row[n];
-  for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
-    const uint32_t i = batchFind(row, n, v);
-    const BatchInst& I = b.insts[i];
-    gridPreSimBody(I.SU, G, I.dv, I.gw, I.sdf, I.sdfDims, (v - row[i]) * 256u + threadIdx.x);
-  }
-}
-
-__global__ void __launch_bounds__(SIM_THREADS) simIntegrateBatch(BatchView b, uint32_t G) {
-  extern __shared__ float4 simSmem[];
-  const uint32_t n = b.hdr->n;
-  const uint32_t* row = b.prefix + BK_INTEGRATE * (BATCH_MAX + 1);
-  const uint32_t total = row[n];
-  for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
-    const uint32_t i = batchFind(row, n, v);
-    const BatchInst& I = b.insts[i];
-    // integration reads positions[1 - current] (prev) and [current] (now), writes the former
-    simIntegrateBody(I.SU, I.S, I.P, G, I.posNew, I.posOld, I.initial, I.segLen, I.dv, I.gw, I.sdf, I.sdfDims,
-                     simSmem, v - row[i]);
-  }
-}
-
-__global__ void __launch_bounds__(256) gridPostSimBatch(BatchView b, uint32_t G) {
-  const uint32_t n = b.hdr->n;
-  const uint32_t* row = b.prefix + BK_GRID_POST * (BATCH_MAX + 1);
-  const uint32_t total = row[n];
-  for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
-    const uint32_t i = batchFind(row, n, v);
-    const BatchInst& I = b.insts[i];
-    // after the swap: prev = the old current positions, now = the new ones
-    gridPostSimBody(I.SU, I.S * I.P, G, I.posOld, I.posNew, (unsigned*)I.dv, (v - row[i]) * 256u + threadIdx.x);
-  }
-}
-
-size_t simSmemMax() {
-  size_t m = 0;
-  for (uint32_t P = 4; P <= 128; P++) m = m > simSmemBytes(P) ? m : simSmemBytes(P);
-  return m;
-}
-
 }  // namespace
 
 cudaError_t launchGridPreSim(HfbCtx* c, const HfbSimUniforms& u, const int32_t* dv, float* gw,
                              const float* sdf, uint32_t sdfDims) {
+  HFB_CHECK_BIND(c);
   uint32_t G = c->cfg.gridDims;
   uint32_t n = G * G * G;
   gridPreSimKernel<<<divCeil(n, 256), 256, 0, c->stream>>>(u, G, (const int4*)dv, (float4*)gw, sdf, sdfDims);
+  HFB_AFTER_LAUNCH(c, "gridPreSimKernel");
   c->launches += 1;
   return cudaGetLastError();
 }
@@ -462,6 +421,7 @@ cudaError_t launchGridPreSim(HfbCtx* c, const HfbSimUniforms& u, const int32_t* 
 cudaError_t launchSimIntegrate(HfbCtx* c, const HfbSimUniforms& u, const HfbHairData& h, float* prev,
                                const float* now, const float* initial, const float* segLen,
                                const int32_t* dv, const float* gw, const float* sdf, uint32_t sdfDims) {
+  HFB_CHECK_BIND(c);
   const uint32_t S = h.strandsCount, P = h.pointsPerStrand;
   const size_t smem = simSmemBytes(P);
   if (smem > c->simSmemSet) {
@@ -473,39 +433,14 @@ cudaError_t launchSimIntegrate(HfbCtx* c, const HfbSimUniforms& u, const HfbHair
   simIntegrateKernel<<<divCeil(S, simStrandsPerBlock(P)), SIM_THREADS, smem, c->stream>>>(
       u, S, P, c->cfg.gridDims, (float4*)prev, (const float4*)now, (const float4*)initial, segLen,
       (const int4*)dv, (const float4*)gw, sdf, sdfDims);
-  c->launches += 1;
-  return cudaGetLastError();
-}
-
-cudaError_t launchBatchSim(HfbCtx* c, const BatchView& b, BatchKind k) {
-  const uint32_t G = c->cfg.gridDims;
-  uint32_t& grid = c->batchGrid[k];
-  if (k == BK_GRID_PRE) {
-    if (!grid) grid = c->smCount * 8u;
-    gridPreSimBatch<<<grid, 256, 0, c->stream>>>(b, G);
-  } else if (k == BK_INTEGRATE) {
-    const size_t smem = simSmemMax();
-    if (!grid) {
-      cudaError_t e = cudaFuncSetAttribute(simIntegrateBatch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      int perSM = 0;
-      if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, simIntegrateBatch, SIM_THREADS, smem);
-      if (e != cudaSuccess) return e;
-      grid = (uint32_t)(perSM > 0 ? perSM : 1) * c->smCount;
-    }
-    simIntegrateBatch<<<grid, SIM_THREADS, smem, c->stream>>>(b, G);
-  } else if (k == BK_GRID_POST) {
-    if (!grid) grid = c->smCount * 8u;
-    gridPostSimBatch<<<grid, 256, 0, c->stream>>>(b, G);
-  } else {
-    return cudaErrorInvalidValue;
-  }
+  HFB_AFTER_LAUNCH(c, "simIntegrateKernel");
   c->launches += 1;
   return cudaGetLastError();
 }
 
 cudaError_t launchGridPostSim(HfbCtx* c, const HfbSimUniforms& u, const HfbHairData& h, const float* prev,
                               const float* now, int32_t* dv) {
+  HFB_CHECK_BIND(c);
   uint32_t G = c->cfg.gridDims;
   cudaError_t e = cudaMemsetAsync(dv, 0, (size_t)G * G * G * 16, c->stream);  // clearDensityVelocityBuffer
   if (e != cudaSuccess) return e;
@@ -513,6 +448,7 @@ cudaError_t launchGridPostSim(HfbCtx* c, const HfbSimUniforms& u, const HfbHairD
   if (N) {
     gridPostSimKernel<<<divCeil(N, 256), 256, 0, c->stream>>>(u, N, G, (const float4*)prev,
                                                                (const float4*)now, (unsigned*)dv);
+    HFB_AFTER_LAUNCH(c, "gridPostSimKernel");
     c->launches += 1;
   }
   return cudaGetLastError();

@@ -1,0 +1,96 @@
+"""Autotuner of batched frames: picks the pass constants a batch runs with.
+
+The candidates are tile size x depth bins (x fine-pass CTA count); each is
+timed on the batch itself with ``hfb_frame_batch`` (CUDA events, after
+warm-up frames), and the fastest candidate that drops no (segment, tile)
+record wins -- a dropped record would change the image, so such a
+candidate is not an equal-accuracy choice.  The segment pool is sized per
+tile area (``avg_segments_per_tile`` scales with the tile's pixel count),
+as the reference sizes it per tile.  Every candidate renders exactly what
+the reference renders with the same constants; the tuner only chooses
+among them.
+"""
+from __future__ import annotations
+
+import dataclasses
+import itertools
+import time
+
+import torch
+
+from .config import HairConfig
+from .lib import Context
+from .renderer import BatchRenderer, Renderer
+
+TILE_SIZES = (8, 16, 32)
+DEPTH_BINS = (4, 8, 16, 32)
+
+
+@dataclasses.dataclass
+class Trial:
+    tile_size: int
+    depth_bins: int
+    processor_count: int
+    ms: float
+    dropped: int
+
+    def as_dict(self):
+        return dataclasses.asdict(self)
+
+
+def candidate_config(base: HairConfig, tile_size: int, depth_bins: int, processor_count: int = 0) -> HairConfig:
+    scale = (tile_size / base.tile_size) ** 2
+    return dataclasses.replace(base, tile_size=tile_size, tile_depth_bins=depth_bins,
+                               processor_count=processor_count,
+                               avg_segments_per_tile=max(16, int(round(base.avg_segments_per_tile * scale))))
+
+
+def time_batch(renderers: list[Renderer], ctx: Context, stream, frames: int, warmup: int) -> tuple[float, int]:
+    """Mean ms per batched frame, and the records dropped meanwhile."""
+    batch = BatchRenderer(renderers)
+    for _ in range(warmup):
+        batch.frame()
+    torch.cuda.synchronize()
+    d0 = ctx.counters()["tileRecordsDropped"]
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(frames):
+        batch.frame()
+    t1.record(stream)
+    torch.cuda.synchronize()
+    return t0.elapsed_time(t1) / frames, ctx.counters()["tileRecordsDropped"] - d0
+
+
+def tune(renderers: list[Renderer], base: HairConfig, device: int, stream=None, tile_sizes=TILE_SIZES,
+         depth_bins=DEPTH_BINS, frames: int = 3, warmup: int = 2, budget_s: float = 120.0):
+    """Times every candidate on the batch; leaves the renderers on the
+    winner's context.  Returns (best HairConfig, its Context, trials)."""
+    trials: list[Trial] = []
+    ctxs: list[Context] = []
+    best = None
+    t_start = time.perf_counter()
+    for ts, b in itertools.product(tile_sizes, depth_bins):
+        if ctxs and time.perf_counter() - t_start > budget_s:
+            break
+        cfg = candidate_config(base, ts, b)
+        ctx = Context(cfg.to_c(), device)
+        ctxs.append(ctx)
+        if stream is not None:
+            ctx.set_stream(stream)
+        for r in renderers:  # frees the previous candidate's raster buffers
+            r.use_config(cfg, ctx)
+        ms, dropped = time_batch(renderers, ctx, stream or torch.cuda.current_stream(), frames, warmup)
+        trials.append(Trial(ts, b, cfg.processor_count, ms, dropped))
+        if dropped == 0 and (best is None or ms < best[0]):
+            best = (ms, cfg, ctx)
+    if best is None:
+        raise RuntimeError("no candidate rendered without dropping records")
+    _, cfg, ctx = best
+    for r in renderers:
+        r.use_config(cfg, ctx)
+    torch.cuda.synchronize()
+    for c in ctxs:
+        if c is not ctx:
+            c.close()
+    return cfg, ctx, trials

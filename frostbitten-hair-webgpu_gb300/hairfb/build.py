@@ -49,7 +49,20 @@ def _headers():
     return hs
 
 
-def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
+CHECKED_LIB = os.path.join(OUT_DIR, "libhairfb_checked.so")
+
+
+def build(force: bool = False, verbose: bool = False, extra_flags=(), checked: bool = False) -> str:
+    """Builds libhairfb.so; with ``checked``, the self-checking variant
+    libhairfb_checked.so (device index checks that print and skip, for
+    diagnosing a fault; select it with HAIRFB_LIBRARY)."""
+    obj_dir, lib = (os.path.join(ROOT, "_build", "checked"), CHECKED_LIB) if checked else (OBJ_DIR, LIB)
+    if checked:
+        extra_flags = tuple(extra_flags) + ("-DHFB_DEVICE_CHECKS",)
+    return _build(force, verbose, extra_flags, obj_dir, lib)
+
+
+def _build(force, verbose, extra_flags, OBJ_DIR, LIB) -> str:
     os.makedirs(OUT_DIR, exist_ok=True)
     os.makedirs(OBJ_DIR, exist_ok=True)
     hdrs = _headers()

@@ -11,7 +11,9 @@ import threading
 
 from .config import HfbConfig
 
-LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libhairfb.so")
+# HAIRFB_LIBRARY selects another build of the library (e.g. the self-checking one)
+LIB_PATH = os.environ.get("HAIRFB_LIBRARY") or \
+    os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libhairfb.so")
 
 HFB_OK = 0
 HFB_ERR_INVALID_ARGUMENT = -1
@@ -94,6 +96,7 @@ SIGNATURES = {
     "hfb_tiles_pass_noalloc": (I, [P, P, P, P, P, P, U32, P]),
     "hfb_frame": (I, [P, P]),
     "hfb_frame_batch": (I, [P, P, U32]),
+    "hfb_frame_batch_profile": (I, [P, P, U32, P]),
 }
 
 _lock = threading.Lock()

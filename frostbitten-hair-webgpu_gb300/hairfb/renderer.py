@@ -50,6 +50,20 @@ class Renderer:
         self.frame_idx = 0
         self.uniforms = UN.pack_render_uniforms(inst.scene, inst.cfg)
 
+    def use_config(self, cfg: HairConfig, ctx: Context) -> None:
+        """Re-targets the renderer to other pass constants (a context of
+        that config): new raster buffers and uniforms; the simulation state
+        and the hair stay resident.  The grid size must not change."""
+        assert cfg.grid_dims == self.cfg.grid_dims and cfg.shading_points == self.cfg.shading_points
+        old = self.rb
+        self.cfg = cfg
+        self.ctx = ctx
+        self.rb = RasterBuffers(ctx, self.inst.width, self.inst.height)
+        for p in (self.grid_pre, self.integrate, self.grid_post, self.shading, self.tiles, self.sort, self.fine):
+            p.ctx = ctx
+        self.uniforms = UN.pack_render_uniforms(self.inst.scene, cfg)
+        old.close()
+
     def sim_uniforms(self, frame_idx: int) -> bytes:
         i = self.inst
         return UN.pack_sim_uniforms(i.sim, i.scene.model_matrix, i.scene.sdf_bounds, i.scene.grid_bounds,

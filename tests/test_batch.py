@@ -1,11 +1,10 @@
 """Whole frames: hfb_frame (one instance, one call) and hfb_frame_batch (many
-instances, one persistent launch per pass, replayed as a captured CUDA
-graph) against the pass-by-pass path on the same instances.
+instances, each instance's passes on one of the context's worker streams)
+against the pass-by-pass path on the same instances.
 
 Bars: positions, density grid, tile counts, per-bin depth bounds, lists and
-the tile list bit-exact (the batched kernels run the same arithmetic);
-shading within 1e-6; pixels within 1/255 (the fine pass may split a heavy
-tile differently when its CTA count differs).
+the tile list bit-exact (the same kernels run the same arithmetic);
+shading within 1e-6; pixels within 1/255.
 """
 
 import numpy as np
@@ -20,6 +19,8 @@ if not torch.cuda.is_available():
     pytest.skip("needs a CUDA GPU", allow_module_level=True)
 
 from hairfb import synthetic  # noqa: E402
+import ctypes  # noqa: E402
+
 from hairfb.lib import Context, HfbInstance  # noqa: E402
 from hairfb.renderer import BatchRenderer, Renderer  # noqa: E402
 
@@ -72,26 +73,45 @@ def test_frame_matches_pass_by_pass():
             _compare(_state(ref), _state(nat), ref, f)
 
 
-def test_frame_batch_matches_each_instance_alone():
-    insts = _instances()
+def _batch_vs_alone(insts, frames, profile_frame=None):
     alone = [Renderer(inst, 0) for inst in insts]
     ctx = Context(insts[0].cfg.to_c(), 0)
     batch = BatchRenderer([Renderer(inst, 0, ctx=ctx) for inst in insts])
     for r in alone:
         r.before_first_frame()
     batch.before_first_frame()
-    l0 = ctx.counters()["launches"]
-    for f in range(4):  # the first batch runs plain launches, the later ones replay the graph
+    for f in range(frames):
         for r in alone:
             r.frame()
-        batch.frame()
+        if f == profile_frame:  # pass by pass on the context's stream, timed
+            n = len(batch.renderers)
+            arr = (HfbInstance * n)(*[r.instance() for r in batch.renderers])
+            pm = (ctypes.c_float * 8)()
+            ctx.call("hfb_frame_batch_profile", arr, n, pm)
+            for r, inst in zip(batch.renderers, arr):
+                r.after_native_frame(inst)
+            assert all(v >= 0.0 for v in pm) and sum(pm) > 0.0, list(pm)
+        else:
+            batch.frame()
         torch.cuda.synchronize()
         for ra, rb in zip(alone, batch.renderers):
             _compare(_state(ra), _state(rb), ra, f)
             assert ra.hair._current == rb.hair._current
-    # one persistent launch per pass kind for the whole batch, every frame
-    per_frame = (ctx.counters()["launches"] - l0) / 4
-    assert per_frame <= 20, per_frame
+    return ctx
+
+
+def test_frame_batch_matches_each_instance_alone():
+    _batch_vs_alone(_instances(), 4, profile_frame=2)
+
+
+def test_frame_batch_more_instances_than_streams():
+    """12 instances on 8 worker streams: streams carry several instances."""
+    rng = np.random.Generator(np.random.PCG64(11))
+    common = dict(tile_size=16, depth_bins=8, slices=4, shading_points=8, grid_dims=32, iterations=4)
+    insts = [synthetic.make_instance(rng, strands=int(rng.integers(200, 1500)), points=int(rng.choice([16, 24, 32])),
+                                     width=int(rng.choice([128, 256])), height=int(rng.choice([128, 192])), **common)
+             for _ in range(12)]
+    _batch_vs_alone(insts, 2)
 
 
 def test_frame_batch_rejects_bad_instances():

@@ -382,6 +382,27 @@ def test_fine_pass_split_tiles_with_full_pools(oracle):
     assert err.max() <= 1.0 / 255.0, f"max pixel error {err.max():.4g} (> 1/255)"
 
 
+@pytest.mark.parametrize("strands,width,height", [(300, 320, 240), (400, 512, 512)])
+def test_fine_schedule_items_match_the_tile_list(oracle, strands, width, height):
+    """Without split tiles the fine pass's work list holds exactly one item
+    per drawn tile (the schedule once counted the idle threads of its last
+    1024-entry chunk as items, and the fine pass read them from stale
+    scratch memory)."""
+    inst = small_instance(strands=strands, width=width, height=height)
+    fr = frame_of(inst)
+    ctx, hair, rb, d = _raster_gpu(inst, fr)
+    hair.shading.copy_(torch.as_tensor(_shading_input(inst)))
+    HairFinePass(ctx).cmd_rasterize_slices_hair(fr.uniforms, hair, d, rb)
+    ctx.sync()
+    cnt = ctx.counters()
+    assert cnt["fineSplitTiles"] == 0, "the case splits tiles: the item count is not the tile count"
+    drawn = int(rb.read_tile_list()[0])
+    assert 0 < drawn < rb.tile_count() and drawn % 1024 != 0, drawn
+    items = int(rb._download(rb.rb.scratch, 1, np.uint32)[0])  # the fine scratch header: [0] = work items
+    assert items == drawn, (items, drawn)
+    assert cnt["badWorkItems"] == 0
+
+
 def test_fine_pass_reads_arbitrary_list_order(oracle):
     """The fine pass walks whatever list it is given: feed it the oracle's
     LIFO lists (not the tiles pass's contiguous layout)."""
