@@ -513,8 +513,7 @@ def report_batched(args, res, world, dist):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded; no public dataset exists for this path)",
         "config": {"workload": "batched64", "describe": WORKLOADS["batched64"],
-                   "step": f"one batched frame of all {n} instances (hfb_frame_batch: each instance's passes on one "
-                           f"of 8 worker streams)",
+                   "step": f"one batched frame of all {n} instances (hfb_frame_batch, captured CUDA graph)",
                    "l2": "inputs larger than L2 (all instances' positions, grids and buffers ~ several GB)",
                    "frames_per_step": n, "tuned": {"tile_size": cfg.tile_size, "depth_bins": cfg.tile_depth_bins,
                                                    "slices": cfg.slices_per_pixel,

@@ -1,24 +1,20 @@
-// Whole frames: one pass of one instance (framePass), and hfb_frame_batch's
-// frame of many instances on worker streams.
+// Whole frames: one pass of one instance (framePass, the launches of
+// hfb_frame), and hfb_frame_batch's batched frame.
 //
-// A batched frame runs each instance's own pass sequence -- the same
-// launches as hfb_frame -- on one of BATCH_STREAMS worker streams forked from
-// the context's stream and joined back into it.  Instances share no device
-// buffer (the device counters take atomics only), so the streams run their
-// instances' kernels side by side: the small launches of a small instance
-// (the one-CTA tile sort and fine schedule, a tiles raster of a few hundred
-// blocks) fill the SMs another instance leaves idle.  Instances go to the
-// stream with the least work so far, largest first.
-#include <algorithm>
-#include <numeric>
-#include <vector>
+// A batched frame runs every pass once for all instances: each pass kind
+// is one persistent launch over the "virtual blocks" (the blocks the
+// single-instance kernel would launch) of every instance.  The host writes
+// one prefix row per pass kind over the instances into a device table with
+// the instances' pointers and uniforms; everything that changes from one
+// batch to the next is data in device memory, so the kernels' launch
+// parameters never change and one captured CUDA graph serves every batch of
+// the context.
+#include <cstring>
 
 #define HFB_TU 5
 #include "hfb_internal.cuh"
 
 namespace hfb {
-
-static_assert(BATCH_STREAMS == sizeof(HfbCtx::batchStreams) / sizeof(cudaStream_t), "stream table size");
 
 // cmdClearBeforeRender of the tiles, fine and sort passes (hairTilesPass.ts:48-52,
 // hairFinePass.ts:50-55, hairTileSortPass.ts:63-68).
@@ -76,74 +72,264 @@ cudaError_t framePass(HfbCtx* c, HfbInstance* in, FramePass p) {
 
 namespace {
 
-// Rough GPU work of one instance's frame, for balancing the streams: the
-// per-point passes and the per-pixel passes.
-double frameWork(const HfbInstance& in) {
-  return (double)in.hair.strandsCount * in.hair.pointsPerStrand +
-         0.25 * (double)in.raster.width * in.raster.height;
+constexpr uint32_t CLEAR_CHUNK = 65536;  // bytes cleared per virtual block
+
+struct Range {
+  unsigned char* p;
+  size_t bytes;
+};
+
+// What a frame clears for one instance before the raster passes: the
+// reference's cmdClearBeforeRender of the tiles, fine and sort passes
+// (hairTilesPass.ts:48-52, hairFinePass.ts:50-55, hairTileSortPass.ts:63-68)
+// and the tiles pass's own counters.
+__host__ __device__ inline uint32_t frameRanges(const HfbConfig& cfg, const BatchInst& I, Range* r) {
+  const size_t TB = (size_t)I.T * cfg.tileDepthBins;
+  const TilesScratch ts = tilesScratchLayout(I.scratch, cfg, I.W, I.H, I.maxDrawn);
+  r[0] = {(unsigned char*)I.tiles, TB * 16};
+  r[1] = {(unsigned char*)I.segCount, (size_t)I.T * 4};
+  r[2] = {(unsigned char*)I.segBuf, 4};
+  r[3] = {(unsigned char*)I.result, 16 + (size_t)I.W * I.H * 16};
+  r[4] = {(unsigned char*)I.tileList, 4};
+  r[5] = {(unsigned char*)I.sortBuckets, (size_t)cfg.sortBuckets * 8};
+  r[6] = {(unsigned char*)ts.binCount, TB * 4};
+  r[7] = {(unsigned char*)ts.largeBins, 4};
+  return 8;
 }
 
-cudaError_t ensureStreams(HfbCtx* c) {
-  cudaError_t e = cudaSuccess;
-  if (!c->batchFork) e = cudaEventCreateWithFlags(&c->batchFork, cudaEventDisableTiming);
-  for (uint32_t s = 0; s < BATCH_STREAMS && e == cudaSuccess; s++) {
-    if (!c->batchStreams[s]) e = cudaStreamCreateWithFlags(&c->batchStreams[s], cudaStreamNonBlocking);
-    if (e == cudaSuccess && !c->batchJoin[s]) e = cudaEventCreateWithFlags(&c->batchJoin[s], cudaEventDisableTiming);
-  }
-  return e;
+// clearDensityVelocityBuffer of GridPostSimPass (gridPostSimPass.ts:33-59)
+__host__ __device__ inline uint32_t gridRanges(const HfbConfig& cfg, const BatchInst& I, Range* r) {
+  r[0] = {(unsigned char*)I.dv, (size_t)cfg.gridDims * cfg.gridDims * cfg.gridDims * 16};
+  return 1;
 }
 
-// Pass by pass over all instances on c->stream, an event between passes.
-cudaError_t frameBatchProfiled(HfbCtx* c, HfbInstance* insts, uint32_t n, float* passMs) {
-  cudaEvent_t ev[FP_COUNT + 1] = {};
-  cudaError_t e = cudaSuccess;
-  for (uint32_t i = 0; i <= FP_COUNT && e == cudaSuccess; i++) e = cudaEventCreate(&ev[i]);
-  if (e == cudaSuccess) e = cudaEventRecord(ev[0], c->stream);
-  for (uint32_t p = 0; p < FP_COUNT && e == cudaSuccess; p++) {
-    for (uint32_t i = 0; i < n && e == cudaSuccess; i++) e = framePass(c, &insts[i], (FramePass)p);
-    if (e == cudaSuccess) e = cudaEventRecord(ev[p + 1], c->stream);
+__host__ __device__ inline uint32_t clearRanges(const HfbConfig& cfg, const BatchInst& I, uint32_t kind,
+                                                Range* r) {
+  return kind == BK_CLEAR_FRAME ? frameRanges(cfg, I, r) : gridRanges(cfg, I, r);
+}
+
+// Zeroes chunk `local` of the instance's ranges: 16-byte stores, then words
+// (every range starts 16-byte aligned and is a whole number of words).
+__global__ void __launch_bounds__(256) clearBatch(BatchView b, HfbConfig cfgParam, uint32_t kind) {
+  const HfbConfig cfg = cfgParam;
+  const uint32_t n = b.hdr->n;
+  const uint32_t* row = b.prefix + kind * (BATCH_MAX + 1);
+  const uint32_t total = row[n];
+  for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
+    const uint32_t i = batchFind(row, n, v);
+    const BatchInst& I = b.insts[i];
+    Range r[8];
+    const uint32_t nr = clearRanges(cfg, I, kind, r);
+    uint32_t c = v - row[i], k = 0;
+    for (; k < nr; k++) {
+      const uint32_t ch = (uint32_t)((r[k].bytes + CLEAR_CHUNK - 1) / CLEAR_CHUNK);
+      if (c < ch) break;
+      c -= ch;
+    }
+    if (k == nr) continue;
+    const size_t off = (size_t)c * CLEAR_CHUNK;
+    const size_t end = off + CLEAR_CHUNK < r[k].bytes ? off + CLEAR_CHUNK : r[k].bytes;
+    unsigned char* p = r[k].p;
+    const size_t end16 = off + ((end - off) & ~size_t(15));
+    for (size_t x = off + threadIdx.x * 16u; x < end16; x += 256u * 16u)
+      *HFB_G(reinterpret_cast<uint4*>(p + x)) = make_uint4(0u, 0u, 0u, 0u);
+    for (size_t x = end16 + threadIdx.x * 4u; x < end; x += 256u * 4u) *HFB_G(reinterpret_cast<uint32_t*>(p + x)) = 0u;
   }
-  if (e == cudaSuccess) e = cudaEventSynchronize(ev[FP_COUNT]);
-  for (uint32_t p = 0; p < FP_COUNT && e == cudaSuccess; p++) e = cudaEventElapsedTime(&passMs[p], ev[p], ev[p + 1]);
-  for (uint32_t i = 0; i <= FP_COUNT; i++)
-    if (ev[i]) cudaEventDestroy(ev[i]);
-  return e;
 }
 
 }  // namespace
 
+uint32_t batchBlocks(const HfbConfig& cfg, BatchKind k, const BatchInst& I) {
+  const uint32_t G3 = cfg.gridDims * cfg.gridDims * cfg.gridDims;
+  const uint32_t TB = I.T * cfg.tileDepthBins;
+  const uint32_t nSeg = (I.strandsToRender < I.S ? I.strandsToRender : I.S) * (I.P - 1u);
+  switch (k) {
+    case BK_CLEAR_FRAME:
+    case BK_CLEAR_GRID: {
+      Range r[8];
+      const uint32_t nr = clearRanges(cfg, I, k, r);
+      uint32_t t = 0;
+      for (uint32_t j = 0; j < nr; j++) t += (uint32_t)((r[j].bytes + CLEAR_CHUNK - 1) / CLEAR_CHUNK);
+      return t;
+    }
+    case BK_GRID_PRE: return divCeil(G3, 256u);
+    case BK_INTEGRATE: return I.S ? divCeil(I.S, simStrandsPerBlock(I.P)) : 0u;
+    case BK_GRID_POST: return divCeil(I.S * I.P, 256u);
+    case BK_RASTER: return divCeil(nSeg, TILES_RASTER_SEGS);
+    case BK_SCAN: return divCeil(TB, 2048u);
+    case BK_SCAN_SUMS: return 1u;
+    case BK_SCATTER: {
+      const uint32_t v = divCeil(nSeg, 1024u);
+      return v < 1u ? 1u : (v > 256u ? 256u : v);
+    }
+    case BK_FINALIZE: return divCeil(TB, 8u);
+    case BK_LARGE: return 4u;
+    case BK_SORT: return 1u;
+    case BK_SCHEDULE: return 1u;
+    case BK_SHADING: return divCeil(I.S * cfg.shadingPoints, 128u);
+    default: return 0u;
+  }
+}
+
+cudaError_t launchBatchClear(HfbCtx* c, const BatchView& b, BatchKind k) {
+  HFB_CHECK_BIND(c);
+  uint32_t& grid = c->batchGrid[k];
+  if (!grid) grid = c->smCount * 8u;
+  clearBatch<<<grid, 256, 0, c->stream>>>(b, c->cfg, (uint32_t)k);
+  HFB_AFTER_LAUNCH(c, "clearBatch");
+  c->launches += 1;
+  return cudaGetLastError();
+}
+
+// The frame's launch sequence (renderer.ts:171-295 order).  With `ev`, an
+// event is recorded before the first pass and after each of the
+// HFB_FRAME_PASSES passes (grid_pre, integrate, grid_post with its grid
+// clear, clear, tiles, sort, fine, shading).
+static cudaError_t batchSequence(HfbCtx* c, const BatchView& b, cudaEvent_t* ev = nullptr) {
+  auto mark = [&](int i) { return ev ? cudaEventRecord(ev[i], c->stream) : cudaSuccess; };
+  cudaError_t e = mark(0);
+  if (e == cudaSuccess) e = launchBatchSim(c, b, BK_GRID_PRE);
+  if (e == cudaSuccess) e = mark(1);
+  if (e == cudaSuccess) e = launchBatchSim(c, b, BK_INTEGRATE);
+  if (e == cudaSuccess) e = mark(2);
+  if (e == cudaSuccess) e = launchBatchClear(c, b, BK_CLEAR_GRID);
+  if (e == cudaSuccess) e = launchBatchSim(c, b, BK_GRID_POST);
+  if (e == cudaSuccess) e = mark(3);
+  if (e == cudaSuccess) e = launchBatchClear(c, b, BK_CLEAR_FRAME);
+  if (e == cudaSuccess) e = mark(4);
+  if (e == cudaSuccess) e = launchBatchTiles(c, b);
+  if (e == cudaSuccess) e = mark(5);
+  if (e == cudaSuccess) e = launchBatchSort(c, b);
+  if (e == cudaSuccess) e = mark(6);
+  if (e == cudaSuccess) e = launchBatchFine(c, b);
+  if (e == cudaSuccess) e = mark(7);
+  if (e == cudaSuccess) e = launchBatchShading(c, b);
+  if (e == cudaSuccess) e = mark(8);
+  return e;
+}
+
+// Fills the staging copy, uploads it and runs the frame for n validated
+// instances.
 cudaError_t frameBatch(HfbCtx* c, HfbInstance* insts, uint32_t n, float* passMs) {
   cudaError_t e = cudaSuccess;
-  if (passMs) {
-    e = frameBatchProfiled(c, insts, n, passMs);
+  if (!c->batchDev) {
+    e = cudaMalloc(&c->batchDev, BATCH_BYTES);
+    for (int k = 0; k < 2 && e == cudaSuccess; k++) {
+      e = cudaMallocHost(&c->batchHost[k], BATCH_BYTES);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->batchCopied[k], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventRecord(c->batchCopied[k], c->stream);
+    }
+    if (e != cudaSuccess) return e;
+  }
+  // the staging copy is rewritten once its previous upload has been read
+  const uint32_t k = c->batchFlip;
+  c->batchFlip ^= 1u;
+  e = cudaEventSynchronize(c->batchCopied[k]);
+  if (e != cudaSuccess) return e;
+  char* h = (char*)c->batchHost[k];
+  BatchHdr* hdr = (BatchHdr*)h;
+  memset(hdr, 0, sizeof(*hdr));
+  hdr->n = n;
+  uint32_t* prefix = (uint32_t*)(h + BATCH_PREFIX_OFF);
+  BatchInst* bi = (BatchInst*)(h + BATCH_INSTS_OFF);
+  const HfbConfig& cfg = c->cfg;
+  for (uint32_t i = 0; i < n; i++) {
+    const HfbInstance& s = insts[i];
+    BatchInst& I = bi[i];
+    memset(&I, 0, sizeof(I));
+    memcpy(&I.U, s.uniforms, sizeof(HfbUniforms));
+    memcpy(&I.SU, s.simUniforms, sizeof(HfbSimUniforms));
+    I.bsphere = make_float4(s.hair.boundingSphere[0], s.hair.boundingSphere[1], s.hair.boundingSphere[2],
+                            s.hair.boundingSphere[3]);
+    I.S = s.hair.strandsCount;
+    I.P = s.hair.pointsPerStrand;
+    I.strandsToRender = s.strandsToRender;
+    I.sdfDims = s.sdfDims;
+    I.W = s.raster.width;
+    I.H = s.raster.height;
+    I.maxDrawn = s.raster.maxDrawnSegments;
+    I.T = divCeil(I.W, cfg.tileSize) * divCeil(I.H, cfg.tileSize);
+    I.aoW = s.ao ? s.aoWidth : 0u;
+    I.aoH = s.ao ? s.aoHeight : 0u;
+    I.smSize = s.shadowMap ? s.shadowMapSize : 0u;
+    I.posNew = (float4*)s.positions[1u - s.current];
+    I.posOld = (const float4*)s.positions[s.current];
+    I.initial = (const float4*)s.positionsInitial;
+    I.tan = (const float4*)s.tangents;
+    I.segLen = s.segmentLengths;
+    I.dv = (int4*)s.densityVelocity;
+    I.gw = (float4*)s.densityGradWind;
+    I.sdf = s.sdf;
+    I.shading = (float4*)s.shading;
+    I.depth = s.sceneDepth;
+    I.shadingDepth = s.shadingDepth ? s.shadingDepth : s.sceneDepth;
+    I.ao = s.ao;
+    I.sm = s.shadowMap;
+    I.tiles = (uint4*)s.raster.tiles;
+    I.segBuf = s.raster.tileSegments;
+    I.segCount = s.raster.segmentCountPerTile;
+    I.sortBuckets = s.raster.sortBuckets;
+    I.tileList = s.raster.tileList;
+    I.result = s.raster.rasterizerResult;
+    I.scratch = (unsigned char*)s.raster.scratch;
+  }
+  for (uint32_t kind = 0; kind < BK_COUNT; kind++) {
+    uint32_t* row = prefix + (size_t)kind * (BATCH_MAX + 1);
+    uint32_t acc = 0;
+    for (uint32_t i = 0; i < n; i++) {
+      row[i] = acc;
+      acc += batchBlocks(cfg, (BatchKind)kind, bi[i]);
+    }
+    row[n] = acc;
+  }
+  const size_t bytes = BATCH_INSTS_OFF + (size_t)n * sizeof(BatchInst);
+  e = cudaMemcpyAsync(c->batchDev, h, bytes, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(c->batchCopied[k], c->stream);
+  if (e != cudaSuccess) return e;
+
+  const BatchView b = batchView(c->batchDev);
+  if (passMs) {  // plain launches with an event between passes
+    cudaEvent_t ev[HFB_FRAME_PASSES + 1] = {};
+    for (int i = 0; i <= HFB_FRAME_PASSES && e == cudaSuccess; i++) e = cudaEventCreate(&ev[i]);
+    if (e == cudaSuccess) e = batchSequence(c, b, ev);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[HFB_FRAME_PASSES]);
+    for (int i = 0; i < HFB_FRAME_PASSES && e == cudaSuccess; i++) e = cudaEventElapsedTime(&passMs[i], ev[i], ev[i + 1]);
+    for (int i = 0; i <= HFB_FRAME_PASSES; i++)
+      if (ev[i]) cudaEventDestroy(ev[i]);
+    if (e != cudaSuccess) return e;
+    for (uint32_t i = 0; i < n; i++) insts[i].current ^= 1u;
+    return cudaGetLastError();
+  }
+#ifdef HFB_DEVICE_CHECKS
+  c->batchGraphLaunches = ~0ull;  // the checked build waits after every launch: no capture
+#endif
+  if (c->batchCalls++ == 0 || c->batchGraphLaunches == ~0ull) {
+    // first batch: plain launches (they also set the kernels' attributes)
+    const uint64_t l0 = c->launches;
+    e = batchSequence(c, b);
+    if (c->batchGraphLaunches != ~0ull) c->batchGraphLaunches = c->launches - l0;
   } else {
-    e = ensureStreams(c);
-    if (e != cudaSuccess) return e;
-    const uint32_t K = n < BATCH_STREAMS ? n : BATCH_STREAMS;
-    // largest instance first, each onto the least-loaded stream
-    std::vector<uint32_t> order(n);
-    std::iota(order.begin(), order.end(), 0u);
-    std::stable_sort(order.begin(), order.end(),
-                     [&](uint32_t a, uint32_t b) { return frameWork(insts[a]) > frameWork(insts[b]); });
-    double load[BATCH_STREAMS] = {};
-    e = cudaEventRecord(c->batchFork, c->stream);
-    for (uint32_t s = 0; s < K && e == cudaSuccess; s++) e = cudaStreamWaitEvent(c->batchStreams[s], c->batchFork, 0);
-    if (e != cudaSuccess) return e;
-    const cudaStream_t caller = c->stream;
-    for (uint32_t k = 0; k < n && e == cudaSuccess; k++) {
-      const uint32_t i = order[k];
-      const uint32_t s = (uint32_t)(std::min_element(load, load + K) - load);
-      load[s] += frameWork(insts[i]);
-      c->stream = c->batchStreams[s];
-      for (uint32_t p = 0; p < FP_COUNT && e == cudaSuccess; p++) e = framePass(c, &insts[i], (FramePass)p);
+    if (!c->batchGraph) {
+      cudaGraph_t g = nullptr;
+      e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+      if (e != cudaSuccess) return e;
+      const uint64_t l0 = c->launches;
+      cudaError_t el = batchSequence(c, b);
+      c->launches = l0;
+      e = cudaStreamEndCapture(c->stream, &g);
+      if (el != cudaSuccess) e = el;
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&c->batchGraph, g, 0);
+      if (g) cudaGraphDestroy(g);
+      if (e != cudaSuccess) {
+        // a stream that cannot be captured (e.g. the legacy default stream): plain launches
+        cudaGetLastError();
+        c->batchGraph = nullptr;
+        c->batchGraphLaunches = ~0ull;
+        return batchSequence(c, b);
+      }
     }
-    c->stream = caller;
-    // join every worker stream back into the caller's stream, also after a failed launch
-    for (uint32_t s = 0; s < K; s++) {
-      cudaError_t ej = cudaEventRecord(c->batchJoin[s], c->batchStreams[s]);
-      if (ej == cudaSuccess) ej = cudaStreamWaitEvent(caller, c->batchJoin[s], 0);
-      if (e == cudaSuccess) e = ej;
-    }
+    e = cudaGraphLaunch(c->batchGraph, c->stream);
+    c->launches += c->batchGraphLaunches;
   }
   if (e != cudaSuccess) return e;
   for (uint32_t i = 0; i < n; i++) insts[i].current ^= 1u;
@@ -151,14 +337,14 @@ cudaError_t frameBatch(HfbCtx* c, HfbInstance* insts, uint32_t n, float* passMs)
 }
 
 void frameBatchRelease(HfbCtx* c) {
-  for (uint32_t s = 0; s < BATCH_STREAMS; s++) {
-    if (c->batchJoin[s]) cudaEventDestroy(c->batchJoin[s]);
-    if (c->batchStreams[s]) cudaStreamDestroy(c->batchStreams[s]);
-    c->batchJoin[s] = nullptr;
-    c->batchStreams[s] = nullptr;
+  if (c->batchGraph) cudaGraphExecDestroy(c->batchGraph);
+  for (int k = 0; k < 2; k++) {
+    if (c->batchCopied[k]) cudaEventDestroy(c->batchCopied[k]);
+    if (c->batchHost[k]) cudaFreeHost(c->batchHost[k]);
   }
-  if (c->batchFork) cudaEventDestroy(c->batchFork);
-  c->batchFork = nullptr;
+  if (c->batchDev) cudaFree(c->batchDev);
+  c->batchGraph = nullptr;
+  c->batchDev = nullptr;
 }
 
 }  // namespace hfb

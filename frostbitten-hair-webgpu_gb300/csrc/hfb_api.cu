@@ -6,6 +6,8 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <utility>
+#include <vector>
 
 #define HFB_TU 4
 #include "hfb_internal.cuh"
@@ -442,14 +444,20 @@ HFB_API int hfb_debug_check_ranges(HfbCtx* c, const unsigned long long* lohi, ui
   cudaError_t e = cudaStreamSynchronize(c->stream);
   if (e == cudaSuccess && !c->checkDev) e = cudaMalloc(&c->checkDev, sizeof(hfb::CheckState));
   if (e != cudaSuccess) return cudaFail(c, e, "debug_check_ranges");
+  // sorted by start, duplicates dropped; overlapping ranges are rejected
+  std::vector<std::pair<unsigned long long, unsigned long long>> r;
+  for (uint32_t i = 0; i < n; i++) r.emplace_back(lohi[2 * i], lohi[2 * i + 1]);
+  r.emplace_back((unsigned long long)c->dCounters, (unsigned long long)c->dCounters + sizeof(hfb::DeviceCounters));
+  std::sort(r.begin(), r.end());
+  r.erase(std::unique(r.begin(), r.end()), r.end());
+  for (size_t i = 1; i < r.size(); i++)
+    HFB_REQUIRE(c, r[i].first >= r[i - 1].second, "overlapping ranges");
   hfb::CheckState* h = new hfb::CheckState();
-  for (uint32_t i = 0; i < n; i++) {
-    h->lo[i] = lohi[2 * i];
-    h->hi[i] = lohi[2 * i + 1];
+  for (size_t i = 0; i < r.size(); i++) {
+    h->lo[i] = r[i].first;
+    h->hi[i] = r[i].second;
   }
-  h->lo[n] = (unsigned long long)c->dCounters;
-  h->hi[n] = h->lo[n] + sizeof(hfb::DeviceCounters);
-  h->nRanges = n + 1;
+  h->nRanges = (uint32_t)r.size();
   e = cudaMemcpy(c->checkDev, h, sizeof(*h), cudaMemcpyHostToDevice);
   delete h;
   if (e != cudaSuccess) return cudaFail(c, e, "debug_check_ranges");

@@ -23,7 +23,7 @@
 namespace hfb {
 
 #ifdef HFB_DEVICE_CHECKS
-constexpr uint32_t CHECK_MAX_RANGES = 96;
+constexpr uint32_t CHECK_MAX_RANGES = 2048;  // sorted by lo, without overlaps
 struct CheckState {
   uint32_t nRanges;
   uint32_t fails;
@@ -40,8 +40,12 @@ __device__ inline bool checkAddr(const void* p, uint32_t bytes, uint32_t where) 
   CheckState* s = hfbCheck;
   if (!s) return true;
   const unsigned long long a = (unsigned long long)p;
-  for (uint32_t i = 0; i < s->nRanges; i++)
-    if (a >= s->lo[i] && a + bytes <= s->hi[i]) return true;
+  uint32_t lo = 0, hi = s->nRanges;  // last range with lo <= a
+  while (hi - lo > 1u) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (s->lo[mid] <= a) lo = mid; else hi = mid;
+  }
+  if (s->nRanges && a >= s->lo[lo] && a + bytes <= s->hi[lo]) return true;
   if (atomicAdd(&s->fails, 1u) == 0u) {
     s->firstWhere = where;
     s->firstAddr = a;

@@ -24,10 +24,16 @@ struct HfbCtx {
   size_t simSmemSet = 0;
   bool largeBinsAttrSet = false;
   int fineBlocksPerSM[3][3] = {};  // [tile 8/16/32][slices 4/8/16]
-  // batched frames: worker streams, the fork event and one join event per stream
-  cudaStream_t batchStreams[8] = {};
-  cudaEvent_t batchFork = nullptr;
-  cudaEvent_t batchJoin[8] = {};
+  // batched frames: device table + two pinned host staging copies, the
+  // persistent grid of each batched kernel, the captured frame graph
+  void* batchDev = nullptr;
+  void* batchHost[2] = {nullptr, nullptr};
+  cudaEvent_t batchCopied[2] = {nullptr, nullptr};
+  uint32_t batchFlip = 0;
+  uint32_t batchGrid[32] = {};
+  cudaGraphExec_t batchGraph = nullptr;
+  uint64_t batchGraphLaunches = 0;  // kernels in the graph
+  uint32_t batchCalls = 0;
   // self-checking build: the device CheckState (hfb_check.cuh), else NULL
   void* checkDev = nullptr;
 };
@@ -136,11 +142,9 @@ __host__ __device__ inline FineScratch fineScratchLayout(void* base, const HfbCo
 }
 
 // ---------------------------------------------------------------------------
-// Whole frames (hfb_frame, hfb_frame_batch).  A frame of one instance is the
-// reference's pass sequence; framePass launches one pass of it on c->stream.
+// Whole frames.  A frame of one instance (hfb_frame) is the reference's pass
+// sequence; framePass launches one pass of it on c->stream.
 // ---------------------------------------------------------------------------
-constexpr uint32_t BATCH_MAX = 1024;   // instances per hfb_frame_batch call
-constexpr uint32_t BATCH_STREAMS = 8;  // worker streams of a batched frame
 enum FramePass : uint32_t {
   FP_GRID_PRE = 0,  // GridPreSimPass
   FP_INTEGRATE,     // HairSimIntegrationPass
@@ -154,11 +158,111 @@ enum FramePass : uint32_t {
 };
 cudaError_t framePass(HfbCtx* c, HfbInstance* in, FramePass p);
 cudaError_t clearRaster(HfbCtx* c, const HfbRasterBuffers& rb);
-// One frame of n checked instances on the worker streams (instance i on
-// stream i mod BATCH_STREAMS), joined back into c->stream; with passMs, the
-// passes run pass by pass over all instances on c->stream instead, with an
-// event between passes, and passMs[p] receives each pass's GPU time.
-// Flips every instance's `current`.
+
+// ---------------------------------------------------------------------------
+// Batched frames (hfb_frame_batch): every pass runs once for all instances.
+// Each batched kernel is persistent and walks "virtual blocks": instance i
+// owns virtual blocks [prefix[k][i], prefix[k][i + 1]) of kind k, and block
+// v of instance i runs the single-instance kernel's body as its block
+// v - prefix[k][i].  Instances, prefix rows and counters live in device
+// memory, so the launch sequence is the same for every batch and is
+// captured once as a CUDA graph.
+// ---------------------------------------------------------------------------
+constexpr uint32_t BATCH_MAX = 1024;  // instances per batch
+enum BatchKind : uint32_t {
+  BK_CLEAR_FRAME = 0,  // raster clears + tiles-pass counters
+  BK_GRID_PRE,
+  BK_INTEGRATE,
+  BK_CLEAR_GRID,       // densityVelocity, after integration read it
+  BK_GRID_POST,
+  BK_RASTER,
+  BK_SCAN,
+  BK_SCAN_SUMS,
+  BK_SCATTER,
+  BK_FINALIZE,
+  BK_LARGE,
+  BK_SORT,
+  BK_SCHEDULE,
+  BK_SHADING,
+  BK_COUNT
+};
+
+// One instance of a batched frame, as the kernels read it.
+struct alignas(16) BatchInst {
+  HfbUniforms U;
+  HfbSimUniforms SU;
+  float4 bsphere;
+  uint32_t S, P, strandsToRender, sdfDims;
+  uint32_t W, H, maxDrawn, T;
+  uint32_t aoW, aoH, smSize, pad0;
+  float4* posNew;        // positions[1 - current]: integration writes it, the raster reads it
+  const float4* posOld;  // positions[current]
+  const float4* initial;
+  const float4* tan;
+  const float* segLen;
+  int4* dv;
+  float4* gw;
+  const float* sdf;
+  float4* shading;
+  const float* depth;         // scene depth of the tiles / fine depth tests
+  const float* shadingDepth;  // depth of the shading attenuation
+  const float* ao;
+  const float* sm;
+  uint4* tiles;
+  uint32_t* segBuf;
+  uint32_t* segCount;
+  uint32_t* sortBuckets;
+  uint32_t* tileList;
+  float* result;
+  unsigned char* scratch;
+};
+
+// Device layout of a batch: header, prefix rows (fixed stride), the fine
+// pass's item prefix, the instances.
+struct BatchHdr {
+  uint32_t n;
+  uint32_t fineQueue;  // next global work item of the batched fine pass
+  uint32_t pad[2];
+};
+constexpr size_t BATCH_PREFIX_OFF = 256;
+constexpr size_t BATCH_ITEMS_OFF = BATCH_PREFIX_OFF + (size_t)BK_COUNT * (BATCH_MAX + 1) * 4;
+constexpr size_t BATCH_INSTS_OFF = (BATCH_ITEMS_OFF + (size_t)(BATCH_MAX + 1) * 4 + 255) & ~size_t(255);
+constexpr size_t BATCH_BYTES = BATCH_INSTS_OFF + (size_t)BATCH_MAX * sizeof(BatchInst);
+
+struct BatchView {
+  BatchHdr* hdr;
+  const uint32_t* prefix;  // [BK_COUNT][BATCH_MAX + 1]
+  uint32_t* itemPrefix;    // [BATCH_MAX + 1]
+  const BatchInst* insts;
+};
+inline BatchView batchView(void* base) {
+  char* p = (char*)base;
+  return {(BatchHdr*)p, (const uint32_t*)(p + BATCH_PREFIX_OFF), (uint32_t*)(p + BATCH_ITEMS_OFF),
+          (const BatchInst*)(p + BATCH_INSTS_OFF)};
+}
+
+// Instance owning virtual block v: the last i with row[i] <= v (row[n] = total).
+__device__ __forceinline__ uint32_t batchFind(const uint32_t* __restrict__ row, uint32_t n, uint32_t v) {
+  uint32_t lo = 0, hi = n;
+  while (hi - lo > 1u) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(&row[mid]) <= v) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+// Batched launchers: one persistent launch of kind k over all instances.
+cudaError_t launchBatchClear(HfbCtx* c, const BatchView& b, BatchKind k);
+cudaError_t launchBatchSim(HfbCtx* c, const BatchView& b, BatchKind k);
+cudaError_t launchBatchShading(HfbCtx* c, const BatchView& b);
+cudaError_t launchBatchTiles(HfbCtx* c, const BatchView& b);
+cudaError_t launchBatchSort(HfbCtx* c, const BatchView& b);
+cudaError_t launchBatchFine(HfbCtx* c, const BatchView& b);
+// Virtual blocks of kind k for one instance (host side).
+uint32_t batchBlocks(const HfbConfig& cfg, BatchKind k, const BatchInst& bi);
+// One frame of n checked instances; flips their `current`.  With passMs, the
+// passes run as plain launches with an event between them, the call waits,
+// and passMs[0..HFB_FRAME_PASSES) receives each pass's GPU time.
 cudaError_t frameBatch(HfbCtx* c, HfbInstance* insts, uint32_t n, float* passMs = nullptr);
 void frameBatchRelease(HfbCtx* c);
 

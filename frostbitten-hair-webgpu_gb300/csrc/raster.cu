@@ -1757,6 +1757,39 @@ fineKernel(const HfbUniforms U, const FineArgs a, const uint32_t* __restrict__ t
   }
 }
 
+// batched: one queue over the work items of every instance
+template <int TS, int MAXL>
+__global__ void __launch_bounds__(TS * TS, TS == 8 ? 6 : TS == 16 ? (MAXL <= 4 ? 3 : 2) : 1)
+fineBatch(BatchView b, FineArgs base, HfbConfig cfgParam) {
+  using SM = FineSmem<TS>;
+  const HfbConfig cfg = cfgParam;
+  extern __shared__ __align__(16) unsigned char fineSmemRaw[];
+  SM& sh = *reinterpret_cast<SM*>(fineSmemRaw);
+  const uint32_t n = b.hdr->n;
+  const uint32_t total = b.itemPrefix[n];
+  while (true) {
+    if (threadIdx.x == 0) sh.queueIdx = atomicAdd(&b.hdr->fineQueue, 1u);
+    __syncthreads();
+    const uint32_t gi = sh.queueIdx;
+    if (gi >= total) break;
+    const uint32_t i = batchFind(b.itemPrefix, n, gi);
+    const BatchInst& I = b.insts[i];
+    FineArgs a = base;
+    a.S = I.S;
+    a.P = I.P;
+    a.pos = I.posNew;
+    a.tan = I.tan;
+    a.shading = I.shading;
+    a.depth = I.depth;
+    a.tiles = I.tiles;
+    a.segBuf = I.segBuf;
+    const FineScratch fs = fineScratchLayout(I.scratch, cfg, I.W, I.H);
+    const uint32_t li = gi - b.itemPrefix[i];
+    if (li < fs.maxItems) fineItem<TS, MAXL>(sh, I.U, a, I.tileList, I.result, fs, (*HFB_G(&fs.items[li])));
+    __syncthreads();
+  }
+}
+
 template <int TS, int MAXL>
 cudaError_t launchFineT(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, const float* pos,
                         const float* tan, const float* shading, const float* depth, HfbRasterBuffers& rb) {
@@ -1803,6 +1836,162 @@ cudaError_t launchFineT(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, c
   return cudaGetLastError();
 }
 
+
+// ---------------------------------------------------------------------------
+// Batched tiles pass, tile sort and fine pass: persistent over the virtual
+// blocks of every instance (hfb_frame_batch).
+// ---------------------------------------------------------------------------
+#define BATCH_LOOP(KIND)                                              \
+  const uint32_t n = b.hdr->n;                                        \
+  const uint32_t* row = b.prefix + (KIND) * (BATCH_MAX + 1);          \
+  const uint32_t totalVb = row[n];                                    \
+  for (uint32_t v = blockIdx.x; v < totalVb; v += gridDim.x) {        \
+    const uint32_t i = batchFind(row, n, v);                          \
+    const BatchInst& I = b.insts[i];                                  \
+    if (!HFB_EXPECT(i < n && I.W && I.H && I.W <= 65536 && I.H <= 65536 && I.scratch && I.segBuf && \
+                    I.T == divCeil(I.W, cfg.tileSize) * divCeil(I.H, cfg.tileSize))) continue; \
+    const uint32_t local = v - row[i], nLocal = row[i + 1] - row[i];  \
+    (void)nLocal; (void)local;                                        \
+    const TilesScratch ts = tilesScratchLayout(I.scratch, cfg, I.W, I.H, I.maxDrawn); \
+    (void)ts;
+
+__global__ void __launch_bounds__(TR_SEGS) tilesRasterBatch(BatchView b, HfbConfig cfgParam,
+                                                             DeviceCounters* __restrict__ counters) {
+  const HfbConfig cfg = cfgParam;
+  __shared__ TrShared sh;
+  BATCH_LOOP(BK_RASTER)
+    tilesRasterBody(I.U, I.P, min(I.strandsToRender, I.S), cfg.tileSize, cfg.tileDepthBins,
+                    cfg.invalidTilesPerSegmentThreshold, I.bsphere, I.posNew, I.tan, I.depth, I.tiles, I.segBuf,
+                    I.segCount, ts.binCount, counters, sh, local);
+  }
+}
+
+__global__ void __launch_bounds__(512) binScanBatch(BatchView b, HfbConfig cfgParam) {
+  const HfbConfig cfg = cfgParam;
+  __shared__ uint32_t warpSums[32];
+  BATCH_LOOP(BK_SCAN)
+    binScanBlocksBody(ts.binCount, ts.binOffset, ts.blockSums, I.T * cfg.tileDepthBins, warpSums, local);
+  }
+}
+
+__global__ void __launch_bounds__(1024) binScanSumsBatch(BatchView b, HfbConfig cfgParam) {
+  const HfbConfig cfg = cfgParam;
+  __shared__ uint32_t warpSums[32];
+  BATCH_LOOP(BK_SCAN_SUMS)
+    binScanSumsBody(ts.blockSums, divCeil(I.T * cfg.tileDepthBins, SCAN_PER_BLOCK), warpSums);
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(256) binScatterBatch(BatchView b, HfbConfig cfgParam,
+                                                        DeviceCounters* __restrict__ counters) {
+  const HfbConfig cfg = cfgParam;
+  BATCH_LOOP(BK_SCATTER)
+    binScatterBody(I.segBuf, I.maxDrawn, ts.binOffset, ts.blockSums, ts.keys, counters, local, nLocal,
+                   I.T * cfg.tileDepthBins);
+  }
+}
+
+__global__ void __launch_bounds__(256) binFinalizeBatch(BatchView b, HfbConfig cfgParam) {
+  const HfbConfig cfg = cfgParam;
+  __shared__ uint32_t smem[8][MEDIUM_BIN];
+  BATCH_LOOP(BK_FINALIZE)
+    binFinalizeBody(I.T * cfg.tileDepthBins, ts.binCount, ts.binOffset, ts.blockSums, ts.keys, I.segBuf, I.tiles,
+                    ts.largeBins, smem, local, nLocal);
+  }
+}
+
+__global__ void __launch_bounds__(1024) largeBinsBatch(BatchView b, HfbConfig cfgParam) {
+  const HfbConfig cfg = cfgParam;
+  extern __shared__ uint32_t sk[];
+  BATCH_LOOP(BK_LARGE)
+    largeBinsBody(ts.largeBins, ts.binCount, ts.binOffset, ts.blockSums, ts.keys, I.segBuf, I.tiles, sk, local,
+                  nLocal);
+  }
+}
+
+__global__ void __launch_bounds__(1024) tileSortBatch(BatchView b, HfbConfig cfgParam) {
+  const HfbConfig cfg = cfgParam;
+  __shared__ SortShared ss;
+  BATCH_LOOP(BK_SORT)
+    tileSortBody(I.T, cfg.sortBuckets, cfg.sortBucketSize, I.segCount, I.sortBuckets, I.tileList, ss);
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(1024) fineScheduleBatch(BatchView b, HfbConfig cfgParam, uint32_t grid,
+                                                          DeviceCounters* __restrict__ counters) {
+  const HfbConfig cfg = cfgParam;
+  __shared__ uint32_t warpSums[32];
+  __shared__ uint32_t totalRecords;
+  BATCH_LOOP(BK_SCHEDULE)
+    const FineScratch fs = fineScratchLayout(I.scratch, cfg, I.W, I.H);
+    const uint32_t dispMode = I.U.displayMode & 0xffu;
+    const bool dbg = dispMode == 4u && ((I.U.displayMode >> 8) & 0xffffu) != 0u;
+    fineScheduleBody(I.tileList, I.segCount, I.tiles, I.T, cfg.tileDepthBins, grid, I.maxDrawn, I.S * I.P,
+                     dbg ? 0u : 1u, fs, counters, warpSums, totalRecords);
+  }
+}
+
+// Exclusive prefix of the instances' work items; resets the batch queue.
+__global__ void __launch_bounds__(1024) fineItemPrefixBatch(BatchView b, HfbConfig cfgParam) {
+  const HfbConfig cfg = cfgParam;
+  __shared__ uint32_t warpSums[32];
+  const uint32_t n = b.hdr->n;
+  uint32_t carry = 0;
+  for (uint32_t i0 = 0; i0 < n; i0 += blockDim.x) {
+    const uint32_t i = i0 + threadIdx.x;
+    uint32_t items = 0;
+    if (i < n) {
+      const BatchInst& I = b.insts[i];
+      items = (*HFB_G(&fineScratchLayout(I.scratch, cfg, I.W, I.H).hdr[0]));
+    }
+    uint32_t chunk;
+    const uint32_t ex = blockExclusiveScan(items, warpSums, chunk);
+    if (i < n) b.itemPrefix[i] = carry + ex;
+    carry += chunk;
+  }
+  if (threadIdx.x == 0) {
+    b.itemPrefix[n] = carry;
+    b.hdr->fineQueue = 0;
+  }
+}
+#undef BATCH_LOOP
+
+template <int TS, int MAXL>
+cudaError_t launchFineBatchT(HfbCtx* c, const BatchView& b) {
+  HFB_CHECK_BIND(c);
+  const HfbConfig& cfg = c->cfg;
+  constexpr size_t SMEM = sizeof(FineSmem<TS>);
+  uint32_t& grid = c->batchGrid[BK_COUNT];  // the fine kernel's persistent grid
+  if (!grid) {
+    cudaError_t e = cudaFuncSetAttribute(fineBatch<TS, MAXL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);
+    int per = 0;
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fineBatch<TS, MAXL>, TS * TS, SMEM);
+    if (e != cudaSuccess) return e;
+    if (per < 1) return cudaErrorInvalidConfiguration;
+    grid = cfg.processorCount ? cfg.processorCount : (uint32_t)per * c->smCount;
+  }
+  DeviceCounters* dc = (DeviceCounters*)c->dCounters;
+  uint32_t& sgrid = c->batchGrid[BK_SCHEDULE];
+  if (!sgrid) sgrid = c->smCount;
+  fineScheduleBatch<<<sgrid, 1024, 0, c->stream>>>(b, cfg, grid, dc);
+  HFB_AFTER_LAUNCH(c, "fineScheduleBatch");
+  fineItemPrefixBatch<<<1, 1024, 0, c->stream>>>(b, cfg);
+  HFB_AFTER_LAUNCH(c, "fineItemPrefixBatch");
+  FineArgs a{};
+  a.B = cfg.tileDepthBins;
+  a.L = cfg.slicesPerPixel;
+  a.SP = cfg.shadingPoints;
+  a.CAP = cfg.avgFragmentsPerSlice * cfg.slicesPerPixel * cfg.tileSize * cfg.tileSize;
+  a.alphaQuadratic = cfg.alphaQuadratic;
+  a.alphaMul = cfg.alphaMultiplier;
+  a.counters = dc;
+  fineBatch<TS, MAXL><<<grid, TS * TS, SMEM, c->stream>>>(b, a, cfg);
+  HFB_AFTER_LAUNCH(c, "fineBatch");
+  c->launches += 3;
+  return cudaGetLastError();
+}
 
 }  // namespace
 
@@ -1878,6 +2067,72 @@ cudaError_t launchFinePass(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h
   if (L <= 4) return launchFineT<32, 4>(c, u, h, pos, tan, shading, depth, rb);
   if (L <= 8) return launchFineT<32, 8>(c, u, h, pos, tan, shading, depth, rb);
   return cudaErrorInvalidValue;  // 32x32 tiles with more than 8 slices: too many registers per pixel
+}
+
+}  // namespace hfb
+
+namespace hfb {
+
+cudaError_t launchBatchTiles(HfbCtx* c, const BatchView& b) {
+  HFB_CHECK_BIND(c);
+  const HfbConfig& cfg = c->cfg;
+  DeviceCounters* dc = (DeviceCounters*)c->dCounters;
+  uint32_t* g = c->batchGrid;
+  if (!g[BK_RASTER]) {
+    int per = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, tilesRasterBatch, TR_SEGS, 0);
+    if (e != cudaSuccess) return e;
+    g[BK_RASTER] = (uint32_t)(per > 0 ? per : 1) * c->smCount;
+    g[BK_SCAN] = c->smCount * 4u;
+    g[BK_SCAN_SUMS] = c->smCount;
+    g[BK_SCATTER] = c->smCount * 8u;
+    g[BK_FINALIZE] = c->smCount * 8u;
+    g[BK_LARGE] = c->smCount;
+    e = cudaFuncSetAttribute(largeBinsBatch, cudaFuncAttributeMaxDynamicSharedMemorySize, LARGE_SMEM_KEYS * 4);
+    if (e != cudaSuccess) return e;
+  }
+  tilesRasterBatch<<<g[BK_RASTER], TR_SEGS, 0, c->stream>>>(b, cfg, dc);
+  HFB_AFTER_LAUNCH(c, "tilesRasterBatch");
+  binScanBatch<<<g[BK_SCAN], 512, 0, c->stream>>>(b, cfg);
+  HFB_AFTER_LAUNCH(c, "binScanBatch");
+  binScanSumsBatch<<<g[BK_SCAN_SUMS], 1024, 0, c->stream>>>(b, cfg);
+  HFB_AFTER_LAUNCH(c, "binScanSumsBatch");
+  binScatterBatch<<<g[BK_SCATTER], 256, 0, c->stream>>>(b, cfg, dc);
+  HFB_AFTER_LAUNCH(c, "binScatterBatch");
+  binFinalizeBatch<<<g[BK_FINALIZE], 256, 0, c->stream>>>(b, cfg);
+  HFB_AFTER_LAUNCH(c, "binFinalizeBatch");
+  largeBinsBatch<<<g[BK_LARGE], 1024, LARGE_SMEM_KEYS * 4, c->stream>>>(b, cfg);
+  HFB_AFTER_LAUNCH(c, "largeBinsBatch");
+  c->launches += 6;
+  return cudaGetLastError();
+}
+
+cudaError_t launchBatchSort(HfbCtx* c, const BatchView& b) {
+  HFB_CHECK_BIND(c);
+  if (c->cfg.sortBuckets > SORT_MAX_BUCKETS) return cudaErrorInvalidValue;
+  uint32_t& grid = c->batchGrid[BK_SORT];
+  if (!grid) grid = c->smCount;
+  tileSortBatch<<<grid, 1024, 0, c->stream>>>(b, c->cfg);
+  HFB_AFTER_LAUNCH(c, "tileSortBatch");
+  c->launches += 1;
+  return cudaGetLastError();
+}
+
+cudaError_t launchBatchFine(HfbCtx* c, const BatchView& b) {
+  const uint32_t TS = c->cfg.tileSize, L = c->cfg.slicesPerPixel;
+  if (TS == 8) {
+    if (L <= 4) return launchFineBatchT<8, 4>(c, b);
+    if (L <= 8) return launchFineBatchT<8, 8>(c, b);
+    return launchFineBatchT<8, 16>(c, b);
+  }
+  if (TS == 16) {
+    if (L <= 4) return launchFineBatchT<16, 4>(c, b);
+    if (L <= 8) return launchFineBatchT<16, 8>(c, b);
+    return launchFineBatchT<16, 16>(c, b);
+  }
+  if (L <= 4) return launchFineBatchT<32, 4>(c, b);
+  if (L <= 8) return launchFineBatchT<32, 8>(c, b);
+  return cudaErrorInvalidValue;
 }
 
 }  // namespace hfb

@@ -221,6 +221,19 @@ shadingKernel(const HfbUniforms U, uint32_t S, uint32_t P, uint32_t SP, float zN
               blockIdx.x * blockDim.x + threadIdx.x);
 }
 
+// batched: persistent over the virtual blocks of every instance
+__global__ void __launch_bounds__(128) shadingBatch(BatchView b, uint32_t SP, float zNear, float zFar) {
+  const uint32_t n = b.hdr->n;
+  const uint32_t* row = b.prefix + BK_SHADING * (BATCH_MAX + 1);
+  const uint32_t total = row[n];
+  for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
+    const uint32_t i = batchFind(row, n, v);
+    const BatchInst& I = b.insts[i];
+    shadingBody(I.U, I.S, I.P, SP, zNear, zFar, I.posNew, I.tan, I.shadingDepth, I.ao, I.aoW, I.aoH, I.sm,
+                I.smSize, I.shading, (v - row[i]) * 128u + threadIdx.x);
+  }
+}
+
 }  // namespace
 
 cudaError_t launchShading(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, const float* pos,
@@ -238,4 +251,16 @@ cudaError_t launchShading(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h,
   return cudaGetLastError();
 }
 
+}  // namespace hfb
+
+namespace hfb {
+cudaError_t launchBatchShading(HfbCtx* c, const BatchView& b) {
+  HFB_CHECK_BIND(c);
+  uint32_t& grid = c->batchGrid[BK_SHADING];
+  if (!grid) grid = c->smCount * 16u;
+  shadingBatch<<<grid, 128, 0, c->stream>>>(b, c->cfg.shadingPoints, c->cfg.cameraNear, c->cfg.cameraFar);
+  HFB_AFTER_LAUNCH(c, "shadingBatch");
+  c->launches += 1;
+  return cudaGetLastError();
+}
 }  // namespace hfb

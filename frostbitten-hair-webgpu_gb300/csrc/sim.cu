@@ -405,6 +405,50 @@ gridPostSimKernel(const HfbSimUniforms u, uint32_t N, uint32_t G, const float4* 
   gridPostSimBody(u, N, G, prev, now, dv, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
+// ---- batched: persistent over the virtual blocks of every instance ----
+__global__ void __launch_bounds__(256) gridPreSimBatch(BatchView b, uint32_t G) {
+  const uint32_t n = b.hdr->n;
+  const uint32_t* row = b.prefix + BK_GRID_PRE * (BATCH_MAX + 1);
+  const uint32_t total = row[n];
+  for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
+    const uint32_t i = batchFind(row, n, v);
+    const BatchInst& I = b.insts[i];
+    gridPreSimBody(I.SU, G, I.dv, I.gw, I.sdf, I.sdfDims, (v - row[i]) * 256u + threadIdx.x);
+  }
+}
+
+__global__ void __launch_bounds__(SIM_THREADS) simIntegrateBatch(BatchView b, uint32_t G) {
+  extern __shared__ float4 simSmem[];
+  const uint32_t n = b.hdr->n;
+  const uint32_t* row = b.prefix + BK_INTEGRATE * (BATCH_MAX + 1);
+  const uint32_t total = row[n];
+  for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
+    const uint32_t i = batchFind(row, n, v);
+    const BatchInst& I = b.insts[i];
+    // integration reads positions[1 - current] (prev) and [current] (now), writes the former
+    simIntegrateBody(I.SU, I.S, I.P, G, I.posNew, I.posOld, I.initial, I.segLen, I.dv, I.gw, I.sdf, I.sdfDims,
+                     simSmem, v - row[i]);
+  }
+}
+
+__global__ void __launch_bounds__(256) gridPostSimBatch(BatchView b, uint32_t G) {
+  const uint32_t n = b.hdr->n;
+  const uint32_t* row = b.prefix + BK_GRID_POST * (BATCH_MAX + 1);
+  const uint32_t total = row[n];
+  for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
+    const uint32_t i = batchFind(row, n, v);
+    const BatchInst& I = b.insts[i];
+    // after the swap: prev = the old current positions, now = the new ones
+    gridPostSimBody(I.SU, I.S * I.P, G, I.posOld, I.posNew, (unsigned*)I.dv, (v - row[i]) * 256u + threadIdx.x);
+  }
+}
+
+size_t simSmemMax() {
+  size_t m = 0;
+  for (uint32_t P = 4; P <= 128; P++) m = m > simSmemBytes(P) ? m : simSmemBytes(P);
+  return m;
+}
+
 }  // namespace
 
 cudaError_t launchGridPreSim(HfbCtx* c, const HfbSimUniforms& u, const int32_t* dv, float* gw,
@@ -434,6 +478,37 @@ cudaError_t launchSimIntegrate(HfbCtx* c, const HfbSimUniforms& u, const HfbHair
       u, S, P, c->cfg.gridDims, (float4*)prev, (const float4*)now, (const float4*)initial, segLen,
       (const int4*)dv, (const float4*)gw, sdf, sdfDims);
   HFB_AFTER_LAUNCH(c, "simIntegrateKernel");
+  c->launches += 1;
+  return cudaGetLastError();
+}
+
+cudaError_t launchBatchSim(HfbCtx* c, const BatchView& b, BatchKind k) {
+  HFB_CHECK_BIND(c);
+  const uint32_t G = c->cfg.gridDims;
+  uint32_t& grid = c->batchGrid[k];
+  if (k == BK_GRID_PRE) {
+    if (!grid) grid = c->smCount * 8u;
+    gridPreSimBatch<<<grid, 256, 0, c->stream>>>(b, G);
+    HFB_AFTER_LAUNCH(c, "gridPreSimBatch");
+  } else if (k == BK_INTEGRATE) {
+    const size_t smem = simSmemMax();
+    if (!grid) {
+      cudaError_t e = cudaFuncSetAttribute(simIntegrateBatch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      int perSM = 0;
+      if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, simIntegrateBatch, SIM_THREADS, smem);
+      if (e != cudaSuccess) return e;
+      grid = (uint32_t)(perSM > 0 ? perSM : 1) * c->smCount;
+    }
+    simIntegrateBatch<<<grid, SIM_THREADS, smem, c->stream>>>(b, G);
+    HFB_AFTER_LAUNCH(c, "simIntegrateBatch");
+  } else if (k == BK_GRID_POST) {
+    if (!grid) grid = c->smCount * 8u;
+    gridPostSimBatch<<<grid, 256, 0, c->stream>>>(b, G);
+    HFB_AFTER_LAUNCH(c, "gridPostSimBatch");
+  } else {
+    return cudaErrorInvalidValue;
+  }
   c->launches += 1;
   return cudaGetLastError();
 }

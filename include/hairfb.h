@@ -304,17 +304,17 @@ HFB_API int hfb_frame(HfbCtx* ctx, HfbInstance* instance);
 
 /* No single counterpart in the reference, which renders one hair object per
  * frame.  One frame of n instances of uneven strand counts, points per
- * strand and viewports: each instance's pass sequence (the launches of
- * hfb_frame) runs on one of the context's worker streams, forked from and
- * joined back into the context's stream, so that the instances' kernels run
- * side by side.  The context's config (tile size, depth bins, slices, grid
- * size) applies to every instance.  Results are those of hfb_frame on each
- * instance alone.  The call flips every instance's `current`.  n <= 1024. */
+ * strand and viewports: every pass runs as one persistent launch over all
+ * instances (instance-offset tables in device memory), the launch sequence
+ * is a CUDA graph captured once per context, and the fine pass pulls the
+ * tiles of all instances from one queue.  The context's config (tile size,
+ * depth bins, slices, grid size) applies to every instance.  Results are
+ * those of hfb_frame on each instance alone.  The call flips every
+ * instance's `current`.  n <= 1024. */
 HFB_API int hfb_frame_batch(HfbCtx* ctx, HfbInstance* instances, uint32_t n);
 
-/* hfb_frame_batch run pass by pass over all instances on the context's
- * stream, with a CUDA event between passes; waits for the frame and writes
- * the GPU time of each pass, in ms, to
+/* hfb_frame_batch run as plain launches with a CUDA event between passes;
+ * waits for the frame and writes the GPU time of each pass, in ms, to
  * passMs[0..7]: grid_pre, integrate, grid_post (with its grid clear),
  * clear (the raster clears), tiles, sort, fine, shading.  For profiling. */
 #define HFB_FRAME_PASSES 8

@@ -1,6 +1,6 @@
 """Whole frames: hfb_frame (one instance, one call) and hfb_frame_batch (many
-instances, each instance's passes on one of the context's worker streams)
-against the pass-by-pass path on the same instances.
+instances, one persistent launch per pass, replayed as a captured CUDA
+graph) against the pass-by-pass path on the same instances.
 
 Bars: positions, density grid, tile counts, per-bin depth bounds, lists and
 the tile list bit-exact (the same kernels run the same arithmetic);
@@ -80,6 +80,7 @@ def _batch_vs_alone(insts, frames, profile_frame=None):
     for r in alone:
         r.before_first_frame()
     batch.before_first_frame()
+    l0 = ctx.counters()["launches"]
     for f in range(frames):
         for r in alone:
             r.frame()
@@ -97,21 +98,24 @@ def _batch_vs_alone(insts, frames, profile_frame=None):
         for ra, rb in zip(alone, batch.renderers):
             _compare(_state(ra), _state(rb), ra, f)
             assert ra.hair._current == rb.hair._current
+    # one persistent launch per pass kind for the whole batch, every frame
+    per_frame = (ctx.counters()["launches"] - l0) / frames
+    assert per_frame <= 20, per_frame
     return ctx
 
 
 def test_frame_batch_matches_each_instance_alone():
-    _batch_vs_alone(_instances(), 4, profile_frame=2)
+    _batch_vs_alone(_instances(), 4, profile_frame=1)
 
 
-def test_frame_batch_more_instances_than_streams():
-    """12 instances on 8 worker streams: streams carry several instances."""
+def test_frame_batch_many_small_instances():
+    """12 instances of uneven sizes, several frames through the captured graph."""
     rng = np.random.Generator(np.random.PCG64(11))
     common = dict(tile_size=16, depth_bins=8, slices=4, shading_points=8, grid_dims=32, iterations=4)
     insts = [synthetic.make_instance(rng, strands=int(rng.integers(200, 1500)), points=int(rng.choice([16, 24, 32])),
                                      width=int(rng.choice([128, 256])), height=int(rng.choice([128, 192])), **common)
              for _ in range(12)]
-    _batch_vs_alone(insts, 2)
+    _batch_vs_alone(insts, 3)
 
 
 def test_frame_batch_rejects_bad_instances():
