@@ -379,17 +379,25 @@ def run_batched(args, rank, world, dist):
     if dist:
         dist.barrier()
     c0 = ctx.counters()
-    step_ms = []
+    # frames back to back (the host prepares the next frame while the GPU
+    # renders); an event between frames gives each frame's GPU time
+    evs = [ev() for _ in range(args.steps + 1)]
     with ClockSampler(dev) as clk:
         torch.cuda.synchronize()
-        for _ in range(args.steps):
-            e0, e1 = ev(), ev()
-            e0.record(stream)
+        evs[0].record(stream)
+        for k in range(args.steps):
             batch.frame()
-            e1.record(stream)
-            torch.cuda.synchronize()
-            step_ms.append(e0.elapsed_time(e1))
+            evs[k + 1].record(stream)
+        torch.cuda.synchronize()
+    step_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
     c1 = ctx.counters()
+    # latency: one frame submitted and waited for at a time (host work included)
+    lat_ms = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        batch.frame()
+        torch.cuda.synchronize()
+        lat_ms.append(1000.0 * (time.perf_counter() - t0))
     launches = c1["launches"] - c0["launches"]
     dropped = c1["tileRecordsDropped"] - c0["tileRecordsDropped"]
 
@@ -433,9 +441,10 @@ def run_batched(args, rank, world, dist):
     from hairfb import uniforms as UN
     h2d = n * (UN.RENDER_UNIFORMS_BYTES + UN.SIM_UNIFORMS_BYTES)
     d2h = sum(h.numel() * 4 for h in imgs)
-    out = dict(step_ms=step_ms, plain_round_ms=plain_round_ms, plain_frame_ms=plain_frame_ms,
+    out = dict(step_ms=step_ms, lat_ms=lat_ms, plain_round_ms=plain_round_ms, plain_frame_ms=plain_frame_ms,
                pass_ms=pass_ms, K=K, e2e_ms=e2e_ms, h2d=h2d, d2h=d2h, clocks=clk.summary(), insts=insts,
                cfg=cfg, trials=[t.as_dict() for t in trials], tune_s=t_tune, launches=launches,
+               groups=getattr(ctx, "batch_groups", 1),
                dropped=dropped, n=n)
     ctx.close()
     return out
@@ -518,11 +527,13 @@ def report_batched(args, res, world, dist):
                    "frames_per_step": n, "tuned": {"tile_size": cfg.tile_size, "depth_bins": cfg.tile_depth_bins,
                                                    "slices": cfg.slices_per_pixel,
                                                    "avg_segments_per_tile": cfg.avg_segments_per_tile,
+                                                   "groups": res["groups"],
                                                    "tune_s": round(res["tune_s"], 1)},
                    "autotune_trials": [{k: (round(v, 3) if isinstance(v, float) else v) for k, v in t.items()}
                                        for t in res["trials"]],
                    "plain_frames_per_s": plain_fps, "batched_over_plain": fps / plain_fps,
                    "p50_ms": q(srt, 0.5), "p99_ms": q(srt, 0.99),
+                   "latency_p50_ms": q(sorted(res["lat_ms"]), 0.5), "latency_p99_ms": q(sorted(res["lat_ms"]), 0.99),
                    "plain_frame_p50_ms": q(psrt, 0.5), "plain_frame_p99_ms": q(psrt, 0.99),
                    "segments_per_s": world * segments * len(srt) / step_s,
                    "tile_records_per_step": sum(res["K"]), "records_dropped": res["dropped"],

@@ -9,12 +9,15 @@
 // batch to the next is data in device memory, so the kernels' launch
 // parameters never change and one captured CUDA graph serves every batch of
 // the context.
+#include <algorithm>
 #include <cstring>
 
 #define HFB_TU 5
 #include "hfb_internal.cuh"
 
 namespace hfb {
+
+static_assert(BATCH_GROUPS_MAX == sizeof(HfbCtx::batchStreams) / sizeof(cudaStream_t), "group stream table");
 
 // cmdClearBeforeRender of the tiles, fine and sort passes (hairTilesPass.ts:48-52,
 // hairFinePass.ts:50-55, hairTileSortPass.ts:63-68).
@@ -175,7 +178,7 @@ cudaError_t launchBatchClear(HfbCtx* c, const BatchView& b, BatchKind k) {
   HFB_CHECK_BIND(c);
   uint32_t& grid = c->batchGrid[k];
   if (!grid) grid = c->smCount * 8u;
-  clearBatch<<<grid, 256, 0, c->stream>>>(b, c->cfg, (uint32_t)k);
+  clearBatch<<<batchLaunchGrid(c, grid), 256, 0, c->stream>>>(b, c->cfg, (uint32_t)k);
   HFB_AFTER_LAUNCH(c, "clearBatch");
   c->launches += 1;
   return cudaGetLastError();
@@ -208,90 +211,173 @@ static cudaError_t batchSequence(HfbCtx* c, const BatchView& b, cudaEvent_t* ev 
   return e;
 }
 
-// Fills the staging copy, uploads it and runs the frame for n validated
-// instances.
+// One instance as the batched kernels read it.
+static void fillInstance(const HfbConfig& cfg, const HfbInstance& s, BatchInst& I) {
+  memset(&I, 0, sizeof(I));
+  memcpy(&I.U, s.uniforms, sizeof(HfbUniforms));
+  memcpy(&I.SU, s.simUniforms, sizeof(HfbSimUniforms));
+  I.bsphere = make_float4(s.hair.boundingSphere[0], s.hair.boundingSphere[1], s.hair.boundingSphere[2],
+                          s.hair.boundingSphere[3]);
+  I.S = s.hair.strandsCount;
+  I.P = s.hair.pointsPerStrand;
+  I.strandsToRender = s.strandsToRender;
+  I.sdfDims = s.sdfDims;
+  I.W = s.raster.width;
+  I.H = s.raster.height;
+  I.maxDrawn = s.raster.maxDrawnSegments;
+  I.T = divCeil(I.W, cfg.tileSize) * divCeil(I.H, cfg.tileSize);
+  I.aoW = s.ao ? s.aoWidth : 0u;
+  I.aoH = s.ao ? s.aoHeight : 0u;
+  I.smSize = s.shadowMap ? s.shadowMapSize : 0u;
+  I.posNew = (float4*)s.positions[1u - s.current];
+  I.posOld = (const float4*)s.positions[s.current];
+  I.initial = (const float4*)s.positionsInitial;
+  I.tan = (const float4*)s.tangents;
+  I.segLen = s.segmentLengths;
+  I.dv = (int4*)s.densityVelocity;
+  I.gw = (float4*)s.densityGradWind;
+  I.sdf = s.sdf;
+  I.shading = (float4*)s.shading;
+  I.depth = s.sceneDepth;
+  I.shadingDepth = s.shadingDepth ? s.shadingDepth : s.sceneDepth;
+  I.ao = s.ao;
+  I.sm = s.shadowMap;
+  I.tiles = (uint4*)s.raster.tiles;
+  I.segBuf = s.raster.tileSegments;
+  I.segCount = s.raster.segmentCountPerTile;
+  I.sortBuckets = s.raster.sortBuckets;
+  I.tileList = s.raster.tileList;
+  I.result = s.raster.rasterizerResult;
+  I.scratch = (unsigned char*)s.raster.scratch;
+}
+
+// Rough GPU work of one instance's frame, for balancing the groups: the
+// per-point passes and the per-pixel passes.
+static double frameWork(const HfbInstance& in) {
+  return (double)in.hair.strandsCount * in.hair.pointsPerStrand +
+         0.25 * (double)in.raster.width * in.raster.height;
+}
+
+static cudaError_t ensureGroupStreams(HfbCtx* c) {
+  cudaError_t e = cudaSuccess;
+  if (!c->batchFork) e = cudaEventCreateWithFlags(&c->batchFork, cudaEventDisableTiming);
+  for (uint32_t g = 0; g < BATCH_GROUPS_MAX && e == cudaSuccess; g++) {
+    if (!c->batchStreams[g]) e = cudaStreamCreateWithFlags(&c->batchStreams[g], cudaStreamNonBlocking);
+    if (e == cudaSuccess && !c->batchJoin[g]) e = cudaEventCreateWithFlags(&c->batchJoin[g], cudaEventDisableTiming);
+  }
+  return e;
+}
+
+// The launch sequence of NG groups: one group on c->stream, or each group
+// on its own worker stream, forked from c->stream and joined back into it.
+static cudaError_t groupsSequence(HfbCtx* c, uint32_t NG) {
+  if (NG == 1) return batchSequence(c, batchView(c->batchDev));
+  const cudaStream_t caller = c->stream;
+  cudaError_t e = cudaEventRecord(c->batchFork, caller);
+  for (uint32_t g = 0; g < NG && e == cudaSuccess; g++) e = cudaStreamWaitEvent(c->batchStreams[g], c->batchFork, 0);
+  if (e != cudaSuccess) return e;
+  c->batchGridDiv = NG;
+  for (uint32_t g = 0; g < NG && e == cudaSuccess; g++) {
+    c->stream = c->batchStreams[g];
+    e = batchSequence(c, batchView((char*)c->batchDev + (size_t)g * BATCH_BYTES));
+  }
+  c->stream = caller;
+  c->batchGridDiv = 1;
+  for (uint32_t g = 0; g < NG; g++) {  // also after a failed launch: the streams stay joined
+    cudaError_t ej = cudaEventRecord(c->batchJoin[g], c->batchStreams[g]);
+    if (ej == cudaSuccess) ej = cudaStreamWaitEvent(caller, c->batchJoin[g], 0);
+    if (e == cudaSuccess) e = ej;
+  }
+  return e;
+}
+
+// Fills the staging copy (one device table per group), uploads it and runs
+// the frame for n validated instances.
 cudaError_t frameBatch(HfbCtx* c, HfbInstance* insts, uint32_t n, float* passMs) {
   cudaError_t e = cudaSuccess;
+  constexpr size_t TABLES = (size_t)BATCH_GROUPS_MAX * BATCH_BYTES;
   if (!c->batchDev) {
-    e = cudaMalloc(&c->batchDev, BATCH_BYTES);
+    e = cudaMalloc(&c->batchDev, TABLES);
     for (int k = 0; k < 2 && e == cudaSuccess; k++) {
-      e = cudaMallocHost(&c->batchHost[k], BATCH_BYTES);
+      e = cudaMallocHost(&c->batchHost[k], TABLES);
       if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->batchCopied[k], cudaEventDisableTiming);
       if (e == cudaSuccess) e = cudaEventRecord(c->batchCopied[k], c->stream);
     }
+    if (e == cudaSuccess) e = ensureGroupStreams(c);
     if (e != cudaSuccess) return e;
+  }
+  // groups: largest instance first, each to the group with the least work so
+  // far (the profiling run keeps one group: its passes are timed one by one)
+  uint32_t NG = passMs ? 1u : (c->batchGroups < n ? c->batchGroups : n);
+  if (NG < 1u) NG = 1u;
+  uint32_t* group = new uint32_t[n];
+  {
+    uint32_t* order = new uint32_t[n];
+    for (uint32_t i = 0; i < n; i++) order[i] = i;
+    std::stable_sort(order, order + n, [&](uint32_t a, uint32_t b) { return frameWork(insts[a]) > frameWork(insts[b]); });
+    double load[BATCH_GROUPS_MAX] = {};
+    for (uint32_t k = 0; k < n; k++) {
+      const uint32_t i = order[k];
+      const uint32_t g = (uint32_t)(std::min_element(load, load + NG) - load);
+      load[g] += frameWork(insts[i]);
+      group[i] = g;
+    }
+    delete[] order;
   }
   // the staging copy is rewritten once its previous upload has been read
   const uint32_t k = c->batchFlip;
   c->batchFlip ^= 1u;
   e = cudaEventSynchronize(c->batchCopied[k]);
-  if (e != cudaSuccess) return e;
-  char* h = (char*)c->batchHost[k];
-  BatchHdr* hdr = (BatchHdr*)h;
-  memset(hdr, 0, sizeof(*hdr));
-  hdr->n = n;
-  uint32_t* prefix = (uint32_t*)(h + BATCH_PREFIX_OFF);
-  BatchInst* bi = (BatchInst*)(h + BATCH_INSTS_OFF);
+  if (e != cudaSuccess) { delete[] group; return e; }
   const HfbConfig& cfg = c->cfg;
+  uint32_t ng[BATCH_GROUPS_MAX] = {};
+  size_t smem = c->simBatchSmem;
   for (uint32_t i = 0; i < n; i++) {
-    const HfbInstance& s = insts[i];
-    BatchInst& I = bi[i];
-    memset(&I, 0, sizeof(I));
-    memcpy(&I.U, s.uniforms, sizeof(HfbUniforms));
-    memcpy(&I.SU, s.simUniforms, sizeof(HfbSimUniforms));
-    I.bsphere = make_float4(s.hair.boundingSphere[0], s.hair.boundingSphere[1], s.hair.boundingSphere[2],
-                            s.hair.boundingSphere[3]);
-    I.S = s.hair.strandsCount;
-    I.P = s.hair.pointsPerStrand;
-    I.strandsToRender = s.strandsToRender;
-    I.sdfDims = s.sdfDims;
-    I.W = s.raster.width;
-    I.H = s.raster.height;
-    I.maxDrawn = s.raster.maxDrawnSegments;
-    I.T = divCeil(I.W, cfg.tileSize) * divCeil(I.H, cfg.tileSize);
-    I.aoW = s.ao ? s.aoWidth : 0u;
-    I.aoH = s.ao ? s.aoHeight : 0u;
-    I.smSize = s.shadowMap ? s.shadowMapSize : 0u;
-    I.posNew = (float4*)s.positions[1u - s.current];
-    I.posOld = (const float4*)s.positions[s.current];
-    I.initial = (const float4*)s.positionsInitial;
-    I.tan = (const float4*)s.tangents;
-    I.segLen = s.segmentLengths;
-    I.dv = (int4*)s.densityVelocity;
-    I.gw = (float4*)s.densityGradWind;
-    I.sdf = s.sdf;
-    I.shading = (float4*)s.shading;
-    I.depth = s.sceneDepth;
-    I.shadingDepth = s.shadingDepth ? s.shadingDepth : s.sceneDepth;
-    I.ao = s.ao;
-    I.sm = s.shadowMap;
-    I.tiles = (uint4*)s.raster.tiles;
-    I.segBuf = s.raster.tileSegments;
-    I.segCount = s.raster.segmentCountPerTile;
-    I.sortBuckets = s.raster.sortBuckets;
-    I.tileList = s.raster.tileList;
-    I.result = s.raster.rasterizerResult;
-    I.scratch = (unsigned char*)s.raster.scratch;
+    const uint32_t g = group[i];
+    char* h = (char*)c->batchHost[k] + (size_t)g * BATCH_BYTES;
+    fillInstance(cfg, insts[i], ((BatchInst*)(h + BATCH_INSTS_OFF))[ng[g]++]);
+    const size_t sb = simSmemBytes(insts[i].hair.pointsPerStrand);
+    smem = smem > sb ? smem : sb;
   }
-  for (uint32_t kind = 0; kind < BK_COUNT; kind++) {
-    uint32_t* row = prefix + (size_t)kind * (BATCH_MAX + 1);
-    uint32_t acc = 0;
-    for (uint32_t i = 0; i < n; i++) {
-      row[i] = acc;
-      acc += batchBlocks(cfg, (BatchKind)kind, bi[i]);
+  delete[] group;
+  // the integration launch stages the longest strands of the batch: a batch
+  // with longer strands than any before it re-sizes it (and the graph)
+  if (smem > c->simBatchSmem) {
+    c->simBatchSmem = smem;
+    c->batchGrid[BK_INTEGRATE] = 0;
+    if (c->batchGraph) {
+      e = cudaStreamSynchronize(c->stream);
+      if (e != cudaSuccess) return e;
+      cudaGraphExecDestroy(c->batchGraph);
+      c->batchGraph = nullptr;
     }
-    row[n] = acc;
   }
-  const size_t bytes = BATCH_INSTS_OFF + (size_t)n * sizeof(BatchInst);
-  e = cudaMemcpyAsync(c->batchDev, h, bytes, cudaMemcpyHostToDevice, c->stream);
+  for (uint32_t g = 0; g < NG && e == cudaSuccess; g++) {
+    char* h = (char*)c->batchHost[k] + (size_t)g * BATCH_BYTES;
+    BatchHdr* hdr = (BatchHdr*)h;
+    memset(hdr, 0, sizeof(*hdr));
+    hdr->n = ng[g];
+    uint32_t* prefix = (uint32_t*)(h + BATCH_PREFIX_OFF);
+    const BatchInst* bi = (const BatchInst*)(h + BATCH_INSTS_OFF);
+    for (uint32_t kind = 0; kind < BK_COUNT; kind++) {
+      uint32_t* row = prefix + (size_t)kind * (BATCH_MAX + 1);
+      uint32_t acc = 0;
+      for (uint32_t i = 0; i < ng[g]; i++) {
+        row[i] = acc;
+        acc += batchBlocks(cfg, (BatchKind)kind, bi[i]);
+      }
+      row[ng[g]] = acc;
+    }
+    const size_t bytes = BATCH_INSTS_OFF + (size_t)ng[g] * sizeof(BatchInst);
+    e = cudaMemcpyAsync((char*)c->batchDev + (size_t)g * BATCH_BYTES, h, bytes, cudaMemcpyHostToDevice, c->stream);
+  }
   if (e == cudaSuccess) e = cudaEventRecord(c->batchCopied[k], c->stream);
   if (e != cudaSuccess) return e;
 
-  const BatchView b = batchView(c->batchDev);
-  if (passMs) {  // plain launches with an event between passes
+  if (passMs) {  // one group, plain launches with an event between passes
     cudaEvent_t ev[HFB_FRAME_PASSES + 1] = {};
     for (int i = 0; i <= HFB_FRAME_PASSES && e == cudaSuccess; i++) e = cudaEventCreate(&ev[i]);
-    if (e == cudaSuccess) e = batchSequence(c, b, ev);
+    if (e == cudaSuccess) e = batchSequence(c, batchView(c->batchDev), ev);
     if (e == cudaSuccess) e = cudaEventSynchronize(ev[HFB_FRAME_PASSES]);
     for (int i = 0; i < HFB_FRAME_PASSES && e == cudaSuccess; i++) e = cudaEventElapsedTime(&passMs[i], ev[i], ev[i + 1]);
     for (int i = 0; i <= HFB_FRAME_PASSES; i++)
@@ -303,30 +389,40 @@ cudaError_t frameBatch(HfbCtx* c, HfbInstance* insts, uint32_t n, float* passMs)
 #ifdef HFB_DEVICE_CHECKS
   c->batchGraphLaunches = ~0ull;  // the checked build waits after every launch: no capture
 #endif
+  if (c->batchGraph && c->batchGraphGroups != NG) {  // made for another number of groups
+    e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return e;
+    cudaGraphExecDestroy(c->batchGraph);
+    c->batchGraph = nullptr;
+  }
   if (c->batchCalls++ == 0 || c->batchGraphLaunches == ~0ull) {
-    // first batch: plain launches (they also set the kernels' attributes)
-    const uint64_t l0 = c->launches;
-    e = batchSequence(c, b);
-    if (c->batchGraphLaunches != ~0ull) c->batchGraphLaunches = c->launches - l0;
+    // the first batch (which also sets the kernels' attributes), or no graph: plain launches
+    e = groupsSequence(c, NG);
   } else {
     if (!c->batchGraph) {
-      cudaGraph_t g = nullptr;
+      cudaGraph_t gr = nullptr;
       e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
       if (e != cudaSuccess) return e;
       const uint64_t l0 = c->launches;
-      cudaError_t el = batchSequence(c, b);
+      cudaError_t el = groupsSequence(c, NG);
+      const uint64_t captured = c->launches - l0;
       c->launches = l0;
-      e = cudaStreamEndCapture(c->stream, &g);
+      e = cudaStreamEndCapture(c->stream, &gr);
       if (el != cudaSuccess) e = el;
-      if (e == cudaSuccess) e = cudaGraphInstantiate(&c->batchGraph, g, 0);
-      if (g) cudaGraphDestroy(g);
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&c->batchGraph, gr, 0);
+      if (gr) cudaGraphDestroy(gr);
       if (e != cudaSuccess) {
         // a stream that cannot be captured (e.g. the legacy default stream): plain launches
         cudaGetLastError();
         c->batchGraph = nullptr;
         c->batchGraphLaunches = ~0ull;
-        return batchSequence(c, b);
+        e = groupsSequence(c, NG);
+        if (e != cudaSuccess) return e;
+        for (uint32_t i = 0; i < n; i++) insts[i].current ^= 1u;
+        return cudaGetLastError();
       }
+      c->batchGraphLaunches = captured;
+      c->batchGraphGroups = NG;
     }
     e = cudaGraphLaunch(c->batchGraph, c->stream);
     c->launches += c->batchGraphLaunches;
@@ -337,6 +433,14 @@ cudaError_t frameBatch(HfbCtx* c, HfbInstance* insts, uint32_t n, float* passMs)
 }
 
 void frameBatchRelease(HfbCtx* c) {
+  for (uint32_t g = 0; g < BATCH_GROUPS_MAX; g++) {
+    if (c->batchJoin[g]) cudaEventDestroy(c->batchJoin[g]);
+    if (c->batchStreams[g]) cudaStreamDestroy(c->batchStreams[g]);
+    c->batchJoin[g] = nullptr;
+    c->batchStreams[g] = nullptr;
+  }
+  if (c->batchFork) cudaEventDestroy(c->batchFork);
+  c->batchFork = nullptr;
   if (c->batchGraph) cudaGraphExecDestroy(c->batchGraph);
   for (int k = 0; k < 2; k++) {
     if (c->batchCopied[k]) cudaEventDestroy(c->batchCopied[k]);

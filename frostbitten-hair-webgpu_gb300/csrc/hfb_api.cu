@@ -420,6 +420,13 @@ int hfb_frame_batch(HfbCtx* c, HfbInstance* insts, uint32_t n) {
   return HFB_OK;
 }
 
+int hfb_ctx_set_batch_groups(HfbCtx* c, uint32_t groups) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, groups >= 1 && groups <= hfb::BATCH_GROUPS_MAX, "batch groups must be in [1, 4]");
+  c->batchGroups = groups;
+  return HFB_OK;
+}
+
 int hfb_frame_batch_profile(HfbCtx* c, HfbInstance* insts, uint32_t n, float* passMs) {
   HFB_CHECK_CTX(c);
   HFB_REQUIRE(c, insts && n > 0 && passMs, "NULL argument or empty batch");

@@ -34,6 +34,15 @@ struct HfbCtx {
   cudaGraphExec_t batchGraph = nullptr;
   uint64_t batchGraphLaunches = 0;  // kernels in the graph
   uint32_t batchCalls = 0;
+  size_t simBatchSmem = 0;  // shared memory of the batched integration launch
+  // groups of a batched frame: each group's passes on its own worker stream,
+  // its persistent launches sized to 1 / groups of the GPU
+  uint32_t batchGroups = 1;       // requested (hfb_ctx_set_batch_groups)
+  uint32_t batchGraphGroups = 0;  // groups the captured graph was made with
+  uint32_t batchGridDiv = 1;      // divisor of the persistent grids while a group launches
+  cudaStream_t batchStreams[4] = {};
+  cudaEvent_t batchFork = nullptr;
+  cudaEvent_t batchJoin[4] = {};
   // self-checking build: the device CheckState (hfb_check.cuh), else NULL
   void* checkDev = nullptr;
 };
@@ -169,6 +178,13 @@ cudaError_t clearRaster(HfbCtx* c, const HfbRasterBuffers& rb);
 // captured once as a CUDA graph.
 // ---------------------------------------------------------------------------
 constexpr uint32_t BATCH_MAX = 1024;  // instances per batch
+constexpr uint32_t BATCH_GROUPS_MAX = 4;
+// Grid of one persistent batched launch: the full-GPU grid `full`, divided
+// among the groups that run side by side.
+inline uint32_t batchLaunchGrid(const HfbCtx* c, uint32_t full) {
+  const uint32_t g = full / c->batchGridDiv;
+  return g ? g : 1u;
+}
 enum BatchKind : uint32_t {
   BK_CLEAR_FRAME = 0,  // raster clears + tiles-pass counters
   BK_GRID_PRE,

@@ -1975,7 +1975,7 @@ cudaError_t launchFineBatchT(HfbCtx* c, const BatchView& b) {
   DeviceCounters* dc = (DeviceCounters*)c->dCounters;
   uint32_t& sgrid = c->batchGrid[BK_SCHEDULE];
   if (!sgrid) sgrid = c->smCount;
-  fineScheduleBatch<<<sgrid, 1024, 0, c->stream>>>(b, cfg, grid, dc);
+  fineScheduleBatch<<<batchLaunchGrid(c, sgrid), 1024, 0, c->stream>>>(b, cfg, batchLaunchGrid(c, grid), dc);
   HFB_AFTER_LAUNCH(c, "fineScheduleBatch");
   fineItemPrefixBatch<<<1, 1024, 0, c->stream>>>(b, cfg);
   HFB_AFTER_LAUNCH(c, "fineItemPrefixBatch");
@@ -1987,7 +1987,7 @@ cudaError_t launchFineBatchT(HfbCtx* c, const BatchView& b) {
   a.alphaQuadratic = cfg.alphaQuadratic;
   a.alphaMul = cfg.alphaMultiplier;
   a.counters = dc;
-  fineBatch<TS, MAXL><<<grid, TS * TS, SMEM, c->stream>>>(b, a, cfg);
+  fineBatch<TS, MAXL><<<batchLaunchGrid(c, grid), TS * TS, SMEM, c->stream>>>(b, a, cfg);
   HFB_AFTER_LAUNCH(c, "fineBatch");
   c->launches += 3;
   return cudaGetLastError();
@@ -2091,17 +2091,17 @@ cudaError_t launchBatchTiles(HfbCtx* c, const BatchView& b) {
     e = cudaFuncSetAttribute(largeBinsBatch, cudaFuncAttributeMaxDynamicSharedMemorySize, LARGE_SMEM_KEYS * 4);
     if (e != cudaSuccess) return e;
   }
-  tilesRasterBatch<<<g[BK_RASTER], TR_SEGS, 0, c->stream>>>(b, cfg, dc);
+  tilesRasterBatch<<<batchLaunchGrid(c, g[BK_RASTER]), TR_SEGS, 0, c->stream>>>(b, cfg, dc);
   HFB_AFTER_LAUNCH(c, "tilesRasterBatch");
-  binScanBatch<<<g[BK_SCAN], 512, 0, c->stream>>>(b, cfg);
+  binScanBatch<<<batchLaunchGrid(c, g[BK_SCAN]), 512, 0, c->stream>>>(b, cfg);
   HFB_AFTER_LAUNCH(c, "binScanBatch");
-  binScanSumsBatch<<<g[BK_SCAN_SUMS], 1024, 0, c->stream>>>(b, cfg);
+  binScanSumsBatch<<<batchLaunchGrid(c, g[BK_SCAN_SUMS]), 1024, 0, c->stream>>>(b, cfg);
   HFB_AFTER_LAUNCH(c, "binScanSumsBatch");
-  binScatterBatch<<<g[BK_SCATTER], 256, 0, c->stream>>>(b, cfg, dc);
+  binScatterBatch<<<batchLaunchGrid(c, g[BK_SCATTER]), 256, 0, c->stream>>>(b, cfg, dc);
   HFB_AFTER_LAUNCH(c, "binScatterBatch");
-  binFinalizeBatch<<<g[BK_FINALIZE], 256, 0, c->stream>>>(b, cfg);
+  binFinalizeBatch<<<batchLaunchGrid(c, g[BK_FINALIZE]), 256, 0, c->stream>>>(b, cfg);
   HFB_AFTER_LAUNCH(c, "binFinalizeBatch");
-  largeBinsBatch<<<g[BK_LARGE], 1024, LARGE_SMEM_KEYS * 4, c->stream>>>(b, cfg);
+  largeBinsBatch<<<batchLaunchGrid(c, g[BK_LARGE]), 1024, LARGE_SMEM_KEYS * 4, c->stream>>>(b, cfg);
   HFB_AFTER_LAUNCH(c, "largeBinsBatch");
   c->launches += 6;
   return cudaGetLastError();
@@ -2112,7 +2112,7 @@ cudaError_t launchBatchSort(HfbCtx* c, const BatchView& b) {
   if (c->cfg.sortBuckets > SORT_MAX_BUCKETS) return cudaErrorInvalidValue;
   uint32_t& grid = c->batchGrid[BK_SORT];
   if (!grid) grid = c->smCount;
-  tileSortBatch<<<grid, 1024, 0, c->stream>>>(b, c->cfg);
+  tileSortBatch<<<batchLaunchGrid(c, grid), 1024, 0, c->stream>>>(b, c->cfg);
   HFB_AFTER_LAUNCH(c, "tileSortBatch");
   c->launches += 1;
   return cudaGetLastError();

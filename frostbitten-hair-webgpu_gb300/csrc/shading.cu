@@ -258,7 +258,7 @@ cudaError_t launchBatchShading(HfbCtx* c, const BatchView& b) {
   HFB_CHECK_BIND(c);
   uint32_t& grid = c->batchGrid[BK_SHADING];
   if (!grid) grid = c->smCount * 16u;
-  shadingBatch<<<grid, 128, 0, c->stream>>>(b, c->cfg.shadingPoints, c->cfg.cameraNear, c->cfg.cameraFar);
+  shadingBatch<<<batchLaunchGrid(c, grid), 128, 0, c->stream>>>(b, c->cfg.shadingPoints, c->cfg.cameraNear, c->cfg.cameraFar);
   HFB_AFTER_LAUNCH(c, "shadingBatch");
   c->launches += 1;
   return cudaGetLastError();

@@ -370,39 +370,100 @@ simIntegrateKernel(const HfbSimUniforms u, uint32_t S, uint32_t P, uint32_t G,
 // ---------------------------------------------------------------------------
 // GridPostSimPass.main, gridPostSimPass.wgsl.ts:45-72 with
 // _addGridDensityVelocity, densityVelocityGrid.wgsl.ts:93-124.
-// One thread per point; i32 atomics (wrapping, order-independent).
+//
+// One thread per point, eight corners, four wrapping i32 adds each.  The
+// adds of a block are first merged per grid node in a shared-memory hash
+// table (neighbouring points of a strand share nodes: a warp's 256 corner
+// updates touch ~100 nodes), then each node's four sums go to global memory
+// as one set of atomics.  Wrapping integer sums do not depend on their
+// order, so the grid is bit-exact whatever the merge; an update that finds
+// no free slot within GP_PROBES goes straight to global memory.
 // ---------------------------------------------------------------------------
+constexpr uint32_t GP_THREADS = 256;
+constexpr uint32_t GP_HASH = 2048;  // slots (power of two)
+constexpr uint32_t GP_PROBES = 32;
+constexpr uint32_t GP_EMPTY = 0xffffffffu;
+
+struct GridPostShared {
+  uint32_t key[GP_HASH];
+  uint4 val[GP_HASH];
+};
+
+__device__ __forceinline__ void gridPostClear(GridPostShared& sh) {
+  for (uint32_t e = threadIdx.x; e < GP_HASH; e += blockDim.x) {
+    sh.key[e] = GP_EMPTY;
+    sh.val[e] = make_uint4(0u, 0u, 0u, 0u);
+  }
+}
+
+__device__ __forceinline__ void gridPostAdd(GridPostShared& sh, unsigned* __restrict__ dv, uint32_t idx,
+                                            uint4 v) {
+  uint32_t h = (idx * 2654435761u) >> (32 - 11);  // Fibonacci hash into GP_HASH = 2^11 slots
+  for (uint32_t p = 0; p < GP_PROBES; p++) {
+    const uint32_t old = atomicCAS(&sh.key[h], GP_EMPTY, idx);
+    if (old == GP_EMPTY || old == idx) {
+      atomicAdd(&sh.val[h].x, v.x);
+      atomicAdd(&sh.val[h].y, v.y);
+      atomicAdd(&sh.val[h].z, v.z);
+      atomicAdd(&sh.val[h].w, v.w);
+      return;
+    }
+    h = (h + 1u) & (GP_HASH - 1u);
+  }
+  unsigned* c = reinterpret_cast<unsigned*>(HFB_G(reinterpret_cast<uint4*>(dv + 4u * idx)));
+  atomicAdd(c + 0, v.x);
+  atomicAdd(c + 1, v.y);
+  atomicAdd(c + 2, v.z);
+  atomicAdd(c + 3, v.w);
+}
+
+// Points [first, first + GP_THREADS) of the N; the table is empty on entry
+// and on exit.  All threads of the block call it.
 __device__ __forceinline__ void gridPostSimBody(const HfbSimUniforms& u, uint32_t N, uint32_t G,
                                                 const float4* __restrict__ prev, const float4* __restrict__ now,
-                                                unsigned* __restrict__ dv, uint32_t i) {
+                                                unsigned* __restrict__ dv, uint32_t i, GridPostShared& sh) {
   const bool valid = i < N;
   float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
   if (valid) { a = __ldg(HFB_G(&prev[i])); b = __ldg(HFB_G(&now[i])); }
   const f3 pn = mk3(b.x, b.y, b.z);
   const f3 vel = sub3(pn, mk3(a.x, a.y, a.z));
   const GridCo co = gridCell(G, gridMin(u), gridMax(u), pn);
-  // Eight corners, four wrapping i32 adds each (fire-and-forget reductions
-  // in L2; the sums do not depend on their order).
-  if (!valid) return;
+  if (valid) {
 #pragma unroll
-  for (uint32_t k = 0; k < 8u; k++) {
-    const uint32_t x = co.mn[0] + (k & 1u), y = co.mn[1] + ((k >> 1) & 1u), z = co.mn[2] + (k >> 2);
-    if (x > co.mx[0] || y > co.mx[1] || z > co.mx[2]) continue;
-    const uint32_t idx = gridIdx(G, x, y, z);
-    const f3 w = cellWeights(x, y, z, co.p);
-    const f3 cv = mul3(vel, w);
-    unsigned* c = reinterpret_cast<unsigned*>(HFB_G(reinterpret_cast<uint4*>(dv + 4u * idx)));
-    atomicAdd(c + 0, (unsigned)gridEncode(cv.x));
-    atomicAdd(c + 1, (unsigned)gridEncode(cv.y));
-    atomicAdd(c + 2, (unsigned)gridEncode(cv.z));
-    atomicAdd(c + 3, (unsigned)gridEncode(len3(w)));
+    for (uint32_t k = 0; k < 8u; k++) {
+      const uint32_t x = co.mn[0] + (k & 1u), y = co.mn[1] + ((k >> 1) & 1u), z = co.mn[2] + (k >> 2);
+      if (x > co.mx[0] || y > co.mx[1] || z > co.mx[2]) continue;
+      const uint32_t idx = gridIdx(G, x, y, z);
+      const f3 w = cellWeights(x, y, z, co.p);
+      const f3 cv = mul3(vel, w);
+      gridPostAdd(sh, dv, idx,
+                  make_uint4((unsigned)gridEncode(cv.x), (unsigned)gridEncode(cv.y), (unsigned)gridEncode(cv.z),
+                             (unsigned)gridEncode(len3(w))));
+    }
   }
+  __syncthreads();
+  for (uint32_t e = threadIdx.x; e < GP_HASH; e += blockDim.x) {
+    const uint32_t idx = sh.key[e];
+    if (idx == GP_EMPTY) continue;
+    const uint4 v = sh.val[e];
+    unsigned* c = reinterpret_cast<unsigned*>(HFB_G(reinterpret_cast<uint4*>(dv + 4u * idx)));
+    atomicAdd(c + 0, v.x);
+    atomicAdd(c + 1, v.y);
+    atomicAdd(c + 2, v.z);
+    atomicAdd(c + 3, v.w);
+    sh.key[e] = GP_EMPTY;
+    sh.val[e] = make_uint4(0u, 0u, 0u, 0u);
+  }
+  __syncthreads();
 }
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(GP_THREADS)
 gridPostSimKernel(const HfbSimUniforms u, uint32_t N, uint32_t G, const float4* __restrict__ prev,
                   const float4* __restrict__ now, unsigned* __restrict__ dv) {
-  gridPostSimBody(u, N, G, prev, now, dv, blockIdx.x * blockDim.x + threadIdx.x);
+  __shared__ GridPostShared sh;
+  gridPostClear(sh);
+  __syncthreads();
+  gridPostSimBody(u, N, G, prev, now, dv, blockIdx.x * blockDim.x + threadIdx.x, sh);
 }
 
 // ---- batched: persistent over the virtual blocks of every instance ----
@@ -417,7 +478,7 @@ __global__ void __launch_bounds__(256) gridPreSimBatch(BatchView b, uint32_t G) 
   }
 }
 
-__global__ void __launch_bounds__(SIM_THREADS) simIntegrateBatch(BatchView b, uint32_t G) {
+__global__ void __launch_bounds__(SIM_THREADS, 4) simIntegrateBatch(BatchView b, uint32_t G) {
   extern __shared__ float4 simSmem[];
   const uint32_t n = b.hdr->n;
   const uint32_t* row = b.prefix + BK_INTEGRATE * (BATCH_MAX + 1);
@@ -431,7 +492,10 @@ __global__ void __launch_bounds__(SIM_THREADS) simIntegrateBatch(BatchView b, ui
   }
 }
 
-__global__ void __launch_bounds__(256) gridPostSimBatch(BatchView b, uint32_t G) {
+__global__ void __launch_bounds__(GP_THREADS) gridPostSimBatch(BatchView b, uint32_t G) {
+  __shared__ GridPostShared sh;
+  gridPostClear(sh);
+  __syncthreads();
   const uint32_t n = b.hdr->n;
   const uint32_t* row = b.prefix + BK_GRID_POST * (BATCH_MAX + 1);
   const uint32_t total = row[n];
@@ -439,15 +503,11 @@ __global__ void __launch_bounds__(256) gridPostSimBatch(BatchView b, uint32_t G)
     const uint32_t i = batchFind(row, n, v);
     const BatchInst& I = b.insts[i];
     // after the swap: prev = the old current positions, now = the new ones
-    gridPostSimBody(I.SU, I.S * I.P, G, I.posOld, I.posNew, (unsigned*)I.dv, (v - row[i]) * 256u + threadIdx.x);
+    gridPostSimBody(I.SU, I.S * I.P, G, I.posOld, I.posNew, (unsigned*)I.dv, (v - row[i]) * GP_THREADS + threadIdx.x,
+                    sh);
   }
 }
 
-size_t simSmemMax() {
-  size_t m = 0;
-  for (uint32_t P = 4; P <= 128; P++) m = m > simSmemBytes(P) ? m : simSmemBytes(P);
-  return m;
-}
 
 }  // namespace
 
@@ -488,10 +548,10 @@ cudaError_t launchBatchSim(HfbCtx* c, const BatchView& b, BatchKind k) {
   uint32_t& grid = c->batchGrid[k];
   if (k == BK_GRID_PRE) {
     if (!grid) grid = c->smCount * 8u;
-    gridPreSimBatch<<<grid, 256, 0, c->stream>>>(b, G);
+    gridPreSimBatch<<<batchLaunchGrid(c, grid), 256, 0, c->stream>>>(b, G);
     HFB_AFTER_LAUNCH(c, "gridPreSimBatch");
   } else if (k == BK_INTEGRATE) {
-    const size_t smem = simSmemMax();
+    const size_t smem = c->simBatchSmem;  // the largest staging any batch of the context has needed
     if (!grid) {
       cudaError_t e = cudaFuncSetAttribute(simIntegrateBatch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       int perSM = 0;
@@ -500,11 +560,11 @@ cudaError_t launchBatchSim(HfbCtx* c, const BatchView& b, BatchKind k) {
       if (e != cudaSuccess) return e;
       grid = (uint32_t)(perSM > 0 ? perSM : 1) * c->smCount;
     }
-    simIntegrateBatch<<<grid, SIM_THREADS, smem, c->stream>>>(b, G);
+    simIntegrateBatch<<<batchLaunchGrid(c, grid), SIM_THREADS, smem, c->stream>>>(b, G);
     HFB_AFTER_LAUNCH(c, "simIntegrateBatch");
   } else if (k == BK_GRID_POST) {
     if (!grid) grid = c->smCount * 8u;
-    gridPostSimBatch<<<grid, 256, 0, c->stream>>>(b, G);
+    gridPostSimBatch<<<batchLaunchGrid(c, grid), GP_THREADS, 0, c->stream>>>(b, G);
     HFB_AFTER_LAUNCH(c, "gridPostSimBatch");
   } else {
     return cudaErrorInvalidValue;
@@ -521,7 +581,7 @@ cudaError_t launchGridPostSim(HfbCtx* c, const HfbSimUniforms& u, const HfbHairD
   if (e != cudaSuccess) return e;
   uint32_t N = h.strandsCount * h.pointsPerStrand;
   if (N) {
-    gridPostSimKernel<<<divCeil(N, 256), 256, 0, c->stream>>>(u, N, G, (const float4*)prev,
+    gridPostSimKernel<<<divCeil(N, GP_THREADS), GP_THREADS, 0, c->stream>>>(u, N, G, (const float4*)prev,
                                                                (const float4*)now, (unsigned*)dv);
     HFB_AFTER_LAUNCH(c, "gridPostSimKernel");
     c->launches += 1;

@@ -1,7 +1,8 @@
 """Autotuner of batched frames: picks the pass constants a batch runs with.
 
-The candidates are tile size x depth bins (x fine-pass CTA count); each is
-timed on the batch itself with ``hfb_frame_batch`` (CUDA events, after
+The candidates are tile size x depth bins, then the number of instance
+groups that run side by side (``hfb_ctx_set_batch_groups``); each is timed
+on the batch itself with ``hfb_frame_batch`` (CUDA events, after
 warm-up frames), and the fastest candidate that drops no (segment, tile)
 record wins -- a dropped record would change the image, so such a
 candidate is not an equal-accuracy choice.  The segment pool is sized per
@@ -24,6 +25,7 @@ from .renderer import BatchRenderer, Renderer
 
 TILE_SIZES = (8, 16, 32)
 DEPTH_BINS = (4, 8, 16, 32)
+GROUPS = (1, 2, 3, 4)
 
 
 @dataclasses.dataclass
@@ -33,6 +35,7 @@ class Trial:
     processor_count: int
     ms: float
     dropped: int
+    groups: int = 1
 
     def as_dict(self):
         return dataclasses.asdict(self)
@@ -63,9 +66,10 @@ def time_batch(renderers: list[Renderer], ctx: Context, stream, frames: int, war
 
 
 def tune(renderers: list[Renderer], base: HairConfig, device: int, stream=None, tile_sizes=TILE_SIZES,
-         depth_bins=DEPTH_BINS, frames: int = 3, warmup: int = 2, budget_s: float = 120.0):
-    """Times every candidate on the batch; leaves the renderers on the
-    winner's context.  Returns (best HairConfig, its Context, trials)."""
+         depth_bins=DEPTH_BINS, frames: int = 3, warmup: int = 2, budget_s: float = 120.0, groups=GROUPS):
+    """Times every candidate on the batch, then the instance groups on the
+    winner; leaves the renderers on the winner's context, set to the best
+    group count.  Returns (best HairConfig, its Context, trials)."""
     trials: list[Trial] = []
     ctxs: list[Context] = []
     best = None
@@ -93,4 +97,15 @@ def tune(renderers: list[Renderer], base: HairConfig, device: int, stream=None, 
     for c in ctxs:
         if c is not ctx:
             c.close()
+    # then the number of instance groups that run side by side
+    best_g = (best[0], 1)
+    for g in groups:
+        if g == 1 or g > len(renderers):
+            continue
+        ctx.set_batch_groups(g)
+        ms, dropped = time_batch(renderers, ctx, stream or torch.cuda.current_stream(), frames, warmup)
+        trials.append(Trial(cfg.tile_size, cfg.tile_depth_bins, cfg.processor_count, ms, dropped, g))
+        if dropped == 0 and ms < best_g[0]:
+            best_g = (ms, g)
+    ctx.set_batch_groups(best_g[1])
     return cfg, ctx, trials

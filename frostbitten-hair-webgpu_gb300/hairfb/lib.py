@@ -97,6 +97,7 @@ SIGNATURES = {
     "hfb_frame": (I, [P, P]),
     "hfb_frame_batch": (I, [P, P, U32]),
     "hfb_frame_batch_profile": (I, [P, P, U32, P]),
+    "hfb_ctx_set_batch_groups": (I, [P, U32]),
 }
 
 _lock = threading.Lock()
@@ -170,6 +171,11 @@ class Context:
 
     def sync(self) -> None:
         self.call("hfb_sync")
+
+    def set_batch_groups(self, groups: int) -> None:
+        """hfb_frame_batch runs its instances in `groups` groups side by side."""
+        self.call("hfb_ctx_set_batch_groups", groups)
+        self.batch_groups = groups
 
     def counters(self) -> dict:
         c = HfbCounters()

@@ -49,6 +49,7 @@ class Renderer:
         self.fine = HairFinePass(self.ctx)
         self.frame_idx = 0
         self.uniforms = UN.pack_render_uniforms(inst.scene, inst.cfg)
+        self._inst = self._inst_uniforms = self._inst_rb = None  # cached HfbInstance (instance())
 
     def use_config(self, cfg: HairConfig, ctx: Context) -> None:
         """Re-targets the renderer to other pass constants (a context of
@@ -97,32 +98,38 @@ class Renderer:
 
     # ---- whole frames through hfb_frame / hfb_frame_batch ----
     def instance(self) -> HfbInstance:
-        """This frame's HfbInstance; the uniform bytes it points to stay
-        alive on the renderer until the next call."""
-        self._u_buf = ctypes.create_string_buffer(self.uniforms, len(self.uniforms))
-        su = self.sim_uniforms(self.frame_idx)
-        self._su_buf = ctypes.create_string_buffer(su, len(su))
-        h = self.hair
-        inst = HfbInstance()
-        inst.uniforms = ctypes.addressof(self._u_buf)
-        inst.simUniforms = ctypes.addressof(self._su_buf)
-        inst.hair = h.hair_data
-        inst.positions[0] = ptr(h.positions_0)
-        inst.positions[1] = ptr(h.positions_1)
-        inst.current = h._current
-        inst.strandsToRender = h.rendered_strand_count()
-        inst.positionsInitial = ptr(h.initial)
-        inst.tangents = ptr(h.tangents)
-        inst.segmentLengths = ptr(h.segment_lengths)
-        inst.densityVelocity = ptr(self.grids.density_velocity)
-        inst.densityGradWind = ptr(self.grids.density_grad_wind)
-        inst.sdf = ptr(self.sdf.texture)
-        inst.sdfDims = self.sdf.dims
-        inst.shading = ptr(h.shading)
-        inst.sceneDepth = ptr(self.scene_depth)
-        inst.shadingDepth = ptr(self.shading_depth)
-        inst.raster = self.rb.rb
-        return inst
+        """This frame's HfbInstance.  The uniform blocks it points to live on
+        the renderer: the render block as packed, the simulation block packed
+        once and patched per frame (frameIdx, wind strength)."""
+        i = self.inst
+        if self._inst is None or self._inst_uniforms is not self.uniforms or self._inst_rb is not self.rb:
+            self._u_buf = ctypes.create_string_buffer(self.uniforms, len(self.uniforms))
+            su = self.sim_uniforms(self.frame_idx)
+            self._su_buf = ctypes.create_string_buffer(su, len(su))
+            h = self.hair
+            inst = HfbInstance()
+            inst.uniforms = ctypes.addressof(self._u_buf)
+            inst.simUniforms = ctypes.addressof(self._su_buf)
+            inst.hair = h.hair_data
+            inst.positions[0] = ptr(h.positions_0)
+            inst.positions[1] = ptr(h.positions_1)
+            inst.positionsInitial = ptr(h.initial)
+            inst.tangents = ptr(h.tangents)
+            inst.segmentLengths = ptr(h.segment_lengths)
+            inst.densityVelocity = ptr(self.grids.density_velocity)
+            inst.densityGradWind = ptr(self.grids.density_grad_wind)
+            inst.sdf = ptr(self.sdf.texture)
+            inst.sdfDims = self.sdf.dims
+            inst.shading = ptr(h.shading)
+            inst.sceneDepth = ptr(self.scene_depth)
+            inst.shadingDepth = ptr(self.shading_depth)
+            inst.raster = self.rb.rb
+            self._inst, self._inst_uniforms, self._inst_rb = inst, self.uniforms, self.rb
+        else:
+            UN.patch_sim_uniforms(self._su_buf, self.frame_idx, i.wind_strength(self.frame_idx))
+        self._inst.current = self.hair._current
+        self._inst.strandsToRender = self.hair.rendered_strand_count()
+        return self._inst
 
     def after_native_frame(self, inst: HfbInstance) -> None:
         self.hair._current = inst.current
@@ -144,6 +151,7 @@ class BatchRenderer:
         self.ctx = renderers[0].ctx
         assert all(r.ctx is self.ctx for r in renderers), "a batch shares one context"
         self.renderers = renderers
+        self._arr = None
 
     def before_first_frame(self) -> None:
         for r in self.renderers:
@@ -151,7 +159,11 @@ class BatchRenderer:
 
     def frame(self) -> None:
         n = len(self.renderers)
-        arr = (HfbInstance * n)(*[r.instance() for r in self.renderers])
+        if self._arr is None or len(self._arr) != n:
+            self._arr = (HfbInstance * n)()
+        arr = self._arr
+        for k, r in enumerate(self.renderers):
+            arr[k] = r.instance()
         self.ctx.call("hfb_frame_batch", arr, n)
         for r, inst in zip(self.renderers, arr):
             r.after_native_frame(inst)

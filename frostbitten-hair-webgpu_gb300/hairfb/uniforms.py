@@ -284,5 +284,19 @@ def pack_sim_uniforms(sim: SimulationParams, model_matrix, sdf_bounds, grid_boun
     return bytes(w.buf)
 
 
+# Byte offsets of the two fields of SimulationUniforms that change from frame
+# to frame when the scene does not (simulationUniformsBuffer.ts:19-51): the
+# wind strength (.w of the wind vector) and frameIdx.
+SIM_WIND_STRENGTH_OFFSET = 156
+SIM_FRAME_IDX_OFFSET = 236
+
+
+def patch_sim_uniforms(block: bytearray, frame_idx: int, wind_strength: float) -> None:
+    """Rewrites frameIdx and the wind strength of a packed SimulationUniforms
+    block in place: the same bytes as pack_sim_uniforms for that frame."""
+    struct.pack_into("<f", block, SIM_WIND_STRENGTH_OFFSET, float(wind_strength))
+    struct.pack_into("<I", block, SIM_FRAME_IDX_OFFSET, int(math.floor(frame_idx)) & 0xFFFFFFFF)
+
+
 def read_f32(block: bytes, off: int, n: int = 1) -> np.ndarray:
     return np.frombuffer(block, dtype=np.float32, count=n, offset=off)

@@ -313,6 +313,13 @@ HFB_API int hfb_frame(HfbCtx* ctx, HfbInstance* instance);
  * instance's `current`.  n <= 1024. */
 HFB_API int hfb_frame_batch(HfbCtx* ctx, HfbInstance* instances, uint32_t n);
 
+/* No counterpart in the reference.  Splits the instances of the following
+ * hfb_frame_batch calls into `groups` (1..4, default 1) groups of about equal
+ * work, each running its passes on its own stream with 1/groups of the GPU's
+ * persistent CTAs, so that different passes of different groups share the
+ * SMs.  Results do not depend on it. */
+HFB_API int hfb_ctx_set_batch_groups(HfbCtx* ctx, uint32_t groups);
+
 /* hfb_frame_batch run as plain launches with a CUDA event between passes;
  * waits for the frame and writes the GPU time of each pass, in ms, to
  * passMs[0..7]: grid_pre, integrate, grid_post (with its grid clear),

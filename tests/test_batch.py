@@ -73,9 +73,10 @@ def test_frame_matches_pass_by_pass():
             _compare(_state(ref), _state(nat), ref, f)
 
 
-def _batch_vs_alone(insts, frames, profile_frame=None):
+def _batch_vs_alone(insts, frames, profile_frame=None, groups=1):
     alone = [Renderer(inst, 0) for inst in insts]
     ctx = Context(insts[0].cfg.to_c(), 0)
+    ctx.set_batch_groups(groups)
     batch = BatchRenderer([Renderer(inst, 0, ctx=ctx) for inst in insts])
     for r in alone:
         r.before_first_frame()
@@ -98,9 +99,9 @@ def _batch_vs_alone(insts, frames, profile_frame=None):
         for ra, rb in zip(alone, batch.renderers):
             _compare(_state(ra), _state(rb), ra, f)
             assert ra.hair._current == rb.hair._current
-    # one persistent launch per pass kind for the whole batch, every frame
+    # one persistent launch per pass kind and group, every frame
     per_frame = (ctx.counters()["launches"] - l0) / frames
-    assert per_frame <= 20, per_frame
+    assert per_frame <= 20 * groups, per_frame
     return ctx
 
 
@@ -108,14 +109,16 @@ def test_frame_batch_matches_each_instance_alone():
     _batch_vs_alone(_instances(), 4, profile_frame=1)
 
 
-def test_frame_batch_many_small_instances():
-    """12 instances of uneven sizes, several frames through the captured graph."""
+@pytest.mark.parametrize("groups", [1, 3])
+def test_frame_batch_many_small_instances(groups):
+    """12 instances of uneven sizes, several frames through the captured
+    graph, in one group or in three groups side by side."""
     rng = np.random.Generator(np.random.PCG64(11))
     common = dict(tile_size=16, depth_bins=8, slices=4, shading_points=8, grid_dims=32, iterations=4)
     insts = [synthetic.make_instance(rng, strands=int(rng.integers(200, 1500)), points=int(rng.choice([16, 24, 32])),
                                      width=int(rng.choice([128, 256])), height=int(rng.choice([128, 192])), **common)
              for _ in range(12)]
-    _batch_vs_alone(insts, 3)
+    _batch_vs_alone(insts, 3, groups=groups)
 
 
 def test_frame_batch_rejects_bad_instances():
@@ -133,4 +136,7 @@ def test_frame_batch_rejects_bad_instances():
     with pytest.raises(Exception, match="1024"):
         ctx.call("hfb_frame_batch", arr, 5000)
     assert ctx.lib.hfb_frame_batch(ctx.handle, None, 0) == 0
+    for bad in (0, 5):
+        with pytest.raises(Exception, match="groups"):
+            ctx.set_batch_groups(bad)
 

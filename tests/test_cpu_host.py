@@ -37,6 +37,22 @@ def test_uniform_block_sizes_and_offsets():
     assert struct.unpack_from("<I", s, UN.SIM_OFF["constraintIterations"])[0] == 7
 
 
+def test_patched_sim_uniforms_equal_a_full_pack():
+    """The per-frame patch of the cached SimulationUniforms block (frameIdx,
+    wind strength) gives the bytes of a full pack of that frame."""
+    rng = np.random.Generator(np.random.PCG64(2))
+    inst = synthetic.make_instance(rng, strands=50, points=8, width=64, height=64, wind_amplitude=1.0)
+
+    def pack(k):
+        return UN.pack_sim_uniforms(inst.sim, inst.scene.model_matrix, inst.scene.sdf_bounds,
+                                    inst.scene.grid_bounds, k, wind_dir=inst.wind_dir,
+                                    wind_strength=inst.wind_strength(k))
+    block = bytearray(pack(0))
+    for k in (1, 2, 17, 1000, 123456):
+        UN.patch_sim_uniforms(block, k, inst.wind_strength(k))
+        assert bytes(block) == pack(k), k
+
+
 def test_config_struct_matches_header():
     assert ctypes.sizeof(HfbConfig) == 64
     txt = open(HEADER).read()
