@@ -200,22 +200,26 @@ int hfb_buffer_clear(HfbCtx* c, void* dst, size_t bytes) {
   HFB_LAUNCH(c, cudaMemsetAsync(dst, 0, bytes, c->stream), "clear");
 }
 
-size_t hfb_raster_scratch_bytes(const HfbConfig* cfg, uint32_t width, uint32_t height) {
-  if (!cfg || width == 0 || height == 0) return 0;
-  uint32_t md = hfb::maxDrawnSegments(*cfg, width, height);
-  return std::max(hfb::tilesScratchLayout(nullptr, *cfg, width, height, md).bytes,
+size_t hfb_raster_scratch_bytes_for(const HfbConfig* cfg, uint32_t width, uint32_t height, uint32_t maxDrawn) {
+  if (!cfg || width == 0 || height == 0 || maxDrawn == 0) return 0;
+  return std::max(hfb::tilesScratchLayout(nullptr, *cfg, width, height, maxDrawn).bytes,
                   hfb::fineScratchLayout(nullptr, *cfg, width, height).bytes);
 }
 
-int hfb_raster_buffers_alloc(HfbCtx* c, uint32_t W, uint32_t H, HfbRasterBuffers* rb) {
+size_t hfb_raster_scratch_bytes(const HfbConfig* cfg, uint32_t width, uint32_t height) {
+  if (!cfg || width == 0 || height == 0) return 0;
+  return hfb_raster_scratch_bytes_for(cfg, width, height, hfb::maxDrawnSegments(*cfg, width, height));
+}
+
+int hfb_raster_buffers_alloc_sized(HfbCtx* c, uint32_t W, uint32_t H, uint32_t maxDrawn, HfbRasterBuffers* rb) {
   HFB_CHECK_CTX(c);
   HFB_REQUIRE(c, rb, "rb is NULL");
   HFB_REQUIRE(c, W > 0 && H > 0 && W <= 16384 && H <= 16384, "viewport must be 1..16384 px");
+  HFB_REQUIRE(c, maxDrawn >= 1 && maxDrawn < 0xFFFFFFF0u, "maxDrawnSegments must be in [1, 2^32 - 16)");
   memset(rb, 0, sizeof(*rb));
   const HfbConfig& cfg = c->cfg;
   size_t T = (size_t)hfb::divCeil(W, cfg.tileSize) * hfb::divCeil(H, cfg.tileSize);
-  uint64_t md = 1ull + (uint64_t)T * cfg.avgSegmentsPerTile;
-  HFB_REQUIRE(c, md < 0xFFFFFFF0ull, "maxDrawnHairSegments overflows u32");
+  const uint64_t md = maxDrawn;
   rb->width = W;
   rb->height = H;
   rb->maxDrawnSegments = (uint32_t)md;
@@ -234,7 +238,7 @@ int hfb_raster_buffers_alloc(HfbCtx* c, uint32_t W, uint32_t H, HfbRasterBuffers
       return fail(c, HFB_ERR_OUT_OF_MEMORY, "raster buffer allocation failed");
     }
   }
-  rb->scratchBytes = hfb_raster_scratch_bytes(&cfg, W, H);
+  rb->scratchBytes = hfb_raster_scratch_bytes_for(&cfg, W, H, (uint32_t)md);
   if (cudaMalloc(&rb->scratch, rb->scratchBytes) != cudaSuccess) {
     cudaGetLastError();
     hfb_raster_buffers_free(c, rb);
@@ -242,6 +246,15 @@ int hfb_raster_buffers_alloc(HfbCtx* c, uint32_t W, uint32_t H, HfbRasterBuffers
   }
   cudaMemsetAsync(rb->scratch, 0, rb->scratchBytes, c->stream);
   return hfb_clear_before_render(c, rb);
+}
+
+int hfb_raster_buffers_alloc(HfbCtx* c, uint32_t W, uint32_t H, HfbRasterBuffers* rb) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, W > 0 && H > 0 && W <= 16384 && H <= 16384, "viewport must be 1..16384 px");
+  const uint64_t T = (uint64_t)hfb::divCeil(W, c->cfg.tileSize) * hfb::divCeil(H, c->cfg.tileSize);
+  const uint64_t md = 1ull + T * c->cfg.avgSegmentsPerTile;
+  HFB_REQUIRE(c, md < 0xFFFFFFF0ull, "maxDrawnHairSegments overflows u32");
+  return hfb_raster_buffers_alloc_sized(c, W, H, (uint32_t)md, rb);
 }
 
 int hfb_raster_buffers_free(HfbCtx* c, HfbRasterBuffers* rb) {
@@ -262,10 +275,9 @@ static std::string checkRaster(const HfbCtx* c, const HfbRasterBuffers* rb) {
       !rb->tileList || !rb->rasterizerResult || !rb->scratch)
     return "a raster buffer is NULL";
   if (rb->width == 0 || rb->height == 0) return "raster buffers have an empty viewport";
-  if (rb->scratchBytes < hfb_raster_scratch_bytes(&c->cfg, rb->width, rb->height))
+  if (rb->maxDrawnSegments == 0) return "maxDrawnSegments is 0";
+  if (rb->scratchBytes < hfb_raster_scratch_bytes_for(&c->cfg, rb->width, rb->height, rb->maxDrawnSegments))
     return "raster scratch is too small";
-  if (rb->maxDrawnSegments != hfb::maxDrawnSegments(c->cfg, rb->width, rb->height))
-    return "maxDrawnSegments does not match the config";
   return "";
 }
 

@@ -83,12 +83,11 @@ extern "C" HFB_API int hfb_tiles_pass_noalloc(HfbCtx* c, const HfbUniforms* u, c
   if (h->strandsCount >= (1u << 24)) return fail(c, HFB_ERR_INVALID_ARGUMENT, "strandsCount must be < 2^24");
   if (!rb->tiles || !rb->tileSegments || !rb->segmentCountPerTile || rb->width == 0 || rb->height == 0)
     return fail(c, HFB_ERR_INVALID_ARGUMENT, "a raster buffer is NULL or the viewport is empty");
-  if (rb->maxDrawnSegments != hfb::maxDrawnSegments(c->cfg, rb->width, rb->height))
-    return fail(c, HFB_ERR_INVALID_ARGUMENT, "maxDrawnSegments does not match the config");
+  if (rb->maxDrawnSegments == 0) return fail(c, HFB_ERR_INVALID_ARGUMENT, "maxDrawnSegments is 0");
   if (!(u->viewport.x == (float)rb->width) || !(u->viewport.y == (float)rb->height) ||
       u->maxDrawnHairSegments != rb->maxDrawnSegments)
     return fail(c, HFB_ERR_INVALID_ARGUMENT, "Uniforms.viewport / maxDrawnHairSegments do not match the raster buffers");
-  const size_t need = hfb_raster_scratch_bytes(&c->cfg, rb->width, rb->height);
+  const size_t need = hfb_raster_scratch_bytes_for(&c->cfg, rb->width, rb->height, rb->maxDrawnSegments);
   if (need > HFB_NOALLOC_SCRATCH_BYTES)
     return fail(c, HFB_ERR_INVALID_ARGUMENT,
                 "the tiles pass needs " + std::to_string(need) + " bytes of working memory for " +

@@ -83,6 +83,8 @@ SIGNATURES = {
     "hfb_buffer_download": (I, [P, P, P, SZ]),
     "hfb_buffer_clear": (I, [P, P, SZ]),
     "hfb_raster_scratch_bytes": (SZ, [P, U32, U32]),
+    "hfb_raster_scratch_bytes_for": (SZ, [P, U32, U32, U32]),
+    "hfb_raster_buffers_alloc_sized": (I, [P, U32, U32, U32, P]),
     "hfb_raster_buffers_alloc": (I, [P, U32, U32, P]),
     "hfb_raster_buffers_free": (I, [P, P]),
     "hfb_grid_pre_sim": (I, [P, P, P, P, P, U32]),

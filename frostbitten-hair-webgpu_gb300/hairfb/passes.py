@@ -168,10 +168,15 @@ class HairShadingPass:
 class RasterBuffers:
     """The viewport-sized buffers the three raster passes share (PassCtx)."""
 
-    def __init__(self, ctx: Context, width: int, height: int):
+    def __init__(self, ctx: Context, width: int, height: int, max_drawn: int | None = None):
+        """max_drawn: the segment pool's size in records (None: the config's
+        1 + tiles * avgSegmentsPerTile)."""
         self.ctx = ctx
         self.rb = HfbRasterBuffers()
-        ctx.call("hfb_raster_buffers_alloc", width, height, byref(self.rb))
+        if max_drawn is None:
+            ctx.call("hfb_raster_buffers_alloc", width, height, byref(self.rb))
+        else:
+            ctx.call("hfb_raster_buffers_alloc_sized", width, height, int(max_drawn), byref(self.rb))
         self.width, self.height = width, height
 
     @property

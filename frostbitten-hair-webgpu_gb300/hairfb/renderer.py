@@ -28,14 +28,18 @@ from .passes import (GridPostSimPass, GridPreSimPass, HairFinePass, HairObject, 
 class Renderer:
     """One hair instance rendered frame by frame through libhairfb.so."""
 
-    def __init__(self, inst: synthetic.Instance, device: int = -1, ctx: Context | None = None):
+    def __init__(self, inst: synthetic.Instance, device: int = -1, ctx: Context | None = None,
+                 max_drawn: int | None = None):
+        """max_drawn: this instance's segment pool in records (None: the
+        config's 1 + tiles * avgSegmentsPerTile)."""
         self.inst = inst
         self.cfg: HairConfig = inst.cfg
         self.ctx = ctx or Context(inst.cfg.to_c(), device)
+        self.max_drawn = max_drawn
         self.hair = HairObject(inst.hair, inst.cfg.shading_points)
         self.sdf = SdfCollider(inst.sdf)
         self.grids = PhysicsGrids(inst.cfg.grid_dims)
-        self.rb = RasterBuffers(self.ctx, inst.width, inst.height)
+        self.rb = RasterBuffers(self.ctx, inst.width, inst.height, max_drawn)
         self.scene_depth = torch.as_tensor(inst.scene_depth).cuda()
         # depth buffer with hair drawn, for the shading attenuation; the
         # hardware hair pass is outside the path, the scene depth stands in
@@ -48,7 +52,7 @@ class Renderer:
         self.sort = HairTileSortPass(self.ctx)
         self.fine = HairFinePass(self.ctx)
         self.frame_idx = 0
-        self.uniforms = UN.pack_render_uniforms(inst.scene, inst.cfg)
+        self.uniforms = UN.pack_render_uniforms(inst.scene, inst.cfg, max_drawn)
         self._inst = self._inst_uniforms = self._inst_rb = None  # cached HfbInstance (instance())
 
     def use_config(self, cfg: HairConfig, ctx: Context) -> None:
@@ -59,10 +63,10 @@ class Renderer:
         old = self.rb
         self.cfg = cfg
         self.ctx = ctx
-        self.rb = RasterBuffers(ctx, self.inst.width, self.inst.height)
+        self.rb = RasterBuffers(ctx, self.inst.width, self.inst.height, self.max_drawn)
         for p in (self.grid_pre, self.integrate, self.grid_post, self.shading, self.tiles, self.sort, self.fine):
             p.ctx = ctx
-        self.uniforms = UN.pack_render_uniforms(self.inst.scene, cfg)
+        self.uniforms = UN.pack_render_uniforms(self.inst.scene, cfg, self.max_drawn)
         old.close()
 
     def sim_uniforms(self, frame_idx: int) -> bytes:

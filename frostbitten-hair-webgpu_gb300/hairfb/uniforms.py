@@ -168,7 +168,7 @@ def shadow_source_matrices(p: SceneParams):
     return pos, view, proj
 
 
-def pack_render_uniforms(p: SceneParams, cfg: HairConfig) -> bytes:
+def pack_render_uniforms(p: SceneParams, cfg: HairConfig, max_drawn: int | None = None) -> bytes:
     """RenderUniformsBuffer.update(), renderUniformsBuffer.ts:205-288."""
     view = p.camera.view()
     proj = p.camera.proj(p.width, p.height)
@@ -234,7 +234,7 @@ def pack_render_uniforms(p: SceneParams, cfg: HairConfig) -> bytes:
     # misc
     w.f32(p.fiber_radius)
     w.f32(0.0)
-    w.u32(cfg.max_drawn_segments(p.width, p.height))
+    w.u32(cfg.max_drawn_segments(p.width, p.height) if max_drawn is None else max_drawn)
     w.u32(p.display_mode | (p.display_mode_extra << 8))
     # background (CONFIG.background)
     for v in (*_col(22, 162, 188), 5.0, *_col(14, 103, 120), 0.5):

@@ -198,11 +198,22 @@ HFB_API int hfb_buffer_upload(HfbCtx* ctx, void* dst, const void* src, size_t by
 HFB_API int hfb_buffer_download(HfbCtx* ctx, void* dst, const void* src, size_t bytes);
 HFB_API int hfb_buffer_clear(HfbCtx* ctx, void* dst, size_t bytes);
 
-/* Bytes of tiles-pass working memory for a viewport. */
+/* Bytes of tiles-pass working memory for a viewport (segment pool sized by
+ * the config: 1 + tiles * avgSegmentsPerTile), or for a given pool size. */
 HFB_API size_t hfb_raster_scratch_bytes(const HfbConfig* cfg, uint32_t width, uint32_t height);
+HFB_API size_t hfb_raster_scratch_bytes_for(const HfbConfig* cfg, uint32_t width, uint32_t height,
+                                            uint32_t maxDrawnSegments);
 /* onViewportResize of HairTilesPass / HairTileSortPass / HairFinePass:
- * allocates every HfbRasterBuffers member for width x height. */
+ * allocates every HfbRasterBuffers member for width x height, with the
+ * segment pool the reference sizes (getLengthOfHairTileSegmentsBuffer,
+ * hairTileSegmentsBuffer.ts:81-87). */
 HFB_API int hfb_raster_buffers_alloc(HfbCtx* ctx, uint32_t width, uint32_t height, HfbRasterBuffers* out);
+/* No counterpart in the reference: the same with a segment pool of
+ * maxDrawnSegments records, for hosts that size each instance's pool (a
+ * server mixing dense small viewports with sparse large ones).  The frame's
+ * Uniforms.maxDrawnHairSegments must carry the same number. */
+HFB_API int hfb_raster_buffers_alloc_sized(HfbCtx* ctx, uint32_t width, uint32_t height, uint32_t maxDrawnSegments,
+                                           HfbRasterBuffers* out);
 HFB_API int hfb_raster_buffers_free(HfbCtx* ctx, HfbRasterBuffers* rb);
 
 /* ---- simulation passes (src/renderer.ts:212-240 order) --------------------- */
