@@ -490,10 +490,9 @@ def run_served(frames_per_session, device, groups=1, seed=0):
 
 def report_batched_peer(res, dist):
     """Non-zero ranks join the max-over-ranks reduction of report_batched."""
-    import torch
-    t = torch.tensor([sum(res["step_ms"]) / 1000.0, sum(res["plain_round_ms"]) / 1000.0,
-                      sum(res["e2e_ms"]) / 1000.0], device="cuda", dtype=torch.float64)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    from hairfb import replicas
+    replicas.max_over_ranks([sum(res["step_ms"]) / 1000.0, sum(res["plain_round_ms"]) / 1000.0,
+                             sum(res["e2e_ms"]) / 1000.0], dist, "cuda")
 
 
 def cpu_batched(insts, seconds):
@@ -517,14 +516,11 @@ def report_batched(args, res, world, dist):
     step_s = sum(res["step_ms"]) / 1000.0
     plain_s = sum(res["plain_round_ms"]) / 1000.0
     e2e_s = sum(res["e2e_ms"]) / 1000.0
-    if dist:
-        import torch
-        t = torch.tensor([step_s, plain_s, e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        step_s, plain_s, e2e_s = float(t[0]), float(t[1]), float(t[2])
+    from hairfb import replicas
+    step_s, plain_s, e2e_s = replicas.max_over_ranks([step_s, plain_s, e2e_s], dist, "cuda")
     n = res["n"]
-    fps = world * n * len(res["step_ms"]) / step_s
-    plain_fps = world * n * len(res["plain_round_ms"]) / plain_s
+    fps = replicas.job_throughput(n * len(res["step_ms"]), world, step_s)
+    plain_fps = replicas.job_throughput(n * len(res["plain_round_ms"]), world, plain_s)
     cfg = res["cfg"]
     insts = [dataclasses.replace(i, cfg=cfg) for i in res["insts"]]
     alg = {}
@@ -667,12 +663,10 @@ def main():
         dev = int(os.environ.get("LOCAL_RANK", "0"))
         torch.cuda.set_device(dev)
         sv = run_served(600, dev, groups=4, seed=rank)
-        if dist:
-            t = torch.tensor([sv["wall_s"]], device="cuda", dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            sv["wall_s"] = float(t[0])
+        from hairfb import replicas
+        sv["wall_s"] = replicas.max_over_ranks([sv["wall_s"]], dist, "cuda")[0]
         if rank == 0:
-            fps = world * sv["frames"] / sv["wall_s"]
+            fps = replicas.job_throughput(sv["frames"], world, sv["wall_s"])
             line = {"metric": "frames/s", "value": fps, "unit": "frames/s", "n_gpus": world, "steps": sv["ticks"],
                     "warmup": 0, "ms_per_step": 1000.0 * sv["wall_s"] / max(1, sv["ticks"]),
                     "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -701,11 +695,9 @@ def main():
     res = run_ours(args, rank, world, dist)
     total = res["total_s"]
     e2e_total = sum(res["e2e_ms"]) / 1000.0
+    from hairfb import replicas
+    total, e2e_total = replicas.max_over_ranks([total, e2e_total], dist, "cuda")
     if dist:
-        import torch
-        t = torch.tensor([total, e2e_total], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total, e2e_total = float(t[0]), float(t[1])
         dist.barrier()
     if rank != 0:
         if dist:
