@@ -538,7 +538,8 @@ def report_batched(args, res, world, dist):
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
-        traffic = json.load(open(tp)).get(f"batched64:{dominant}")
+        # measured at one pass config; reported only when the tuner chose it
+        traffic = json.load(open(tp)).get(f"batched64:ts{cfg.tile_size}_b{cfg.tile_depth_bins}:{dominant}")
     srt = sorted(res["step_ms"])
     q = lambda v, x: v[min(len(v) - 1, int(round(x * (len(v) - 1))))]  # noqa: E731
     psrt = sorted(res["plain_frame_ms"])
