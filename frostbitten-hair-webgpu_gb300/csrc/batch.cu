@@ -166,7 +166,7 @@ uint32_t batchBlocks(const HfbConfig& cfg, BatchKind k, const BatchInst& I) {
       return v < 1u ? 1u : (v > 256u ? 256u : v);
     }
     case BK_FINALIZE: return divCeil(TB, 8u);
-    case BK_LARGE: return 4u;
+    case BK_LARGE: return 16u;
     case BK_SORT: return 1u;
     case BK_SCHEDULE: return 1u;
     case BK_SHADING: return divCeil(I.S * cfg.shadingPoints, 128u);

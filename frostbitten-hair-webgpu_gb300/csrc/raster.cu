@@ -163,8 +163,8 @@ __device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* war
 // own thread, tile by tile (rasterSegmentSerial).
 // ---------------------------------------------------------------------------
 constexpr uint32_t TR_SEGS = TILES_RASTER_SEGS;  // segments (and threads) per block
-constexpr uint32_t TR_SLOTS = 1024; // (segment, tile) accumulators per block
-constexpr uint32_t TR_CHUNK = 4096; // pairs per A1 / A2 round
+constexpr uint32_t TR_SLOTS = 768;  // (segment, tile) accumulators per block
+constexpr uint32_t TR_CHUNK = 2048; // pairs per A1 / A2 round
 
 struct TrShared {
   float ox[4][TR_SEGS], oy[4][TR_SEGS], ex[4][TR_SEGS], ey[4][TR_SEGS];  // edge tests (insideQuad order)
@@ -467,7 +467,7 @@ __device__ __forceinline__ void tilesRasterBody(const HfbUniforms& U, uint32_t P
   __syncthreads();  // the block's staging is reused by its next segments
 }
 
-__global__ void __launch_bounds__(TR_SEGS)
+__global__ void __launch_bounds__(TR_SEGS, 6)
 tilesRasterKernel(const HfbUniforms U, uint32_t P, uint32_t nStrands, uint32_t TS, uint32_t B,
                   uint32_t threshold, float4 bsphere, const float4* __restrict__ pos,
                   const float4* __restrict__ tan, const float* __restrict__ depth, uint4* __restrict__ tiles,
@@ -1855,7 +1855,7 @@ cudaError_t launchFineT(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, c
     const TilesScratch ts = tilesScratchLayout(I.scratch, cfg, I.W, I.H, I.maxDrawn); \
     (void)ts;
 
-__global__ void __launch_bounds__(TR_SEGS) tilesRasterBatch(BatchView b, HfbConfig cfgParam,
+__global__ void __launch_bounds__(TR_SEGS, 6) tilesRasterBatch(BatchView b, HfbConfig cfgParam,
                                                              DeviceCounters* __restrict__ counters) {
   const HfbConfig cfg = cfgParam;
   __shared__ TrShared sh;
@@ -2087,7 +2087,7 @@ cudaError_t launchBatchTiles(HfbCtx* c, const BatchView& b) {
     g[BK_SCAN_SUMS] = c->smCount;
     g[BK_SCATTER] = c->smCount * 8u;
     g[BK_FINALIZE] = c->smCount * 8u;
-    g[BK_LARGE] = c->smCount;
+    g[BK_LARGE] = c->smCount * 2u;
     e = cudaFuncSetAttribute(largeBinsBatch, cudaFuncAttributeMaxDynamicSharedMemorySize, LARGE_SMEM_KEYS * 4);
     if (e != cudaSuccess) return e;
   }

@@ -242,7 +242,7 @@ def stress(seed: int = 0, **kw) -> Instance:
     rng = np.random.Generator(np.random.PCG64(seed))
     args = dict(strands=200000, points=32, width=3840, height=2160, depth_bins=32, slices=8,
                 shading_points=32, iterations=8, sdf_dims=128, grid_dims=64, ponytail=0.6,
-                ellipsoid=True, avg_segments_per_tile=384)
+                ellipsoid=True, avg_segments_per_tile=1024)
     args.update(kw)
     return make_instance(rng, **args)
 
