@@ -454,7 +454,7 @@ def run_batched(args, rank, world, dist):
     out = dict(served=served, step_ms=step_ms, lat_ms=lat_ms, plain_round_ms=plain_round_ms, plain_frame_ms=plain_frame_ms,
                pass_ms=pass_ms, K=K, e2e_ms=e2e_ms, h2d=h2d, d2h=d2h, clocks=clk.summary(), insts=insts,
                cfg=cfg, trials=[t.as_dict() for t in trials], tune_s=t_tune, launches=launches,
-               groups=getattr(ctx, "batch_groups", 1),
+               groups=getattr(ctx, "batch_groups", 1), pipelined=getattr(ctx, "batch_pipeline", False),
                dropped=dropped, n=n)
     ctx.close()
     return out
@@ -562,7 +562,7 @@ def report_batched(args, res, world, dist):
                    "frames_per_step": n, "tuned": {"tile_size": cfg.tile_size, "depth_bins": cfg.tile_depth_bins,
                                                    "slices": cfg.slices_per_pixel,
                                                    "avg_segments_per_tile": cfg.avg_segments_per_tile,
-                                                   "groups": res["groups"],
+                                                   "groups": res["groups"], "pipelined": res["pipelined"],
                                                    "tune_s": round(res["tune_s"], 1)},
                    "autotune_trials": [{k: (round(v, 3) if isinstance(v, float) else v) for k, v in t.items()}
                                        for t in res["trials"]],

@@ -184,11 +184,12 @@ cudaError_t launchBatchClear(HfbCtx* c, const BatchView& b, BatchKind k) {
   return cudaGetLastError();
 }
 
-// The frame's launch sequence (renderer.ts:171-295 order).  With `ev`, an
-// event is recorded before the first pass and after each of the
-// HFB_FRAME_PASSES passes (grid_pre, integrate, grid_post with its grid
-// clear, clear, tiles, sort, fine, shading).
-static cudaError_t batchSequence(HfbCtx* c, const BatchView& b, cudaEvent_t* ev = nullptr) {
+// The frame's launch sequence (renderer.ts:171-295 order): the simulation
+// passes, then the raster passes.  With `ev`, an event is recorded before the
+// first pass and after each of the HFB_FRAME_PASSES passes (grid_pre,
+// integrate, grid_post with its grid clear, clear, tiles, sort, fine,
+// shading).
+static cudaError_t simSequence(HfbCtx* c, const BatchView& b, cudaEvent_t* ev = nullptr) {
   auto mark = [&](int i) { return ev ? cudaEventRecord(ev[i], c->stream) : cudaSuccess; };
   cudaError_t e = mark(0);
   if (e == cudaSuccess) e = launchBatchSim(c, b, BK_GRID_PRE);
@@ -198,7 +199,12 @@ static cudaError_t batchSequence(HfbCtx* c, const BatchView& b, cudaEvent_t* ev 
   if (e == cudaSuccess) e = launchBatchClear(c, b, BK_CLEAR_GRID);
   if (e == cudaSuccess) e = launchBatchSim(c, b, BK_GRID_POST);
   if (e == cudaSuccess) e = mark(3);
-  if (e == cudaSuccess) e = launchBatchClear(c, b, BK_CLEAR_FRAME);
+  return e;
+}
+
+static cudaError_t rasterSequence(HfbCtx* c, const BatchView& b, cudaEvent_t* ev = nullptr) {
+  auto mark = [&](int i) { return ev ? cudaEventRecord(ev[i], c->stream) : cudaSuccess; };
+  cudaError_t e = launchBatchClear(c, b, BK_CLEAR_FRAME);
   if (e == cudaSuccess) e = mark(4);
   if (e == cudaSuccess) e = launchBatchTiles(c, b);
   if (e == cudaSuccess) e = mark(5);
@@ -208,6 +214,12 @@ static cudaError_t batchSequence(HfbCtx* c, const BatchView& b, cudaEvent_t* ev 
   if (e == cudaSuccess) e = mark(7);
   if (e == cudaSuccess) e = launchBatchShading(c, b);
   if (e == cudaSuccess) e = mark(8);
+  return e;
+}
+
+static cudaError_t batchSequence(HfbCtx* c, const BatchView& b, cudaEvent_t* ev = nullptr) {
+  cudaError_t e = simSequence(c, b, ev);
+  if (e == cudaSuccess) e = rasterSequence(c, b, ev);
   return e;
 }
 
@@ -291,11 +303,77 @@ static cudaError_t groupsSequence(HfbCtx* c, uint32_t NG) {
   return e;
 }
 
+// Pipelined batches: the device table slots after the groups' tables.
+static char* pipeTable(HfbCtx* c, uint32_t slot) {
+  return (char*)c->batchDev + (size_t)(BATCH_GROUPS_MAX + slot) * BATCH_BYTES;
+}
+
+static cudaError_t ensurePipe(HfbCtx* c) {
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < 2 && e == cudaSuccess; i++) {
+    if (!c->pipeStream[i]) e = cudaStreamCreateWithFlags(&c->pipeStream[i], cudaStreamNonBlocking);
+    if (e == cudaSuccess && !c->pipeSimDone[i]) e = cudaEventCreateWithFlags(&c->pipeSimDone[i], cudaEventDisableTiming);
+    if (e == cudaSuccess && !c->pipeRasterDone[i])
+      e = cudaEventCreateWithFlags(&c->pipeRasterDone[i], cudaEventDisableTiming);
+    if (e == cudaSuccess && !c->pipeCaller[i]) e = cudaEventCreateWithFlags(&c->pipeCaller[i], cudaEventDisableTiming);
+  }
+  return e;
+}
+
+static void pipeGraphsRelease(HfbCtx* c) {
+  for (int i = 0; i < 2; i++)
+    for (int j = 0; j < 2; j++) {
+      if (c->pipeGraph[i][j]) cudaGraphExecDestroy(c->pipeGraph[i][j]);
+      c->pipeGraph[i][j] = nullptr;
+    }
+}
+
+// One half of a pipelined frame (part 0: simulation, 1: raster) on its
+// stream: plain launches for the first use of each table slot (they also set
+// the kernels' attributes), then the slot's captured graph.
+static cudaError_t pipePart(HfbCtx* c, uint32_t part, uint32_t slot) {
+  const cudaStream_t caller = c->stream;
+  c->stream = c->pipeStream[part];
+  const BatchView b = batchView(pipeTable(c, slot));
+  auto seq = [&]() { return part == 0u ? simSequence(c, b) : rasterSequence(c, b); };
+  cudaError_t e = cudaSuccess;
+#ifdef HFB_DEVICE_CHECKS
+  const bool plain = true;  // the checked build waits after every launch: no capture
+#else
+  const bool plain = c->pipeCalls <= 2u;
+#endif
+  if (plain) {
+    e = seq();
+  } else {
+    cudaGraphExec_t& ge = c->pipeGraph[slot][part];
+    if (!ge) {
+      cudaGraph_t gr = nullptr;
+      e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess) {
+        const uint64_t l0 = c->launches;
+        cudaError_t el = seq();
+        c->pipeGraphLaunches[slot][part] = c->launches - l0;
+        c->launches = l0;
+        e = cudaStreamEndCapture(c->stream, &gr);
+        if (el != cudaSuccess) e = el;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, gr, 0);
+        if (gr) cudaGraphDestroy(gr);
+      }
+    }
+    if (e == cudaSuccess) {
+      e = cudaGraphLaunch(ge, c->stream);
+      c->launches += c->pipeGraphLaunches[slot][part];
+    }
+  }
+  c->stream = caller;
+  return e;
+}
+
 // Fills the staging copy (one device table per group), uploads it and runs
 // the frame for n validated instances.
 cudaError_t frameBatch(HfbCtx* c, HfbInstance* insts, uint32_t n, float* passMs) {
   cudaError_t e = cudaSuccess;
-  constexpr size_t TABLES = (size_t)BATCH_GROUPS_MAX * BATCH_BYTES;
+  constexpr size_t TABLES = (size_t)(BATCH_GROUPS_MAX + 2) * BATCH_BYTES;  // groups + two pipeline slots
   if (!c->batchDev) {
     e = cudaMalloc(&c->batchDev, TABLES);
     for (int k = 0; k < 2 && e == cudaSuccess; k++) {
@@ -308,7 +386,8 @@ cudaError_t frameBatch(HfbCtx* c, HfbInstance* insts, uint32_t n, float* passMs)
   }
   // groups: largest instance first, each to the group with the least work so
   // far (the profiling run keeps one group: its passes are timed one by one)
-  uint32_t NG = passMs ? 1u : (c->batchGroups < n ? c->batchGroups : n);
+  const bool pipe = c->batchPipeline && !passMs;
+  uint32_t NG = (passMs || pipe) ? 1u : (c->batchGroups < n ? c->batchGroups : n);
   if (NG < 1u) NG = 1u;
   uint32_t* group = new uint32_t[n];
   {
@@ -345,12 +424,13 @@ cudaError_t frameBatch(HfbCtx* c, HfbInstance* insts, uint32_t n, float* passMs)
   if (smem > c->simBatchSmem) {
     c->simBatchSmem = smem;
     c->batchGrid[BK_INTEGRATE] = 0;
-    if (c->batchGraph) {
-      e = cudaStreamSynchronize(c->stream);
-      if (e != cudaSuccess) return e;
-      cudaGraphExecDestroy(c->batchGraph);
-      c->batchGraph = nullptr;
-    }
+    e = cudaStreamSynchronize(c->stream);
+    for (int i = 0; i < 2 && e == cudaSuccess; i++)
+      if (c->pipeStream[i]) e = cudaStreamSynchronize(c->pipeStream[i]);
+    if (e != cudaSuccess) return e;
+    if (c->batchGraph) cudaGraphExecDestroy(c->batchGraph);
+    c->batchGraph = nullptr;
+    pipeGraphsRelease(c);
   }
   for (uint32_t g = 0; g < NG && e == cudaSuccess; g++) {
     char* h = (char*)c->batchHost[k] + (size_t)g * BATCH_BYTES;
@@ -368,10 +448,39 @@ cudaError_t frameBatch(HfbCtx* c, HfbInstance* insts, uint32_t n, float* passMs)
       }
       row[ng[g]] = acc;
     }
+    if (pipe) break;  // uploaded on the simulation stream below
     const size_t bytes = BATCH_INSTS_OFF + (size_t)ng[g] * sizeof(BatchInst);
     e = cudaMemcpyAsync((char*)c->batchDev + (size_t)g * BATCH_BYTES, h, bytes, cudaMemcpyHostToDevice, c->stream);
   }
-  if (e == cudaSuccess) e = cudaEventRecord(c->batchCopied[k], c->stream);
+  if (e != cudaSuccess) return e;
+  if (pipe) {
+    // Table slot k.  The frame's simulation waits for the caller's stream as
+    // of the previous call (or this one, the first time) and for the raster
+    // passes of the frame before the previous one, which read the table slot
+    // and the position buffer this simulation writes; it runs beside the
+    // previous frame's raster passes.  The raster passes wait for this
+    // simulation and, on their own stream, for the previous raster passes;
+    // the caller's stream waits for them.
+    e = ensurePipe(c);
+    if (e == cudaSuccess) e = cudaEventRecord(c->pipeCaller[k], c->stream);
+    const cudaStream_t S = c->pipeStream[0], R = c->pipeStream[1];
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(S, c->pipeCaller[c->pipeCalls == 0 ? k : 1u - k], 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(S, c->pipeRasterDone[k], 0);
+    const size_t bytes = BATCH_INSTS_OFF + (size_t)n * sizeof(BatchInst);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(pipeTable(c, k), c->batchHost[k], bytes, cudaMemcpyHostToDevice, S);
+    if (e == cudaSuccess) e = cudaEventRecord(c->batchCopied[k], S);
+    c->pipeCalls++;
+    if (e == cudaSuccess) e = pipePart(c, 0, k);
+    if (e == cudaSuccess) e = cudaEventRecord(c->pipeSimDone[k], S);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(R, c->pipeSimDone[k], 0);
+    if (e == cudaSuccess) e = pipePart(c, 1, k);
+    if (e == cudaSuccess) e = cudaEventRecord(c->pipeRasterDone[k], R);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->pipeRasterDone[k], 0);
+    if (e != cudaSuccess) return e;
+    for (uint32_t i = 0; i < n; i++) insts[i].current ^= 1u;
+    return cudaGetLastError();
+  }
+  e = cudaEventRecord(c->batchCopied[k], c->stream);
   if (e != cudaSuccess) return e;
 
   if (passMs) {  // one group, plain launches with an event between passes
@@ -433,6 +542,15 @@ cudaError_t frameBatch(HfbCtx* c, HfbInstance* insts, uint32_t n, float* passMs)
 }
 
 void frameBatchRelease(HfbCtx* c) {
+  pipeGraphsRelease(c);
+  for (int i = 0; i < 2; i++) {
+    if (c->pipeStream[i]) cudaStreamDestroy(c->pipeStream[i]);
+    for (cudaEvent_t* ev : {&c->pipeSimDone[i], &c->pipeRasterDone[i], &c->pipeCaller[i]}) {
+      if (*ev) cudaEventDestroy(*ev);
+      *ev = nullptr;
+    }
+    c->pipeStream[i] = nullptr;
+  }
   for (uint32_t g = 0; g < BATCH_GROUPS_MAX; g++) {
     if (c->batchJoin[g]) cudaEventDestroy(c->batchJoin[g]);
     if (c->batchStreams[g]) cudaStreamDestroy(c->batchStreams[g]);

@@ -439,6 +439,18 @@ int hfb_ctx_set_batch_groups(HfbCtx* c, uint32_t groups) {
   return HFB_OK;
 }
 
+int hfb_ctx_set_batch_pipeline(HfbCtx* c, uint32_t on) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, on <= 1u, "pipeline must be 0 or 1");
+  if ((on != 0u) != c->batchPipeline) {  // a clean start: nothing of the other mode in flight
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cudaFail(c, e, "ctx_set_batch_pipeline");
+    c->batchPipeline = on != 0u;
+    c->pipeCalls = 0;
+  }
+  return HFB_OK;
+}
+
 int hfb_frame_batch_profile(HfbCtx* c, HfbInstance* insts, uint32_t n, float* passMs) {
   HFB_CHECK_CTX(c);
   HFB_REQUIRE(c, insts && n > 0 && passMs, "NULL argument or empty batch");

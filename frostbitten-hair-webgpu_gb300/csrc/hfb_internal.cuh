@@ -43,6 +43,16 @@ struct HfbCtx {
   cudaStream_t batchStreams[4] = {};
   cudaEvent_t batchFork = nullptr;
   cudaEvent_t batchJoin[4] = {};
+  // pipelined batches (hfb_ctx_set_batch_pipeline): the simulation passes on
+  // one stream, the raster passes on another, two device tables in turn
+  bool batchPipeline = false;
+  uint64_t pipeCalls = 0;
+  cudaStream_t pipeStream[2] = {};         // [0] simulation, [1] raster
+  cudaEvent_t pipeSimDone[2] = {};         // per table slot
+  cudaEvent_t pipeRasterDone[2] = {};
+  cudaEvent_t pipeCaller[2] = {};          // the caller's stream at each call
+  cudaGraphExec_t pipeGraph[2][2] = {};    // [slot][simulation / raster]
+  uint64_t pipeGraphLaunches[2][2] = {};
   // self-checking build: the device CheckState (hfb_check.cuh), else NULL
   void* checkDev = nullptr;
 };

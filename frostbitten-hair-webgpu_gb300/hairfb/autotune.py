@@ -36,7 +36,7 @@ class Trial:
     processor_count: int
     ms: float
     dropped: int
-    groups: int = 1
+    groups: int = 1  # 0: the pipelined frame
 
     def as_dict(self):
         return dataclasses.asdict(self)
@@ -115,4 +115,10 @@ def tune(renderers: list[Renderer], base: HairConfig, device: int, stream=None, 
         if dropped == 0 and ms < best_g[0] * (1.0 - MIN_GAIN):
             best_g = (ms, g)
     ctx.set_batch_groups(best_g[1])
+    # then the pipelined frame (the simulation beside the previous raster passes)
+    ctx.set_batch_pipeline(True)
+    ms, dropped = time_batch(renderers, ctx, stream or torch.cuda.current_stream(), frames, warmup)
+    trials.append(Trial(cfg.tile_size, cfg.tile_depth_bins, cfg.processor_count, ms, dropped, 0))
+    if not (dropped == 0 and ms < best_g[0] * (1.0 - MIN_GAIN)):
+        ctx.set_batch_pipeline(False)
     return cfg, ctx, trials

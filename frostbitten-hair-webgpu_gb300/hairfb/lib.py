@@ -100,6 +100,7 @@ SIGNATURES = {
     "hfb_frame_batch": (I, [P, P, U32]),
     "hfb_frame_batch_profile": (I, [P, P, U32, P]),
     "hfb_ctx_set_batch_groups": (I, [P, U32]),
+    "hfb_ctx_set_batch_pipeline": (I, [P, U32]),
 }
 
 _lock = threading.Lock()
@@ -178,6 +179,12 @@ class Context:
         """hfb_frame_batch runs its instances in `groups` groups side by side."""
         self.call("hfb_ctx_set_batch_groups", groups)
         self.batch_groups = groups
+
+    def set_batch_pipeline(self, on: bool) -> None:
+        """hfb_frame_batch overlaps a frame's simulation with the previous
+        frame's raster passes (see hfb_ctx_set_batch_pipeline)."""
+        self.call("hfb_ctx_set_batch_pipeline", 1 if on else 0)
+        self.batch_pipeline = bool(on)
 
     def counters(self) -> dict:
         c = HfbCounters()

@@ -331,6 +331,17 @@ HFB_API int hfb_frame_batch(HfbCtx* ctx, HfbInstance* instances, uint32_t n);
  * SMs.  Results do not depend on it. */
 HFB_API int hfb_ctx_set_batch_groups(HfbCtx* ctx, uint32_t groups);
 
+/* No counterpart in the reference.  With on = 1, hfb_frame_batch runs the
+ * simulation passes and the raster passes of a frame on two internal streams
+ * with two device tables in turn, so that a frame's simulation runs beside
+ * the previous frame's raster passes (one group; groups are ignored).  A
+ * frame's results are ordered on the context's stream as before, but its
+ * simulation does not wait for work the caller enqueued on that stream after
+ * the previous hfb_frame_batch call: inputs such a frame reads (the instances'
+ * device buffers) must be ready when the call is made.  Switching waits for
+ * the device. */
+HFB_API int hfb_ctx_set_batch_pipeline(HfbCtx* ctx, uint32_t on);
+
 /* hfb_frame_batch run as plain launches with a CUDA event between passes;
  * waits for the frame and writes the GPU time of each pass, in ms, to
  * passMs[0..7]: grid_pre, integrate, grid_post (with its grid clear),

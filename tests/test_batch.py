@@ -73,10 +73,11 @@ def test_frame_matches_pass_by_pass():
             _compare(_state(ref), _state(nat), ref, f)
 
 
-def _batch_vs_alone(insts, frames, profile_frame=None, groups=1):
+def _batch_vs_alone(insts, frames, profile_frame=None, groups=1, pipeline=False):
     alone = [Renderer(inst, 0) for inst in insts]
     ctx = Context(insts[0].cfg.to_c(), 0)
     ctx.set_batch_groups(groups)
+    ctx.set_batch_pipeline(pipeline)
     batch = BatchRenderer([Renderer(inst, 0, ctx=ctx) for inst in insts])
     for r in alone:
         r.before_first_frame()
@@ -121,6 +122,34 @@ def test_frame_batch_many_small_instances(groups):
     _batch_vs_alone(insts, 3, groups=groups)
 
 
+def test_frame_batch_pipelined_each_frame():
+    """Simulation and raster passes on two streams, two tables in turn; the
+    first frames run plain launches, the later ones the captured graphs."""
+    _batch_vs_alone(_instances(), 6, pipeline=True)
+
+
+def test_frame_batch_pipelined_back_to_back():
+    """Frames submitted without waiting in between, so that each frame's
+    simulation overlaps the previous frame's raster passes: the state after
+    the last frame equals each instance's alone."""
+    insts = _instances()
+    frames = 7
+    alone = [Renderer(inst, 0) for inst in insts]
+    ctx = Context(insts[0].cfg.to_c(), 0)
+    ctx.set_batch_pipeline(True)
+    batch = BatchRenderer([Renderer(inst, 0, ctx=ctx) for inst in insts])
+    for r in alone:
+        r.before_first_frame()
+        for _ in range(frames):
+            r.frame()
+    batch.before_first_frame()
+    for _ in range(frames):
+        batch.frame()
+    torch.cuda.synchronize()
+    for ra, rb in zip(alone, batch.renderers):
+        _compare(_state(ra), _state(rb), ra, frames - 1)
+
+
 def test_frame_batch_rejects_bad_instances():
     insts = _instances()[:2]
     ctx = Context(insts[0].cfg.to_c(), 0)
@@ -139,4 +168,6 @@ def test_frame_batch_rejects_bad_instances():
     for bad in (0, 5):
         with pytest.raises(Exception, match="groups"):
             ctx.set_batch_groups(bad)
+    with pytest.raises(Exception, match="pipeline"):
+        ctx.call("hfb_ctx_set_batch_pipeline", 2)
 
