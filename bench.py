@@ -425,11 +425,11 @@ def run_batched(args, rank, world, dist):
 
     # ---- per-pass times of one batched frame (plain launches + events) ----
     arr = (HfbInstance * n)(*[r.instance() for r in rs])
-    pm = (ctypes.c_float * 8)()
+    names = ["grid_pre", "integrate", "grid_post", "clear", "tiles", "sort", "fine", "hair_depth", "shading"]
+    pm = (ctypes.c_float * len(names))()
     ctx.call("hfb_frame_batch_profile", arr, n, pm)
     for r, inst in zip(rs, arr):
         r.after_native_frame(inst)
-    names = ["grid_pre", "integrate", "grid_post", "clear", "tiles", "sort", "fine", "shading"]
     pass_ms = {k: float(pm[i]) for i, k in enumerate(names)}
     K = [read_records(r) for r in rs]
 

@@ -63,9 +63,13 @@ cudaError_t framePass(HfbCtx* c, HfbInstance* in, FramePass p) {
       return launchTileSort(c, rb);
     case FP_FINE:
       return launchFinePass(c, u, h, prev, in->tangents, in->shading, in->sceneDepth, rb);
+    case FP_HAIR_DEPTH:
+      if (!in->hairDepth) return cudaSuccess;
+      return launchHairDepth(c, u, h, prev, in->tangents, in->strandsToRender, in->sceneDepth, in->hairDepth, rb);
     case FP_SHADING:
       if (!h.strandsCount) return cudaSuccess;
-      return launchShading(c, u, h, prev, in->tangents, in->shadingDepth ? in->shadingDepth : in->sceneDepth,
+      return launchShading(c, u, h, prev, in->tangents,
+                           in->hairDepth ? in->hairDepth : in->shadingDepth ? in->shadingDepth : in->sceneDepth,
                            in->ao, in->ao ? in->aoWidth : 0u, in->ao ? in->aoHeight : 0u, in->shadowMap,
                            in->shadowMap ? in->shadowMapSize : 0u, in->shading);
     default:
@@ -140,7 +144,36 @@ __global__ void __launch_bounds__(256) clearBatch(BatchView b, HfbConfig cfgPara
   }
 }
 
+// sceneDepth -> hairDepth, chunk `local` of the instance's W*H floats; chunk
+// 0 also zeroes the count of the hair depth's big-triangle list.
+__global__ void __launch_bounds__(256) depthCopyBatch(BatchView b) {
+  const uint32_t n = b.hdr->n;
+  const uint32_t* row = b.prefix + BK_DEPTH_COPY * (BATCH_MAX + 1);
+  const uint32_t total = row[n];
+  for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
+    const uint32_t i = batchFind(row, n, v);
+    const BatchInst& I = b.insts[i];
+    const size_t bytes = (size_t)I.W * I.H * 4, off = (size_t)(v - row[i]) * CLEAR_CHUNK;
+    const size_t end = off + CLEAR_CHUNK < bytes ? off + CLEAR_CHUNK : bytes;
+    const unsigned char* src = (const unsigned char*)I.depth;
+    unsigned char* dst = (unsigned char*)I.hairDepth;
+    for (size_t x = off + threadIdx.x * 4u; x < end; x += 256u * 4u)
+      *HFB_G(reinterpret_cast<uint32_t*>(dst + x)) = *HFB_G(reinterpret_cast<const uint32_t*>(src + x));
+    if (v == row[i] && threadIdx.x == 0) *HFB_G(reinterpret_cast<uint32_t*>(I.scratch)) = 0u;
+  }
+}
+
 }  // namespace
+
+cudaError_t launchBatchDepthCopy(HfbCtx* c, const BatchView& b) {
+  HFB_CHECK_BIND(c);
+  uint32_t& grid = c->batchGrid[BK_DEPTH_COPY];
+  if (!grid) grid = c->smCount * 8u;
+  depthCopyBatch<<<batchLaunchGrid(c, grid), 256, 0, c->stream>>>(b);
+  HFB_AFTER_LAUNCH(c, "depthCopyBatch");
+  c->launches += 1;
+  return cudaGetLastError();
+}
 
 uint32_t batchBlocks(const HfbConfig& cfg, BatchKind k, const BatchInst& I) {
   const uint32_t G3 = cfg.gridDims * cfg.gridDims * cfg.gridDims;
@@ -170,6 +203,8 @@ uint32_t batchBlocks(const HfbConfig& cfg, BatchKind k, const BatchInst& I) {
     case BK_SORT: return 1u;
     case BK_SCHEDULE: return 1u;
     case BK_SHADING: return divCeil(I.S * cfg.shadingPoints, 128u);
+    case BK_DEPTH_COPY: return I.hairDepth ? divCeil((uint32_t)(((size_t)I.W * I.H * 4 + CLEAR_CHUNK - 1) / CLEAR_CHUNK), 1u) : 0u;
+    case BK_HAIR_DEPTH: return I.hairDepth ? divCeil(nSeg, 256u) : 0u;
     default: return 0u;
   }
 }
@@ -188,7 +223,7 @@ cudaError_t launchBatchClear(HfbCtx* c, const BatchView& b, BatchKind k) {
 // passes, then the raster passes.  With `ev`, an event is recorded before the
 // first pass and after each of the HFB_FRAME_PASSES passes (grid_pre,
 // integrate, grid_post with its grid clear, clear, tiles, sort, fine,
-// shading).
+// hair_depth, shading).
 static cudaError_t simSequence(HfbCtx* c, const BatchView& b, cudaEvent_t* ev = nullptr) {
   auto mark = [&](int i) { return ev ? cudaEventRecord(ev[i], c->stream) : cudaSuccess; };
   cudaError_t e = mark(0);
@@ -212,8 +247,11 @@ static cudaError_t rasterSequence(HfbCtx* c, const BatchView& b, cudaEvent_t* ev
   if (e == cudaSuccess) e = mark(6);
   if (e == cudaSuccess) e = launchBatchFine(c, b);
   if (e == cudaSuccess) e = mark(7);
-  if (e == cudaSuccess) e = launchBatchShading(c, b);
+  if (e == cudaSuccess) e = launchBatchDepthCopy(c, b);
+  if (e == cudaSuccess) e = launchBatchHairDepth(c, b);
   if (e == cudaSuccess) e = mark(8);
+  if (e == cudaSuccess) e = launchBatchShading(c, b);
+  if (e == cudaSuccess) e = mark(9);
   return e;
 }
 
@@ -251,7 +289,8 @@ static void fillInstance(const HfbConfig& cfg, const HfbInstance& s, BatchInst& 
   I.sdf = s.sdf;
   I.shading = (float4*)s.shading;
   I.depth = s.sceneDepth;
-  I.shadingDepth = s.shadingDepth ? s.shadingDepth : s.sceneDepth;
+  I.shadingDepth = s.hairDepth ? s.hairDepth : s.shadingDepth ? s.shadingDepth : s.sceneDepth;
+  I.hairDepth = s.hairDepth;
   I.ao = s.ao;
   I.sm = s.shadowMap;
   I.tiles = (uint4*)s.raster.tiles;
@@ -261,6 +300,7 @@ static void fillInstance(const HfbConfig& cfg, const HfbInstance& s, BatchInst& 
   I.tileList = s.raster.tileList;
   I.result = s.raster.rasterizerResult;
   I.scratch = (unsigned char*)s.raster.scratch;
+  I.scratchBytes = s.raster.scratchBytes;
 }
 
 // Rough GPU work of one instance's frame, for balancing the groups: the

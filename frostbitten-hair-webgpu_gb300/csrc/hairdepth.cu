@@ -1,0 +1,244 @@
+// Hair depth prepass: HwHairPass.cmdDrawHair's depth output as CUDA.
+//
+// The reference draws every hair segment as two triangles with the hardware
+// rasterizer (hwHairPass.ts:71-160, vertex shader hwRasterizeHair,
+// hwRasterizeHair.wgsl.ts:23-57, index order hairIndexBuffer.ts:29-46) into
+// the depth buffer that already holds the scene, with depthCompare 'less'
+// (PIPELINE_DEPTH_ON, passes/_shared/shared.ts:22-26).  The shading pass then
+// reads that depth (renderer.ts:286-296).  This restates it:
+//
+// - vertex 2*id + k of segment id = strand*P + seg (k = 0..3) is point
+//   seg + k/2 in view space (modelViewMat), moved by fiberRadius along
+//   safeNormalize(cross(tangentVS, (0, 0, 1))) -- plus for even k, minus for
+//   odd k (the tangent is transformed with w = 1, as the reference does) --
+//   and projected (projMatrix); triangles (0, 1, 2) and (2, 1, 3);
+// - coverage is tested at pixel centres (x + 0.5, y + 0.5) in framebuffer
+//   coordinates (rows down), both windings drawn (cullMode 'none'), edges
+//   inclusive; depth = NDC z interpolated with the screen-space barycentric
+//   weights; a triangle with a vertex behind the camera (w <= 0) is not
+//   drawn (no near-plane clipping); depth outside [0, 1] is discarded;
+// - the 'less' test is an atomic minimum on the depth's bits (non-negative
+//   floats order like their bits), so the result does not depend on the
+//   order of the fragments.
+// The GPU's own rasterizer rules (fixed-point vertex snapping, the top-left
+// tie-break, depth24 storage) are implementation-defined and not reproduced;
+// the oracle (oracle_hair_depth) follows the rules above.
+#define HFB_TU 7
+#include "hfb_internal.cuh"
+#include "hfb_math.cuh"
+
+namespace hfb {
+namespace {
+
+constexpr uint32_t HD_THREADS = 256;
+constexpr uint32_t HD_BIG_AREA = 1024;  // pixels: larger triangles are drawn by a whole block
+
+struct ScreenV {
+  float x, y, z;
+  bool ok;
+};
+
+struct Tri {
+  ScreenV v[3];
+};
+
+__device__ __forceinline__ float edgeFn(float ax, float ay, float bx, float by, float px, float py) {
+  return fsub(fmul(fsub(bx, ax), fsub(py, ay)), fmul(fsub(by, ay), fsub(px, ax)));
+}
+
+// The four screen-space vertices of segment (strand, seg).
+__device__ __forceinline__ void segmentQuad(const HfbUniforms& U, const float4* __restrict__ pos,
+                                            const float4* __restrict__ tan, uint32_t P, uint32_t strand,
+                                            uint32_t seg, float W, float H, ScreenV (&q)[4]) {
+#pragma unroll
+  for (uint32_t k = 0; k < 4u; k++) {
+    const size_t i = (size_t)strand * P + seg + (k >> 1);
+    const float4 p = __ldg(HFB_G(&pos[i]));
+    const float4 t = __ldg(HFB_G(&tan[i]));
+    const f4 pVS = m4v(U.modelViewMat.m, mk4(p.x, p.y, p.z, 1.0f));
+    const f4 tVS = m4v(U.modelViewMat.m, mk4(t.x, t.y, t.z, 1.0f));
+    const f3 c = cross3(xyz(tVS), mk3(0.0f, 0.0f, 1.0f));
+    const f3 right = dot3(c, c) >= 1e-7f ? norm3(c) : mk3(0.0f, 0.0f, 0.0f);  // safeNormalize3
+    const f3 th = mul3s(right, U.fiberRadius);
+    const f3 e = (k & 1u) ? sub3(xyz(pVS), th) : add3(xyz(pVS), th);
+    const f4 clip = m4v(U.projMatrix.m, mk4(e.x, e.y, e.z, 1.0f));
+    ScreenV v;
+    v.ok = clip.w > 0.0f;
+    const float nx = clip.x / clip.w, ny = clip.y / clip.w;
+    v.z = clip.z / clip.w;
+    v.x = fmul(fadd(fmul(nx, 0.5f), 0.5f), W);
+    v.y = fmul(fsub(0.5f, fmul(ny, 0.5f)), H);
+    q[k] = v;
+  }
+}
+
+// Pixel range [x0, x1] x [y0, y1] whose centres lie in the triangle's box;
+// false if the triangle is not drawn at all.
+__device__ __forceinline__ bool triBox(const Tri& t, uint32_t W, uint32_t H, float& area, int& x0, int& x1, int& y0,
+                                       int& y1) {
+  if (!t.v[0].ok || !t.v[1].ok || !t.v[2].ok) return false;
+  area = edgeFn(t.v[0].x, t.v[0].y, t.v[1].x, t.v[1].y, t.v[2].x, t.v[2].y);
+  if (!(area != 0.0f) || !isfinite(area)) return false;
+  const float mnx = fminf(fminf(t.v[0].x, t.v[1].x), t.v[2].x), mxx = fmaxf(fmaxf(t.v[0].x, t.v[1].x), t.v[2].x);
+  const float mny = fminf(fminf(t.v[0].y, t.v[1].y), t.v[2].y), mxy = fmaxf(fmaxf(t.v[0].y, t.v[1].y), t.v[2].y);
+  if (!(mxx >= 0.5f && mxy >= 0.5f && mnx <= (float)W - 0.5f && mny <= (float)H - 0.5f)) return false;
+  x0 = (int)fmaxf(ceilf(fsub(mnx, 0.5f)), 0.0f);
+  y0 = (int)fmaxf(ceilf(fsub(mny, 0.5f)), 0.0f);
+  x1 = (int)fminf(floorf(fsub(mxx, 0.5f)), (float)W - 1.0f);
+  y1 = (int)fminf(floorf(fsub(mxy, 0.5f)), (float)H - 1.0f);
+  return x0 <= x1 && y0 <= y1;
+}
+
+__device__ __forceinline__ void triPixel(const Tri& t, float area, uint32_t W, int x, int y,
+                                         unsigned* __restrict__ depth) {
+  const float px = fadd((float)x, 0.5f), py = fadd((float)y, 0.5f);
+  float w0 = edgeFn(t.v[1].x, t.v[1].y, t.v[2].x, t.v[2].y, px, py);
+  float w1 = edgeFn(t.v[2].x, t.v[2].y, t.v[0].x, t.v[0].y, px, py);
+  float w2 = edgeFn(t.v[0].x, t.v[0].y, t.v[1].x, t.v[1].y, px, py);
+  if (area < 0.0f) { w0 = -w0; w1 = -w1; w2 = -w2; }
+  if (!(w0 >= 0.0f && w1 >= 0.0f && w2 >= 0.0f)) return;
+  const float a = fabsf(area);
+  const float z = fadd(fadd(fmul(w0 / a, t.v[0].z), fmul(w1 / a, t.v[1].z)), fmul(w2 / a, t.v[2].z));
+  if (!(z >= 0.0f && z <= 1.0f)) return;
+  atomicMin(HFB_G(&depth[(size_t)y * W + x]), __float_as_uint(fadd(z, 0.0f)));  // -0 -> +0
+}
+
+// One thread per segment: both triangles in the thread, or onto the big
+// list (entries segment << 1 | triangle; capacity `bigCap`, overflow drawn
+// in the thread).
+__device__ __forceinline__ void hairDepthBody(const HfbUniforms& U, uint32_t P, uint32_t nStrands,
+                                              const float4* __restrict__ pos, const float4* __restrict__ tan,
+                                              unsigned* __restrict__ depth, uint32_t* __restrict__ big,
+                                              uint32_t bigCap, uint32_t gid) {
+  const uint32_t segs = P - 1u, nSeg = nStrands * segs;
+  if (gid >= nSeg) return;
+  const uint32_t W = f2u(U.viewport.x), H = f2u(U.viewport.y);
+  const uint32_t strand = gid / segs, seg = gid - strand * segs;
+  ScreenV q[4];
+  segmentQuad(U, pos, tan, P, strand, seg, U.viewport.x, U.viewport.y, q);
+#pragma unroll
+  for (uint32_t tr = 0; tr < 2u; tr++) {
+    Tri t;
+    t.v[0] = tr ? q[2] : q[0];
+    t.v[1] = q[1];
+    t.v[2] = tr ? q[3] : q[2];
+    float area;
+    int x0, x1, y0, y1;
+    if (!triBox(t, W, H, area, x0, x1, y0, y1)) continue;
+    const uint64_t px = (uint64_t)(x1 - x0 + 1) * (uint64_t)(y1 - y0 + 1);
+    if (px > HD_BIG_AREA) {
+      const uint32_t slot = atomicAdd(HFB_G(&big[0]), 1u);
+      if (slot < bigCap) {
+        *HFB_G(&big[1u + slot]) = (gid << 1) | tr;
+        continue;
+      }
+    }
+    for (int y = y0; y <= y1; y++)
+      for (int x = x0; x <= x1; x++) triPixel(t, area, W, x, y, depth);
+  }
+}
+
+// The big list, one block per triangle.
+__device__ __forceinline__ void hairDepthBigBody(const HfbUniforms& U, uint32_t P, const float4* __restrict__ pos,
+                                                 const float4* __restrict__ tan, unsigned* __restrict__ depth,
+                                                 const uint32_t* __restrict__ big, uint32_t bigCap, uint32_t blk,
+                                                 uint32_t nblk) {
+  const uint32_t n = min(*HFB_G(&big[0]), bigCap);
+  const uint32_t W = f2u(U.viewport.x), H = f2u(U.viewport.y);
+  const uint32_t segs = P - 1u;
+  for (uint32_t e = blk; e < n; e += nblk) {
+    const uint32_t ent = *HFB_G(&big[1u + e]);
+    const uint32_t gid = ent >> 1, tr = ent & 1u;
+    const uint32_t strand = gid / segs, seg = gid - strand * segs;
+    ScreenV q[4];
+    segmentQuad(U, pos, tan, P, strand, seg, U.viewport.x, U.viewport.y, q);
+    Tri t;
+    t.v[0] = tr ? q[2] : q[0];
+    t.v[1] = q[1];
+    t.v[2] = tr ? q[3] : q[2];
+    float area;
+    int x0, x1, y0, y1;
+    if (!triBox(t, W, H, area, x0, x1, y0, y1)) continue;
+    const uint32_t bw = (uint32_t)(x1 - x0 + 1), bh = (uint32_t)(y1 - y0 + 1);
+    for (uint64_t i = threadIdx.x; i < (uint64_t)bw * bh; i += blockDim.x)
+      triPixel(t, area, W, x0 + (int)(i % bw), y0 + (int)(i / bw), depth);
+  }
+}
+
+__global__ void __launch_bounds__(HD_THREADS)
+hairDepthKernel(const HfbUniforms U, uint32_t P, uint32_t nStrands, const float4* __restrict__ pos,
+                const float4* __restrict__ tan, unsigned* __restrict__ depth, uint32_t* __restrict__ big,
+                uint32_t bigCap) {
+  hairDepthBody(U, P, nStrands, pos, tan, depth, big, bigCap, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__global__ void __launch_bounds__(HD_THREADS)
+hairDepthBigKernel(const HfbUniforms U, uint32_t P, const float4* __restrict__ pos, const float4* __restrict__ tan,
+                   unsigned* __restrict__ depth, const uint32_t* __restrict__ big, uint32_t bigCap) {
+  hairDepthBigBody(U, P, pos, tan, depth, big, bigCap, blockIdx.x, gridDim.x);
+}
+
+// ---- batched: persistent over every instance ----
+__global__ void __launch_bounds__(HD_THREADS) hairDepthBatch(BatchView b) {
+  const uint32_t n = b.hdr->n;
+  const uint32_t* row = b.prefix + BK_HAIR_DEPTH * (BATCH_MAX + 1);
+  const uint32_t total = row[n];
+  for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
+    const uint32_t i = batchFind(row, n, v);
+    const BatchInst& I = b.insts[i];
+    uint32_t* big = reinterpret_cast<uint32_t*>(I.scratch);
+    hairDepthBody(I.U, I.P, min(I.strandsToRender, I.S), I.posNew, I.tan, reinterpret_cast<unsigned*>(I.hairDepth),
+                  big, hairDepthBigCap(I.scratchBytes), (v - row[i]) * HD_THREADS + threadIdx.x);
+  }
+}
+
+__global__ void __launch_bounds__(HD_THREADS) hairDepthBigBatch(BatchView b) {
+  const uint32_t n = b.hdr->n;
+  for (uint32_t i = 0; i < n; i++) {  // every block takes a share of each instance's list
+    const BatchInst& I = b.insts[i];
+    if (!I.hairDepth) continue;
+    hairDepthBigBody(I.U, I.P, I.posNew, I.tan, reinterpret_cast<unsigned*>(I.hairDepth),
+                     reinterpret_cast<const uint32_t*>(I.scratch), hairDepthBigCap(I.scratchBytes), blockIdx.x,
+                     gridDim.x);
+  }
+}
+
+}  // namespace
+
+cudaError_t launchHairDepth(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, const float* pos, const float* tan,
+                            uint32_t strandsToRender, const float* sceneDepth, float* hairDepth,
+                            HfbRasterBuffers& rb) {
+  HFB_CHECK_BIND(c);
+  const size_t px = (size_t)rb.width * rb.height;
+  cudaError_t e = cudaMemcpyAsync(hairDepth, sceneDepth, px * 4, cudaMemcpyDeviceToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(rb.scratch, 0, 4, c->stream);  // the big list's count
+  if (e != cudaSuccess) return e;
+  const uint32_t nStrands = min(strandsToRender, h.strandsCount);
+  const uint32_t nSeg = nStrands * (h.pointsPerStrand - 1u);
+  if (nSeg == 0) return cudaSuccess;
+  const uint32_t cap = hairDepthBigCap(rb.scratchBytes);
+  uint32_t* big = reinterpret_cast<uint32_t*>(rb.scratch);
+  hairDepthKernel<<<divCeil(nSeg, HD_THREADS), HD_THREADS, 0, c->stream>>>(
+      u, h.pointsPerStrand, nStrands, (const float4*)pos, (const float4*)tan, (unsigned*)hairDepth, big, cap);
+  HFB_AFTER_LAUNCH(c, "hairDepthKernel");
+  hairDepthBigKernel<<<c->smCount * 4u, HD_THREADS, 0, c->stream>>>(u, h.pointsPerStrand, (const float4*)pos,
+                                                                    (const float4*)tan, (unsigned*)hairDepth, big,
+                                                                    cap);
+  HFB_AFTER_LAUNCH(c, "hairDepthBigKernel");
+  c->launches += 2;
+  return cudaGetLastError();
+}
+
+cudaError_t launchBatchHairDepth(HfbCtx* c, const BatchView& b) {
+  HFB_CHECK_BIND(c);
+  uint32_t& grid = c->batchGrid[BK_HAIR_DEPTH];
+  if (!grid) grid = c->smCount * 8u;
+  hairDepthBatch<<<batchLaunchGrid(c, grid), HD_THREADS, 0, c->stream>>>(b);
+  HFB_AFTER_LAUNCH(c, "hairDepthBatch");
+  hairDepthBigBatch<<<batchLaunchGrid(c, c->smCount * 4u), HD_THREADS, 0, c->stream>>>(b);
+  HFB_AFTER_LAUNCH(c, "hairDepthBigBatch");
+  c->launches += 2;
+  return cudaGetLastError();
+}
+
+}  // namespace hfb

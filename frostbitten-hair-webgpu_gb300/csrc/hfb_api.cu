@@ -383,6 +383,18 @@ int hfb_fine_pass(HfbCtx* c, const HfbUniforms* u, const HfbHairData* h, const f
   HFB_LAUNCH(c, hfb::launchFinePass(c, *u, *h, pos, tan, shading, depth, *rb), "fine_pass");
 }
 
+int hfb_hair_depth(HfbCtx* c, const HfbUniforms* u, const HfbHairData* h, const float* pos, const float* tan,
+                   uint32_t strandsToRender, const float* sceneDepth, float* hairDepth, HfbRasterBuffers* rb) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, pos && tan && sceneDepth && hairDepth, "NULL argument");
+  HFB_REQUIRE(c, aligned16(pos) && aligned16(tan), "vec4 buffers must be 16-byte aligned");
+  std::string err = validateHair(h);
+  if (err.empty()) err = checkRaster(c, rb);
+  if (err.empty()) err = checkViewport(u, rb);
+  HFB_REQUIRE(c, err.empty(), err);
+  HFB_LAUNCH(c, hfb::launchHairDepth(c, *u, *h, pos, tan, strandsToRender, sceneDepth, hairDepth, *rb), "hair_depth");
+}
+
 // Checks one instance of a frame (the union of the per-pass checks).
 static std::string checkInstance(const HfbCtx* c, const HfbInstance* in) {
   if (!in) return "instance is NULL";

@@ -172,6 +172,7 @@ enum FramePass : uint32_t {
   FP_TILES,         // HairTilesPass
   FP_SORT,          // HairTileSortPass
   FP_FINE,          // HairFinePass
+  FP_HAIR_DEPTH,    // HwHairPass's depth (only for instances with hairDepth)
   FP_SHADING,       // HairShadingPass
   FP_COUNT
 };
@@ -210,6 +211,8 @@ enum BatchKind : uint32_t {
   BK_SORT,
   BK_SCHEDULE,
   BK_SHADING,
+  BK_DEPTH_COPY,       // sceneDepth -> hairDepth (and the big-triangle list's count)
+  BK_HAIR_DEPTH,
   BK_COUNT
 };
 
@@ -241,6 +244,8 @@ struct alignas(16) BatchInst {
   uint32_t* tileList;
   float* result;
   unsigned char* scratch;
+  size_t scratchBytes;
+  float* hairDepth;           // NULL: no hair depth prepass
 };
 
 // Device layout of a batch: header, prefix rows (fixed stride), the fine
@@ -284,6 +289,17 @@ cudaError_t launchBatchShading(HfbCtx* c, const BatchView& b);
 cudaError_t launchBatchTiles(HfbCtx* c, const BatchView& b);
 cudaError_t launchBatchSort(HfbCtx* c, const BatchView& b);
 cudaError_t launchBatchFine(HfbCtx* c, const BatchView& b);
+cudaError_t launchBatchHairDepth(HfbCtx* c, const BatchView& b);
+cudaError_t launchBatchDepthCopy(HfbCtx* c, const BatchView& b);
+// Hair depth prepass (hairdepth.cu); entries of its big-triangle list in a
+// raster scratch area of `bytes` (word 0 = count).
+cudaError_t launchHairDepth(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, const float* pos, const float* tan,
+                            uint32_t strandsToRender, const float* sceneDepth, float* hairDepth,
+                            HfbRasterBuffers& rb);
+__host__ __device__ inline uint32_t hairDepthBigCap(size_t bytes) {
+  const size_t n = bytes / 4 > 1 ? bytes / 4 - 1 : 0;
+  return (uint32_t)(n < 0x7FFFFFFFu ? n : 0x7FFFFFFFu);
+}
 // Virtual blocks of kind k for one instance (host side).
 uint32_t batchBlocks(const HfbConfig& cfg, BatchKind k, const BatchInst& bi);
 // One frame of n checked instances; flips their `current`.  With passMs, the

@@ -53,7 +53,7 @@ class HfbInstance(ctypes.Structure):
                 ("sdf", ctypes.c_void_p), ("sdfDims", ctypes.c_uint32), ("shadowMapSize", ctypes.c_uint32),
                 ("shading", ctypes.c_void_p), ("sceneDepth", ctypes.c_void_p), ("shadingDepth", ctypes.c_void_p),
                 ("ao", ctypes.c_void_p), ("aoWidth", ctypes.c_uint32), ("aoHeight", ctypes.c_uint32),
-                ("shadowMap", ctypes.c_void_p), ("raster", HfbRasterBuffers)]
+                ("shadowMap", ctypes.c_void_p), ("raster", HfbRasterBuffers), ("hairDepth", ctypes.c_void_p)]
 
 
 class HfbCounters(ctypes.Structure):
@@ -65,7 +65,7 @@ class HfbCounters(ctypes.Structure):
 
 assert ctypes.sizeof(HfbHairData) == 32
 assert ctypes.sizeof(HfbCounters) == 64
-assert ctypes.sizeof(HfbInstance) == 256
+assert ctypes.sizeof(HfbInstance) == 264
 
 # every symbol include/hairfb.h declares: name -> (restype, argtypes)
 P, U32, SZ, I = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_size_t, ctypes.c_int
@@ -96,6 +96,7 @@ SIGNATURES = {
     "hfb_tile_sort": (I, [P, P]),
     "hfb_fine_pass": (I, [P, P, P, P, P, P, P, P]),
     "hfb_tiles_pass_noalloc": (I, [P, P, P, P, P, P, U32, P]),
+    "hfb_hair_depth": (I, [P, P, P, P, P, U32, P, P, P]),
     "hfb_frame": (I, [P, P]),
     "hfb_frame_batch": (I, [P, P, U32]),
     "hfb_frame_batch_profile": (I, [P, P, U32, P]),

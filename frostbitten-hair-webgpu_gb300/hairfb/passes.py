@@ -259,6 +259,23 @@ class HairFinePass:
                       ptr(hair.tangents), ptr(hair.shading), ptr(depth), byref(rb.rb))
 
 
+class HwHairPass:
+    """src/passes/hwHair/hwHairPass.ts: the depth it draws (cmdDrawHair's depth
+    attachment), which the shading pass reads."""
+    NAME = "HwHairPass"
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+
+    def cmd_draw_hair_depth(self, uniforms: bytes, hair: HairObject, scene_depth: torch.Tensor,
+                            hair_depth: torch.Tensor, rb: RasterBuffers):
+        """hair_depth = scene_depth with the hair's triangles drawn over it
+        (depth test 'less')."""
+        self.ctx.call("hfb_hair_depth", _ub(uniforms), byref(hair.hair_data), ptr(hair.positions),
+                      ptr(hair.tangents), hair.rendered_strand_count(), ptr(scene_depth), ptr(hair_depth),
+                      byref(rb.rb))
+
+
 def clear_before_render(ctx: Context, rb: RasterBuffers):
     """cmdClearBeforeRender of the tiles, fine and sort passes."""
     ctx.call("hfb_clear_before_render", byref(rb.rb))

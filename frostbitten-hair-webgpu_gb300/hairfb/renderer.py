@@ -21,7 +21,7 @@ from . import synthetic, uniforms as UN
 from .config import HairConfig
 from .lib import Context, HfbInstance, ptr
 from .passes import (GridPostSimPass, GridPreSimPass, HairFinePass, HairObject, HairShadingPass,
-                     HairSimIntegrationPass, HairTileSortPass, HairTilesPass, PhysicsGrids,
+                     HairSimIntegrationPass, HairTileSortPass, HairTilesPass, HwHairPass, PhysicsGrids,
                      RasterBuffers, SdfCollider, clear_before_render)
 
 
@@ -29,9 +29,12 @@ class Renderer:
     """One hair instance rendered frame by frame through libhairfb.so."""
 
     def __init__(self, inst: synthetic.Instance, device: int = -1, ctx: Context | None = None,
-                 max_drawn: int | None = None):
+                 max_drawn: int | None = None, hair_depth: bool = False):
         """max_drawn: this instance's segment pool in records (None: the
-        config's 1 + tiles * avgSegmentsPerTile)."""
+        config's 1 + tiles * avgSegmentsPerTile).  hair_depth: draw the hair's
+        depth over the scene depth after the fine pass (HwHairPass) and shade
+        with it, as the reference does; otherwise the shading reads the scene
+        depth."""
         self.inst = inst
         self.cfg: HairConfig = inst.cfg
         self.ctx = ctx or Context(inst.cfg.to_c(), device)
@@ -41,9 +44,10 @@ class Renderer:
         self.grids = PhysicsGrids(inst.cfg.grid_dims)
         self.rb = RasterBuffers(self.ctx, inst.width, inst.height, max_drawn)
         self.scene_depth = torch.as_tensor(inst.scene_depth).cuda()
-        # depth buffer with hair drawn, for the shading attenuation; the
-        # hardware hair pass is outside the path, the scene depth stands in
-        self.shading_depth = self.scene_depth
+        # depth buffer with hair drawn, for the shading attenuation; before the
+        # first frame draws the hair it holds the scene alone
+        self.hair_depth = self.scene_depth.clone() if hair_depth else None
+        self.shading_depth = self.hair_depth if hair_depth else self.scene_depth
         self.grid_pre = GridPreSimPass(self.ctx)
         self.integrate = HairSimIntegrationPass(self.ctx)
         self.grid_post = GridPostSimPass(self.ctx)
@@ -51,6 +55,7 @@ class Renderer:
         self.tiles = HairTilesPass(self.ctx)
         self.sort = HairTileSortPass(self.ctx)
         self.fine = HairFinePass(self.ctx)
+        self.hw_hair = HwHairPass(self.ctx)
         self.frame_idx = 0
         self.uniforms = UN.pack_render_uniforms(inst.scene, inst.cfg, max_drawn)
         self._inst = self._inst_uniforms = self._inst_rb = None  # cached HfbInstance (instance())
@@ -64,7 +69,8 @@ class Renderer:
         self.cfg = cfg
         self.ctx = ctx
         self.rb = RasterBuffers(ctx, self.inst.width, self.inst.height, self.max_drawn)
-        for p in (self.grid_pre, self.integrate, self.grid_post, self.shading, self.tiles, self.sort, self.fine):
+        for p in (self.grid_pre, self.integrate, self.grid_post, self.shading, self.tiles, self.sort, self.fine,
+                  self.hw_hair):
             p.ctx = ctx
         self.uniforms = UN.pack_render_uniforms(self.inst.scene, cfg, self.max_drawn)
         old.close()
@@ -92,6 +98,8 @@ class Renderer:
         self.tiles.cmd_draw_hair_to_tiles(self.uniforms, self.hair, self.scene_depth, self.rb)
         self.sort.cmd_sort_hair_tiles(self.rb)
         self.fine.cmd_rasterize_slices_hair(self.uniforms, self.hair, self.scene_depth, self.rb)
+        if self.hair_depth is not None:  # updateResourcesForNextFrame, renderer.ts:286-296
+            self.hw_hair.cmd_draw_hair_depth(self.uniforms, self.hair, self.scene_depth, self.hair_depth, self.rb)
         self.shading.cmd_compute_shading_points(self.uniforms, self.hair, self.shading_depth)
 
     def frame(self) -> None:
@@ -128,6 +136,7 @@ class Renderer:
             inst.sceneDepth = ptr(self.scene_depth)
             inst.shadingDepth = ptr(self.shading_depth)
             inst.raster = self.rb.rb
+            inst.hairDepth = ptr(self.hair_depth) if self.hair_depth is not None else None
             self._inst, self._inst_uniforms, self._inst_rb = inst, self.uniforms, self.rb
         else:
             UN.patch_sim_uniforms(self._su_buf, self.frame_idx, i.wind_strength(self.frame_idx))

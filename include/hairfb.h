@@ -308,7 +308,24 @@ typedef struct HfbInstance {
   uint32_t aoWidth, aoHeight;
   const float* shadowMap;             /* NULL = unshadowed */
   HfbRasterBuffers raster;            /* from hfb_raster_buffers_alloc */
+  /* W*H f32, NULL = none.  If set, the frame copies sceneDepth into it and
+   * draws the hair's depth over it after the fine pass (hfb_hair_depth), and
+   * the shading pass reads it instead of shadingDepth: the depth buffer with
+   * the hair drawn that HwHairPass leaves for the shading
+   * (renderer.ts:286-296). */
+  float* hairDepth;
 } HfbInstance;
+
+/* HwHairPass.cmdDrawHair's depth output (hwHairPass.ts:71-160): copies
+ * sceneDepth (W*H f32) into hairDepth and draws every rendered hair segment's
+ * two triangles (hwRasterizeHair.wgsl.ts:23-57) over it with depth test
+ * 'less'.  Coverage at pixel centres, edges inclusive, depth = NDC z
+ * interpolated in screen space; the GPU rasterizer's own snapping and
+ * depth24 storage are not reproduced.  Uses rb's scratch as working memory
+ * (the raster passes' scratch is free after the fine pass). */
+HFB_API int hfb_hair_depth(HfbCtx* ctx, const HfbUniforms* uniforms, const HfbHairData* hair, const float* positions,
+                           const float* tangents, uint32_t strandsToRender, const float* sceneDepth,
+                           float* hairDepth, HfbRasterBuffers* rb);
 
 /* One frame of one instance (the per-pass entries above, in order). */
 HFB_API int hfb_frame(HfbCtx* ctx, HfbInstance* instance);
@@ -344,9 +361,10 @@ HFB_API int hfb_ctx_set_batch_pipeline(HfbCtx* ctx, uint32_t on);
 
 /* hfb_frame_batch run as plain launches with a CUDA event between passes;
  * waits for the frame and writes the GPU time of each pass, in ms, to
- * passMs[0..7]: grid_pre, integrate, grid_post (with its grid clear),
- * clear (the raster clears), tiles, sort, fine, shading.  For profiling. */
-#define HFB_FRAME_PASSES 8
+ * passMs[0..8]: grid_pre, integrate, grid_post (with its grid clear),
+ * clear (the raster clears), tiles, sort, fine, hair_depth, shading.  For
+ * profiling. */
+#define HFB_FRAME_PASSES 9
 HFB_API int hfb_frame_batch_profile(HfbCtx* ctx, HfbInstance* instances, uint32_t n, float* passMs);
 
 /* No counterpart in the reference.  hfb_tiles_pass for callers that cannot
@@ -375,13 +393,13 @@ static_assert(sizeof(HfbConfig) == 64, "HfbConfig layout");
 static_assert(sizeof(HfbHairData) == 32, "HfbHairData layout");
 static_assert(sizeof(HfbUniforms) == 1184, "Uniforms layout");
 static_assert(sizeof(HfbSimUniforms) == 304, "SimulationUniforms layout");
-static_assert(sizeof(HfbInstance) == 256, "HfbInstance layout");
+static_assert(sizeof(HfbInstance) == 264, "HfbInstance layout");
 #else
 _Static_assert(sizeof(HfbConfig) == 64, "HfbConfig layout");
 _Static_assert(sizeof(HfbHairData) == 32, "HfbHairData layout");
 _Static_assert(sizeof(HfbUniforms) == 1184, "Uniforms layout");
 _Static_assert(sizeof(HfbSimUniforms) == 304, "SimulationUniforms layout");
-_Static_assert(sizeof(HfbInstance) == 256, "HfbInstance layout");
+_Static_assert(sizeof(HfbInstance) == 264, "HfbInstance layout");
 #endif
 
 #endif /* HAIRFB_H */

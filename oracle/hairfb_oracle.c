@@ -1293,6 +1293,86 @@ static inline float linearizeDepth(float n, float f, float d) { return n * f / (
  * depth: W*H (row 0 = top); ao: aoW*aoH or NULL (= 1.0); shadowMap: smSize^2
  * or NULL (= 1.0).  shading: S*SP vec4f output.
  */
+/* ---- HwHairPass's depth (hwHairPass.ts:71-160, hwRasterizeHair.wgsl.ts:23-57,
+ * index order hairIndexBuffer.ts:29-46), with the rasterizer rules the CUDA
+ * prepass uses: coverage at pixel centres, both windings, edges inclusive,
+ * depth = NDC z interpolated with the screen-space barycentric weights,
+ * triangles with a vertex behind the camera not drawn, depth outside [0, 1]
+ * discarded, depth test 'less' (the minimum). ---- */
+typedef struct { float x, y, z; int ok; } OScreenV;
+
+static float hdEdge(float ax, float ay, float bx, float by, float px, float py) {
+  return (bx - ax) * (py - ay) - (by - ay) * (px - ax);
+}
+
+static void hdQuad(const ORenderUniforms* U, const float* pos, const float* tan, uint32_t P, uint32_t strand,
+                   uint32_t seg, OScreenV q[4]) {
+  float W = U->viewport.x, H = U->viewport.y;
+  for (uint32_t k = 0; k < 4u; k++) {
+    size_t i = (size_t)strand * P + seg + (k >> 1);
+    const float* p = pos + 4 * i;
+    const float* t = tan + 4 * i;
+    v4 pVS = m4v(&U->modelViewMat, V4(p[0], p[1], p[2], 1.0f));
+    v4 tVS = m4v(&U->modelViewMat, V4(t[0], t[1], t[2], 1.0f));
+    v3 c = cross3(xyz(tVS), V3(0.0f, 0.0f, 1.0f));
+    v3 right = dot3(c, c) >= 1e-7f ? norm3(c) : V3(0.0f, 0.0f, 0.0f); /* safeNormalize3 */
+    v3 th = mul3s(right, U->fiberRadius);
+    v3 e = (k & 1u) ? sub3(xyz(pVS), th) : add3(xyz(pVS), th);
+    v4 clip = m4v(&U->projMatrix, V4(e.x, e.y, e.z, 1.0f));
+    OScreenV v;
+    v.ok = clip.w > 0.0f;
+    float nx = clip.x / clip.w, ny = clip.y / clip.w;
+    v.z = clip.z / clip.w;
+    v.x = (nx * 0.5f + 0.5f) * W;
+    v.y = (0.5f - ny * 0.5f) * H;
+    q[k] = v;
+  }
+}
+
+static void hdTriangle(const OScreenV* a, const OScreenV* b, const OScreenV* c, uint32_t W, uint32_t H,
+                       float* depth) {
+  if (!a->ok || !b->ok || !c->ok) return;
+  float area = hdEdge(a->x, a->y, b->x, b->y, c->x, c->y);
+  if (!(area != 0.0f) || !isfinite(area)) return;
+  float mnx = fminf(fminf(a->x, b->x), c->x), mxx = fmaxf(fmaxf(a->x, b->x), c->x);
+  float mny = fminf(fminf(a->y, b->y), c->y), mxy = fmaxf(fmaxf(a->y, b->y), c->y);
+  if (!(mxx >= 0.5f && mxy >= 0.5f && mnx <= (float)W - 0.5f && mny <= (float)H - 0.5f)) return;
+  int x0 = (int)fmaxf(ceilf(mnx - 0.5f), 0.0f), y0 = (int)fmaxf(ceilf(mny - 0.5f), 0.0f);
+  int x1 = (int)fminf(floorf(mxx - 0.5f), (float)W - 1.0f), y1 = (int)fminf(floorf(mxy - 0.5f), (float)H - 1.0f);
+  float aa = fabsf(area);
+  for (int y = y0; y <= y1; y++)
+    for (int x = x0; x <= x1; x++) {
+      float px = (float)x + 0.5f, py = (float)y + 0.5f;
+      float w0 = hdEdge(b->x, b->y, c->x, c->y, px, py);
+      float w1 = hdEdge(c->x, c->y, a->x, a->y, px, py);
+      float w2 = hdEdge(a->x, a->y, b->x, b->y, px, py);
+      if (area < 0.0f) { w0 = -w0; w1 = -w1; w2 = -w2; }
+      if (!(w0 >= 0.0f && w1 >= 0.0f && w2 >= 0.0f)) continue;
+      float z = (w0 / aa) * a->z + (w1 / aa) * b->z + (w2 / aa) * c->z;
+      if (!(z >= 0.0f && z <= 1.0f)) continue;
+      z = z + 0.0f;
+      float* d = depth + (size_t)y * W + x;
+      if (z < *d) *d = z;
+    }
+}
+
+/* depth: W*H f32, the scene depth on entry, with the hair drawn on exit */
+EXPORT void oracle_hair_depth(const void* uniforms, const void* hairData, const float* positions,
+                              const float* tangents, uint32_t strandsToRender, float* depth) {
+  const ORenderUniforms* U = (const ORenderUniforms*)uniforms;
+  const OHairData* HD = (const OHairData*)hairData;
+  uint32_t W = f2u(U->viewport.x), H = f2u(U->viewport.y);
+  uint32_t P = HD->pointsPerStrand, S = HD->strandsCount;
+  uint32_t nStrands = strandsToRender < S ? strandsToRender : S;
+  for (uint32_t strand = 0; strand < nStrands; strand++)
+    for (uint32_t seg = 0; seg + 1u < P; seg++) {
+      OScreenV q[4];
+      hdQuad(U, positions, tangents, P, strand, seg, q);
+      hdTriangle(&q[0], &q[1], &q[2], W, H, depth);
+      hdTriangle(&q[2], &q[1], &q[3], W, H, depth);
+    }
+}
+
 EXPORT void oracle_shading(const OracleConfig* cfg, const void* uniforms, const void* hairData,
                            const float* positions, const float* tangents, const float* depth,
                            const float* ao, uint32_t aoW, uint32_t aoH,

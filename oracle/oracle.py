@@ -72,6 +72,7 @@ def _declare(lib):
     lib.oracle_sim_integrate.argtypes = [P, P, P, P, P, P, P, P, P, P, U]
     lib.oracle_grid_post_sim.argtypes = [P, P, P, P, P, P]
     lib.oracle_shading.argtypes = [P, P, P, P, P, P, P, U, U, P, U, P]
+    lib.oracle_hair_depth.argtypes = [P, P, P, P, U, P]
     lib.oracle_sample_sdf.argtypes = [P, U, P, P, P]
     lib.oracle_sample_sdf.restype = ctypes.c_float
     lib.oracle_f32_to_f16.argtypes = [ctypes.c_float]
@@ -190,6 +191,15 @@ def grid_post_sim(cfg, sim_uniforms: bytes, hair_data: bytes, prev, now):
     c = cfg.to_c()
     u, h = _Bytes(sim_uniforms), _Bytes(hair_data)
     lib.oracle_grid_post_sim(_p(c), u.ptr, h.ptr, _p(_f32(prev)), _p(_f32(now)), _p(out))
+    return out
+
+
+def hair_depth(uniforms: bytes, hair_data: bytes, positions, tangents, strands_to_render, scene_depth):
+    """HwHairPass's depth: scene_depth (W*H) with the hair drawn over it."""
+    lib = load()
+    out = np.array(scene_depth, dtype=np.float32, copy=True).reshape(-1)
+    u, h = _Bytes(uniforms), _Bytes(hair_data)
+    lib.oracle_hair_depth(u.ptr, h.ptr, _p(_f32(positions)), _p(_f32(tangents)), strands_to_render, _p(out))
     return out
 
 

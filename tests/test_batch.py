@@ -59,11 +59,12 @@ def _compare(a, b, r: Renderer, frame):
     assert err <= 1.0 / 255.0, f"{tag}: pixel error {err:.4g}"
 
 
-def test_frame_matches_pass_by_pass():
+@pytest.mark.parametrize("hair_depth", [False, True])
+def test_frame_matches_pass_by_pass(hair_depth):
     insts = _instances()
     for inst in insts:
-        ref = Renderer(inst, 0)
-        nat = Renderer(inst, 0)
+        ref = Renderer(inst, 0, hair_depth=hair_depth)
+        nat = Renderer(inst, 0, hair_depth=hair_depth)
         ref.before_first_frame()
         nat.before_first_frame()
         for f in range(3):
@@ -71,6 +72,8 @@ def test_frame_matches_pass_by_pass():
             nat.frame_native()
             torch.cuda.synchronize()
             _compare(_state(ref), _state(nat), ref, f)
+            if hair_depth:
+                assert np.array_equal(ref.hair_depth.cpu().numpy(), nat.hair_depth.cpu().numpy()), f"frame {f}"
 
 
 def _batch_vs_alone(insts, frames, profile_frame=None, groups=1, pipeline=False):
@@ -89,7 +92,7 @@ def _batch_vs_alone(insts, frames, profile_frame=None, groups=1, pipeline=False)
         if f == profile_frame:  # pass by pass on the context's stream, timed
             n = len(batch.renderers)
             arr = (HfbInstance * n)(*[r.instance() for r in batch.renderers])
-            pm = (ctypes.c_float * 8)()
+            pm = (ctypes.c_float * 9)()
             ctx.call("hfb_frame_batch_profile", arr, n, pm)
             for r, inst in zip(batch.renderers, arr):
                 r.after_native_frame(inst)
@@ -120,6 +123,26 @@ def test_frame_batch_many_small_instances(groups):
                                      width=int(rng.choice([128, 256])), height=int(rng.choice([128, 192])), **common)
              for _ in range(12)]
     _batch_vs_alone(insts, 3, groups=groups)
+
+
+def test_frame_batch_with_hair_depth():
+    """Instances that draw the hair depth after the fine pass and shade with
+    it: the batched frames equal each instance's frames alone."""
+    insts = _instances()
+    alone = [Renderer(inst, 0, hair_depth=True) for inst in insts]
+    ctx = Context(insts[0].cfg.to_c(), 0)
+    batch = BatchRenderer([Renderer(inst, 0, ctx=ctx, hair_depth=True) for inst in insts])
+    for r in alone:
+        r.before_first_frame()
+    batch.before_first_frame()
+    for f in range(3):
+        for r in alone:
+            r.frame()
+        batch.frame()
+        torch.cuda.synchronize()
+        for ra, rb in zip(alone, batch.renderers):
+            _compare(_state(ra), _state(rb), ra, f)
+            assert np.array_equal(ra.hair_depth.cpu().numpy(), rb.hair_depth.cpu().numpy()), f"frame {f}: depth"
 
 
 def test_frame_batch_pipelined_each_frame():

@@ -466,3 +466,47 @@ def test_invalid_arguments_return_errors():
         ctx.call("hfb_grid_post_sim", None, None, misaligned.data_ptr(), misaligned.data_ptr(),
                  misaligned.data_ptr())
     ctx.sync()  # the context stays usable
+
+
+@pytest.mark.parametrize("kw,lod", [(dict(), 100.0), (dict(width=1000, height=700), 70.0),
+                                    (dict(strands=300, fiber_radius=0.02), 100.0)])
+def test_hair_depth_bit_exact(oracle, kw, lod):
+    """HwHairPass's depth (hfb_hair_depth) against the oracle, bit for bit:
+    the 2,000-strand case, partial edge tiles with LOD, and quads wide enough
+    (fiber radius 0.02) that their triangles take the block-per-triangle path."""
+    from hairfb.passes import HwHairPass
+    inst = small_instance(**kw)
+    fr = frame_of(inst)
+    ctx = _ctx(inst)
+    hair = HairObject(inst.hair, inst.cfg.shading_points)
+    hair.lod_render_percent = lod
+    rb = RasterBuffers(ctx, inst.width, inst.height)
+    scene = torch.as_tensor(inst.scene_depth).cuda()
+    out = torch.empty_like(scene)
+    HwHairPass(ctx).cmd_draw_hair_depth(fr.uniforms, hair, scene, out, rb)
+    ctx.sync()
+    o = oracle.hair_depth(fr.uniforms, inst.hair.hair_data, inst.hair.asset.positions, inst.hair.tangents,
+                          hair.rendered_strand_count(), inst.scene_depth)
+    g = out.cpu().numpy()
+    assert (o < inst.scene_depth).sum() > 100, "the hair covers nothing: the case does not test"
+    assert np.array_equal(g.view(np.uint32), o.view(np.uint32)), f"{int((g != o).sum())} pixels differ"
+
+
+def test_shading_reads_the_hair_depth(oracle):
+    """A frame with the hair depth prepass: the depth it leaves is the
+    oracle's for the frame's positions, and the shading computed from it
+    matches the oracle's shading on that depth."""
+    from hairfb.renderer import Renderer
+    inst = small_instance(strands=1500)
+    r = Renderer(inst, 0, hair_depth=True)
+    r.before_first_frame()
+    r.frame()
+    torch.cuda.synchronize()
+    pos = r.hair.positions.cpu().numpy()
+    tan = r.hair.tangents.cpu().numpy()
+    o = oracle.hair_depth(r.uniforms, inst.hair.hair_data, pos, tan, inst.hair.asset.strands, inst.scene_depth)
+    assert (o < inst.scene_depth).sum() > 100
+    assert np.array_equal(r.hair_depth.cpu().numpy().view(np.uint32), o.view(np.uint32))
+    osh = oracle.shading(inst.cfg, r.uniforms, inst.hair.hair_data, pos, tan, o, inst.hair.asset.strands)
+    g = r.hair.shading.cpu().numpy()
+    assert np.allclose(g, osh, rtol=1e-5, atol=1e-5), float(np.abs(g - osh).max())
