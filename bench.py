@@ -70,7 +70,42 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--serve-frames", type=int, default=60,
                     help="frames per session of the serving run in the batched64 line (0 = none)")
+    ap.add_argument("--capture-frames", type=int, default=0,
+                    help="profiler runs: set up the workload, render this many frames (batched64: batched "
+                         "frames at --tile-size/--depth-bins, no tuning), print 'ok' and exit; no timing")
+    ap.add_argument("--tile-size", type=int, default=16)
+    ap.add_argument("--depth-bins", type=int, default=8)
     return ap.parse_args()
+
+
+def capture(args):
+    """A fixed number of frames for an ncu capture: the workload's renderers
+    (hair depth on), the first-frame setup, then `--capture-frames` frames."""
+    import dataclasses
+    import torch
+    from hairfb import renderer as R
+    from hairfb.lib import Context
+    if args.workload == "batched64":
+        insts = batched_instances(seed=0)
+        cfg = dataclasses.replace(insts[0].cfg, tile_size=args.tile_size, tile_depth_bins=args.depth_bins)
+        insts = [dataclasses.replace(i, cfg=cfg) for i in insts]
+        ctx = Context(cfg.to_c(), 0)
+        rs = [R.Renderer(i, 0, ctx=ctx, hair_depth=True) for i in insts]
+        for r in rs:
+            r.before_first_frame()
+        b = R.BatchRenderer(rs)
+        for _ in range(args.capture_frames):
+            b.frame()
+    else:
+        inst = make_instance(args.workload, seed=0)
+        r = R.Renderer(inst, 0, hair_depth=True)
+        r.before_first_frame()
+        for _ in range(args.capture_frames):
+            r.frame_native()
+        ctx = r.ctx
+    ctx.sync()
+    print(f"ok: {args.capture_frames} frames of {args.workload}, "
+          f"{torch.cuda.max_memory_allocated() / 1e9:.2f} GB allocated by torch", flush=True)
 
 
 def make_instance(name, seed):
@@ -105,6 +140,8 @@ def algorithmic_bytes(inst, K):
         "sort": T * 4 + (4 + T) * 4 + cfg.sort_buckets * 8,
         # lists read (8), heads (16), shading read, depth read, result write
         "fine": Npt * 32 + S * SP * 16 + W * H * (4 + 16) + K * 8 + T * B * 16,
+        # positions + tangents, scene depth read and hair depth written
+        "hair_depth": Npt * 32 + W * H * 8,
         "shading": Npt * 32 + S * SP * (16 + 8),
     }
 
@@ -187,7 +224,8 @@ def cpu_frame_runner(inst):
     su0 = UN.pack_sim_uniforms(inst.sim, inst.scene.model_matrix, inst.scene.sdf_bounds,
                                inst.scene.grid_bounds, 0, wind_dir=inst.wind_dir)
     st["dv"] = O.grid_post_sim(cfg, su0, hb.hair_data, st["prev"], st["now"])
-    st["shade"] = O.shading(cfg, u, hb.hair_data, st["now"], hb.tangents, inst.scene_depth, hb.asset.strands)
+    hd = O.hair_depth(u, hb.hair_data, st["now"], hb.tangents, hb.asset.strands, inst.scene_depth)
+    st["shade"] = O.shading(cfg, u, hb.hair_data, st["now"], hb.tangents, hd, hb.asset.strands)
 
     def frame():
         f = st["f"]
@@ -204,8 +242,8 @@ def cpu_frame_runner(inst):
         _, tl = O.tile_sort(cfg, inst.width, inst.height, cnt)
         O.fine_pass(cfg, u, hb.hair_data, st["now"], hb.tangents, st["shade"], inst.scene_depth, tiles,
                     segs, tl, inst.width, inst.height)
-        st["shade"] = O.shading(cfg, u, hb.hair_data, st["now"], hb.tangents, inst.scene_depth,
-                                hb.asset.strands)
+        hd = O.hair_depth(u, hb.hair_data, st["now"], hb.tangents, hb.asset.strands, inst.scene_depth)
+        st["shade"] = O.shading(cfg, u, hb.hair_data, st["now"], hb.tangents, hd, hb.asset.strands)
         st["f"] = f + 1
     return frame
 
@@ -246,10 +284,10 @@ def run_ours(args, rank, world, dist):
     torch.cuda.set_stream(stream)
     ctx = Context(inst.cfg.to_c(), dev)
     ctx.set_stream(stream)
-    r = R.Renderer(inst, ctx=ctx)
+    r = R.Renderer(inst, ctx=ctx, hair_depth=True)
     r.before_first_frame()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    names = ["grid_pre", "integrate", "grid_post", "clear", "tiles", "sort", "fine", "shading"]
+    names = ["grid_pre", "integrate", "grid_post", "clear", "tiles", "sort", "fine", "hair_depth", "shading"]
 
     def timed_frame(ev):
         su = r.sim_uniforms(r.frame_idx)
@@ -268,8 +306,10 @@ def run_ours(args, rank, world, dist):
         ev[6].record(stream)
         r.fine.cmd_rasterize_slices_hair(r.uniforms, r.hair, r.scene_depth, r.rb)
         ev[7].record(stream)
-        r.shading.cmd_compute_shading_points(r.uniforms, r.hair, r.shading_depth)
+        r.hw_hair.cmd_draw_hair_depth(r.uniforms, r.hair, r.scene_depth, r.hair_depth, r.rb)
         ev[8].record(stream)
+        r.shading.cmd_compute_shading_points(r.uniforms, r.hair, r.shading_depth)
+        ev[9].record(stream)
         r.frame_idx += 1
 
     for _ in range(args.warmup):
@@ -284,10 +324,10 @@ def run_ours(args, rank, world, dist):
         torch.cuda.synchronize()
         for _ in range(args.steps):
             flush.fill_(1.0)  # L2 flush, outside the timed events
-            ev = [torch.cuda.Event(enable_timing=True) for _ in range(9)]
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(names) + 1)]
             timed_frame(ev)
             torch.cuda.synchronize()
-            frame_ms.append(ev[0].elapsed_time(ev[8]))
+            frame_ms.append(ev[0].elapsed_time(ev[len(names)]))
             for i, n in enumerate(names):
                 pass_ms[n].append(ev[i].elapsed_time(ev[i + 1]))
     launches = ctx.counters()["launches"] - launches0
@@ -316,6 +356,7 @@ def run_ours(args, rank, world, dist):
         r.tiles.cmd_draw_hair_to_tiles(u, r.hair, depth_d, r.rb)
         r.sort.cmd_sort_hair_tiles(r.rb)
         r.fine.cmd_rasterize_slices_hair(u, r.hair, depth_d, r.rb)
+        r.hw_hair.cmd_draw_hair_depth(u, r.hair, depth_d, r.hair_depth, r.rb)
         r.shading.cmd_compute_shading_points(u, r.hair, r.shading_depth)
         r.frame_idx += 1
         ctx.call("hfb_buffer_download", img_h.data_ptr(), r.rb.rb.rasterizerResult, img_h.numel() * 4)
@@ -368,7 +409,7 @@ def run_batched(args, rank, world, dist):
     base = insts[0].cfg
     ctx0 = Context(base.to_c(), dev)
     ctx0.set_stream(stream)
-    rs = [R.Renderer(i, dev, ctx=ctx0) for i in insts]
+    rs = [R.Renderer(i, dev, ctx=ctx0, hair_depth=True) for i in insts]
     for r in rs:
         r.before_first_frame()
     torch.cuda.synchronize()
@@ -538,8 +579,13 @@ def report_batched(args, res, world, dist):
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
-        # measured at one pass config; reported only when the tuner chose it
-        traffic = json.load(open(tp)).get(f"batched64:ts{cfg.tile_size}_b{cfg.tile_depth_bins}:{dominant}")
+        # measured at one pass config; the raster passes' figure is reported only
+        # when the tuner chose that config, the simulation's does not depend on it
+        tj = json.load(open(tp))
+        traffic = tj.get(f"batched64:ts{cfg.tile_size}_b{cfg.tile_depth_bins}:{dominant}")
+        if traffic is None and dominant in ("grid_pre", "integrate", "grid_post"):
+            traffic = next((v for k, v in tj.items() if k.startswith("batched64:") and k.endswith(":" + dominant)),
+                           None)
     srt = sorted(res["step_ms"])
     q = lambda v, x: v[min(len(v) - 1, int(round(x * (len(v) - 1))))]  # noqa: E731
     psrt = sorted(res["plain_frame_ms"])
@@ -608,6 +654,9 @@ def main():
             dist.init_process_group("nccl")
 
     wl = args.workload
+    if args.capture_frames > 0:
+        capture(args)
+        return
     if args.impl == "reference" and wl == "batched64":
         insts = batched_instances(seed=0)
         frames = [cpu_frame_runner(i) for i in insts]

@@ -204,7 +204,7 @@ uint32_t batchBlocks(const HfbConfig& cfg, BatchKind k, const BatchInst& I) {
     case BK_SCHEDULE: return 1u;
     case BK_SHADING: return divCeil(I.S * cfg.shadingPoints, 128u);
     case BK_DEPTH_COPY: return I.hairDepth ? divCeil((uint32_t)(((size_t)I.W * I.H * 4 + CLEAR_CHUNK - 1) / CLEAR_CHUNK), 1u) : 0u;
-    case BK_HAIR_DEPTH: return I.hairDepth ? divCeil(nSeg, 256u) : 0u;
+    case BK_HAIR_DEPTH: return I.hairDepth && I.P > 1u ? hairDepthBlocks(I.S * I.P) : 0u;
     default: return 0u;
   }
 }

@@ -30,8 +30,29 @@
 namespace hfb {
 namespace {
 
-constexpr uint32_t HD_THREADS = 256;
-constexpr uint32_t HD_BIG_AREA = 1024;  // pixels: larger triangles are drawn by a whole block
+constexpr uint32_t HD_THREADS = 256;             // points per block: each point's two vertices once
+constexpr uint32_t HD_SEGS = HD_THREADS - 1u;    // segment starts per block (the last point is shared)
+constexpr uint32_t HD_BIG_AREA = 1024;           // pixels: larger triangles are drawn by a whole block
+constexpr uint32_t HD_VIEW_FLOATS = 35;
+
+// The uniforms the pass reads: modelViewMat, projMatrix, fiberRadius, viewport.
+struct HdView {
+  float mv[16], pr[16];
+  float radius, W, H;
+};
+static_assert(sizeof(HdView) == HD_VIEW_FLOATS * 4, "HdView layout");
+
+__host__ __device__ inline float hdViewField(const HfbUniforms& U, uint32_t k) {
+  return k < 16u ? U.modelViewMat.m[k] : k < 32u ? U.projMatrix.m[k - 16u]
+                                        : k == 32u ? U.fiberRadius : k == 33u ? U.viewport.x : U.viewport.y;
+}
+
+inline HdView hdView(const HfbUniforms& U) {
+  HdView v;
+  float* f = reinterpret_cast<float*>(&v);
+  for (uint32_t k = 0; k < HD_VIEW_FLOATS; k++) f[k] = hdViewField(U, k);
+  return v;
+}
 
 struct ScreenV {
   float x, y, z;
@@ -46,31 +67,35 @@ __device__ __forceinline__ float edgeFn(float ax, float ay, float bx, float by, 
   return fsub(fmul(fsub(bx, ax), fsub(py, ay)), fmul(fsub(by, ay), fsub(px, ax)));
 }
 
-// The four screen-space vertices of segment (strand, seg).
-__device__ __forceinline__ void segmentQuad(const HfbUniforms& U, const float4* __restrict__ pos,
-                                            const float4* __restrict__ tan, uint32_t P, uint32_t strand,
-                                            uint32_t seg, float W, float H, ScreenV (&q)[4]) {
-#pragma unroll
-  for (uint32_t k = 0; k < 4u; k++) {
-    const size_t i = (size_t)strand * P + seg + (k >> 1);
-    const float4 p = __ldg(HFB_G(&pos[i]));
-    const float4 t = __ldg(HFB_G(&tan[i]));
-    const f4 pVS = m4v(U.modelViewMat.m, mk4(p.x, p.y, p.z, 1.0f));
-    const f4 tVS = m4v(U.modelViewMat.m, mk4(t.x, t.y, t.z, 1.0f));
-    const f3 c = cross3(xyz(tVS), mk3(0.0f, 0.0f, 1.0f));
-    const f3 right = dot3(c, c) >= 1e-7f ? norm3(c) : mk3(0.0f, 0.0f, 0.0f);  // safeNormalize3
-    const f3 th = mul3s(right, U.fiberRadius);
-    const f3 e = (k & 1u) ? sub3(xyz(pVS), th) : add3(xyz(pVS), th);
-    const f4 clip = m4v(U.projMatrix.m, mk4(e.x, e.y, e.z, 1.0f));
-    ScreenV v;
-    v.ok = clip.w > 0.0f;
-    const float nx = clip.x / clip.w, ny = clip.y / clip.w;
-    v.z = clip.z / clip.w;
-    v.x = fmul(fadd(fmul(nx, 0.5f), 0.5f), W);
-    v.y = fmul(fsub(0.5f, fmul(ny, 0.5f)), H);
-    q[k] = v;
-  }
+__device__ __forceinline__ ScreenV projectScreen(const HdView& V, f3 e) {
+  const f4 clip = m4v(V.pr, mk4(e.x, e.y, e.z, 1.0f));
+  ScreenV v;
+  v.ok = clip.w > 0.0f;
+  const float nx = clip.x / clip.w, ny = clip.y / clip.w;
+  v.z = clip.z / clip.w;
+  v.x = fmul(fadd(fmul(nx, 0.5f), 0.5f), V.W);
+  v.y = fmul(fsub(0.5f, fmul(ny, 0.5f)), V.H);
+  return v;
 }
+
+// The two vertices of point i: in view space (modelViewMat), moved by
+// fiberRadius along safeNormalize(cross(tangentVS, (0, 0, 1))) -- plus for
+// `a` (even vertex ids), minus for `b` (odd ones) -- and projected.
+__device__ __forceinline__ void pointPair(const HdView& V, const float4* __restrict__ pos,
+                                          const float4* __restrict__ tan, size_t i, ScreenV& a, ScreenV& b) {
+  const float4 p = __ldg(HFB_G(&pos[i]));
+  const float4 t = __ldg(HFB_G(&tan[i]));
+  const f4 pVS = m4v(V.mv, mk4(p.x, p.y, p.z, 1.0f));
+  const f4 tVS = m4v(V.mv, mk4(t.x, t.y, t.z, 1.0f));
+  const f3 c = cross3(xyz(tVS), mk3(0.0f, 0.0f, 1.0f));
+  const f3 right = dot3(c, c) >= 1e-7f ? norm3(c) : mk3(0.0f, 0.0f, 0.0f);  // safeNormalize3
+  const f3 th = mul3s(right, V.radius);
+  a = projectScreen(V, add3(xyz(pVS), th));
+  b = projectScreen(V, sub3(xyz(pVS), th));
+}
+
+__device__ __forceinline__ float4 packV(const ScreenV& v) { return make_float4(v.x, v.y, v.z, v.ok ? 1.0f : 0.0f); }
+__device__ __forceinline__ ScreenV unpackV(float4 f) { return {f.x, f.y, f.z, f.w != 0.0f}; }
 
 // Pixel range [x0, x1] x [y0, y1] whose centres lie in the triangle's box;
 // false if the triangle is not drawn at all.
@@ -103,59 +128,73 @@ __device__ __forceinline__ void triPixel(const Tri& t, float area, uint32_t W, i
   atomicMin(HFB_G(&depth[(size_t)y * W + x]), __float_as_uint(fadd(z, 0.0f)));  // -0 -> +0
 }
 
-// One thread per segment: both triangles in the thread, or onto the big
-// list (entries segment << 1 | triangle; capacity `bigCap`, overflow drawn
-// in the thread).
-__device__ __forceinline__ void hairDepthBody(const HfbUniforms& U, uint32_t P, uint32_t nStrands,
-                                              const float4* __restrict__ pos, const float4* __restrict__ tan,
-                                              unsigned* __restrict__ depth, uint32_t* __restrict__ big,
-                                              uint32_t bigCap, uint32_t gid) {
-  const uint32_t segs = P - 1u, nSeg = nStrands * segs;
-  if (gid >= nSeg) return;
-  const uint32_t W = f2u(U.viewport.x), H = f2u(U.viewport.y);
-  const uint32_t strand = gid / segs, seg = gid - strand * segs;
-  ScreenV q[4];
-  segmentQuad(U, pos, tan, P, strand, seg, U.viewport.x, U.viewport.y, q);
-#pragma unroll
-  for (uint32_t tr = 0; tr < 2u; tr++) {
-    Tri t;
-    t.v[0] = tr ? q[2] : q[0];
-    t.v[1] = q[1];
-    t.v[2] = tr ? q[3] : q[2];
-    float area;
-    int x0, x1, y0, y1;
-    if (!triBox(t, W, H, area, x0, x1, y0, y1)) continue;
-    const uint64_t px = (uint64_t)(x1 - x0 + 1) * (uint64_t)(y1 - y0 + 1);
-    if (px > HD_BIG_AREA) {
-      const uint32_t slot = atomicAdd(HFB_G(&big[0]), 1u);
-      if (slot < bigCap) {
-        *HFB_G(&big[1u + slot]) = (gid << 1) | tr;
-        continue;
-      }
-    }
-    for (int y = y0; y <= y1; y++)
-      for (int x = x0; x <= x1; x++) triPixel(t, area, W, x, y, depth);
+// Triangle tr of the segment whose quad is q: (0, 1, 2) or (2, 1, 3).
+__device__ __forceinline__ Tri segTri(const ScreenV (&q)[4], uint32_t tr) {
+  Tri t;
+  t.v[0] = tr ? q[2] : q[0];
+  t.v[1] = q[1];
+  t.v[2] = tr ? q[3] : q[2];
+  return t;
+}
+
+// One block of HD_THREADS points starting at point blk * HD_SEGS: every
+// thread projects its point's two vertices into shared memory, then each of
+// the first HD_SEGS threads draws the segment from its point to the next
+// (when that point is not its strand's last) -- both triangles in the
+// thread, or onto the big list (entries point << 1 | triangle; capacity
+// `bigCap`, overflow drawn in the thread).  Called by every thread of the
+// block.
+__device__ __forceinline__ void hairDepthBlock(const HdView& V, uint32_t P, uint32_t nPts,
+                                               const float4* __restrict__ pos, const float4* __restrict__ tan,
+                                               unsigned* __restrict__ depth, uint32_t* __restrict__ big,
+                                               uint32_t bigCap, uint32_t blk, float4 (*sv)[2]) {
+  const uint32_t pt = blk * HD_SEGS + threadIdx.x;
+  if (pt < nPts) {
+    ScreenV a, b;
+    pointPair(V, pos, tan, pt, a, b);
+    sv[threadIdx.x][0] = packV(a);
+    sv[threadIdx.x][1] = packV(b);
   }
+  __syncthreads();
+  if (threadIdx.x < HD_SEGS && pt + 1u < nPts && pt % P != P - 1u) {
+    const uint32_t W = f2u(V.W), H = f2u(V.H);
+    const ScreenV q[4] = {unpackV(sv[threadIdx.x][0]), unpackV(sv[threadIdx.x][1]), unpackV(sv[threadIdx.x + 1][0]),
+                          unpackV(sv[threadIdx.x + 1][1])};
+#pragma unroll
+    for (uint32_t tr = 0; tr < 2u; tr++) {
+      const Tri t = segTri(q, tr);
+      float area;
+      int x0, x1, y0, y1;
+      if (!triBox(t, W, H, area, x0, x1, y0, y1)) continue;
+      const uint64_t px = (uint64_t)(x1 - x0 + 1) * (uint64_t)(y1 - y0 + 1);
+      if (px > HD_BIG_AREA && pt < 0x80000000u) {
+        const uint32_t slot = atomicAdd(HFB_G(&big[0]), 1u);
+        if (slot < bigCap) {
+          *HFB_G(&big[1u + slot]) = (pt << 1) | tr;
+          continue;
+        }
+      }
+      for (int y = y0; y <= y1; y++)
+        for (int x = x0; x <= x1; x++) triPixel(t, area, W, x, y, depth);
+    }
+  }
+  __syncthreads();  // sv is rewritten by the block's next points
 }
 
 // The big list, one block per triangle.
-__device__ __forceinline__ void hairDepthBigBody(const HfbUniforms& U, uint32_t P, const float4* __restrict__ pos,
+__device__ __forceinline__ void hairDepthBigBody(const HdView& V, const float4* __restrict__ pos,
                                                  const float4* __restrict__ tan, unsigned* __restrict__ depth,
                                                  const uint32_t* __restrict__ big, uint32_t bigCap, uint32_t blk,
                                                  uint32_t nblk) {
   const uint32_t n = min(*HFB_G(&big[0]), bigCap);
-  const uint32_t W = f2u(U.viewport.x), H = f2u(U.viewport.y);
-  const uint32_t segs = P - 1u;
+  const uint32_t W = f2u(V.W), H = f2u(V.H);
   for (uint32_t e = blk; e < n; e += nblk) {
     const uint32_t ent = *HFB_G(&big[1u + e]);
-    const uint32_t gid = ent >> 1, tr = ent & 1u;
-    const uint32_t strand = gid / segs, seg = gid - strand * segs;
+    const uint32_t pt = ent >> 1, tr = ent & 1u;
     ScreenV q[4];
-    segmentQuad(U, pos, tan, P, strand, seg, U.viewport.x, U.viewport.y, q);
-    Tri t;
-    t.v[0] = tr ? q[2] : q[0];
-    t.v[1] = q[1];
-    t.v[2] = tr ? q[3] : q[2];
+    pointPair(V, pos, tan, pt, q[0], q[1]);
+    pointPair(V, pos, tan, (size_t)pt + 1u, q[2], q[3]);
+    const Tri t = segTri(q, tr);
     float area;
     int x0, x1, y0, y1;
     if (!triBox(t, W, H, area, x0, x1, y0, y1)) continue;
@@ -166,44 +205,63 @@ __device__ __forceinline__ void hairDepthBigBody(const HfbUniforms& U, uint32_t 
 }
 
 __global__ void __launch_bounds__(HD_THREADS)
-hairDepthKernel(const HfbUniforms U, uint32_t P, uint32_t nStrands, const float4* __restrict__ pos,
+hairDepthKernel(const HdView V, uint32_t P, uint32_t nPts, const float4* __restrict__ pos,
                 const float4* __restrict__ tan, unsigned* __restrict__ depth, uint32_t* __restrict__ big,
                 uint32_t bigCap) {
-  hairDepthBody(U, P, nStrands, pos, tan, depth, big, bigCap, blockIdx.x * blockDim.x + threadIdx.x);
+  __shared__ float4 sv[HD_THREADS][2];
+  hairDepthBlock(V, P, nPts, pos, tan, depth, big, bigCap, blockIdx.x, sv);
 }
 
 __global__ void __launch_bounds__(HD_THREADS)
-hairDepthBigKernel(const HfbUniforms U, uint32_t P, const float4* __restrict__ pos, const float4* __restrict__ tan,
+hairDepthBigKernel(const HdView V, const float4* __restrict__ pos, const float4* __restrict__ tan,
                    unsigned* __restrict__ depth, const uint32_t* __restrict__ big, uint32_t bigCap) {
-  hairDepthBigBody(U, P, pos, tan, depth, big, bigCap, blockIdx.x, gridDim.x);
+  hairDepthBigBody(V, pos, tan, depth, big, bigCap, blockIdx.x, gridDim.x);
+}
+
+// The instance's HdView into shared memory (every thread calls; synced).
+__device__ __forceinline__ void loadView(const HfbUniforms& U, HdView& V) {
+  __syncthreads();  // the previous instance's view is no longer read
+  if (threadIdx.x < HD_VIEW_FLOATS) reinterpret_cast<float*>(&V)[threadIdx.x] = hdViewField(U, threadIdx.x);
+  __syncthreads();
 }
 
 // ---- batched: persistent over every instance ----
 __global__ void __launch_bounds__(HD_THREADS) hairDepthBatch(BatchView b) {
+  __shared__ float4 sv[HD_THREADS][2];
+  __shared__ HdView V;
   const uint32_t n = b.hdr->n;
   const uint32_t* row = b.prefix + BK_HAIR_DEPTH * (BATCH_MAX + 1);
   const uint32_t total = row[n];
+  uint32_t cur = 0xFFFFFFFFu;
   for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
     const uint32_t i = batchFind(row, n, v);
     const BatchInst& I = b.insts[i];
-    uint32_t* big = reinterpret_cast<uint32_t*>(I.scratch);
-    hairDepthBody(I.U, I.P, min(I.strandsToRender, I.S), I.posNew, I.tan, reinterpret_cast<unsigned*>(I.hairDepth),
-                  big, hairDepthBigCap(I.scratchBytes), (v - row[i]) * HD_THREADS + threadIdx.x);
+    if (i != cur) {
+      loadView(I.U, V);
+      cur = i;
+    }
+    hairDepthBlock(V, I.P, min(I.strandsToRender, I.S) * I.P, I.posNew, I.tan,
+                   reinterpret_cast<unsigned*>(I.hairDepth), reinterpret_cast<uint32_t*>(I.scratch),
+                   hairDepthBigCap(I.scratchBytes), v - row[i], sv);
   }
 }
 
 __global__ void __launch_bounds__(HD_THREADS) hairDepthBigBatch(BatchView b) {
+  __shared__ HdView V;
   const uint32_t n = b.hdr->n;
   for (uint32_t i = 0; i < n; i++) {  // every block takes a share of each instance's list
     const BatchInst& I = b.insts[i];
     if (!I.hairDepth) continue;
-    hairDepthBigBody(I.U, I.P, I.posNew, I.tan, reinterpret_cast<unsigned*>(I.hairDepth),
+    loadView(I.U, V);
+    hairDepthBigBody(V, I.posNew, I.tan, reinterpret_cast<unsigned*>(I.hairDepth),
                      reinterpret_cast<const uint32_t*>(I.scratch), hairDepthBigCap(I.scratchBytes), blockIdx.x,
                      gridDim.x);
   }
 }
 
 }  // namespace
+
+uint32_t hairDepthBlocks(uint32_t points) { return divCeil(points, HD_SEGS); }
 
 cudaError_t launchHairDepth(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, const float* pos, const float* tan,
                             uint32_t strandsToRender, const float* sceneDepth, float* hairDepth,
@@ -214,16 +272,16 @@ cudaError_t launchHairDepth(HfbCtx* c, const HfbUniforms& u, const HfbHairData& 
   if (e == cudaSuccess) e = cudaMemsetAsync(rb.scratch, 0, 4, c->stream);  // the big list's count
   if (e != cudaSuccess) return e;
   const uint32_t nStrands = min(strandsToRender, h.strandsCount);
-  const uint32_t nSeg = nStrands * (h.pointsPerStrand - 1u);
-  if (nSeg == 0) return cudaSuccess;
+  const uint32_t nPts = nStrands * h.pointsPerStrand;
+  if (h.pointsPerStrand < 2u || nPts == 0) return cudaSuccess;
   const uint32_t cap = hairDepthBigCap(rb.scratchBytes);
   uint32_t* big = reinterpret_cast<uint32_t*>(rb.scratch);
-  hairDepthKernel<<<divCeil(nSeg, HD_THREADS), HD_THREADS, 0, c->stream>>>(
-      u, h.pointsPerStrand, nStrands, (const float4*)pos, (const float4*)tan, (unsigned*)hairDepth, big, cap);
+  const HdView V = hdView(u);
+  hairDepthKernel<<<hairDepthBlocks(nPts), HD_THREADS, 0, c->stream>>>(
+      V, h.pointsPerStrand, nPts, (const float4*)pos, (const float4*)tan, (unsigned*)hairDepth, big, cap);
   HFB_AFTER_LAUNCH(c, "hairDepthKernel");
-  hairDepthBigKernel<<<c->smCount * 4u, HD_THREADS, 0, c->stream>>>(u, h.pointsPerStrand, (const float4*)pos,
-                                                                    (const float4*)tan, (unsigned*)hairDepth, big,
-                                                                    cap);
+  hairDepthBigKernel<<<c->smCount * 4u, HD_THREADS, 0, c->stream>>>(V, (const float4*)pos, (const float4*)tan,
+                                                                    (unsigned*)hairDepth, big, cap);
   HFB_AFTER_LAUNCH(c, "hairDepthBigKernel");
   c->launches += 2;
   return cudaGetLastError();

@@ -296,6 +296,8 @@ cudaError_t launchBatchDepthCopy(HfbCtx* c, const BatchView& b);
 cudaError_t launchHairDepth(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, const float* pos, const float* tan,
                             uint32_t strandsToRender, const float* sceneDepth, float* hairDepth,
                             HfbRasterBuffers& rb);
+// Blocks of the hair depth pass over `points` points.
+uint32_t hairDepthBlocks(uint32_t points);
 __host__ __device__ inline uint32_t hairDepthBigCap(size_t bytes) {
   const size_t n = bytes / 4 > 1 ? bytes / 4 - 1 : 0;
   return (uint32_t)(n < 0x7FFFFFFFu ? n : 0x7FFFFFFFu);

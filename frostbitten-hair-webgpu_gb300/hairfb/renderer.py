@@ -85,6 +85,8 @@ class Renderer:
         the first shading."""
         su = self.sim_uniforms(0)
         self.grid_post.cmd_update_grids_after_sim(su, self.hair, self.grids)
+        if self.hair_depth is not None:  # updateResourcesForNextFrame: hwHair, then the shading
+            self.hw_hair.cmd_draw_hair_depth(self.uniforms, self.hair, self.scene_depth, self.hair_depth, self.rb)
         self.shading.cmd_compute_shading_points(self.uniforms, self.hair, self.shading_depth)
 
     def simulate(self) -> None:

@@ -160,8 +160,11 @@ class Server:
     """Sessions on one context (one pass config for all of them)."""
 
     def __init__(self, cfg: HairConfig, device: int = 0, budget_bytes: int = 150 << 30, stream=None,
-                 groups: int = 1, make_instance=None):
+                 groups: int = 1, make_instance=None, hair_depth: bool = True):
+        """hair_depth: each session's frame draws the hair depth for its
+        shading (the reference's frame); False shades with the scene depth."""
         self.cfg = cfg
+        self.hair_depth = hair_depth
         self.device = device
         self.ctx = Context(cfg.to_c(), device)
         if stream is not None:
@@ -182,13 +185,13 @@ class Server:
 
     def session_bytes(self, spec: SessionSpec) -> int:
         """Device memory of an admitted session: hair buffers, grids, SDF,
-        depth inputs and its raster buffers."""
+        scene (and hair) depth and its raster buffers."""
         c = self.cfg
         n = spec.strands * spec.points
         hair = n * 16 * 4 + n * 4 + spec.strands * c.shading_points * 16  # 3 positions + tangents, lengths, shading
         grids = 2 * 16 * c.grid_dims ** 3
         sdf = 4 * 32 ** 3
-        depth = 4 * spec.width * spec.height
+        depth = 4 * spec.width * spec.height * (2 if self.hair_depth else 1)
         tx, ty = -(-spec.width // c.tile_size), -(-spec.height // c.tile_size)
         T = tx * ty
         md = pool_records(spec)
@@ -199,7 +202,8 @@ class Server:
 
     def admit(self, s: Session, now: float) -> None:
         s.inst = self._make(s.spec)
-        s.renderer = Renderer(s.inst, self.device, ctx=self.ctx, max_drawn=pool_records(s.spec))
+        s.renderer = Renderer(s.inst, self.device, ctx=self.ctx, max_drawn=pool_records(s.spec),
+                              hair_depth=self.hair_depth)
         s.renderer.before_first_frame()
         s.admitted_s = now
         self.used += s.bytes

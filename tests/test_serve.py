@@ -51,7 +51,7 @@ def test_served_sessions_equal_sessions_alone():
             r = s.renderer
             final[s.spec.sid] = (r.hair.positions.cpu().numpy().copy(),
                                  r.grids.density_velocity.cpu().numpy().copy(),
-                                 r.rb.read_result()[4:].copy())
+                                 r.rb.read_result()[4:].copy(), r.hair.shading.cpu().numpy().copy())
 
     st = server.run(specs, frame_done)
     assert st.frames == sum(s.frames for s in specs)
@@ -61,14 +61,15 @@ def test_served_sessions_equal_sessions_alone():
     server.close()
 
     for sp in specs:
-        r = Renderer(factory(sp), 0, max_drawn=serve.pool_records(sp))
+        r = Renderer(factory(sp), 0, max_drawn=serve.pool_records(sp), hair_depth=True)
         r.before_first_frame()
         for _ in range(sp.frames):
             r.frame_native()
         torch.cuda.synchronize()
-        pos, dv, px = final[sp.sid]
+        pos, dv, px, shade = final[sp.sid]
         assert np.array_equal(r.hair.positions.cpu().numpy(), pos), f"session {sp.sid}: positions"
         assert np.array_equal(r.grids.density_velocity.cpu().numpy(), dv), f"session {sp.sid}: density grid"
+        assert np.abs(r.hair.shading.cpu().numpy() - shade).max() <= 1e-6, f"session {sp.sid}: shading"
         err = np.abs(r.rb.read_result()[4:] - px).max()
         assert err <= 1.0 / 255.0, f"session {sp.sid}: pixel error {err}"
         r.rb.close()
