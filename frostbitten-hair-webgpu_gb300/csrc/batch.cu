@@ -54,7 +54,7 @@ cudaError_t framePass(HfbCtx* c, HfbInstance* in, FramePass p) {
       return launchSimIntegrate(c, su, h, prev, now, in->positionsInitial, in->segmentLengths,
                                 in->densityVelocity, in->densityGradWind, in->sdf, in->sdfDims);
     case FP_GRID_POST:  // after the swap: "prev" = the old positions, "now" = the new ones
-      return launchGridPostSim(c, su, h, now, prev, in->densityVelocity);
+      return launchGridPostSim(c, su, h, now, prev, in->densityVelocity, in->gridOrder);
     case FP_CLEAR:
       return clearRaster(c, rb);
     case FP_TILES:
@@ -190,7 +190,7 @@ uint32_t batchBlocks(const HfbConfig& cfg, BatchKind k, const BatchInst& I) {
     }
     case BK_GRID_PRE: return divCeil(G3, 256u);
     case BK_INTEGRATE: return I.S ? divCeil(I.S, simStrandsPerBlock(I.P)) : 0u;
-    case BK_GRID_POST: return divCeil(I.S * I.P, 256u);
+    case BK_GRID_POST: return gridPostBlocks(I.S * I.P);
     case BK_RASTER: return divCeil(nSeg, TILES_RASTER_SEGS);
     case BK_SCAN: return divCeil(TB, 2048u);
     case BK_SCAN_SUMS: return 1u;
@@ -291,6 +291,7 @@ static void fillInstance(const HfbConfig& cfg, const HfbInstance& s, BatchInst& 
   I.depth = s.sceneDepth;
   I.shadingDepth = s.hairDepth ? s.hairDepth : s.shadingDepth ? s.shadingDepth : s.sceneDepth;
   I.hairDepth = s.hairDepth;
+  I.gridOrder = s.gridOrder;
   I.ao = s.ao;
   I.sm = s.shadowMap;
   I.tiles = (uint4*)s.raster.tiles;

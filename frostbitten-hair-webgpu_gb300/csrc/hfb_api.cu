@@ -3,6 +3,7 @@
 // argument errors into HFB_ERR_* codes plus a message; nothing throws across
 // the boundary.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -333,7 +334,60 @@ int hfb_grid_post_sim(HfbCtx* c, const HfbSimUniforms* u, const HfbHairData* h, 
   std::string err = validateHair(h);
   HFB_REQUIRE(c, err.empty(), err);
   HFB_REQUIRE(c, aligned16(prev) && aligned16(now) && aligned16(dv), "vec4 buffers must be 16-byte aligned");
-  HFB_LAUNCH(c, hfb::launchGridPostSim(c, *u, *h, prev, now, dv), "grid_post_sim");
+  HFB_LAUNCH(c, hfb::launchGridPostSim(c, *u, *h, prev, now, dv, nullptr), "grid_post_sim");
+}
+
+int hfb_grid_post_sim_ordered(HfbCtx* c, const HfbSimUniforms* u, const HfbHairData* h, const float* prev,
+                              const float* now, int32_t* dv, const uint32_t* order) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, u && prev && now && dv, "NULL argument");
+  std::string err = validateHair(h);
+  HFB_REQUIRE(c, err.empty(), err);
+  HFB_REQUIRE(c, aligned16(prev) && aligned16(now) && aligned16(dv), "vec4 buffers must be 16-byte aligned");
+  HFB_LAUNCH(c, hfb::launchGridPostSim(c, *u, *h, prev, now, dv, order), "grid_post_sim");
+}
+
+namespace {
+// Bits 0..9 of v spread to every third bit.
+uint64_t mortonSpread(uint32_t v) {
+  uint64_t x = v & 0x3ffu;
+  x = (x | (x << 16)) & 0x030000FFull;
+  x = (x | (x << 8)) & 0x0300F00Full;
+  x = (x | (x << 4)) & 0x030C30C3ull;
+  x = (x | (x << 2)) & 0x09249249ull;
+  return x;
+}
+}  // namespace
+
+int hfb_strand_grid_order(const float* pos, uint32_t S, uint32_t P, uint32_t* out) {
+  if (!out || (S && (!pos || P == 0))) return HFB_ERR_INVALID_ARGUMENT;
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (uint32_t s = 0; s < S; s++)
+    for (int a = 0; a < 3; a++) {
+      const float v = pos[(size_t)s * P * 4 + a];
+      if (std::isfinite(v)) {
+        lo[a] = std::min(lo[a], v);
+        hi[a] = std::max(hi[a], v);
+      }
+    }
+  std::vector<std::pair<uint64_t, uint32_t>> keys(S);
+  for (uint32_t s = 0; s < S; s++) {
+    uint64_t code = 0;
+    for (int a = 0; a < 3; a++) {
+      const float v = pos[(size_t)s * P * 4 + a];
+      const double ext = (double)hi[a] - (double)lo[a];
+      double t = std::isfinite(v) && ext > 0.0 ? ((double)v - (double)lo[a]) / ext : 0.0;
+      t = std::min(std::max(t, 0.0), 1.0);
+      code |= mortonSpread((uint32_t)(t * 1023.0)) << a;
+    }
+    keys[s] = {code, s};
+  }
+  std::stable_sort(keys.begin(), keys.end(),
+                   [](const std::pair<uint64_t, uint32_t>& x, const std::pair<uint64_t, uint32_t>& y) {
+                     return x.first < y.first;
+                   });
+  for (uint32_t s = 0; s < S; s++) out[s] = keys[s].second;
+  return HFB_OK;
 }
 
 int hfb_shading(HfbCtx* c, const HfbUniforms* u, const HfbHairData* h, const float* pos,

@@ -109,7 +109,7 @@ cudaError_t launchSimIntegrate(HfbCtx* c, const HfbSimUniforms& u, const HfbHair
                                const float* now, const float* initial, const float* segLen,
                                const int32_t* dv, const float* gw, const float* sdf, uint32_t sdfDims);
 cudaError_t launchGridPostSim(HfbCtx* c, const HfbSimUniforms& u, const HfbHairData& h, const float* prev,
-                              const float* now, int32_t* dv);
+                              const float* now, int32_t* dv, const uint32_t* strandOrder);
 cudaError_t launchShading(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, const float* pos,
                           const float* tan, const float* depth, const float* ao, uint32_t aoW,
                           uint32_t aoH, const float* sm, uint32_t smSize, float* shading);
@@ -246,6 +246,7 @@ struct alignas(16) BatchInst {
   unsigned char* scratch;
   size_t scratchBytes;
   float* hairDepth;           // NULL: no hair depth prepass
+  const uint32_t* gridOrder;  // strand order of the grid splat, NULL = identity
 };
 
 // Device layout of a batch: header, prefix rows (fixed stride), the fine
@@ -296,6 +297,8 @@ cudaError_t launchBatchDepthCopy(HfbCtx* c, const BatchView& b);
 cudaError_t launchHairDepth(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, const float* pos, const float* tan,
                             uint32_t strandsToRender, const float* sceneDepth, float* hairDepth,
                             HfbRasterBuffers& rb);
+// Blocks of the grid splat (GridPostSimPass) over `points` points.
+uint32_t gridPostBlocks(uint32_t points);
 // Blocks of the hair depth pass over `points` points.
 uint32_t hairDepthBlocks(uint32_t points);
 __host__ __device__ inline uint32_t hairDepthBigCap(size_t bytes) {

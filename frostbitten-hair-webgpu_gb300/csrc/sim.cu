@@ -371,16 +371,18 @@ simIntegrateKernel(const HfbSimUniforms u, uint32_t S, uint32_t P, uint32_t G,
 // GridPostSimPass.main, gridPostSimPass.wgsl.ts:45-72 with
 // _addGridDensityVelocity, densityVelocityGrid.wgsl.ts:93-124.
 //
-// One thread per point, eight corners, four wrapping i32 adds each.  The
-// adds of a block are first merged per grid node in a shared-memory hash
-// table (neighbouring points of a strand share nodes: a warp's 256 corner
-// updates touch ~100 nodes), then each node's four sums go to global memory
-// as one set of atomics.  Wrapping integer sums do not depend on their
-// order, so the grid is bit-exact whatever the merge; an update that finds
-// no free slot within GP_PROBES goes straight to global memory.
+// One thread per point, eight corners, four wrapping i32 adds each.  A block
+// takes GP_POINTS points, strand after strand in the order strandOrder gives
+// (neighbouring strands next to each other: their points share grid nodes),
+// and first merges its adds per grid node in a shared-memory hash table;
+// each node's four sums then go to global memory as one set of atomics.
+// Wrapping integer sums do not depend on their order, so the grid is
+// bit-exact whatever the strand order and the merge; an update that finds no
+// free slot within GP_PROBES goes straight to global memory.
 // ---------------------------------------------------------------------------
 constexpr uint32_t GP_THREADS = 256;
-constexpr uint32_t GP_HASH = 2048;  // slots (power of two)
+constexpr uint32_t GP_POINTS = 1024;  // points per block (four per thread)
+constexpr uint32_t GP_HASH = 2048;    // slots (power of two)
 constexpr uint32_t GP_PROBES = 32;
 constexpr uint32_t GP_EMPTY = 0xffffffffu;
 
@@ -417,18 +419,26 @@ __device__ __forceinline__ void gridPostAdd(GridPostShared& sh, unsigned* __rest
   atomicAdd(c + 3, v.w);
 }
 
-// Points [first, first + GP_THREADS) of the N; the table is empty on entry
-// and on exit.  All threads of the block call it.
-__device__ __forceinline__ void gridPostSimBody(const HfbSimUniforms& u, uint32_t N, uint32_t G,
+// Ordered points [blk * GP_POINTS, (blk + 1) * GP_POINTS) of the S * P: the
+// ordered point v is point v % P of strand order[v / P].  The table is empty
+// on entry and on exit.  All threads of the block call it.
+__device__ __forceinline__ void gridPostSimBody(const HfbSimUniforms& u, uint32_t S, uint32_t P, uint32_t G,
                                                 const float4* __restrict__ prev, const float4* __restrict__ now,
-                                                unsigned* __restrict__ dv, uint32_t i, GridPostShared& sh) {
-  const bool valid = i < N;
-  float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
-  if (valid) { a = __ldg(HFB_G(&prev[i])); b = __ldg(HFB_G(&now[i])); }
-  const f3 pn = mk3(b.x, b.y, b.z);
-  const f3 vel = sub3(pn, mk3(a.x, a.y, a.z));
-  const GridCo co = gridCell(G, gridMin(u), gridMax(u), pn);
-  if (valid) {
+                                                unsigned* __restrict__ dv, const uint32_t* __restrict__ order,
+                                                uint32_t blk, GridPostShared& sh) {
+  const uint32_t N = S * P;
+  const f3 gmin = gridMin(u), gmax = gridMax(u);
+#pragma unroll 1
+  for (uint32_t r = 0; r < GP_POINTS / GP_THREADS; r++) {
+    const uint32_t v = blk * GP_POINTS + r * GP_THREADS + threadIdx.x;
+    if (v >= N) break;
+    const uint32_t ls = v / P, j = v - ls * P;
+    const uint32_t s = order ? min(__ldg(HFB_G(&order[ls])), S - 1u) : ls;
+    const size_t i = (size_t)s * P + j;
+    const float4 a = __ldg(HFB_G(&prev[i])), b = __ldg(HFB_G(&now[i]));
+    const f3 pn = mk3(b.x, b.y, b.z);
+    const f3 vel = sub3(pn, mk3(a.x, a.y, a.z));
+    const GridCo co = gridCell(G, gmin, gmax, pn);
 #pragma unroll
     for (uint32_t k = 0; k < 8u; k++) {
       const uint32_t x = co.mn[0] + (k & 1u), y = co.mn[1] + ((k >> 1) & 1u), z = co.mn[2] + (k >> 2);
@@ -458,12 +468,12 @@ __device__ __forceinline__ void gridPostSimBody(const HfbSimUniforms& u, uint32_
 }
 
 __global__ void __launch_bounds__(GP_THREADS)
-gridPostSimKernel(const HfbSimUniforms u, uint32_t N, uint32_t G, const float4* __restrict__ prev,
-                  const float4* __restrict__ now, unsigned* __restrict__ dv) {
+gridPostSimKernel(const HfbSimUniforms u, uint32_t S, uint32_t P, uint32_t G, const float4* __restrict__ prev,
+                  const float4* __restrict__ now, unsigned* __restrict__ dv, const uint32_t* __restrict__ order) {
   __shared__ GridPostShared sh;
   gridPostClear(sh);
   __syncthreads();
-  gridPostSimBody(u, N, G, prev, now, dv, blockIdx.x * blockDim.x + threadIdx.x, sh);
+  gridPostSimBody(u, S, P, G, prev, now, dv, order, blockIdx.x, sh);
 }
 
 // ---- batched: persistent over the virtual blocks of every instance ----
@@ -503,8 +513,7 @@ __global__ void __launch_bounds__(GP_THREADS) gridPostSimBatch(BatchView b, uint
     const uint32_t i = batchFind(row, n, v);
     const BatchInst& I = b.insts[i];
     // after the swap: prev = the old current positions, now = the new ones
-    gridPostSimBody(I.SU, I.S * I.P, G, I.posOld, I.posNew, (unsigned*)I.dv, (v - row[i]) * GP_THREADS + threadIdx.x,
-                    sh);
+    gridPostSimBody(I.SU, I.S, I.P, G, I.posOld, I.posNew, (unsigned*)I.dv, I.gridOrder, v - row[i], sh);
   }
 }
 
@@ -573,16 +582,18 @@ cudaError_t launchBatchSim(HfbCtx* c, const BatchView& b, BatchKind k) {
   return cudaGetLastError();
 }
 
+uint32_t gridPostBlocks(uint32_t points) { return divCeil(points, GP_POINTS); }
+
 cudaError_t launchGridPostSim(HfbCtx* c, const HfbSimUniforms& u, const HfbHairData& h, const float* prev,
-                              const float* now, int32_t* dv) {
+                              const float* now, int32_t* dv, const uint32_t* strandOrder) {
   HFB_CHECK_BIND(c);
   uint32_t G = c->cfg.gridDims;
   cudaError_t e = cudaMemsetAsync(dv, 0, (size_t)G * G * G * 16, c->stream);  // clearDensityVelocityBuffer
   if (e != cudaSuccess) return e;
-  uint32_t N = h.strandsCount * h.pointsPerStrand;
+  const uint32_t N = h.strandsCount * h.pointsPerStrand;
   if (N) {
-    gridPostSimKernel<<<divCeil(N, GP_THREADS), GP_THREADS, 0, c->stream>>>(u, N, G, (const float4*)prev,
-                                                               (const float4*)now, (unsigned*)dv);
+    gridPostSimKernel<<<gridPostBlocks(N), GP_THREADS, 0, c->stream>>>(
+        u, h.strandsCount, h.pointsPerStrand, G, (const float4*)prev, (const float4*)now, (unsigned*)dv, strandOrder);
     HFB_AFTER_LAUNCH(c, "gridPostSimKernel");
     c->launches += 1;
   }

@@ -53,7 +53,8 @@ class HfbInstance(ctypes.Structure):
                 ("sdf", ctypes.c_void_p), ("sdfDims", ctypes.c_uint32), ("shadowMapSize", ctypes.c_uint32),
                 ("shading", ctypes.c_void_p), ("sceneDepth", ctypes.c_void_p), ("shadingDepth", ctypes.c_void_p),
                 ("ao", ctypes.c_void_p), ("aoWidth", ctypes.c_uint32), ("aoHeight", ctypes.c_uint32),
-                ("shadowMap", ctypes.c_void_p), ("raster", HfbRasterBuffers), ("hairDepth", ctypes.c_void_p)]
+                ("shadowMap", ctypes.c_void_p), ("raster", HfbRasterBuffers), ("hairDepth", ctypes.c_void_p),
+                ("gridOrder", ctypes.c_void_p)]
 
 
 class HfbCounters(ctypes.Structure):
@@ -65,7 +66,7 @@ class HfbCounters(ctypes.Structure):
 
 assert ctypes.sizeof(HfbHairData) == 32
 assert ctypes.sizeof(HfbCounters) == 64
-assert ctypes.sizeof(HfbInstance) == 264
+assert ctypes.sizeof(HfbInstance) == 272
 
 # every symbol include/hairfb.h declares: name -> (restype, argtypes)
 P, U32, SZ, I = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_size_t, ctypes.c_int
@@ -90,6 +91,8 @@ SIGNATURES = {
     "hfb_grid_pre_sim": (I, [P, P, P, P, P, U32]),
     "hfb_sim_integrate": (I, [P, P, P, P, P, P, P, P, P, P, U32]),
     "hfb_grid_post_sim": (I, [P, P, P, P, P, P]),
+    "hfb_grid_post_sim_ordered": (I, [P, P, P, P, P, P, P]),
+    "hfb_strand_grid_order": (I, [P, U32, U32, P]),
     "hfb_shading": (I, [P, P, P, P, P, P, P, U32, U32, P, U32, P]),
     "hfb_clear_before_render": (I, [P, P]),
     "hfb_tiles_pass": (I, [P, P, P, P, P, P, U32, P]),
@@ -128,6 +131,19 @@ def load(path: str = LIB_PATH):
         if _lib is None:
             _lib = open_library(path)
     return _lib
+
+
+def strand_grid_order(positions, strands: int, points: int):
+    """hfb_strand_grid_order: the strands sorted by their root's Morton code
+    (a uint32 numpy array), the order the grid splat visits them in."""
+    import numpy as np
+    pos = np.ascontiguousarray(positions, dtype=np.float32)
+    assert pos.size >= strands * points * 4
+    out = np.empty(strands, np.uint32)
+    rc = load().hfb_strand_grid_order(pos.ctypes.data, strands, points, out.ctypes.data)
+    if rc != HFB_OK:
+        raise HfbError(rc, "hfb_strand_grid_order failed")
+    return out
 
 
 def ptr(x) -> int | None:

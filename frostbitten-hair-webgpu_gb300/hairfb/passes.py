@@ -17,7 +17,7 @@ import torch
 from . import hair_object as HO
 from .config import HairConfig
 from .formats import SdfVolume
-from .lib import Context, HfbHairData, HfbRasterBuffers, byref, ptr
+from .lib import Context, HfbHairData, HfbRasterBuffers, byref, ptr, strand_grid_order
 
 
 def _dev(a, dtype=None) -> torch.Tensor:
@@ -52,6 +52,8 @@ class HairObject:
         self.tangents = _dev(buffers.tangents)
         self.segment_lengths = _dev(buffers.segment_lengths)
         self.shading = _dev(HO.initial_shading(a.strands, shading_points))
+        # the order the grid splat visits the strands in (neighbouring roots together)
+        self.grid_order = _dev(strand_grid_order(a.positions, a.strands, a.points_per_strand).view(np.int32))
         self.hair_data = HfbHairData()
         for i in range(3):
             self.hair_data.boundingSphere[i] = float(buffers.sphere_center[i])
@@ -142,8 +144,9 @@ class GridPostSimPass:
         self.ctx = ctx
 
     def cmd_update_grids_after_sim(self, sim_uniforms: bytes, hair: HairObject, grids: PhysicsGrids):
-        self.ctx.call("hfb_grid_post_sim", _ub(sim_uniforms), byref(hair.hair_data),
-                      ptr(hair.positions_prev), ptr(hair.positions), ptr(grids.density_velocity))
+        self.ctx.call("hfb_grid_post_sim_ordered", _ub(sim_uniforms), byref(hair.hair_data),
+                      ptr(hair.positions_prev), ptr(hair.positions), ptr(grids.density_velocity),
+                      ptr(hair.grid_order))
 
 
 # ---------------------------------------------------------------------------

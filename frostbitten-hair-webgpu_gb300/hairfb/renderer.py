@@ -139,6 +139,7 @@ class Renderer:
             inst.shadingDepth = ptr(self.shading_depth)
             inst.raster = self.rb.rb
             inst.hairDepth = ptr(self.hair_depth) if self.hair_depth is not None else None
+            inst.gridOrder = ptr(h.grid_order)
             self._inst, self._inst_uniforms, self._inst_rb = inst, self.uniforms, self.rb
         else:
             UN.patch_sim_uniforms(self._su_buf, self.frame_idx, i.wind_strength(self.frame_idx))

@@ -240,6 +240,22 @@ HFB_API int hfb_sim_integrate(HfbCtx* ctx, const HfbSimUniforms* u, const HfbHai
 HFB_API int hfb_grid_post_sim(HfbCtx* ctx, const HfbSimUniforms* u, const HfbHairData* hair,
                       const float* positionsPrev, const float* positionsNow, int32_t* densityVelocity);
 
+/* hfb_grid_post_sim visiting the strands in the order strandOrder (device,
+ * strandsCount u32, a permutation; NULL = 0, 1, 2, ...).  The splat is a sum
+ * of wrapping i32 adds, so the grid is the same for every order; an order
+ * that puts neighbouring strands next to each other (hfb_strand_grid_order)
+ * lets a block merge more of its adds before they reach global memory. */
+HFB_API int hfb_grid_post_sim_ordered(HfbCtx* ctx, const HfbSimUniforms* u, const HfbHairData* hair,
+                              const float* positionsPrev, const float* positionsNow, int32_t* densityVelocity,
+                              const uint32_t* strandOrder);
+
+/* Host: the strands of a hair asset (positions: host, strandsCount *
+ * pointsPerStrand vec4f) sorted by the Morton code of their root within the
+ * roots' bounding box (10 bits per axis; ties keep strand order).  Writes
+ * strandsCount indices to orderOut (host). */
+HFB_API int hfb_strand_grid_order(const float* positions, uint32_t strandsCount, uint32_t pointsPerStrand,
+                          uint32_t* orderOut);
+
 /* ---- shading (HairShadingPass.cmdComputeShadingPoints, hairShadingPass.ts:41-68) ---- */
 /* depth: width*height f32 (row 0 = top); ao: aoWidth*aoHeight f32 or NULL
  * (unoccluded); shadowMap: shadowMapSize^2 f32 or NULL (no shadow).
@@ -314,6 +330,9 @@ typedef struct HfbInstance {
    * the hair drawn that HwHairPass leaves for the shading
    * (renderer.ts:286-296). */
   float* hairDepth;
+  /* device, strandsCount u32 or NULL: the order the grid splat visits the
+   * strands in (hfb_grid_post_sim_ordered) */
+  const uint32_t* gridOrder;
 } HfbInstance;
 
 /* HwHairPass.cmdDrawHair's depth output (hwHairPass.ts:71-160): copies
@@ -393,13 +412,13 @@ static_assert(sizeof(HfbConfig) == 64, "HfbConfig layout");
 static_assert(sizeof(HfbHairData) == 32, "HfbHairData layout");
 static_assert(sizeof(HfbUniforms) == 1184, "Uniforms layout");
 static_assert(sizeof(HfbSimUniforms) == 304, "SimulationUniforms layout");
-static_assert(sizeof(HfbInstance) == 264, "HfbInstance layout");
+static_assert(sizeof(HfbInstance) == 272, "HfbInstance layout");
 #else
 _Static_assert(sizeof(HfbConfig) == 64, "HfbConfig layout");
 _Static_assert(sizeof(HfbHairData) == 32, "HfbHairData layout");
 _Static_assert(sizeof(HfbUniforms) == 1184, "Uniforms layout");
 _Static_assert(sizeof(HfbSimUniforms) == 304, "SimulationUniforms layout");
-_Static_assert(sizeof(HfbInstance) == 264, "HfbInstance layout");
+_Static_assert(sizeof(HfbInstance) == 272, "HfbInstance layout");
 #endif
 
 #endif /* HAIRFB_H */

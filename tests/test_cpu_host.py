@@ -166,3 +166,30 @@ def test_product_has_no_cpu_fallback(tmp_path):
     from hairfb import lib as L
     with pytest.raises(FileNotFoundError):
         L.open_library(str(tmp_path / "libhairfb.so"))
+
+
+def test_strand_grid_order_is_a_morton_permutation():
+    """hfb_strand_grid_order (host code, no GPU): a permutation of the
+    strands whose roots' Morton codes do not decrease."""
+    from hairfb import synthetic
+    from hairfb.lib import strand_grid_order
+    rng = np.random.Generator(np.random.PCG64(3))
+    inst = synthetic.make_instance(rng, strands=3000, points=16, width=64, height=64)
+    a = inst.hair.asset
+    order = strand_grid_order(a.positions, a.strands, a.points_per_strand)
+    assert np.array_equal(np.sort(order), np.arange(a.strands))
+    roots = a.positions.reshape(a.strands, a.points_per_strand, 4)[:, 0, :3].astype(np.float64)
+    lo, hi = roots.min(0), roots.max(0)
+    q = np.clip(((roots - lo) / (hi - lo) * 1023.0).astype(np.int64), 0, 1023)
+
+    def spread(v):
+        out = np.zeros_like(v)
+        for b in range(10):
+            out |= ((v >> b) & 1) << (3 * b)
+        return out
+    code = spread(q[:, 0]) | (spread(q[:, 1]) << 1) | (spread(q[:, 2]) << 2)
+    assert (np.diff(code[order]) >= 0).all()
+    # neighbours in the order are near each other: far closer than in strand order
+    d_order = np.linalg.norm(np.diff(roots[order], axis=0), axis=1).mean()
+    d_plain = np.linalg.norm(np.diff(roots, axis=0), axis=1).mean()
+    assert d_order < 0.5 * d_plain

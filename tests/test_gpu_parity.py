@@ -212,6 +212,47 @@ def test_density_grid_wraps_like_the_reference(oracle):
     assert np.array_equal(grids.density_velocity.cpu().numpy(), o)
 
 
+@pytest.mark.parametrize("order", ["identity", "reversed", "random"])
+def test_grid_splat_does_not_depend_on_strand_order(oracle, order):
+    """The grid splat visits the strands in a given order (Morton order of
+    the roots by default): the identity, a reversed and a random order give
+    the oracle's grid bit for bit."""
+    from hairfb.passes import _dev
+    inst = small_instance(strands=5000, points=24)
+    hb = inst.hair
+    su = _sim_inputs(inst, 3)
+    ctx = _ctx(inst)
+    hair = HairObject(hb, inst.cfg.shading_points)
+    grids = PhysicsGrids(inst.cfg.grid_dims)
+    rng = np.random.default_rng(4)
+    now = hb.asset.positions.copy()
+    now[:, :3] += rng.normal(0, 2e-3, now[:, :3].shape).astype(np.float32) * (now[:, 3:] > 0)
+    hair.positions.copy_(torch.as_tensor(now))
+    S = hb.asset.strands
+    perm = {"identity": np.arange(S), "reversed": np.arange(S)[::-1],
+            "random": rng.permutation(S)}[order].astype(np.int32)
+    from hairfb.lib import byref, ptr
+    ctx.call("hfb_grid_post_sim_ordered", ctypes_ub(su), byref(hair.hair_data), ptr(hair.positions_prev),
+             ptr(hair.positions), ptr(grids.density_velocity), ptr(_dev(perm)))
+    ctx.sync()
+    odv = oracle.grid_post_sim(inst.cfg, su, hb.hair_data, hb.asset.positions, now)
+    assert np.array_equal(grids.density_velocity.cpu().numpy(), odv)
+    # the default (Morton) order and the unordered entry point agree too
+    morton = PhysicsGrids(inst.cfg.grid_dims)
+    GridPostSimPass(ctx).cmd_update_grids_after_sim(su, hair, morton)
+    plain = PhysicsGrids(inst.cfg.grid_dims)
+    ctx.call("hfb_grid_post_sim", ctypes_ub(su), byref(hair.hair_data), ptr(hair.positions_prev),
+             ptr(hair.positions), ptr(plain.density_velocity))
+    ctx.sync()
+    assert np.array_equal(morton.density_velocity.cpu().numpy(), odv)
+    assert np.array_equal(plain.density_velocity.cpu().numpy(), odv)
+
+
+def ctypes_ub(b: bytes):
+    from hairfb.passes import _ub
+    return _ub(b)
+
+
 def test_simulation_60_steps(oracle):
     inst = small_instance(strands=1500, points=24, curl=True, wind_amplitude=1.0, iterations=4)
     hb = inst.hair
