@@ -137,48 +137,118 @@ __device__ __forceinline__ Tri segTri(const ScreenV (&q)[4], uint32_t tr) {
   return t;
 }
 
+// A triangle's pixel box for the warp's shared pixel loop.
+struct HdSlot {
+  float area;
+  int x0, y0;
+  uint32_t bw;
+};
+
+struct HdShared {
+  float4 sv[HD_THREADS][2];              // each point's two screen vertices (x, y, z, drawable)
+  HdSlot slot[HD_THREADS / 32][64];       // per warp: lane * 2 + triangle
+  uint32_t start[HD_THREADS / 32][32];    // per warp: first pixel test of each lane's triangles
+  uint32_t c0[HD_THREADS / 32][32];       // per warp: pixel tests of each lane's triangle 0
+};
+
+// The quad of the segment whose first point has block index k.
+__device__ __forceinline__ void blockQuad(const HdShared& sh, uint32_t k, ScreenV (&q)[4]) {
+  q[0] = unpackV(sh.sv[k][0]);
+  q[1] = unpackV(sh.sv[k][1]);
+  q[2] = unpackV(sh.sv[k + 1][0]);
+  q[3] = unpackV(sh.sv[k + 1][1]);
+}
+
 // One block of HD_THREADS points starting at point blk * HD_SEGS: every
-// thread projects its point's two vertices into shared memory, then each of
-// the first HD_SEGS threads draws the segment from its point to the next
-// (when that point is not its strand's last) -- both triangles in the
-// thread, or onto the big list (entries point << 1 | triangle; capacity
-// `bigCap`, overflow drawn in the thread).  Called by every thread of the
-// block.
+// thread projects its point's two vertices into shared memory; each of the
+// first HD_SEGS threads owns the segment from its point to the next (when
+// that point is not its strand's last) and boxes its two triangles.  A box
+// of more than HD_BIG_AREA pixels goes onto the big list (entries
+// point << 1 | triangle; capacity `bigCap`); the others' pixel tests are
+// shared out over the warp's lanes (an exclusive scan of the box sizes),
+// so a lane with a long thin triangle does not hold up the other 31.  A big
+// triangle that finds the list full is drawn by its own thread.  Called by
+// every thread of the block.
 __device__ __forceinline__ void hairDepthBlock(const HdView& V, uint32_t P, uint32_t nPts,
                                                const float4* __restrict__ pos, const float4* __restrict__ tan,
                                                unsigned* __restrict__ depth, uint32_t* __restrict__ big,
-                                               uint32_t bigCap, uint32_t blk, float4 (*sv)[2]) {
-  const uint32_t pt = blk * HD_SEGS + threadIdx.x;
+                                               uint32_t bigCap, uint32_t blk, HdShared& sh) {
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, wp = tid >> 5;
+  const uint32_t pt = blk * HD_SEGS + tid;
   if (pt < nPts) {
     ScreenV a, b;
     pointPair(V, pos, tan, pt, a, b);
-    sv[threadIdx.x][0] = packV(a);
-    sv[threadIdx.x][1] = packV(b);
+    sh.sv[tid][0] = packV(a);
+    sh.sv[tid][1] = packV(b);
   }
   __syncthreads();
-  if (threadIdx.x < HD_SEGS && pt + 1u < nPts && pt % P != P - 1u) {
-    const uint32_t W = f2u(V.W), H = f2u(V.H);
-    const ScreenV q[4] = {unpackV(sv[threadIdx.x][0]), unpackV(sv[threadIdx.x][1]), unpackV(sv[threadIdx.x + 1][0]),
-                          unpackV(sv[threadIdx.x + 1][1])};
+  const uint32_t W = f2u(V.W), H = f2u(V.H);
+  uint32_t c[2] = {0u, 0u};
+  bool own[2] = {false, false};  // big, list full: drawn by this thread
+  if (tid < HD_SEGS && pt + 1u < nPts && pt % P != P - 1u) {
+    ScreenV q[4];
+    blockQuad(sh, tid, q);
 #pragma unroll
     for (uint32_t tr = 0; tr < 2u; tr++) {
       const Tri t = segTri(q, tr);
       float area;
       int x0, x1, y0, y1;
       if (!triBox(t, W, H, area, x0, x1, y0, y1)) continue;
-      const uint64_t px = (uint64_t)(x1 - x0 + 1) * (uint64_t)(y1 - y0 + 1);
-      if (px > HD_BIG_AREA && pt < 0x80000000u) {
-        const uint32_t slot = atomicAdd(HFB_G(&big[0]), 1u);
-        if (slot < bigCap) {
+      const uint32_t bw = (uint32_t)(x1 - x0 + 1), bh = (uint32_t)(y1 - y0 + 1);
+      if ((uint64_t)bw * bh > HD_BIG_AREA) {
+        const uint32_t slot = pt < 0x80000000u ? atomicAdd(HFB_G(&big[0]), 1u) : bigCap;
+        if (slot < bigCap)
           *HFB_G(&big[1u + slot]) = (pt << 1) | tr;
-          continue;
-        }
+        else
+          own[tr] = true;
+        continue;
       }
+      c[tr] = bw * bh;
+      sh.slot[wp][lane * 2u + tr] = {area, x0, y0, bw};
+    }
+  }
+  // exclusive scan of the lanes' pixel tests
+  const uint32_t mine = c[0] + c[1];
+  uint32_t incl = mine;
+#pragma unroll
+  for (uint32_t d = 1; d < 32u; d <<= 1) {
+    const uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += o;
+  }
+  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+  sh.start[wp][lane] = incl - mine;
+  sh.c0[wp][lane] = c[0];
+  __syncwarp();
+  for (uint32_t k = lane; k < total; k += 32u) {
+    uint32_t lo = 0, hi = 31;  // the last lane whose tests start at or before k owns test k
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi + 1u) >> 1;
+      if (sh.start[wp][mid] <= k) lo = mid; else hi = mid - 1u;
+    }
+    uint32_t local = k - sh.start[wp][lo];
+    const uint32_t n0 = sh.c0[wp][lo];
+    const uint32_t tr = local >= n0 ? 1u : 0u;
+    if (tr) local -= n0;
+    const HdSlot sl = sh.slot[wp][lo * 2u + tr];
+    ScreenV q[4];
+    blockQuad(sh, wp * 32u + lo, q);
+    const uint32_t row = local / sl.bw;
+    triPixel(segTri(q, tr), sl.area, W, sl.x0 + (int)(local - row * sl.bw), sl.y0 + (int)row, depth);
+  }
+  if (own[0] || own[1]) {
+    ScreenV q[4];
+    blockQuad(sh, tid, q);
+    for (uint32_t tr = 0; tr < 2u; tr++) {
+      if (!own[tr]) continue;
+      const Tri t = segTri(q, tr);
+      float area;
+      int x0, x1, y0, y1;
+      if (!triBox(t, W, H, area, x0, x1, y0, y1)) continue;
       for (int y = y0; y <= y1; y++)
         for (int x = x0; x <= x1; x++) triPixel(t, area, W, x, y, depth);
     }
   }
-  __syncthreads();  // sv is rewritten by the block's next points
+  __syncthreads();  // the shared state is rewritten by the block's next points
 }
 
 // The big list, one block per triangle.
@@ -208,8 +278,8 @@ __global__ void __launch_bounds__(HD_THREADS)
 hairDepthKernel(const HdView V, uint32_t P, uint32_t nPts, const float4* __restrict__ pos,
                 const float4* __restrict__ tan, unsigned* __restrict__ depth, uint32_t* __restrict__ big,
                 uint32_t bigCap) {
-  __shared__ float4 sv[HD_THREADS][2];
-  hairDepthBlock(V, P, nPts, pos, tan, depth, big, bigCap, blockIdx.x, sv);
+  __shared__ HdShared sh;
+  hairDepthBlock(V, P, nPts, pos, tan, depth, big, bigCap, blockIdx.x, sh);
 }
 
 __global__ void __launch_bounds__(HD_THREADS)
@@ -227,7 +297,7 @@ __device__ __forceinline__ void loadView(const HfbUniforms& U, HdView& V) {
 
 // ---- batched: persistent over every instance ----
 __global__ void __launch_bounds__(HD_THREADS) hairDepthBatch(BatchView b) {
-  __shared__ float4 sv[HD_THREADS][2];
+  __shared__ HdShared sh;
   __shared__ HdView V;
   const uint32_t n = b.hdr->n;
   const uint32_t* row = b.prefix + BK_HAIR_DEPTH * (BATCH_MAX + 1);
@@ -242,7 +312,7 @@ __global__ void __launch_bounds__(HD_THREADS) hairDepthBatch(BatchView b) {
     }
     hairDepthBlock(V, I.P, min(I.strandsToRender, I.S) * I.P, I.posNew, I.tan,
                    reinterpret_cast<unsigned*>(I.hairDepth), reinterpret_cast<uint32_t*>(I.scratch),
-                   hairDepthBigCap(I.scratchBytes), v - row[i], sv);
+                   hairDepthBigCap(I.scratchBytes), v - row[i], sh);
   }
 }
 
