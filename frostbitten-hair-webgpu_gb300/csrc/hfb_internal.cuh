@@ -21,7 +21,6 @@ struct HfbCtx {
   unsigned long long* dCounters = nullptr;
   uint64_t launches = 0;
   // per-context launch set-up done once (kernel attributes, occupancy)
-  size_t simSmemSet = 0;
   bool largeBinsAttrSet = false;
   int fineBlocksPerSM[3][3] = {};  // [tile 8/16/32][slices 4/8/16]
   // batched frames: device table + two pinned host staging copies, the
@@ -95,10 +94,10 @@ uint32_t maxDrawnSegments(const HfbConfig& cfg, uint32_t W, uint32_t H);
 // Strands per integration block for P points per strand: one chain warp per
 // block for P <= 32, fewer strands for longer strands (shared memory ~38 KB).
 __host__ __device__ inline uint32_t simStrandsPerBlock(uint32_t P) {
-  return P <= 32u ? 32u : (1024u / P > 8u ? 1024u / P : 8u);
+  return 1024u / P > 8u ? 1024u / P : 8u;  // NB * P <= 1024: four points per thread
 }
 __host__ __device__ inline size_t simSmemBytes(uint32_t P) {
-  return (size_t)simStrandsPerBlock(P) * (P + 1u) * (2u * sizeof(float4) + sizeof(float));
+  return (size_t)simStrandsPerBlock(P) * (P + 1u) * (2u * sizeof(float4) + sizeof(float)) + (size_t)P * 4u;
 }
 constexpr uint32_t TILES_RASTER_SEGS = 128;  // segments per tiles-raster block
 

@@ -6,6 +6,9 @@
 // fp32 order of hfb_math.cuh, so results are reproducible run to run; the
 // grid splat is integer (i32 fixed point, wrapping adds), hence order-free.
 #define HFB_TU 1
+#include <algorithm>
+#include <atomic>
+
 #include "hfb_internal.cuh"
 #include "hfb_math.cuh"
 
@@ -198,6 +201,7 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
   float4* lc = wk + NB * R;  // [NB][R] triangle-bending constants (h0, w0, w1, w2) of the triplet at j,
                              // or the initial tangent into j for the points matchInitialTangent moves
   float* sl = reinterpret_cast<float*>(lc + NB * R);  // [NB][R] segment lengths
+  float* att = sl + NB * R;                            // [P] global-shape attenuation of point index j
   const uint32_t tid = threadIdx.x;
   const uint32_t s0 = blk * NB;
   const uint32_t nStr = min(NB, S - s0);
@@ -228,6 +232,13 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
     }
     lc[ls * R + pt] = c;
   }
+  for (uint32_t j = tid; j < P; j += SIM_THREADS) {  // applyConstraint_global's attenuation (constraints.wgsl.ts:31-49)
+    const float x = (float)j / (float)(P - 1u);
+    att[j] = fsub(1.0f, sat(fsub(x, u.globalConstrExtent) / u.globalConstrFade));
+  }
+  // i / P for the block's points (i < NB * P <= 1024, P <= 128): floor(i * ceil(2^32 / P) / 2^32)
+  // is exact there, the error i * (ceil(2^32 / P) * P - 2^32) < 1024 * 128 being far below 2^32
+  const uint32_t divP = (uint32_t)((0x100000000ull + P - 1u) / P);
   __syncthreads();
 
   const uint32_t iters = u.constraintIterations;
@@ -265,12 +276,10 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
     __syncthreads();
     // global shape, :193-206, constraints.wgsl.ts:31-49 (point-parallel)
     for (uint32_t i = tid; i < nPts; i += SIM_THREADS) {
-      const uint32_t ls = i / P, j = i - ls * P;
+      const uint32_t ls = __umulhi(i, divP), j = i - ls * P;
       if (j == 0u) continue;
-      const float x = (float)j / (float)(P - 1u);
-      const float att = fsub(1.0f, sat(fsub(x, u.globalConstrExtent) / u.globalConstrFade));
       const float4 pi = __ldg(HFB_G(&initial[(size_t)s0 * P + i]));
-      const float k = fmul(kGlob, att);
+      const float k = fmul(kGlob, att[j]);
       float4 p = wk[ls * R + j];
       f3 dvv = mk3(fsub(pi.x, p.x), fsub(pi.y, p.y), fsub(pi.z, p.z));
       f3 d = mul3s(mul3s(dvv, p.w), k);
@@ -319,7 +328,7 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
     __syncthreads();
     // collisions, :236-261, collisions.wgsl.ts:4-61 (point-parallel)
     for (uint32_t i = tid; i < nPts; i += SIM_THREADS) {
-      const uint32_t ls = i / P, j = i - ls * P;
+      const uint32_t ls = __umulhi(i, divP), j = i - ls * P;
       if (j == 0u) continue;
       float4 pos = wk[ls * R + j];
       {
@@ -531,18 +540,32 @@ cudaError_t launchGridPreSim(HfbCtx* c, const HfbSimUniforms& u, const int32_t* 
   return cudaGetLastError();
 }
 
+// The dynamic shared memory limit of a kernel is a setting of the function
+// for the whole process (per device), not of a context: contexts with
+// different strand lengths would lower it under one another's launches.  It
+// is raised once, to what the longest strands need.
+static cudaError_t simSmemLimit(const void* fn, int which) {
+  static std::atomic<uint64_t> done[2] = {};  // bit d: set on device d
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const uint64_t bit = 1ull << (dev & 63);
+  if (done[which].load() & bit) return cudaSuccess;
+  size_t most = 0;
+  for (uint32_t P = 2; P <= 256; P++) most = std::max(most, simSmemBytes(P));
+  e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)most);
+  if (e == cudaSuccess) done[which].fetch_or(bit);
+  return e;
+}
+
 cudaError_t launchSimIntegrate(HfbCtx* c, const HfbSimUniforms& u, const HfbHairData& h, float* prev,
                                const float* now, const float* initial, const float* segLen,
                                const int32_t* dv, const float* gw, const float* sdf, uint32_t sdfDims) {
   HFB_CHECK_BIND(c);
   const uint32_t S = h.strandsCount, P = h.pointsPerStrand;
   const size_t smem = simSmemBytes(P);
-  if (smem > c->simSmemSet) {
-    cudaError_t e = cudaFuncSetAttribute(simIntegrateKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return e;
-    c->simSmemSet = smem;
-  }
+  cudaError_t e = simSmemLimit((const void*)simIntegrateKernel, 0);
+  if (e != cudaSuccess) return e;
   simIntegrateKernel<<<divCeil(S, simStrandsPerBlock(P)), SIM_THREADS, smem, c->stream>>>(
       u, S, P, c->cfg.gridDims, (float4*)prev, (const float4*)now, (const float4*)initial, segLen,
       (const int4*)dv, (const float4*)gw, sdf, sdfDims);
@@ -562,7 +585,7 @@ cudaError_t launchBatchSim(HfbCtx* c, const BatchView& b, BatchKind k) {
   } else if (k == BK_INTEGRATE) {
     const size_t smem = c->simBatchSmem;  // the largest staging any batch of the context has needed
     if (!grid) {
-      cudaError_t e = cudaFuncSetAttribute(simIntegrateBatch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaError_t e = simSmemLimit((const void*)simIntegrateBatch, 1);
       int perSM = 0;
       if (e == cudaSuccess)
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, simIntegrateBatch, SIM_THREADS, smem);

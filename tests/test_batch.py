@@ -76,6 +76,20 @@ def test_frame_matches_pass_by_pass(hair_depth):
                 assert np.array_equal(ref.hair_depth.cpu().numpy(), nat.hair_depth.cpu().numpy()), f"frame {f}"
 
 
+def test_contexts_with_different_strand_lengths_interleave():
+    """The integration's shared-memory limit is a per-kernel setting of the
+    process: contexts whose strands differ in length (so in staging size)
+    run in any order, each again after the other."""
+    insts = _instances()
+    rs = [Renderer(inst, 0) for inst in insts]
+    for r in rs:
+        r.before_first_frame()
+    for order in (rs, rs[::-1], rs):
+        for r in order:
+            r.frame()
+    torch.cuda.synchronize()
+
+
 def _batch_vs_alone(insts, frames, profile_frame=None, groups=1, pipeline=False):
     alone = [Renderer(inst, 0) for inst in insts]
     ctx = Context(insts[0].cfg.to_c(), 0)
