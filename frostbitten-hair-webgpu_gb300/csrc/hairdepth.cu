@@ -137,18 +137,20 @@ __device__ __forceinline__ Tri segTri(const ScreenV (&q)[4], uint32_t tr) {
   return t;
 }
 
-// A triangle's pixel box for the warp's shared pixel loop.
-struct HdSlot {
-  float area;
+// A segment's two triangles for the warp's shared pixel loop: their pixel
+// boxes (an empty box for a triangle not drawn here), areas, and the union
+// of the boxes that the loop walks.
+struct HdUnit {
+  int bx0[2], bx1[2], by0[2], by1[2];
+  float area[2];
   int x0, y0;
-  uint32_t bw;
+  uint32_t bw, divBw;  // union box width and ceil(2^32 / width) (0 for width 1: 2^32 does not fit)
 };
 
 struct HdShared {
-  float4 sv[HD_THREADS][2];              // each point's two screen vertices (x, y, z, drawable)
-  HdSlot slot[HD_THREADS / 32][64];       // per warp: lane * 2 + triangle
-  uint32_t start[HD_THREADS / 32][32];    // per warp: first pixel test of each lane's triangles
-  uint32_t c0[HD_THREADS / 32][32];       // per warp: pixel tests of each lane's triangle 0
+  float4 sv[HD_THREADS][2];            // each point's two screen vertices (x, y, z, drawable)
+  HdUnit unit[HD_THREADS];             // each thread's segment
+  uint32_t start[HD_THREADS / 32][32]; // per warp: first pixel of each lane's union box
 };
 
 // The quad of the segment whose first point has block index k.
@@ -164,11 +166,12 @@ __device__ __forceinline__ void blockQuad(const HdShared& sh, uint32_t k, Screen
 // first HD_SEGS threads owns the segment from its point to the next (when
 // that point is not its strand's last) and boxes its two triangles.  A box
 // of more than HD_BIG_AREA pixels goes onto the big list (entries
-// point << 1 | triangle; capacity `bigCap`); the others' pixel tests are
-// shared out over the warp's lanes (an exclusive scan of the box sizes),
-// so a lane with a long thin triangle does not hold up the other 31.  A big
-// triangle that finds the list full is drawn by its own thread.  Called by
-// every thread of the block.
+// point << 1 | triangle; capacity `bigCap`); the pixels of the union of a
+// segment's other boxes are shared out over the warp's lanes (an exclusive
+// scan of the union sizes), each pixel tested against both triangles
+// within their own boxes, so a lane with a long thin segment does not hold
+// up the other 31.  A big triangle that finds the list full is drawn by its
+// own thread.  Called by every thread of the block.
 __device__ __forceinline__ void hairDepthBlock(const HdView& V, uint32_t P, uint32_t nPts,
                                                const float4* __restrict__ pos, const float4* __restrict__ tan,
                                                unsigned* __restrict__ depth, uint32_t* __restrict__ big,
@@ -183,13 +186,17 @@ __device__ __forceinline__ void hairDepthBlock(const HdView& V, uint32_t P, uint
   }
   __syncthreads();
   const uint32_t W = f2u(V.W), H = f2u(V.H);
-  uint32_t c[2] = {0u, 0u};
+  uint32_t mine = 0;
   bool own[2] = {false, false};  // big, list full: drawn by this thread
   if (tid < HD_SEGS && pt + 1u < nPts && pt % P != P - 1u) {
     ScreenV q[4];
     blockQuad(sh, tid, q);
+    HdUnit un;
+    int ux0 = 0x7fffffff, uy0 = 0x7fffffff, ux1 = -1, uy1 = -1;
 #pragma unroll
     for (uint32_t tr = 0; tr < 2u; tr++) {
+      un.bx0[tr] = 1; un.bx1[tr] = 0; un.by0[tr] = 1; un.by1[tr] = 0;  // empty
+      un.area[tr] = 0.0f;
       const Tri t = segTri(q, tr);
       float area;
       int x0, x1, y0, y1;
@@ -203,12 +210,20 @@ __device__ __forceinline__ void hairDepthBlock(const HdView& V, uint32_t P, uint
           own[tr] = true;
         continue;
       }
-      c[tr] = bw * bh;
-      sh.slot[wp][lane * 2u + tr] = {area, x0, y0, bw};
+      un.bx0[tr] = x0; un.bx1[tr] = x1; un.by0[tr] = y0; un.by1[tr] = y1;
+      un.area[tr] = area;
+      ux0 = min(ux0, x0); ux1 = max(ux1, x1); uy0 = min(uy0, y0); uy1 = max(uy1, y1);
+    }
+    if (ux1 >= ux0) {  // the union of the boxes drawn here
+      un.x0 = ux0;
+      un.y0 = uy0;
+      un.bw = (uint32_t)(ux1 - ux0 + 1);
+      un.divBw = un.bw > 1u ? (uint32_t)((0x100000000ull + un.bw - 1u) / un.bw) : 0u;
+      mine = un.bw * (uint32_t)(uy1 - uy0 + 1);
+      sh.unit[tid] = un;
     }
   }
-  // exclusive scan of the lanes' pixel tests
-  const uint32_t mine = c[0] + c[1];
+  // exclusive scan of the lanes' union boxes
   uint32_t incl = mine;
 #pragma unroll
   for (uint32_t d = 1; d < 32u; d <<= 1) {
@@ -217,23 +232,27 @@ __device__ __forceinline__ void hairDepthBlock(const HdView& V, uint32_t P, uint
   }
   const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
   sh.start[wp][lane] = incl - mine;
-  sh.c0[wp][lane] = c[0];
   __syncwarp();
   for (uint32_t k = lane; k < total; k += 32u) {
-    uint32_t lo = 0, hi = 31;  // the last lane whose tests start at or before k owns test k
+    uint32_t lo = 0, hi = 31;  // the last lane whose pixels start at or before k owns pixel k
     while (lo < hi) {
       const uint32_t mid = (lo + hi + 1u) >> 1;
       if (sh.start[wp][mid] <= k) lo = mid; else hi = mid - 1u;
     }
-    uint32_t local = k - sh.start[wp][lo];
-    const uint32_t n0 = sh.c0[wp][lo];
-    const uint32_t tr = local >= n0 ? 1u : 0u;
-    if (tr) local -= n0;
-    const HdSlot sl = sh.slot[wp][lo * 2u + tr];
+    const uint32_t o = wp * 32u + lo;
+    const HdUnit& un = sh.unit[o];
+    const uint32_t local = k - sh.start[wp][lo];
+    // the union of two boxes of at most HD_BIG_AREA pixels each is at most
+    // 2048 wide and holds fewer than 2^21 pixels, so local * (divBw * bw - 2^32)
+    // < 2^21 * 2^11 and the multiply-high quotient is exact
+    const uint32_t row = un.bw > 1u ? __umulhi(local, un.divBw) : local;
+    const int x = un.x0 + (int)(local - row * un.bw), y = un.y0 + (int)row;
     ScreenV q[4];
-    blockQuad(sh, wp * 32u + lo, q);
-    const uint32_t row = local / sl.bw;
-    triPixel(segTri(q, tr), sl.area, W, sl.x0 + (int)(local - row * sl.bw), sl.y0 + (int)row, depth);
+    blockQuad(sh, o, q);
+#pragma unroll
+    for (uint32_t tr = 0; tr < 2u; tr++)
+      if (x >= un.bx0[tr] && x <= un.bx1[tr] && y >= un.by0[tr] && y <= un.by1[tr])
+        triPixel(segTri(q, tr), un.area[tr], W, x, y, depth);
   }
   if (own[0] || own[1]) {
     ScreenV q[4];
