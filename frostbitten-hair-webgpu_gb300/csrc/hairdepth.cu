@@ -128,6 +128,91 @@ __device__ __forceinline__ void triPixel(const Tri& t, float area, uint32_t W, i
   atomicMin(HFB_G(&depth[(size_t)y * W + x]), __float_as_uint(fadd(z, 0.0f)));  // -0 -> +0
 }
 
+// Row y's pixels of the triangle: [L, R] (in: the box's x range) narrowed to
+// the pixels whose centres pass all three edge tests of triPixel; false if
+// none do.  For a fixed row an edge value fsub(C, fmul(B, fsub(px, ax)))
+// is monotone in px (each rounded step is), so each edge passes on a prefix
+// or a suffix of the row.  Its end is searched with the same float test,
+// from the pixel where the edge crosses the row in real arithmetic:
+// galloping away from that guess, then bisecting, so the span holds exactly
+// the pixels the per-pixel test accepts whatever the guess.  Needs no
+// overflow to infinity in the products (spanSafe).
+__device__ __forceinline__ bool rowSpan(const Tri& t, bool neg, int y, int& L, int& R) {
+  const float py = fadd((float)y, 0.5f);
+#pragma unroll
+  for (int e = 0; e < 3; e++) {
+    // the edges of triPixel: w0 = (v1, v2), w1 = (v2, v0), w2 = (v0, v1)
+    const ScreenV& a = t.v[e == 0 ? 1 : e == 1 ? 2 : 0];
+    const ScreenV& b = t.v[e == 0 ? 2 : e == 1 ? 0 : 1];
+    auto pass = [&](int x) {
+      const float w = edgeFn(a.x, a.y, b.x, b.y, fadd((float)x, 0.5f), py);
+      return (neg ? -w : w) >= 0.0f;
+    };
+    const float B = fsub(b.y, a.y);
+    const float dir = neg ? -B : B;
+    if (dir == 0.0f) {  // the edge value is the same along the row
+      if (!pass(L)) return false;
+      continue;
+    }
+    // the edge passes on a prefix of the row when dir > 0, on a suffix when
+    // dir < 0; f is false then true along [L, R] either way, and the edge's
+    // end is where f first holds (R + 1: never)
+    const bool prefix = dir > 0.0f;
+    auto f = [&](int x) { return prefix ? !pass(x) : pass(x); };
+    const float cross = a.x + (py - a.y) * (b.x - a.x) / B - 0.5f;  // real-arithmetic guess
+    const int g = (int)fminf(fmaxf(cross, (float)L), (float)R);
+    int lo, hi;  // f(lo) false or lo = L - 1; f(hi) true or hi = R + 1
+    if (f(g)) {
+      hi = g;
+      int step = 1;
+      lo = g - 1;
+      while (lo >= L && f(lo)) {
+        hi = lo;
+        lo = hi - (step <<= 1);
+      }
+      if (lo < L - 1) lo = L - 1;
+    } else {
+      lo = g;
+      int step = 1;
+      hi = g + 1;
+      while (hi <= R && !f(hi)) {
+        lo = hi;
+        hi = lo + (step <<= 1);
+      }
+      if (hi > R + 1) hi = R + 1;
+    }
+    while (hi - lo > 1) {  // f(lo) false (or lo = L - 1), f(hi) true (or hi = R + 1)
+      const int mid = lo + (hi - lo) / 2;
+      if (f(mid)) hi = mid; else lo = mid;
+    }
+    // hi: the first x where f is true
+    if (prefix) R = hi - 1; else L = hi;
+    if (L > R) return false;
+  }
+  return true;
+}
+
+// Vertex coordinates below 2^24 in magnitude: the edge products stay finite
+// (no inf - inf), so rowSpan's monotonicity holds.
+__device__ __forceinline__ bool spanSafe(const Tri& t) {
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < 3; k++) ok = ok && fabsf(t.v[k].x) < 16777216.0f && fabsf(t.v[k].y) < 16777216.0f;
+  return ok;
+}
+
+// Every pixel of the triangle's box [x0, x1] x [y0, y1], rows y0 + first,
+// y0 + first + step, ...: by row spans, or pixel by pixel when spanSafe fails.
+__device__ __forceinline__ void drawRows(const Tri& t, float area, uint32_t W, int x0, int x1, int y0, int y1,
+                                         int first, int step, unsigned* __restrict__ depth) {
+  const bool safe = spanSafe(t), neg = area < 0.0f;
+  for (int y = y0 + first; y <= y1; y += step) {
+    int L = x0, R = x1;
+    if (safe && !rowSpan(t, neg, y, L, R)) continue;
+    for (int x = L; x <= R; x++) triPixel(t, area, W, x, y, depth);
+  }
+}
+
 // Triangle tr of the segment whose quad is q: (0, 1, 2) or (2, 1, 3).
 __device__ __forceinline__ Tri segTri(const ScreenV (&q)[4], uint32_t tr) {
   Tri t;
@@ -263,14 +348,13 @@ __device__ __forceinline__ void hairDepthBlock(const HdView& V, uint32_t P, uint
       float area;
       int x0, x1, y0, y1;
       if (!triBox(t, W, H, area, x0, x1, y0, y1)) continue;
-      for (int y = y0; y <= y1; y++)
-        for (int x = x0; x <= x1; x++) triPixel(t, area, W, x, y, depth);
+      drawRows(t, area, W, x0, x1, y0, y1, 0, 1, depth);
     }
   }
   __syncthreads();  // the shared state is rewritten by the block's next points
 }
 
-// The big list, one block per triangle.
+// The big list, one block per triangle, its rows spread over the threads.
 __device__ __forceinline__ void hairDepthBigBody(const HdView& V, const float4* __restrict__ pos,
                                                  const float4* __restrict__ tan, unsigned* __restrict__ depth,
                                                  const uint32_t* __restrict__ big, uint32_t bigCap, uint32_t blk,
@@ -287,13 +371,11 @@ __device__ __forceinline__ void hairDepthBigBody(const HdView& V, const float4* 
     float area;
     int x0, x1, y0, y1;
     if (!triBox(t, W, H, area, x0, x1, y0, y1)) continue;
-    const uint32_t bw = (uint32_t)(x1 - x0 + 1), bh = (uint32_t)(y1 - y0 + 1);
-    for (uint64_t i = threadIdx.x; i < (uint64_t)bw * bh; i += blockDim.x)
-      triPixel(t, area, W, x0 + (int)(i % bw), y0 + (int)(i / bw), depth);
+    drawRows(t, area, W, x0, x1, y0, y1, (int)threadIdx.x, (int)blockDim.x, depth);  // a row per thread
   }
 }
 
-__global__ void __launch_bounds__(HD_THREADS)
+__global__ void __launch_bounds__(HD_THREADS, 4)
 hairDepthKernel(const HdView V, uint32_t P, uint32_t nPts, const float4* __restrict__ pos,
                 const float4* __restrict__ tan, unsigned* __restrict__ depth, uint32_t* __restrict__ big,
                 uint32_t bigCap) {
@@ -315,7 +397,7 @@ __device__ __forceinline__ void loadView(const HfbUniforms& U, HdView& V) {
 }
 
 // ---- batched: persistent over every instance ----
-__global__ void __launch_bounds__(HD_THREADS) hairDepthBatch(BatchView b) {
+__global__ void __launch_bounds__(HD_THREADS, 4) hairDepthBatch(BatchView b) {
   __shared__ HdShared sh;
   __shared__ HdView V;
   const uint32_t n = b.hdr->n;

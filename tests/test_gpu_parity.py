@@ -533,6 +533,32 @@ def test_hair_depth_bit_exact(oracle, kw, lod):
     assert np.array_equal(g.view(np.uint32), o.view(np.uint32)), f"{int((g != o).sum())} pixels differ"
 
 
+def test_hair_depth_exploded_strands_bit_exact(oracle):
+    """Points thrown far apart (as a simulation that blows up leaves them):
+    long segments whose triangles cover large parts of the viewport take the
+    block-per-triangle path and its row spans; still bit-exact."""
+    from hairfb.passes import HwHairPass
+    inst = small_instance(strands=400, points=16)
+    fr = frame_of(inst)
+    ctx = _ctx(inst)
+    hair = HairObject(inst.hair, inst.cfg.shading_points)
+    rng = np.random.default_rng(9)
+    pos = inst.hair.asset.positions.copy()
+    far = rng.random(len(pos)) < 0.05
+    pos[far, :3] += rng.normal(0, 0.3, (int(far.sum()), 3)).astype(np.float32)
+    hair.positions.copy_(torch.as_tensor(pos))
+    rb = RasterBuffers(ctx, inst.width, inst.height)
+    scene = torch.as_tensor(inst.scene_depth).cuda()
+    out = torch.empty_like(scene)
+    HwHairPass(ctx).cmd_draw_hair_depth(fr.uniforms, hair, scene, out, rb)
+    ctx.sync()
+    o = oracle.hair_depth(fr.uniforms, inst.hair.hair_data, pos, inst.hair.tangents, inst.hair.asset.strands,
+                          inst.scene_depth)
+    g = out.cpu().numpy()
+    assert (o < inst.scene_depth).sum() > 20000, "the long segments cover little: the case does not test"
+    assert np.array_equal(g.view(np.uint32), o.view(np.uint32)), f"{int((g != o).sum())} pixels differ"
+
+
 def test_shading_reads_the_hair_depth(oracle):
     """A frame with the hair depth prepass: the depth it leaves is the
     oracle's for the frame's positions, and the shading computed from it
