@@ -192,12 +192,13 @@ __device__ __forceinline__ bool rowSpan(const Tri& t, bool neg, int y, int& L, i
   return true;
 }
 
-// Vertex coordinates below 2^24 in magnitude: the edge products stay finite
-// (no inf - inf), so rowSpan's monotonicity holds.
+// Vertex coordinates below 1e18 in magnitude (pixel centres are far below):
+// every difference stays below 2^61 and every product below 2^122, so the
+// edge values are finite (no inf - inf) and rowSpan's monotonicity holds.
 __device__ __forceinline__ bool spanSafe(const Tri& t) {
   bool ok = true;
 #pragma unroll
-  for (int k = 0; k < 3; k++) ok = ok && fabsf(t.v[k].x) < 16777216.0f && fabsf(t.v[k].y) < 16777216.0f;
+  for (int k = 0; k < 3; k++) ok = ok && fabsf(t.v[k].x) < 1e18f && fabsf(t.v[k].y) < 1e18f;
   return ok;
 }
 
