@@ -55,6 +55,9 @@ WORKLOADS = {
     "plain_small": "2,000 x 16 strands, 640x480, 16 px tiles, 8 depth bins, 4 slices, 8 shading points",
     # the 4K stress frame: 200k strands
     "stress": "200,000 x 32 strands (60% ponytail), 3840x2160, 32 depth bins, 8 slices, 32 shading points",
+    # a hair asset in the reference's formats (--tfx, --sdf) with the reference's default constants
+    "asset": "a TFX hair asset (+ binary SDF) at 1920x1080 with the reference's default CONFIG: 8 px tiles, "
+             "32 depth bins, 8 slices, 64 shading points, 64^3 grids, 7 iterations",
 }
 
 
@@ -73,6 +76,8 @@ def parse():
     ap.add_argument("--capture-frames", type=int, default=0,
                     help="profiler runs: set up the workload, render this many frames (batched64: batched "
                          "frames at --tile-size/--depth-bins, no tuning), print 'ok' and exit; no timing")
+    ap.add_argument("--tfx", help="hair asset (TFX file) of the asset workload")
+    ap.add_argument("--sdf", help="binary SDF of the asset workload's head (optional)")
     ap.add_argument("--tile-size", type=int, default=16)
     ap.add_argument("--depth-bins", type=int, default=8)
     return ap.parse_args()
@@ -108,8 +113,28 @@ def capture(args):
           f"{torch.cuda.max_memory_allocated() / 1e9:.2f} GB allocated by torch", flush=True)
 
 
+ASSET_FILES = {}  # --tfx / --sdf of the "asset" workload
+
+
+def data_label(wl):
+    if wl == "asset":
+        return f"hair asset {os.path.basename(ASSET_FILES.get('tfx', ''))} (+ SDF " \
+               f"{os.path.basename(ASSET_FILES.get('sdf') or '') or 'none'}), the user's files"
+    return "synthetic (seeded; no public dataset exists for this path)"
+
+
 def make_instance(name, seed):
     from hairfb import synthetic
+    if name == "asset":
+        if "tfx" not in ASSET_FILES:
+            raise SystemExit("the asset workload needs --tfx FILE (and optionally --sdf FILE)")
+        with open(ASSET_FILES["tfx"], "rb") as f:
+            tfx = f.read()
+        sdf = None
+        if ASSET_FILES.get("sdf"):
+            with open(ASSET_FILES["sdf"], "rb") as f:
+                sdf = f.read()
+        return synthetic.asset_instance(tfx, sdf)
     return getattr(synthetic, name)(seed=seed)
 
 
@@ -660,6 +685,8 @@ def report_batched(args, res, world, dist):
 
 def main():
     args = parse()
+    if args.tfx:
+        ASSET_FILES.update(tfx=args.tfx, sdf=args.sdf)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     dist = None
@@ -722,7 +749,7 @@ def main():
             "impl": "reference", "metric": "frames/s", "value": fps, "unit": "frames/s",
             "n_gpus": args.gpus, "steps": n, "warmup": max(1, min(args.warmup, 3)), "ms_per_step": 1000.0 * el / n,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic",
+            "data": data_label(wl),
             "config": {"workload": wl, "describe": WORKLOADS[wl],
                        "implementation": "C restatement of the reference WGSL passes, OpenMP"},
             "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
@@ -813,7 +840,7 @@ def main():
         "metric": "frames/s", "value": fps, "unit": "frames/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": frame_avg,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded; no public dataset exists for this path)",
+        "data": data_label(wl),
         "config": {"workload": wl, "describe": WORKLOADS[wl], "l2": "flushed (256 MiB write) between frames",
                    "p50_ms": p(0.5), "p99_ms": p(0.99), "segments_per_s": world * segments * len(srt) / total,
                    "tile_records_per_frame": K, "pass_ms": {k: round(v, 4) for k, v in pass_avg.items()},

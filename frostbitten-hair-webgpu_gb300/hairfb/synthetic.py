@@ -208,6 +208,106 @@ def make_instance(rng, *, strands, points, width, height, tile_size=16, depth_bi
                     wind_amplitude=wind_amplitude)
 
 
+def sdf_depth(width: int, height: int, camera: Camera, vol: SdfVolume, scale: int = 4,
+              steps: int = 96) -> np.ndarray:
+    """NDC depth of the SDF's zero surface seen by the camera (sphere tracing
+    on the host, trilinear distances, at 1/scale of the viewport then
+    repeated to it); 1.0 where a ray misses.  Row 0 is the top."""
+    w, h = max(1, width // scale), max(1, height // scale)
+    view = M.to_rows(camera.view())
+    proj = M.to_rows(camera.proj(width, height))
+    vp = proj @ view
+    inv_vp = np.linalg.inv(vp)
+    xs = (np.arange(w) + 0.5) / w * 2.0 - 1.0
+    ys = 1.0 - (np.arange(h) + 0.5) / h * 2.0
+    X, Y = np.meshgrid(xs, ys)
+    near = np.stack([X, Y, np.zeros_like(X), np.ones_like(X)], -1) @ inv_vp.T
+    far = np.stack([X, Y, np.ones_like(X), np.ones_like(X)], -1) @ inv_vp.T
+    o = (near[..., :3] / near[..., 3:]).reshape(-1, 3)
+    d = _unit(far[..., :3] / far[..., 3:] - near[..., :3] / near[..., 3:]).reshape(-1, 3)
+    D = vol.dims
+    lo, hi = np.asarray(vol.bounds_min, np.float64), np.asarray(vol.bounds_max, np.float64)
+    grid = vol.distances.reshape(D, D, D).astype(np.float64)  # [z][y][x]
+
+    def dist(p):
+        t = np.clip((p - lo) / (hi - lo), 0.0, 1.0) * D - 0.5
+        i0 = np.clip(np.floor(t).astype(np.int64), 0, D - 1)
+        i1 = np.clip(i0 + 1, 0, D - 1)
+        f = np.clip(t - np.floor(t), 0.0, 1.0)
+        out = 0.0
+        for dz in (0, 1):
+            for dy in (0, 1):
+                for dx in (0, 1):
+                    wgt = ((f[:, 0] if dx else 1 - f[:, 0]) * (f[:, 1] if dy else 1 - f[:, 1])
+                           * (f[:, 2] if dz else 1 - f[:, 2]))
+                    out = out + wgt * grid[(i1 if dz else i0)[:, 2], (i1 if dy else i0)[:, 1], (i1 if dx else i0)[:, 0]]
+        # outside the volume the distance grows at least with the distance to it
+        outside = np.linalg.norm(p - np.clip(p, lo, hi), axis=1)
+        return out + outside
+
+    # start where the ray enters the volume's box
+    with np.errstate(divide="ignore", invalid="ignore"):
+        t0 = (lo - o) / d
+        t1 = (hi - o) / d
+    tmin = np.nanmax(np.minimum(t0, t1), axis=1).clip(0.0)
+    tmax = np.nanmin(np.maximum(t0, t1), axis=1)
+    t = tmin.copy()
+    hit = np.zeros(len(o), bool)
+    alive = tmax > tmin
+    eps = float(np.min(hi - lo)) * 1e-3
+    for _ in range(steps):
+        if not alive.any():
+            break
+        idx = np.nonzero(alive)[0]
+        dd = dist(o[idx] + t[idx, None] * d[idx])
+        h_now = dd < eps
+        hit[idx[h_now]] = True
+        t[idx] += np.maximum(dd, eps * 0.5)
+        alive[idx[h_now | (t[idx] > tmax[idx])]] = False
+    p = o + t[:, None] * d
+    clip = np.concatenate([p, np.ones((len(p), 1))], -1) @ vp.T
+    z = np.where(hit, clip[:, 2] / clip[:, 3], 1.0).reshape(h, w)
+    z = np.repeat(np.repeat(z, scale, 0), scale, 1)
+    full = np.ones((height, width))
+    full[: z.shape[0], : z.shape[1]] = z[:height, :width]
+    return full.astype(np.float32).reshape(-1)
+
+
+def asset_instance(tfx: bytes, sdf: bytes | None = None, width: int = 1920, height: int = 1080,
+                   **cfg_kw) -> Instance:
+    """A hair asset in the reference's file formats (a TFX file and,
+    optionally, the binary SDF of its head), set up as the reference's
+    default scene: CONFIG's pass constants (tile 8, 32 depth bins, 8 slices,
+    64 shading points, 64^3 grids, 7 iterations) unless given, its
+    simulation settings and collision sphere (constants.ts:186-340), the
+    camera framing the hair's bounding sphere.  The scene depth is the SDF's
+    zero surface (the head) where an SDF is given, else the collision
+    sphere's."""
+    from .formats import parse_sdf, parse_tfx
+    asset = parse_tfx(tfx)
+    hb = build_hair_buffers(asset)
+    cfg = HairConfig(**cfg_kw)
+    sim = SimulationParams()
+    if sdf is not None:
+        vol = parse_sdf(sdf)
+    else:
+        R = float(hb.sphere_radius) * 1.1
+        c = hb.sphere_center.astype(np.float64)
+        cs = sim.collision_sphere
+        vol = sdf_from_function(sphere_sdf(np.asarray(cs[:3]), cs[3]), 32, c - R, c + R)
+    gmin, gmax = scale_bounding_box(hb.bbox[0], hb.bbox[1], sim.grid_scale)
+    cam = framing_camera(hb.sphere_center, float(hb.sphere_radius))
+    scene = SceneParams(width=width, height=height, camera=cam,
+                        sdf_bounds=(vol.bounds_min, vol.bounds_max), grid_bounds=(gmin, gmax),
+                        hair_sphere=(hb.sphere_center, float(hb.sphere_radius)),
+                        collision_sphere=sim.collision_sphere, sdf_distance_offset=sim.sdf_distance_offset)
+    cs = np.asarray(sim.collision_sphere[:3], np.float64)
+    depth = sdf_depth(width, height, cam, vol) if sdf is not None else \
+        sphere_depth(width, height, cam, cs, sim.collision_sphere[3])
+    return Instance(cfg, sim, hb, vol, scene, depth, cs, float(sim.collision_sphere[3]),
+                    np.asarray(M.spherical_to_cartesian(sim.wind_dir_phi, sim.wind_dir_theta)))
+
+
 def plain_small(seed: int = 0, **kw) -> Instance:
     """2,000 x 16 strands at 640x480, tiles 16, 8 bins, 4 slices, 8 shading
     points, 32^3 sphere SDF and grids, one step at dt 1/60, no wind."""

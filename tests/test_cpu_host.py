@@ -193,3 +193,22 @@ def test_strand_grid_order_is_a_morton_permutation():
     d_order = np.linalg.norm(np.diff(roots[order], axis=0), axis=1).mean()
     d_plain = np.linalg.norm(np.diff(roots, axis=0), axis=1).mean()
     assert d_order < 0.5 * d_plain
+
+
+def test_asset_instance_from_reference_formats():
+    """synthetic.asset_instance on files in the reference's formats (a TFX
+    written from a grown asset and the binary SDF of a sphere): the
+    reference's default pass constants, and a scene depth that hits the
+    head where the SDF's zero surface is in view."""
+    rng = np.random.Generator(np.random.PCG64(5))
+    grown = synthetic.grow_hair(rng, 500, 16, center=(0.0, 1.5, 0.0), head_radius=0.1)
+    tfx = formats.write_tfx(grown)
+    vol = synthetic.sdf_from_function(synthetic.sphere_sdf(np.array([0.0, 1.5, 0.0]), 0.1), 32,
+                                      np.array([-0.2, 1.3, -0.2]), np.array([0.2, 1.7, 0.2]))
+    inst = synthetic.asset_instance(tfx, formats.write_sdf(vol), width=320, height=180)
+    assert inst.hair.asset.strands == 500 and inst.hair.asset.points_per_strand == 16
+    assert (inst.cfg.tile_size, inst.cfg.tile_depth_bins, inst.cfg.slices_per_pixel, inst.cfg.shading_points) \
+        == (8, 32, 8, 64)
+    assert inst.scene_depth.shape == (320 * 180,)
+    hit = inst.scene_depth < 1.0
+    assert 0.01 < hit.mean() < 0.9 and (inst.scene_depth[hit] > 0.0).all()
