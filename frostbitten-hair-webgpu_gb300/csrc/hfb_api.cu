@@ -449,6 +449,16 @@ int hfb_hair_depth(HfbCtx* c, const HfbUniforms* u, const HfbHairData* h, const 
   HFB_LAUNCH(c, hfb::launchHairDepth(c, *u, *h, pos, tan, strandsToRender, sceneDepth, hairDepth, *rb), "hair_depth");
 }
 
+int hfb_present(HfbCtx* c, const HfbUniforms* u, const HfbRasterBuffers* rb, const float* scene, uint8_t* rgba) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, u && rgba, "NULL argument");
+  HFB_REQUIRE(c, !scene || aligned16(scene), "vec4 buffers must be 16-byte aligned");
+  std::string err = checkRaster(c, rb);
+  if (err.empty()) err = checkViewport(u, rb);
+  HFB_REQUIRE(c, err.empty(), err);
+  HFB_LAUNCH(c, hfb::launchPresent(c, *u, rb->width, rb->height, rb->rasterizerResult + 4, scene, rgba), "present");
+}
+
 // Checks one instance of a frame (the union of the per-pass checks).
 static std::string checkInstance(const HfbCtx* c, const HfbInstance* in) {
   if (!in) return "instance is NULL";

@@ -296,7 +296,9 @@ cudaError_t launchBatchDepthCopy(HfbCtx* c, const BatchView& b);
 cudaError_t launchHairDepth(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, const float* pos, const float* tan,
                             uint32_t strandsToRender, const float* sceneDepth, float* hairDepth,
                             HfbRasterBuffers& rb);
-// Blocks of the grid splat (GridPostSimPass) over `points` points.
+cudaError_t launchPresent(HfbCtx* c, const HfbUniforms& u, uint32_t W, uint32_t H, const float* result,
+                          const float* scene, uint8_t* rgba);
+// Blocks of the grid splat (GridPostSimPass) over `strands` strands.
 uint32_t gridPostBlocks(uint32_t points);
 // Blocks of the hair depth pass over `points` points.
 uint32_t hairDepthBlocks(uint32_t points);

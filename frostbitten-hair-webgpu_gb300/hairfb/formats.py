@@ -76,3 +76,16 @@ def write_sdf(vol: SdfVolume) -> bytes:
     hdr = struct.pack("<II", vol.dims, 0)
     b = np.concatenate([np.asarray(vol.bounds_min, np.float32), np.asarray(vol.bounds_max, np.float32)])
     return hdr + b.tobytes() + np.ascontiguousarray(vol.distances, np.float32).tobytes()
+
+
+def write_png(rgba) -> bytes:
+    """An (H, W, 4) uint8 image as PNG bytes (8-bit RGBA, no filtering)."""
+    import zlib
+    img = np.ascontiguousarray(rgba, dtype=np.uint8)
+    h, w = img.shape[:2]
+    raw = b"".join(b"\x00" + img[y].tobytes() for y in range(h))
+
+    def chunk(tag: bytes, data: bytes) -> bytes:
+        return struct.pack(">I", len(data)) + tag + data + struct.pack(">I", zlib.crc32(tag + data) & 0xFFFFFFFF)
+    return (b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 6, 0, 0, 0))
+            + chunk(b"IDAT", zlib.compress(raw, 6)) + chunk(b"IEND", b""))

@@ -100,6 +100,7 @@ SIGNATURES = {
     "hfb_fine_pass": (I, [P, P, P, P, P, P, P, P]),
     "hfb_tiles_pass_noalloc": (I, [P, P, P, P, P, P, U32, P]),
     "hfb_hair_depth": (I, [P, P, P, P, P, U32, P, P, P]),
+    "hfb_present": (I, [P, P, P, P, P]),
     "hfb_frame": (I, [P, P]),
     "hfb_frame_batch": (I, [P, P, U32]),
     "hfb_frame_batch_profile": (I, [P, P, U32, P]),

@@ -279,6 +279,25 @@ class HwHairPass:
                       byref(rb.rb))
 
 
+class PresentPass:
+    """src/passes/hairCombine/hairCombinePass.ts + src/passes/presentPass/
+    presentPass.ts (final display mode): the frame's 8-bit image."""
+    NAME = "PresentPass"
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+
+    def cmd_draw(self, uniforms: bytes, rb: RasterBuffers, scene_color: torch.Tensor | None = None,
+                 out: torch.Tensor | None = None) -> torch.Tensor:
+        """The fine pass's result over scene_color ((H, W, 4) float32, row 0
+        at the top; None = black), tone mapped: (H, W, 4) uint8, row 0 at
+        the top."""
+        if out is None:
+            out = torch.empty((rb.height, rb.width, 4), dtype=torch.uint8, device="cuda")
+        self.ctx.call("hfb_present", _ub(uniforms), byref(rb.rb), ptr(scene_color), ptr(out))
+        return out
+
+
 def clear_before_render(ctx: Context, rb: RasterBuffers):
     """cmdClearBeforeRender of the tiles, fine and sort passes."""
     ctx.call("hfb_clear_before_render", byref(rb.rb))

@@ -22,7 +22,7 @@ from .config import HairConfig
 from .lib import Context, HfbInstance, ptr
 from .passes import (GridPostSimPass, GridPreSimPass, HairFinePass, HairObject, HairShadingPass,
                      HairSimIntegrationPass, HairTileSortPass, HairTilesPass, HwHairPass, PhysicsGrids,
-                     RasterBuffers, SdfCollider, clear_before_render)
+                     PresentPass, RasterBuffers, SdfCollider, clear_before_render)
 
 
 class Renderer:
@@ -103,6 +103,12 @@ class Renderer:
         if self.hair_depth is not None:  # updateResourcesForNextFrame, renderer.ts:286-296
             self.hw_hair.cmd_draw_hair_depth(self.uniforms, self.hair, self.scene_depth, self.hair_depth, self.rb)
         self.shading.cmd_compute_shading_points(self.uniforms, self.hair, self.shading_depth)
+
+    def image(self, scene_color: torch.Tensor | None = None) -> torch.Tensor:
+        """The last frame composited over scene_color and presented
+        (HairCombinePass + PresentPass): (H, W, 4) uint8 on the device, row
+        0 at the top; formats.write_png makes a PNG of it."""
+        return PresentPass(self.ctx).cmd_draw(self.uniforms, self.rb, scene_color)
 
     def frame(self) -> None:
         """cmdRender, renderer.ts:171-210 (hair passes only), pass by pass."""

@@ -342,6 +342,16 @@ typedef struct HfbInstance {
  * interpolated in screen space; the GPU rasterizer's own snapping and
  * depth24 storage are not reproduced.  Uses rb's scratch as working memory
  * (the raster passes' scratch is free after the fine pass). */
+/* HairCombinePass + PresentPass (hairCombinePass.wgsl.ts:51-89 with its
+ * src-alpha blend, presentPass.wgsl.ts main_fs in DISPLAY_MODE_FINAL): the
+ * fine pass's result (rb, read upside down as the combine pass does) over
+ * sceneColor (W*H vec4f, row 0 at the top; NULL = black), then the 8x8
+ * Bayer dither, exposure, ACES tone mapping and gamma of Uniforms.colorMgmt
+ * (gamma, exposure, dither strength), stored as unorm8: rgba is W*H RGBA8
+ * (device), row 0 at the top, alpha 255. */
+HFB_API int hfb_present(HfbCtx* ctx, const HfbUniforms* uniforms, const HfbRasterBuffers* rb,
+                        const float* sceneColor, uint8_t* rgba);
+
 HFB_API int hfb_hair_depth(HfbCtx* ctx, const HfbUniforms* uniforms, const HfbHairData* hair, const float* positions,
                            const float* tangents, uint32_t strandsToRender, const float* sceneDepth,
                            float* hairDepth, HfbRasterBuffers* rb);

@@ -1373,6 +1373,48 @@ EXPORT void oracle_hair_depth(const void* uniforms, const void* hairData, const 
     }
 }
 
+/* HairCombinePass (hairCombinePass.wgsl.ts:51-89: fragment row y reads
+ * result row H - 1 - y; blend src-alpha, one-minus-src-alpha over the scene
+ * colour, hairCombinePass.ts:40-52) and PresentPass (presentPass.wgsl.ts
+ * main_fs, DISPLAY_MODE_FINAL: 8x8 Bayer dither, dither.wgsl.ts:26-53;
+ * exposure; ACES, aces.wgsl.ts:6-13; gamma), stored as unorm8 (round to
+ * nearest even).  result: W*H vec4f (the pixels of HairRasterResult);
+ * scene: W*H vec4f or NULL (black); out: W*H RGBA8, row 0 at the top. */
+static const uint8_t PRESENT_BAYER[64] = {0,  32, 8,  40, 2,  34, 10, 42, 48, 16, 56, 24, 50, 18, 58, 26,
+                                          12, 44, 4,  36, 14, 46, 6,  38, 60, 28, 52, 20, 62, 30, 54, 22,
+                                          3,  35, 11, 43, 1,  33, 9,  41, 51, 19, 59, 27, 49, 17, 57, 25,
+                                          15, 47, 7,  39, 13, 45, 5,  37, 63, 31, 55, 23, 61, 29, 53, 21};
+
+static float presentAces(float x) {
+  float num = x * (2.51f * x + 0.03f);
+  float den = x * (2.43f * x + 0.59f) + 0.14f;
+  return sat(num / den);
+}
+
+EXPORT void oracle_present(const void* uniforms, const float* result, const float* scene, uint8_t* out) {
+  const ORenderUniforms* U = (const ORenderUniforms*)uniforms;
+  uint32_t W = f2u(U->viewport.x), H = f2u(U->viewport.y);
+  float gamma = U->colorMgmt.x, exposure = U->colorMgmt.y, ditherStr = U->colorMgmt.z;
+  for (uint32_t y = 0; y < H; y++)
+    for (uint32_t x = 0; x < W; x++) {
+      size_t i = (size_t)y * W + x;
+      const float* src = result + 4 * ((size_t)(H - 1u - y) * W + x);
+      float dst[4] = {0.0f, 0.0f, 0.0f, 1.0f};
+      if (scene) memcpy(dst, scene + 4 * i, sizeof dst);
+      float ia = 1.0f - src[3];
+      float dither = (float)PRESENT_BAYER[(y % 8u) * 8u + (x % 8u)] / 63.0f * ditherStr / 256.0f;
+      for (int k = 0; k < 3; k++) {
+        float v = src[k] * src[3] + dst[k] * ia;
+        v = v + dither;
+        v = v * exposure;
+        v = presentAces(v);
+        v = powf(v, 1.0f / gamma);
+        out[4 * i + k] = (uint8_t)nearbyintf(sat(v) * 255.0f);
+      }
+      out[4 * i + 3] = 255;
+    }
+}
+
 EXPORT void oracle_shading(const OracleConfig* cfg, const void* uniforms, const void* hairData,
                            const float* positions, const float* tangents, const float* depth,
                            const float* ao, uint32_t aoW, uint32_t aoH,

@@ -73,6 +73,7 @@ def _declare(lib):
     lib.oracle_grid_post_sim.argtypes = [P, P, P, P, P, P]
     lib.oracle_shading.argtypes = [P, P, P, P, P, P, P, U, U, P, U, P]
     lib.oracle_hair_depth.argtypes = [P, P, P, P, U, P]
+    lib.oracle_present.argtypes = [P, P, P, P]
     lib.oracle_sample_sdf.argtypes = [P, U, P, P, P]
     lib.oracle_sample_sdf.restype = ctypes.c_float
     lib.oracle_f32_to_f16.argtypes = [ctypes.c_float]
@@ -201,6 +202,21 @@ def hair_depth(uniforms: bytes, hair_data: bytes, positions, tangents, strands_t
     u, h = _Bytes(uniforms), _Bytes(hair_data)
     lib.oracle_hair_depth(u.ptr, h.ptr, _p(_f32(positions)), _p(_f32(tangents)), strands_to_render, _p(out))
     return out
+
+
+def present(uniforms: bytes, result, scene_color=None):
+    """HairCombinePass + PresentPass: result = the W*H vec4f pixels of the
+    fine pass (without the header), scene_color W*H vec4f or None; returns
+    (H, W, 4) uint8, row 0 at the top."""
+    lib = load()
+    u = _Bytes(uniforms)
+    res = _f32(result)
+    n = res.size // 4
+    out = np.zeros(n * 4, np.uint8)
+    sc = _f32(scene_color) if scene_color is not None else None
+    lib.oracle_present(u.ptr, _p(res), _p(sc) if sc is not None else None, out.ctypes.data)
+    W = int(round(np.frombuffer(uniforms, np.float32)[16 * 9]))
+    return out.reshape(-1, W, 4)
 
 
 def shading(cfg, uniforms: bytes, hair_data: bytes, positions, tangents, depth, strands,

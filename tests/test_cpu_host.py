@@ -212,3 +212,18 @@ def test_asset_instance_from_reference_formats():
     assert inst.scene_depth.shape == (320 * 180,)
     hit = inst.scene_depth < 1.0
     assert 0.01 < hit.mean() < 0.9 and (inst.scene_depth[hit] > 0.0).all()
+
+
+def test_png_writer():
+    """formats.write_png: signature, IHDR fields and the pixels back through zlib."""
+    import zlib
+    img = np.random.default_rng(2).integers(0, 256, (7, 5, 4), dtype=np.uint8)
+    png = formats.write_png(img)
+    assert png[:8] == b"\x89PNG\r\n\x1a\n"
+    w, h, depth, ctype = struct.unpack(">IIBB", png[16:26])
+    assert (w, h, depth, ctype) == (5, 7, 8, 6)
+    idat = png.index(b"IDAT")
+    n = struct.unpack(">I", png[idat - 4:idat])[0]
+    raw = zlib.decompress(png[idat + 4:idat + 4 + n])
+    rows = np.frombuffer(raw, np.uint8).reshape(7, 1 + 5 * 4)
+    assert (rows[:, 0] == 0).all() and np.array_equal(rows[:, 1:].reshape(7, 5, 4), img)

@@ -559,6 +559,36 @@ def test_hair_depth_exploded_strands_bit_exact(oracle):
     assert np.array_equal(g.view(np.uint32), o.view(np.uint32)), f"{int((g != o).sum())} pixels differ"
 
 
+@pytest.mark.parametrize("scene", [False, True])
+def test_present_within_1_255(oracle, scene, tmp_path):
+    """HairCombinePass + PresentPass on a rendered frame (over black, and over
+    a scene colour image): every channel within 1 of the oracle's unorm8
+    (pow is not correctly rounded on either side); the image is written as
+    a PNG."""
+    from hairfb import formats
+    from hairfb.passes import PresentPass
+    from hairfb.renderer import Renderer
+    inst = small_instance(strands=1500)
+    r = Renderer(inst, 0, hair_depth=True)
+    r.before_first_frame()
+    r.frame()
+    r.frame()
+    rng = np.random.default_rng(1)
+    sc = rng.uniform(0.0, 2.0, (inst.height, inst.width, 4)).astype(np.float32) if scene else None
+    img = PresentPass(r.ctx).cmd_draw(r.uniforms, r.rb, torch.as_tensor(sc).cuda() if scene else None)
+    r.ctx.sync()
+    g = img.cpu().numpy()
+    o = oracle.present(r.uniforms, r.rb.read_result()[4:], sc)
+    assert g.shape == o.shape == (inst.height, inst.width, 4)
+    diff = np.abs(g.astype(np.int32) - o.astype(np.int32))
+    assert diff.max() <= 1, f"max difference {diff.max()} at {np.unravel_index(diff.argmax(), diff.shape)}"
+    assert (g[..., 3] == 255).all()
+    assert len(np.unique(g[..., :3].reshape(-1, 3), axis=0)) > 50, "a flat image: the case does not test"
+    png = formats.write_png(g)
+    (tmp_path / "frame.png").write_bytes(png)
+    assert png[:8] == b"\x89PNG\r\n\x1a\n"
+
+
 def test_shading_reads_the_hair_depth(oracle):
     """A frame with the hair depth prepass: the depth it leaves is the
     oracle's for the frame's positions, and the shading computed from it
