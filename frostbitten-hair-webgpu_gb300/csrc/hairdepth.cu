@@ -405,7 +405,8 @@ __global__ void __launch_bounds__(HD_THREADS, 4) hairDepthBatch(BatchView b) {
   const uint32_t* row = b.prefix + BK_HAIR_DEPTH * (BATCH_MAX + 1);
   const uint32_t total = row[n];
   uint32_t cur = 0xFFFFFFFFu;
-  for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
+  __shared__ uint32_t vbNext;
+  for (uint32_t v = batchNext(b.hdr, BK_HAIR_DEPTH, &vbNext); v < total; v = batchNext(b.hdr, BK_HAIR_DEPTH, &vbNext)) {
     const uint32_t i = batchFind(row, n, v);
     const BatchInst& I = b.insts[i];
     if (i != cur) {

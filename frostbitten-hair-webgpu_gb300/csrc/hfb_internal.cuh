@@ -254,7 +254,9 @@ struct BatchHdr {
   uint32_t n;
   uint32_t fineQueue;  // next global work item of the batched fine pass
   uint32_t pad[2];
+  uint32_t queue[BK_COUNT];  // next virtual block of each kind (batchNext)
 };
+static_assert(sizeof(BatchHdr) <= 256, "the batch header fits before the prefix rows");
 constexpr size_t BATCH_PREFIX_OFF = 256;
 constexpr size_t BATCH_ITEMS_OFF = BATCH_PREFIX_OFF + (size_t)BK_COUNT * (BATCH_MAX + 1) * 4;
 constexpr size_t BATCH_INSTS_OFF = (BATCH_ITEMS_OFF + (size_t)(BATCH_MAX + 1) * 4 + 255) & ~size_t(255);
@@ -280,6 +282,17 @@ __device__ __forceinline__ uint32_t batchFind(const uint32_t* __restrict__ row, 
     if (__ldg(&row[mid]) <= v) lo = mid; else hi = mid;
   }
   return lo;
+}
+
+// The next virtual block of kind k for the calling CTA, from the header's
+// counter (zeroed by every frame's table upload): CTAs take blocks as they
+// finish, so uneven blocks do not leave some CTAs with a long tail.  Every
+// thread of the CTA calls it; `slot` is a shared word.
+__device__ __forceinline__ uint32_t batchNext(BatchHdr* hdr, uint32_t k, uint32_t* slot) {
+  __syncthreads();  // the previous block number has been read by every thread
+  if (threadIdx.x == 0) *slot = atomicAdd(&hdr->queue[k], 1u);
+  __syncthreads();
+  return *slot;
 }
 
 // Batched launchers: one persistent launch of kind k over all instances.

@@ -1845,7 +1845,9 @@ cudaError_t launchFineT(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, c
   const uint32_t n = b.hdr->n;                                        \
   const uint32_t* row = b.prefix + (KIND) * (BATCH_MAX + 1);          \
   const uint32_t totalVb = row[n];                                    \
-  for (uint32_t v = blockIdx.x; v < totalVb; v += gridDim.x) {        \
+  __shared__ uint32_t vbNext;                                         \
+  for (uint32_t v = batchNext(b.hdr, (KIND), &vbNext); v < totalVb;  \
+       v = batchNext(b.hdr, (KIND), &vbNext)) {                       \
     const uint32_t i = batchFind(row, n, v);                          \
     const BatchInst& I = b.insts[i];                                  \
     if (!HFB_EXPECT(i < n && I.W && I.H && I.W <= 65536 && I.H <= 65536 && I.scratch && I.segBuf && \

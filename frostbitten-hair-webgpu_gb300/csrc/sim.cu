@@ -490,7 +490,8 @@ __global__ void __launch_bounds__(256) gridPreSimBatch(BatchView b, uint32_t G) 
   const uint32_t n = b.hdr->n;
   const uint32_t* row = b.prefix + BK_GRID_PRE * (BATCH_MAX + 1);
   const uint32_t total = row[n];
-  for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
+  __shared__ uint32_t vbNext;
+  for (uint32_t v = batchNext(b.hdr, BK_GRID_PRE, &vbNext); v < total; v = batchNext(b.hdr, BK_GRID_PRE, &vbNext)) {
     const uint32_t i = batchFind(row, n, v);
     const BatchInst& I = b.insts[i];
     gridPreSimBody(I.SU, G, I.dv, I.gw, I.sdf, I.sdfDims, (v - row[i]) * 256u + threadIdx.x);
@@ -502,7 +503,8 @@ __global__ void __launch_bounds__(SIM_THREADS, 4) simIntegrateBatch(BatchView b,
   const uint32_t n = b.hdr->n;
   const uint32_t* row = b.prefix + BK_INTEGRATE * (BATCH_MAX + 1);
   const uint32_t total = row[n];
-  for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
+  __shared__ uint32_t vbNext;
+  for (uint32_t v = batchNext(b.hdr, BK_INTEGRATE, &vbNext); v < total; v = batchNext(b.hdr, BK_INTEGRATE, &vbNext)) {
     const uint32_t i = batchFind(row, n, v);
     const BatchInst& I = b.insts[i];
     // integration reads positions[1 - current] (prev) and [current] (now), writes the former
@@ -518,7 +520,8 @@ __global__ void __launch_bounds__(GP_THREADS) gridPostSimBatch(BatchView b, uint
   const uint32_t n = b.hdr->n;
   const uint32_t* row = b.prefix + BK_GRID_POST * (BATCH_MAX + 1);
   const uint32_t total = row[n];
-  for (uint32_t v = blockIdx.x; v < total; v += gridDim.x) {
+  __shared__ uint32_t vbNext;
+  for (uint32_t v = batchNext(b.hdr, BK_GRID_POST, &vbNext); v < total; v = batchNext(b.hdr, BK_GRID_POST, &vbNext)) {
     const uint32_t i = batchFind(row, n, v);
     const BatchInst& I = b.insts[i];
     // after the swap: prev = the old current positions, now = the new ones
