@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(256) depthCopyBatch(BatchView b) {
     unsigned char* dst = (unsigned char*)I.hairDepth;
     for (size_t x = off + threadIdx.x * 4u; x < end; x += 256u * 4u)
       *HFB_G(reinterpret_cast<uint32_t*>(dst + x)) = *HFB_G(reinterpret_cast<const uint32_t*>(src + x));
-    if (v == row[i] && threadIdx.x == 0) *HFB_G(reinterpret_cast<uint32_t*>(I.scratch)) = 0u;
+    if (v == row[i] && threadIdx.x == 0 && I.hdList) *HFB_G(I.hdList) = 0u;
   }
 }
 
@@ -302,6 +302,10 @@ static void fillInstance(const HfbConfig& cfg, const HfbInstance& s, BatchInst& 
   I.result = s.raster.rasterizerResult;
   I.scratch = (unsigned char*)s.raster.scratch;
   I.scratchBytes = s.raster.scratchBytes;
+  I.hdList = s.hairDepth ? hairDepthList(s.raster.scratch, s.raster.scratchBytes,
+                                         rasterPassScratchBytes(cfg, I.W, I.H, s.raster.maxDrawnSegments), &I.hdCap)
+                         : nullptr;
+  if (!I.hdList) I.hdCap = 0;
 }
 
 // Rough GPU work of one instance's frame, for balancing the groups: the

@@ -289,7 +289,7 @@ __device__ __forceinline__ void hairDepthBlock(const HdView& V, uint32_t P, uint
       if (!triBox(t, W, H, area, x0, x1, y0, y1)) continue;
       const uint32_t bw = (uint32_t)(x1 - x0 + 1), bh = (uint32_t)(y1 - y0 + 1);
       if ((uint64_t)bw * bh > HD_BIG_AREA) {
-        const uint32_t slot = pt < 0x80000000u ? atomicAdd(HFB_G(&big[0]), 1u) : bigCap;
+        const uint32_t slot = bigCap > 0u && pt < 0x80000000u ? atomicAdd(HFB_G(&big[0]), 1u) : bigCap;
         if (slot < bigCap)
           *HFB_G(&big[1u + slot]) = (pt << 1) | tr;
         else
@@ -360,7 +360,7 @@ __device__ __forceinline__ void hairDepthBigBody(const HdView& V, const float4* 
                                                  const float4* __restrict__ tan, unsigned* __restrict__ depth,
                                                  const uint32_t* __restrict__ big, uint32_t bigCap, uint32_t blk,
                                                  uint32_t nblk) {
-  const uint32_t n = min(*HFB_G(&big[0]), bigCap);
+  const uint32_t n = bigCap ? min(*HFB_G(&big[0]), bigCap) : 0u;
   const uint32_t W = f2u(V.W), H = f2u(V.H);
   for (uint32_t e = blk; e < n; e += nblk) {
     const uint32_t ent = *HFB_G(&big[1u + e]);
@@ -414,8 +414,7 @@ __global__ void __launch_bounds__(HD_THREADS, 4) hairDepthBatch(BatchView b) {
       cur = i;
     }
     hairDepthBlock(V, I.P, min(I.strandsToRender, I.S) * I.P, I.posNew, I.tan,
-                   reinterpret_cast<unsigned*>(I.hairDepth), reinterpret_cast<uint32_t*>(I.scratch),
-                   hairDepthBigCap(I.scratchBytes), v - row[i], sh);
+                   reinterpret_cast<unsigned*>(I.hairDepth), I.hdList, I.hdCap, v - row[i], sh);
   }
 }
 
@@ -426,8 +425,7 @@ __global__ void __launch_bounds__(HD_THREADS) hairDepthBigBatch(BatchView b) {
     const BatchInst& I = b.insts[i];
     if (!I.hairDepth) continue;
     loadView(I.U, V);
-    hairDepthBigBody(V, I.posNew, I.tan, reinterpret_cast<unsigned*>(I.hairDepth),
-                     reinterpret_cast<const uint32_t*>(I.scratch), hairDepthBigCap(I.scratchBytes), blockIdx.x,
+    hairDepthBigBody(V, I.posNew, I.tan, reinterpret_cast<unsigned*>(I.hairDepth), I.hdList, I.hdCap, blockIdx.x,
                      gridDim.x);
   }
 }
@@ -441,14 +439,15 @@ cudaError_t launchHairDepth(HfbCtx* c, const HfbUniforms& u, const HfbHairData& 
                             HfbRasterBuffers& rb) {
   HFB_CHECK_BIND(c);
   const size_t px = (size_t)rb.width * rb.height;
+  uint32_t cap = 0;
+  uint32_t* big = hairDepthList(rb.scratch, rb.scratchBytes,
+                                rasterPassScratchBytes(c->cfg, rb.width, rb.height, rb.maxDrawnSegments), &cap);
   cudaError_t e = cudaMemcpyAsync(hairDepth, sceneDepth, px * 4, cudaMemcpyDeviceToDevice, c->stream);
-  if (e == cudaSuccess) e = cudaMemsetAsync(rb.scratch, 0, 4, c->stream);  // the big list's count
+  if (e == cudaSuccess && big) e = cudaMemsetAsync(big, 0, 4, c->stream);  // the big list's count
   if (e != cudaSuccess) return e;
   const uint32_t nStrands = min(strandsToRender, h.strandsCount);
   const uint32_t nPts = nStrands * h.pointsPerStrand;
   if (h.pointsPerStrand < 2u || nPts == 0) return cudaSuccess;
-  const uint32_t cap = hairDepthBigCap(rb.scratchBytes);
-  uint32_t* big = reinterpret_cast<uint32_t*>(rb.scratch);
   const HdView V = hdView(u);
   hairDepthKernel<<<hairDepthBlocks(nPts), HD_THREADS, 0, c->stream>>>(
       V, h.pointsPerStrand, nPts, (const float4*)pos, (const float4*)tan, (unsigned*)hairDepth, big, cap);

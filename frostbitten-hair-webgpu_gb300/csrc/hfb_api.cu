@@ -203,8 +203,7 @@ int hfb_buffer_clear(HfbCtx* c, void* dst, size_t bytes) {
 
 size_t hfb_raster_scratch_bytes_for(const HfbConfig* cfg, uint32_t width, uint32_t height, uint32_t maxDrawn) {
   if (!cfg || width == 0 || height == 0 || maxDrawn == 0) return 0;
-  return std::max(hfb::tilesScratchLayout(nullptr, *cfg, width, height, maxDrawn).bytes,
-                  hfb::fineScratchLayout(nullptr, *cfg, width, height).bytes);
+  return hfb::rasterPassScratchBytes(*cfg, width, height, maxDrawn) + (hfb::HD_LIST_ENTRIES + 1u) * 4u;
 }
 
 size_t hfb_raster_scratch_bytes(const HfbConfig* cfg, uint32_t width, uint32_t height) {

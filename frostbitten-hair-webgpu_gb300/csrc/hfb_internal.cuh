@@ -245,6 +245,8 @@ struct alignas(16) BatchInst {
   unsigned char* scratch;
   size_t scratchBytes;
   float* hairDepth;           // NULL: no hair depth prepass
+  uint32_t* hdList;           // the hair depth pass's big-triangle list (word 0: count), or NULL
+  uint32_t hdCap, pad1;
   const uint32_t* gridOrder;  // strand order of the grid splat, NULL = identity
 };
 
@@ -311,14 +313,30 @@ cudaError_t launchHairDepth(HfbCtx* c, const HfbUniforms& u, const HfbHairData& 
                             HfbRasterBuffers& rb);
 cudaError_t launchPresent(HfbCtx* c, const HfbUniforms& u, uint32_t W, uint32_t H, const float* result,
                           const float* scene, uint8_t* rgba);
-// Blocks of the grid splat (GridPostSimPass) over `strands` strands.
+// The hair depth pass's list of big triangles has its own region of the
+// raster scratch, after the tiles and fine passes' working memory, so the
+// pass can run beside them: HD_LIST_ENTRIES entries + the count.
+constexpr size_t HD_LIST_ENTRIES = 65536;
+inline size_t rasterPassScratchBytes(const HfbConfig& cfg, uint32_t W, uint32_t H, uint32_t maxDrawn) {
+  const size_t t = tilesScratchLayout(nullptr, cfg, W, H, maxDrawn).bytes;
+  const size_t f = fineScratchLayout(nullptr, cfg, W, H).bytes;
+  return alignUp256(t > f ? t : f);
+}
+// The list (word 0: count) and its capacity for a scratch buffer; capacity 0
+// (every big triangle drawn by its own thread) if the buffer has no room.
+inline uint32_t* hairDepthList(void* scratch, size_t scratchBytes, size_t passBytes, uint32_t* cap) {
+  if (!scratch || scratchBytes < passBytes + 8u) {
+    *cap = 0;
+    return nullptr;
+  }
+  const size_t n = (scratchBytes - passBytes) / 4u - 1u;
+  *cap = (uint32_t)(n < HD_LIST_ENTRIES ? n : HD_LIST_ENTRIES);
+  return reinterpret_cast<uint32_t*>((char*)scratch + passBytes);
+}
+// Blocks of the grid splat (GridPostSimPass) over `points` points.
 uint32_t gridPostBlocks(uint32_t points);
 // Blocks of the hair depth pass over `points` points.
 uint32_t hairDepthBlocks(uint32_t points);
-__host__ __device__ inline uint32_t hairDepthBigCap(size_t bytes) {
-  const size_t n = bytes / 4 > 1 ? bytes / 4 - 1 : 0;
-  return (uint32_t)(n < 0x7FFFFFFFu ? n : 0x7FFFFFFFu);
-}
 // Virtual blocks of kind k for one instance (host side).
 uint32_t batchBlocks(const HfbConfig& cfg, BatchKind k, const BatchInst& bi);
 // One frame of n checked instances; flips their `current`.  With passMs, the
