@@ -24,6 +24,8 @@
 // tie-break, depth24 storage) are implementation-defined and not reproduced;
 // the oracle (oracle_hair_depth) follows the rules above.
 #define HFB_TU 7
+#include <cuda_fp16.h>
+
 #include "hfb_internal.cuh"
 #include "hfb_math.cuh"
 
@@ -114,8 +116,18 @@ __device__ __forceinline__ bool triBox(const Tri& t, uint32_t W, uint32_t H, flo
   return x0 <= x1 && y0 <= y1;
 }
 
-__device__ __forceinline__ void triPixel(const Tri& t, float area, uint32_t W, int x, int y,
-                                         unsigned* __restrict__ depth) {
+// Where a pass writes: the depth ('less' test as an atomic minimum of the
+// depth bits) or, in the winner pass (WIN), the smallest primitive index
+// among the fragments whose depth equals the final one (the first drawn of
+// equal depths keeps the pixel, as in draw order).
+struct HdOut {
+  unsigned* depth;
+  unsigned* winner;
+  uint32_t W;
+};
+
+template <bool WIN>
+__device__ __forceinline__ void triPixel(const Tri& t, float area, const HdOut& o, int x, int y, uint32_t prim) {
   const float px = fadd((float)x, 0.5f), py = fadd((float)y, 0.5f);
   float w0 = edgeFn(t.v[1].x, t.v[1].y, t.v[2].x, t.v[2].y, px, py);
   float w1 = edgeFn(t.v[2].x, t.v[2].y, t.v[0].x, t.v[0].y, px, py);
@@ -125,7 +137,13 @@ __device__ __forceinline__ void triPixel(const Tri& t, float area, uint32_t W, i
   const float a = fabsf(area);
   const float z = fadd(fadd(fmul(w0 / a, t.v[0].z), fmul(w1 / a, t.v[1].z)), fmul(w2 / a, t.v[2].z));
   if (!(z >= 0.0f && z <= 1.0f)) return;
-  atomicMin(HFB_G(&depth[(size_t)y * W + x]), __float_as_uint(fadd(z, 0.0f)));  // -0 -> +0
+  const size_t p = (size_t)y * o.W + x;
+  const unsigned zb = __float_as_uint(fadd(z, 0.0f));  // -0 -> +0
+  if (WIN) {
+    if (zb == *HFB_G(&o.depth[p])) atomicMin(HFB_G(&o.winner[p]), prim);
+  } else {
+    atomicMin(HFB_G(&o.depth[p]), zb);
+  }
 }
 
 // Row y's pixels of the triangle: [L, R] (in: the box's x range) narrowed to
@@ -204,13 +222,14 @@ __device__ __forceinline__ bool spanSafe(const Tri& t) {
 
 // Every pixel of the triangle's box [x0, x1] x [y0, y1], rows y0 + first,
 // y0 + first + step, ...: by row spans, or pixel by pixel when spanSafe fails.
-__device__ __forceinline__ void drawRows(const Tri& t, float area, uint32_t W, int x0, int x1, int y0, int y1,
-                                         int first, int step, unsigned* __restrict__ depth) {
+template <bool WIN>
+__device__ __forceinline__ void drawRows(const Tri& t, float area, const HdOut& o, int x0, int x1, int y0, int y1,
+                                         int first, int step, uint32_t prim) {
   const bool safe = spanSafe(t), neg = area < 0.0f;
   for (int y = y0 + first; y <= y1; y += step) {
     int L = x0, R = x1;
     if (safe && !rowSpan(t, neg, y, L, R)) continue;
-    for (int x = L; x <= R; x++) triPixel(t, area, W, x, y, depth);
+    for (int x = L; x <= R; x++) triPixel<WIN>(t, area, o, x, y, prim);
   }
 }
 
@@ -258,9 +277,16 @@ __device__ __forceinline__ void blockQuad(const HdShared& sh, uint32_t k, Screen
 // within their own boxes, so a lane with a long thin segment does not hold
 // up the other 31.  A big triangle that finds the list full is drawn by its
 // own thread.  Called by every thread of the block.
+// prim: the primitive index of triangle tr of the segment from point pt,
+// (strand * (P - 1) + segment) * 2 + tr, the order the reference draws them.
+__device__ __forceinline__ uint32_t primOf(uint32_t pt, uint32_t P, uint32_t tr) {
+  return ((pt - pt / P) << 1) | tr;
+}
+
+template <bool WIN>
 __device__ __forceinline__ void hairDepthBlock(const HdView& V, uint32_t P, uint32_t nPts,
                                                const float4* __restrict__ pos, const float4* __restrict__ tan,
-                                               unsigned* __restrict__ depth, uint32_t* __restrict__ big,
+                                               const HdOut& out, uint32_t* __restrict__ big,
                                                uint32_t bigCap, uint32_t blk, HdShared& sh) {
   const uint32_t tid = threadIdx.x, lane = tid & 31u, wp = tid >> 5;
   const uint32_t pt = blk * HD_SEGS + tid;
@@ -335,10 +361,11 @@ __device__ __forceinline__ void hairDepthBlock(const HdView& V, uint32_t P, uint
     const int x = un.x0 + (int)(local - row * un.bw), y = un.y0 + (int)row;
     ScreenV q[4];
     blockQuad(sh, o, q);
+    const uint32_t opt = blk * HD_SEGS + o;
 #pragma unroll
     for (uint32_t tr = 0; tr < 2u; tr++)
       if (x >= un.bx0[tr] && x <= un.bx1[tr] && y >= un.by0[tr] && y <= un.by1[tr])
-        triPixel(segTri(q, tr), un.area[tr], W, x, y, depth);
+        triPixel<WIN>(segTri(q, tr), un.area[tr], out, x, y, primOf(opt, P, tr));
   }
   if (own[0] || own[1]) {
     ScreenV q[4];
@@ -349,15 +376,16 @@ __device__ __forceinline__ void hairDepthBlock(const HdView& V, uint32_t P, uint
       float area;
       int x0, x1, y0, y1;
       if (!triBox(t, W, H, area, x0, x1, y0, y1)) continue;
-      drawRows(t, area, W, x0, x1, y0, y1, 0, 1, depth);
+      drawRows<WIN>(t, area, out, x0, x1, y0, y1, 0, 1, primOf(pt, P, tr));
     }
   }
   __syncthreads();  // the shared state is rewritten by the block's next points
 }
 
 // The big list, one block per triangle, its rows spread over the threads.
-__device__ __forceinline__ void hairDepthBigBody(const HdView& V, const float4* __restrict__ pos,
-                                                 const float4* __restrict__ tan, unsigned* __restrict__ depth,
+template <bool WIN>
+__device__ __forceinline__ void hairDepthBigBody(const HdView& V, uint32_t P, const float4* __restrict__ pos,
+                                                 const float4* __restrict__ tan, const HdOut& out,
                                                  const uint32_t* __restrict__ big, uint32_t bigCap, uint32_t blk,
                                                  uint32_t nblk) {
   const uint32_t n = bigCap ? min(*HFB_G(&big[0]), bigCap) : 0u;
@@ -372,22 +400,104 @@ __device__ __forceinline__ void hairDepthBigBody(const HdView& V, const float4* 
     float area;
     int x0, x1, y0, y1;
     if (!triBox(t, W, H, area, x0, x1, y0, y1)) continue;
-    drawRows(t, area, W, x0, x1, y0, y1, (int)threadIdx.x, (int)blockDim.x, depth);  // a row per thread
+    drawRows<WIN>(t, area, out, x0, x1, y0, y1, (int)threadIdx.x, (int)blockDim.x, primOf(pt, P, tr));  // row/thread
   }
 }
 
+template <bool WIN>
 __global__ void __launch_bounds__(HD_THREADS, 4)
 hairDepthKernel(const HdView V, uint32_t P, uint32_t nPts, const float4* __restrict__ pos,
-                const float4* __restrict__ tan, unsigned* __restrict__ depth, uint32_t* __restrict__ big,
-                uint32_t bigCap) {
+                const float4* __restrict__ tan, const HdOut out, uint32_t* __restrict__ big, uint32_t bigCap) {
   __shared__ HdShared sh;
-  hairDepthBlock(V, P, nPts, pos, tan, depth, big, bigCap, blockIdx.x, sh);
+  hairDepthBlock<WIN>(V, P, nPts, pos, tan, out, big, bigCap, blockIdx.x, sh);
 }
 
+template <bool WIN>
 __global__ void __launch_bounds__(HD_THREADS)
-hairDepthBigKernel(const HdView V, const float4* __restrict__ pos, const float4* __restrict__ tan,
-                   unsigned* __restrict__ depth, const uint32_t* __restrict__ big, uint32_t bigCap) {
-  hairDepthBigBody(V, pos, tan, depth, big, bigCap, blockIdx.x, gridDim.x);
+hairDepthBigKernel(const HdView V, uint32_t P, const float4* __restrict__ pos, const float4* __restrict__ tan,
+                   const HdOut out, const uint32_t* __restrict__ big, uint32_t bigCap) {
+  hairDepthBigBody<WIN>(V, P, pos, tan, out, big, bigCap, blockIdx.x, gridDim.x);
+}
+
+// ---- the hair's normals: HwHairPass's second colour output ----
+// A vertex of the quad with what the fragment shader interpolates: the
+// screen position, 1 / clip.w and tangentWS = modelMatrix * (tangent, 1)
+// (hwHairPass.wgsl.ts:60-66, w = 1 as the reference writes it).
+struct NVert {
+  ScreenV s;
+  float w;
+  f3 t;
+};
+
+__device__ __forceinline__ NVert normalVertex(const HfbMat4& model, const HdView& V, const float4* __restrict__ pos,
+                                              const float4* __restrict__ tan, size_t i, bool plus) {
+  ScreenV a, b;
+  pointPair(V, pos, tan, i, a, b);
+  NVert n;
+  n.s = plus ? a : b;
+  // clip.w of the vertex, as projectScreen computed it
+  const float4 p = __ldg(HFB_G(&pos[i]));
+  const float4 t = __ldg(HFB_G(&tan[i]));
+  const f4 pVS = m4v(V.mv, mk4(p.x, p.y, p.z, 1.0f));
+  const f4 tVS = m4v(V.mv, mk4(t.x, t.y, t.z, 1.0f));
+  const f3 c = cross3(xyz(tVS), mk3(0.0f, 0.0f, 1.0f));
+  const f3 right = dot3(c, c) >= 1e-7f ? norm3(c) : mk3(0.0f, 0.0f, 0.0f);
+  const f3 th = mul3s(right, V.radius);
+  const f3 e = plus ? add3(xyz(pVS), th) : sub3(xyz(pVS), th);
+  n.w = m4v(V.pr, mk4(e.x, e.y, e.z, 1.0f)).w;
+  n.t = xyz(m4v(model.m, mk4(t.x, t.y, t.z, 1.0f)));
+  return n;
+}
+
+// encodeOctahedronNormal (shaderSnippets.wgls.ts:25-46) of normalize(t),
+// each component then stored as f16 (the rg16float target).
+__device__ __forceinline__ float2 octNormal(f3 t0) {
+  const f3 t = norm3(t0);
+  const float s = fadd(fadd(fabsf(t.x), fabsf(t.y)), fabsf(t.z));
+  float nx = t.x / s, ny = t.y / s;
+  const float nz = t.z / s;
+  if (nz < 0.0f) {
+    const float sx = nx >= 0.0f ? 1.0f : -1.0f, sy = ny >= 0.0f ? 1.0f : -1.0f;
+    const float ax = fmul(fsub(1.0f, fabsf(ny)), sx), ay = fmul(fsub(1.0f, fabsf(nx)), sy);
+    nx = ax;
+    ny = ay;
+  }
+  return make_float2(__half2float(__float2half_rn(fadd(fmul(nx, 0.5f), 0.5f))),
+                     __half2float(__float2half_rn(fadd(fmul(ny, 0.5f), 0.5f))));
+}
+
+// Per pixel: the winning fragment's tangent, interpolated perspective-
+// correctly (screen barycentrics b_i weighted by 1 / w_i), normalised and
+// encoded; pixels without hair keep their normal.
+__global__ void __launch_bounds__(256)
+hairNormalResolve(const HfbMat4 model, const HdView V, uint32_t P, const float4* __restrict__ pos,
+                  const float4* __restrict__ tan, const unsigned* __restrict__ winner, float2* __restrict__ normals) {
+  const uint32_t W = f2u(V.W), H = f2u(V.H);
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= W * H) return;
+  const unsigned prim = __ldg(HFB_G(&winner[i]));
+  if (prim == 0xFFFFFFFFu) return;
+  const uint32_t tr = prim & 1u, segIdx = prim >> 1, strand = segIdx / (P - 1u), seg = segIdx - strand * (P - 1u);
+  const size_t pt = (size_t)strand * P + seg;
+  const NVert q[4] = {normalVertex(model, V, pos, tan, pt, true), normalVertex(model, V, pos, tan, pt, false),
+                      normalVertex(model, V, pos, tan, pt + 1u, true),
+                      normalVertex(model, V, pos, tan, pt + 1u, false)};
+  const NVert& v0 = tr ? q[2] : q[0];
+  const NVert& v1 = q[1];
+  const NVert& v2 = tr ? q[3] : q[2];
+  const float px = fadd((float)(i % W), 0.5f), py = fadd((float)(i / W), 0.5f);
+  const float area = edgeFn(v0.s.x, v0.s.y, v1.s.x, v1.s.y, v2.s.x, v2.s.y);
+  float b0 = edgeFn(v1.s.x, v1.s.y, v2.s.x, v2.s.y, px, py);
+  float b1 = edgeFn(v2.s.x, v2.s.y, v0.s.x, v0.s.y, px, py);
+  float b2 = edgeFn(v0.s.x, v0.s.y, v1.s.x, v1.s.y, px, py);
+  if (area < 0.0f) { b0 = -b0; b1 = -b1; b2 = -b2; }
+  const float a = fabsf(area);
+  const float p0 = (b0 / a) / v0.w, p1 = (b1 / a) / v1.w, p2 = (b2 / a) / v2.w;
+  const float sum = fadd(fadd(p0, p1), p2);
+  const f3 t = mk3(fadd(fadd(fmul(p0, v0.t.x), fmul(p1, v1.t.x)), fmul(p2, v2.t.x)) / sum,
+                   fadd(fadd(fmul(p0, v0.t.y), fmul(p1, v1.t.y)), fmul(p2, v2.t.y)) / sum,
+                   fadd(fadd(fmul(p0, v0.t.z), fmul(p1, v1.t.z)), fmul(p2, v2.t.z)) / sum);
+  *HFB_G(&normals[i]) = octNormal(t);
 }
 
 // The instance's HdView into shared memory (every thread calls; synced).
@@ -413,8 +523,9 @@ __global__ void __launch_bounds__(HD_THREADS, 4) hairDepthBatch(BatchView b) {
       loadView(I.U, V);
       cur = i;
     }
-    hairDepthBlock(V, I.P, min(I.strandsToRender, I.S) * I.P, I.posNew, I.tan,
-                   reinterpret_cast<unsigned*>(I.hairDepth), I.hdList, I.hdCap, v - row[i], sh);
+    const HdOut out = {reinterpret_cast<unsigned*>(I.hairDepth), nullptr, I.W};
+    hairDepthBlock<false>(V, I.P, min(I.strandsToRender, I.S) * I.P, I.posNew, I.tan, out, I.hdList, I.hdCap,
+                          v - row[i], sh);
   }
 }
 
@@ -425,8 +536,8 @@ __global__ void __launch_bounds__(HD_THREADS) hairDepthBigBatch(BatchView b) {
     const BatchInst& I = b.insts[i];
     if (!I.hairDepth) continue;
     loadView(I.U, V);
-    hairDepthBigBody(V, I.posNew, I.tan, reinterpret_cast<unsigned*>(I.hairDepth), I.hdList, I.hdCap, blockIdx.x,
-                     gridDim.x);
+    const HdOut out = {reinterpret_cast<unsigned*>(I.hairDepth), nullptr, I.W};
+    hairDepthBigBody<false>(V, I.P, I.posNew, I.tan, out, I.hdList, I.hdCap, blockIdx.x, gridDim.x);
   }
 }
 
@@ -449,13 +560,43 @@ cudaError_t launchHairDepth(HfbCtx* c, const HfbUniforms& u, const HfbHairData& 
   const uint32_t nPts = nStrands * h.pointsPerStrand;
   if (h.pointsPerStrand < 2u || nPts == 0) return cudaSuccess;
   const HdView V = hdView(u);
-  hairDepthKernel<<<hairDepthBlocks(nPts), HD_THREADS, 0, c->stream>>>(
-      V, h.pointsPerStrand, nPts, (const float4*)pos, (const float4*)tan, (unsigned*)hairDepth, big, cap);
+  const HdOut out = {(unsigned*)hairDepth, nullptr, rb.width};
+  hairDepthKernel<false><<<hairDepthBlocks(nPts), HD_THREADS, 0, c->stream>>>(
+      V, h.pointsPerStrand, nPts, (const float4*)pos, (const float4*)tan, out, big, cap);
   HFB_AFTER_LAUNCH(c, "hairDepthKernel");
-  hairDepthBigKernel<<<c->smCount * 4u, HD_THREADS, 0, c->stream>>>(V, (const float4*)pos, (const float4*)tan,
-                                                                    (unsigned*)hairDepth, big, cap);
+  hairDepthBigKernel<false><<<c->smCount * 4u, HD_THREADS, 0, c->stream>>>(
+      V, h.pointsPerStrand, (const float4*)pos, (const float4*)tan, out, big, cap);
   HFB_AFTER_LAUNCH(c, "hairDepthBigKernel");
   c->launches += 2;
+  return cudaGetLastError();
+}
+
+cudaError_t launchHairNormals(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h,
+                              const float* pos, const float* tan, uint32_t strandsToRender, const float* hairDepth,
+                              float* normals, uint32_t* winner, HfbRasterBuffers& rb) {
+  HFB_CHECK_BIND(c);
+  const size_t px = (size_t)rb.width * rb.height;
+  uint32_t cap = 0;
+  uint32_t* big = hairDepthList(rb.scratch, rb.scratchBytes,
+                                rasterPassScratchBytes(c->cfg, rb.width, rb.height, rb.maxDrawnSegments), &cap);
+  cudaError_t e = cudaMemsetAsync(winner, 0xFF, px * 4, c->stream);
+  if (e == cudaSuccess && big) e = cudaMemsetAsync(big, 0, 4, c->stream);
+  if (e != cudaSuccess) return e;
+  const uint32_t nStrands = min(strandsToRender, h.strandsCount);
+  const uint32_t nPts = nStrands * h.pointsPerStrand;
+  if (h.pointsPerStrand < 2u || nPts == 0) return cudaSuccess;
+  const HdView V = hdView(u);
+  const HdOut out = {(unsigned*)hairDepth, winner, rb.width};
+  hairDepthKernel<true><<<hairDepthBlocks(nPts), HD_THREADS, 0, c->stream>>>(
+      V, h.pointsPerStrand, nPts, (const float4*)pos, (const float4*)tan, out, big, cap);
+  HFB_AFTER_LAUNCH(c, "hairDepthKernel<winner>");
+  hairDepthBigKernel<true><<<c->smCount * 4u, HD_THREADS, 0, c->stream>>>(
+      V, h.pointsPerStrand, (const float4*)pos, (const float4*)tan, out, big, cap);
+  HFB_AFTER_LAUNCH(c, "hairDepthBigKernel<winner>");
+  hairNormalResolve<<<divCeil((uint32_t)px, 256u), 256, 0, c->stream>>>(
+      u.modelMatrix, V, h.pointsPerStrand, (const float4*)pos, (const float4*)tan, winner, (float2*)normals);
+  HFB_AFTER_LAUNCH(c, "hairNormalResolve");
+  c->launches += 3;
   return cudaGetLastError();
 }
 

@@ -448,6 +448,30 @@ int hfb_hair_depth(HfbCtx* c, const HfbUniforms* u, const HfbHairData* h, const 
   HFB_LAUNCH(c, hfb::launchHairDepth(c, *u, *h, pos, tan, strandsToRender, sceneDepth, hairDepth, *rb), "hair_depth");
 }
 
+int hfb_hair_normals(HfbCtx* c, const HfbUniforms* u, const HfbHairData* h, const float* pos, const float* tan,
+                     uint32_t strandsToRender, const float* hairDepth, float* normals, uint32_t* winner,
+                     HfbRasterBuffers* rb) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, u && pos && tan && hairDepth && normals && winner, "NULL argument");
+  HFB_REQUIRE(c, aligned16(pos) && aligned16(tan), "vec4 buffers must be 16-byte aligned");
+  std::string err = validateHair(h);
+  if (err.empty()) err = checkRaster(c, rb);
+  if (err.empty()) err = checkViewport(u, rb);
+  HFB_REQUIRE(c, err.empty(), err);
+  HFB_LAUNCH(c, hfb::launchHairNormals(c, *u, *h, pos, tan, strandsToRender, hairDepth, normals, winner, *rb),
+             "hair_normals");
+}
+
+int hfb_gtao(HfbCtx* c, const HfbUniforms* u, const float* depth, const float* normals, float scale, float* ao) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, u && depth && normals && ao, "NULL argument");
+  HFB_REQUIRE(c, scale > 0.0f && scale <= 1.0f, "scale must be in (0, 1]");
+  HFB_REQUIRE(c, u->viewport.x >= 1.0f && u->viewport.y >= 1.0f && u->viewport.x <= 65536.0f &&
+                     u->viewport.y <= 65536.0f, "the viewport must be in [1, 65536]");
+  HFB_REQUIRE(c, u->ao.numDirections <= 64 && u->ao.numSteps <= 64, "numDirections and numSteps must be <= 64");
+  HFB_LAUNCH(c, hfb::launchGtao(c, *u, depth, normals, scale, ao), "gtao");
+}
+
 int hfb_present(HfbCtx* c, const HfbUniforms* u, const HfbRasterBuffers* rb, const float* scene, uint8_t* rgba) {
   HFB_CHECK_CTX(c);
   HFB_REQUIRE(c, u && rgba, "NULL argument");

@@ -311,6 +311,13 @@ cudaError_t launchBatchDepthCopy(HfbCtx* c, const BatchView& b);
 cudaError_t launchHairDepth(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, const float* pos, const float* tan,
                             uint32_t strandsToRender, const float* sceneDepth, float* hairDepth,
                             HfbRasterBuffers& rb);
+cudaError_t launchHairNormals(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, const float* pos, const float* tan,
+                              uint32_t strandsToRender, const float* hairDepth, float* normals, uint32_t* winner,
+                              HfbRasterBuffers& rb);
+// AO texture extent: ceil(viewport * scale), as the reference sizes it (renderer.ts:405-409).
+uint32_t aoExtent(float viewport, float scale);
+cudaError_t launchGtao(HfbCtx* c, const HfbUniforms& u, const float* depth, const float* normals, float scale,
+                       float* ao);
 cudaError_t launchPresent(HfbCtx* c, const HfbUniforms& u, uint32_t W, uint32_t H, const float* result,
                           const float* scene, uint8_t* rgba);
 // The hair depth pass's list of big triangles has its own region of the

@@ -26,7 +26,7 @@ OBJ_DIR = os.path.join(ROOT, "_build")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden", "--expt-relaxed-constexpr"]
-SOURCES = ["hfb_api.cu", "sim.cu", "shading.cu", "raster.cu", "noalloc.cu", "batch.cu", "hairdepth.cu", "present.cu"]
+SOURCES = ["hfb_api.cu", "sim.cu", "shading.cu", "raster.cu", "noalloc.cu", "batch.cu", "hairdepth.cu", "present.cu", "ao.cu"]
 
 
 def nvcc() -> str:

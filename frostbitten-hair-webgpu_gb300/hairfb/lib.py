@@ -101,6 +101,8 @@ SIGNATURES = {
     "hfb_tiles_pass_noalloc": (I, [P, P, P, P, P, P, U32, P]),
     "hfb_hair_depth": (I, [P, P, P, P, P, U32, P, P, P]),
     "hfb_present": (I, [P, P, P, P, P]),
+    "hfb_hair_normals": (I, [P, P, P, P, P, U32, P, P, P, P]),
+    "hfb_gtao": (I, [P, P, P, P, ctypes.c_float, P]),
     "hfb_frame": (I, [P, P]),
     "hfb_frame_batch": (I, [P, P, U32]),
     "hfb_frame_batch_profile": (I, [P, P, U32, P]),

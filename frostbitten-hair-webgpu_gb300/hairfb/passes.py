@@ -278,6 +278,17 @@ class HwHairPass:
                       ptr(hair.tangents), hair.rendered_strand_count(), ptr(scene_depth), ptr(hair_depth),
                       byref(rb.rb))
 
+    def cmd_draw_hair_normals(self, uniforms: bytes, hair: HairObject, hair_depth: torch.Tensor,
+                              normals: torch.Tensor, rb: RasterBuffers, winner: torch.Tensor | None = None):
+        """The pass's normal output: normals ((H*W, 2) float32, in/out) gets
+        the hair's octahedron-encoded tangent where the hair is in front in
+        hair_depth (as cmd_draw_hair_depth left it)."""
+        if winner is None:
+            winner = torch.empty(rb.width * rb.height, dtype=torch.int32, device="cuda")
+        self.ctx.call("hfb_hair_normals", _ub(uniforms), byref(hair.hair_data), ptr(hair.positions),
+                      ptr(hair.tangents), hair.rendered_strand_count(), ptr(hair_depth), ptr(normals), ptr(winner),
+                      byref(rb.rb))
+
 
 class PresentPass:
     """src/passes/hairCombine/hairCombinePass.ts + src/passes/presentPass/
@@ -295,6 +306,23 @@ class PresentPass:
         if out is None:
             out = torch.empty((rb.height, rb.width, 4), dtype=torch.uint8, device="cuda")
         self.ctx.call("hfb_present", _ub(uniforms), byref(rb.rb), ptr(scene_color), ptr(out))
+        return out
+
+
+class AoPass:
+    """src/passes/aoPass/aoPass.ts: GTAO from the depth and the normals."""
+    NAME = "AoPass"
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+
+    def cmd_calc_ao(self, uniforms: bytes, depth: torch.Tensor, normals: torch.Tensor, width: int, height: int,
+                    scale: float = 0.5) -> torch.Tensor:
+        """(ceil(height*scale), ceil(width*scale)) float32 AO (r16float
+        values), for hfb_shading's ao input."""
+        import math
+        out = torch.empty((math.ceil(height * scale), math.ceil(width * scale)), dtype=torch.float32, device="cuda")
+        self.ctx.call("hfb_gtao", _ub(uniforms), ptr(depth), ptr(normals), ctypes.c_float(scale), ptr(out))
         return out
 
 

@@ -22,19 +22,24 @@ from .config import HairConfig
 from .lib import Context, HfbInstance, ptr
 from .passes import (GridPostSimPass, GridPreSimPass, HairFinePass, HairObject, HairShadingPass,
                      HairSimIntegrationPass, HairTileSortPass, HairTilesPass, HwHairPass, PhysicsGrids,
-                     PresentPass, RasterBuffers, SdfCollider, clear_before_render)
+                     PresentPass, RasterBuffers, SdfCollider, AoPass, clear_before_render)
 
 
 class Renderer:
     """One hair instance rendered frame by frame through libhairfb.so."""
 
     def __init__(self, inst: synthetic.Instance, device: int = -1, ctx: Context | None = None,
-                 max_drawn: int | None = None, hair_depth: bool = False):
+                 max_drawn: int | None = None, hair_depth: bool = False, ao: bool = False):
         """max_drawn: this instance's segment pool in records (None: the
         config's 1 + tiles * avgSegmentsPerTile).  hair_depth: draw the hair's
         depth over the scene depth after the fine pass (HwHairPass) and shade
         with it, as the reference does; otherwise the shading reads the scene
-        depth."""
+        depth.  ao (with hair_depth): also the hair's normals and GTAO
+        (AoPass) after it, which the shading then reads, as the reference's
+        updateResourcesForNextFrame does (renderer.ts:286-296); the scene's
+        normals are the reference's clear value, 0 (no mesh pass here).
+        These run in the pass-by-pass frames (frame()); hfb_frame and
+        hfb_frame_batch take the AO as an input instead."""
         self.inst = inst
         self.cfg: HairConfig = inst.cfg
         self.ctx = ctx or Context(inst.cfg.to_c(), device)
@@ -48,6 +53,11 @@ class Renderer:
         # first frame draws the hair it holds the scene alone
         self.hair_depth = self.scene_depth.clone() if hair_depth else None
         self.shading_depth = self.hair_depth if hair_depth else self.scene_depth
+        assert hair_depth or not ao, "AO needs the hair depth"
+        n = inst.width * inst.height
+        self.normals = torch.zeros((n, 2), dtype=torch.float32, device="cuda") if ao else None
+        self.winner = torch.empty(n, dtype=torch.int32, device="cuda") if ao else None
+        self.ao = None
         self.grid_pre = GridPreSimPass(self.ctx)
         self.integrate = HairSimIntegrationPass(self.ctx)
         self.grid_post = GridPostSimPass(self.ctx)
@@ -85,9 +95,7 @@ class Renderer:
         the first shading."""
         su = self.sim_uniforms(0)
         self.grid_post.cmd_update_grids_after_sim(su, self.hair, self.grids)
-        if self.hair_depth is not None:  # updateResourcesForNextFrame: hwHair, then the shading
-            self.hw_hair.cmd_draw_hair_depth(self.uniforms, self.hair, self.scene_depth, self.hair_depth, self.rb)
-        self.shading.cmd_compute_shading_points(self.uniforms, self.hair, self.shading_depth)
+        self._resources_for_next_frame()
 
     def simulate(self) -> None:
         su = self.sim_uniforms(self.frame_idx)
@@ -100,8 +108,22 @@ class Renderer:
         self.tiles.cmd_draw_hair_to_tiles(self.uniforms, self.hair, self.scene_depth, self.rb)
         self.sort.cmd_sort_hair_tiles(self.rb)
         self.fine.cmd_rasterize_slices_hair(self.uniforms, self.hair, self.scene_depth, self.rb)
-        if self.hair_depth is not None:  # updateResourcesForNextFrame, renderer.ts:286-296
+        self._resources_for_next_frame()
+
+    def _resources_for_next_frame(self) -> None:
+        """updateResourcesForNextFrame, renderer.ts:286-296: hwHair (depth,
+        and normals when AO is on), AO, then the shading."""
+        if self.hair_depth is not None:
             self.hw_hair.cmd_draw_hair_depth(self.uniforms, self.hair, self.scene_depth, self.hair_depth, self.rb)
+        if self.normals is not None:
+            self.normals.zero_()  # CONFIG.clearNormals
+            self.hw_hair.cmd_draw_hair_normals(self.uniforms, self.hair, self.hair_depth, self.normals, self.rb,
+                                               self.winner)
+            self.ao = AoPass(self.ctx).cmd_calc_ao(self.uniforms, self.hair_depth, self.normals,
+                                                   self.inst.width, self.inst.height)
+            self.shading.cmd_compute_shading_points(self.uniforms, self.hair, self.shading_depth, self.ao,
+                                                    (self.ao.shape[1], self.ao.shape[0]))
+            return
         self.shading.cmd_compute_shading_points(self.uniforms, self.hair, self.shading_depth)
 
     def image(self, scene_color: torch.Tensor | None = None) -> torch.Tensor:

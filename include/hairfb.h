@@ -352,6 +352,28 @@ typedef struct HfbInstance {
 HFB_API int hfb_present(HfbCtx* ctx, const HfbUniforms* uniforms, const HfbRasterBuffers* rb,
                         const float* sceneColor, uint8_t* rgba);
 
+/* HwHairPass.cmdDrawHair's normal output (hwHairPass.wgsl.ts:88-97): at every
+ * pixel where the hair is in front (its depth equals hairDepth, as
+ * hfb_hair_depth left it), the octahedron encoding of the normalised
+ * tangent the fragment interpolates (perspective-correct) from
+ * modelMatrix * (tangent, 1), stored as rg16float values; the fragment
+ * that wins a pixel is the first drawn among those at its depth (strand,
+ * segment, triangle order).  normals: W*H vec2f (device), in/out: pixels
+ * without hair keep their value (the scene's normals, or 0 as the
+ * reference clears them).  winner: W*H u32 of device working memory. */
+HFB_API int hfb_hair_normals(HfbCtx* ctx, const HfbUniforms* uniforms, const HfbHairData* hair,
+                             const float* positions, const float* tangents, uint32_t strandsToRender,
+                             const float* hairDepth, float* normals, uint32_t* winner, HfbRasterBuffers* rb);
+
+/* AoPass.cmdCalcAo (aoPass.wgsl.ts, gtao.wgsl.ts): ground-truth ambient
+ * occlusion at ceil(W*scale) x ceil(H*scale) texels (the reference's
+ * CONFIG.ao.textureSizeMul, 0.5) from depth (W*H f32, e.g. hfb_hair_depth's)
+ * and normals (W*H vec2f octahedron, e.g. hfb_hair_normals'), with the
+ * Uniforms.ao parameters; stored as r16float values in ao (device f32).
+ * The shading reads it (hfb_shading's ao, aoWidth, aoHeight). */
+HFB_API int hfb_gtao(HfbCtx* ctx, const HfbUniforms* uniforms, const float* depth, const float* normals, float scale,
+                     float* ao);
+
 HFB_API int hfb_hair_depth(HfbCtx* ctx, const HfbUniforms* uniforms, const HfbHairData* hair, const float* positions,
                            const float* tangents, uint32_t strandsToRender, const float* sceneDepth,
                            float* hairDepth, HfbRasterBuffers* rb);

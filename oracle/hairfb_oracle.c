@@ -1373,6 +1373,223 @@ EXPORT void oracle_hair_depth(const void* uniforms, const void* hairData, const 
     }
 }
 
+/* HwHairPass's normal output (hwHairPass.wgsl.ts:60-97): the winning
+ * fragment at each pixel is the first in draw order (strand, segment,
+ * triangle) whose depth equals hairDepth; its tangent (modelMatrix *
+ * (tangent, 1), interpolated with perspective-correct barycentrics: screen
+ * barycentrics b_i over w_i) normalised, octahedron-encoded
+ * (shaderSnippets.wgls.ts:25-46) and stored as f16 (rg16float).  normals:
+ * W*H*2 floats, in/out. */
+typedef struct { OScreenV s; float w; v3 t; } ONVert;
+
+static void hnVert(const ORenderUniforms* U, const float* pos, const float* tan, size_t i, int plus, ONVert* out) {
+  float W = U->viewport.x, H = U->viewport.y;
+  const float* p = pos + 4 * i;
+  const float* t = tan + 4 * i;
+  v4 pVS = m4v(&U->modelViewMat, V4(p[0], p[1], p[2], 1.0f));
+  v4 tVS = m4v(&U->modelViewMat, V4(t[0], t[1], t[2], 1.0f));
+  v3 c = cross3(xyz(tVS), V3(0.0f, 0.0f, 1.0f));
+  v3 right = dot3(c, c) >= 1e-7f ? norm3(c) : V3(0.0f, 0.0f, 0.0f);
+  v3 th = mul3s(right, U->fiberRadius);
+  v3 e = plus ? add3(xyz(pVS), th) : sub3(xyz(pVS), th);
+  v4 clip = m4v(&U->projMatrix, V4(e.x, e.y, e.z, 1.0f));
+  out->s.ok = clip.w > 0.0f;
+  float nx = clip.x / clip.w, ny = clip.y / clip.w;
+  out->s.z = clip.z / clip.w;
+  out->s.x = (nx * 0.5f + 0.5f) * W;
+  out->s.y = (0.5f - ny * 0.5f) * H;
+  out->w = clip.w;
+  out->t = xyz(m4v(&U->modelMatrix, V4(t[0], t[1], t[2], 1.0f)));
+}
+
+static void hnOct(v3 t0, float* out) {
+  v3 t = norm3(t0);
+  float s = (fabsf(t.x) + fabsf(t.y)) + fabsf(t.z);
+  float nx = t.x / s, ny = t.y / s, nz = t.z / s;
+  if (nz < 0.0f) {
+    float sx = nx >= 0.0f ? 1.0f : -1.0f, sy = ny >= 0.0f ? 1.0f : -1.0f;
+    float ax = (1.0f - fabsf(ny)) * sx, ay = (1.0f - fabsf(nx)) * sy;
+    nx = ax;
+    ny = ay;
+  }
+  out[0] = f16_to_f32(f32_to_f16_rne(nx * 0.5f + 0.5f));
+  out[1] = f16_to_f32(f32_to_f16_rne(ny * 0.5f + 0.5f));
+}
+
+EXPORT void oracle_hair_normals(const void* uniforms, const void* hairData, const float* positions,
+                                const float* tangents, uint32_t strandsToRender, const float* hairDepth,
+                                float* normals) {
+  const ORenderUniforms* U = (const ORenderUniforms*)uniforms;
+  const OHairData* HD = (const OHairData*)hairData;
+  uint32_t W = f2u(U->viewport.x), H = f2u(U->viewport.y);
+  uint32_t P = HD->pointsPerStrand, S = HD->strandsCount;
+  uint32_t nStrands = strandsToRender < S ? strandsToRender : S;
+  uint32_t* win = (uint32_t*)malloc((size_t)W * H * 4);
+  for (size_t i = 0; i < (size_t)W * H; i++) win[i] = 0xFFFFFFFFu;
+  for (uint32_t strand = 0; strand < nStrands; strand++)
+    for (uint32_t seg = 0; seg + 1u < P; seg++) {
+      OScreenV q[4];
+      hdQuad(U, positions, tangents, P, strand, seg, q);
+      for (uint32_t tr = 0; tr < 2u; tr++) {
+        const OScreenV* a = tr ? &q[2] : &q[0];
+        const OScreenV* b = &q[1];
+        const OScreenV* c = tr ? &q[3] : &q[2];
+        if (!a->ok || !b->ok || !c->ok) continue;
+        float area = hdEdge(a->x, a->y, b->x, b->y, c->x, c->y);
+        if (!(area != 0.0f) || !isfinite(area)) continue;
+        float mnx = fminf(fminf(a->x, b->x), c->x), mxx = fmaxf(fmaxf(a->x, b->x), c->x);
+        float mny = fminf(fminf(a->y, b->y), c->y), mxy = fmaxf(fmaxf(a->y, b->y), c->y);
+        if (!(mxx >= 0.5f && mxy >= 0.5f && mnx <= (float)W - 0.5f && mny <= (float)H - 0.5f)) continue;
+        int x0 = (int)fmaxf(ceilf(mnx - 0.5f), 0.0f), y0 = (int)fmaxf(ceilf(mny - 0.5f), 0.0f);
+        int x1 = (int)fminf(floorf(mxx - 0.5f), (float)W - 1.0f), y1 = (int)fminf(floorf(mxy - 0.5f), (float)H - 1.0f);
+        float aa = fabsf(area);
+        uint32_t prim = ((strand * (P - 1u) + seg) << 1) | tr;
+        for (int y = y0; y <= y1; y++)
+          for (int x = x0; x <= x1; x++) {
+            float px = (float)x + 0.5f, py = (float)y + 0.5f;
+            float w0 = hdEdge(b->x, b->y, c->x, c->y, px, py);
+            float w1 = hdEdge(c->x, c->y, a->x, a->y, px, py);
+            float w2 = hdEdge(a->x, a->y, b->x, b->y, px, py);
+            if (area < 0.0f) { w0 = -w0; w1 = -w1; w2 = -w2; }
+            if (!(w0 >= 0.0f && w1 >= 0.0f && w2 >= 0.0f)) continue;
+            float z = (w0 / aa * a->z + w1 / aa * b->z) + w2 / aa * c->z;
+            if (!(z >= 0.0f && z <= 1.0f)) continue;
+            z = z + 0.0f;
+            size_t pi = (size_t)y * W + x;
+            uint32_t zb, db;
+            memcpy(&zb, &z, 4);
+            memcpy(&db, &hairDepth[pi], 4);
+            if (zb == db && win[pi] == 0xFFFFFFFFu) win[pi] = prim;
+          }
+      }
+    }
+  for (size_t pi = 0; pi < (size_t)W * H; pi++) {
+    uint32_t prim = win[pi];
+    if (prim == 0xFFFFFFFFu) continue;
+    uint32_t tr = prim & 1u, segIdx = prim >> 1, strand = segIdx / (P - 1u), seg = segIdx - strand * (P - 1u);
+    size_t pt = (size_t)strand * P + seg;
+    ONVert q[4];
+    hnVert(U, positions, tangents, pt, 1, &q[0]);
+    hnVert(U, positions, tangents, pt, 0, &q[1]);
+    hnVert(U, positions, tangents, pt + 1u, 1, &q[2]);
+    hnVert(U, positions, tangents, pt + 1u, 0, &q[3]);
+    const ONVert* v0 = tr ? &q[2] : &q[0];
+    const ONVert* v1 = &q[1];
+    const ONVert* v2 = tr ? &q[3] : &q[2];
+    float px = (float)(pi % W) + 0.5f, py = (float)(pi / W) + 0.5f;
+    float area = hdEdge(v0->s.x, v0->s.y, v1->s.x, v1->s.y, v2->s.x, v2->s.y);
+    float b0 = hdEdge(v1->s.x, v1->s.y, v2->s.x, v2->s.y, px, py);
+    float b1 = hdEdge(v2->s.x, v2->s.y, v0->s.x, v0->s.y, px, py);
+    float b2 = hdEdge(v0->s.x, v0->s.y, v1->s.x, v1->s.y, px, py);
+    if (area < 0.0f) { b0 = -b0; b1 = -b1; b2 = -b2; }
+    float a = fabsf(area);
+    float p0 = (b0 / a) / v0->w, p1 = (b1 / a) / v1->w, p2 = (b2 / a) / v2->w;
+    float sum = (p0 + p1) + p2;
+    v3 t = V3(((p0 * v0->t.x + p1 * v1->t.x) + p2 * v2->t.x) / sum, ((p0 * v0->t.y + p1 * v1->t.y) + p2 * v2->t.y) / sum,
+              ((p0 * v0->t.z + p1 * v1->t.z) + p2 * v2->t.z) / sum);
+    hnOct(t, normals + 2 * pi);
+  }
+  free(win);
+}
+
+/* AoPass + GTAO (aoPass.wgsl.ts main_fs, gtao.wgsl.ts): see the CUDA pass;
+ * out: ceil(W * scale) x ceil(H * scale) floats, r16float values.  Loads
+ * outside the textures read 0; a negative coordinate saturates to 0. */
+typedef struct { const float* depth; uint32_t W, H; float vw, vh; const mat4* pinv; } OGtao;
+
+static float aoLoadDepth(const OGtao* a, float px, float py) {
+  uint32_t x = f2u(px), y = f2u(py);
+  return x < a->W && y < a->H ? a->depth[(size_t)y * a->W + x] : 0.0f;
+}
+static float aoLin(float d) { return (0.01f * 100.0f) / (100.0f + (0.01f - 100.0f) * d); }
+static v3 aoReproject(const OGtao* a, float px, float py) {
+  float d = aoLoadDepth(a, px, py);
+  float x = (px / a->vw) * 2.0f - 1.0f, y = (py / a->vh) * 2.0f - 1.0f;
+  v4 c = m4v(a->pinv, V4(x, y, d, 1.0f));
+  return V3(c.x / c.w, c.y / c.w, aoLin(d));
+}
+static float aoRound(float v) { return v < 0.5f ? floorf(v) : ceilf(v); }
+static float aoFalloff(float dist, float s2, float e2) { return 2.0f * sat((dist - s2) / (e2 - s2)); }
+static float aoFract(float x) { return x - floorf(x); }
+static v3 aoDecodeOct(float fx0, float fy0) {
+  float fx = fx0 * 2.0f - 1.0f, fy = fy0 * 2.0f - 1.0f;
+  v3 n = V3(fx, fy, (1.0f - fabsf(fx)) - fabsf(fy));
+  float t = sat(-n.z);
+  n.x = n.x >= 0.0f ? n.x - t : n.x + t;
+  n.y = n.y >= 0.0f ? n.y - t : n.y + t;
+  return norm3(n);
+}
+
+EXPORT void oracle_gtao(const void* uniforms, const float* depth, const float* normals, float scale, float* out) {
+  const ORenderUniforms* U = (const ORenderUniforms*)uniforms;
+  const float PI = 3.141592653589793f, HALF_PI = 1.5707963267948966f, ZFAR = 100.0f;
+  OGtao a = {depth, f2u(U->viewport.x), f2u(U->viewport.y), U->viewport.x, U->viewport.y, &U->projMatrixInv};
+  uint32_t aoW = (uint32_t)ceilf(U->viewport.x * scale), aoH = (uint32_t)ceilf(U->viewport.y * scale);
+  const OGtao* A = &a;
+#pragma omp parallel for schedule(static)
+  for (uint32_t i = 0; i < aoW * aoH; i++) {
+    float px = ((float)(i % aoW) + 0.5f) / scale, py = ((float)(i / aoW) + 0.5f) / scale;
+    uint32_t nx = f2u(px), ny = f2u(py);
+    float no[2] = {0.0f, 0.0f};
+    if (nx < A->W && ny < A->H) memcpy(no, normals + 2 * ((size_t)ny * A->W + nx), sizeof no);
+    v3 normalWS = aoDecodeOct(no[0], no[1]);
+    v3 posVS = aoReproject(A, px, py);
+    v3 nVS = xyz(m4v(&U->viewMatrix, V4(normalWS.x, normalWS.y, normalWS.z, 1.0f)));
+    nVS.z = -nVS.z;
+    v3 toCam = norm3(V3(-posVS.x, -posVS.y, -posVS.z));
+    float ao = 0.0f;
+    if (!(posVS.z >= 0.999f * ZFAR)) {
+      float nSteps = (float)U->ao.numSteps;
+      float radius = fmaxf(nSteps, U->ao.radius * (posVS.z / ZFAR));
+      float stepSize = radius / nSteps;
+      float rotJitter = PI * aoFract(52.9829189f * aoFract(px * 0.06711056f + py * 0.00583715f));
+      float jitterMod = (px + py) * 0.25f;
+      float radiusJitter = (aoFract(jitterMod) * stepSize) * 0.25f;
+      for (uint32_t d = 0; d < U->ao.numDirections; d++) {
+        float phi = (float)d * (PI / (float)U->ao.numDirections) + U->ao.directionOffset * PI;
+        phi = phi + rotJitter;
+        float step = 1.0f + 0.25f * stepSize;
+        step = step + radiusJitter;
+        float dx = cosf(phi), dy = sinf(phi);
+        float h1 = -1.0f, h2 = -1.0f;
+        for (uint32_t j = 0; j < U->ao.numSteps; j++) {
+          float ox = aoRound(dx * step), oy = aoRound(dy * step);
+          v3 s = aoReproject(A, px + ox, py + oy);
+          v3 ws = sub3(s, posVS);
+          float d2 = len3(ws);
+          float c = dot3(ws, toCam) * (1.0f / sqrtf(d2));
+          h1 = fmaxf(h1, c - aoFalloff(d2, U->ao.falloffStart2, U->ao.falloffEnd2));
+          s = aoReproject(A, px - ox, py - oy);
+          ws = sub3(s, posVS);
+          d2 = len3(ws);
+          c = dot3(ws, toCam) * (1.0f / sqrtf(d2));
+          h2 = fmaxf(h2, c - aoFalloff(d2, U->ao.falloffStart2, U->ao.falloffEnd2));
+          step = step + stepSize;
+        }
+        h1 = acosf(h1);
+        h2 = acosf(h2);
+        v3 dir = V3(dx, dy, 0.0f);
+        v3 bit = norm3(cross3(dir, toCam));
+        v3 tng = cross3(toCam, bit);
+        v3 nxv = sub3(nVS, mul3s(bit, dot3(nVS, bit)));
+        float nnx = len3(nxv);
+        float nnxInv = 1.0f / (nnx + 1e-6f);
+        float cosxi = dot3(nxv, tng) * nnxInv;
+        float gamma = acosf(cosxi) - HALF_PI;
+        float cosgamma = dot3(nxv, toCam) * nnxInv;
+        float singamma2 = -2.0f * cosxi;
+        h1 = gamma + fmaxf(-h1 - gamma, -HALF_PI);
+        h2 = gamma + fminf(h2 - gamma, HALF_PI);
+        float t1 = (h1 * singamma2 + cosgamma) - cosf(2.0f * h1 - gamma);
+        float t2 = (h2 * singamma2 + cosgamma) - cosf(2.0f * h2 - gamma);
+        ao = ao + (nnx * 0.25f) * (t1 + t2);
+      }
+      ao = ao / (float)U->ao.numDirections;
+    }
+    out[i] = f16_to_f32(f32_to_f16_rne(ao));
+  }
+}
+
 /* HairCombinePass (hairCombinePass.wgsl.ts:51-89: fragment row y reads
  * result row H - 1 - y; blend src-alpha, one-minus-src-alpha over the scene
  * colour, hairCombinePass.ts:40-52) and PresentPass (presentPass.wgsl.ts

@@ -74,6 +74,8 @@ def _declare(lib):
     lib.oracle_shading.argtypes = [P, P, P, P, P, P, P, U, U, P, U, P]
     lib.oracle_hair_depth.argtypes = [P, P, P, P, U, P]
     lib.oracle_present.argtypes = [P, P, P, P]
+    lib.oracle_hair_normals.argtypes = [P, P, P, P, U, P, P]
+    lib.oracle_gtao.argtypes = [P, P, P, ctypes.c_float, P]
     lib.oracle_sample_sdf.argtypes = [P, U, P, P, P]
     lib.oracle_sample_sdf.restype = ctypes.c_float
     lib.oracle_f32_to_f16.argtypes = [ctypes.c_float]
@@ -202,6 +204,31 @@ def hair_depth(uniforms: bytes, hair_data: bytes, positions, tangents, strands_t
     u, h = _Bytes(uniforms), _Bytes(hair_data)
     lib.oracle_hair_depth(u.ptr, h.ptr, _p(_f32(positions)), _p(_f32(tangents)), strands_to_render, _p(out))
     return out
+
+
+def hair_normals(uniforms: bytes, hair_data: bytes, positions, tangents, strands_to_render, hair_depth,
+                 normals=None):
+    """HwHairPass's normal output: (W*H, 2) float32 (f16 values), pixels
+    without hair keep `normals` (zeros when None)."""
+    lib = load()
+    u, h = _Bytes(uniforms), _Bytes(hair_data)
+    hd = _f32(hair_depth).reshape(-1)
+    out = np.zeros((hd.size, 2), np.float32) if normals is None else np.array(normals, np.float32, copy=True)
+    lib.oracle_hair_normals(u.ptr, h.ptr, _p(_f32(positions)), _p(_f32(tangents)), strands_to_render, _p(hd),
+                            _p(out))
+    return out
+
+
+def gtao(uniforms: bytes, depth, normals, scale=0.5):
+    """AoPass: (ceil(H*scale), ceil(W*scale)) float32 (f16 values)."""
+    import math
+    lib = load()
+    u = _Bytes(uniforms)
+    vp = np.frombuffer(uniforms, np.float32)[16 * 9:16 * 9 + 2]
+    aw, ah = math.ceil(float(vp[0]) * scale), math.ceil(float(vp[1]) * scale)
+    out = np.zeros(aw * ah, np.float32)
+    lib.oracle_gtao(u.ptr, _p(_f32(depth).reshape(-1)), _p(_f32(normals).reshape(-1)), scale, _p(out))
+    return out.reshape(ah, aw)
 
 
 def present(uniforms: bytes, result, scene_color=None):

@@ -589,6 +589,73 @@ def test_present_within_1_255(oracle, scene, tmp_path):
     assert png[:8] == b"\x89PNG\r\n\x1a\n"
 
 
+@pytest.mark.parametrize("kw", [dict(), dict(strands=300, fiber_radius=0.02)])
+def test_hair_normals_and_gtao(oracle, kw):
+    """HwHairPass's normals (bit-exact: the winner of each pixel, the
+    perspective-correct tangent, the f16 octahedron encoding) and GTAO on
+    the hair depth and those normals (the transcendentals differ by an ulp
+    or so, which can move a sample by a pixel: nearly every texel within
+    4e-3, the mean far below)."""
+    from hairfb.passes import AoPass, HwHairPass
+    inst = small_instance(**kw)
+    fr = frame_of(inst)
+    ctx = _ctx(inst)
+    hair = HairObject(inst.hair, inst.cfg.shading_points)
+    rb = RasterBuffers(ctx, inst.width, inst.height)
+    scene = torch.as_tensor(inst.scene_depth).cuda()
+    hd = torch.empty_like(scene)
+    hw = HwHairPass(ctx)
+    hw.cmd_draw_hair_depth(fr.uniforms, hair, scene, hd, rb)
+    rng = np.random.default_rng(6)
+    base = rng.uniform(0.0, 1.0, (inst.width * inst.height, 2)).astype(np.float32)  # the scene's normals
+    normals = torch.as_tensor(base).cuda()
+    hw.cmd_draw_hair_normals(fr.uniforms, hair, hd, normals, rb)
+    ctx.sync()
+    hdn = hd.cpu().numpy()
+    on = oracle.hair_normals(fr.uniforms, inst.hair.hair_data, inst.hair.asset.positions, inst.hair.tangents,
+                             inst.hair.asset.strands, hdn, base)
+    gn = normals.cpu().numpy()
+    changed = (on != base).any(1)
+    assert changed.sum() > 1000, "few hair pixels: the case does not test"
+    assert np.array_equal(gn.view(np.uint32), on.view(np.uint32)), f"{int((gn != on).any(1).sum())} normals differ"
+    ao = AoPass(ctx).cmd_calc_ao(fr.uniforms, hd, normals, inst.width, inst.height)
+    ctx.sync()
+    oao = oracle.gtao(fr.uniforms, hdn, on)
+    g = ao.cpu().numpy()
+    assert g.shape == oao.shape and np.isfinite(oao).all() and np.isfinite(g).all()
+    assert np.abs(oao).max() > 0.05, "no occlusion anywhere: the case does not test"
+    err = np.abs(g - oao)
+    assert (err <= 4e-3).mean() >= 0.995 and err.mean() < 1e-3, (float(err.max()), float(err.mean()))
+
+
+def test_frame_with_ao_matches_the_oracle_chain(oracle):
+    """A frame with the hair depth, the hair's normals and GTAO before the
+    shading (Renderer(ao=True)): the oracle's chain on the frame's positions
+    (hair depth, normals, GTAO, shading with that AO) gives the same shading
+    within 1e-5 where the GPU and oracle AO agree."""
+    from hairfb.renderer import Renderer
+    inst = small_instance(strands=1500)
+    r = Renderer(inst, 0, hair_depth=True, ao=True)
+    r.before_first_frame()
+    r.frame()
+    r.ctx.sync()
+    pos = r.hair.positions.cpu().numpy()
+    tan = r.hair.tangents.cpu().numpy()
+    hb = inst.hair
+    od = oracle.hair_depth(r.uniforms, hb.hair_data, pos, tan, hb.asset.strands, inst.scene_depth)
+    assert np.array_equal(r.hair_depth.cpu().numpy().view(np.uint32), od.view(np.uint32))
+    on = oracle.hair_normals(r.uniforms, hb.hair_data, pos, tan, hb.asset.strands, od)
+    assert np.array_equal(r.normals.cpu().numpy().view(np.uint32), on.view(np.uint32))
+    gao = r.ao.cpu().numpy()
+    oao = oracle.gtao(r.uniforms, od, on)
+    assert (np.abs(gao - oao) <= 4e-3).mean() >= 0.995
+    # the shading on the GPU's AO (the AO's own tolerance is checked above)
+    osh = oracle.shading(inst.cfg, r.uniforms, hb.hair_data, pos, tan, od, hb.asset.strands, ao=gao.reshape(-1),
+                         ao_size=(gao.shape[1], gao.shape[0]))
+    g = r.hair.shading.cpu().numpy()
+    assert np.allclose(g, osh, rtol=1e-5, atol=1e-5), float(np.abs(g - osh).max())
+
+
 def test_shading_reads_the_hair_depth(oracle):
     """A frame with the hair depth prepass: the depth it leaves is the
     oracle's for the frame's positions, and the shading computed from it
