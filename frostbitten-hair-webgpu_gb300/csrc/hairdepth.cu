@@ -379,7 +379,7 @@ __device__ __forceinline__ void hairDepthBlock(const HdView& V, uint32_t P, uint
       drawRows<WIN>(t, area, out, x0, x1, y0, y1, 0, 1, primOf(pt, P, tr));
     }
   }
-  __syncthreads();  // the shared state is rewritten by the block's next points
+  // the shared state is rewritten by the CTA's next points only after batchNext's barrier
 }
 
 // The big list, one block per triangle, its rows spread over the threads.
@@ -515,8 +515,9 @@ __global__ void __launch_bounds__(HD_THREADS, 4) hairDepthBatch(BatchView b) {
   const uint32_t* row = b.prefix + BK_HAIR_DEPTH * (BATCH_MAX + 1);
   const uint32_t total = row[n];
   uint32_t cur = 0xFFFFFFFFu;
-  __shared__ uint32_t vbNext;
-  for (uint32_t v = batchNext(b.hdr, BK_HAIR_DEPTH, &vbNext); v < total; v = batchNext(b.hdr, BK_HAIR_DEPTH, &vbNext)) {
+  __shared__ uint32_t vbNext[2];
+  uint32_t vbPar = 0;
+  for (uint32_t v = batchNext(b.hdr, BK_HAIR_DEPTH, vbNext, vbPar); v < total; v = batchNext(b.hdr, BK_HAIR_DEPTH, vbNext, vbPar)) {
     const uint32_t i = batchFind(row, n, v);
     const BatchInst& I = b.insts[i];
     if (i != cur) {

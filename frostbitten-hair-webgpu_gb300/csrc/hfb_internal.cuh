@@ -289,12 +289,17 @@ __device__ __forceinline__ uint32_t batchFind(const uint32_t* __restrict__ row, 
 // The next virtual block of kind k for the calling CTA, from the header's
 // counter (zeroed by every frame's table upload): CTAs take blocks as they
 // finish, so uneven blocks do not leave some CTAs with a long tail.  Every
-// thread of the CTA calls it; `slot` is a shared word.
-__device__ __forceinline__ uint32_t batchNext(BatchHdr* hdr, uint32_t k, uint32_t* slot) {
-  __syncthreads();  // the previous block number has been read by every thread
-  if (threadIdx.x == 0) *slot = atomicAdd(&hdr->queue[k], 1u);
+// thread of the CTA calls it; `slots` are two shared words used in turn
+// (`parity`, per thread): the write of a call can only meet reads of the
+// call two before, which every thread finished before the barrier of the
+// call in between.  The barrier also orders a block body's shared-memory
+// reads before the next body's writes.
+__device__ __forceinline__ uint32_t batchNext(BatchHdr* hdr, uint32_t k, uint32_t* slots, uint32_t& parity) {
+  if (threadIdx.x == 0) slots[parity] = atomicAdd(&hdr->queue[k], 1u);
   __syncthreads();
-  return *slot;
+  const uint32_t v = slots[parity];
+  parity ^= 1u;
+  return v;
 }
 
 // Batched launchers: one persistent launch of kind k over all instances.

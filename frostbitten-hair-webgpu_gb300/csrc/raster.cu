@@ -1845,9 +1845,10 @@ cudaError_t launchFineT(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, c
   const uint32_t n = b.hdr->n;                                        \
   const uint32_t* row = b.prefix + (KIND) * (BATCH_MAX + 1);          \
   const uint32_t totalVb = row[n];                                    \
-  __shared__ uint32_t vbNext;                                         \
-  for (uint32_t v = batchNext(b.hdr, (KIND), &vbNext); v < totalVb;  \
-       v = batchNext(b.hdr, (KIND), &vbNext)) {                       \
+  __shared__ uint32_t vbNext[2];                                      \
+  uint32_t vbPar = 0;                                                 \
+  for (uint32_t v = batchNext(b.hdr, (KIND), vbNext, vbPar); v < totalVb; \
+       v = batchNext(b.hdr, (KIND), vbNext, vbPar)) {                 \
     const uint32_t i = batchFind(row, n, v);                          \
     const BatchInst& I = b.insts[i];                                  \
     if (!HFB_EXPECT(i < n && I.W && I.H && I.W <= 65536 && I.H <= 65536 && I.scratch && I.segBuf && \

@@ -226,8 +226,9 @@ __global__ void __launch_bounds__(128) shadingBatch(BatchView b, uint32_t SP, fl
   const uint32_t n = b.hdr->n;
   const uint32_t* row = b.prefix + BK_SHADING * (BATCH_MAX + 1);
   const uint32_t total = row[n];
-  __shared__ uint32_t vbNext;
-  for (uint32_t v = batchNext(b.hdr, BK_SHADING, &vbNext); v < total; v = batchNext(b.hdr, BK_SHADING, &vbNext)) {
+  __shared__ uint32_t vbNext[2];
+  uint32_t vbPar = 0;
+  for (uint32_t v = batchNext(b.hdr, BK_SHADING, vbNext, vbPar); v < total; v = batchNext(b.hdr, BK_SHADING, vbNext, vbPar)) {
     const uint32_t i = batchFind(row, n, v);
     const BatchInst& I = b.insts[i];
     shadingBody(I.U, I.S, I.P, SP, zNear, zFar, I.posNew, I.tan, I.shadingDepth, I.ao, I.aoW, I.aoH, I.sm,

@@ -363,7 +363,7 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
     const uint32_t ls = i / P, pt = i - ls * P;
     *HFB_G(&prev[(size_t)s0 * P + i]) = wk[ls * R + pt];
   }
-  __syncthreads();  // the block's staging is reused by its next strands
+  // the staging is rewritten by the CTA's next strands only after batchNext's barrier
 }
 
 __global__ void __launch_bounds__(SIM_THREADS)
@@ -473,7 +473,7 @@ __device__ __forceinline__ void gridPostSimBody(const HfbSimUniforms& u, uint32_
     sh.key[e] = GP_EMPTY;
     sh.val[e] = make_uint4(0u, 0u, 0u, 0u);
   }
-  __syncthreads();
+  // the next points' adds come after batchNext's barrier, with the table empty
 }
 
 __global__ void __launch_bounds__(GP_THREADS)
@@ -490,8 +490,9 @@ __global__ void __launch_bounds__(256) gridPreSimBatch(BatchView b, uint32_t G) 
   const uint32_t n = b.hdr->n;
   const uint32_t* row = b.prefix + BK_GRID_PRE * (BATCH_MAX + 1);
   const uint32_t total = row[n];
-  __shared__ uint32_t vbNext;
-  for (uint32_t v = batchNext(b.hdr, BK_GRID_PRE, &vbNext); v < total; v = batchNext(b.hdr, BK_GRID_PRE, &vbNext)) {
+  __shared__ uint32_t vbNext[2];
+  uint32_t vbPar = 0;
+  for (uint32_t v = batchNext(b.hdr, BK_GRID_PRE, vbNext, vbPar); v < total; v = batchNext(b.hdr, BK_GRID_PRE, vbNext, vbPar)) {
     const uint32_t i = batchFind(row, n, v);
     const BatchInst& I = b.insts[i];
     gridPreSimBody(I.SU, G, I.dv, I.gw, I.sdf, I.sdfDims, (v - row[i]) * 256u + threadIdx.x);
@@ -503,8 +504,9 @@ __global__ void __launch_bounds__(SIM_THREADS, 4) simIntegrateBatch(BatchView b,
   const uint32_t n = b.hdr->n;
   const uint32_t* row = b.prefix + BK_INTEGRATE * (BATCH_MAX + 1);
   const uint32_t total = row[n];
-  __shared__ uint32_t vbNext;
-  for (uint32_t v = batchNext(b.hdr, BK_INTEGRATE, &vbNext); v < total; v = batchNext(b.hdr, BK_INTEGRATE, &vbNext)) {
+  __shared__ uint32_t vbNext[2];
+  uint32_t vbPar = 0;
+  for (uint32_t v = batchNext(b.hdr, BK_INTEGRATE, vbNext, vbPar); v < total; v = batchNext(b.hdr, BK_INTEGRATE, vbNext, vbPar)) {
     const uint32_t i = batchFind(row, n, v);
     const BatchInst& I = b.insts[i];
     // integration reads positions[1 - current] (prev) and [current] (now), writes the former
@@ -520,8 +522,9 @@ __global__ void __launch_bounds__(GP_THREADS) gridPostSimBatch(BatchView b, uint
   const uint32_t n = b.hdr->n;
   const uint32_t* row = b.prefix + BK_GRID_POST * (BATCH_MAX + 1);
   const uint32_t total = row[n];
-  __shared__ uint32_t vbNext;
-  for (uint32_t v = batchNext(b.hdr, BK_GRID_POST, &vbNext); v < total; v = batchNext(b.hdr, BK_GRID_POST, &vbNext)) {
+  __shared__ uint32_t vbNext[2];
+  uint32_t vbPar = 0;
+  for (uint32_t v = batchNext(b.hdr, BK_GRID_POST, vbNext, vbPar); v < total; v = batchNext(b.hdr, BK_GRID_POST, vbNext, vbPar)) {
     const uint32_t i = batchFind(row, n, v);
     const BatchInst& I = b.insts[i];
     // after the swap: prev = the old current positions, now = the new ones
