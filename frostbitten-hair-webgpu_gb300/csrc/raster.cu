@@ -831,7 +831,7 @@ constexpr uint32_t RUN_ENDS = 1u << 31;
 constexpr uint32_t FINE_SPLIT_MIN = 256;  // records: tiles below this are never split
 
 template <int TS> struct FineDims;
-template <> struct FineDims<8> { static constexpr uint32_t STAGE = 64, PAIRS = 1024; };
+template <> struct FineDims<8> { static constexpr uint32_t STAGE = 64, PAIRS = 768; };
 template <> struct FineDims<16> { static constexpr uint32_t STAGE = 96, PAIRS = 2048; };
 template <> struct FineDims<32> { static constexpr uint32_t STAGE = 256, PAIRS = 4096; };
 
@@ -1739,7 +1739,7 @@ __device__ __forceinline__ void fineItem(FineSmem<TS>& sh, const HfbUniforms& U,
 }
 
 template <int TS, int MAXL>
-__global__ void __launch_bounds__(TS * TS, TS == 8 ? 6 : TS == 16 ? (MAXL <= 4 ? 4 : 2) : 1)
+__global__ void __launch_bounds__(TS * TS, TS == 8 ? (MAXL <= 4 ? 8 : 6) : TS == 16 ? (MAXL <= 4 ? 4 : 2) : 1)
 fineKernel(const HfbUniforms U, const FineArgs a, const uint32_t* __restrict__ tileList, float* __restrict__ result,
            FineScratch fs) {
   using SM = FineSmem<TS>;
@@ -1759,7 +1759,7 @@ fineKernel(const HfbUniforms U, const FineArgs a, const uint32_t* __restrict__ t
 
 // batched: one queue over the work items of every instance
 template <int TS, int MAXL>
-__global__ void __launch_bounds__(TS * TS, TS == 8 ? 6 : TS == 16 ? (MAXL <= 4 ? 4 : 2) : 1)
+__global__ void __launch_bounds__(TS * TS, TS == 8 ? (MAXL <= 4 ? 8 : 6) : TS == 16 ? (MAXL <= 4 ? 4 : 2) : 1)
 fineBatch(BatchView b, FineArgs base, HfbConfig cfgParam) {
   using SM = FineSmem<TS>;
   const HfbConfig cfg = cfgParam;
