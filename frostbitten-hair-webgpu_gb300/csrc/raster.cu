@@ -163,8 +163,8 @@ __device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* war
 // own thread, tile by tile (rasterSegmentSerial).
 // ---------------------------------------------------------------------------
 constexpr uint32_t TR_SEGS = TILES_RASTER_SEGS;  // segments (and threads) per block
-constexpr uint32_t TR_SLOTS = 768;  // (segment, tile) accumulators per block
-constexpr uint32_t TR_CHUNK = 2048; // pairs per A1 / A2 round
+constexpr uint32_t TR_SLOTS = 512;  // (segment, tile) accumulators per block
+constexpr uint32_t TR_CHUNK = 1024; // pairs per A1 / A2 round
 
 struct TrShared {
   float ox[4][TR_SEGS], oy[4][TR_SEGS], ex[4][TR_SEGS], ey[4][TR_SEGS];  // edge tests (insideQuad order)
@@ -1858,7 +1858,7 @@ cudaError_t launchFineT(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, c
     const TilesScratch ts = tilesScratchLayout(I.scratch, cfg, I.W, I.H, I.maxDrawn); \
     (void)ts;
 
-__global__ void __launch_bounds__(TR_SEGS, 6) tilesRasterBatch(BatchView b, HfbConfig cfgParam,
+__global__ void __launch_bounds__(TR_SEGS, 7) tilesRasterBatch(BatchView b, HfbConfig cfgParam,
                                                              DeviceCounters* __restrict__ counters) {
   const HfbConfig cfg = cfgParam;
   __shared__ TrShared sh;
