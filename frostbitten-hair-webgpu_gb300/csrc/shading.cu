@@ -222,7 +222,7 @@ shadingKernel(const HfbUniforms U, uint32_t S, uint32_t P, uint32_t SP, float zN
 }
 
 // batched: persistent over the virtual blocks of every instance
-__global__ void __launch_bounds__(128) shadingBatch(BatchView b, uint32_t SP, float zNear, float zFar) {
+__global__ void __launch_bounds__(128, 6) shadingBatch(BatchView b, uint32_t SP, float zNear, float zFar) {
   const uint32_t n = b.hdr->n;
   const uint32_t* row = b.prefix + BK_SHADING * (BATCH_MAX + 1);
   const uint32_t total = row[n];

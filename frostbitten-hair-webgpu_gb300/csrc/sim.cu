@@ -515,7 +515,7 @@ __global__ void __launch_bounds__(SIM_THREADS, 4) simIntegrateBatch(BatchView b,
   }
 }
 
-__global__ void __launch_bounds__(GP_THREADS) gridPostSimBatch(BatchView b, uint32_t G) {
+__global__ void __launch_bounds__(GP_THREADS, 5) gridPostSimBatch(BatchView b, uint32_t G) {
   __shared__ GridPostShared sh;
   gridPostClear(sh);
   __syncthreads();
