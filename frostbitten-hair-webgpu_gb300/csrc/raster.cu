@@ -163,9 +163,14 @@ __device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* war
 // own thread, tile by tile (rasterSegmentSerial).
 // ---------------------------------------------------------------------------
 constexpr uint32_t TR_SEGS = TILES_RASTER_SEGS;  // segments (and threads) per block
-constexpr uint32_t TR_SLOTS = 512;  // (segment, tile) accumulators per block
-constexpr uint32_t TR_CHUNK = 1024; // pairs per A1 / A2 round
+// (segment, tile) accumulators per block and pairs per A1 / A2 round: the
+// single-instance kernel keeps more of a large frame's long segments in
+// shared memory (768, 2,048: 6 CTAs per SM); the batched one, whose
+// instances are smaller, trades them for a seventh CTA (512, 1,024).
+constexpr uint32_t TR_SLOTS = 768, TR_CHUNK = 2048;
+constexpr uint32_t TR_SLOTS_BATCH = 512, TR_CHUNK_BATCH = 1024;
 
+template <uint32_t TR_SLOTS, uint32_t TR_CHUNK>
 struct TrShared {
   float ox[4][TR_SEGS], oy[4][TR_SEGS], ex[4][TR_SEGS], ey[4][TR_SEGS];  // edge tests (insideQuad order)
   float dp[4][TR_SEGS];                                                 // depthsProj
@@ -264,13 +269,15 @@ __device__ void rasterSegmentSerial(const HfbUniforms& U, const ProjSeg& s, uint
   }
 }
 
+template <uint32_t TR_SLOTS, uint32_t TR_CHUNK>
 __device__ __forceinline__ void tilesRasterBody(const HfbUniforms& U, uint32_t P, uint32_t nStrands, uint32_t TS,
                                                 uint32_t B, uint32_t threshold, float4 bsphere,
                                                 const float4* __restrict__ pos, const float4* __restrict__ tan,
                                                 const float* __restrict__ depth, uint4* __restrict__ tiles,
                                                 uint32_t* __restrict__ segBuf, uint32_t* __restrict__ segCount,
                                                 uint32_t* __restrict__ binCount,
-                                                DeviceCounters* __restrict__ counters, TrShared& sh, uint32_t blk) {
+                                                DeviceCounters* __restrict__ counters, TrShared<TR_SLOTS, TR_CHUNK>& sh,
+                                                uint32_t blk) {
   const uint32_t tid = threadIdx.x, lane = tid & 31u;
   const uint32_t segsPerStrand = P - 1u;
   const uint32_t nSeg = nStrands * segsPerStrand;
@@ -473,9 +480,9 @@ tilesRasterKernel(const HfbUniforms U, uint32_t P, uint32_t nStrands, uint32_t T
                   const float4* __restrict__ tan, const float* __restrict__ depth, uint4* __restrict__ tiles,
                   uint32_t* __restrict__ segBuf, uint32_t* __restrict__ segCount,
                   uint32_t* __restrict__ binCount, DeviceCounters* __restrict__ counters) {
-  __shared__ TrShared sh;
-  tilesRasterBody(U, P, nStrands, TS, B, threshold, bsphere, pos, tan, depth, tiles, segBuf, segCount, binCount,
-                  counters, sh, blockIdx.x);
+  __shared__ TrShared<TR_SLOTS, TR_CHUNK> sh;
+  tilesRasterBody<TR_SLOTS, TR_CHUNK>(U, P, nStrands, TS, B, threshold, bsphere, pos, tan, depth, tiles, segBuf,
+                                      segCount, binCount, counters, sh, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -1861,9 +1868,9 @@ cudaError_t launchFineT(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, c
 __global__ void __launch_bounds__(TR_SEGS, 7) tilesRasterBatch(BatchView b, HfbConfig cfgParam,
                                                              DeviceCounters* __restrict__ counters) {
   const HfbConfig cfg = cfgParam;
-  __shared__ TrShared sh;
+  __shared__ TrShared<TR_SLOTS_BATCH, TR_CHUNK_BATCH> sh;
   BATCH_LOOP(BK_RASTER)
-    tilesRasterBody(I.U, I.P, min(I.strandsToRender, I.S), cfg.tileSize, cfg.tileDepthBins,
+    tilesRasterBody<TR_SLOTS_BATCH, TR_CHUNK_BATCH>(I.U, I.P, min(I.strandsToRender, I.S), cfg.tileSize, cfg.tileDepthBins,
                     cfg.invalidTilesPerSegmentThreshold, I.bsphere, I.posNew, I.tan, I.depth, I.tiles, I.segBuf,
                     I.segCount, ts.binCount, counters, sh, local);
   }
