@@ -33,7 +33,8 @@ namespace hfb {
 namespace {
 
 constexpr uint32_t HD_THREADS = 256;             // points per block: each point's two vertices once
-constexpr uint32_t HD_SEGS = HD_THREADS - 1u;    // segment starts per block (the last point is shared)
+constexpr uint32_t HD_WARP_SEGS = 31;            // segment starts per warp: its 32 points, the last shared
+constexpr uint32_t HD_SEGS = (HD_THREADS / 32u) * HD_WARP_SEGS;  // segment starts per block
 constexpr uint32_t HD_BIG_AREA = 1024;           // pixels: larger triangles are drawn by a whole block
 constexpr uint32_t HD_VIEW_FLOATS = 35;
 
@@ -266,10 +267,11 @@ __device__ __forceinline__ void blockQuad(const HdShared& sh, uint32_t k, Screen
   q[3] = unpackV(sh.sv[k + 1][1]);
 }
 
-// One block of HD_THREADS points starting at point blk * HD_SEGS: every
-// thread projects its point's two vertices into shared memory; each of the
-// first HD_SEGS threads owns the segment from its point to the next (when
-// that point is not its strand's last) and boxes its two triangles.  A box
+// One block of segment starts [blk * HD_SEGS, (blk + 1) * HD_SEGS): each
+// warp projects the two vertices of 32 consecutive points into shared
+// memory and its first 31 lanes own the segments from their point to the
+// next (when that point is not its strand's last): the warps need no
+// barrier between them.  A lane boxes its segment's two triangles.  A box
 // of more than HD_BIG_AREA pixels goes onto the big list (entries
 // point << 1 | triangle; capacity `bigCap`); the pixels of the union of a
 // segment's other boxes are shared out over the warp's lanes (an exclusive
@@ -289,18 +291,20 @@ __device__ __forceinline__ void hairDepthBlock(const HdView& V, uint32_t P, uint
                                                const HdOut& out, uint32_t* __restrict__ big,
                                                uint32_t bigCap, uint32_t blk, HdShared& sh) {
   const uint32_t tid = threadIdx.x, lane = tid & 31u, wp = tid >> 5;
-  const uint32_t pt = blk * HD_SEGS + tid;
+  // warp wp: points blk * HD_SEGS + wp * 31 + lane; its segments start at lanes 0..30,
+  // so a segment's two points are projected by the same warp
+  const uint32_t pt = blk * HD_SEGS + wp * HD_WARP_SEGS + lane;
   if (pt < nPts) {
     ScreenV a, b;
     pointPair(V, pos, tan, pt, a, b);
     sh.sv[tid][0] = packV(a);
     sh.sv[tid][1] = packV(b);
   }
-  __syncthreads();
+  __syncwarp();
   const uint32_t W = f2u(V.W), H = f2u(V.H);
   uint32_t mine = 0;
   bool own[2] = {false, false};  // big, list full: drawn by this thread
-  if (tid < HD_SEGS && pt + 1u < nPts && pt % P != P - 1u) {
+  if (lane < HD_WARP_SEGS && pt + 1u < nPts && pt % P != P - 1u) {
     ScreenV q[4];
     blockQuad(sh, tid, q);
     HdUnit un;
@@ -361,7 +365,7 @@ __device__ __forceinline__ void hairDepthBlock(const HdView& V, uint32_t P, uint
     const int x = un.x0 + (int)(local - row * un.bw), y = un.y0 + (int)row;
     ScreenV q[4];
     blockQuad(sh, o, q);
-    const uint32_t opt = blk * HD_SEGS + o;
+    const uint32_t opt = blk * HD_SEGS + wp * HD_WARP_SEGS + lo;
 #pragma unroll
     for (uint32_t tr = 0; tr < 2u; tr++)
       if (x >= un.bx0[tr] && x <= un.bx1[tr] && y >= un.by0[tr] && y <= un.by1[tr])
