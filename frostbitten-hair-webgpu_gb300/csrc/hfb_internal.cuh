@@ -91,10 +91,11 @@ struct FineScratch {
 };
 uint32_t maxDrawnSegments(const HfbConfig& cfg, uint32_t W, uint32_t H);
 
-// Strands per integration block for P points per strand: one chain warp per
-// block for P <= 32, fewer strands for longer strands (shared memory ~38 KB).
+// Strands per integration block for P points per strand: 1024 / P (at least
+// 8), so a block's 256 threads take four points each in the point phases and
+// its staging stays near 38 KB (64 strands of 16 points, 32 of 32).
 __host__ __device__ inline uint32_t simStrandsPerBlock(uint32_t P) {
-  return 1024u / P > 8u ? 1024u / P : 8u;  // NB * P <= 1024: four points per thread
+  return 1024u / P > 8u ? 1024u / P : 8u;
 }
 __host__ __device__ inline size_t simSmemBytes(uint32_t P) {
   return (size_t)simStrandsPerBlock(P) * (P + 1u) * (2u * sizeof(float4) + sizeof(float)) + (size_t)P * 4u;
