@@ -14,6 +14,8 @@ positions within 1e-5 relative after 60 steps):
   correctly rounded on either side;
 - fine pass: every pixel channel within 1/255.
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -26,7 +28,7 @@ torch = pytest.importorskip("torch")
 if not torch.cuda.is_available():
     pytest.skip("needs a CUDA GPU", allow_module_level=True)
 
-from hairfb.lib import Context  # noqa: E402
+from hairfb.lib import Context, byref, ptr  # noqa: E402
 from hairfb.passes import (GridPostSimPass, GridPreSimPass, HairFinePass, HairObject,  # noqa: E402
                            HairShadingPass, HairSimIntegrationPass, HairTileSortPass, HairTilesPass,
                            PhysicsGrids, RasterBuffers, SdfCollider, clear_before_render)
@@ -506,6 +508,18 @@ def test_invalid_arguments_return_errors():
     with pytest.raises(HfbError):
         ctx.call("hfb_grid_post_sim", None, None, misaligned.data_ptr(), misaligned.data_ptr(),
                  misaligned.data_ptr())
+    # the later passes: NULL buffers, a viewport that does not match, a bad AO scale
+    from hairfb.passes import _ub
+    with pytest.raises(HfbError) as e:
+        ctx.call("hfb_present", _ub(fr.uniforms), byref(rb.rb), None, None)
+    assert "NULL" in str(e.value)
+    with pytest.raises(HfbError) as e:
+        ctx.call("hfb_hair_depth", _ub(fr.uniforms), byref(hair.hair_data), ptr(hair.positions), ptr(hair.tangents),
+                 hair.rendered_strand_count(), ptr(d), ptr(d), byref(rb.rb))
+    assert "viewport" in str(e.value)
+    with pytest.raises(HfbError) as e:
+        ctx.call("hfb_gtao", _ub(fr.uniforms), ptr(d), ptr(d), ctypes.c_float(0.0), ptr(d))
+    assert "scale" in str(e.value)
     ctx.sync()  # the context stays usable
 
 
