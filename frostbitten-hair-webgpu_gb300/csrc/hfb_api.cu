@@ -158,6 +158,22 @@ int hfb_get_counters(HfbCtx* c, HfbCounters* out) {
   return HFB_OK;
 }
 
+int hfb_check_constant_division(HfbCtx* c, uint64_t out[3]) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, out, "out is NULL");
+  unsigned long long* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, 3 * sizeof(unsigned long long));
+  if (e != cudaSuccess) return cudaFail(c, e, "hfb_check_constant_division");
+  unsigned long long h[3] = {0, 0, 0};
+  e = hfb::launchConstDivCheck(c, d);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(d);
+  if (e != cudaSuccess) return cudaFail(c, e, "hfb_check_constant_division");
+  for (int i = 0; i < 3; i++) out[i] = h[i];
+  return HFB_OK;
+}
+
 int hfb_buffer_alloc(HfbCtx* c, size_t bytes, void** out) {
   HFB_CHECK_CTX(c);
   HFB_REQUIRE(c, out, "out is NULL");

@@ -306,6 +306,8 @@ __device__ __forceinline__ uint32_t batchNext(BatchHdr* hdr, uint32_t k, uint32_
 // Batched launchers: one persistent launch of kind k over all instances.
 cudaError_t launchBatchClear(HfbCtx* c, const BatchView& b, BatchKind k);
 cudaError_t launchBatchSim(HfbCtx* c, const BatchView& b, BatchKind k);
+// hfb_check_constant_division: cnt[3] on the device, zeroed here
+cudaError_t launchConstDivCheck(HfbCtx* c, unsigned long long* cnt);
 cudaError_t launchBatchShading(HfbCtx* c, const BatchView& b);
 cudaError_t launchBatchTiles(HfbCtx* c, const BatchView& b);
 cudaError_t launchBatchSort(HfbCtx* c, const BatchView& b);

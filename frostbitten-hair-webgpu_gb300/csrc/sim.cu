@@ -22,7 +22,27 @@ constexpr float SDF_GRAD_OFFSET = (float)(0.0033918858971446753 * 0.1);
 constexpr float FLOAT_EPSILON = 1e-7f;
 
 __device__ __forceinline__ int32_t gridEncode(float v) { return f2i(fmul(v, GRID_MUL)); }
-__device__ __forceinline__ float gridDecode(int32_t v) { return (float)v / GRID_MUL; }
+
+// Division by the constants 1e6 and 3 as a correctly rounded multiplication
+// by the reciprocal, RN(x * Ch + RN(x * Cl)) with Ch + Cl the reciprocal split
+// into two floats (Brisebarre and Muller, "Correctly rounded multiplication by
+// arbitrary precision constants", IEEE Trans. Computers 57(2), 2008): one
+// multiply and one FMA instead of an IEEE division.  For these two constants
+// it gives the IEEE quotient x / d bit for bit for every finite x with
+// |x| >= 2^-92 (d = 1e6) and |x| > 2^-123 (d = 3); hfb_check_constant_division
+// compares it with the device's division over all 2^32 inputs.
+constexpr float RCP_1E6_HI = 0x1.0c6f7ap-20f, RCP_1E6_LO = 0x1.6bdb1ap-49f;
+constexpr float RCP_3_HI = 0x1.555556p-2f, RCP_3_LO = -0x1.555556p-27f;
+__device__ __forceinline__ float mulRcp(float x, float hi, float lo) { return __fmaf_rn(x, hi, fmul(x, lo)); }
+
+// (float)v / 1e6: a converted i32 is 0 or at least 1 in magnitude
+__device__ __forceinline__ float gridDecode(int32_t v) { return mulRcp((float)v, RCP_1E6_HI, RCP_1E6_LO); }
+
+__device__ __forceinline__ float divBy3(float x) {
+  const float a = fabsf(x);
+  return a > 0x1p-123f && a < INFINITY ? mulRcp(x, RCP_3_HI, RCP_3_LO) : x / 3.0f;
+}
+__device__ __forceinline__ f3 div3sBy3(f3 v) { return {divBy3(v.x), divBy3(v.y), divBy3(v.z)}; }
 
 __device__ __forceinline__ uint32_t gridIdx(uint32_t G, uint32_t x, uint32_t y, uint32_t z) {
   return clampu(z, 0u, G - 1u) * G * G + clampu(y, 0u, G - 1u) * G + clampu(x, 0u, G - 1u);
@@ -147,8 +167,16 @@ __global__ void __launch_bounds__(256) gridPreSimKernel(const HfbSimUniforms u, 
 // constants, the initial tangents) is staged beside the points, so a chain
 // step touches shared memory only.
 // ---------------------------------------------------------------------------
-constexpr uint32_t SIM_THREADS = 256;
+constexpr uint32_t SIM_THREADS = 256;        // threads per block of the single-instance kernel
+constexpr uint32_t SIM_BATCH_THREADS = 256;  // and of the batched one (4 blocks per SM; 128-thread
+                                             // blocks, 5 per SM, were slower: 4.15 ms against 3.80)
 
+
+// p + z for z a signed zero whose sign is that of c xor the bit in s: p itself
+// unless p is -0 and z is +0
+__device__ __forceinline__ void zeroSum(float& p, float c, uint32_t s) {
+  if (__float_as_uint(p) == 0x80000000u && ((__float_as_uint(c) ^ s) & 0x80000000u) == 0u) p = 0.0f;
+}
 
 // Verlet step of one point with the grid forces (:125-162, integration.wgsl.ts:8-28)
 __device__ __forceinline__ float4 verletPoint(const HfbSimUniforms& u, uint32_t G, f3 gmin, f3 gmax,
@@ -190,6 +218,7 @@ __device__ __forceinline__ float4 verletPoint(const HfbSimUniforms& u, uint32_t 
   return make_float4(r.x, r.y, r.z, posNow.w);
 }
 
+template <uint32_t NT>
 __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32_t S, uint32_t P, uint32_t G,
                                                  float4* __restrict__ prev, const float4* __restrict__ now,
                                                  const float4* __restrict__ initial, const float* __restrict__ segLen,
@@ -211,7 +240,7 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
   const uint32_t jTan = P >= 3u ? P - 3u : 0u;
 
   // --- Verlet + forces and the chain constants, point-parallel ---
-  for (uint32_t i = tid; i < nPts; i += SIM_THREADS) {
+  for (uint32_t i = tid; i < nPts; i += NT) {
     const uint32_t ls = i / P, pt = i - ls * P;
     const size_t gi = (size_t)s0 * P + i;
     const f4 posNow = ld4(__ldg(HFB_G(&now[gi])));
@@ -222,7 +251,7 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
     float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
     if (pt + 3u < P) {  // applyConstraint_localShape constants (constraints.wgsl.ts:54-99)
       const float4 i1 = __ldg(HFB_G(&initial[gi + 1u])), i2 = __ldg(HFB_G(&initial[gi + 2u]));
-      f3 cI = div3s(add3(add3(mk3(i0.x, i0.y, i0.z), mk3(i1.x, i1.y, i1.z)), mk3(i2.x, i2.y, i2.z)), 3.0f);
+      f3 cI = div3sBy3(add3(add3(mk3(i0.x, i0.y, i0.z), mk3(i1.x, i1.y, i1.z)), mk3(i2.x, i2.y, i2.z)));
       const float h0 = len3(sub3(cI, mk3(i1.x, i1.y, i1.z)));
       const float wT = fadd(fadd(i0.w, fmul(2.0f, i1.w)), i2.w);
       c = make_float4(h0, fmul(i0.w / wT, 2.0f), fmul(i1.w / wT, -4.0f), fmul(i2.w / wT, 2.0f));
@@ -232,7 +261,7 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
     }
     lc[ls * R + pt] = c;
   }
-  for (uint32_t j = tid; j < P; j += SIM_THREADS) {  // applyConstraint_global's attenuation (constraints.wgsl.ts:31-49)
+  for (uint32_t j = tid; j < P; j += NT) {  // applyConstraint_global's attenuation (constraints.wgsl.ts:31-49)
     const float x = (float)j / (float)(P - 1u);
     att[j] = fsub(1.0f, sat(fsub(x, u.globalConstrExtent) / u.globalConstrFade));
   }
@@ -250,12 +279,13 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
   const float kGlob = u.stiffnessGlobalConstr / (float)iters;
   const float kLoc = u.stiffnessLocalConstr / (float)iters;
   const float kColl = u.stiffnessCollisions / (float)iters;
+  const bool kCollFinite = fabsf(kColl) < INFINITY;
   const float kSdf = u.stiffnessSDF / (float)iters;
   for (uint32_t it = 0; it < iters; it++) {
     // length constraint (Gauss-Seidel), :176-190, constraints.wgsl.ts:5-28
-    if (tid < nStr) {
-      float4* w = wk + tid * R;
-      const float* L = sl + tid * R;
+    for (uint32_t ls = tid; ls < nStr; ls += NT) {
+      float4* w = wk + ls * R;
+      const float* L = sl + ls * R;
       float4 a = w[0];
       for (uint32_t j = 0; j + 1u < P; j++) {
         float4 b = w[j + 1u];
@@ -264,7 +294,9 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
         f3 tng = mk3(fsub(b.x, a.x), fsub(b.y, a.y), fsub(b.z, a.z));
         float actual = len3(tng);
         float corr = fsub(1.0f, expected / actual);
-        float df = fmul(corr, kLen) / fadd(fadd(w0, w1), FLOAT_EPSILON);
+        // two movable points (the common case) make the divisor exactly 2: a halving, exact as a product
+        const float num = fmul(corr, kLen), den = fadd(fadd(w0, w1), FLOAT_EPSILON);
+        float df = den == 2.0f ? fmul(num, 0.5f) : num / den;
         f3 delta = mul3s(tng, df);
         a.x = fadd(a.x, fmul(delta.x, w0)); a.y = fadd(a.y, fmul(delta.y, w0)); a.z = fadd(a.z, fmul(delta.z, w0));
         b.x = fsub(b.x, fmul(w1, delta.x)); b.y = fsub(b.y, fmul(w1, delta.y)); b.z = fsub(b.z, fmul(w1, delta.z));
@@ -275,7 +307,7 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
     }
     __syncthreads();
     // global shape, :193-206, constraints.wgsl.ts:31-49 (point-parallel)
-    for (uint32_t i = tid; i < nPts; i += SIM_THREADS) {
+    for (uint32_t i = tid; i < nPts; i += NT) {
       const uint32_t ls = __umulhi(i, divP), j = i - ls * P;
       if (j == 0u) continue;
       const float4 pi = __ldg(HFB_G(&initial[(size_t)s0 * P + i]));
@@ -288,16 +320,16 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
     }
     __syncthreads();
     // local shape (triangle bending, Gauss-Seidel), :209-232, constraints.wgsl.ts:54-120
-    if (tid < nStr) {
-      float4* w = wk + tid * R;
-      const float4* C = lc + tid * R;
+    for (uint32_t ls = tid; ls < nStr; ls += NT) {
+      float4* w = wk + ls * R;
+      const float4* C = lc + ls * R;
       uint32_t jj = 0;
       if (P >= 3u) {
         float4 p0 = w[0], p1 = w[1];
         for (; jj + 3u < P; jj++) {
           float4 p2 = w[jj + 2u];
           const float4 cc = C[jj];
-          f3 c = div3s(add3(add3(mk3(p0.x, p0.y, p0.z), mk3(p1.x, p1.y, p1.z)), mk3(p2.x, p2.y, p2.z)), 3.0f);
+          f3 c = div3sBy3(add3(add3(mk3(p0.x, p0.y, p0.z), mk3(p1.x, p1.y, p1.z)), mk3(p2.x, p2.y, p2.z)));
           f3 hv = sub3(mk3(p1.x, p1.y, p1.z), c);
           float h = len3(hv);
           f3 delta = mul3s(hv, fsub(1.0f, cc.x / h));
@@ -327,16 +359,25 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
     }
     __syncthreads();
     // collisions, :236-261, collisions.wgsl.ts:4-61 (point-parallel)
-    for (uint32_t i = tid; i < nPts; i += SIM_THREADS) {
+    for (uint32_t i = tid; i < nPts; i += NT) {
       const uint32_t ls = __umulhi(i, divP), j = i - ls * P;
       if (j == 0u) continue;
       float4 pos = wk[ls * R + j];
       {
         f3 v = mk3(fsub(pos.x, sph.x), fsub(pos.y, sph.y), fsub(pos.z, sph.z));
-        float dist = fsub(len3(v), sph.w);
+        const float l = len3(v);
+        float dist = fsub(l, sph.w);
         float dts = fmaxf(0.0f, -dist);
-        f3 d = mul3s(mul3s(norm3(v), dts), kColl);
-        pos.x = fadd(pos.x, d.x); pos.y = fadd(pos.y, d.y); pos.z = fadd(pos.z, d.z);
+        if (dts == 0.0f && l > 0.0f && l < INFINITY && kCollFinite) {
+          // outside the sphere the correction (v / l) * dts * kColl is a signed zero, the sign
+          // of v's component times those of dts and kColl; adding it changes only a -0
+          // coordinate, into +0 when the zero is +0
+          const uint32_t sz = (__float_as_uint(dts) ^ __float_as_uint(kColl)) & 0x80000000u;
+          zeroSum(pos.x, v.x, sz); zeroSum(pos.y, v.y, sz); zeroSum(pos.z, v.z, sz);
+        } else {
+          f3 d = mul3s(mul3s(norm3(v), dts), kColl);
+          pos.x = fadd(pos.x, d.x); pos.y = fadd(pos.y, d.y); pos.z = fadd(pos.z, d.z);
+        }
       }
       if (j > 2u) {
         f3 q = mk3(pos.x, pos.y, pos.z);
@@ -359,7 +400,7 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
     __syncthreads();
   }
   // --- write back into the PREV buffer, coalesced (:268-272) ---
-  for (uint32_t i = tid; i < nPts; i += SIM_THREADS) {
+  for (uint32_t i = tid; i < nPts; i += NT) {
     const uint32_t ls = i / P, pt = i - ls * P;
     *HFB_G(&prev[(size_t)s0 * P + i]) = wk[ls * R + pt];
   }
@@ -373,7 +414,7 @@ simIntegrateKernel(const HfbSimUniforms u, uint32_t S, uint32_t P, uint32_t G,
                    const int4* __restrict__ dv, const float4* __restrict__ gw,
                    const float* __restrict__ sdf, uint32_t D) {
   extern __shared__ float4 simSmem[];
-  simIntegrateBody(u, S, P, G, prev, now, initial, segLen, dv, gw, sdf, D, simSmem, blockIdx.x);
+  simIntegrateBody<SIM_THREADS>(u, S, P, G, prev, now, initial, segLen, dv, gw, sdf, D, simSmem, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -499,7 +540,7 @@ __global__ void __launch_bounds__(256) gridPreSimBatch(BatchView b, uint32_t G) 
   }
 }
 
-__global__ void __launch_bounds__(SIM_THREADS, 4) simIntegrateBatch(BatchView b, uint32_t G) {
+__global__ void __launch_bounds__(SIM_BATCH_THREADS, 4) simIntegrateBatch(BatchView b, uint32_t G) {
   extern __shared__ float4 simSmem[];
   const uint32_t n = b.hdr->n;
   const uint32_t* row = b.prefix + BK_INTEGRATE * (BATCH_MAX + 1);
@@ -510,7 +551,7 @@ __global__ void __launch_bounds__(SIM_THREADS, 4) simIntegrateBatch(BatchView b,
     const uint32_t i = batchFind(row, n, v);
     const BatchInst& I = b.insts[i];
     // integration reads positions[1 - current] (prev) and [current] (now), writes the former
-    simIntegrateBody(I.SU, I.S, I.P, G, I.posNew, I.posOld, I.initial, I.segLen, I.dv, I.gw, I.sdf, I.sdfDims,
+    simIntegrateBody<SIM_BATCH_THREADS>(I.SU, I.S, I.P, G, I.posNew, I.posOld, I.initial, I.segLen, I.dv, I.gw, I.sdf, I.sdfDims,
                      simSmem, v - row[i]);
   }
 }
@@ -533,7 +574,40 @@ __global__ void __launch_bounds__(GP_THREADS, 5) gridPostSimBatch(BatchView b, u
 }
 
 
+// Compares the reciprocal forms above with the IEEE division over all 2^32
+// inputs: cnt[0] x / 3 over every non-NaN float, cnt[1] (float)v / 1e6 over
+// every i32 v, cnt[2] x / 1e6 over every finite float with |x| >= 2^-92.
+__global__ void __launch_bounds__(256) constDivCheckKernel(unsigned long long* __restrict__ cnt) {
+  unsigned long long bad3 = 0, badGrid = 0, bad6 = 0;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (1ull << 32); i += stride) {
+    const uint32_t bits = (uint32_t)i;
+    const float x = __uint_as_float(bits);
+    if (x == x) {
+      bad3 += __float_as_uint(divBy3(x)) != __float_as_uint(x / 3.0f);
+      const float a = fabsf(x);
+      if (a >= 0x1p-92f && a < INFINITY)
+        bad6 += __float_as_uint(mulRcp(x, RCP_1E6_HI, RCP_1E6_LO)) != __float_as_uint(x / GRID_MUL);
+    }
+    const int32_t v = (int32_t)bits;
+    badGrid += __float_as_uint(gridDecode(v)) != __float_as_uint((float)v / GRID_MUL);
+  }
+  if (bad3) atomicAdd(&cnt[0], bad3);
+  if (badGrid) atomicAdd(&cnt[1], badGrid);
+  if (bad6) atomicAdd(&cnt[2], bad6);
+}
+
 }  // namespace
+
+cudaError_t launchConstDivCheck(HfbCtx* c, unsigned long long* cnt) {
+  HFB_CHECK_BIND(c);
+  cudaError_t e = cudaMemsetAsync(cnt, 0, 3 * sizeof(unsigned long long), c->stream);
+  if (e != cudaSuccess) return e;
+  constDivCheckKernel<<<c->smCount * 8u, 256, 0, c->stream>>>(cnt);
+  HFB_AFTER_LAUNCH(c, "constDivCheckKernel");
+  c->launches += 1;
+  return cudaGetLastError();
+}
 
 cudaError_t launchGridPreSim(HfbCtx* c, const HfbSimUniforms& u, const int32_t* dv, float* gw,
                              const float* sdf, uint32_t sdfDims) {
@@ -594,11 +668,11 @@ cudaError_t launchBatchSim(HfbCtx* c, const BatchView& b, BatchKind k) {
       cudaError_t e = simSmemLimit((const void*)simIntegrateBatch, 1);
       int perSM = 0;
       if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, simIntegrateBatch, SIM_THREADS, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, simIntegrateBatch, SIM_BATCH_THREADS, smem);
       if (e != cudaSuccess) return e;
       grid = (uint32_t)(perSM > 0 ? perSM : 1) * c->smCount;
     }
-    simIntegrateBatch<<<batchLaunchGrid(c, grid), SIM_THREADS, smem, c->stream>>>(b, G);
+    simIntegrateBatch<<<batchLaunchGrid(c, grid), SIM_BATCH_THREADS, smem, c->stream>>>(b, G);
     HFB_AFTER_LAUNCH(c, "simIntegrateBatch");
   } else if (k == BK_GRID_POST) {
     if (!grid) grid = c->smCount * 8u;

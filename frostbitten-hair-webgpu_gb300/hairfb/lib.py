@@ -78,6 +78,7 @@ SIGNATURES = {
     "hfb_ctx_set_stream": (I, [P, P]),
     "hfb_sync": (I, [P]),
     "hfb_get_counters": (I, [P, P]),
+    "hfb_check_constant_division": (I, [P, P]),
     "hfb_buffer_alloc": (I, [P, SZ, P]),
     "hfb_buffer_free": (I, [P, P]),
     "hfb_buffer_upload": (I, [P, P, P, SZ]),

@@ -189,6 +189,14 @@ HFB_API int hfb_ctx_set_stream(HfbCtx* ctx, void* stream);
 HFB_API int hfb_sync(HfbCtx* ctx);
 /* Synchronizes, then copies the counters. */
 HFB_API int hfb_get_counters(HfbCtx* ctx, HfbCounters* out);
+/* Self-check of the simulation's divisions by the constants 3 and 1e6, which
+ * its kernels compute as correctly rounded multiplications by the reciprocal
+ * (one multiply and one FMA): compares them with the device's IEEE division
+ * over all 2^32 inputs and writes the mismatch counts, all 0 expected:
+ * out[0] x / 3 over every non-NaN float, out[1] (float)v / 1e6 over every
+ * int32 v, out[2] x / 1e6 over every finite float with |x| >= 2^-92.
+ * Synchronizes. */
+HFB_API int hfb_check_constant_division(HfbCtx* ctx, uint64_t out[3]);
 
 /* ---- buffers ------------------------------------------------------------ */
 HFB_API int hfb_buffer_alloc(HfbCtx* ctx, size_t bytes, void** out);

@@ -493,6 +493,18 @@ def test_fine_pass_debug_slices_mode(oracle):
     assert np.array_equal(rb.read_result()[4:], ores[4:])
 
 
+def test_constant_division_forms_equal_ieee_division():
+    """The simulation divides by 3 and 1e6 as correctly rounded multiplications
+    by the reciprocal; over all 2^32 inputs they equal the device's IEEE
+    division bit for bit (x / 3 for every non-NaN x, (float)v / 1e6 for every
+    int32 v, x / 1e6 for every finite |x| >= 2^-92)."""
+    ctx = _ctx(small_instance(strands=10))
+    out = (ctypes.c_uint64 * 3)()
+    ctx.call("hfb_check_constant_division", out)
+    assert list(out) == [0, 0, 0]
+    ctx.close()
+
+
 def test_invalid_arguments_return_errors():
     from hairfb.lib import HfbError
     inst = small_instance(strands=10)
