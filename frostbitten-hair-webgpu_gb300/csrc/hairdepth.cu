@@ -15,7 +15,8 @@
 // - coverage is tested at pixel centres (x + 0.5, y + 0.5) in framebuffer
 //   coordinates (rows down), both windings drawn (cullMode 'none'), edges
 //   inclusive; depth = NDC z interpolated with the screen-space barycentric
-//   weights; a triangle with a vertex behind the camera (w <= 0) is not
+//   weights, as (w0 z0 + w1 z1 + w2 z2) / area (the edge values w_i summed
+//   before the one division); a triangle with a vertex behind the camera (w <= 0) is not
 //   drawn (no near-plane clipping); depth outside [0, 1] is discarded;
 // - the 'less' test is an atomic minimum on the depth's bits (non-negative
 //   floats order like their bits), so the result does not depend on the
@@ -136,7 +137,7 @@ __device__ __forceinline__ void triPixel(const Tri& t, float area, const HdOut& 
   if (area < 0.0f) { w0 = -w0; w1 = -w1; w2 = -w2; }
   if (!(w0 >= 0.0f && w1 >= 0.0f && w2 >= 0.0f)) return;
   const float a = fabsf(area);
-  const float z = fadd(fadd(fmul(w0 / a, t.v[0].z), fmul(w1 / a, t.v[1].z)), fmul(w2 / a, t.v[2].z));
+  const float z = fadd(fadd(fmul(w0, t.v[0].z), fmul(w1, t.v[1].z)), fmul(w2, t.v[2].z)) / a;
   if (!(z >= 0.0f && z <= 1.0f)) return;
   const size_t p = (size_t)y * o.W + x;
   const unsigned zb = __float_as_uint(fadd(z, 0.0f));  // -0 -> +0

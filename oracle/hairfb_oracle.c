@@ -1297,6 +1297,7 @@ static inline float linearizeDepth(float n, float f, float d) { return n * f / (
  * index order hairIndexBuffer.ts:29-46), with the rasterizer rules the CUDA
  * prepass uses: coverage at pixel centres, both windings, edges inclusive,
  * depth = NDC z interpolated with the screen-space barycentric weights,
+ * (w0 z0 + w1 z1 + w2 z2) / area,
  * triangles with a vertex behind the camera not drawn, depth outside [0, 1]
  * discarded, depth test 'less' (the minimum). ---- */
 typedef struct { float x, y, z; int ok; } OScreenV;
@@ -1348,7 +1349,7 @@ static void hdTriangle(const OScreenV* a, const OScreenV* b, const OScreenV* c, 
       float w2 = hdEdge(a->x, a->y, b->x, b->y, px, py);
       if (area < 0.0f) { w0 = -w0; w1 = -w1; w2 = -w2; }
       if (!(w0 >= 0.0f && w1 >= 0.0f && w2 >= 0.0f)) continue;
-      float z = (w0 / aa) * a->z + (w1 / aa) * b->z + (w2 / aa) * c->z;
+      float z = (w0 * a->z + w1 * b->z + w2 * c->z) / aa;
       if (!(z >= 0.0f && z <= 1.0f)) continue;
       z = z + 0.0f;
       float* d = depth + (size_t)y * W + x;
@@ -1452,7 +1453,7 @@ EXPORT void oracle_hair_normals(const void* uniforms, const void* hairData, cons
             float w2 = hdEdge(a->x, a->y, b->x, b->y, px, py);
             if (area < 0.0f) { w0 = -w0; w1 = -w1; w2 = -w2; }
             if (!(w0 >= 0.0f && w1 >= 0.0f && w2 >= 0.0f)) continue;
-            float z = (w0 / aa * a->z + w1 / aa * b->z) + w2 / aa * c->z;
+            float z = (w0 * a->z + w1 * b->z + w2 * c->z) / aa;
             if (!(z >= 0.0f && z <= 1.0f)) continue;
             z = z + 0.0f;
             size_t pi = (size_t)y * W + x;
