@@ -168,8 +168,9 @@ __global__ void __launch_bounds__(256) gridPreSimKernel(const HfbSimUniforms u, 
 // step touches shared memory only.
 // ---------------------------------------------------------------------------
 constexpr uint32_t SIM_THREADS = 256;        // threads per block of the single-instance kernel
-constexpr uint32_t SIM_BATCH_THREADS = 256;  // and of the batched one (4 blocks per SM; 128-thread
-                                             // blocks, 5 per SM, were slower: 4.15 ms against 3.80)
+constexpr uint32_t SIM_BATCH_THREADS = 256;  // and of the batched one: 4 blocks per SM (5 blocks of
+                                             // 128 threads took 4.15 ms against 3.80, 5 of 192 3.43
+                                             // against 3.38, on the 64-instance frame)
 
 
 // p + z for z a signed zero whose sign is that of c xor the bit in s: p itself
