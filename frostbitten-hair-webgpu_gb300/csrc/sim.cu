@@ -453,7 +453,10 @@ __device__ __forceinline__ void gridPostAdd(GridPostShared& sh, unsigned* __rest
                                             uint4 v) {
   uint32_t h = (idx * 2654435761u) >> (32 - 11);  // Fibonacci hash into GP_HASH = 2^11 slots
   for (uint32_t p = 0; p < GP_PROBES; p++) {
-    const uint32_t old = atomicCAS(&sh.key[h], GP_EMPTY, idx);
+    // a slot's key only ever changes from GP_EMPTY to a node index, so a plain read that finds the
+    // node (the common case once its first add is in) needs no compare-and-swap
+    uint32_t old = *reinterpret_cast<volatile const uint32_t*>(&sh.key[h]);
+    if (old == GP_EMPTY) old = atomicCAS(&sh.key[h], GP_EMPTY, idx);
     if (old == GP_EMPTY || old == idx) {
       atomicAdd(&sh.val[h].x, v.x);
       atomicAdd(&sh.val[h].y, v.y);
