@@ -513,7 +513,8 @@ __device__ __forceinline__ void loadView(const HfbUniforms& U, HdView& V) {
 }
 
 // ---- batched: persistent over every instance ----
-__global__ void __launch_bounds__(HD_THREADS, 4) hairDepthBatch(BatchView b) {
+// 5 blocks per SM (48 registers): 1.33 ms against 1.40 at 4 on the 64-instance frame
+__global__ void __launch_bounds__(HD_THREADS, 5) hairDepthBatch(BatchView b) {
   __shared__ HdShared sh;
   __shared__ HdView V;
   const uint32_t n = b.hdr->n;
