@@ -410,7 +410,7 @@ __device__ __forceinline__ void hairDepthBigBody(const HdView& V, uint32_t P, co
 }
 
 template <bool WIN>
-__global__ void __launch_bounds__(HD_THREADS, 4)
+__global__ void __launch_bounds__(HD_THREADS, 5)
 hairDepthKernel(const HdView V, uint32_t P, uint32_t nPts, const float4* __restrict__ pos,
                 const float4* __restrict__ tan, const HdOut out, uint32_t* __restrict__ big, uint32_t bigCap) {
   __shared__ HdShared sh;
