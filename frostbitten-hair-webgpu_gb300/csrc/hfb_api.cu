@@ -109,6 +109,7 @@ int hfb_ctx_create(const HfbConfig* cfg, int device, HfbCtx** out) {
   if (e != cudaSuccess) { cudaStreamDestroy(c->ownStream); delete c; return HFB_ERR_OUT_OF_MEMORY; }
   cudaMemsetAsync(c->dCounters, 0, sizeof(hfb::DeviceCounters), c->stream);
   cudaStreamSynchronize(c->stream);
+  hfb::noallocPrepare(c);
   *out = c;
   return HFB_OK;
 }
@@ -150,7 +151,6 @@ int hfb_get_counters(HfbCtx* c, HfbCounters* out) {
   out->tileRecords = d.tileRecords;
   out->tileRecordsDropped = d.tileRecordsDropped;
   out->finePoolFullBins = d.finePoolFullBins;
-  out->waitTimeouts = d.waitTimeouts;
   out->launches = c->launches;
   out->fineSplitTiles = d.fineSplitTiles;
   out->fineSplitRedone = d.fineSplitRedone;

@@ -54,6 +54,11 @@ struct HfbCtx {
   uint64_t pipeGraphLaunches[2][2] = {};
   // self-checking build: the device CheckState (hfb_check.cuh), else NULL
   void* checkDev = nullptr;
+  // device address of hfb_tiles_pass_noalloc's fixed array on this
+  // context's device, looked up when the context is created (NULL if that
+  // failed; noallocError then says why)
+  void* noallocScratch = nullptr;
+  std::string noallocError;
 };
 
 namespace hfb {
@@ -63,7 +68,6 @@ struct DeviceCounters {
   unsigned long long tileRecords;
   unsigned long long tileRecordsDropped;
   unsigned long long finePoolFullBins;
-  unsigned long long waitTimeouts;
   unsigned long long fineSplitTiles;
   unsigned long long fineSplitRedone;
   unsigned long long badWorkItems;
@@ -178,6 +182,14 @@ enum FramePass : uint32_t {
 };
 cudaError_t framePass(HfbCtx* c, HfbInstance* in, FramePass p);
 cudaError_t clearRaster(HfbCtx* c, const HfbRasterBuffers& rb);
+
+// Looks up the device address of hfb_tiles_pass_noalloc's fixed array with
+// the context's device current (noalloc.cu), which also loads that code
+// onto the device and makes the array resident; called by hfb_ctx_create.
+// Sets c->noallocScratch, or c->noallocError on failure.
+void noallocPrepare(HfbCtx* c);
+// Loads the tiles pass's kernels onto the current device (raster.cu).
+cudaError_t tilesPassLoad(HfbCtx* c);
 
 // ---------------------------------------------------------------------------
 // Batched frames (hfb_frame_batch): every pass runs once for all instances.

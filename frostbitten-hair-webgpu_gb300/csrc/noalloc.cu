@@ -21,12 +21,20 @@
 //     the pass zeroes what must start at zero on every call, and two calls
 //     whose work overlaps on the GPU (different streams or contexts on the
 //     same device, without ordering between them) race on the array;
-//   - the first call on a device looks the array's device address up with
-//     that device current (cudaGetSymbolAddress) and caches it; make that
-//     first call before any stream capture;
+//   - the array's device address is looked up when a context is created
+//     (hfb_ctx_create, with the context's device current, through
+//     cudaGetSymbolAddress) and kept in the context.  CUDA loads a
+//     library's device code lazily, one source file at a time, so that
+//     lookup is also what loads this file's code onto the device and
+//     allocates the array: it happens once per device, inside
+//     hfb_ctx_create, never inside hfb_tiles_pass_noalloc.  The same set-up
+//     loads the tiles pass's kernels (a kernel's first launch would load
+//     its code, which takes device memory too).  A context keeps
+//     the address for its whole life; a device reset (cudaDeviceReset)
+//     invalidates every context anyway, and contexts created after it look
+//     the address up again;
 //   - the call allocates nothing: no cudaMalloc, no cudaFree, no allocating
 //     library routine.  The caller still passes every input and output.
-#include <mutex>
 #include <string>
 
 #define HFB_TU 6
@@ -37,36 +45,35 @@ namespace {
 // The tiles pass's working memory for hfb_tiles_pass_noalloc.
 static __device__ __align__(256) unsigned char g_tilesScratch[HFB_NOALLOC_SCRATCH_BYTES];
 
-constexpr int kMaxDevices = 128;
-std::mutex g_lock;
-void* g_scratchAddress[kMaxDevices] = {};  // device address of g_tilesScratch per device
-
 int fail(HfbCtx* c, int code, const std::string& msg) {
   c->lastError = msg;
   return code;
 }
 
-// Set-up, once per device, with that device current.
-int scratchAddress(HfbCtx* c, void** out) {
-  const int dev = c->device;
-  if (dev < 0 || dev >= kMaxDevices) return fail(c, HFB_ERR_INVALID_ARGUMENT, "device index out of range");
-  std::lock_guard<std::mutex> guard(g_lock);
-  if (g_scratchAddress[dev] == nullptr) {
-    int current = -1;
-    cudaError_t e = cudaGetDevice(&current);
-    if (e == cudaSuccess && current != dev) e = cudaSetDevice(dev);
-    void* p = nullptr;
-    if (e == cudaSuccess) e = cudaGetSymbolAddress(&p, g_tilesScratch);
-    if (current >= 0 && current != dev) cudaSetDevice(current);
-    if (e != cudaSuccess) {
-      return fail(c, HFB_ERR_CUDA, std::string("cudaGetSymbolAddress of the fixed tiles-pass array: ") +
-                                       cudaGetErrorString(e));
-    }
-    g_scratchAddress[dev] = p;
+}  // namespace
+
+namespace hfb {
+
+// Set-up at context creation, with the context's device current.
+void noallocPrepare(HfbCtx* c) {
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_tilesScratch);
+  // the pass's kernels too: their first launch would otherwise load them
+  if (e == cudaSuccess) e = tilesPassLoad(c);
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // not sticky: the context stays usable for every other pass
+    c->noallocScratch = nullptr;
+    c->noallocError = std::string("loading the fixed tiles-pass array and the tiles pass's kernels failed when "
+                                  "the context was created: ") + cudaGetErrorString(e);
+    return;
   }
-  *out = g_scratchAddress[dev];
-  return HFB_OK;
+  c->noallocScratch = p;
+  c->noallocError.clear();
 }
+
+}  // namespace hfb
+
+namespace {
 
 bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
 
@@ -94,9 +101,8 @@ extern "C" HFB_API int hfb_tiles_pass_noalloc(HfbCtx* c, const HfbUniforms* u, c
                     std::to_string(rb->width) + "x" + std::to_string(rb->height) +
                     "; the fixed array holds " + std::to_string((size_t)HFB_NOALLOC_SCRATCH_BYTES) +
                     ": use hfb_tiles_pass with HfbRasterBuffers.scratch");
-  void* scratch = nullptr;
-  int rc = scratchAddress(c, &scratch);
-  if (rc != HFB_OK) return rc;
+  void* scratch = c->noallocScratch;  // looked up by hfb_ctx_create
+  if (!scratch) return fail(c, HFB_ERR_CUDA, c->noallocError);
   HfbRasterBuffers r = *rb;
   r.scratch = scratch;
   r.scratchBytes = HFB_NOALLOC_SCRATCH_BYTES;

@@ -2049,6 +2049,26 @@ cudaError_t launchTilesPass(HfbCtx* c, const HfbUniforms& u, const HfbHairData& 
   return cudaGetLastError();
 }
 
+// Loads the tiles pass's kernels onto the current device and sets the
+// large-bins kernel's shared-memory attribute.  CUDA loads device code
+// lazily, at a kernel's first launch or attribute query, and loading takes
+// device memory for the code; hfb_tiles_pass_noalloc's set-up calls this at
+// context creation so that its own launches load (allocate) nothing.
+cudaError_t tilesPassLoad(HfbCtx* c) {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, tilesRasterKernel);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, binScanBlocks);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, binScanSums);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, binScatterKernel);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, binFinalizeKernel);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, largeBinsKernel);
+  if (e == cudaSuccess && !c->largeBinsAttrSet) {
+    e = cudaFuncSetAttribute(largeBinsKernel, cudaFuncAttributeMaxDynamicSharedMemorySize, LARGE_SMEM_KEYS * 4);
+    if (e == cudaSuccess) c->largeBinsAttrSet = true;
+  }
+  return e;
+}
+
 cudaError_t launchTileSort(HfbCtx* c, HfbRasterBuffers& rb) {
   HFB_CHECK_BIND(c);
   const HfbConfig& cfg = c->cfg;

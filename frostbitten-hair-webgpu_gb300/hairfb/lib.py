@@ -19,7 +19,6 @@ HFB_OK = 0
 HFB_ERR_INVALID_ARGUMENT = -1
 HFB_ERR_OUT_OF_MEMORY = -2
 HFB_ERR_CUDA = -3
-HFB_ERR_TIMEOUT = -5
 HFB_ERR_UNSUPPORTED = -6
 
 
@@ -59,13 +58,13 @@ class HfbInstance(ctypes.Structure):
 
 class HfbCounters(ctypes.Structure):
     _fields_ = [("tileRecords", ctypes.c_uint64), ("tileRecordsDropped", ctypes.c_uint64),
-                ("finePoolFullBins", ctypes.c_uint64), ("waitTimeouts", ctypes.c_uint64),
+                ("finePoolFullBins", ctypes.c_uint64),
                 ("launches", ctypes.c_uint64), ("fineSplitTiles", ctypes.c_uint64),
                 ("fineSplitRedone", ctypes.c_uint64), ("badWorkItems", ctypes.c_uint64)]
 
 
 assert ctypes.sizeof(HfbHairData) == 32
-assert ctypes.sizeof(HfbCounters) == 64
+assert ctypes.sizeof(HfbCounters) == 56
 assert ctypes.sizeof(HfbInstance) == 272
 
 # every symbol include/hairfb.h declares: name -> (restype, argtypes)

@@ -45,7 +45,6 @@ extern "C" {
 #define HFB_ERR_INVALID_ARGUMENT (-1)
 #define HFB_ERR_OUT_OF_MEMORY (-2)
 #define HFB_ERR_CUDA (-3)
-#define HFB_ERR_TIMEOUT (-5)
 #define HFB_ERR_UNSUPPORTED (-6)
 
 /* Pass constants the reference splices into its WGSL at pipeline creation
@@ -160,12 +159,14 @@ typedef struct HfbRasterBuffers {
   size_t scratchBytes;
 } HfbRasterBuffers;
 
-/* Counters accumulated over the context's lifetime (read with hfb_get_counters). */
+/* Counters accumulated over the context's lifetime (read with hfb_get_counters).
+ * No kernel of the library waits on another block, stream or rank (the
+ * persistent kernels take work from atomic counters and a split tile's last
+ * group merges it), so there is no device wait to time out or count. */
 typedef struct HfbCounters {
   uint64_t tileRecords;        /* (segment, tile) records attempted (sum of drawnSegmentsCount) */
   uint64_t tileRecordsDropped; /* records lost because the segment pool was full */
   uint64_t finePoolFullBins;   /* tile depth bins whose fragment pool filled (fine pass break) */
-  uint64_t waitTimeouts;       /* bounded device waits that gave up */
   uint64_t launches;           /* kernels launched by the library */
   uint64_t fineSplitTiles;     /* fine pass: tiles split into groups of depth bins across CTAs */
   uint64_t fineSplitRedone;    /* fine pass: split tiles redone in order (a later group could fill a pool) */
@@ -435,9 +436,11 @@ HFB_API int hfb_frame_batch_profile(HfbCtx* ctx, HfbInstance* instances, uint32_
  * by every GPU that loads it until exit; rb->scratch is ignored and may be
  * NULL.  Viewports needing more (hfb_raster_scratch_bytes) are rejected with
  * HFB_ERR_INVALID_ARGUMENT.  Calls share the array: calls whose work
- * overlaps on the GPU race.  The first call on a device looks the array up
- * (cudaGetSymbolAddress) and should come before any stream capture.  The
- * call allocates nothing. */
+ * overlaps on the GPU race.  hfb_ctx_create looks the array's address up
+ * (cudaGetSymbolAddress, with the context's device current) and loads the
+ * pass's kernels, which is when the array and the code take their device
+ * memory (CUDA loads device code lazily); the call itself allocates
+ * nothing. */
 #define HFB_NOALLOC_SCRATCH_BYTES (16u << 20)
 HFB_API int hfb_tiles_pass_noalloc(HfbCtx* ctx, const HfbUniforms* u, const HfbHairData* hair,
                                    const float* positions, const float* tangents, const float* depth,
