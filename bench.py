@@ -22,6 +22,7 @@ built with OpenMP, on all host threads -- on the same workload and metric.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -44,13 +45,18 @@ WORKLOADS = {
                  "1024^2}, own camera and own 32^3 sphere SDF each, 64^3 grids, 4 slices, 8 shading points, "
                  "7 iterations; tile size and depth bins autotuned over {8, 16, 32} x {4, 8, 16, 32}",
     # serving: Poisson arrivals, continuous batching under a memory budget
-    "served256": "256 sessions arriving as a Poisson process of 2,000/s, strands log-uniform [500, 50k] "
-                 "(8 levels), 32 points, square viewports of log-uniform area [256^2, 2048^2] (8 levels), "
-                 "600 frames each, 150 GB device-memory budget, 16 px tiles, 8 depth bins, 4 slices, "
-                 "8 shading points, 64^3 grids, 32^3 SDF",
+    "served256": "256 sessions (strands log-uniform [500, 50k] in 8 levels, 32 points, square viewports of "
+                 "log-uniform area [256^2, 2048^2] in 8 levels, own state resident on the device) asking for "
+                 "600 frames each as Poisson processes of 2,000 frame requests/s in total, 150 GB "
+                 "device-memory budget, 16 px tiles, 8 depth bins, 4 slices, 8 shading points, 64^3 grids, "
+                 "32^3 SDF; then a run of 60 frames per session under a budget of a quarter of their memory",
     # one full frame: 10k strands at 1080p
     "plain_full": "10,000 x 32 curly strands, 1920x1080, 16 px tiles, 16 depth bins, 4 slices, "
                   "16 shading points, 4 iterations, 64^3 SDF, 64^3 grids, sinusoidal wind",
+    # the same at the 32^3 grids the configuration names, each frame from rest
+    "plain_full_grid32": "10,000 x 32 curly strands, 1920x1080, 16 px tiles, 16 depth bins, 4 slices, "
+                         "16 shading points, 4 iterations, 64^3 SDF, 32^3 grids, sinusoidal wind; every frame "
+                         "from rest (the i32 density wraps at 32^3 within a few frames and the hair blows apart)",
     # the small case the reference also runs on a CPU adapter
     "plain_small": "2,000 x 16 strands, 640x480, 16 px tiles, 8 depth bins, 4 slices, 8 shading points",
     # the 4K stress frame: 200k strands
@@ -59,6 +65,11 @@ WORKLOADS = {
     "asset": "a TFX hair asset (+ binary SDF) at 1920x1080 with the reference's default CONFIG: 8 px tiles, "
              "32 depth bins, 8 slices, 64 shading points, 64^3 grids, 7 iterations",
 }
+
+
+# workloads whose every timed frame starts from the asset at rest: their
+# hair blows apart within a few frames on the reference's i32 density grid
+FROM_REST = ("stress", "plain_full_grid32")
 
 
 def parse():
@@ -76,6 +87,8 @@ def parse():
     ap.add_argument("--capture-frames", type=int, default=0,
                     help="profiler runs: set up the workload, render this many frames (batched64: batched "
                          "frames at --tile-size/--depth-bins, no tuning), print 'ok' and exit; no timing")
+    ap.add_argument("--capture-sessions", type=int, default=24,
+                    help="--capture-frames of served256: how many of its sessions the batch holds")
     ap.add_argument("--tfx", help="hair asset (TFX file) of the asset workload")
     ap.add_argument("--sdf", help="binary SDF of the asset workload's head (optional)")
     ap.add_argument("--tile-size", type=int, default=16)
@@ -90,12 +103,21 @@ def capture(args):
     import torch
     from hairfb import renderer as R
     from hairfb.lib import Context
-    if args.workload == "batched64":
-        insts = batched_instances(seed=0)
+    if args.workload in ("batched64", "served256"):
+        if args.workload == "batched64":
+            insts = batched_instances(seed=0)
+            pools = [None] * len(insts)
+        else:  # the first --capture-sessions sessions of the serving workload
+            from hairfb import serve
+            specs = serve.snap(serve.poisson_sessions(seed=0, count=256, rate_hz=2000.0, frames=600))
+            specs = specs[:args.capture_sessions]
+            fac = serve.SessionFactory(served_config(), seed=0)
+            insts = [fac(sp) for sp in specs]
+            pools = [serve.pool_records(sp) for sp in specs]
         cfg = dataclasses.replace(insts[0].cfg, tile_size=args.tile_size, tile_depth_bins=args.depth_bins)
         insts = [dataclasses.replace(i, cfg=cfg) for i in insts]
         ctx = Context(cfg.to_c(), 0)
-        rs = [R.Renderer(i, 0, ctx=ctx, hair_depth=True) for i in insts]
+        rs = [R.Renderer(i, 0, ctx=ctx, hair_depth=True, max_drawn=m) for i, m in zip(insts, pools)]
         for r in rs:
             r.before_first_frame()
         b = R.BatchRenderer(rs)
@@ -135,6 +157,8 @@ def make_instance(name, seed):
             with open(ASSET_FILES["sdf"], "rb") as f:
                 sdf = f.read()
         return synthetic.asset_instance(tfx, sdf)
+    if name == "plain_full_grid32":
+        return synthetic.plain_full(seed=seed, grid_dims=32)
     return getattr(synthetic, name)(seed=seed)
 
 
@@ -345,7 +369,7 @@ def run_ours(args, rank, world, dist):
     # reference's i32 fixed-point density within a few frames and the hair
     # blows apart (reference arithmetic, reproduced), so every frame there
     # starts from the asset at rest, reset outside the timed region
-    from_rest = args.workload == "stress"
+    from_rest = args.workload in FROM_REST
 
     def rest():
         if from_rest:
@@ -442,6 +466,59 @@ def read_records(r):
     return int(out[0])
 
 
+def e2e_frames(args, batch, stream):
+    """Frames through the public calls with host inputs and outputs: each
+    step is hfb_frame_batch (both uniform blocks of every instance go up
+    from host memory inside the call), then every instance's frame image
+    (hfb_present: the hair over a black scene, tone mapped to RGBA8, what the
+    reference presents) is copied into pinned host memory.  The copies run
+    on a stream of their own while the next frame renders, into two host
+    buffers used in turn; a frame's images are presented only once the
+    copies that last read their device buffers are done.  Returns (seconds
+    for --steps frames after --warmup, H2D bytes per step, D2H bytes per
+    step); the host waits for the last copy before the clock stops."""
+    import torch
+    from hairfb import uniforms as UN
+    from hairfb.lib import byref, ptr
+    # (context, renderers, stream) of each part of the batch
+    parts = [(b.ctx, b.renderers, b.ctx.stream_obj) for b in batch.batches] if hasattr(batch, "batches") \
+        else [(batch.ctx, batch.renderers, stream)]
+    rs = [r for _, prs, _ in parts for r in prs]
+    dev_img = [{id(r): torch.empty(r.inst.height * r.inst.width * 4, dtype=torch.uint8, device="cuda") for r in rs}
+               for _ in range(2)]
+    host_img = [[torch.empty(r.inst.height * r.inst.width * 4, dtype=torch.uint8).pin_memory() for r in rs]
+                for _ in range(2)]
+    ub = {id(r): ctypes.cast(ctypes.c_char_p(r.uniforms), ctypes.c_void_p) for r in rs}
+    copy_stream = torch.cuda.Stream()
+    copied = [None, None]
+    t0 = None
+    for k in range(args.warmup + args.steps):
+        if k == args.warmup:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+        slot = k & 1
+        batch.frame()
+        for pctx, prs, pst in parts:
+            if copied[slot] is not None:  # the copies of two frames ago read these device images
+                pst.wait_event(copied[slot])
+            for r in prs:
+                pctx.call("hfb_present", ub[id(r)], byref(r.rb.rb), None, ptr(dev_img[slot][id(r)]))
+            done = torch.cuda.Event()
+            done.record(pst)
+            copy_stream.wait_event(done)
+        with torch.cuda.stream(copy_stream):
+            for r, h in zip(rs, host_img[slot]):
+                h.copy_(dev_img[slot][id(r)], non_blocking=True)
+        copied[slot] = torch.cuda.Event()
+        copied[slot].record(copy_stream)
+    copy_stream.synchronize()
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    h2d = len(rs) * (UN.RENDER_UNIFORMS_BYTES + UN.SIM_UNIFORMS_BYTES)
+    d2h = sum(h.numel() for h in host_img[0])
+    return el, h2d, d2h
+
+
 def run_batched(args, rank, world, dist):
     import ctypes
     import torch
@@ -463,11 +540,19 @@ def run_batched(args, rank, world, dist):
         r.before_first_frame()
     torch.cuda.synchronize()
     t_tune = time.perf_counter()
-    cfg, ctx, trials = AT.tune(rs, base, dev, stream, budget_s=args.tune_budget)
+    tuned = AT.tune(rs, base, dev, stream, budget_s=args.tune_budget)
     t_tune = time.perf_counter() - t_tune
     ctx0.close()
-    batch = R.BatchRenderer(rs)
+    batch = tuned.batch
+    ctxs = tuned.ctxs
     ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+
+    def counters():
+        tot = {}
+        for c in ctxs:
+            for k, v in c.counters().items():
+                tot[k] = tot.get(k, 0) + v
+        return tot
 
     # ---- batched frames ----
     for _ in range(args.warmup):
@@ -475,7 +560,7 @@ def run_batched(args, rank, world, dist):
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    c0 = ctx.counters()
+    c0 = counters()
     # frames back to back (the host prepares the next frame while the GPU
     # renders); an event between frames gives each frame's GPU time
     evs = [ev() for _ in range(args.steps + 1)]
@@ -487,7 +572,7 @@ def run_batched(args, rank, world, dist):
             evs[k + 1].record(stream)
         torch.cuda.synchronize()
     step_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
-    c1 = ctx.counters()
+    c1 = counters()
     # latency: one frame submitted and waited for at a time (host work included)
     lat_ms = []
     for _ in range(args.steps):
@@ -498,105 +583,154 @@ def run_batched(args, rank, world, dist):
     launches = c1["launches"] - c0["launches"]
     dropped = c1["tileRecordsDropped"] - c0["tileRecordsDropped"]
 
-    # ---- the plain per-frame path: hfb_frame on one instance after another ----
-    for r in rs:
-        r.frame_native()
-    torch.cuda.synchronize()
-    plain_round_ms, plain_frame_ms = [], []
-    for _ in range(args.steps):
-        evs = [ev() for _ in range(n + 1)]
-        evs[0].record(stream)
-        for j, r in enumerate(rs):
-            r.frame_native()
-            evs[j + 1].record(stream)
-        torch.cuda.synchronize()
-        plain_round_ms.append(evs[0].elapsed_time(evs[n]))
-        plain_frame_ms += [evs[j].elapsed_time(evs[j + 1]) for j in range(n)]
-
-    # ---- per-pass times of one batched frame (plain launches + events) ----
-    arr = (HfbInstance * n)(*[r.instance() for r in rs])
+    # ---- per-pass times of one batched frame (plain launches + events; the
+    # parts of a split batch one after another, their times summed) ----
+    own_streams = [c.stream_obj for c in ctxs]
+    for c in ctxs:
+        c.set_stream(stream)
     names = ["grid_pre", "integrate", "grid_post", "clear", "tiles", "sort", "fine", "hair_depth", "shading"]
-    pm = (ctypes.c_float * len(names))()
-    ctx.call("hfb_frame_batch_profile", arr, n, pm)
-    for r, inst in zip(rs, arr):
-        r.after_native_frame(inst)
-    pass_ms = {k: float(pm[i]) for i, k in enumerate(names)}
+    pass_ms = {k: 0.0 for k in names}
+    for _, _, pctx, prs in tuned.parts:
+        arr = (HfbInstance * len(prs))(*[r.instance() for r in prs])
+        pm = (ctypes.c_float * len(names))()
+        pctx.call("hfb_frame_batch_profile", arr, len(prs), pm)
+        for r, inst in zip(prs, arr):
+            r.after_native_frame(inst)
+        for i, k in enumerate(names):
+            pass_ms[k] += float(pm[i])
     K = [read_records(r) for r in rs]
+    torch.cuda.synchronize()
+    for c, st in zip(ctxs, own_streams):  # back to the parts' own streams
+        c.set_stream(st)
 
-    # ---- e2e: the public call with host inputs, every image read back ----
-    imgs = [torch.empty(4 + 4 * i.width * i.height, dtype=torch.float32).pin_memory() for i in insts]
-    e2e_ms = []
-    for k in range(args.warmup + args.steps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        batch.frame()  # uniform blocks go up from host memory inside the call
-        for r, h in zip(rs, imgs):
-            ctx.call("hfb_buffer_download", h.data_ptr(), r.rb.rb.rasterizerResult, h.numel() * 4)
-        torch.cuda.synchronize()
-        if k >= args.warmup:
-            e2e_ms.append(1000.0 * (time.perf_counter() - t0))
-    from hairfb import uniforms as UN
-    h2d = n * (UN.RENDER_UNIFORMS_BYTES + UN.SIM_UNIFORMS_BYTES)
-    d2h = sum(h.numel() * 4 for h in imgs)
+    # ---- e2e: the public calls with host inputs, every frame's image read back ----
+    e2e_s, h2d, d2h = e2e_frames(args, batch, stream)
+    cfg_of = [r.cfg for r in rs]  # each instance's batched constants
+
+    # ---- the plain per-frame path: hfb_frame on one instance after another,
+    # all on one stream, at the pass constants fastest for it (its own
+    # choice among the batch's and two common ones) ----
+    from hairfb import autotune as AT2
+    plain_trials = []
+    plain_ctxs = []
+
+    def plain_round(nrounds):
+        rounds, frames = [], []
+        for _ in range(nrounds):
+            evs = [ev() for _ in range(n + 1)]
+            evs[0].record(stream)
+            for j, r in enumerate(rs):
+                r.frame_native()
+                evs[j + 1].record(stream)
+            torch.cuda.synchronize()
+            rounds.append(evs[0].elapsed_time(evs[n]))
+            frames += [evs[j].elapsed_time(evs[j + 1]) for j in range(n)]
+        return rounds, frames
+
+    for c in ctxs:
+        c.set_stream(stream)
+    plain_round(1)  # warm-up at the batch's constants
+    best_plain = (sum(plain_round(2)[0]) / 2, "batch's")
+    plain_trials.append({"constants": "batch's", "ms_per_round": round(best_plain[0], 3)})
+    chosen = None
+    for ts, b in ((8, 4), (16, 8), (16, 4)):
+        pcfg = AT2.candidate_config(base, ts, b)
+        pctx = Context(pcfg.to_c(), dev)
+        pctx.set_stream(stream)
+        plain_ctxs.append(pctx)
+        for r in rs:
+            r.use_config(pcfg, pctx)
+        plain_round(1)
+        ms = sum(plain_round(2)[0]) / 2
+        plain_trials.append({"tile_size": ts, "depth_bins": b, "ms_per_round": round(ms, 3)})
+        if ms < best_plain[0]:
+            best_plain = (ms, f"{ts} px, {b} bins")
+            chosen = (pcfg, pctx)
+    if chosen is None:  # the batch's own constants were fastest
+        for (_, pcfg, pctx, prs) in tuned.parts:
+            for r in prs:
+                r.use_config(pcfg, pctx)
+    else:
+        for r in rs:
+            r.use_config(*chosen)
+    plain_round(1)
+    plain_round_ms, plain_frame_ms = plain_round(args.steps)
+    torch.cuda.synchronize()
     served = None
     if args.serve_frames > 0 and world == 1:
-        served = run_served(args.serve_frames, dev, groups=getattr(ctx, "batch_groups", 1))
+        served = run_served(args.serve_frames, dev)
     out = dict(served=served, step_ms=step_ms, lat_ms=lat_ms, plain_round_ms=plain_round_ms, plain_frame_ms=plain_frame_ms,
-               pass_ms=pass_ms, K=K, e2e_ms=e2e_ms, h2d=h2d, d2h=d2h, clocks=clk.summary(), insts=insts,
-               cfg=cfg, trials=[t.as_dict() for t in trials], tune_s=t_tune, launches=launches,
-               groups=getattr(ctx, "batch_groups", 1), pipelined=getattr(ctx, "batch_pipeline", False),
-               dropped=dropped, n=n)
-    ctx.close()
+               pass_ms=pass_ms, K=K, e2e_s=e2e_s, h2d=h2d, d2h=d2h, clocks=clk.summary(), insts=insts,
+               cfg=tuned.cfg, cfg_of=cfg_of, tuned=tuned.describe(),
+               trials=[t.as_dict() for t in tuned.trials], tune_s=t_tune, launches=launches,
+               dropped=dropped, n=n, plain_trials=plain_trials, plain_constants=best_plain[1])
+    for c in ctxs + plain_ctxs:
+        c.close()
     return out
 
 
-def run_served(frames_per_session, device, groups=1, seed=0):
-    """The serving workload: sessions admitted under the memory budget, one
-    hfb_frame_batch call per tick over every admitted session.  Host assets
-    are generated before the clock starts (a server loads them)."""
+def served_config():
+    """Pass constants of the serving workload."""
+    from hairfb.config import HairConfig
+    return HairConfig(tile_size=16, tile_depth_bins=8, slices_per_pixel=4, shading_points=8, grid_dims=64)
+
+
+def run_served(frames_per_session, device, seed=0, rate_hz=2000.0, budget_bytes=150 << 30, session_rate_hz=2000.0,
+               lanes=2, tick_budget_ms=5.0, count=256):
+    """The serving workload: `count` sessions arriving as a Poisson process of
+    `session_rate_hz`, admitted under the memory budget; once its state is
+    on the device each session asks for `frames_per_session` frames as a
+    Poisson process of rate_hz / count (rate_hz in total when every
+    session is active); ticks of the oldest requests run on `lanes`
+    contexts.  Host assets are generated before the clock starts (a server
+    loads them)."""
     import torch
     from hairfb import serve
-    from hairfb.config import HairConfig
-    cfg = HairConfig(tile_size=16, tile_depth_bins=8, slices_per_pixel=4, shading_points=8, grid_dims=64)
-    specs = serve.snap(serve.poisson_sessions(seed=seed, count=256, rate_hz=2000.0, frames=frames_per_session))
+    cfg = served_config()
+    specs = serve.snap(serve.poisson_sessions(seed=seed, count=count, rate_hz=session_rate_hz,
+                                              frames=frames_per_session))
     factory = serve.SessionFactory(cfg, seed=seed)
     t0 = time.perf_counter()
     factory.prepare(specs)
     prep_s = time.perf_counter() - t0
-    server = serve.Server(cfg, device, budget_bytes=150 << 30, groups=groups, make_instance=factory)
+    server = serve.Server(cfg, device, budget_bytes=budget_bytes, lanes=lanes, tick_budget_ms=tick_budget_ms,
+                          make_instance=factory)
     torch.cuda.synchronize()
-    st = server.run(specs)
+    st = server.run(specs, rate_hz=rate_hz, seed=seed)
     server.close()
     torch.cuda.empty_cache()
-    return {"frames_per_s": st.frames_per_s, "frames": st.frames, "wall_s": st.wall_s, "ticks": st.ticks,
-            "frame_p50_ms": st.pct(0.5), "frame_p99_ms": st.pct(0.99),
+    return {"frames_per_s": st.frames_per_s, "offered_frames_per_s": st.offered_hz, "frames": st.frames,
+            "wall_s": st.wall_s, "ticks": st.ticks, "frames_per_tick": round(st.frames_per_tick, 2),
+            "lanes": st.lanes, "tick_budget_ms": tick_budget_ms,
+            "request_p50_ms": st.pct(0.5), "request_p99_ms": st.pct(0.99), "request_max_ms": st.pct(1.0),
+            "tick_gpu_p50_ms": st.pct(0.5, "tick_gpu_ms"), "tick_gpu_p99_ms": st.pct(0.99, "tick_gpu_ms"),
             "admit_wait_p50_ms": st.pct(0.5, "admit_wait_ms"), "admit_wait_p99_ms": st.pct(0.99, "admit_wait_ms"),
             "peak_sessions": st.peak_sessions, "peak_bytes": st.peak_bytes, "budget_bytes": st.budget_bytes,
             "records_dropped": st.dropped, "frames_per_session": frames_per_session, "sessions": len(specs),
             "host_asset_prep_s": round(prep_s, 1),
-            "note": "frames/s over the wall clock from the first arrival to the last frame (admission, uploads "
-                    "and first-frame setup included); frame latency = the tick that rendered the frame"}
+            "note": "latency per frame request, from its arrival to the host seeing its frame complete; "
+                    "frames/s from the first request to the last frame"}
 
 
 def report_batched_peer(res, dist):
     """Non-zero ranks join the max-over-ranks reduction of report_batched."""
     from hairfb import replicas
     replicas.max_over_ranks([sum(res["step_ms"]) / 1000.0, sum(res["plain_round_ms"]) / 1000.0,
-                             sum(res["e2e_ms"]) / 1000.0], dist, "cuda")
+                             res["e2e_s"]], dist, "cuda")
 
 
 def cpu_batched(insts, seconds):
     """Instance frames/s of the restated reference on the host, on a bounded
-    sample: the instances in order, one frame each, for ~`seconds`."""
-    frames = [cpu_frame_runner(i) for i in insts[:8]]
-    for f in frames:
-        f()  # warm-up
+    sample: every instance in order, one frame each, for ~`seconds` (at
+    least one frame of each of them)."""
+    frames = [cpu_frame_runner(i) for i in insts]
+    frames[0]()  # warm-up (page-in, thread pool)
     k, t0 = 0, time.perf_counter()
     while True:
         frames[k % len(frames)]()
         k += 1
         el = time.perf_counter() - t0
-        if el >= seconds:
+        if el >= seconds and k >= len(frames):
             return k, el
 
 
@@ -605,14 +739,14 @@ def report_batched(args, res, world, dist):
     from hairfb import autotune as AT  # noqa: F401
     step_s = sum(res["step_ms"]) / 1000.0
     plain_s = sum(res["plain_round_ms"]) / 1000.0
-    e2e_s = sum(res["e2e_ms"]) / 1000.0
+    e2e_s = res["e2e_s"]
     from hairfb import replicas
     step_s, plain_s, e2e_s = replicas.max_over_ranks([step_s, plain_s, e2e_s], dist, "cuda")
     n = res["n"]
     fps = replicas.job_throughput(n * len(res["step_ms"]), world, step_s)
     plain_fps = replicas.job_throughput(n * len(res["plain_round_ms"]), world, plain_s)
     cfg = res["cfg"]
-    insts = [dataclasses.replace(i, cfg=cfg) for i in res["insts"]]
+    insts = [dataclasses.replace(i, cfg=c) for i, c in zip(res["insts"], res["cfg_of"])]
     alg = {}
     for inst, k in zip(insts, res["K"]):
         for key, v in algorithmic_bytes(inst, k).items():
@@ -631,7 +765,8 @@ def report_batched(args, res, world, dist):
         # measured at one pass config; the raster passes' figure is reported only
         # when the tuner chose that config, the simulation's does not depend on it
         tj = json.load(open(tp))
-        traffic = tj.get(f"batched64:ts{cfg.tile_size}_b{cfg.tile_depth_bins}:{dominant}")
+        traffic = tj.get(f"batched64:ts{cfg.tile_size}_b{cfg.tile_depth_bins}:{dominant}") \
+            if len(res["tuned"]["parts"]) == 1 else None
         if traffic is None and dominant in ("grid_pre", "integrate", "grid_post"):
             traffic = next((v for k, v in tj.items() if k.startswith("batched64:") and k.endswith(":" + dominant)),
                            None)
@@ -644,8 +779,8 @@ def report_batched(args, res, world, dist):
     if not args.no_cpu_baseline:
         k, el = cpu_batched(res["insts"], args.cpu_seconds)
         cpu = {"value": k / el, "unit": "frames/s", "cores": host_threads(), "kind": "port",
-               "sample": f"{k} instance frames (the first 8 instances in turn) on the host, C restatement of "
-                         f"the reference WGSL with OpenMP, {el:.1f} s"}
+               "sample": f"{k} instance frames (all {len(res['insts'])} instances in turn) on the host, C "
+                         f"restatement of the reference WGSL with OpenMP, {el:.1f} s"}
     line = {
         "metric": "frames/s", "value": fps, "unit": "frames/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1000.0 / len(res["step_ms"]),
@@ -654,14 +789,11 @@ def report_batched(args, res, world, dist):
         "config": {"workload": "batched64", "describe": WORKLOADS["batched64"],
                    "step": f"one batched frame of all {n} instances (hfb_frame_batch, captured CUDA graph)",
                    "l2": "inputs larger than L2 (all instances' positions, grids and buffers ~ several GB)",
-                   "frames_per_step": n, "tuned": {"tile_size": cfg.tile_size, "depth_bins": cfg.tile_depth_bins,
-                                                   "slices": cfg.slices_per_pixel,
-                                                   "avg_segments_per_tile": cfg.avg_segments_per_tile,
-                                                   "groups": res["groups"], "pipelined": res["pipelined"],
-                                                   "tune_s": round(res["tune_s"], 1)},
+                   "frames_per_step": n, "tuned": dict(res["tuned"], tune_s=round(res["tune_s"], 1)),
                    "autotune_trials": [{k: (round(v, 3) if isinstance(v, float) else v) for k, v in t.items()}
                                        for t in res["trials"]],
                    "plain_frames_per_s": plain_fps, "batched_over_plain": fps / plain_fps,
+                   "plain_constants": res["plain_constants"], "plain_trials": res["plain_trials"],
                    "p50_ms": q(srt, 0.5), "p99_ms": q(srt, 0.99),
                    "latency_p50_ms": q(sorted(res["lat_ms"]), 0.5), "latency_p99_ms": q(sorted(res["lat_ms"]), 0.99),
                    "plain_frame_p50_ms": q(psrt, 0.5), "plain_frame_p99_ms": q(psrt, 0.99),
@@ -671,8 +803,11 @@ def report_batched(args, res, world, dist):
                    "step_algorithmic_bytes": frame_bytes,
                    "served": res["served"],
                    "step_hbm_roofline_frac": frame_bytes * (fps / n) / world / (peak * 1e9)},
-        "e2e": {"value": world * n * len(res["e2e_ms"]) / e2e_s, "unit": "frames/s",
-                "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"]},
+        "e2e": {"value": world * n * args.steps / e2e_s, "unit": "frames/s",
+                "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"],
+                "what": "hfb_frame_batch with both uniform blocks of every instance from host memory, then every "
+                        "instance's presented RGBA8 image (hfb_present) copied to pinned host memory on a copy "
+                        "stream overlapping the next frame; host clock over the steps, last copy included"},
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
                      "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                      "algorithmic_bytes": alg[dominant]},
@@ -709,33 +844,40 @@ def main():
         capture(args)
         return
     if args.impl == "reference" and wl == "batched64":
+        # the same step as the GPU arm: one frame of every one of the 64
+        # instances, W warm-up steps, then K timed steps
         insts = batched_instances(seed=0)
+        n = len(insts)
         frames = [cpu_frame_runner(i) for i in insts]
-        w = max(1, min(args.warmup, 3))
-        for k in range(w):
-            frames[k % len(frames)]()
+        for _ in range(args.warmup):
+            for f in frames:
+                f()
         t0 = time.perf_counter()
-        for k in range(args.steps):
-            frames[k % len(frames)]()
+        for _ in range(args.steps):
+            for f in frames:
+                f()
         el = time.perf_counter() - t0
-        fps = args.steps / el
+        fps = n * args.steps / el
         line = {
             "impl": "reference", "metric": "frames/s", "value": fps, "unit": "frames/s",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": w, "ms_per_step": 1000.0 * el / args.steps,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * el / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic",
+            "data": "synthetic (seeded; no public dataset exists for this path)",
             "config": {"workload": wl, "describe": WORKLOADS[wl],
-                       "step": "one instance frame, the instances in turn",
-                       "implementation": "C restatement of the reference WGSL passes, OpenMP"},
+                       "step": f"one frame of every one of the {n} instances",
+                       "frames_per_step": n,
+                       "implementation": "C restatement of the reference WGSL passes, OpenMP, at the workload's "
+                                         "pass constants (16 px tiles, 8 depth bins, 4 slices)"},
             "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": host_threads(), "kind": "port",
-                             "sample": f"{args.steps} instance frames (instances 0..{args.steps - 1} mod 64)"},
+                             "sample": f"{args.steps} steps x {n} instance frames (every instance once per step) "
+                                       f"after {args.warmup} warm-up steps, {el:.1f} s"},
             "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }
         print(json.dumps(line), flush=True)
         return
     if args.impl == "reference":
         inst = make_instance(wl, seed=0)
-        frame = cpu_frame_runner(inst, from_rest=wl == "stress")
+        frame = cpu_frame_runner(inst, from_rest=wl in FROM_REST)
         for _ in range(max(1, min(args.warmup, 3))):
             frame()
         t0 = time.perf_counter()
@@ -763,7 +905,11 @@ def main():
         import torch
         dev = int(os.environ.get("LOCAL_RANK", "0"))
         torch.cuda.set_device(dev)
-        sv = run_served(600, dev, groups=4, seed=rank)
+        sv = run_served(600, dev, seed=rank)
+        # the same sessions under a budget that binds: a quarter of what all
+        # 256 need, sessions arriving over 4 s, 60 frames each
+        sv["budget_binding"] = run_served(60, dev, seed=rank, budget_bytes=sv["peak_bytes"] // 4,
+                                          session_rate_hz=64.0)
         from hairfb import replicas
         sv["wall_s"] = replicas.max_over_ranks([sv["wall_s"]], dist, "cuda")[0]
         if rank == 0:
@@ -773,7 +919,8 @@ def main():
                     "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                     "data": "synthetic (seeded Poisson sessions; no public dataset exists for this path)",
                     "config": {"workload": wl, "describe": WORKLOADS[wl], "served": sv,
-                               "step": "one tick: every admitted session's next frame (hfb_frame_batch)"},
+                               "step": "one tick: the oldest pending frame requests, one per session, "
+                                       "within the tick's GPU-time budget (hfb_frame_batch)"},
                     "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
                     "roofline": None, "cpu_baseline": None, "gpu_launches": None}
             print(json.dumps(line), flush=True)
@@ -830,11 +977,11 @@ def main():
 
     cpu = None
     if not args.no_cpu_baseline:
-        n, el = time_cpu(inst, args.cpu_seconds, from_rest=wl == "stress")
+        n, el = time_cpu(inst, args.cpu_seconds, from_rest=wl in FROM_REST)
         cpu = {"value": n / el, "unit": "frames/s", "cores": host_threads(), "kind": "port",
                "sample": f"{n} full frames of {wl} on the host (C restatement of the reference "
                          f"WGSL, OpenMP) after 1 warm-up frame, {el:.1f} s"
-                         + (", each from the asset at rest" if wl == "stress" else "")}
+                         + (", each from the asset at rest" if wl in FROM_REST else "")}
 
     line = {
         "metric": "frames/s", "value": fps, "unit": "frames/s", "n_gpus": world,
@@ -849,7 +996,7 @@ def main():
                    **({"frames": "each timed frame starts from the asset at rest (positions, grids and the "
                                  "first-frame setup reset before it, outside the timed region): the hair blows "
                                  "apart after a few frames on the reference's i32 density arithmetic"}
-                      if wl == "stress" else {})},
+                      if wl in FROM_REST else {})},
         "e2e": {"value": world * len(res["e2e_ms"]) / e2e_total, "unit": "frames/s",
                 "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"]},
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,

@@ -95,14 +95,23 @@ struct FineScratch {
 };
 uint32_t maxDrawnSegments(const HfbConfig& cfg, uint32_t W, uint32_t H);
 
-// Strands per integration block for P points per strand: 1024 / P (at least
-// 8), so a block's 256 threads take four points each in the point phases and
-// its staging stays near 38 KB (64 strands of 16 points, 32 of 32).
+// Strands per integration block for P points per strand: 2048 / P, between
+// 8 and 128, so a block's 128 threads take sixteen points each in the point
+// phases and its staging (the points only) stays near 34 KB: 64 strands of
+// 32 points, 128 of 16.
 __host__ __device__ inline uint32_t simStrandsPerBlock(uint32_t P) {
-  return 1024u / P > 8u ? 1024u / P : 8u;
+  const uint32_t n = 2048u / P;
+  return n > 128u ? 128u : n < 8u ? 8u : n;
+}
+// The same for one instance launched alone (hfb_sim_integrate, hfb_frame):
+// fewer strands per block (at least 8) while that gives up to two blocks per SM.
+__host__ __device__ inline uint32_t simStrandsPerBlockFor(uint32_t S, uint32_t P, uint32_t smCount) {
+  const uint32_t full = simStrandsPerBlock(P);
+  const uint32_t want = (S + 2u * smCount - 1u) / (2u * smCount);  // strands per block for 2 blocks per SM
+  return want >= full ? full : want < 8u ? 8u : want;
 }
 __host__ __device__ inline size_t simSmemBytes(uint32_t P) {
-  return (size_t)simStrandsPerBlock(P) * (P + 1u) * (2u * sizeof(float4) + sizeof(float)) + (size_t)P * 4u;
+  return (size_t)simStrandsPerBlock(P) * (P + 1u) * sizeof(float4) + (size_t)P * 4u;
 }
 constexpr uint32_t TILES_RASTER_SEGS = 128;  // segments per tiles-raster block
 

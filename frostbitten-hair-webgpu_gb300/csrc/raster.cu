@@ -365,13 +365,20 @@ __device__ __forceinline__ void tilesRasterBody(const HfbUniforms& U, uint32_t P
       uint32_t p = c0 + tid * per;
       const uint32_t pEnd = min(p + per, c0 + n);
       uint32_t k = 0, rx = 0, ry = 0, w = 1, x0 = 0, y0 = 0;
-      float eox[4], eoy[4], eex[4], eey[4];
+      // edgeFunction (swRasterizeHair.wgsl.ts:128-130) is (x - ox) * ey - (y - oy) * ex: the
+      // second product is the same along a row and is formed once per row (the same values)
+      float eox[4], eey[4], rowT[4];
       auto loadSeg = [&](uint32_t kk) {
         x0 = sh.cx0[kk]; y0 = sh.cy0[kk]; w = sh.cw[kk];
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-          eox[i] = sh.ox[i][kk]; eoy[i] = sh.oy[i][kk]; eex[i] = sh.ex[i][kk]; eey[i] = sh.ey[i][kk];
+          eox[i] = sh.ox[i][kk]; eey[i] = sh.ey[i][kk];
         }
+      };
+      auto setRow = [&]() {
+        const float py = (float)(y0 + ry);
+#pragma unroll
+        for (int i = 0; i < 4; i++) rowT[i] = fmul(fsub(py, sh.oy[i][k]), sh.ex[i][k]);
       };
       if (p < pEnd) {
         uint32_t lo = 0, hi = TR_SEGS;  // last k with pairBase[k] <= p
@@ -384,16 +391,17 @@ __device__ __forceinline__ void tilesRasterBody(const HfbUniforms& U, uint32_t P
         const uint32_t r = p - sh.pairBase[k];
         ry = r / w;
         rx = r - ry * w;
+        setRow();
       }
       for (uint32_t it = 0; it < per; it++) {
         const bool valid = p < pEnd;
         bool pass = false;
         if (valid) {
-          const f2 pf = mk2((float)(x0 + rx), (float)(y0 + ry));
+          const float px = (float)(x0 + rx);
           pass = true;
 #pragma unroll
-          for (int i = 0; i < 4; i++) {  // edgeFunction, swRasterizeHair.wgsl.ts:128-130
-            const float C = fsub(fmul(fsub(pf.x, eox[i]), eey[i]), fmul(fsub(pf.y, eoy[i]), eex[i]));
+          for (int i = 0; i < 4; i++) {  // edgeFunction >= 0
+            const float C = fsub(fmul(fsub(px, eox[i]), eey[i]), rowT[i]);
             pass = pass && C >= 0.0f;
           }
         }
@@ -416,6 +424,7 @@ __device__ __forceinline__ void tilesRasterBody(const HfbUniforms& U, uint32_t P
               loadSeg(k);
               ry = 0;
             }
+            if (p < pEnd) setRow();
           }
         }
       }
@@ -842,10 +851,24 @@ template <> struct FineDims<8> { static constexpr uint32_t STAGE = 64, PAIRS = 7
 template <> struct FineDims<16> { static constexpr uint32_t STAGE = 96, PAIRS = 2048; };
 template <> struct FineDims<32> { static constexpr uint32_t STAGE = 256, PAIRS = 4096; };
 
+// Shared inputs of the fine pass.
+struct FineArgs {
+  uint32_t S, P, B, L, SP, CAP, alphaQuadratic;
+  float alphaMul;
+  const float4* __restrict__ pos;
+  const float4* __restrict__ tan;
+  const float4* __restrict__ shading;
+  const float* __restrict__ depth;
+  const uint4* __restrict__ tiles;
+  const uint32_t* __restrict__ segBuf;
+  DeviceCounters* counters;
+};
+
 template <int TS>
 struct FineSmem {
   static constexpr uint32_t NT = TS * TS, STAGE = FineDims<TS>::STAGE, PAIRS = FineDims<TS>::PAIRS;
   static_assert(PAIRS >= NT, "a segment box covers up to TS*TS pairs");
+  static_assert(2 * 6 * STAGE * sizeof(float) <= PAIRS * sizeof(uint2), "stagePoint's scratch fits in frag");
   float4 shade[STAGE][NSHADE];   // the shading entries each staged segment can sample
   uint2 frag[PAIRS];             // A1: pixel | segment << 16 of a passing pair; A2: its colour as 4 x f16
   uint32_t pairInfo[PAIRS];      // per pair: fragment index | slice << 16, or PAIR_NONE
@@ -863,12 +886,16 @@ struct FineSmem {
   uint32_t pixMask[STAGE / 32][NT];  // bit k of pixel p: staged segment k left a fragment at p
   // the tile
   uint4 head[64];                    // HairTileResult per depth bin
+  float td0[64], td1[64];            // its depth range (_getTileDepth), for the slices of its fragments
   uint32_t binOff[65];               // tile mode: first entry of each bin in the tile's sequence
   float zbuf[NT];
   uint32_t doneMask[NT / 32];
   // the round
   uint32_t runBin[MAX_RUNS], runK0[MAX_RUNS], runK1[MAX_RUNS], runOff[MAX_RUNS];
   uint32_t red[32];
+  // the work item's instance (written by one thread per item): read where used, so that none of
+  // it stays in registers across the tile's rounds
+  FineArgs args;
   uint32_t nRuns, nStaged, nSeg, passCount, queueIdx, bad, tileMode, total, walkNext;
   uint32_t mode, cutSeg, cutSlots, roundFrags, e0, eLast, arrive;
 };
@@ -903,61 +930,133 @@ __device__ __forceinline__ uint32_t blockExclusive(uint32_t v, uint32_t* red, ui
   return pre + x - v;
 }
 
-// Projects staged segment k: edge-test constants, depths, the pixel-
-// independent part of interpolateHairQuad, the tile-local box of the pixels
-// that can pass the edge tests ([floor(min), ceil(max)] of the vertices), and
-// the shading entries its fragments can sample (tFull is monotonic in the
-// segment coordinate, so they are [i0(t = 0), i1(t = 1)]).  Returns the
-// box area.
+// The shading entries staged segment (st, sg) can sample (tFull is
+// monotonic in the segment coordinate, so they are [i0(t = 0), i1(t = 1)],
+// at most NSHADE of them): loads them into sh.shade[k], returns
+// first | count << 16.
 template <int TS>
-__device__ __forceinline__ uint32_t stageSegment(FineSmem<TS>& sh, uint32_t k, uint32_t bin, const HfbUniforms& U,
-                                                 const float4* __restrict__ pos, const float4* __restrict__ tan,
-                                                 const float4* __restrict__ shading, uint32_t S, uint32_t P,
-                                                 uint32_t SP, f2 size, uint32_t x0, uint32_t y0) {
-  const uint32_t st = sh.strand[k], sg = sh.segIdx[k];
+__device__ __forceinline__ uint32_t stageShade(FineSmem<TS>& sh, uint32_t k, uint32_t st, uint32_t sg,
+                                               const float4* __restrict__ shading, uint32_t P, uint32_t SP) {
+  uint32_t a0, a1, b0, b1;
+  remapToIndices(SP, fadd((float)sg, 0.0f) / (float)(P - 1u), a0, a1);
+  remapToIndices(SP, fadd((float)sg, 1.0f) / (float)(P - 1u), b0, b1);
+  const uint32_t ne = min(b1 - a0 + 1u, NSHADE);
+  const size_t sb = (size_t)st * SP;
+  for (uint32_t j = 0; j < ne; j++) sh.shade[k][j] = __ldg(HFB_G(&shading[sb + a0 + j]));
+  return a0 | (ne << 16);
+}
+
+// Staged segment k from its projection s: edge-test constants, depths, the
+// pixel-independent part of interpolateHairQuad, and the tile-local box of
+// the pixels that can pass the edge tests ([floor(min), ceil(max)] of the
+// vertices).  shade: first | count << 16 of its staged shading entries
+// (stageShade).  Returns the box area.
+template <int TS>
+__device__ __forceinline__ uint32_t stageFromProjection(FineSmem<TS>& sh, uint32_t k, uint32_t bin, const ProjSeg& s,
+                                                        uint32_t shade, uint32_t x0, uint32_t y0) {
   uint32_t box = EMPTY_BOX, area = 0, shadeBase = bin << 24;
-  if (st < S && sg + 1u < P) {  // otherwise not a segment of this hair: covers no pixel
-    const ProjSeg s = projectSegment(U, pos, tan, P, st, sg, size);
-    float mnx = floorf(fminf(fminf(s.v00.x, s.v01.x), fminf(s.v10.x, s.v11.x))) - (float)x0;
-    float mny = floorf(fminf(fminf(s.v00.y, s.v01.y), fminf(s.v10.y, s.v11.y))) - (float)y0;
-    float mxx = ceilf(fmaxf(fmaxf(s.v00.x, s.v01.x), fmaxf(s.v10.x, s.v11.x))) - (float)x0;
-    float mxy = ceilf(fmaxf(fmaxf(s.v00.y, s.v01.y), fmaxf(s.v10.y, s.v11.y))) - (float)y0;
-    if (mnx <= mxx && mny <= mxy && mxx >= 0.0f && mxy >= 0.0f && mnx <= (float)(TS - 1) && mny <= (float)(TS - 1)) {
-      const uint32_t bx0 = (uint32_t)fmaxf(mnx, 0.0f), by0 = (uint32_t)fmaxf(mny, 0.0f);
-      const uint32_t bx1 = (uint32_t)fminf(mxx, (float)(TS - 1)), by1 = (uint32_t)fminf(mxy, (float)(TS - 1));
-      box = bx0 | (by0 << 8) | (bx1 << 16) | (by1 << 24);
-      area = (bx1 - bx0 + 1u) * (by1 - by0 + 1u);
-      // edge tests in the order insideQuad evaluates them
-      const f2 o[4] = {s.v01, s.v11, s.v10, s.v00};
-      const f2 e[4] = {s.v00, s.v01, s.v11, s.v10};
+  float mnx = floorf(fminf(fminf(s.v00.x, s.v01.x), fminf(s.v10.x, s.v11.x))) - (float)x0;
+  float mny = floorf(fminf(fminf(s.v00.y, s.v01.y), fminf(s.v10.y, s.v11.y))) - (float)y0;
+  float mxx = ceilf(fmaxf(fmaxf(s.v00.x, s.v01.x), fmaxf(s.v10.x, s.v11.x))) - (float)x0;
+  float mxy = ceilf(fmaxf(fmaxf(s.v00.y, s.v01.y), fmaxf(s.v10.y, s.v11.y))) - (float)y0;
+  if (mnx <= mxx && mny <= mxy && mxx >= 0.0f && mxy >= 0.0f && mnx <= (float)(TS - 1) && mny <= (float)(TS - 1)) {
+    const uint32_t bx0 = (uint32_t)fmaxf(mnx, 0.0f), by0 = (uint32_t)fmaxf(mny, 0.0f);
+    const uint32_t bx1 = (uint32_t)fminf(mxx, (float)(TS - 1)), by1 = (uint32_t)fminf(mxy, (float)(TS - 1));
+    box = bx0 | (by0 << 8) | (bx1 << 16) | (by1 << 24);
+    area = (bx1 - bx0 + 1u) * (by1 - by0 + 1u);
+    // edge tests in the order insideQuad evaluates them
+    const f2 o[4] = {s.v01, s.v11, s.v10, s.v00};
+    const f2 e[4] = {s.v00, s.v01, s.v11, s.v10};
 #pragma unroll
-      for (int i = 0; i < 4; i++) {
-        sh.ox[i][k] = o[i].x;
-        sh.oy[i][k] = o[i].y;
-        sh.ex[i][k] = fsub(e[i].x, o[i].x);
-        sh.ey[i][k] = fsub(e[i].y, o[i].y);
-      }
-      sh.dp[0][k] = s.depthsProj.x;
-      sh.dp[1][k] = s.depthsProj.y;
-      sh.dp[2][k] = s.depthsProj.z;
-      sh.dp[3][k] = s.depthsProj.w;
-      const QuadConst q = quadConst(s);
-      sh.qsx[k] = q.sm.x; sh.qsy[k] = q.sm.y; sh.qax[k] = q.ab.x; sh.qay[k] = q.ab.y;
-      sh.qd2[k] = q.d2; sh.qlse[k] = q.lse; sh.qws[k] = q.wS; sh.qwe[k] = q.wE; sh.qd22[k] = q.d22;
-      uint32_t a0, a1, b0, b1;
-      remapToIndices(SP, fadd((float)sg, 0.0f) / (float)(P - 1u), a0, a1);
-      remapToIndices(SP, fadd((float)sg, 1.0f) / (float)(P - 1u), b0, b1);
-      const uint32_t ne = min(b1 - a0 + 1u, NSHADE);
-      const size_t sb = (size_t)st * SP;
-      for (uint32_t j = 0; j < ne; j++) sh.shade[k][j] = __ldg(HFB_G(&shading[sb + a0 + j]));
-      shadeBase |= a0 | (ne << 16);
+    for (int i = 0; i < 4; i++) {
+      sh.ox[i][k] = o[i].x;
+      sh.oy[i][k] = o[i].y;
+      sh.ex[i][k] = fsub(e[i].x, o[i].x);
+      sh.ey[i][k] = fsub(e[i].y, o[i].y);
     }
+    sh.dp[0][k] = s.depthsProj.x;
+    sh.dp[1][k] = s.depthsProj.y;
+    sh.dp[2][k] = s.depthsProj.z;
+    sh.dp[3][k] = s.depthsProj.w;
+    const QuadConst q = quadConst(s);
+    sh.qsx[k] = q.sm.x; sh.qsy[k] = q.sm.y; sh.qax[k] = q.ab.x; sh.qay[k] = q.ab.y;
+    sh.qd2[k] = q.d2; sh.qlse[k] = q.lse; sh.qws[k] = q.wS; sh.qwe[k] = q.wE; sh.qd22[k] = q.d22;
+    shadeBase |= shade;
   }
   sh.box[k] = box;
   sh.shadeBase[k] = shadeBase;
   sh.cntEdge[k] = 0;
   sh.cntFrag[k] = 0;
   return area;
+}
+
+// Projects staged segment k (both points, projectSegment) and stages it.
+template <int TS>
+__device__ __forceinline__ uint32_t stageSegment(FineSmem<TS>& sh, uint32_t k, uint32_t bin, const HfbUniforms& U,
+                                                 const float4* __restrict__ pos, const float4* __restrict__ tan,
+                                                 const float4* __restrict__ shading, uint32_t S, uint32_t P,
+                                                 uint32_t SP, f2 size, uint32_t x0, uint32_t y0) {
+  const uint32_t st = sh.strand[k], sg = sh.segIdx[k];
+  if (st < S && sg + 1u < P) {  // otherwise not a segment of this hair: covers no pixel
+    const ProjSeg s = projectSegment(U, pos, tan, P, st, sg, size);
+    return stageFromProjection<TS>(sh, k, bin, s, stageShade<TS>(sh, k, st, sg, shading, P, SP), x0, y0);
+  }
+  sh.box[k] = EMPTY_BOX;
+  sh.shadeBase[k] = bin << 24;
+  sh.cntEdge[k] = 0;
+  sh.cntFrag[k] = 0;
+  return 0u;
+}
+
+// With two threads per staged segment: thread `end` of segment k projects
+// point sg + end of it (projectHairPoint) into the round's point scratch
+// (the fragment list's storage, free until the edge tests); the end-point
+// thread also stages the segment's shading entries.
+template <int TS>
+__device__ __forceinline__ void stagePoint(FineSmem<TS>& sh, uint32_t k, uint32_t end, const HfbUniforms& U,
+                                           const float4* __restrict__ pos, const float4* __restrict__ tan,
+                                           const float4* __restrict__ shading, uint32_t S, uint32_t P, uint32_t SP,
+                                           f2 size) {
+  constexpr uint32_t STAGE = FineSmem<TS>::STAGE;
+  float* pt = reinterpret_cast<float*>(sh.frag) + end * 6u * STAGE;  // [6][STAGE] per end
+  const uint32_t st = sh.strand[k], sg = sh.segIdx[k];
+  if (!(st < S && sg + 1u < P)) return;
+  const size_t i = (size_t)st * P + sg + end;
+  f2 o0, o1;
+  float z0, z1;
+  projectHairPoint(U.modelMatrix.m, U.vpMatrix.m, mk3(U.cameraPosition.x, U.cameraPosition.y, U.cameraPosition.z),
+                   ld4(__ldg(HFB_G(&pos[i]))), ld4(__ldg(HFB_G(&tan[i]))), size, U.fiberRadius, o0, o1, z0, z1);
+  pt[0u * STAGE + k] = o0.x;
+  pt[1u * STAGE + k] = o0.y;
+  pt[2u * STAGE + k] = o1.x;
+  pt[3u * STAGE + k] = o1.y;
+  pt[4u * STAGE + k] = z0;
+  pt[5u * STAGE + k] = z1;
+  if (end) sh.shadeBase[k] = stageShade<TS>(sh, k, st, sg, shading, P, SP);
+}
+
+// Stages segment k from the two points stagePoint left.
+template <int TS>
+__device__ __forceinline__ uint32_t stageFromPoints(FineSmem<TS>& sh, uint32_t k, uint32_t bin, uint32_t S,
+                                                    uint32_t P, uint32_t x0, uint32_t y0) {
+  constexpr uint32_t STAGE = FineSmem<TS>::STAGE;
+  const uint32_t st = sh.strand[k], sg = sh.segIdx[k];
+  if (!(st < S && sg + 1u < P)) {
+    sh.box[k] = EMPTY_BOX;
+    sh.shadeBase[k] = bin << 24;
+    sh.cntEdge[k] = 0;
+    sh.cntFrag[k] = 0;
+    return 0u;
+  }
+  const float* p0 = reinterpret_cast<const float*>(sh.frag);
+  const float* p1 = p0 + 6u * STAGE;
+  ProjSeg s;
+  s.v00 = mk2(p0[0u * STAGE + k], p0[1u * STAGE + k]);
+  s.v01 = mk2(p0[2u * STAGE + k], p0[3u * STAGE + k]);
+  s.v10 = mk2(p1[0u * STAGE + k], p1[1u * STAGE + k]);
+  s.v11 = mk2(p1[2u * STAGE + k], p1[3u * STAGE + k]);
+  s.depthsProj = mk4(p0[4u * STAGE + k], p0[5u * STAGE + k], p1[4u * STAGE + k], p1[5u * STAGE + k]);
+  return stageFromProjection<TS>(sh, k, bin, s, sh.shadeBase[k], x0, y0);
 }
 
 // Fragment colour of staged segment k at segment coordinates w and depth hd
@@ -1040,18 +1139,6 @@ __device__ __forceinline__ uint32_t buildRuns(FineSmem<TS>& sh, uint32_t B, uint
   return n;
 }
 
-// Shared inputs of the fine pass.
-struct FineArgs {
-  uint32_t S, P, B, L, SP, CAP, alphaQuadratic;
-  float alphaMul;
-  const float4* __restrict__ pos;
-  const float4* __restrict__ tan;
-  const float4* __restrict__ shading;
-  const float* __restrict__ depth;
-  const uint4* __restrict__ tiles;
-  const uint32_t* __restrict__ segBuf;
-  DeviceCounters* counters;
-};
 
 // Rasterizes depth bins [b0, b1) of tile tileIdx in order, every pixel
 // starting from an empty colour (processTile per bin + reduceHairSlices,
@@ -1066,20 +1153,13 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
   using SM = FineSmem<TS>;
   constexpr uint32_t NT = SM::NT, STAGE = SM::STAGE, PAIRS = SM::PAIRS, NW = NT / 32u;
   constexpr uint32_t MODE_FAST = 0, MODE_TIGHTEN = 1, MODE_ABORT = 2;
-  const uint32_t S = a.S, P = a.P, B = a.B, L = a.L, SP = a.SP, CAP = a.CAP, alphaQuadratic = a.alphaQuadratic;
-  const float alphaMul = a.alphaMul;
-  const float4* __restrict__ pos = a.pos;
-  const float4* __restrict__ tan = a.tan;
-  const float4* __restrict__ shading = a.shading;
-  const uint32_t* __restrict__ segBuf = a.segBuf;
-  DeviceCounters* __restrict__ counters = a.counters;
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const uint32_t lx = tid % TS, ly = tid / TS;
   const f2 size = mk2(U.viewport.x, U.viewport.y);
   const uint32_t W = f2u(size.x), H = f2u(size.y);
   const uint32_t tilesX = divCeil(W, TS);
   const uint32_t maxDrawn = U.maxDrawnHairSegments;
-  const uint32_t maxProcessed = S * P;  // MAX_PROCESSED_SEGMENTS, hairFinePass.wgsl.ts:212
+  const uint32_t maxProcessed = a.S * a.P;  // MAX_PROCESSED_SEGMENTS, hairFinePass.wgsl.ts:212
   const uint32_t dispMode = U.displayMode & 0xffu;
   const uint32_t dbgMax = dispMode == 4u ? ((U.displayMode >> 8) & 0xffffu) : 0u;  // getDbgSlicesModeMaxSlices
   const bool isDbg = dbgMax != 0u;
@@ -1095,7 +1175,12 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
     if (lane == 0) sh.doneMask[warp] = dm;
   }
   fin = mk4(0.f, 0.f, 0.f, 0.f);  // rasterizerResult was cleared before the pass
-  if (tid < B) sh.head[tid] = (*HFB_G(&a.tiles[ty * tilesX * B + tx * B + tid]));
+  if (tid < a.B) {
+    const uint4 h = (*HFB_G(&a.tiles[ty * tilesX * a.B + tx * a.B + tid]));
+    sh.head[tid] = h;
+    sh.td0[tid] = (float)(0xffffffffu - h.x) / F_MAX_U32;  // _getTileDepth
+    sh.td1[tid] = (float)h.y / F_MAX_U32;
+  }
   __syncthreads();
 
   // ---- tile mode: every depth bin's list carries a length hint (padding0,
@@ -1103,7 +1188,7 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
   // tiles pass writes; otherwise each list is walked ----
   if (warp == 0) {
     uint32_t ok = 1, sum = 0;
-    for (uint32_t c0 = 0; c0 < B; c0 += 32) {
+    for (uint32_t c0 = 0; c0 < a.B; c0 += 32) {
       const uint32_t bb = c0 + lane;
       uint32_t nb = 0;
       if (bb >= b0 && bb < b1) {
@@ -1118,12 +1203,12 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
         const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
         if (lane >= (uint32_t)o) incl += y;
       }
-      if (bb < B) sh.binOff[bb] = sum + incl - nb;
+      if (bb < a.B) sh.binOff[bb] = sum + incl - nb;
       sum += __shfl_sync(0xffffffffu, incl, 31);
     }
     ok = __all_sync(0xffffffffu, ok);
     if (lane == 0) {
-      sh.binOff[B] = sum;
+      sh.binOff[a.B] = sum;
       sh.total = sum;
       sh.tileMode = ok;
       sh.bad = 0;
@@ -1134,7 +1219,7 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
   if (tileMode) {  // check every link of the contiguous layout
     const uint32_t total = sh.total;
     for (uint32_t k = tid; k < total; k += NT) {
-      uint32_t lo = 0, hi = B;  // bin of k: binOff[lo] <= k < binOff[lo + 1]
+      uint32_t lo = 0, hi = a.B;  // bin of k: binOff[lo] <= k < binOff[lo + 1]
       while (hi - lo > 1u) {
         const uint32_t mid = (lo + hi) >> 1;
         if (sh.binOff[mid] <= k) lo = mid; else hi = mid;
@@ -1143,7 +1228,7 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
       const uint32_t j = k - sh.binOff[lo];
       const uint32_t idx = h.z - 1u - j;
       if (!HFB_EXPECT(idx < maxDrawn)) { sh.bad = 1; continue; }
-      const uint32_t nxt = __ldg(HFB_G(&segBuf[2u + 2u * idx]));
+      const uint32_t nxt = __ldg(HFB_G(&a.segBuf[2u + 2u * idx]));
       if (nxt != ((j + 1u == h.w) ? INVALID_PTR : idx - 1u)) sh.bad = 1;
     }
     __syncthreads();
@@ -1175,7 +1260,7 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
         while (r + 1u < nRuns && sh.runK0[r + 1u] <= k) r++;
         const uint32_t b = sh.runBin[r] & 0xffu;
         const uint32_t idx = sh.head[b].z - 1u - (sh.runOff[r] + k - sh.runK0[r]);
-        const uint32_t enc = HFB_EXPECT(idx < maxDrawn) ? __ldg(HFB_G(&segBuf[1u + 2u * idx])) : 0xffffffffu;
+        const uint32_t enc = HFB_EXPECT(idx < maxDrawn) ? __ldg(HFB_G(&a.segBuf[1u + 2u * idx])) : 0xffffffffu;
         sh.strand[k] = enc & 0x00ffffffu;
         sh.segIdx[k] = enc >> 24;
         sh.listIdx[k] = idx;
@@ -1195,8 +1280,8 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
           const bool inRange = lane < want && lane <= p;
           uint2 e = make_uint2(0u, INVALID_PTR);
           if (inRange) {
-            e.x = __ldg(HFB_G(&segBuf[1u + 2u * cand]));
-            e.y = __ldg(HFB_G(&segBuf[2u + 2u * cand]));
+            e.x = __ldg(HFB_G(&a.segBuf[1u + 2u * cand]));
+            e.y = __ldg(HFB_G(&a.segBuf[2u + 2u * cand]));
           }
           const bool chain = inRange && e.y == cand - 1u;
           const uint32_t brk = __ballot_sync(0xffffffffu, !chain);
@@ -1239,11 +1324,25 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
       const uint32_t nStaged = sh.nStaged;
 #pragma unroll
       for (uint32_t w = 0; w < STAGE / 32; w++) sh.pixMask[w][tid] = 0u;
-      for (uint32_t k = tid; k < nStaged; k += NT) {
-        uint32_t r = 0;
-        while (r + 1u < nRuns && sh.runK0[r + 1u] <= k) r++;
-        sh.pairBase[k] = stageSegment<TS>(sh, k, sh.runBin[r] & 0xffu, U, pos, tan, shading, S, P, SP, size,
-                                          tbp.x0, tbp.y0);
+      if constexpr (2u * STAGE <= NT) {
+        // two threads per segment: one projects its first point, one its second
+        if (tid < 2u * nStaged) {
+          const uint32_t end = tid >= nStaged ? 1u : 0u;
+          stagePoint<TS>(sh, tid - end * nStaged, end, U, a.pos, a.tan, a.shading, a.S, a.P, a.SP, size);
+        }
+        __syncthreads();
+        for (uint32_t k = tid; k < nStaged; k += NT) {
+          uint32_t r = 0;
+          while (r + 1u < nRuns && sh.runK0[r + 1u] <= k) r++;
+          sh.pairBase[k] = stageFromPoints<TS>(sh, k, sh.runBin[r] & 0xffu, a.S, a.P, tbp.x0, tbp.y0);
+        }
+      } else {
+        for (uint32_t k = tid; k < nStaged; k += NT) {
+          uint32_t r = 0;
+          while (r + 1u < nRuns && sh.runK0[r + 1u] <= k) r++;
+          sh.pairBase[k] = stageSegment<TS>(sh, k, sh.runBin[r] & 0xffu, U, a.pos, a.tan, a.shading, a.S, a.P,
+                                            a.SP, size, tbp.x0, tbp.y0);
+        }
       }
       __syncthreads();
       // exclusive prefix of the areas; the round keeps the longest prefix
@@ -1291,7 +1390,9 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
       uint32_t p = tid * per;
       const uint32_t pEnd = min(p + per, nPairs);
       uint32_t k = 0, rx = 0, ry = 0, bw = 1, bh = 1, bx0 = 0, by0 = 0, myCnt = 0;
-      float eox[4], eoy[4], eex[4], eey[4];
+      // edgeFunction (swRasterizeHair.wgsl.ts:128-130) is (x - ox) * ey - (y - oy) * ex: the
+      // second product is the same along a row and is formed once per row (the same values)
+      float eox[4], eey[4], rowT[4];
       auto loadSeg = [&](uint32_t kk) {
         const uint32_t bx = sh.box[kk];
         bx0 = bx & 0xffu;
@@ -1300,8 +1401,13 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
         bh = (bx >> 24) - by0 + 1u;
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-          eox[i] = sh.ox[i][kk]; eoy[i] = sh.oy[i][kk]; eex[i] = sh.ex[i][kk]; eey[i] = sh.ey[i][kk];
+          eox[i] = sh.ox[i][kk]; eey[i] = sh.ey[i][kk];
         }
+      };
+      auto setRow = [&]() {
+        const float py = (float)(tbp.y0 + by0 + ry);
+#pragma unroll
+        for (int i = 0; i < 4; i++) rowT[i] = fmul(fsub(py, sh.oy[i][k]), sh.ex[i][k]);
       };
       if (p < pEnd) {
         uint32_t lo = 0, hi = nSeg;  // last k with pairBase[k] <= p
@@ -1314,6 +1420,7 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
         const uint32_t r = p - sh.pairBase[k];
         ry = r / bw;
         rx = r - ry * bw;
+        setRow();
       }
       for (uint32_t it = 0; it < per; it++) {
         const bool valid = p < pEnd;
@@ -1323,11 +1430,11 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
           const uint32_t qx = bx0 + rx, qy = by0 + ry;
           pix = qy * TS + qx;
           if (!((sh.doneMask[pix >> 5] >> (pix & 31u)) & 1u)) {
-            const f2 pf = mk2((float)(tbp.x0 + qx), (float)(tbp.y0 + qy));
+            const float px = (float)(tbp.x0 + qx);
             pass = true;
 #pragma unroll
-            for (int i = 0; i < 4; i++) {  // edgeFunction, swRasterizeHair.wgsl.ts:128-130
-              const float C = fsub(fmul(fsub(pf.x, eox[i]), eey[i]), fmul(fsub(pf.y, eoy[i]), eex[i]));
+            for (int i = 0; i < 4; i++) {  // edgeFunction >= 0
+              const float C = fsub(fmul(fsub(px, eox[i]), eey[i]), rowT[i]);
               pass = pass && C >= 0.0f;
             }
           }
@@ -1353,7 +1460,10 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
                 while (sh.pairBase[k + 1u] <= p) k++;  // next segment with pairs
                 loadSeg(k);
                 ry = 0;
+                setRow();
               }
+            } else if (p < pEnd) {
+              setRow();
             }
           }
         }
@@ -1363,46 +1473,62 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
     __syncthreads();
 
     // ---------------- can a bin fill its pool in this round? ----------------
-    if (warp == 0) {
-      uint32_t mode = MODE_FAST, keep = nRuns, e0 = 0, eLast = 0;
-      for (uint32_t r = 0; r < nRuns; r++) {
-        uint32_t e = 0;
-        for (uint32_t k = sh.runK0[r] + lane; k < sh.runK1[r]; k += 32) e += sh.cntEdge[k];
-        e = __reduce_add_sync(0xffffffffu, e);
-        const uint32_t base = r == 0u ? runningUB : 0u;
-        if (r == 0u) e0 = e;
-        if (base + e > CAP) {
-          if (r == 0u) { mode = MODE_TIGHTEN; keep = 1; } else { keep = r; }
-          break;
+    // The edge-test passes bound the fragments: when the passes of the whole
+    // round, on top of what the cursor's bin may already hold, fit in a pool,
+    // no bin can fill its pool and nothing needs counting (the common case:
+    // every thread sees passCount after the barrier above).  Otherwise one
+    // warp sums the passes run by run.  e0 / eLast carry the bounds of the
+    // first and last run (the round's total where it is enough).
+    uint32_t mode = MODE_FAST, e0 = sh.passCount, eLast = e0;
+    if (runningUB + e0 > a.CAP) {
+      if (warp == 0) {
+        uint32_t wmode = MODE_FAST, keep = nRuns, we0 = 0, weLast = 0;
+        for (uint32_t r = 0; r < nRuns; r++) {
+          uint32_t e = 0;
+          for (uint32_t k = sh.runK0[r] + lane; k < sh.runK1[r]; k += 32) e += sh.cntEdge[k];
+          e = __reduce_add_sync(0xffffffffu, e);
+          const uint32_t base = r == 0u ? runningUB : 0u;
+          if (r == 0u) we0 = e;
+          if (base + e > a.CAP) {
+            if (r == 0u) { wmode = MODE_TIGHTEN; keep = 1; } else { keep = r; }
+            break;
+          }
+          weLast = e;
         }
-        eLast = e;
-      }
-      if (independent && (mode == MODE_TIGHTEN || keep < nRuns)) mode = MODE_ABORT;
-      if (lane == 0) {
-        sh.mode = mode;
-        sh.e0 = e0;
-        sh.eLast = eLast;
-        if (keep < nRuns) {  // the round ends where that bin's run starts
-          sh.nRuns = keep;
-          sh.nSeg = sh.runK1[keep - 1u];
+        if (independent && (wmode == MODE_TIGHTEN || keep < nRuns)) wmode = MODE_ABORT;
+        if (lane == 0) {
+          sh.mode = wmode;
+          sh.e0 = we0;
+          sh.eLast = weLast;
+          if (keep < nRuns) {  // the round ends where that bin's run starts
+            sh.nRuns = keep;
+            sh.nSeg = sh.runK1[keep - 1u];
+          }
+          sh.roundFrags = 0;
         }
-        sh.roundFrags = 0;
       }
+      __syncthreads();
+      mode = sh.mode;
+      e0 = sh.e0;
+      eLast = sh.eLast;
+      if (mode == MODE_ABORT) return false;  // a pool could fill: this group cannot stand alone
+      nRuns = sh.nRuns;
+      nSeg = sh.nSeg;
     }
-    __syncthreads();
-    if (sh.mode == MODE_ABORT) return false;  // a pool could fill: this group cannot stand alone
-    nRuns = sh.nRuns;
-    nSeg = sh.nSeg;
     bool exact = false;
-    if (sh.mode == MODE_TIGHTEN) {
+    if (mode == MODE_TIGHTEN) {
       running += blockSum<NW>(pending, sh.red, lane, warp);
       pending = 0;
       runningUB = running;
-      exact = runningUB + sh.e0 > CAP;
+      exact = runningUB + e0 > a.CAP;
     }
 
     // ---------------- A2: fragments, one thread per passing pair ----------------
     {
+      // the arguments this phase reads, in registers for the phase only
+      const uint32_t P = a.P, SP = a.SP, L = a.L, alphaQuadratic = a.alphaQuadratic;
+      const float alphaMul = a.alphaMul;
+      const float4* __restrict__ shading = a.shading;
       const uint32_t nPass = sh.passCount;
       for (uint32_t i = tid; i < nPass; i += NT) {
         const uint32_t e = sh.frag[i].x;
@@ -1420,12 +1546,11 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
         const f2 w = interpolateHairQuadPre(qc, mk2(sh.ox[3][k], sh.oy[3][k]), pf);
         const float hd = interpolateHairF32(w, mk4(sh.dp[0][k], sh.dp[1][k], sh.dp[2][k], sh.dp[3][k]));
         if (!(hd < sh.zbuf[pix])) continue;  // depth test with GL_LESS (skip when >=)
-        const uint4 h = sh.head[sh.shadeBase[k] >> 24];
-        const float td0 = (float)(0xffffffffu - h.x) / F_MAX_U32;  // _getTileDepth
-        const float td1 = (float)h.y / F_MAX_U32;
+        const uint32_t kb = sh.shadeBase[k] >> 24;
+        const float td0 = sh.td0[kb], td1 = sh.td1[kb];
         uint32_t slice;
-        const uint2 col = fragmentColour<TS>(sh, k, w, hd, P, SP, L, td0, td1, alphaQuadratic, alphaMul,
-                                             shading, slice);
+        const uint2 col = fragmentColour<TS>(sh, k, w, hd, P, SP, L, td0, td1, alphaQuadratic, alphaMul, shading,
+                                             slice);
         sh.frag[i] = col;
         const uint32_t bx = sh.box[k];
         sh.pairInfo[sh.pairBase[k] + (qy - ((bx >> 8) & 0xffu)) * (((bx >> 16) & 0xffu) - (bx & 0xffu) + 1u) +
@@ -1449,11 +1574,11 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
             const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
             if (lane >= (uint32_t)o) incl += y;
           }
-          const uint32_t fb = __ballot_sync(0xffffffffu, k < nSeg && running + carry + incl >= CAP);
+          const uint32_t fb = __ballot_sync(0xffffffffu, k < nSeg && running + carry + incl >= a.CAP);
           if (fb) {
             const uint32_t j = (uint32_t)(__ffs(fb) - 1);
             cut = k0 + j;
-            cutSlots = CAP - (running + carry + __shfl_sync(0xffffffffu, incl - c, j));
+            cutSlots = a.CAP - (running + carry + __shfl_sync(0xffffffffu, incl - c, j));
             break;
           }
           carry += __shfl_sync(0xffffffffu, incl, 31);
@@ -1466,7 +1591,7 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
             sh.nSeg = cut + 1u;
             sh.runK1[0] = cut + 1u;
             sh.runBin[0] |= RUN_ENDS;  // the reference breaks after the filling segment
-            atomicAdd(HFB_G(&counters->finePoolFullBins), 1ull);
+            atomicAdd(HFB_G(&a.counters->finePoolFullBins), 1ull);
           }
         }
       }
@@ -1483,6 +1608,7 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
     }
 
     // ---------------- B: every pixel blends its fragments in list order ----------------
+    const uint32_t L = a.L;
     for (uint32_t r = 0; r < nRuns; r++) {
       const uint32_t rb = sh.runBin[r], k0 = sh.runK0[r], k1 = sh.runK1[r];
       if (!done && k0 < k1) {
@@ -1543,11 +1669,11 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
         runningUB = running;
         pending = 0;
       } else {
-        runningUB += sh.e0;
+        runningUB += e0;
       }
     } else {
       running = 0;
-      runningUB = sh.eLast;
+      runningUB = eLast;
     }
     if (tileMode) {
       const uint32_t lb = lastBin & 0xffu;
@@ -1672,7 +1798,7 @@ fineScheduleKernel(const uint32_t* __restrict__ tileList, const uint32_t* __rest
 // One work item of the fine pass: a tile, or one group of depth bins of a
 // split tile (then the last group to finish merges the tile).
 template <int TS, int MAXL>
-__device__ __forceinline__ void fineItem(FineSmem<TS>& sh, const HfbUniforms& U, const FineArgs a,
+__device__ __forceinline__ void fineItem(FineSmem<TS>& sh, const HfbUniforms& U, const FineArgs& a,
                                          const uint32_t* __restrict__ tileList, float* __restrict__ result,
                                          const FineScratch fs, const uint4 item) {
   using SM = FineSmem<TS>;
@@ -1746,7 +1872,7 @@ __device__ __forceinline__ void fineItem(FineSmem<TS>& sh, const HfbUniforms& U,
 }
 
 template <int TS, int MAXL>
-__global__ void __launch_bounds__(TS * TS, TS == 8 ? (MAXL <= 4 ? 8 : 6) : TS == 16 ? (MAXL <= 4 ? 4 : 2) : 1)
+__global__ void __launch_bounds__(TS * TS, TS == 8 ? (MAXL <= 4 ? 8 : 6) : TS == 16 ? (MAXL <= 4 ? 3 : 2) : 1)
 fineKernel(const HfbUniforms U, const FineArgs a, const uint32_t* __restrict__ tileList, float* __restrict__ result,
            FineScratch fs) {
   using SM = FineSmem<TS>;
@@ -1754,19 +1880,20 @@ fineKernel(const HfbUniforms U, const FineArgs a, const uint32_t* __restrict__ t
   SM& sh = *reinterpret_cast<SM*>(fineSmemRaw);
   const uint32_t nItems = min((*HFB_G(&fs.hdr[0])), fs.maxItems);
   uint32_t* queue = reinterpret_cast<uint32_t*>(result);  // tileQueueAtomicIdx, getNextTileIdx :294-303
+  if (threadIdx.x == 0) sh.args = a;
   while (true) {
     if (threadIdx.x == 0) sh.queueIdx = atomicAdd(HFB_G(queue), 1u);
     __syncthreads();
     const uint32_t it = sh.queueIdx;
     if (it >= nItems) break;
-    fineItem<TS, MAXL>(sh, U, a, tileList, result, fs, (*HFB_G(&fs.items[it])));
+    fineItem<TS, MAXL>(sh, U, sh.args, tileList, result, fs, (*HFB_G(&fs.items[it])));
     __syncthreads();  // the tile's shared state is rewritten for the next item
   }
 }
 
 // batched: one queue over the work items of every instance
 template <int TS, int MAXL>
-__global__ void __launch_bounds__(TS * TS, TS == 8 ? (MAXL <= 4 ? 8 : 6) : TS == 16 ? (MAXL <= 4 ? 4 : 2) : 1)
+__global__ void __launch_bounds__(TS * TS, TS == 8 ? (MAXL <= 4 ? 8 : 6) : TS == 16 ? (MAXL <= 4 ? 3 : 2) : 1)
 fineBatch(BatchView b, FineArgs base, HfbConfig cfgParam) {
   using SM = FineSmem<TS>;
   const HfbConfig cfg = cfgParam;
@@ -1775,24 +1902,31 @@ fineBatch(BatchView b, FineArgs base, HfbConfig cfgParam) {
   const uint32_t n = b.hdr->n;
   const uint32_t total = b.itemPrefix[n];
   while (true) {
-    if (threadIdx.x == 0) sh.queueIdx = atomicAdd(&b.hdr->fineQueue, 1u);
+    if (threadIdx.x == 0) {
+      const uint32_t gi = atomicAdd(&b.hdr->fineQueue, 1u);
+      sh.queueIdx = gi;
+      if (gi < total) {  // the item's instance, for every thread of the CTA
+        const BatchInst& I = b.insts[batchFind(b.itemPrefix, n, gi)];
+        FineArgs a = base;
+        a.S = I.S;
+        a.P = I.P;
+        a.pos = I.posNew;
+        a.tan = I.tan;
+        a.shading = I.shading;
+        a.depth = I.depth;
+        a.tiles = I.tiles;
+        a.segBuf = I.segBuf;
+        sh.args = a;
+      }
+    }
     __syncthreads();
     const uint32_t gi = sh.queueIdx;
     if (gi >= total) break;
     const uint32_t i = batchFind(b.itemPrefix, n, gi);
     const BatchInst& I = b.insts[i];
-    FineArgs a = base;
-    a.S = I.S;
-    a.P = I.P;
-    a.pos = I.posNew;
-    a.tan = I.tan;
-    a.shading = I.shading;
-    a.depth = I.depth;
-    a.tiles = I.tiles;
-    a.segBuf = I.segBuf;
     const FineScratch fs = fineScratchLayout(I.scratch, cfg, I.W, I.H);
     const uint32_t li = gi - b.itemPrefix[i];
-    if (li < fs.maxItems) fineItem<TS, MAXL>(sh, I.U, a, I.tileList, I.result, fs, (*HFB_G(&fs.items[li])));
+    if (li < fs.maxItems) fineItem<TS, MAXL>(sh, I.U, sh.args, I.tileList, I.result, fs, (*HFB_G(&fs.items[li])));
     __syncthreads();
   }
 }

@@ -157,20 +157,28 @@ __global__ void __launch_bounds__(256) gridPreSimKernel(const HfbSimUniforms u, 
 // ---------------------------------------------------------------------------
 // HairSimIntegrationPass.main, hairSimIntegrationPass.wgsl.ts:79-273
 //
-// A block holds NB strands in shared memory, laid out [strand][point + 1]:
-// one thread per strand walks the Gauss-Seidel chains (length and local
-// shape must stay sequential along the strand, as in the reference), and
-// the whole block runs the per-point phases (Verlet and forces, global
-// shape, sphere and SDF collisions) and the coalesced loads and stores.
-// The padding makes both access patterns conflict-free.  Everything the
-// chains need from the initial pose (segment lengths, the triangle-bending
-// constants, the initial tangents) is staged beside the points, so a chain
-// step touches shared memory only.
+// A block holds NB strands' points in shared memory, laid out
+// [strand][point + 1]: one thread per strand walks the Gauss-Seidel chains
+// (length and local shape must stay sequential along the strand, as in the
+// reference), and the whole block runs the per-point phases (Verlet and
+// forces, global shape, sphere and SDF collisions) and the coalesced loads
+// and stores.  The padding makes both access patterns conflict-free.
+//
+// The chains are latency-bound (each step waits on the last: an IEEE square
+// root and division per step), so what sets the pass's speed is how many
+// chains an SM walks at once, and shared memory is what bounds that.  Only
+// the points live there (16 B each): the triangle-bending constants and
+// initial tangents the local chain reads are written, in the Verlet phase,
+// over the block's own points of the PREV buffer -- each thread reads its
+// point's previous position first, and nothing else reads those addresses
+// until the final positions overwrite them -- and the segment lengths are
+// read from their buffer; the chains prefetch both a step ahead.  A block of
+// 128 threads holds 2,048 points (64 strands of 32, 128 of 16), six blocks
+// per SM: 384 strands of 32 points in flight per SM, three chain warps per
+// scheduler.
 // ---------------------------------------------------------------------------
-constexpr uint32_t SIM_THREADS = 256;        // threads per block of the single-instance kernel
-constexpr uint32_t SIM_BATCH_THREADS = 256;  // and of the batched one: 4 blocks per SM (5 blocks of
-                                             // 128 threads took 4.15 ms against 3.80, 5 of 192 3.43
-                                             // against 3.38, on the 64-instance frame)
+constexpr uint32_t SIM_THREADS = 128;        // threads per block of the single-instance kernel
+constexpr uint32_t SIM_BATCH_THREADS = 128;  // and of the batched one (6 blocks per SM)
 
 
 // p + z for z a signed zero whose sign is that of c xor the bit in s: p itself
@@ -219,19 +227,51 @@ __device__ __forceinline__ float4 verletPoint(const HfbSimUniforms& u, uint32_t 
   return make_float4(r.x, r.y, r.z, posNow.w);
 }
 
+// applyCollisionsSphere, collisions.wgsl.ts:4-20: pushes pos out of the sphere by kColl.
+__device__ __forceinline__ void sphereCollide(float4& pos, const f4 sph, float kColl, bool kCollFinite) {
+  f3 v = mk3(fsub(pos.x, sph.x), fsub(pos.y, sph.y), fsub(pos.z, sph.z));
+  const float l = len3(v);
+  float dist = fsub(l, sph.w);
+  float dts = fmaxf(0.0f, -dist);
+  if (dts == 0.0f && l > 0.0f && l < INFINITY && kCollFinite) {
+    // outside the sphere the correction (v / l) * dts * kColl is a signed zero, the sign
+    // of v's component times those of dts and kColl; adding it changes only a -0
+    // coordinate, into +0 when the zero is +0
+    const uint32_t sz = (__float_as_uint(dts) ^ __float_as_uint(kColl)) & 0x80000000u;
+    zeroSum(pos.x, v.x, sz); zeroSum(pos.y, v.y, sz); zeroSum(pos.z, v.z, sz);
+  } else {
+    f3 d = mul3s(mul3s(norm3(v), dts), kColl);
+    pos.x = fadd(pos.x, d.x); pos.y = fadd(pos.y, d.y); pos.z = fadd(pos.z, d.z);
+  }
+}
+
+// applyCollisionsSdf, collisions.wgsl.ts:23-61, given the distance d sampled at q (pos's xyz).
+__device__ __forceinline__ void sdfPush(float4& pos, const f3 q, float d, const float* __restrict__ sdf, uint32_t D,
+                                        const f3 smin, const f3 smax, float sdfOffset, float kSdf) {
+  float dOff = fadd(d, sdfOffset);
+  if (!(dOff >= 0.0f)) {
+    const float o = SDF_GRAD_OFFSET;
+    f3 cd;
+    cd.x = sampleSDF(sdf, D, smin, smax, add3(q, mk3(fmul(o, 1.0f), fmul(o, 0.0f), fmul(o, 0.0f))));
+    cd.y = sampleSDF(sdf, D, smin, smax, add3(q, mk3(fmul(o, 0.0f), fmul(o, 1.0f), fmul(o, 0.0f))));
+    cd.z = sampleSDF(sdf, D, smin, smax, add3(q, mk3(fmul(o, 0.0f), fmul(o, 0.0f), fmul(o, 1.0f))));
+    cd = sub3(cd, mk3(d, d, d));
+    f3 corr = mul3s(norm3(cd), -dOff);
+    f3 dd = mul3s(corr, kSdf);
+    pos.x = fadd(pos.x, dd.x); pos.y = fadd(pos.y, dd.y); pos.z = fadd(pos.z, dd.z);
+  }
+}
+
 template <uint32_t NT>
 __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32_t S, uint32_t P, uint32_t G,
                                                  float4* __restrict__ prev, const float4* __restrict__ now,
                                                  const float4* __restrict__ initial, const float* __restrict__ segLen,
                                                  const int4* __restrict__ dv, const float4* __restrict__ gw,
                                                  const float* __restrict__ sdf, uint32_t D, float4* simSmem,
-                                                 uint32_t blk) {
-  const uint32_t NB = simStrandsPerBlock(P), R = P + 1u;  // row stride (padded)
+                                                 uint32_t blk, uint32_t NB) {
+  const uint32_t R = P + 1u;  // row stride (padded)
   float4* wk = simSmem;                                   // [NB][R] positions
-  float4* lc = wk + NB * R;  // [NB][R] triangle-bending constants (h0, w0, w1, w2) of the triplet at j,
-                             // or the initial tangent into j for the points matchInitialTangent moves
-  float* sl = reinterpret_cast<float*>(lc + NB * R);  // [NB][R] segment lengths
-  float* att = sl + NB * R;                            // [P] global-shape attenuation of point index j
+  float* att = reinterpret_cast<float*>(wk + NB * R);     // [P] global-shape attenuation of point index j
   const uint32_t tid = threadIdx.x;
   const uint32_t s0 = blk * NB;
   const uint32_t nStr = min(NB, S - s0);
@@ -239,15 +279,18 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
   const f3 gmin = gridMin(u), gmax = gridMax(u);
   // first point matchInitialTangent moves: the triplet loop ends at P - 3
   const uint32_t jTan = P >= 3u ? P - 3u : 0u;
+  // the block's points of the PREV buffer: read once by the Verlet phase, then
+  // the chain constants of each point, then the new positions
+  float4* const lcg = prev + (size_t)s0 * P;
 
   // --- Verlet + forces and the chain constants, point-parallel ---
+#pragma unroll 2
   for (uint32_t i = tid; i < nPts; i += NT) {
     const uint32_t ls = i / P, pt = i - ls * P;
     const size_t gi = (size_t)s0 * P + i;
     const f4 posNow = ld4(__ldg(HFB_G(&now[gi])));
     wk[ls * R + pt] = pt == 0u ? make_float4(posNow.x, posNow.y, posNow.z, posNow.w)
                                : verletPoint(u, G, gmin, gmax, s0 + ls, posNow, ld4(*HFB_G(&prev[gi])), dv, gw);
-    sl[ls * R + pt] = __ldg(HFB_G(&segLen[gi]));
     const float4 i0 = __ldg(HFB_G(&initial[gi]));
     float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
     if (pt + 3u < P) {  // applyConstraint_localShape constants (constraints.wgsl.ts:54-99)
@@ -260,16 +303,16 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
       const float4 im = __ldg(HFB_G(&initial[gi - 1u]));
       c = make_float4(fsub(i0.x, im.x), fsub(i0.y, im.y), fsub(i0.z, im.z), 0.0f);
     }
-    lc[ls * R + pt] = c;
+    *HFB_G(&prev[gi]) = c;  // over the previous position this thread has just read
   }
   for (uint32_t j = tid; j < P; j += NT) {  // applyConstraint_global's attenuation (constraints.wgsl.ts:31-49)
     const float x = (float)j / (float)(P - 1u);
     att[j] = fsub(1.0f, sat(fsub(x, u.globalConstrExtent) / u.globalConstrFade));
   }
-  // i / P for the block's points (i < NB * P <= 1024, P <= 128): floor(i * ceil(2^32 / P) / 2^32)
-  // is exact there, the error i * (ceil(2^32 / P) * P - 2^32) < 1024 * 128 being far below 2^32
+  // i / P for the block's points (i < NB * P <= 2048, P <= 256): floor(i * ceil(2^32 / P) / 2^32)
+  // is exact there, the error i * (ceil(2^32 / P) * P - 2^32) < 2048 * 256 being far below 2^32
   const uint32_t divP = (uint32_t)((0x100000000ull + P - 1u) / P);
-  __syncthreads();
+  __syncthreads();  // also makes the constants in PREV visible to the block's chain threads
 
   const uint32_t iters = u.constraintIterations;
   const f3 smin = mk3(u.sdf.boundsMin.x, u.sdf.boundsMin.y, u.sdf.boundsMin.z);
@@ -286,11 +329,12 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
     // length constraint (Gauss-Seidel), :176-190, constraints.wgsl.ts:5-28
     for (uint32_t ls = tid; ls < nStr; ls += NT) {
       float4* w = wk + ls * R;
-      const float* L = sl + ls * R;
+      const float* L = segLen + (size_t)(s0 + ls) * P;
       float4 a = w[0];
+      float expected = __ldg(HFB_G(&L[0])), nextExpected = __ldg(HFB_G(&L[1]));  // P >= 2
       for (uint32_t j = 0; j + 1u < P; j++) {
+        const float nextExpected2 = j + 2u < P ? __ldg(HFB_G(&L[j + 2u])) : 0.0f;  // two steps ahead
         float4 b = w[j + 1u];
-        const float expected = L[j];
         const float w0 = a.w, w1 = b.w;
         f3 tng = mk3(fsub(b.x, a.x), fsub(b.y, a.y), fsub(b.z, a.z));
         float actual = len3(tng);
@@ -303,11 +347,14 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
         b.x = fsub(b.x, fmul(w1, delta.x)); b.y = fsub(b.y, fmul(w1, delta.y)); b.z = fsub(b.z, fmul(w1, delta.z));
         w[j] = a;
         a = b;
+        expected = nextExpected;
+        nextExpected = nextExpected2;
       }
       w[P - 1u] = a;
     }
     __syncthreads();
     // global shape, :193-206, constraints.wgsl.ts:31-49 (point-parallel)
+#pragma unroll 2
     for (uint32_t i = tid; i < nPts; i += NT) {
       const uint32_t ls = __umulhi(i, divP), j = i - ls * P;
       if (j == 0u) continue;
@@ -323,13 +370,15 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
     // local shape (triangle bending, Gauss-Seidel), :209-232, constraints.wgsl.ts:54-120
     for (uint32_t ls = tid; ls < nStr; ls += NT) {
       float4* w = wk + ls * R;
-      const float4* C = lc + ls * R;
+      const float4* C = lcg + (size_t)ls * P;
       uint32_t jj = 0;
       if (P >= 3u) {
         float4 p0 = w[0], p1 = w[1];
+        // the constants come from L2 (written this frame): loaded two steps ahead
+        float4 cc = *HFB_G(&C[0]), ccNext = *HFB_G(&C[1]);
         for (; jj + 3u < P; jj++) {
+          const float4 ccNext2 = *HFB_G(&C[jj + 2u]);  // jj + 2 < P
           float4 p2 = w[jj + 2u];
-          const float4 cc = C[jj];
           f3 c = div3sBy3(add3(add3(mk3(p0.x, p0.y, p0.z), mk3(p1.x, p1.y, p1.z)), mk3(p2.x, p2.y, p2.z)));
           f3 hv = sub3(mk3(p1.x, p1.y, p1.z), c);
           float h = len3(hv);
@@ -342,6 +391,8 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
           w[jj] = p0;
           p0 = p1;
           p1 = p2;
+          cc = ccNext;
+          ccNext = ccNext2;
         }
         w[jj] = p0;
         w[jj + 1u] = p1;
@@ -350,7 +401,7 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
         if (jj == 0u) continue;
         const float4 p0 = w[jj - 1u];
         float4 p1 = w[jj];
-        const float4 t = C[jj];
+        const float4 t = *HFB_G(&C[jj]);
         f3 proj = add3(mk3(p0.x, p0.y, p0.z), mk3(t.x, t.y, t.z));
         f3 delta = sub3(proj, mk3(p1.x, p1.y, p1.z));
         f3 d = mul3s(delta, fmul(kLoc, p1.w));
@@ -364,43 +415,16 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
       const uint32_t ls = __umulhi(i, divP), j = i - ls * P;
       if (j == 0u) continue;
       float4 pos = wk[ls * R + j];
-      {
-        f3 v = mk3(fsub(pos.x, sph.x), fsub(pos.y, sph.y), fsub(pos.z, sph.z));
-        const float l = len3(v);
-        float dist = fsub(l, sph.w);
-        float dts = fmaxf(0.0f, -dist);
-        if (dts == 0.0f && l > 0.0f && l < INFINITY && kCollFinite) {
-          // outside the sphere the correction (v / l) * dts * kColl is a signed zero, the sign
-          // of v's component times those of dts and kColl; adding it changes only a -0
-          // coordinate, into +0 when the zero is +0
-          const uint32_t sz = (__float_as_uint(dts) ^ __float_as_uint(kColl)) & 0x80000000u;
-          zeroSum(pos.x, v.x, sz); zeroSum(pos.y, v.y, sz); zeroSum(pos.z, v.z, sz);
-        } else {
-          f3 d = mul3s(mul3s(norm3(v), dts), kColl);
-          pos.x = fadd(pos.x, d.x); pos.y = fadd(pos.y, d.y); pos.z = fadd(pos.z, d.z);
-        }
-      }
+      sphereCollide(pos, sph, kColl, kCollFinite);
       if (j > 2u) {
-        f3 q = mk3(pos.x, pos.y, pos.z);
-        float d = sampleSDF(sdf, D, smin, smax, q);
-        float dOff = fadd(d, sdfOffset);
-        if (!(dOff >= 0.0f)) {
-          const float o = SDF_GRAD_OFFSET;
-          f3 cd;
-          cd.x = sampleSDF(sdf, D, smin, smax, add3(q, mk3(fmul(o, 1.0f), fmul(o, 0.0f), fmul(o, 0.0f))));
-          cd.y = sampleSDF(sdf, D, smin, smax, add3(q, mk3(fmul(o, 0.0f), fmul(o, 1.0f), fmul(o, 0.0f))));
-          cd.z = sampleSDF(sdf, D, smin, smax, add3(q, mk3(fmul(o, 0.0f), fmul(o, 0.0f), fmul(o, 1.0f))));
-          cd = sub3(cd, mk3(d, d, d));
-          f3 corr = mul3s(norm3(cd), -dOff);
-          f3 dd = mul3s(corr, kSdf);
-          pos.x = fadd(pos.x, dd.x); pos.y = fadd(pos.y, dd.y); pos.z = fadd(pos.z, dd.z);
-        }
+        const f3 q = mk3(pos.x, pos.y, pos.z);
+        sdfPush(pos, q, sampleSDF(sdf, D, smin, smax, q), sdf, D, smin, smax, sdfOffset, kSdf);
       }
       wk[ls * R + j] = pos;
     }
     __syncthreads();
   }
-  // --- write back into the PREV buffer, coalesced (:268-272) ---
+  // --- write back into the PREV buffer, coalesced (:268-272), over the chain constants ---
   for (uint32_t i = tid; i < nPts; i += NT) {
     const uint32_t ls = i / P, pt = i - ls * P;
     *HFB_G(&prev[(size_t)s0 * P + i]) = wk[ls * R + pt];
@@ -408,14 +432,14 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
   // the staging is rewritten by the CTA's next strands only after batchNext's barrier
 }
 
-__global__ void __launch_bounds__(SIM_THREADS)
+__global__ void __launch_bounds__(SIM_THREADS, 6)
 simIntegrateKernel(const HfbSimUniforms u, uint32_t S, uint32_t P, uint32_t G,
                    float4* __restrict__ prev, const float4* __restrict__ now,
                    const float4* __restrict__ initial, const float* __restrict__ segLen,
                    const int4* __restrict__ dv, const float4* __restrict__ gw,
-                   const float* __restrict__ sdf, uint32_t D) {
+                   const float* __restrict__ sdf, uint32_t D, uint32_t NB) {
   extern __shared__ float4 simSmem[];
-  simIntegrateBody<SIM_THREADS>(u, S, P, G, prev, now, initial, segLen, dv, gw, sdf, D, simSmem, blockIdx.x);
+  simIntegrateBody<SIM_THREADS>(u, S, P, G, prev, now, initial, segLen, dv, gw, sdf, D, simSmem, blockIdx.x, NB);
 }
 
 // ---------------------------------------------------------------------------
@@ -545,7 +569,7 @@ __global__ void __launch_bounds__(256, 5) gridPreSimBatch(BatchView b, uint32_t 
   }
 }
 
-__global__ void __launch_bounds__(SIM_BATCH_THREADS, 4) simIntegrateBatch(BatchView b, uint32_t G) {
+__global__ void __launch_bounds__(SIM_BATCH_THREADS, 6) simIntegrateBatch(BatchView b, uint32_t G) {
   extern __shared__ float4 simSmem[];
   const uint32_t n = b.hdr->n;
   const uint32_t* row = b.prefix + BK_INTEGRATE * (BATCH_MAX + 1);
@@ -557,7 +581,7 @@ __global__ void __launch_bounds__(SIM_BATCH_THREADS, 4) simIntegrateBatch(BatchV
     const BatchInst& I = b.insts[i];
     // integration reads positions[1 - current] (prev) and [current] (now), writes the former
     simIntegrateBody<SIM_BATCH_THREADS>(I.SU, I.S, I.P, G, I.posNew, I.posOld, I.initial, I.segLen, I.dv, I.gw, I.sdf, I.sdfDims,
-                     simSmem, v - row[i]);
+                     simSmem, v - row[i], simStrandsPerBlock(I.P));
   }
 }
 
@@ -648,12 +672,15 @@ cudaError_t launchSimIntegrate(HfbCtx* c, const HfbSimUniforms& u, const HfbHair
                                const int32_t* dv, const float* gw, const float* sdf, uint32_t sdfDims) {
   HFB_CHECK_BIND(c);
   const uint32_t S = h.strandsCount, P = h.pointsPerStrand;
-  const size_t smem = simSmemBytes(P);
+  // one instance alone rarely fills the GPU: its blocks take fewer strands
+  // (down to 8) until there are two per SM, so that more chains run at once
+  const uint32_t NB = simStrandsPerBlockFor(S, P, (uint32_t)c->smCount);
+  const size_t smem = (size_t)NB * (P + 1u) * sizeof(float4) + (size_t)P * 4u;
   cudaError_t e = simSmemLimit((const void*)simIntegrateKernel, 0);
   if (e != cudaSuccess) return e;
-  simIntegrateKernel<<<divCeil(S, simStrandsPerBlock(P)), SIM_THREADS, smem, c->stream>>>(
+  simIntegrateKernel<<<divCeil(S, NB), SIM_THREADS, smem, c->stream>>>(
       u, S, P, c->cfg.gridDims, (float4*)prev, (const float4*)now, (const float4*)initial, segLen,
-      (const int4*)dv, (const float4*)gw, sdf, sdfDims);
+      (const int4*)dv, (const float4*)gw, sdf, sdfDims, NB);
   HFB_AFTER_LAUNCH(c, "simIntegrateKernel");
   c->launches += 1;
   return cudaGetLastError();

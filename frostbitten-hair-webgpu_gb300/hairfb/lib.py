@@ -186,6 +186,7 @@ class Context:
         """Run on a torch.cuda.Stream (or raw cudaStream_t int); None = the
         context's own stream.  Handle 0 (torch's default stream) is the
         legacy default stream, passed as cudaStreamLegacy."""
+        self.stream_obj = stream
         if stream is None:
             self.call("hfb_ctx_set_stream", None)
             return

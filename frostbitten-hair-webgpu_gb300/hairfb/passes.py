@@ -41,19 +41,24 @@ class HairObject:
     """GPU buffers of one hair object; tick-tock positions
     (src/scene/hair/hairObject.ts:29-155)."""
 
-    def __init__(self, buffers: HO.HairBuffers, shading_points: int):
+    def __init__(self, buffers: HO.HairBuffers, shading_points: int, upload=None, grid_order=None):
+        """upload: host array -> device tensor (default: a blocking copy);
+        grid_order: the asset's strand_grid_order, if already known."""
+        up = upload or _dev
         a = buffers.asset
         self.buffers = buffers
         self.strands_count = a.strands
         self.points_per_strand = a.points_per_strand
-        self.initial = _dev(a.positions)
+        self.initial = up(a.positions)
         self.positions_0 = self.initial.clone()
         self.positions_1 = self.initial.clone()
-        self.tangents = _dev(buffers.tangents)
-        self.segment_lengths = _dev(buffers.segment_lengths)
-        self.shading = _dev(HO.initial_shading(a.strands, shading_points))
+        self.tangents = up(buffers.tangents)
+        self.segment_lengths = up(buffers.segment_lengths)
+        self.shading = up(HO.initial_shading(a.strands, shading_points))
         # the order the grid splat visits the strands in (neighbouring roots together)
-        self.grid_order = _dev(strand_grid_order(a.positions, a.strands, a.points_per_strand).view(np.int32))
+        if grid_order is None:
+            grid_order = strand_grid_order(a.positions, a.strands, a.points_per_strand).view(np.int32)
+        self.grid_order = up(grid_order)
         self.hair_data = HfbHairData()
         for i in range(3):
             self.hair_data.boundingSphere[i] = float(buffers.sphere_center[i])
@@ -84,10 +89,10 @@ class HairObject:
 
 
 class SdfCollider:
-    def __init__(self, vol: SdfVolume):
+    def __init__(self, vol: SdfVolume, upload=None):
         self.dims = int(vol.dims)
         self.bounds = (np.asarray(vol.bounds_min, np.float32), np.asarray(vol.bounds_max, np.float32))
-        self.texture = _dev(vol.distances)
+        self.texture = (upload or _dev)(vol.distances)
 
 
 class PhysicsGrids:
@@ -171,23 +176,59 @@ class HairShadingPass:
 class RasterBuffers:
     """The viewport-sized buffers the three raster passes share (PassCtx)."""
 
-    def __init__(self, ctx: Context, width: int, height: int, max_drawn: int | None = None):
+    def __init__(self, ctx: Context, width: int, height: int, max_drawn: int | None = None,
+                 pooled: bool = False):
         """max_drawn: the segment pool's size in records (None: the config's
-        1 + tiles * avgSegmentsPerTile)."""
+        1 + tiles * avgSegmentsPerTile).  pooled: carve the buffers out of one
+        tensor from torch's caching allocator on the current stream instead
+        of hfb_raster_buffers_alloc_sized's cudaMalloc calls, so that making
+        and dropping them never waits for the device (cudaFree does); a
+        server admitting and retiring sessions while frames run uses it."""
         self.ctx = ctx
         self.rb = HfbRasterBuffers()
-        if max_drawn is None:
+        self._block = None
+        if pooled:
+            self._alloc_pooled(width, height, max_drawn)
+        elif max_drawn is None:
             ctx.call("hfb_raster_buffers_alloc", width, height, byref(self.rb))
         else:
             ctx.call("hfb_raster_buffers_alloc_sized", width, height, int(max_drawn), byref(self.rb))
         self.width, self.height = width, height
+
+    def _alloc_pooled(self, width: int, height: int, max_drawn: int | None) -> None:
+        c = self.ctx.cfg
+        tiles = (-(-width // c.tileSize)) * (-(-height // c.tileSize))
+        md = 1 + tiles * c.avgSegmentsPerTile if max_drawn is None else int(max_drawn)
+        scratch = int(self.ctx.lib.hfb_raster_scratch_bytes_for(byref(c), width, height, md))
+        sizes = [tiles * c.tileDepthBins * 16, 4 + md * 8, tiles * 4, c.sortBuckets * 8, (4 + tiles) * 4,
+                 16 + width * height * 16, scratch]
+        offs, total = [], 0
+        for n in sizes:  # every buffer 256-byte aligned
+            offs.append(total)
+            total += (n + 255) // 256 * 256
+        # zeroed: the cleared state of hfb_raster_buffers_alloc_sized
+        self._block = torch.zeros(total, dtype=torch.uint8, device="cuda")
+        base = self._block.data_ptr()
+        rb = self.rb
+        rb.width, rb.height, rb.maxDrawnSegments = width, height, md
+        (rb.tiles, rb.tileSegments, rb.segmentCountPerTile, rb.sortBuckets, rb.tileList, rb.rasterizerResult,
+         rb.scratch) = [base + o for o in offs]
+        rb.scratchBytes = scratch
+
+    @property
+    def nbytes(self) -> int:
+        """Device bytes of a pooled set (0 for the library's allocations)."""
+        return 0 if self._block is None else self._block.numel()
 
     @property
     def max_drawn_segments(self) -> int:
         return int(self.rb.maxDrawnSegments)
 
     def close(self):
-        if self.rb.tiles:
+        if self._block is not None:
+            self._block = None  # back to torch's cache; the caller ensured no frame still uses it
+            self.rb = HfbRasterBuffers()
+        elif self.rb.tiles:
             self.ctx.call("hfb_raster_buffers_free", byref(self.rb))
 
     # ---- readback helpers (numpy copies of the reference-layout buffers) ----

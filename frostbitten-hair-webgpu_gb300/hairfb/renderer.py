@@ -29,7 +29,8 @@ class Renderer:
     """One hair instance rendered frame by frame through libhairfb.so."""
 
     def __init__(self, inst: synthetic.Instance, device: int = -1, ctx: Context | None = None,
-                 max_drawn: int | None = None, hair_depth: bool = False, ao: bool = False):
+                 max_drawn: int | None = None, hair_depth: bool = False, ao: bool = False,
+                 pooled: bool = False, upload=None, grid_order=None):
         """max_drawn: this instance's segment pool in records (None: the
         config's 1 + tiles * avgSegmentsPerTile).  hair_depth: draw the hair's
         depth over the scene depth after the fine pass (HwHairPass) and shade
@@ -39,16 +40,19 @@ class Renderer:
         updateResourcesForNextFrame does (renderer.ts:286-296); the scene's
         normals are the reference's clear value, 0 (no mesh pass here).
         These run in the pass-by-pass frames (frame()); hfb_frame and
-        hfb_frame_batch take the AO as an input instead."""
+        hfb_frame_batch take the AO as an input instead.  pooled: the raster
+        buffers come from torch's caching allocator (RasterBuffers).  upload:
+        host array -> device tensor for the static data (default: blocking
+        copies); grid_order: the asset's strand order for the grid splat."""
         self.inst = inst
         self.cfg: HairConfig = inst.cfg
         self.ctx = ctx or Context(inst.cfg.to_c(), device)
         self.max_drawn = max_drawn
-        self.hair = HairObject(inst.hair, inst.cfg.shading_points)
-        self.sdf = SdfCollider(inst.sdf)
+        self.hair = HairObject(inst.hair, inst.cfg.shading_points, upload, grid_order)
+        self.sdf = SdfCollider(inst.sdf, upload)
         self.grids = PhysicsGrids(inst.cfg.grid_dims)
-        self.rb = RasterBuffers(self.ctx, inst.width, inst.height, max_drawn)
-        self.scene_depth = torch.as_tensor(inst.scene_depth).cuda()
+        self.rb = RasterBuffers(self.ctx, inst.width, inst.height, max_drawn, pooled=pooled)
+        self.scene_depth = upload(inst.scene_depth) if upload else torch.as_tensor(inst.scene_depth).cuda()
         # depth buffer with hair drawn, for the shading attenuation; before the
         # first frame draws the hair it holds the scene alone
         self.hair_depth = self.scene_depth.clone() if hair_depth else None
@@ -72,18 +76,27 @@ class Renderer:
 
     def use_config(self, cfg: HairConfig, ctx: Context) -> None:
         """Re-targets the renderer to other pass constants (a context of
-        that config): new raster buffers and uniforms; the simulation state
-        and the hair stay resident.  The grid size must not change."""
+        that config): new uniforms, and new raster buffers unless their
+        sizes (tile size, depth bins, segment pool) are unchanged; the
+        simulation state and the hair stay resident.  The grid size must not
+        change."""
         assert cfg.grid_dims == self.cfg.grid_dims and cfg.shading_points == self.cfg.shading_points
+        same_buffers = (cfg.tile_size, cfg.tile_depth_bins, cfg.sort_buckets) == \
+            (self.cfg.tile_size, self.cfg.tile_depth_bins, self.cfg.sort_buckets) and \
+            (self.max_drawn is not None or cfg.avg_segments_per_tile == self.cfg.avg_segments_per_tile)
         old = self.rb
         self.cfg = cfg
         self.ctx = ctx
-        self.rb = RasterBuffers(ctx, self.inst.width, self.inst.height, self.max_drawn)
+        if not same_buffers:
+            self.rb = RasterBuffers(ctx, self.inst.width, self.inst.height, self.max_drawn)
+        else:
+            self.rb.ctx = ctx
         for p in (self.grid_pre, self.integrate, self.grid_post, self.shading, self.tiles, self.sort, self.fine,
                   self.hw_hair):
             p.ctx = ctx
         self.uniforms = UN.pack_render_uniforms(self.inst.scene, cfg, self.max_drawn)
-        old.close()
+        if not same_buffers:
+            old.close()
 
     def sim_uniforms(self, frame_idx: int) -> bytes:
         i = self.inst
@@ -211,3 +224,27 @@ class BatchRenderer:
         self.ctx.call("hfb_frame_batch", arr, n)
         for r, inst in zip(self.renderers, arr):
             r.after_native_frame(inst)
+
+
+class SplitBatchRenderer:
+    """Instance groups that carry their own pass constants: each group is a
+    BatchRenderer on its own context (and stream), the groups' batched
+    frames run side by side, and the caller's stream waits for all of them.
+    Results are those of each instance rendered alone with its group's
+    constants."""
+
+    def __init__(self, groups: list[list[Renderer]], stream: torch.cuda.Stream):
+        self.batches = [BatchRenderer(g) for g in groups if g]
+        self.stream = stream
+        self.renderers = [r for b in self.batches for r in b.renderers]
+
+    def frame(self) -> None:
+        start = torch.cuda.Event()
+        start.record(self.stream)
+        for b in self.batches:
+            s = b.ctx.stream_obj
+            s.wait_event(start)
+            b.frame()
+            done = torch.cuda.Event()
+            done.record(s)
+            self.stream.wait_event(done)

@@ -11,7 +11,8 @@ The reference pins three things with binary fixtures next to its tests:
 - src/scene/sdfCollider/__test__/sdf-binary.snapshot.bin -- that test's
   snapshot (each distance truncated to a u8 by the snapshot helper), copied.
 
-Run from the repository root:  python tests/golden/make_golden.py [REF_ROOT]
+Run from the repository root:  python tests/golden/make_golden.py REF_ROOT
+(REF_ROOT: a checkout of the reference project)
 """
 import os
 import shutil
@@ -36,4 +37,6 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py REF_ROOT  (a checkout of the reference project)")
+    main(sys.argv[1])

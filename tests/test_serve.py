@@ -1,7 +1,7 @@
-"""Serving: admission under a memory budget and continuous batching
-(hairfb/serve.py).  A session's frames in the served mix equal the same
-session's frames rendered alone through hfb_frame: positions and density
-grid bit-exact, pixels within 1/255."""
+"""Serving: admission under a memory budget and continuous batching of
+frame requests (hairfb/serve.py).  A session's frames in the served mix
+equal the same session's frames rendered alone through hfb_frame: positions
+and density grid bit-exact, pixels within 1/255."""
 
 import numpy as np
 import pytest
@@ -29,6 +29,24 @@ def test_poisson_sessions_and_snap():
     assert all(abs(np.log(a.strands / b.strands)) < 0.4 for a, b in zip(sp, snapped))
 
 
+def test_request_times_are_a_poisson_process():
+    sp = serve.SessionSpec(3, 0.0, 1000, 32, 256, 256, 4000, 0)
+    t = serve.request_times(sp, 8.0, seed=0)
+    assert len(t) == 4000 and np.all(np.diff(t) > 0)
+    gaps = np.diff(np.concatenate([[0.0], t]))
+    assert abs(gaps.mean() - 1 / 8.0) < 0.01 and abs(gaps.std() / gaps.mean() - 1.0) < 0.05  # exponential
+    assert np.array_equal(t, serve.request_times(sp, 8.0, seed=0))  # seeded
+
+
+def test_cost_model_fits_tick_times():
+    cm = serve.CostModel()
+    rng = np.random.Generator(np.random.PCG64(1))
+    for _ in range(64):
+        pts, pix = rng.uniform(1e4, 2e6), rng.uniform(6e4, 4e6)
+        cm.add(pts, pix, 0.3 + 2e-7 * pts + 1e-7 * pix)
+    assert abs(cm.ms(1e6, 1e6) - (0.3 + 0.2 + 0.1)) < 1e-6
+
+
 @pytest.mark.gpu
 def test_served_sessions_equal_sessions_alone():
     torch = pytest.importorskip("torch")
@@ -53,8 +71,9 @@ def test_served_sessions_equal_sessions_alone():
                                  r.grids.density_velocity.cpu().numpy().copy(),
                                  r.rb.read_result()[4:].copy(), r.hair.shading.cpu().numpy().copy())
 
-    st = server.run(specs, frame_done)
-    assert st.frames == sum(s.frames for s in specs)
+    st = server.run(specs, frame_done=frame_done, per_session_rate_hz=300.0)
+    assert st.frames == sum(s.frames for s in specs) == len(st.latency_ms)
+    assert all(v > 0.0 for v in st.latency_ms)
     assert st.dropped == 0
     assert st.peak_bytes <= server.budget and st.peak_sessions < len(specs), (st.peak_sessions, st.peak_bytes)
     assert max(st.admit_wait_ms) > 0.0  # someone waited for memory
