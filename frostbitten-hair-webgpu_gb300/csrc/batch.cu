@@ -57,12 +57,16 @@ cudaError_t framePass(HfbCtx* c, HfbInstance* in, FramePass p) {
       return launchGridPostSim(c, su, h, now, prev, in->densityVelocity, in->gridOrder);
     case FP_CLEAR:
       return clearRaster(c, rb);
-    case FP_TILES:
-      return launchTilesPass(c, u, h, prev, in->tangents, in->sceneDepth, in->strandsToRender, rb);
+    case FP_TILES: {
+      // the segments' projections, for this frame's fine pass
+      const cudaError_t e = ensureProjCache(c, (size_t)h.strandsCount * (h.pointsPerStrand - 1u));
+      if (e != cudaSuccess) return e;
+      return launchTilesPass(c, u, h, prev, in->tangents, in->sceneDepth, in->strandsToRender, rb, c->projCache);
+    }
     case FP_SORT:
       return launchTileSort(c, rb);
     case FP_FINE:
-      return launchFinePass(c, u, h, prev, in->tangents, in->shading, in->sceneDepth, rb);
+      return launchFinePass(c, u, h, prev, in->tangents, in->shading, in->sceneDepth, rb, c->projCache);
     case FP_HAIR_DEPTH:
       if (!in->hairDepth) return cudaSuccess;
       return launchHairDepth(c, u, h, prev, in->tangents, in->strandsToRender, in->sceneDepth, in->hairDepth, rb);
@@ -75,6 +79,29 @@ cudaError_t framePass(HfbCtx* c, HfbInstance* in, FramePass p) {
     default:
       return cudaErrorInvalidValue;
   }
+}
+
+cudaError_t ensureProjCache(HfbCtx* c, size_t segments) {
+  const size_t need = segments * SEG_PROJ_VEC4 * sizeof(float4);
+  if (need <= c->projCacheBytes) return cudaSuccess;
+  // the frames in flight may still read the old cache
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  for (int i = 0; i < 2 && e == cudaSuccess; i++)
+    if (c->pipeStream[i]) e = cudaStreamSynchronize(c->pipeStream[i]);
+  for (uint32_t g = 0; g < BATCH_GROUPS_MAX && e == cudaSuccess; g++)
+    if (c->batchStreams[g]) e = cudaStreamSynchronize(c->batchStreams[g]);
+  if (e != cudaSuccess) return e;
+  if (c->projCache) cudaFree(c->projCache);
+  c->projCache = nullptr;
+  c->projCacheBytes = 0;
+  const size_t bytes = need + need / 4;  // room to grow
+  e = cudaMalloc(&c->projCache, bytes);
+  if (e != cudaSuccess) {
+    c->projCache = nullptr;
+    return e;
+  }
+  c->projCacheBytes = bytes;
+  return cudaSuccess;
 }
 
 namespace {
@@ -454,12 +481,21 @@ cudaError_t frameBatch(HfbCtx* c, HfbInstance* insts, uint32_t n, float* passMs)
   e = cudaEventSynchronize(c->batchCopied[k]);
   if (e != cudaSuccess) { delete[] group; return e; }
   const HfbConfig& cfg = c->cfg;
+  // the frame's projected segments: one region per instance, written by the
+  // tiles pass and read by the fine pass
+  size_t segs = 0;
+  for (uint32_t i = 0; i < n; i++) segs += (size_t)insts[i].hair.strandsCount * (insts[i].hair.pointsPerStrand - 1u);
+  e = ensureProjCache(c, segs);
+  if (e != cudaSuccess) { delete[] group; return e; }
   uint32_t ng[BATCH_GROUPS_MAX] = {};
-  size_t smem = c->simBatchSmem;
+  size_t smem = c->simBatchSmem, segOff = 0;
   for (uint32_t i = 0; i < n; i++) {
     const uint32_t g = group[i];
     char* h = (char*)c->batchHost[k] + (size_t)g * BATCH_BYTES;
-    fillInstance(cfg, insts[i], ((BatchInst*)(h + BATCH_INSTS_OFF))[ng[g]++]);
+    BatchInst& I = ((BatchInst*)(h + BATCH_INSTS_OFF))[ng[g]++];
+    fillInstance(cfg, insts[i], I);
+    I.proj = c->projCache + segOff * SEG_PROJ_VEC4;
+    segOff += (size_t)insts[i].hair.strandsCount * (insts[i].hair.pointsPerStrand - 1u);
     const size_t sb = simSmemBytes(insts[i].hair.pointsPerStrand);
     smem = smem > sb ? smem : sb;
   }
@@ -612,6 +648,9 @@ void frameBatchRelease(HfbCtx* c) {
   if (c->batchDev) cudaFree(c->batchDev);
   c->batchGraph = nullptr;
   c->batchDev = nullptr;
+  if (c->projCache) cudaFree(c->projCache);
+  c->projCache = nullptr;
+  c->projCacheBytes = 0;
 }
 
 }  // namespace hfb

@@ -59,6 +59,10 @@ struct HfbCtx {
   // failed; noallocError then says why)
   void* noallocScratch = nullptr;
   std::string noallocError;
+  // the projected segments of a whole frame (hfb_frame, hfb_frame_batch):
+  // written by the tiles pass, read by the fine pass; grown on demand
+  float4* projCache = nullptr;
+  size_t projCacheBytes = 0;
 };
 
 namespace hfb {
@@ -126,13 +130,18 @@ cudaError_t launchGridPostSim(HfbCtx* c, const HfbSimUniforms& u, const HfbHairD
 cudaError_t launchShading(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, const float* pos,
                           const float* tan, const float* depth, const float* ao, uint32_t aoW,
                           uint32_t aoH, const float* sm, uint32_t smSize, float* shading);
+// proj (NULL = none): per segment, SEG_PROJ_VEC4 float4 of its projection
+// (projectSegment) that the tiles pass writes and the fine pass of the same
+// frame reads instead of projecting again (whole frames only, where the
+// library runs both passes on the same positions and uniforms).
+constexpr uint32_t SEG_PROJ_VEC4 = 3;  // v00, v01 | v10, v11 | depthsProj
 cudaError_t launchTilesPass(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, const float* pos,
                             const float* tan, const float* depth, uint32_t strandsToRender,
-                            HfbRasterBuffers& rb);
+                            HfbRasterBuffers& rb, float4* proj = nullptr);
 cudaError_t launchTileSort(HfbCtx* c, HfbRasterBuffers& rb);
 cudaError_t launchFinePass(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, const float* pos,
                            const float* tan, const float* shading, const float* depth,
-                           HfbRasterBuffers& rb);
+                           HfbRasterBuffers& rb, const float4* proj = nullptr);
 
 __host__ __device__ inline uint32_t divCeil(uint32_t a, uint32_t b) { return (a + b - 1u) / b; }
 __host__ __device__ inline size_t alignUp256(size_t v) { return (v + 255u) & ~size_t(255u); }
@@ -197,6 +206,9 @@ cudaError_t clearRaster(HfbCtx* c, const HfbRasterBuffers& rb);
 // onto the device and makes the array resident; called by hfb_ctx_create.
 // Sets c->noallocScratch, or c->noallocError on failure.
 void noallocPrepare(HfbCtx* c);
+// Makes c->projCache hold at least `segments` projected segments (waits for
+// the context's streams before replacing a smaller one).
+cudaError_t ensureProjCache(HfbCtx* c, size_t segments);
 // Loads the tiles pass's kernels onto the current device (raster.cu).
 cudaError_t tilesPassLoad(HfbCtx* c);
 
@@ -270,6 +282,7 @@ struct alignas(16) BatchInst {
   uint32_t* hdList;           // the hair depth pass's big-triangle list (word 0: count), or NULL
   uint32_t hdCap, pad1;
   const uint32_t* gridOrder;  // strand order of the grid splat, NULL = identity
+  float4* proj;               // the frame's projected segments (SEG_PROJ_VEC4 each), or NULL
 };
 
 // Device layout of a batch: header, prefix rows (fixed stride), the fine

@@ -277,7 +277,7 @@ __device__ __forceinline__ void tilesRasterBody(const HfbUniforms& U, uint32_t P
                                                 uint32_t* __restrict__ segBuf, uint32_t* __restrict__ segCount,
                                                 uint32_t* __restrict__ binCount,
                                                 DeviceCounters* __restrict__ counters, TrShared<TR_SLOTS, TR_CHUNK>& sh,
-                                                uint32_t blk) {
+                                                uint32_t blk, float4* __restrict__ projOut) {
   const uint32_t tid = threadIdx.x, lane = tid & 31u;
   const uint32_t segsPerStrand = P - 1u;
   const uint32_t nSeg = nStrands * segsPerStrand;
@@ -299,6 +299,12 @@ __device__ __forceinline__ void tilesRasterBody(const HfbUniforms& U, uint32_t P
     const uint32_t strand = gid / segsPerStrand, seg = gid - strand * segsPerStrand;
     key = (strand << 8) | seg;
     s = projectSegment(U, pos, tan, P, strand, seg, size);
+    if (projOut) {  // for the fine pass of the same frame
+      float4* o = projOut + (size_t)gid * SEG_PROJ_VEC4;
+      o[0] = make_float4(s.v00.x, s.v00.y, s.v01.x, s.v01.y);
+      o[1] = make_float4(s.v10.x, s.v10.y, s.v11.x, s.v11.y);
+      o[2] = make_float4(s.depthsProj.x, s.depthsProj.y, s.depthsProj.z, s.depthsProj.w);
+    }
     // getRasterizedHairBounds, swRasterizeHair.wgsl.ts:111-124
     const float bx1 = fminf(ceilf(fmaxf(fmaxf(s.v00.x, s.v01.x), fmaxf(s.v10.x, s.v11.x))), size.x);
     const float by1 = fminf(ceilf(fmaxf(fmaxf(s.v00.y, s.v01.y), fmaxf(s.v10.y, s.v11.y))), size.y);
@@ -488,10 +494,10 @@ tilesRasterKernel(const HfbUniforms U, uint32_t P, uint32_t nStrands, uint32_t T
                   uint32_t threshold, float4 bsphere, const float4* __restrict__ pos,
                   const float4* __restrict__ tan, const float* __restrict__ depth, uint4* __restrict__ tiles,
                   uint32_t* __restrict__ segBuf, uint32_t* __restrict__ segCount,
-                  uint32_t* __restrict__ binCount, DeviceCounters* __restrict__ counters) {
+                  uint32_t* __restrict__ binCount, DeviceCounters* __restrict__ counters, float4* __restrict__ proj) {
   __shared__ TrShared<TR_SLOTS, TR_CHUNK> sh;
   tilesRasterBody<TR_SLOTS, TR_CHUNK>(U, P, nStrands, TS, B, threshold, bsphere, pos, tan, depth, tiles, segBuf,
-                                      segCount, binCount, counters, sh, blockIdx.x);
+                                      segCount, binCount, counters, sh, blockIdx.x, proj);
 }
 
 // ---------------------------------------------------------------------------
@@ -862,6 +868,7 @@ struct FineArgs {
   const uint4* __restrict__ tiles;
   const uint32_t* __restrict__ segBuf;
   DeviceCounters* counters;
+  const float4* __restrict__ proj;  // the tiles pass's projected segments (SEG_PROJ_VEC4 each), or NULL
 };
 
 template <int TS>
@@ -999,6 +1006,30 @@ __device__ __forceinline__ uint32_t stageSegment(FineSmem<TS>& sh, uint32_t k, u
   const uint32_t st = sh.strand[k], sg = sh.segIdx[k];
   if (st < S && sg + 1u < P) {  // otherwise not a segment of this hair: covers no pixel
     const ProjSeg s = projectSegment(U, pos, tan, P, st, sg, size);
+    return stageFromProjection<TS>(sh, k, bin, s, stageShade<TS>(sh, k, st, sg, shading, P, SP), x0, y0);
+  }
+  sh.box[k] = EMPTY_BOX;
+  sh.shadeBase[k] = bin << 24;
+  sh.cntEdge[k] = 0;
+  sh.cntFrag[k] = 0;
+  return 0u;
+}
+
+// Stages segment k from its projection in the tiles pass's cache.
+template <int TS>
+__device__ __forceinline__ uint32_t stageCached(FineSmem<TS>& sh, uint32_t k, uint32_t bin,
+                                                const float4* __restrict__ proj, const float4* __restrict__ shading,
+                                                uint32_t S, uint32_t P, uint32_t SP, uint32_t x0, uint32_t y0) {
+  const uint32_t st = sh.strand[k], sg = sh.segIdx[k];
+  if (st < S && sg + 1u < P) {
+    const float4* q = proj + ((size_t)st * (P - 1u) + sg) * SEG_PROJ_VEC4;
+    const float4 a = __ldg(HFB_G(&q[0])), b = __ldg(HFB_G(&q[1])), d = __ldg(HFB_G(&q[2]));
+    ProjSeg s;
+    s.v00 = mk2(a.x, a.y);
+    s.v01 = mk2(a.z, a.w);
+    s.v10 = mk2(b.x, b.y);
+    s.v11 = mk2(b.z, b.w);
+    s.depthsProj = mk4(d.x, d.y, d.z, d.w);
     return stageFromProjection<TS>(sh, k, bin, s, stageShade<TS>(sh, k, st, sg, shading, P, SP), x0, y0);
   }
   sh.box[k] = EMPTY_BOX;
@@ -1324,7 +1355,15 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
       const uint32_t nStaged = sh.nStaged;
 #pragma unroll
       for (uint32_t w = 0; w < STAGE / 32; w++) sh.pixMask[w][tid] = 0u;
-      if constexpr (2u * STAGE <= NT) {
+      if (a.proj) {
+        // the tiles pass projected every segment of the frame already
+        for (uint32_t k = tid; k < nStaged; k += NT) {
+          uint32_t r = 0;
+          while (r + 1u < nRuns && sh.runK0[r + 1u] <= k) r++;
+          sh.pairBase[k] = stageCached<TS>(sh, k, sh.runBin[r] & 0xffu, a.proj, a.shading, a.S, a.P, a.SP, tbp.x0,
+                                           tbp.y0);
+        }
+      } else if constexpr (2u * STAGE <= NT) {
         // two threads per segment: one projects its first point, one its second
         if (tid < 2u * nStaged) {
           const uint32_t end = tid >= nStaged ? 1u : 0u;
@@ -1880,13 +1919,20 @@ fineKernel(const HfbUniforms U, const FineArgs a, const uint32_t* __restrict__ t
   SM& sh = *reinterpret_cast<SM*>(fineSmemRaw);
   const uint32_t nItems = min((*HFB_G(&fs.hdr[0])), fs.maxItems);
   uint32_t* queue = reinterpret_cast<uint32_t*>(result);  // tileQueueAtomicIdx, getNextTileIdx :294-303
+  // The device functions get the uniforms and the arguments from shared
+  // memory, never an address of a kernel parameter (whose generic address
+  // lies in the parameter space, which instructions for global memory
+  // reject: error 717, invalid address space).
+  __shared__ HfbUniforms Us;
+  for (uint32_t w = threadIdx.x; w < sizeof(HfbUniforms) / 4u; w += blockDim.x)
+    reinterpret_cast<uint32_t*>(&Us)[w] = reinterpret_cast<const uint32_t*>(&U)[w];
   if (threadIdx.x == 0) sh.args = a;
   while (true) {
     if (threadIdx.x == 0) sh.queueIdx = atomicAdd(HFB_G(queue), 1u);
     __syncthreads();
     const uint32_t it = sh.queueIdx;
     if (it >= nItems) break;
-    fineItem<TS, MAXL>(sh, U, sh.args, tileList, result, fs, (*HFB_G(&fs.items[it])));
+    fineItem<TS, MAXL>(sh, Us, sh.args, tileList, result, fs, (*HFB_G(&fs.items[it])));
     __syncthreads();  // the tile's shared state is rewritten for the next item
   }
 }
@@ -1916,6 +1962,7 @@ fineBatch(BatchView b, FineArgs base, HfbConfig cfgParam) {
         a.depth = I.depth;
         a.tiles = I.tiles;
         a.segBuf = I.segBuf;
+        a.proj = I.proj;
         sh.args = a;
       }
     }
@@ -1933,7 +1980,8 @@ fineBatch(BatchView b, FineArgs base, HfbConfig cfgParam) {
 
 template <int TS, int MAXL>
 cudaError_t launchFineT(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, const float* pos,
-                        const float* tan, const float* shading, const float* depth, HfbRasterBuffers& rb) {
+                        const float* tan, const float* shading, const float* depth, HfbRasterBuffers& rb,
+                        const float4* proj) {
   HFB_CHECK_BIND(c);
   const HfbConfig& cfg = c->cfg;
   constexpr size_t SMEM = sizeof(FineSmem<TS>);
@@ -1971,6 +2019,7 @@ cudaError_t launchFineT(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, c
   a.tiles = (const uint4*)rb.tiles;
   a.segBuf = rb.tileSegments;
   a.counters = (DeviceCounters*)c->dCounters;
+  a.proj = proj;
   fineKernel<TS, MAXL><<<grid, TS * TS, SMEM, c->stream>>>(u, a, rb.tileList, rb.rasterizerResult, fs);
   HFB_AFTER_LAUNCH(c, "fineKernel");
   c->launches += 2;
@@ -2006,7 +2055,7 @@ __global__ void __launch_bounds__(TR_SEGS, 7) tilesRasterBatch(BatchView b, HfbC
   BATCH_LOOP(BK_RASTER)
     tilesRasterBody<TR_SLOTS_BATCH, TR_CHUNK_BATCH>(I.U, I.P, min(I.strandsToRender, I.S), cfg.tileSize, cfg.tileDepthBins,
                     cfg.invalidTilesPerSegmentThreshold, I.bsphere, I.posNew, I.tan, I.depth, I.tiles, I.segBuf,
-                    I.segCount, ts.binCount, counters, sh, local);
+                    I.segCount, ts.binCount, counters, sh, local, I.proj);
   }
 }
 
@@ -2140,7 +2189,8 @@ cudaError_t launchFineBatchT(HfbCtx* c, const BatchView& b) {
 }  // namespace
 
 cudaError_t launchTilesPass(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, const float* pos,
-                            const float* tan, const float* depth, uint32_t strandsToRender, HfbRasterBuffers& rb) {
+                            const float* tan, const float* depth, uint32_t strandsToRender, HfbRasterBuffers& rb,
+                            float4* proj) {
   HFB_CHECK_BIND(c);
   const HfbConfig& cfg = c->cfg;
   const uint32_t W = rb.width, H = rb.height, TS = cfg.tileSize, B = cfg.tileDepthBins;
@@ -2157,7 +2207,7 @@ cudaError_t launchTilesPass(HfbCtx* c, const HfbUniforms& u, const HfbHairData& 
     float4 bs = make_float4(h.boundingSphere[0], h.boundingSphere[1], h.boundingSphere[2], h.boundingSphere[3]);
     tilesRasterKernel<<<divCeil(nSeg, TR_SEGS), TR_SEGS, 0, c->stream>>>(
         u, h.pointsPerStrand, nStrands, TS, B, cfg.invalidTilesPerSegmentThreshold, bs, (const float4*)pos,
-        (const float4*)tan, depth, (uint4*)rb.tiles, rb.tileSegments, rb.segmentCountPerTile, s.binCount, dc);
+        (const float4*)tan, depth, (uint4*)rb.tiles, rb.tileSegments, rb.segmentCountPerTile, s.binCount, dc, proj);
     HFB_AFTER_LAUNCH(c, "tilesRasterKernel");
   }
   const uint32_t nBlocks = divCeil(TB, SCAN_PER_BLOCK);
@@ -2216,20 +2266,21 @@ cudaError_t launchTileSort(HfbCtx* c, HfbRasterBuffers& rb) {
 }
 
 cudaError_t launchFinePass(HfbCtx* c, const HfbUniforms& u, const HfbHairData& h, const float* pos,
-                           const float* tan, const float* shading, const float* depth, HfbRasterBuffers& rb) {
+                           const float* tan, const float* shading, const float* depth, HfbRasterBuffers& rb,
+                           const float4* proj) {
   const uint32_t TS = c->cfg.tileSize, L = c->cfg.slicesPerPixel;
   if (TS == 8) {
-    if (L <= 4) return launchFineT<8, 4>(c, u, h, pos, tan, shading, depth, rb);
-    if (L <= 8) return launchFineT<8, 8>(c, u, h, pos, tan, shading, depth, rb);
-    return launchFineT<8, 16>(c, u, h, pos, tan, shading, depth, rb);
+    if (L <= 4) return launchFineT<8, 4>(c, u, h, pos, tan, shading, depth, rb, proj);
+    if (L <= 8) return launchFineT<8, 8>(c, u, h, pos, tan, shading, depth, rb, proj);
+    return launchFineT<8, 16>(c, u, h, pos, tan, shading, depth, rb, proj);
   }
   if (TS == 16) {
-    if (L <= 4) return launchFineT<16, 4>(c, u, h, pos, tan, shading, depth, rb);
-    if (L <= 8) return launchFineT<16, 8>(c, u, h, pos, tan, shading, depth, rb);
-    return launchFineT<16, 16>(c, u, h, pos, tan, shading, depth, rb);
+    if (L <= 4) return launchFineT<16, 4>(c, u, h, pos, tan, shading, depth, rb, proj);
+    if (L <= 8) return launchFineT<16, 8>(c, u, h, pos, tan, shading, depth, rb, proj);
+    return launchFineT<16, 16>(c, u, h, pos, tan, shading, depth, rb, proj);
   }
-  if (L <= 4) return launchFineT<32, 4>(c, u, h, pos, tan, shading, depth, rb);
-  if (L <= 8) return launchFineT<32, 8>(c, u, h, pos, tan, shading, depth, rb);
+  if (L <= 4) return launchFineT<32, 4>(c, u, h, pos, tan, shading, depth, rb, proj);
+  if (L <= 8) return launchFineT<32, 8>(c, u, h, pos, tan, shading, depth, rb, proj);
   return cudaErrorInvalidValue;  // 32x32 tiles with more than 8 slices: too many registers per pixel
 }
 
