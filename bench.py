@@ -48,7 +48,7 @@ WORKLOADS = {
     "served256": "256 sessions (strands log-uniform [500, 50k] in 8 levels, 32 points, square viewports of "
                  "log-uniform area [256^2, 2048^2] in 8 levels, own state resident on the device) asking for "
                  "600 frames each as Poisson processes of 2,000 frame requests/s in total, 150 GB "
-                 "device-memory budget, 16 px tiles, 8 depth bins, 4 slices, 8 shading points, 64^3 grids, "
+                 "device-memory budget, 16 px tiles, 16 depth bins, 4 slices, 8 shading points, 64^3 grids, "
                  "32^3 SDF; then a run of 60 frames per session under a budget of a quarter of their memory",
     # one full frame: 10k strands at 1080p
     "plain_full": "10,000 x 32 curly strands, 1920x1080, 16 px tiles, 16 depth bins, 4 slices, "
@@ -89,6 +89,9 @@ def parse():
                          "frames at --tile-size/--depth-bins, no tuning), print 'ok' and exit; no timing")
     ap.add_argument("--capture-sessions", type=int, default=24,
                     help="--capture-frames of served256: how many of its sessions the batch holds")
+    ap.add_argument("--capture-instances", type=int, default=64,
+                    help="--capture-frames of batched64: how many of its instances the batch holds "
+                         "(fewer for a capture with a small device footprint)")
     ap.add_argument("--tfx", help="hair asset (TFX file) of the asset workload")
     ap.add_argument("--sdf", help="binary SDF of the asset workload's head (optional)")
     ap.add_argument("--tile-size", type=int, default=16)
@@ -105,7 +108,7 @@ def capture(args):
     from hairfb.lib import Context
     if args.workload in ("batched64", "served256"):
         if args.workload == "batched64":
-            insts = batched_instances(seed=0)
+            insts = batched_instances(seed=0)[:args.capture_instances]
             pools = [None] * len(insts)
         else:  # the first --capture-sessions sessions of the serving workload
             from hairfb import serve
@@ -672,11 +675,13 @@ def run_batched(args, rank, world, dist):
 def served_config():
     """Pass constants of the serving workload."""
     from hairfb.config import HairConfig
-    return HairConfig(tile_size=16, tile_depth_bins=8, slices_per_pixel=4, shading_points=8, grid_dims=64)
+    # 16 px tiles with 16 depth bins: the fastest of 8/16/32 px x 4-16 bins on both the
+    # sessions of at least 1024^2 and the smaller ones (measured per viewport class)
+    return HairConfig(tile_size=16, tile_depth_bins=16, slices_per_pixel=4, shading_points=8, grid_dims=64)
 
 
 def run_served(frames_per_session, device, seed=0, rate_hz=2000.0, budget_bytes=150 << 30, session_rate_hz=2000.0,
-               lanes=2, tick_budget_ms=5.0, count=256):
+               lanes=2, tick_budget_ms=12.0, count=256):
     """The serving workload: `count` sessions arriving as a Poisson process of
     `session_rate_hz`, admitted under the memory budget; once its state is
     on the device each session asks for `frames_per_session` frames as a
@@ -910,6 +915,12 @@ def main():
         # 256 need, sessions arriving over 4 s, 60 frames each
         sv["budget_binding"] = run_served(60, dev, seed=rank, budget_bytes=sv["peak_bytes"] // 4,
                                           session_rate_hz=64.0)
+        # lower offered rates (30 frames per session each): where the p99 stays within 16.7 ms
+        sv["rate_sweep"] = [{k: (round(v, 2) if isinstance(v, float) else v) for k, v in
+                             run_served(30, dev, seed=rank, rate_hz=hz).items()
+                             if k in ("offered_frames_per_s", "frames_per_s", "request_p50_ms", "request_p99_ms",
+                                      "frames_per_tick", "tick_gpu_p50_ms")}
+                            for hz in (1000.0, 1200.0, 1400.0, 1600.0)]
         from hairfb import replicas
         sv["wall_s"] = replicas.max_over_ranks([sv["wall_s"]], dist, "cuda")[0]
         if rank == 0:

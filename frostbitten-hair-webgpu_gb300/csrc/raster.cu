@@ -854,7 +854,7 @@ constexpr uint32_t FINE_SPLIT_MIN = 256;  // records: tiles below this are never
 
 template <int TS> struct FineDims;
 template <> struct FineDims<8> { static constexpr uint32_t STAGE = 64, PAIRS = 768; };
-template <> struct FineDims<16> { static constexpr uint32_t STAGE = 96, PAIRS = 2048; };
+template <> struct FineDims<16> { static constexpr uint32_t STAGE = 128, PAIRS = 2048; };  // 96: 2-3 % slower, 160: 4 % slower
 template <> struct FineDims<32> { static constexpr uint32_t STAGE = 256, PAIRS = 4096; };
 
 // Shared inputs of the fine pass.
