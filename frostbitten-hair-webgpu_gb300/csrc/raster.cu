@@ -178,9 +178,10 @@ struct TrShared {
       qwe[TR_SEGS], qd22[TR_SEGS];                                      // QuadConst
   uint32_t cx0[TR_SEGS], cy0[TR_SEGS], cw[TR_SEGS];  // candidate rectangle origin and width
   uint32_t tminx[TR_SEGS], tminy[TR_SEGS], tsx[TR_SEGS];
+  float blo[TR_SEGS], bhi[TR_SEGS];  // depth range over which the bin follows from the depth alone
   uint32_t pairBase[TR_SEGS + 1], slotBase[TR_SEGS + 1];
   uint32_t accMin[TR_SLOTS], accMax[TR_SLOTS], accBin[TR_SLOTS];
-  uint32_t pass[TR_CHUNK];  // segment | pair offset << 7
+  uint32_t pass[TR_CHUNK];  // segment | column in the rectangle << 7 | row << 19
   uint32_t warpSums[32];
   uint32_t passCount;
 };
@@ -199,6 +200,43 @@ __device__ __forceinline__ uint32_t viewDepthBin(const HfbUniforms& U, uint32_t 
                                                  float hd) {
   const f3 vs = projectVertex(U.projMatrixInv.m, mk4(p.x, p.y, hd, 1.0f));
   return (B - 1u) - getDepthBin(B, dv0, dv1, vs.z);
+}
+
+// A (segment, tile) record keeps the smallest bin over its passing pixels.
+// When the inverse projection's z row is (0, 0, m10, m14) and its w row
+// (0, 0, m11, m15) -- a perspective or orthographic projection -- a pixel's
+// view depth does not depend on the pixel: for x, y >= 0 the zero entries
+// give signed zeros that the sums absorb, so z = m14 / RN(RN(m11 h) + m15)
+// when |m10 h| stays below a quarter ulp of m14 (the z row then rounds to
+// m14 exactly).  That is a monotone function of the depth h while the
+// denominator keeps one sign, and getDepthBin is monotone in z (u32(NaN)
+// is 0), so the smallest bin over a set of depths is the bin of its smallest
+// or of its largest depth: the record needs two bins, not one per pixel.
+// binRange returns the range [lo, hi] of depths over which that holds for a
+// segment (empty when it does not): its four projected depths widened by
+// 1e-5 of their magnitude -- the interpolated depths, mixes of the four with
+// weights clamped to [0, 1], stay within 1e-6 of it -- checked on both ends.
+__device__ __forceinline__ bool binRowsFromDepth(const float* M) {
+  return (__float_as_uint(M[2]) << 1) == 0u && (__float_as_uint(M[6]) << 1) == 0u &&
+         (__float_as_uint(M[3]) << 1) == 0u && (__float_as_uint(M[7]) << 1) == 0u && M[14] != 0.0f &&
+         M[15] != 0.0f && isfinite(M[10]) && isfinite(M[11]) && isfinite(M[14]) && isfinite(M[15]);
+}
+
+__device__ __forceinline__ void binRange(const float* M, bool rows, f4 dp, float& lo, float& hi) {
+  lo = __int_as_float(0x7f800000);
+  hi = -lo;
+  if (!rows) return;
+  const float a = fminf(fminf(dp.x, dp.y), fminf(dp.z, dp.w)), b = fmaxf(fmaxf(dp.x, dp.y), fmaxf(dp.z, dp.w));
+  const bool finite = isfinite(dp.x) && isfinite(dp.y) && isfinite(dp.z) && isfinite(dp.w);
+  if (!finite || !(fabsf(a) < 1e30f && fabsf(b) < 1e30f)) return;
+  const float m = fadd(fmul(1e-5f, fadd(fabsf(a), fabsf(b))), 1e-30f);
+  const float l = fsub(a, m), h = fadd(b, m);
+  if (!(fmul(fmul(fabsf(M[10]), fmaxf(fabsf(l), fabsf(h))), 1.0001f) < fmul(fabsf(M[14]), 0x1p-26f))) return;
+  const float w0 = fadd(fmul(M[11], l), M[15]), w1 = fadd(fmul(M[11], h), M[15]);
+  if (isfinite(w0) && isfinite(w1) && ((w0 > 0.0f && w1 > 0.0f) || (w0 < 0.0f && w1 < 0.0f))) {
+    lo = l;
+    hi = h;
+  }
 }
 
 // Stores one (segment, tile) record, :220-237 (warp-aggregated pointer
@@ -289,6 +327,8 @@ __device__ __forceinline__ void tilesRasterBody(const HfbUniforms& U, uint32_t P
   // getHairDepthBoundsVS, :242-246
   const f4 bsVS = m4v(U.modelViewMat.m, mk4(bsphere.x, bsphere.y, bsphere.z, 1.0f));
   const float dv0 = fsub(bsVS.z, bsphere.w), dv1 = fadd(bsVS.z, bsphere.w);
+  const bool binRows = binRowsFromDepth(U.projMatrixInv.m);
+  const uint32_t tsShift = (uint32_t)(__ffs((int)TS) - 1);  // TS is 8, 16 or 32
 
   // ---- project this thread's segment ----
   uint32_t pairs = 0, slots = 0, key = 0;
@@ -317,7 +357,7 @@ __device__ __forceinline__ void tilesRasterBody(const HfbUniforms& U, uint32_t P
       const uint32_t cx1 = min(ux1 + 1u, W - 1u), cy1 = min(uy1 + 1u, H - 1u);
       const uint32_t cwid = cx1 > ux0 ? cx1 - ux0 : 0u, chei = cy1 > uy0 ? cy1 - uy0 : 0u;
       if (cwid && chei) {
-        if ((uint64_t)cwid * chei >= (1ull << 24)) {
+        if ((uint64_t)cwid * chei >= (1ull << 24) || cwid > 4096u || chei > 8192u) {
           serial = true;  // beyond the pair encoding: its own walk
         } else {
           pairs = cwid * chei;
@@ -337,6 +377,9 @@ __device__ __forceinline__ void tilesRasterBody(const HfbUniforms& U, uint32_t P
       }
       sh.dp[0][tid] = s.depthsProj.x; sh.dp[1][tid] = s.depthsProj.y;
       sh.dp[2][tid] = s.depthsProj.z; sh.dp[3][tid] = s.depthsProj.w;
+      float blo, bhi;
+      binRange(U.projMatrixInv.m, binRows, s.depthsProj, blo, bhi);
+      sh.blo[tid] = blo; sh.bhi[tid] = bhi;
       const QuadConst q = quadConst(s);
       sh.qsx[tid] = q.sm.x; sh.qsy[tid] = q.sm.y; sh.qax[tid] = q.ab.x; sh.qay[tid] = q.ab.y;
       sh.qd2[tid] = q.d2; sh.qlse[tid] = q.lse; sh.qws[tid] = q.wS; sh.qwe[tid] = q.wE; sh.qd22[tid] = q.d22;
@@ -418,7 +461,7 @@ __device__ __forceinline__ void tilesRasterBody(const HfbUniforms& U, uint32_t P
           if (lane == leader) base = atomicAdd(&sh.passCount, (uint32_t)__popc(bal));
           base = __shfl_sync(0xffffffffu, base, leader);
           const uint32_t at = base + __popc(bal & ((1u << lane) - 1u));
-          if (pass && HFB_EXPECT(at < TR_CHUNK && k < TR_SEGS)) sh.pass[at] = k | ((p - sh.pairBase[k]) << 7);
+          if (pass && HFB_EXPECT(at < TR_CHUNK && k < TR_SEGS)) sh.pass[at] = k | (rx << 7) | (ry << 19);
         }
         if (valid) {
           p++;
@@ -440,9 +483,7 @@ __device__ __forceinline__ void tilesRasterBody(const HfbUniforms& U, uint32_t P
     const uint32_t nPass = sh.passCount;
     for (uint32_t i = tid; i < nPass; i += TR_SEGS) {
       const uint32_t e = sh.pass[i];
-      const uint32_t k = e & 0x7fu, r = e >> 7;
-      const uint32_t w = sh.cw[k];
-      const uint32_t ry = r / w, rx = r - ry * w;
+      const uint32_t k = e & 0x7fu, rx = (e >> 7) & 0xfffu, ry = e >> 19;
       const uint32_t x = sh.cx0[k] + rx, y = sh.cy0[k] + ry;
       const f2 p = mk2((float)x, (float)y);
       QuadConst qc;
@@ -455,9 +496,11 @@ __device__ __forceinline__ void tilesRasterBody(const HfbUniforms& U, uint32_t P
       const float hd = interpolateHairF32(wq, mk4(sh.dp[0][k], sh.dp[1][k], sh.dp[2][k], sh.dp[3][k]));
       const float zb = loadTex2DClamp(depth, W, H, (int)x, (int)H - (int)y);
       if (hd > zb) continue;  // depth test, :193-195
-      const uint32_t slot = sh.slotBase[k] + (y / TS - sh.tminy[k]) * sh.tsx[k] + (x / TS - sh.tminx[k]);
+      const uint32_t slot =
+          sh.slotBase[k] + ((y >> tsShift) - sh.tminy[k]) * sh.tsx[k] + ((x >> tsShift) - sh.tminx[k]);
       if (!HFB_EXPECT(slot < TR_SLOTS)) continue;
-      atomicMin(&sh.accBin[slot], viewDepthBin(U, B, dv0, dv1, p, hd));
+      if (!(hd >= sh.blo[k] && hd <= sh.bhi[k]))  // else the record's bin comes from its depth range (E)
+        atomicMin(&sh.accBin[slot], viewDepthBin(U, B, dv0, dv1, p, hd));
       if (!isnan(hd)) {  // fminf / fmaxf ignore a NaN depth
         atomicMin(&sh.accMin[slot], orderedBits(hd));
         atomicMax(&sh.accMax[slot], orderedBits(hd));
@@ -480,8 +523,14 @@ __device__ __forceinline__ void tilesRasterBody(const HfbUniforms& U, uint32_t P
     const uint32_t ty = sh.tminy[k] + l / sh.tsx[k], tx = sh.tminx[k] + l % sh.tsx[k];
     const uint32_t g = blk * TR_SEGS + k;
     const uint32_t strand = g / segsPerStrand, seg = g - strand * segsPerStrand;
-    storeTileRecord(tiles, segBuf, segCount, binCount, counters, maxDrawn, tilesX, B, tx, ty, sh.accBin[i], dmin,
-                    orderedFloat(sh.accMax[i]), (strand << 8) | seg, tilesX * divCeil(H, TS));
+    const float dmax = orderedFloat(sh.accMax[i]);
+    uint32_t bin = sh.accBin[i];
+    if (sh.blo[k] <= sh.bhi[k]) {  // the smallest bin is at one end of the depths (binRange)
+      const f2 p0 = mk2(0.0f, 0.0f);
+      bin = min(bin, min(viewDepthBin(U, B, dv0, dv1, p0, dmin), viewDepthBin(U, B, dv0, dv1, p0, dmax)));
+    }
+    storeTileRecord(tiles, segBuf, segCount, binCount, counters, maxDrawn, tilesX, B, tx, ty, bin, dmin, dmax,
+                    (strand << 8) | seg, tilesX * divCeil(H, TS));
   }
   if (serial)
     rasterSegmentSerial(U, s, W, H, TS, B, tilesX, maxDrawn, dv0, dv1, key, ux0, uy0, ux1, uy1, depth, tiles,

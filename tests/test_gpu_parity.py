@@ -86,6 +86,27 @@ def test_tiles_pass_bit_exact(oracle, tile, bins):
     _compare_tiles(oracle, inst, fr, rb)
 
 
+@pytest.mark.parametrize("entry,value", [(None, None), (2, 2e-5), (7, -2e-4), (10, 0.05), (10, 1e-12)])
+def test_tiles_pass_bins_for_any_inverse_projection(oracle, entry, value):
+    """The record's depth bin, the smallest over its passing pixels, is taken
+    from the depths' two ends when the inverse projection's z and w rows do
+    not read the pixel (a perspective projection, entry None), and pixel by
+    pixel otherwise: a non-zero x / y entry of those rows, or a depth term
+    in the z row large enough to round into it (entry 10 = 0.05; 1e-12
+    rounds away).  Both give the oracle's bins and lists."""
+    import dataclasses
+    inst = small_instance(strands=1200, tile_size=8, depth_bins=32)
+    fr = frame_of(inst)
+    if entry is not None:
+        u = bytearray(fr.uniforms)
+        off = UN.OFF["projMatrixInv"] + 4 * entry
+        u[off:off + 4] = np.float32(value).tobytes()
+        fr = dataclasses.replace(fr, uniforms=bytes(u))
+    ctx, hair, rb, _ = _raster_gpu(inst, fr)
+    ot, _, _ = _compare_tiles(oracle, inst, fr, rb)
+    assert len(np.unique(np.nonzero(ot[:, 2])[0] % inst.cfg.tile_depth_bins)) > 10, "too few bins in use"
+
+
 def test_tiles_pass_partial_tiles_and_lod(oracle):
     # 1000x700 with 16px tiles leaves partial edge tiles; LOD renders 70%
     inst = small_instance(width=1000, height=700)
