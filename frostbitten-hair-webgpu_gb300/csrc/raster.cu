@@ -404,66 +404,76 @@ __device__ __forceinline__ void tilesRasterBody(const HfbUniforms& U, uint32_t P
   }
   __syncthreads();
 
-  for (uint32_t c0 = 0; c0 < pairTotal; c0 += TR_CHUNK) {
-    const uint32_t n = min(TR_CHUNK, pairTotal - c0);
+  // Each thread walks one contiguous range of the block's pairs.  A round's
+  // A1 appends passing pairs until the list holds TR_CHUNK of them: a thread
+  // whose passing pair finds the list full stops there and retests that pair
+  // in the next round.  A2 then has a full list to share out, and the block
+  // meets at its barriers once per TR_CHUNK passing pixels rather than once
+  // per TR_CHUNK candidate pairs.
+  // edgeFunction (swRasterizeHair.wgsl.ts:128-130) is (x - ox) * ey - (y - oy) * ex: the
+  // second product is the same along a row and is formed once per row (the same values)
+  const uint32_t per = divCeil(pairTotal, TR_SEGS);
+  uint32_t p = tid * per;
+  const uint32_t pEnd = min(p + per, pairTotal);
+  uint32_t k = 0, rx = 0, ry = 0, w = 1, x0 = 0, y0 = 0;
+  float eox[4], eey[4], rowT[4];
+  auto loadSeg = [&](uint32_t kk) {
+    x0 = sh.cx0[kk]; y0 = sh.cy0[kk]; w = sh.cw[kk];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      eox[i] = sh.ox[i][kk]; eey[i] = sh.ey[i][kk];
+    }
+  };
+  auto setRow = [&]() {
+    const float py = (float)(y0 + ry);
+#pragma unroll
+    for (int i = 0; i < 4; i++) rowT[i] = fmul(fsub(py, sh.oy[i][k]), sh.ex[i][k]);
+  };
+  if (p < pEnd) {
+    uint32_t lo = 0, hi = TR_SEGS;  // last k with pairBase[k] <= p
+    while (hi - lo > 1u) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (sh.pairBase[mid] <= p) lo = mid; else hi = mid;
+    }
+    k = lo;
+    loadSeg(k);
+    const uint32_t r = p - sh.pairBase[k];
+    ry = r / w;
+    rx = r - ry * w;
+    setRow();
+  }
+  while (__syncthreads_or(p < pEnd)) {
     if (tid == 0) sh.passCount = 0;
     __syncthreads();
-    // ---- A1: edge tests, contiguous pairs per thread ----
-    {
-      const uint32_t per = divCeil(n, TR_SEGS);
-      uint32_t p = c0 + tid * per;
-      const uint32_t pEnd = min(p + per, c0 + n);
-      uint32_t k = 0, rx = 0, ry = 0, w = 1, x0 = 0, y0 = 0;
-      // edgeFunction (swRasterizeHair.wgsl.ts:128-130) is (x - ox) * ey - (y - oy) * ex: the
-      // second product is the same along a row and is formed once per row (the same values)
-      float eox[4], eey[4], rowT[4];
-      auto loadSeg = [&](uint32_t kk) {
-        x0 = sh.cx0[kk]; y0 = sh.cy0[kk]; w = sh.cw[kk];
+    // ---- A1: edge tests along the thread's range until the list is full ----
+    bool stalled = false;
+    while (true) {
+      const bool act = p < pEnd && !stalled;
+      if (!__any_sync(0xffffffffu, act)) break;
+      bool pass = false;
+      if (act) {
+        const float px = (float)(x0 + rx);
+        pass = true;
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
-          eox[i] = sh.ox[i][kk]; eey[i] = sh.ey[i][kk];
+        for (int i = 0; i < 4; i++) {  // edgeFunction >= 0
+          const float C = fsub(fmul(fsub(px, eox[i]), eey[i]), rowT[i]);
+          pass = pass && C >= 0.0f;
         }
-      };
-      auto setRow = [&]() {
-        const float py = (float)(y0 + ry);
-#pragma unroll
-        for (int i = 0; i < 4; i++) rowT[i] = fmul(fsub(py, sh.oy[i][k]), sh.ex[i][k]);
-      };
-      if (p < pEnd) {
-        uint32_t lo = 0, hi = TR_SEGS;  // last k with pairBase[k] <= p
-        while (hi - lo > 1u) {
-          const uint32_t mid = (lo + hi) >> 1;
-          if (sh.pairBase[mid] <= p) lo = mid; else hi = mid;
-        }
-        k = lo;
-        loadSeg(k);
-        const uint32_t r = p - sh.pairBase[k];
-        ry = r / w;
-        rx = r - ry * w;
-        setRow();
       }
-      for (uint32_t it = 0; it < per; it++) {
-        const bool valid = p < pEnd;
-        bool pass = false;
-        if (valid) {
-          const float px = (float)(x0 + rx);
-          pass = true;
-#pragma unroll
-          for (int i = 0; i < 4; i++) {  // edgeFunction >= 0
-            const float C = fsub(fmul(fsub(px, eox[i]), eey[i]), rowT[i]);
-            pass = pass && C >= 0.0f;
-          }
-        }
-        const uint32_t bal = __ballot_sync(0xffffffffu, pass);
-        if (bal) {
-          const uint32_t leader = (uint32_t)(__ffs(bal) - 1);
-          uint32_t base = 0;
-          if (lane == leader) base = atomicAdd(&sh.passCount, (uint32_t)__popc(bal));
-          base = __shfl_sync(0xffffffffu, base, leader);
-          const uint32_t at = base + __popc(bal & ((1u << lane) - 1u));
-          if (pass && HFB_EXPECT(at < TR_CHUNK && k < TR_SEGS)) sh.pass[at] = k | (rx << 7) | (ry << 19);
-        }
-        if (valid) {
+      const uint32_t bal = __ballot_sync(0xffffffffu, pass);
+      uint32_t at = 0;
+      if (bal) {
+        const uint32_t leader = (uint32_t)(__ffs(bal) - 1);
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(&sh.passCount, (uint32_t)__popc(bal));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        at = base + __popc(bal & ((1u << lane) - 1u));
+      }
+      if (act) {
+        if (pass && at >= TR_CHUNK) {
+          stalled = true;  // the list is full: this pair goes first in the next round
+        } else {
+          if (pass && HFB_EXPECT(k < TR_SEGS)) sh.pass[at] = k | (rx << 7) | (ry << 19);
           p++;
           if (++rx == w) {
             rx = 0;
@@ -480,7 +490,7 @@ __device__ __forceinline__ void tilesRasterBody(const HfbUniforms& U, uint32_t P
     }
     __syncthreads();
     // ---- A2: depth, depth test and bin of every passing pixel ----
-    const uint32_t nPass = sh.passCount;
+    const uint32_t nPass = min(sh.passCount, TR_CHUNK);
     for (uint32_t i = tid; i < nPass; i += TR_SEGS) {
       const uint32_t e = sh.pass[i];
       const uint32_t k = e & 0x7fu, rx = (e >> 7) & 0xfffu, ry = e >> 19;
@@ -506,8 +516,7 @@ __device__ __forceinline__ void tilesRasterBody(const HfbUniforms& U, uint32_t P
         atomicMax(&sh.accMax[slot], orderedBits(hd));
       }
     }
-    __syncthreads();
-  }
+  }  // the loop's barrier ends A2 before the next round and before E
 
   // ---- E: one record per (segment, tile) that took a pixel ----
   for (uint32_t i = tid; i < slotTotal && i < TR_SLOTS; i += TR_SEGS) {

@@ -178,12 +178,15 @@ def _sim_inputs(inst, frame_idx=0):
                                 wind_strength=inst.wind_strength(frame_idx))
 
 
-@pytest.mark.parametrize("maker", ["small", "curly_wind", "many_strands"])
+@pytest.mark.parametrize("maker", ["small", "curly_wind", "many_strands", "odd"])
 def test_grids_and_one_step_bit_exact(oracle, maker):
     """Both integration kernels: warp per strand (moderate strand counts)
-    and thread per strand (many strands)."""
+    and thread per strand (many strands); "odd": 24-point strands that
+    straddle warps and a point count that ends in a partial warp."""
     if maker == "small":
         inst = small_instance()
+    elif maker == "odd":
+        inst = small_instance(strands=1001, points=24)
     elif maker == "many_strands":
         inst = small_instance(strands=24000, points=16, iterations=3)
     else:
@@ -604,6 +607,47 @@ def test_hair_depth_exploded_strands_bit_exact(oracle):
     g = out.cpu().numpy()
     assert (o < inst.scene_depth).sum() > 20000, "the long segments cover little: the case does not test"
     assert np.array_equal(g.view(np.uint32), o.view(np.uint32)), f"{int((g != o).sum())} pixels differ"
+
+
+@pytest.mark.parametrize("tile", [8, 16])
+def test_tiles_and_fine_pass_exploded_strands(oracle, tile):
+    """Points thrown far apart, some of them next to and behind the camera:
+    long segments across many tiles, quads with huge or non-finite projected
+    corners, edges nearly parallel to the rows.  The tiles pass stays
+    bit-exact and the fine pass (whose edge tests list each box row's
+    passing interval) within 1/255."""
+    inst = small_instance(strands=1000, points=16, tile_size=tile, depth_bins=8)
+    fr = frame_of(inst)
+    rng = np.random.default_rng(11)
+    pos = inst.hair.asset.positions.copy()
+    far = rng.random(len(pos)) < 0.05
+    pos[far, :3] += rng.normal(0, 0.3, (int(far.sum()), 3)).astype(np.float32)
+    eye = np.asarray(inst.scene.camera.eye, np.float32)
+    near = np.nonzero(rng.random(len(pos)) < 0.004)[0]
+    pos[near, :3] = eye + rng.normal(0, 0.02, (len(near), 3)).astype(np.float32)
+    hair = HairObject(inst.hair, inst.cfg.shading_points)
+    hair.positions.copy_(torch.as_tensor(pos))
+    ctx, hair, rb, d = _raster_gpu(inst, fr, hair=hair)
+    hb = inst.hair
+    ot, osg, oc = oracle.tiles_pass(inst.cfg, fr.uniforms, hb.hair_data, pos, hb.tangents, inst.scene_depth,
+                                    hb.asset.strands, inst.width, inst.height, fr.max_drawn)
+    gt, gsg = rb.read_tiles(), rb.read_tile_segments()
+    assert int(osg[0]) > 0 and gsg[0] == osg[0] and int(osg[0]) < fr.max_drawn
+    assert np.array_equal(rb.read_segment_counts(), oc)
+    assert np.array_equal(gt[:, :2], ot[:, :2])
+    assert walk_lists(gt, gsg, fr.max_drawn) == walk_lists(ot, osg, fr.max_drawn)
+    shade = _shading_input(inst)
+    hair.shading.copy_(torch.as_tensor(shade))
+    HairFinePass(ctx).cmd_rasterize_slices_hair(fr.uniforms, hair, d, rb)
+    ctx.sync()
+    _, otl = oracle.tile_sort(inst.cfg, inst.width, inst.height, oc)
+    ores = oracle.fine_pass(inst.cfg, fr.uniforms, hb.hair_data, pos, hb.tangents, shade, inst.scene_depth, ot, osg,
+                            otl, inst.width, inst.height)
+    g = rb.read_result()[4:].reshape(-1, 4)
+    o = ores[4:].reshape(-1, 4)
+    assert (o[:, 3] > 0).sum() > 15000, "the frame covers little: the case does not test"
+    assert np.abs(g - o).max() <= 1.0 / 255.0
+    assert np.array_equal(g[:, 3] > 0, o[:, 3] > 0), "coverage differs"
 
 
 @pytest.mark.parametrize("scene", [False, True])
