@@ -905,7 +905,6 @@ tileSortKernel(uint32_t T, uint32_t NB, uint32_t bucketSize, const uint32_t* __r
 // ---------------------------------------------------------------------------
 constexpr uint32_t NSHADE = 4;              // shading entries staged per segment
 constexpr uint32_t MAX_RUNS = 66;           // runs of one round: at most one per depth bin (+1)
-constexpr uint32_t PAIR_NONE = 0xffffffffu; // pair without a fragment
 constexpr uint32_t EMPTY_BOX = 0x0000ffffu; // x0 = y0 = 255 > x1 = y1 = 0
 constexpr uint32_t RUN_ENDS = 1u << 31;
 constexpr uint32_t FINE_SPLIT_MIN = 256;  // records: tiles below this are never split
@@ -936,7 +935,7 @@ struct FineSmem {
   static_assert(2 * 6 * STAGE * sizeof(float) <= PAIRS * sizeof(uint2), "stagePoint's scratch fits in frag");
   float4 shade[STAGE][NSHADE];   // the shading entries each staged segment can sample
   uint2 frag[PAIRS];             // A1: pixel | segment << 16 of a passing pair; A2: its colour as 4 x f16
-  uint32_t pairInfo[PAIRS];      // per pair: fragment index | slice << 16, or PAIR_NONE
+  uint32_t pairInfo[PAIRS];      // per box pair with a fragment (pixMask): fragment index | slice << 16
   // staged segments, one array per quantity (consecutive segments in consecutive banks)
   float ox[4][STAGE], oy[4][STAGE];  // first vertex of the four edge tests: v01, v11, v10, v00
   float ex[4][STAGE], ey[4][STAGE];  // second - first vertex of each edge test
@@ -947,6 +946,7 @@ struct FineSmem {
   uint32_t box[STAGE];               // tile-local pixel box x0 | y0 << 8 | x1 << 16 | y1 << 24
   uint32_t shadeBase[STAGE];         // first staged shading index | count << 16 | depth bin << 24
   uint32_t pairBase[STAGE + 1];      // exclusive prefix of the box areas
+  uint32_t rowBase[STAGE + 1];       // exclusive prefix of the box heights (A1's items)
   uint32_t cntEdge[STAGE], cntFrag[STAGE];
   uint32_t pixMask[STAGE / 32][NT];  // bit k of pixel p: staged segment k left a fragment at p
   // the tile
@@ -1445,23 +1445,30 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
       // exclusive prefix of the areas; the round keeps the longest prefix
       // of segments whose pairs fit
       if (warp == 0) {
-        uint32_t carry = 0, nSeg = nStaged;
+        uint32_t carry = 0, carryRows = 0, nSeg = nStaged;
         for (uint32_t k0 = 0; k0 < nStaged; k0 += 32) {
           const uint32_t k = k0 + lane;
           const uint32_t a = k < nStaged ? sh.pairBase[k] : 0u;
-          uint32_t incl = a;
+          const uint32_t rows = a ? (sh.box[k] >> 24) - ((sh.box[k] >> 8) & 0xffu) + 1u : 0u;
+          uint32_t incl = a, inclRows = rows;
 #pragma unroll
           for (int o = 1; o < 32; o <<= 1) {
             const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= (uint32_t)o) incl += y;
+            const uint32_t yr = __shfl_up_sync(0xffffffffu, inclRows, o);
+            if (lane >= (uint32_t)o) { incl += y; inclRows += yr; }
           }
-          if (k < nStaged) sh.pairBase[k] = carry + incl - a;
+          if (k < nStaged) {
+            sh.pairBase[k] = carry + incl - a;
+            sh.rowBase[k] = carryRows + inclRows - rows;
+          }
           const uint32_t over = __ballot_sync(0xffffffffu, k < nStaged && carry + incl > PAIRS);
           if (over && nSeg == nStaged) nSeg = k0 + (uint32_t)(__ffs(over) - 1);
           carry += __shfl_sync(0xffffffffu, incl, 31);
+          carryRows += __shfl_sync(0xffffffffu, inclRows, 31);
         }
         if (lane == 0) {
           sh.pairBase[nStaged] = carry;
+          sh.rowBase[nStaged] = carryRows;
           sh.passCount = 0;
           if (nSeg < nStaged) {  // drop the segments from nSeg on
             if (tileMode) {
@@ -1481,86 +1488,95 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
     nRuns = sh.nRuns;
     const uint32_t nPairs = sh.pairBase[nSeg];
 
-    // ---------------- A1: edge tests, one thread per pair ----------------
+    // ---------------- A1: edge tests, one thread per (segment, box row) ----------------
+    // A thread tests every pixel of a box row (the row term of edgeFunction,
+    // swRasterizeHair.wgsl.ts:128-130, formed once) into a bit mask, drops the
+    // pixels that are done, and appends the rest with one shared atomic per warp.
     {
-      const uint32_t per = divCeil(nPairs, NT);
-      uint32_t p = tid * per;
-      const uint32_t pEnd = min(p + per, nPairs);
-      uint32_t k = 0, rx = 0, ry = 0, bw = 1, bh = 1, bx0 = 0, by0 = 0, myCnt = 0;
-      // edgeFunction (swRasterizeHair.wgsl.ts:128-130) is (x - ox) * ey - (y - oy) * ex: the
-      // second product is the same along a row and is formed once per row (the same values)
-      float eox[4], eey[4], rowT[4];
+      const uint32_t nRows = sh.rowBase[nSeg];
+      const uint32_t per = divCeil(nRows, NT);
+      uint32_t it0 = tid * per;
+      const uint32_t itEnd = min(it0 + per, nRows);
+      uint32_t k = 0, ry = 0, myCnt = 0, bx0 = 0, bx1 = 0, by0 = 0, bh = 0;
+      float eox[4], eey[4];
       auto loadSeg = [&](uint32_t kk) {
         const uint32_t bx = sh.box[kk];
         bx0 = bx & 0xffu;
         by0 = (bx >> 8) & 0xffu;
-        bw = ((bx >> 16) & 0xffu) - bx0 + 1u;
+        bx1 = (bx >> 16) & 0xffu;
         bh = (bx >> 24) - by0 + 1u;
 #pragma unroll
         for (int i = 0; i < 4; i++) {
           eox[i] = sh.ox[i][kk]; eey[i] = sh.ey[i][kk];
         }
       };
-      auto setRow = [&]() {
-        const float py = (float)(tbp.y0 + by0 + ry);
-#pragma unroll
-        for (int i = 0; i < 4; i++) rowT[i] = fmul(fsub(py, sh.oy[i][k]), sh.ex[i][k]);
-      };
-      if (p < pEnd) {
-        uint32_t lo = 0, hi = nSeg;  // last k with pairBase[k] <= p
+      if (it0 < itEnd) {
+        uint32_t lo = 0, hi = nSeg;  // last k with rowBase[k] <= it0
         while (hi - lo > 1u) {
           const uint32_t mid = (lo + hi) >> 1;
-          if (sh.pairBase[mid] <= p) lo = mid; else hi = mid;
+          if (sh.rowBase[mid] <= it0) lo = mid; else hi = mid;
         }
         k = lo;
         loadSeg(k);
-        const uint32_t r = p - sh.pairBase[k];
-        ry = r / bw;
-        rx = r - ry * bw;
-        setRow();
+        ry = it0 - sh.rowBase[k];
       }
       for (uint32_t it = 0; it < per; it++) {
-        const bool valid = p < pEnd;
-        bool pass = false;
-        uint32_t pix = 0;
+        const bool valid = it0 < itEnd;
+        uint32_t live = 0, rowPix = 0;
         if (valid) {
-          const uint32_t qx = bx0 + rx, qy = by0 + ry;
-          pix = qy * TS + qx;
-          if (!((sh.doneMask[pix >> 5] >> (pix & 31u)) & 1u)) {
+          const uint32_t qy = by0 + ry;
+          const float py = (float)(tbp.y0 + qy);
+          float rowT[4];
+#pragma unroll
+          for (int i = 0; i < 4; i++) rowT[i] = fmul(fsub(py, sh.oy[i][k]), sh.ex[i][k]);
+          uint32_t bits = 0;
+#pragma unroll
+          for (uint32_t qx = 0; qx < (uint32_t)TS; qx++) {
+            if (qx < bx0 || qx > bx1) continue;
             const float px = (float)(tbp.x0 + qx);
-            pass = true;
+            bool pass = true;
 #pragma unroll
             for (int i = 0; i < 4; i++) {  // edgeFunction >= 0
               const float C = fsub(fmul(fsub(px, eox[i]), eey[i]), rowT[i]);
               pass = pass && C >= 0.0f;
             }
+            bits |= pass ? 1u << qx : 0u;
           }
-          sh.pairInfo[p] = PAIR_NONE;
+          rowPix = qy * TS;
+          const uint32_t rowDone = (sh.doneMask[rowPix >> 5] >> (rowPix & 31u)) &
+                                   (TS == 32 ? 0xffffffffu : ((1u << (TS & 31)) - 1u));
+          live = bits & ~rowDone;
         }
-        const uint32_t bal = __ballot_sync(0xffffffffu, pass);
-        if (bal) {
-          const uint32_t leader = (uint32_t)(__ffs(bal) - 1);
+        // warp-aggregated append of the row's pixels
+        const uint32_t n = (uint32_t)__popc(live);
+        uint32_t incl = n;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= (uint32_t)o) incl += y;
+        }
+        const uint32_t warpTotal = __shfl_sync(0xffffffffu, incl, 31);
+        if (warpTotal) {
           uint32_t base = 0;
-          if (lane == leader) base = atomicAdd(&sh.passCount, (uint32_t)__popc(bal));
-          base = __shfl_sync(0xffffffffu, base, leader);
-          if (pass) sh.frag[base + __popc(bal & ((1u << lane) - 1u))].x = pix | (k << 16);
+          if (lane == 31) base = atomicAdd(&sh.passCount, warpTotal);
+          base = __shfl_sync(0xffffffffu, base, 31) + incl - n;
+          while (live) {
+            const uint32_t qx = (uint32_t)(__ffs(live) - 1);
+            live &= live - 1u;
+            if (HFB_EXPECT(base < PAIRS)) sh.frag[base].x = (rowPix + qx) | (k << 16);
+            base++;
+          }
         }
-        myCnt += pass ? 1u : 0u;
+        myCnt += n;
         if (valid) {
-          p++;
-          if (++rx == bw) {
-            rx = 0;
-            if (++ry == bh) {  // segment done
-              if (myCnt) atomicAdd(&sh.cntEdge[k], myCnt);
-              myCnt = 0;
-              if (p < pEnd) {
-                while (sh.pairBase[k + 1u] <= p) k++;  // next segment with pairs
-                loadSeg(k);
-                ry = 0;
-                setRow();
-              }
-            } else if (p < pEnd) {
-              setRow();
+          it0++;
+          if (++ry == bh) {  // segment done
+            if (myCnt) atomicAdd(&sh.cntEdge[k], myCnt);
+            myCnt = 0;
+            if (it0 < itEnd) {
+              while (sh.rowBase[k + 1u] <= it0) k++;  // next segment with rows
+              loadSeg(k);
+              ry = 0;
             }
           }
         }
@@ -1695,10 +1711,13 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
       __syncthreads();
       const uint32_t cut = sh.cutSeg;
       if (cut != INVALID_PTR) {  // slots of the filling segment in pixel order
-        const uint32_t base = sh.pairBase[cut], area = sh.pairBase[cut + 1u] - base;
-        const bool has = tid < area && sh.pairInfo[base + tid] != PAIR_NONE;
+        const uint32_t b = sh.box[cut], bxa = b & 0xffu, bya = (b >> 8) & 0xffu;
+        const uint32_t bw = ((b >> 16) & 0xffu) - bxa + 1u, area = sh.pairBase[cut + 1u] - sh.pairBase[cut];
+        const uint32_t pix = tid < area ? (bya + tid / bw) * TS + bxa + tid % bw : 0u;
+        const uint32_t bit = 1u << (cut & 31u);
+        const bool has = tid < area && (sh.pixMask[cut >> 5][pix] & bit) != 0u;
         const uint32_t rank = blockExclusive<NW>(has ? 1u : 0u, sh.red, lane, warp);
-        if (has && rank >= sh.cutSlots) sh.pairInfo[base + tid] = PAIR_NONE;
+        if (has && rank >= sh.cutSlots) sh.pixMask[cut >> 5][pix] &= ~bit;  // the pool is full
         __syncthreads();
       }
       nSeg = sh.nSeg;
@@ -1719,7 +1738,7 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
             const uint32_t bx0 = b & 0xffu, by0 = (b >> 8) & 0xffu;
             const uint32_t info =
                 sh.pairInfo[sh.pairBase[j] + (ly - by0) * (((b >> 16) & 0xffu) - bx0 + 1u) + (lx - bx0)];
-            if (info != PAIR_NONE && HFB_EXPECT((info & 0xffffu) < PAIRS)) {  // not dropped by a full pool
+            if (HFB_EXPECT((info & 0xffffu) < PAIRS)) {
               blendFragment<MAXL>(acc, info >> 16, sh.frag[info & 0xffffu]);
               nFrag++;
               pending++;
