@@ -181,9 +181,9 @@ struct TrShared {
   float blo[TR_SEGS], bhi[TR_SEGS];  // depth range over which the bin follows from the depth alone
   uint32_t pairBase[TR_SEGS + 1], slotBase[TR_SEGS + 1];
   uint32_t accMin[TR_SLOTS], accMax[TR_SLOTS], accBin[TR_SLOTS];
-  uint32_t pass[TR_CHUNK];  // segment | column in the rectangle << 7 | row << 19
+  uint32_t pass[TR_CHUNK];  // segment | column in the rectangle << 7 | row << 19, one region per warp
   uint32_t warpSums[32];
-  uint32_t passCount;
+  uint32_t regionCount[TR_SEGS / 32];  // entries in each warp's region of pass
 };
 
 // order-preserving u32 image of a float (NaN excluded by the caller)
@@ -405,13 +405,16 @@ __device__ __forceinline__ void tilesRasterBody(const HfbUniforms& U, uint32_t P
   __syncthreads();
 
   // Each thread walks one contiguous range of the block's pairs.  A round's
-  // A1 appends passing pairs until the list holds TR_CHUNK of them: a thread
-  // whose passing pair finds the list full stops there and retests that pair
-  // in the next round.  A2 then has a full list to share out, and the block
-  // meets at its barriers once per TR_CHUNK passing pixels rather than once
-  // per TR_CHUNK candidate pairs.
+  // A1 appends passing pairs to its warp's region of the list (a count kept
+  // in registers: no atomic) until a region is full; the warp then stops,
+  // its lanes at the pairs they have not yet appended, which the next round
+  // retests.  A2 then has a full list to share out, and the block meets at
+  // its barriers about once per TR_CHUNK passing pixels rather than once per
+  // TR_CHUNK candidate pairs.
   // edgeFunction (swRasterizeHair.wgsl.ts:128-130) is (x - ox) * ey - (y - oy) * ex: the
   // second product is the same along a row and is formed once per row (the same values)
+  constexpr uint32_t REGION = TR_CHUNK / (TR_SEGS / 32);
+  const uint32_t warp = tid >> 5;
   const uint32_t per = divCeil(pairTotal, TR_SEGS);
   uint32_t p = tid * per;
   const uint32_t pEnd = min(p + per, pairTotal);
@@ -443,12 +446,11 @@ __device__ __forceinline__ void tilesRasterBody(const HfbUniforms& U, uint32_t P
     setRow();
   }
   while (__syncthreads_or(p < pEnd)) {
-    if (tid == 0) sh.passCount = 0;
-    __syncthreads();
-    // ---- A1: edge tests along the thread's range until the list is full ----
-    bool stalled = false;
-    while (true) {
-      const bool act = p < pEnd && !stalled;
+    // ---- A1: edge tests along the thread's range until the warp's region is full ----
+    uint32_t* const region = sh.pass + warp * REGION;
+    uint32_t cnt = 0;  // the warp's entries (the same in every lane)
+    while (cnt < REGION) {
+      const bool act = p < pEnd;
       if (!__any_sync(0xffffffffu, act)) break;
       bool pass = false;
       if (act) {
@@ -461,38 +463,39 @@ __device__ __forceinline__ void tilesRasterBody(const HfbUniforms& U, uint32_t P
         }
       }
       const uint32_t bal = __ballot_sync(0xffffffffu, pass);
-      uint32_t at = 0;
-      if (bal) {
-        const uint32_t leader = (uint32_t)(__ffs(bal) - 1);
-        uint32_t base = 0;
-        if (lane == leader) base = atomicAdd(&sh.passCount, (uint32_t)__popc(bal));
-        base = __shfl_sync(0xffffffffu, base, leader);
-        at = base + __popc(bal & ((1u << lane) - 1u));
-      }
-      if (act) {
-        if (pass && at >= TR_CHUNK) {
-          stalled = true;  // the list is full: this pair goes first in the next round
-        } else {
-          if (pass && HFB_EXPECT(k < TR_SEGS)) sh.pass[at] = k | (rx << 7) | (ry << 19);
-          p++;
-          if (++rx == w) {
-            rx = 0;
-            ry++;
-            if (p < pEnd && p >= sh.pairBase[k + 1u]) {  // next segment with pairs
-              while (sh.pairBase[k + 1u] <= p) k++;
-              loadSeg(k);
-              ry = 0;
-            }
-            if (p < pEnd) setRow();
+      const uint32_t at = cnt + __popc(bal & ((1u << lane) - 1u));
+      const bool fits = !pass || at < REGION;  // else the region is full: the pair goes first next round
+      if (pass && fits && HFB_EXPECT(k < TR_SEGS)) region[at] = k | (rx << 7) | (ry << 19);
+      cnt = min(cnt + (uint32_t)__popc(bal), REGION);
+      if (act && fits) {
+        p++;
+        if (++rx == w) {
+          rx = 0;
+          ry++;
+          if (p < pEnd && p >= sh.pairBase[k + 1u]) {  // next segment with pairs
+            while (sh.pairBase[k + 1u] <= p) k++;
+            loadSeg(k);
+            ry = 0;
           }
+          if (p < pEnd) setRow();
         }
       }
     }
+    if (lane == 0) sh.regionCount[warp] = cnt;
     __syncthreads();
     // ---- A2: depth, depth test and bin of every passing pixel ----
-    const uint32_t nPass = min(sh.passCount, TR_CHUNK);
+    uint32_t rc[TR_SEGS / 32], nPass = 0;
+#pragma unroll
+    for (uint32_t r = 0; r < TR_SEGS / 32; r++) {
+      rc[r] = sh.regionCount[r];
+      nPass += rc[r];
+    }
     for (uint32_t i = tid; i < nPass; i += TR_SEGS) {
-      const uint32_t e = sh.pass[i];
+      uint32_t r = 0, o = i;  // entry i of the regions laid end to end
+#pragma unroll
+      for (uint32_t q = 0; q + 1u < TR_SEGS / 32; q++)
+        if (r == q && o >= rc[q]) { o -= rc[q]; r++; }
+      const uint32_t e = sh.pass[r * REGION + o];
       const uint32_t k = e & 0x7fu, rx = (e >> 7) & 0xfffu, ry = e >> 19;
       const uint32_t x = sh.cx0[k] + rx, y = sh.cy0[k] + ry;
       const f2 p = mk2((float)x, (float)y);
