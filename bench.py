@@ -7,9 +7,9 @@ SimIntegration -> GridPostSim -> clear -> Tiles -> TileSort -> Fine ->
 Shading (src/renderer.ts:171-295 order).  ``value`` is device-timed
 frames/s with every input resident in HBM; the L2 is flushed (a 256 MiB
 write) between timed frames, outside the timed events.  ``e2e`` is the same
-metric through the public API with the per-frame inputs (both uniform blocks
-and the scene depth buffer) copied from pinned host memory and the frame's
-image (the rasterizer result) read back every step.
+metric through the public API with the per-frame inputs (both uniform blocks,
+and for one instance the scene depth buffer) copied from pinned host memory
+and the frame's presented RGBA8 image (hfb_present) read back every step.
 
 Under torchrun each rank renders its own instance (replicas, weak scaling):
 value = frames of all ranks / max over ranks of the timed region.
@@ -409,10 +409,15 @@ def run_ours(args, rank, world, dist):
     records = (ctx.counters()["tileRecords"] - rec0) / args.steps
     total_s = sum(frame_ms) / 1000.0
 
-    # ---- e2e through the public API with host buffers ----
+    # ---- e2e through the public API with host buffers: the scene depth and
+    # both uniform blocks up, the frame, then the presented image (hfb_present:
+    # the hair over a black scene, tone mapped to RGBA8, what the reference
+    # presents) down to pinned host memory ----
     from hairfb import uniforms as UN
+    from hairfb.lib import byref, ptr
     depth_h = torch.from_numpy(inst.scene_depth).pin_memory()
-    img_h = torch.empty(4 + 4 * inst.width * inst.height, dtype=torch.float32).pin_memory()
+    img_h = torch.empty(4 * inst.width * inst.height, dtype=torch.uint8).pin_memory()
+    img_d = torch.empty(4 * inst.width * inst.height, dtype=torch.uint8, device="cuda")
     depth_d = torch.empty_like(depth_h, device="cuda")
     e2e_ms = []
     for k in range(args.warmup + args.steps):
@@ -435,13 +440,15 @@ def run_ours(args, rank, world, dist):
         r.hw_hair.cmd_draw_hair_depth(u, r.hair, depth_d, r.hair_depth, r.rb)
         r.shading.cmd_compute_shading_points(u, r.hair, r.shading_depth)
         r.frame_idx += 1
-        ctx.call("hfb_buffer_download", img_h.data_ptr(), r.rb.rb.rasterizerResult, img_h.numel() * 4)
+        ub = ctypes.cast(ctypes.c_char_p(u), ctypes.c_void_p)
+        ctx.call("hfb_present", ub, byref(r.rb.rb), None, ptr(img_d))
+        img_h.copy_(img_d, non_blocking=True)
         t1.record(stream)
         torch.cuda.synchronize()
         if k >= args.warmup:
             e2e_ms.append(t0.elapsed_time(t1))
     h2d = depth_h.numel() * 4 + UN.RENDER_UNIFORMS_BYTES + UN.SIM_UNIFORMS_BYTES
-    d2h = img_h.numel() * 4
+    d2h = img_h.numel()
 
     out = dict(frame_ms=frame_ms, pass_ms=pass_ms, total_s=total_s, launches=launches, records=records,
                e2e_ms=e2e_ms, h2d=h2d, d2h=d2h, clocks=clk.summary(), inst=inst)
@@ -1009,7 +1016,10 @@ def main():
                                  "apart after a few frames on the reference's i32 density arithmetic"}
                       if wl in FROM_REST else {})},
         "e2e": {"value": world * len(res["e2e_ms"]) / e2e_total, "unit": "frames/s",
-                "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"]},
+                "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"],
+                "what": "per frame: the scene depth and both uniform blocks from pinned host memory, the "
+                        "passes through the public calls, hfb_present, the RGBA8 image to pinned host "
+                        "memory; CUDA events around each frame"},
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
                      "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                      "algorithmic_bytes": alg[dominant]},
