@@ -206,12 +206,25 @@ class ServeStats:
     tick_gpu_ms: list[float]
     first_request_s: float = 0.0
     last_done_s: float = 0.0
+    done_s: list = dataclasses.field(default_factory=list)  # per frame: when the host saw it complete
+    all_active_s: float = 0.0      # the last session started asking for frames
+    first_finished_s: float = 0.0  # the first session had all its frames
 
     @property
     def frames_per_s(self) -> float:
         """Frames over the time from the first request to the last frame."""
         span = self.last_done_s - self.first_request_s
         return self.frames / span if span > 0 else 0.0
+
+    @property
+    def steady_frames_per_s(self) -> float:
+        """Frames completed per second while every session was asking for
+        frames (from the last session's first request to the first
+        session's last frame): the rate at the full offered load."""
+        t0, t1 = self.all_active_s, self.first_finished_s
+        if not t1 > t0:
+            return 0.0
+        return sum(1 for t in self.done_s if t0 <= t <= t1) / (t1 - t0)
 
     def pct(self, q: float, which: str = "latency_ms") -> float:
         v = sorted(getattr(self, which))
@@ -395,7 +408,8 @@ class Server:
         active: list[Session] = []        # ready: issuing requests
         heap: list = []                   # (next request time, sid, session)
         ticks: list[Tick | None] = [None] * len(self.ctxs)
-        lat, waits, tick_ms = [], [], []
+        lat, waits, tick_ms, done_t = [], [], [], []
+        all_active, first_finished = 0.0, math.inf
         n_ticks = frames = peak_sessions = peak_bytes = admitting = 0
         first_req, last_done = math.inf, 0.0
         d0 = sum(c.counters()["tileRecordsDropped"] for c in self.ctxs)
@@ -424,6 +438,7 @@ class Server:
                     self.cost.add(tk.units[0], tk.units[1], ms)
                     for s, a in zip(tk.sessions, tk.arrivals):
                         lat.append(1000.0 * (now - a))
+                        done_t.append(now)
                         last_done = max(last_done, now)
                         s.busy = False
                         s.done += 1
@@ -432,6 +447,7 @@ class Server:
                             frame_done(s)
                         if s.done >= s.spec.frames:
                             s.finished_s = now
+                            first_finished = min(first_finished, now)
                             self.retire(s)
                             active.remove(s)
                             remaining -= 1
@@ -445,6 +461,7 @@ class Server:
                 if s.ready_ev.query():
                     s.ready_s = time.perf_counter() - t0
                     s.offsets = s.ready_s + request_times(s.spec, per, seed)
+                    all_active = max(all_active, float(s.offsets[0]))
                     heapq.heappush(heap, (float(s.offsets[0]), s.spec.sid, s))
                     loading.remove(s)
                     active.append(s)
@@ -488,6 +505,9 @@ class Server:
                         len(self.ctxs), per * len(specs), frames / max(1, n_ticks), tick_ms)
         st.first_request_s = first_req if math.isfinite(first_req) else 0.0
         st.last_done_s = last_done
+        st.done_s = done_t
+        st.all_active_s = all_active
+        st.first_finished_s = first_finished if math.isfinite(first_finished) else 0.0
         return st
 
     def close(self) -> None:

@@ -48,6 +48,19 @@ def test_cost_model_fits_tick_times():
 
 
 @pytest.mark.gpu
+def test_steady_rate_counts_the_window_where_every_session_asks():
+    """steady_frames_per_s: frames completed between the last session's first
+    request and the first session's last frame, per second of that window."""
+    st = serve.ServeStats(frames=7, wall_s=10.0, ticks=7, latency_ms=[1.0] * 7, admit_wait_ms=[0.0],
+                          peak_sessions=2, peak_bytes=0, budget_bytes=1, dropped=0, lanes=1, offered_hz=2.0,
+                          frames_per_tick=1.0, tick_gpu_ms=[1.0] * 7)
+    st.done_s = [0.5, 1.5, 2.0, 2.5, 3.0, 3.5, 9.0]
+    st.all_active_s, st.first_finished_s = 1.0, 3.0
+    assert st.steady_frames_per_s == pytest.approx(4 / 2.0)
+    st.first_finished_s = 0.5  # no window: a session finished before the last one started
+    assert st.steady_frames_per_s == 0.0
+
+
 def test_served_sessions_equal_sessions_alone():
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
