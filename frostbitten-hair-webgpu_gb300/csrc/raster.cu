@@ -20,6 +20,7 @@
 // The resulting lists are canonical: they do not depend on atomic order.
 #include <cooperative_groups.h>
 #include <cuda_fp16.h>
+#include <type_traits>
 
 #define HFB_TU 3
 #include "hfb_internal.cuh"
@@ -1405,7 +1406,10 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
         }
       }
     }
-    __syncthreads();
+    // In tile mode the runs were published at the barrier above and each thread
+    // projects the segments it staged itself (the cached and the one-thread-per-
+    // segment projections): no barrier is needed before the projection.
+    if (!(tileMode && (a.proj != nullptr || 2u * STAGE > NT))) __syncthreads();
     uint32_t nRuns = sh.nRuns;
     if (nRuns == 0u) break;  // tile mode: no depth bin left
     const bool fresh = sh.runOff[0] == 0u;  // run 0 starts its bin
@@ -1448,27 +1452,45 @@ __device__ __forceinline__ bool fineTile(FineSmem<TS>& sh, const HfbUniforms& U,
       // exclusive prefix of the areas; the round keeps the longest prefix
       // of segments whose pairs fit
       if (warp == 0) {
-        uint32_t carry = 0, carryRows = 0, nSeg = nStaged;
-        for (uint32_t k0 = 0; k0 < nStaged; k0 += 32) {
-          const uint32_t k = k0 + lane;
+        // the box areas (high half) and heights (low half) scanned together, all chunks of
+        // 32 segments at once (independent shuffle chains); the halves cannot carry into each
+        // other: at most STAGE * TS * TS and STAGE * TS, below 2^16 up to 16 px tiles
+        using V = std::conditional_t<(TS <= 16), uint32_t, unsigned long long>;
+        constexpr uint32_t SH = TS <= 16 ? 16u : 32u, NC = STAGE / 32u;
+        constexpr V LOW = ((V)1 << SH) - 1u;
+        V val[NC], incl[NC];
+#pragma unroll
+        for (uint32_t c = 0; c < NC; c++) {
+          const uint32_t k = c * 32u + lane;
           const uint32_t a = k < nStaged ? sh.pairBase[k] : 0u;
           const uint32_t rows = a ? (sh.box[k] >> 24) - ((sh.box[k] >> 8) & 0xffu) + 1u : 0u;
-          uint32_t incl = a, inclRows = rows;
-#pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-            const uint32_t yr = __shfl_up_sync(0xffffffffu, inclRows, o);
-            if (lane >= (uint32_t)o) { incl += y; inclRows += yr; }
-          }
-          if (k < nStaged) {
-            sh.pairBase[k] = carry + incl - a;
-            sh.rowBase[k] = carryRows + inclRows - rows;
-          }
-          const uint32_t over = __ballot_sync(0xffffffffu, k < nStaged && carry + incl > PAIRS);
-          if (over && nSeg == nStaged) nSeg = k0 + (uint32_t)(__ffs(over) - 1);
-          carry += __shfl_sync(0xffffffffu, incl, 31);
-          carryRows += __shfl_sync(0xffffffffu, inclRows, 31);
+          val[c] = ((V)a << SH) | rows;
+          incl[c] = val[c];
         }
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+          for (uint32_t c = 0; c < NC; c++) {
+            const V y = __shfl_up_sync(0xffffffffu, incl[c], o);
+            if (lane >= (uint32_t)o) incl[c] += y;
+          }
+        }
+        V carryBoth = 0;
+        uint32_t nSeg = nStaged;
+#pragma unroll
+        for (uint32_t c = 0; c < NC; c++) {
+          const uint32_t k = c * 32u + lane;
+          const V ex = carryBoth + incl[c] - val[c];
+          if (k < nStaged) {
+            sh.pairBase[k] = (uint32_t)(ex >> SH);
+            sh.rowBase[k] = (uint32_t)(ex & LOW);
+          }
+          const uint32_t over =
+              __ballot_sync(0xffffffffu, k < nStaged && (uint32_t)((carryBoth + incl[c]) >> SH) > PAIRS);
+          if (over && nSeg == nStaged) nSeg = c * 32u + (uint32_t)(__ffs(over) - 1);
+          carryBoth += __shfl_sync(0xffffffffu, incl[c], 31);
+        }
+        const uint32_t carry = (uint32_t)(carryBoth >> SH), carryRows = (uint32_t)(carryBoth & LOW);
         if (lane == 0) {
           sh.pairBase[nStaged] = carry;
           sh.rowBase[nStaged] = carryRows;
