@@ -207,6 +207,7 @@ class ServeStats:
     first_request_s: float = 0.0
     last_done_s: float = 0.0
     done_s: list = dataclasses.field(default_factory=list)  # per frame: when the host saw it complete
+    arrival_s: list = dataclasses.field(default_factory=list)  # per frame: when its request arrived
     all_active_s: float = 0.0      # the last session started asking for frames
     first_finished_s: float = 0.0  # the first session had all its frames
 
@@ -225,6 +226,15 @@ class ServeStats:
         if not t1 > t0:
             return 0.0
         return sum(1 for t in self.done_s if t0 <= t <= t1) / (t1 - t0)
+
+    def steady_pct(self, q: float) -> float:
+        """Latency percentile (ms) of the requests that arrived and completed
+        while every session was asking for frames (the steady window of
+        steady_frames_per_s): the start, when sessions are still being
+        admitted, and the end, when they retire, are left out."""
+        t0, t1 = self.all_active_s, self.first_finished_s
+        v = sorted(l for l, a, d in zip(self.latency_ms, self.arrival_s, self.done_s) if a >= t0 and d <= t1)
+        return v[min(len(v) - 1, int(round(q * (len(v) - 1))))] if v else 0.0
 
     def pct(self, q: float, which: str = "latency_ms") -> float:
         v = sorted(getattr(self, which))
@@ -408,7 +418,7 @@ class Server:
         active: list[Session] = []        # ready: issuing requests
         heap: list = []                   # (next request time, sid, session)
         ticks: list[Tick | None] = [None] * len(self.ctxs)
-        lat, waits, tick_ms, done_t = [], [], [], []
+        lat, waits, tick_ms, done_t, arr_t = [], [], [], [], []
         all_active, first_finished = 0.0, math.inf
         n_ticks = frames = peak_sessions = peak_bytes = admitting = 0
         first_req, last_done = math.inf, 0.0
@@ -439,6 +449,7 @@ class Server:
                     for s, a in zip(tk.sessions, tk.arrivals):
                         lat.append(1000.0 * (now - a))
                         done_t.append(now)
+                        arr_t.append(a)
                         last_done = max(last_done, now)
                         s.busy = False
                         s.done += 1
@@ -506,6 +517,7 @@ class Server:
         st.first_request_s = first_req if math.isfinite(first_req) else 0.0
         st.last_done_s = last_done
         st.done_s = done_t
+        st.arrival_s = arr_t
         st.all_active_s = all_active
         st.first_finished_s = first_finished if math.isfinite(first_finished) else 0.0
         return st

@@ -57,8 +57,12 @@ def test_steady_rate_counts_the_window_where_every_session_asks():
     st.done_s = [0.5, 1.5, 2.0, 2.5, 3.0, 3.5, 9.0]
     st.all_active_s, st.first_finished_s = 1.0, 3.0
     assert st.steady_frames_per_s == pytest.approx(4 / 2.0)
+    st.latency_ms = [9.0, 1.0, 2.0, 3.0, 4.0, 5.0, 9.0]
+    st.arrival_s = [0.4, 1.4, 1.9, 2.4, 2.9, 2.9, 8.0]
+    # the window holds the requests that arrived at or after 1.0 and completed by 3.0
+    assert st.steady_pct(0.0) == 1.0 and st.steady_pct(1.0) == 4.0
     st.first_finished_s = 0.5  # no window: a session finished before the last one started
-    assert st.steady_frames_per_s == 0.0
+    assert st.steady_frames_per_s == 0.0 and st.steady_pct(0.99) == 0.0
 
 
 def test_served_sessions_equal_sessions_alone():
