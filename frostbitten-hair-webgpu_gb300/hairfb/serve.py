@@ -38,6 +38,7 @@ from __future__ import annotations
 import collections
 import ctypes
 import dataclasses
+import gc
 import heapq
 import math
 import queue
@@ -404,12 +405,19 @@ class Server:
         worker.start()
         switch = sys.getswitchinterval()
         sys.setswitchinterval(1e-4)  # the loop gets the interpreter back quickly from the admission thread
+        # no garbage-collector pauses inside the request loop (its objects are freed by
+        # reference counting; one collection runs after it)
+        collecting = gc.isenabled()
+        gc.disable()
         try:
             return self._serve(specs, per, seed, frame_done, todo, loaded)
         finally:
             todo.put(None)
             worker.join()
             sys.setswitchinterval(switch)
+            if collecting:
+                gc.enable()
+                gc.collect()
 
     def _serve(self, specs, per, seed, frame_done, todo, loaded) -> ServeStats:
         pending = collections.deque(sorted(specs, key=lambda sp: sp.arrival_s))
