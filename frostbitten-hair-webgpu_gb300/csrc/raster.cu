@@ -152,9 +152,10 @@ __device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* war
 // ([0, W - 1) x [0, H - 1): getTileBoundsPx clamps the tile ends to W - 1 /
 // H - 1), each belonging to tile (x / TS, y / TS).  The block then runs:
 //   A1  one thread per (segment, candidate pixel) pair: the edge tests;
-//       passing pairs are appended to a list;
+//       passing pairs are appended to the warp's region of a list;
 //   A2  one thread per passing pixel: interpolated depth, the depth test
-//       against the scene, the view-space depth bin, folded into the
+//       against the scene and, where the bin does not follow from the depth
+//       range (binRange), the view-space depth bin, folded into the
 //       (segment, tile) accumulators with shared-memory atomics (min / max
 //       over an order-preserving u32 image of the depth, min of the bin):
 //       the result does not depend on the order;
@@ -164,7 +165,7 @@ __device__ __forceinline__ uint32_t blockExclusiveScan(uint32_t v, uint32_t* war
 // own thread, tile by tile (rasterSegmentSerial).
 // ---------------------------------------------------------------------------
 constexpr uint32_t TR_SEGS = TILES_RASTER_SEGS;  // segments (and threads) per block
-// (segment, tile) accumulators per block and pairs per A1 / A2 round: the
+// (segment, tile) accumulators per block and list entries per A1 / A2 round: the
 // single-instance kernel keeps more of a large frame's long segments in
 // shared memory (768, 2,048: 6 CTAs per SM); the batched one, whose
 // instances are smaller, trades them for a seventh CTA (512, 1,024).
@@ -883,9 +884,10 @@ tileSortKernel(uint32_t T, uint32_t NB, uint32_t bucketSize, const uint32_t* __r
 // hairFinePass.wgsl.ts:205-288).  Their lists are staged in rounds of up to
 // STAGE segments -- short bins share a round, a long bin spans several -- and
 // each round runs in three phases:
-//   A1  one thread per (segment, pixel of the segment's tile-local bounding
-//       box) pair: the four edge tests of processHairSegment (:5-20); the
-//       passing pairs are appended to a list;
+//   A1  one thread per (segment, row of the segment's tile-local bounding
+//       box): the four edge tests of processHairSegment (:5-20) on every
+//       pixel of the row into a bit mask; the passing pixels that are not
+//       done are appended to a list, one shared atomic per warp;
 //   A2  one thread per passing pair: segment-space interpolation, the depth
 //       test and the fragment colour (:21-53), rounded through f16 like
 //       pack2x16float (hairSlicesDataBuffer.ts:50-63);
