@@ -225,7 +225,7 @@ uint32_t batchBlocks(const HfbConfig& cfg, BatchKind k, const BatchInst& I) {
       const uint32_t v = divCeil(nSeg, 1024u);
       return v < 1u ? 1u : (v > 256u ? 256u : v);
     }
-    case BK_FINALIZE: return divCeil(TB, 8u);
+    case BK_FINALIZE: return divCeil(TB, 32u);  // a warp takes 4 consecutive bins
     case BK_LARGE: return 16u;
     case BK_SORT: return 1u;
     case BK_SCHEDULE: return 1u;

@@ -14,8 +14,9 @@
 //                    order independent.
 //   2. binScan       exclusive prefix of the per-(tile, bin) record counts.
 //   3. binScatter    counting-sort scatter of the record keys into CSR order.
-//   4. binFinalize   one warp per (tile, bin): sort its keys ascending and
-//                    write the reference's linked list (head -> largest key).
+//   4. binFinalize   sort each (tile, bin)'s keys ascending and write the
+//                    reference's linked list (head -> largest key): 8 lanes
+//                    per bin of at most 8 records, a warp per larger bin.
 //   5. largeBins     one CTA per bin with more than 1024 records.
 // The resulting lists are canonical: they do not depend on atomic order.
 #include <cooperative_groups.h>
@@ -660,49 +661,80 @@ __device__ __forceinline__ void binFinalizeBody(uint32_t TB, const uint32_t* __r
                                                 uint32_t* __restrict__ largeBins, uint32_t (*smem)[MEDIUM_BIN],
                                                 uint32_t blk, uint32_t nblk) {
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t grp = lane >> 3, gl = lane & 7u;  // four groups of 8 lanes
   const uint32_t gw = (blk * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nw = (nblk * blockDim.x) >> 5;
+  const uint32_t drawn = (*HFB_G(&segBuf[0]));
   uint32_t* s = smem[warp];
-  for (uint32_t ti = gw; ti < TB; ti += nw) {
-    const uint32_t n = (*HFB_G(&binCount[ti]));
-    if (n == 0) continue;
-    const uint32_t end = (*HFB_G(&blockSums[ti / SCAN_PER_BLOCK])) + (*HFB_G(&binOffset[ti]));  // cursor ended at bin end
-    const uint32_t start = end - n;
-    if (!HFB_EXPECT(n <= end && end <= (*HFB_G(&segBuf[0])))) continue;
-    if (n <= SMALL_BIN) {
-      uint32_t v = lane < n ? (*HFB_G(&keys[start + lane])) : 0xffffffffu;
-      // bitonic sort across the warp, ascending
+  // A warp takes 4 consecutive bins: a group of 8 lanes sorts and links a bin
+  // of at most 8 records (most bins), the whole warp each larger bin.
+  for (uint32_t base = gw * 4u; base < TB; base += nw * 4u) {
+    const uint32_t tg = base + grp;
+    uint32_t ng = 0, endg = 0;
+    if (tg < TB) {
+      ng = (*HFB_G(&binCount[tg]));
+      if (ng) endg = (*HFB_G(&blockSums[tg / SCAN_PER_BLOCK])) + (*HFB_G(&binOffset[tg]));  // bin end
+    }
+    const bool ok = ng != 0u && HFB_EXPECT(ng <= endg && endg <= drawn);
+    const bool small = ok && ng <= 8u;
+    const uint32_t smallLanes = __ballot_sync(0xffffffffu, small);
+    if (small) {
+      const uint32_t start = endg - ng;
+      uint32_t v = gl < ng ? (*HFB_G(&keys[start + gl])) : 0xffffffffu;
+      // bitonic sort across the group's 8 lanes, ascending
 #pragma unroll
-      for (uint32_t k = 2; k <= 32; k <<= 1) {
+      for (uint32_t k = 2; k <= 8; k <<= 1) {
 #pragma unroll
         for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-          uint32_t o = __shfl_xor_sync(0xffffffffu, v, j);
-          bool asc = (lane & k) == 0, low = (lane & j) == 0;
+          const uint32_t o = __shfl_xor_sync(smallLanes, v, j);
+          const bool asc = (gl & k) == 0, low = (gl & j) == 0;
           v = (asc == low) ? min(v, o) : max(v, o);
         }
       }
-      if (lane < n) writeList(segBuf, tiles, ti, start, lane, n, v);
-    } else if (n <= MEDIUM_BIN) {
-      uint32_t N = 64;
-      while (N < n) N <<= 1;
-      for (uint32_t i = lane; i < N; i += 32) s[i] = i < n ? (*HFB_G(&keys[start + i])) : 0xffffffffu;
-      __syncwarp();
-      for (uint32_t k = 2; k <= N; k <<= 1) {
-        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-          for (uint32_t c = lane; c < N / 2; c += 32) {
-            uint32_t a = 2u * j * (c / j) + (c % j), b = a + j;
-            uint32_t x = s[a], y = s[b];
-            bool asc = (a & k) == 0;
-            if ((x > y) == asc) { s[a] = y; s[b] = x; }
+      if (gl < ng) writeList(segBuf, tiles, tg, start, gl, ng, v);
+    }
+    uint32_t bigs = __ballot_sync(0xffffffffu, ok && !small && gl == 0u);  // one bit per group
+    while (bigs) {
+      const uint32_t src = (uint32_t)(__ffs(bigs) - 1);
+      bigs &= bigs - 1u;
+      const uint32_t ti = base + (src >> 3);
+      const uint32_t n = __shfl_sync(0xffffffffu, ng, src), end = __shfl_sync(0xffffffffu, endg, src);
+      const uint32_t start = end - n;
+      if (n <= SMALL_BIN) {
+        uint32_t v = lane < n ? (*HFB_G(&keys[start + lane])) : 0xffffffffu;
+        // bitonic sort across the warp, ascending
+#pragma unroll
+        for (uint32_t k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+          for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            uint32_t o = __shfl_xor_sync(0xffffffffu, v, j);
+            bool asc = (lane & k) == 0, low = (lane & j) == 0;
+            v = (asc == low) ? min(v, o) : max(v, o);
           }
-          __syncwarp();
         }
+        if (lane < n) writeList(segBuf, tiles, ti, start, lane, n, v);
+      } else if (n <= MEDIUM_BIN) {
+        uint32_t N = 64;
+        while (N < n) N <<= 1;
+        for (uint32_t i = lane; i < N; i += 32) s[i] = i < n ? (*HFB_G(&keys[start + i])) : 0xffffffffu;
+        __syncwarp();
+        for (uint32_t k = 2; k <= N; k <<= 1) {
+          for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t c = lane; c < N / 2; c += 32) {
+              uint32_t a = 2u * j * (c / j) + (c % j), b = a + j;
+              uint32_t x = s[a], y = s[b];
+              bool asc = (a & k) == 0;
+              if ((x > y) == asc) { s[a] = y; s[b] = x; }
+            }
+            __syncwarp();
+          }
+        }
+        for (uint32_t i = lane; i < n; i += 32) writeList(segBuf, tiles, ti, start, i, n, s[i]);
+        __syncwarp();
+      } else if (lane == 0) {
+        uint32_t slot = atomicAdd(HFB_G(&largeBins[0]), 1u);
+        (*HFB_G(&largeBins[1u + slot])) = ti;
       }
-      for (uint32_t i = lane; i < n; i += 32) writeList(segBuf, tiles, ti, start, i, n, s[i]);
-      __syncwarp();
-    } else if (lane == 0) {
-      uint32_t slot = atomicAdd(HFB_G(&largeBins[0]), 1u);
-      (*HFB_G(&largeBins[1u + slot])) = ti;
     }
   }
 }
@@ -2322,7 +2354,7 @@ cudaError_t launchTilesPass(HfbCtx* c, const HfbUniforms& u, const HfbHairData& 
   binScatterKernel<<<c->smCount * 4, 256, 0, c->stream>>>(rb.tileSegments, rb.maxDrawnSegments, s.binOffset,
                                                           s.blockSums, s.keys, dc, TB);
   HFB_AFTER_LAUNCH(c, "binScatterKernel");
-  binFinalizeKernel<<<min(divCeil(TB, 8), (uint32_t)c->smCount * 16), 256, 0, c->stream>>>(
+  binFinalizeKernel<<<min(divCeil(TB, 32), (uint32_t)c->smCount * 16), 256, 0, c->stream>>>(
       TB, s.binCount, s.binOffset, s.blockSums, s.keys, rb.tileSegments, (uint4*)rb.tiles, s.largeBins);
   HFB_AFTER_LAUNCH(c, "binFinalizeKernel");
   if (!c->largeBinsAttrSet) {
