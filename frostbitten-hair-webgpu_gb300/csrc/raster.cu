@@ -15,8 +15,9 @@
 //   2. binScan       exclusive prefix of the per-(tile, bin) record counts.
 //   3. binScatter    counting-sort scatter of the record keys into CSR order.
 //   4. binFinalize   sort each (tile, bin)'s keys ascending and write the
-//                    reference's linked list (head -> largest key): 8 lanes
-//                    per bin of at most 8 records, a warp per larger bin.
+//                    reference's linked list (head -> largest key): a warp
+//                    per bin (single instance); in the batched frame 8 lanes
+//                    per bin of at most 8 records and a warp per larger bin.
 //   5. largeBins     one CTA per bin with more than 1024 records.
 // The resulting lists are canonical: they do not depend on atomic order.
 #include <cooperative_groups.h>
@@ -654,22 +655,91 @@ __device__ __forceinline__ void writeList(uint32_t* __restrict__ segBuf, uint4* 
   }
 }
 
+// Sorts and links the larger bin ti (more than 8 records) with the whole warp.
+__device__ __forceinline__ void finalizeBinWarp(uint32_t ti, uint32_t n, uint32_t start, uint32_t lane,
+                                                uint32_t* __restrict__ keys, uint32_t* __restrict__ segBuf,
+                                                uint4* __restrict__ tiles, uint32_t* __restrict__ largeBins,
+                                                uint32_t* s) {
+  if (n <= SMALL_BIN) {
+    uint32_t v = lane < n ? (*HFB_G(&keys[start + lane])) : 0xffffffffu;
+    // bitonic sort across the warp, ascending
+#pragma unroll
+    for (uint32_t k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+      for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+        uint32_t o = __shfl_xor_sync(0xffffffffu, v, j);
+        bool asc = (lane & k) == 0, low = (lane & j) == 0;
+        v = (asc == low) ? min(v, o) : max(v, o);
+      }
+    }
+    if (lane < n) writeList(segBuf, tiles, ti, start, lane, n, v);
+  } else if (n <= MEDIUM_BIN) {
+    uint32_t N = 64;
+    while (N < n) N <<= 1;
+    for (uint32_t i = lane; i < N; i += 32) s[i] = i < n ? (*HFB_G(&keys[start + i])) : 0xffffffffu;
+    __syncwarp();
+    for (uint32_t k = 2; k <= N; k <<= 1) {
+      for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+        for (uint32_t c = lane; c < N / 2; c += 32) {
+          uint32_t a = 2u * j * (c / j) + (c % j), b = a + j;
+          uint32_t x = s[a], y = s[b];
+          bool asc = (a & k) == 0;
+          if ((x > y) == asc) { s[a] = y; s[b] = x; }
+        }
+        __syncwarp();
+      }
+    }
+    for (uint32_t i = lane; i < n; i += 32) writeList(segBuf, tiles, ti, start, i, n, s[i]);
+    __syncwarp();
+  } else if (lane == 0) {
+    uint32_t slot = atomicAdd(HFB_G(&largeBins[0]), 1u);
+    (*HFB_G(&largeBins[1u + slot])) = ti;
+  }
+}
+
+// One warp per bin, the warps of the grid striding over the bins (the
+// single-instance launch: a fixed grid, where spreading the larger bins over
+// every warp keeps the tail short).
+__device__ __forceinline__ void binFinalizeWarpBody(uint32_t TB, const uint32_t* __restrict__ binCount,
+                                                    const uint32_t* __restrict__ binOffset,
+                                                    const uint32_t* __restrict__ blockSums,
+                                                    uint32_t* __restrict__ keys, uint32_t* __restrict__ segBuf,
+                                                    uint4* __restrict__ tiles, uint32_t* __restrict__ largeBins,
+                                                    uint32_t (*smem)[MEDIUM_BIN], uint32_t blk, uint32_t nblk) {
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t gw = (blk * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nw = (nblk * blockDim.x) >> 5;
+  const uint32_t drawn = (*HFB_G(&segBuf[0]));
+  for (uint32_t ti = gw; ti < TB; ti += nw) {
+    const uint32_t n = (*HFB_G(&binCount[ti]));
+    if (n == 0) continue;
+    const uint32_t end = (*HFB_G(&blockSums[ti / SCAN_PER_BLOCK])) + (*HFB_G(&binOffset[ti]));  // bin end
+    if (!HFB_EXPECT(n <= end && end <= drawn)) continue;
+    finalizeBinWarp(ti, n, end - n, lane, keys, segBuf, tiles, largeBins, smem[warp]);
+  }
+}
+
+// A block takes 32 consecutive bins at a time (blockDim 256: 8 warps of 4
+// bins): a group of 8 lanes sorts and links a bin of at most 8 records (most
+// bins), the larger ones go to a block queue that the warps then share, one
+// warp per bin.  All threads of the block call it.  (The batched launch,
+// whose persistent blocks take these 32-bin pieces dynamically.)
 __device__ __forceinline__ void binFinalizeBody(uint32_t TB, const uint32_t* __restrict__ binCount,
                                                 const uint32_t* __restrict__ binOffset,
                                                 const uint32_t* __restrict__ blockSums, uint32_t* __restrict__ keys,
                                                 uint32_t* __restrict__ segBuf, uint4* __restrict__ tiles,
                                                 uint32_t* __restrict__ largeBins, uint32_t (*smem)[MEDIUM_BIN],
                                                 uint32_t blk, uint32_t nblk) {
-  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  __shared__ uint32_t bigTi[32], bigN[32], bigEnd[32], nBig;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nWarps = blockDim.x >> 5;
   const uint32_t grp = lane >> 3, gl = lane & 7u;  // four groups of 8 lanes
-  const uint32_t gw = (blk * blockDim.x + threadIdx.x) >> 5;
-  const uint32_t nw = (nblk * blockDim.x) >> 5;
+  const uint32_t perBlock = nWarps * 4u;
   const uint32_t drawn = (*HFB_G(&segBuf[0]));
   uint32_t* s = smem[warp];
-  // A warp takes 4 consecutive bins: a group of 8 lanes sorts and links a bin
-  // of at most 8 records (most bins), the whole warp each larger bin.
-  for (uint32_t base = gw * 4u; base < TB; base += nw * 4u) {
-    const uint32_t tg = base + grp;
+  for (uint32_t bbase = blk * perBlock; bbase < TB; bbase += nblk * perBlock) {
+    if (threadIdx.x == 0) nBig = 0;
+    __syncthreads();
+    const uint32_t tg = bbase + warp * 4u + grp;
     uint32_t ng = 0, endg = 0;
     if (tg < TB) {
       ng = (*HFB_G(&binCount[tg]));
@@ -692,50 +762,17 @@ __device__ __forceinline__ void binFinalizeBody(uint32_t TB, const uint32_t* __r
         }
       }
       if (gl < ng) writeList(segBuf, tiles, tg, start, gl, ng, v);
+    } else if (ok && gl == 0u) {
+      const uint32_t q = atomicAdd(&nBig, 1u);  // < 32: one per group of the block
+      bigTi[q] = tg;
+      bigN[q] = ng;
+      bigEnd[q] = endg;
     }
-    uint32_t bigs = __ballot_sync(0xffffffffu, ok && !small && gl == 0u);  // one bit per group
-    while (bigs) {
-      const uint32_t src = (uint32_t)(__ffs(bigs) - 1);
-      bigs &= bigs - 1u;
-      const uint32_t ti = base + (src >> 3);
-      const uint32_t n = __shfl_sync(0xffffffffu, ng, src), end = __shfl_sync(0xffffffffu, endg, src);
-      const uint32_t start = end - n;
-      if (n <= SMALL_BIN) {
-        uint32_t v = lane < n ? (*HFB_G(&keys[start + lane])) : 0xffffffffu;
-        // bitonic sort across the warp, ascending
-#pragma unroll
-        for (uint32_t k = 2; k <= 32; k <<= 1) {
-#pragma unroll
-          for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-            uint32_t o = __shfl_xor_sync(0xffffffffu, v, j);
-            bool asc = (lane & k) == 0, low = (lane & j) == 0;
-            v = (asc == low) ? min(v, o) : max(v, o);
-          }
-        }
-        if (lane < n) writeList(segBuf, tiles, ti, start, lane, n, v);
-      } else if (n <= MEDIUM_BIN) {
-        uint32_t N = 64;
-        while (N < n) N <<= 1;
-        for (uint32_t i = lane; i < N; i += 32) s[i] = i < n ? (*HFB_G(&keys[start + i])) : 0xffffffffu;
-        __syncwarp();
-        for (uint32_t k = 2; k <= N; k <<= 1) {
-          for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-            for (uint32_t c = lane; c < N / 2; c += 32) {
-              uint32_t a = 2u * j * (c / j) + (c % j), b = a + j;
-              uint32_t x = s[a], y = s[b];
-              bool asc = (a & k) == 0;
-              if ((x > y) == asc) { s[a] = y; s[b] = x; }
-            }
-            __syncwarp();
-          }
-        }
-        for (uint32_t i = lane; i < n; i += 32) writeList(segBuf, tiles, ti, start, i, n, s[i]);
-        __syncwarp();
-      } else if (lane == 0) {
-        uint32_t slot = atomicAdd(HFB_G(&largeBins[0]), 1u);
-        (*HFB_G(&largeBins[1u + slot])) = ti;
-      }
-    }
+    __syncthreads();
+    const uint32_t nb = nBig;
+    for (uint32_t q = warp; q < nb; q += nWarps)
+      finalizeBinWarp(bigTi[q], bigN[q], bigEnd[q] - bigN[q], lane, keys, segBuf, tiles, largeBins, s);
+    __syncthreads();  // the queue is rewritten by the next 32 bins
   }
 }
 
@@ -744,7 +781,8 @@ binFinalizeKernel(uint32_t TB, const uint32_t* __restrict__ binCount, const uint
                   const uint32_t* __restrict__ blockSums, uint32_t* __restrict__ keys,
                   uint32_t* __restrict__ segBuf, uint4* __restrict__ tiles, uint32_t* __restrict__ largeBins) {
   __shared__ uint32_t smem[8][MEDIUM_BIN];
-  binFinalizeBody(TB, binCount, binOffset, blockSums, keys, segBuf, tiles, largeBins, smem, blockIdx.x, gridDim.x);
+  binFinalizeWarpBody(TB, binCount, binOffset, blockSums, keys, segBuf, tiles, largeBins, smem, blockIdx.x,
+                      gridDim.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -2354,7 +2392,7 @@ cudaError_t launchTilesPass(HfbCtx* c, const HfbUniforms& u, const HfbHairData& 
   binScatterKernel<<<c->smCount * 4, 256, 0, c->stream>>>(rb.tileSegments, rb.maxDrawnSegments, s.binOffset,
                                                           s.blockSums, s.keys, dc, TB);
   HFB_AFTER_LAUNCH(c, "binScatterKernel");
-  binFinalizeKernel<<<min(divCeil(TB, 32), (uint32_t)c->smCount * 16), 256, 0, c->stream>>>(
+  binFinalizeKernel<<<min(divCeil(TB, 8), (uint32_t)c->smCount * 16), 256, 0, c->stream>>>(
       TB, s.binCount, s.binOffset, s.blockSums, s.keys, rb.tileSegments, (uint4*)rb.tiles, s.largeBins);
   HFB_AFTER_LAUNCH(c, "binFinalizeKernel");
   if (!c->largeBinsAttrSet) {
