@@ -655,6 +655,67 @@ __device__ __forceinline__ void writeList(uint32_t* __restrict__ segBuf, uint4* 
   }
 }
 
+// Bitonic sorting network (Batcher) on N keys in shared memory, ascending, N a
+// power of two >= 64.  Stage (k, j) compares the keys at x and x + j for every
+// x with bit j clear, ascending where bit k of x is clear.  The stages with
+// j <= 32 stay inside aligned runs of 64 keys: a warp holds such a run in
+// registers (positions p and p + 32 in lane p % 32; the j = 32 exchange within
+// a lane, j <= 16 across lanes by shuffles) and runs all of them between two
+// passes over shared memory.
+
+// The j <= 32 stages of the merge steps k = kFrom .. kTo (doubling) on every
+// 64-key run; the caller's warps warp0, warp0 + nWarps, ... take the runs.
+__device__ __forceinline__ void bitonicRuns64(uint32_t* s, uint32_t N, uint32_t kFrom, uint32_t kTo, uint32_t lane,
+                                              uint32_t warp0, uint32_t nWarps) {
+  for (uint32_t r = warp0; r < N / 64u; r += nWarps) {
+    const uint32_t p0 = r * 64u + lane, p1 = p0 + 32u;
+    uint32_t e0 = s[p0], e1 = s[p1];
+    for (uint32_t k = kFrom; k <= kTo; k <<= 1) {
+      uint32_t j = k >> 1;
+      if (j >= 32u) {
+        const bool asc = (p0 & k) == 0u;
+        const uint32_t lo = min(e0, e1), hi = max(e0, e1);
+        e0 = asc ? lo : hi;
+        e1 = asc ? hi : lo;
+        j = 16u;
+      }
+      for (; j > 0u; j >>= 1) {
+        const uint32_t o0 = __shfl_xor_sync(0xffffffffu, e0, j), o1 = __shfl_xor_sync(0xffffffffu, e1, j);
+        const bool low = (lane & j) == 0u;
+        e0 = (((p0 & k) == 0u) == low) ? min(e0, o0) : max(e0, o0);
+        e1 = (((p1 & k) == 0u) == low) ? min(e1, o1) : max(e1, o1);
+      }
+    }
+    s[p0] = e0;
+    s[p1] = e1;
+  }
+}
+
+// Sorts s[0, N).  BLOCK: every thread of the block calls it (block barriers);
+// else one warp does (warp barriers).
+template <bool BLOCK>
+__device__ __forceinline__ void bitonicSort(uint32_t* s, uint32_t N) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t t0 = BLOCK ? threadIdx.x : lane, nT = BLOCK ? blockDim.x : 32u;
+  const uint32_t w0 = BLOCK ? threadIdx.x >> 5 : 0u, nW = BLOCK ? blockDim.x >> 5 : 1u;
+  auto sync = [] { if (BLOCK) __syncthreads(); else __syncwarp(); };
+  bitonicRuns64(s, N, 2u, 64u, lane, w0, nW);
+  sync();
+  for (uint32_t k = 128u; k <= N; k <<= 1) {
+    for (uint32_t j = k >> 1; j >= 64u; j >>= 1) {
+      const uint32_t lj = __ffs(j) - 1u;  // j = 2^lj
+      for (uint32_t c = t0; c < N / 2u; c += nT) {
+        const uint32_t a = ((c >> lj) << (lj + 1u)) | (c & (j - 1u)), b = a + j;
+        const uint32_t x = s[a], y = s[b];
+        if ((x > y) == ((a & k) == 0u)) { s[a] = y; s[b] = x; }
+      }
+      sync();
+    }
+    bitonicRuns64(s, N, k, k, lane, w0, nW);
+    sync();
+  }
+}
+
 // Sorts and links the larger bin ti (more than 8 records) with the whole warp.
 __device__ __forceinline__ void finalizeBinWarp(uint32_t ti, uint32_t n, uint32_t start, uint32_t lane,
                                                 uint32_t* __restrict__ keys, uint32_t* __restrict__ segBuf,
@@ -678,17 +739,7 @@ __device__ __forceinline__ void finalizeBinWarp(uint32_t ti, uint32_t n, uint32_
     while (N < n) N <<= 1;
     for (uint32_t i = lane; i < N; i += 32) s[i] = i < n ? (*HFB_G(&keys[start + i])) : 0xffffffffu;
     __syncwarp();
-    for (uint32_t k = 2; k <= N; k <<= 1) {
-      for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-        for (uint32_t c = lane; c < N / 2; c += 32) {
-          uint32_t a = 2u * j * (c / j) + (c % j), b = a + j;
-          uint32_t x = s[a], y = s[b];
-          bool asc = (a & k) == 0;
-          if ((x > y) == asc) { s[a] = y; s[b] = x; }
-        }
-        __syncwarp();
-      }
-    }
+    bitonicSort<false>(s, N);
     for (uint32_t i = lane; i < n; i += 32) writeList(segBuf, tiles, ti, start, i, n, s[i]);
     __syncwarp();
   } else if (lane == 0) {
@@ -786,8 +837,9 @@ binFinalizeKernel(uint32_t TB, const uint32_t* __restrict__ binCount, const uint
 }
 
 // ---------------------------------------------------------------------------
-// 5. largeBins: one CTA per bin with > MEDIUM_BIN records.  Runs of
-//    LARGE_SMEM_KEYS are bitonic-sorted in shared memory, then merged pairwise
+// 5. largeBins: one CTA per bin with > MEDIUM_BIN records.  A bin of at most
+//    LARGE_SMEM_KEYS records is bitonic-sorted in shared memory and linked
+//    from there; a larger one in runs of LARGE_SMEM_KEYS, then merged pairwise
 //    through the bin's own list slots (free until the final write) by rank
 //    search (keys are unique).
 // ---------------------------------------------------------------------------
@@ -808,22 +860,19 @@ __device__ __forceinline__ void largeBinsBody(const uint32_t* __restrict__ large
     // sort runs in shared memory
     for (uint32_t r0 = 0; r0 < n; r0 += LARGE_SMEM_KEYS) {
       uint32_t m = min(LARGE_SMEM_KEYS, n - r0);
-      uint32_t N = 2;
+      uint32_t N = 64;
       while (N < m) N <<= 1;
       for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) sk[i] = i < m ? (*HFB_G(&a[r0 + i])) : 0xffffffffu;
       __syncthreads();
-      for (uint32_t k = 2; k <= N; k <<= 1)
-        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-          for (uint32_t c = threadIdx.x; c < N / 2; c += blockDim.x) {
-            uint32_t x0 = 2u * j * (c / j) + (c % j), x1 = x0 + j;
-            uint32_t x = sk[x0], y = sk[x1];
-            bool asc = (x0 & k) == 0;
-            if ((x > y) == asc) { sk[x0] = y; sk[x1] = x; }
-          }
-          __syncthreads();
-        }
+      bitonicSort<true>(sk, N);
+      if (m == n) break;  // one run: the list is written from shared memory below
       for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) (*HFB_G(&a[r0 + i])) = sk[i];
       __syncthreads();
+    }
+    if (n <= LARGE_SMEM_KEYS) {
+      for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) writeList(segBuf, tiles, ti, start, i, n, sk[i]);
+      __syncthreads();
+      continue;
     }
     // merge passes (ping-pong between a and tmp)
     uint32_t* src = a;

@@ -172,7 +172,8 @@ __global__ void __launch_bounds__(256) gridPreSimKernel(const HfbSimUniforms u, 
 // over the block's own points of the PREV buffer -- each thread reads its
 // point's previous position first, and nothing else reads those addresses
 // until the final positions overwrite them -- and the segment lengths are
-// read from their buffer; the chains prefetch both a step ahead.  A block of
+// read from their buffer, four at a time where a strand's row is 16-byte
+// aligned; the chains load both ahead of the steps that use them.  A block of
 // 128 threads holds 2,048 points (64 strands of 32, 128 of 16), six blocks
 // per SM: 384 strands of 32 points in flight per SM, three chain warps per
 // scheduler.
@@ -262,6 +263,25 @@ __device__ __forceinline__ void sdfPush(float4& pos, const f3 q, float d, const 
   }
 }
 
+// One step of the length chain (applyConstraint_length, constraints.wgsl.ts:5-28):
+// segment j between a (point j, carried in registers) and point j + 1 of the
+// staged strand w; writes point j and carries point j + 1 on in a.
+__device__ __forceinline__ void lengthStep(float4* w, uint32_t j, float4& a, float expected, float kLen) {
+  float4 b = w[j + 1u];
+  const float w0 = a.w, w1 = b.w;
+  f3 tng = mk3(fsub(b.x, a.x), fsub(b.y, a.y), fsub(b.z, a.z));
+  float actual = len3(tng);
+  float corr = fsub(1.0f, expected / actual);
+  // two movable points (the common case) make the divisor exactly 2: a halving, exact as a product
+  const float num = fmul(corr, kLen), den = fadd(fadd(w0, w1), FLOAT_EPSILON);
+  float df = den == 2.0f ? fmul(num, 0.5f) : num / den;
+  f3 delta = mul3s(tng, df);
+  a.x = fadd(a.x, fmul(delta.x, w0)); a.y = fadd(a.y, fmul(delta.y, w0)); a.z = fadd(a.z, fmul(delta.z, w0));
+  b.x = fsub(b.x, fmul(w1, delta.x)); b.y = fsub(b.y, fmul(w1, delta.y)); b.z = fsub(b.z, fmul(w1, delta.z));
+  w[j] = a;
+  a = b;
+}
+
 template <uint32_t NT>
 __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32_t S, uint32_t P, uint32_t G,
                                                  float4* __restrict__ prev, const float4* __restrict__ now,
@@ -320,6 +340,8 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
   const float sdfOffset = u.sdf.boundsMax.w;
   const f4 sph = mk4(u.collisionSphere.x, u.collisionSphere.y, u.collisionSphere.z, u.collisionSphere.w);
   const float kLen = u.stiffnessLengthConstr;
+  // a strand's lengths load as float4s when its row starts on a 16-byte boundary
+  const bool len4 = (P & 3u) == 0u && (reinterpret_cast<uintptr_t>(segLen) & 15u) == 0u;
   const float kGlob = u.stiffnessGlobalConstr / (float)iters;
   const float kLoc = u.stiffnessLocalConstr / (float)iters;
   const float kColl = u.stiffnessCollisions / (float)iters;
@@ -331,24 +353,29 @@ __device__ __forceinline__ void simIntegrateBody(const HfbSimUniforms& u, uint32
       float4* w = wk + ls * R;
       const float* L = segLen + (size_t)(s0 + ls) * P;
       float4 a = w[0];
-      float expected = __ldg(HFB_G(&L[0])), nextExpected = __ldg(HFB_G(&L[1]));  // P >= 2
-      for (uint32_t j = 0; j + 1u < P; j++) {
-        const float nextExpected2 = j + 2u < P ? __ldg(HFB_G(&L[j + 2u])) : 0.0f;  // two steps ahead
-        float4 b = w[j + 1u];
-        const float w0 = a.w, w1 = b.w;
-        f3 tng = mk3(fsub(b.x, a.x), fsub(b.y, a.y), fsub(b.z, a.z));
-        float actual = len3(tng);
-        float corr = fsub(1.0f, expected / actual);
-        // two movable points (the common case) make the divisor exactly 2: a halving, exact as a product
-        const float num = fmul(corr, kLen), den = fadd(fadd(w0, w1), FLOAT_EPSILON);
-        float df = den == 2.0f ? fmul(num, 0.5f) : num / den;
-        f3 delta = mul3s(tng, df);
-        a.x = fadd(a.x, fmul(delta.x, w0)); a.y = fadd(a.y, fmul(delta.y, w0)); a.z = fadd(a.z, fmul(delta.z, w0));
-        b.x = fsub(b.x, fmul(w1, delta.x)); b.y = fsub(b.y, fmul(w1, delta.y)); b.z = fsub(b.z, fmul(w1, delta.z));
-        w[j] = a;
-        a = b;
-        expected = nextExpected;
-        nextExpected = nextExpected2;
+      if (len4) {
+        // the lengths of steps 4g .. 4g + 3 in one 16-byte load, the next group's issued
+        // before this group's steps: four to seven steps ahead
+        const float4* L4 = reinterpret_cast<const float4*>(L);
+        const uint32_t NG = P >> 2;
+        float4 cur = __ldg(HFB_G(&L4[0]));
+        for (uint32_t g = 0; g < NG; g++) {
+          const float4 nxt = g + 1u < NG ? __ldg(HFB_G(&L4[g + 1u])) : cur;
+          const uint32_t j = g << 2;
+          lengthStep(w, j, a, cur.x, kLen);
+          lengthStep(w, j + 1u, a, cur.y, kLen);
+          lengthStep(w, j + 2u, a, cur.z, kLen);
+          if (g + 1u < NG) lengthStep(w, j + 3u, a, cur.w, kLen);  // step P - 1 does not exist
+          cur = nxt;
+        }
+      } else {
+        float expected = __ldg(HFB_G(&L[0])), nextExpected = __ldg(HFB_G(&L[1]));  // P >= 2
+        for (uint32_t j = 0; j + 1u < P; j++) {
+          const float nextExpected2 = j + 2u < P ? __ldg(HFB_G(&L[j + 2u])) : 0.0f;  // two steps ahead
+          lengthStep(w, j, a, expected, kLen);
+          expected = nextExpected;
+          nextExpected = nextExpected2;
+        }
       }
       w[P - 1u] = a;
     }
@@ -446,11 +473,13 @@ simIntegrateKernel(const HfbSimUniforms u, uint32_t S, uint32_t P, uint32_t G,
 // GridPostSimPass.main, gridPostSimPass.wgsl.ts:45-72 with
 // _addGridDensityVelocity, densityVelocityGrid.wgsl.ts:93-124.
 //
-// One thread per point, eight corners, four wrapping i32 adds each.  A block
-// takes GP_POINTS points, strand after strand in the order strandOrder gives
-// (neighbouring strands next to each other: their points share grid nodes),
-// and first merges its adds per grid node in a shared-memory hash table;
-// each node's four sums then go to global memory as one set of atomics.
+// Each point adds to the eight corners of its cell, four wrapping i32 adds
+// each.  A block takes GP_POINTS points, strand after strand in the order
+// strandOrder gives (neighbouring strands next to each other: their points
+// share grid nodes), a thread GP_PPT consecutive ones: the points of a run
+// in one cell sum their corner values in registers, each run's sums merge
+// per grid node in a shared-memory hash table, and each node's four sums
+// then go to global memory as one set of atomics.
 // Wrapping integer sums do not depend on their order, so the grid is
 // bit-exact whatever the strand order and the merge; an update that finds no
 // free slot within GP_PROBES goes straight to global memory.
@@ -460,16 +489,21 @@ constexpr uint32_t GP_POINTS = 1024;  // points per block (four per thread)
 constexpr uint32_t GP_HASH = 2048;    // slots (power of two)
 constexpr uint32_t GP_PROBES = 32;
 constexpr uint32_t GP_EMPTY = 0xffffffffu;
+constexpr uint32_t GP_PPT = GP_POINTS / GP_THREADS;  // consecutive points per thread
+constexpr uint32_t GP_NO_CELL = 0xffffffffu;
+constexpr uint32_t GP_BATCH_BLOCKS = 3;  // blocks per SM of the batched kernel (the run sums need registers)
 
 struct GridPostShared {
   uint32_t key[GP_HASH];
-  uint4 val[GP_HASH];
+  // the four sums of a slot in four arrays: slot h's words sit in bank h mod 32
+  // (one uint4 per slot would put slots h and h + 8 in the same banks)
+  unsigned vx[GP_HASH], vy[GP_HASH], vz[GP_HASH], vw[GP_HASH];
 };
 
 __device__ __forceinline__ void gridPostClear(GridPostShared& sh) {
   for (uint32_t e = threadIdx.x; e < GP_HASH; e += blockDim.x) {
     sh.key[e] = GP_EMPTY;
-    sh.val[e] = make_uint4(0u, 0u, 0u, 0u);
+    sh.vx[e] = 0u; sh.vy[e] = 0u; sh.vz[e] = 0u; sh.vw[e] = 0u;
   }
 }
 
@@ -482,10 +516,10 @@ __device__ __forceinline__ void gridPostAdd(GridPostShared& sh, unsigned* __rest
     uint32_t old = *reinterpret_cast<volatile const uint32_t*>(&sh.key[h]);
     if (old == GP_EMPTY) old = atomicCAS(&sh.key[h], GP_EMPTY, idx);
     if (old == GP_EMPTY || old == idx) {
-      atomicAdd(&sh.val[h].x, v.x);
-      atomicAdd(&sh.val[h].y, v.y);
-      atomicAdd(&sh.val[h].z, v.z);
-      atomicAdd(&sh.val[h].w, v.w);
+      atomicAdd(&sh.vx[h], v.x);
+      atomicAdd(&sh.vy[h], v.y);
+      atomicAdd(&sh.vz[h], v.z);
+      atomicAdd(&sh.vw[h], v.w);
       return;
     }
     h = (h + 1u) & (GP_HASH - 1u);
@@ -506,41 +540,67 @@ __device__ __forceinline__ void gridPostSimBody(const HfbSimUniforms& u, uint32_
                                                 uint32_t blk, GridPostShared& sh) {
   const uint32_t N = S * P;
   const f3 gmin = gridMin(u), gmax = gridMax(u);
+  // a thread's GP_PPT consecutive ordered points: those of one strand that fall in
+  // the same cell add their corner values in registers first (wrapping, as the
+  // table and the grid do), and the cell's sums go to the table when the cell
+  // changes or the points end -- one set of table adds per run of points
+  uint4 acc[8];
+  uint32_t c0 = 0, c1 = 0, c2 = 0, cm = GP_NO_CELL;  // the cell being summed; cm: its corner mask
+  const uint32_t vb = blk * GP_POINTS + threadIdx.x * GP_PPT;
 #pragma unroll 1
-  for (uint32_t r = 0; r < GP_POINTS / GP_THREADS; r++) {
-    const uint32_t v = blk * GP_POINTS + r * GP_THREADS + threadIdx.x;
-    if (v >= N) break;
-    const uint32_t ls = v / P, j = v - ls * P;
-    const uint32_t s = order ? min(__ldg(HFB_G(&order[ls])), S - 1u) : ls;
-    const size_t i = (size_t)s * P + j;
-    const float4 a = __ldg(HFB_G(&prev[i])), b = __ldg(HFB_G(&now[i]));
-    const f3 pn = mk3(b.x, b.y, b.z);
-    const f3 vel = sub3(pn, mk3(a.x, a.y, a.z));
-    const GridCo co = gridCell(G, gmin, gmax, pn);
+  for (uint32_t r = 0; r <= GP_PPT; r++) {
+    const uint32_t v = vb + r;
+    const bool more = r < GP_PPT && v < N;
+    GridCo co;
+    f3 vel;
+    uint32_t m = GP_NO_CELL;
+    if (more) {
+      const uint32_t ls = v / P, j = v - ls * P;
+      const uint32_t s = order ? min(__ldg(HFB_G(&order[ls])), S - 1u) : ls;
+      const size_t i = (size_t)s * P + j;
+      const float4 a = __ldg(HFB_G(&prev[i])), b = __ldg(HFB_G(&now[i]));
+      const f3 pn = mk3(b.x, b.y, b.z);
+      vel = sub3(pn, mk3(a.x, a.y, a.z));
+      co = gridCell(G, gmin, gmax, pn);
+      // corner k = x + 2y + 4z (offsets from mn) exists when each of its offsets is 0 or mx > mn there
+      m = (co.mx[0] > co.mn[0] ? 1u : 0u) | (co.mx[1] > co.mn[1] ? 2u : 0u) | (co.mx[2] > co.mn[2] ? 4u : 0u);
+    }
+    if (!more || m != cm || co.mn[0] != c0 || co.mn[1] != c1 || co.mn[2] != c2) {
+      if (cm != GP_NO_CELL) {
+#pragma unroll
+        for (uint32_t k = 0; k < 8u; k++)
+          if ((k & ~cm) == 0u)
+            gridPostAdd(sh, dv, gridIdx(G, c0 + (k & 1u), c1 + ((k >> 1) & 1u), c2 + (k >> 2)), acc[k]);
+      }
+      if (!more) break;
+#pragma unroll
+      for (uint32_t k = 0; k < 8u; k++) acc[k] = make_uint4(0u, 0u, 0u, 0u);
+      c0 = co.mn[0]; c1 = co.mn[1]; c2 = co.mn[2]; cm = m;
+    }
 #pragma unroll
     for (uint32_t k = 0; k < 8u; k++) {
+      if ((k & ~m) != 0u) continue;
       const uint32_t x = co.mn[0] + (k & 1u), y = co.mn[1] + ((k >> 1) & 1u), z = co.mn[2] + (k >> 2);
-      if (x > co.mx[0] || y > co.mx[1] || z > co.mx[2]) continue;
-      const uint32_t idx = gridIdx(G, x, y, z);
       const f3 w = cellWeights(x, y, z, co.p);
       const f3 cv = mul3(vel, w);
-      gridPostAdd(sh, dv, idx,
-                  make_uint4((unsigned)gridEncode(cv.x), (unsigned)gridEncode(cv.y), (unsigned)gridEncode(cv.z),
-                             (unsigned)gridEncode(len3(w))));
+      acc[k].x += (unsigned)gridEncode(cv.x);
+      acc[k].y += (unsigned)gridEncode(cv.y);
+      acc[k].z += (unsigned)gridEncode(cv.z);
+      acc[k].w += (unsigned)gridEncode(len3(w));
     }
   }
   __syncthreads();
   for (uint32_t e = threadIdx.x; e < GP_HASH; e += blockDim.x) {
     const uint32_t idx = sh.key[e];
     if (idx == GP_EMPTY) continue;
-    const uint4 v = sh.val[e];
+    const uint4 v = make_uint4(sh.vx[e], sh.vy[e], sh.vz[e], sh.vw[e]);
     unsigned* c = reinterpret_cast<unsigned*>(HFB_G(reinterpret_cast<uint4*>(dv + 4u * idx)));
     atomicAdd(c + 0, v.x);
     atomicAdd(c + 1, v.y);
     atomicAdd(c + 2, v.z);
     atomicAdd(c + 3, v.w);
     sh.key[e] = GP_EMPTY;
-    sh.val[e] = make_uint4(0u, 0u, 0u, 0u);
+    sh.vx[e] = 0u; sh.vy[e] = 0u; sh.vz[e] = 0u; sh.vw[e] = 0u;
   }
   // the next points' adds come after batchNext's barrier, with the table empty
 }
@@ -585,7 +645,7 @@ __global__ void __launch_bounds__(SIM_BATCH_THREADS, 6) simIntegrateBatch(BatchV
   }
 }
 
-__global__ void __launch_bounds__(GP_THREADS, 5) gridPostSimBatch(BatchView b, uint32_t G) {
+__global__ void __launch_bounds__(GP_THREADS, GP_BATCH_BLOCKS) gridPostSimBatch(BatchView b, uint32_t G) {
   __shared__ GridPostShared sh;
   gridPostClear(sh);
   __syncthreads();
@@ -707,7 +767,12 @@ cudaError_t launchBatchSim(HfbCtx* c, const BatchView& b, BatchKind k) {
     simIntegrateBatch<<<batchLaunchGrid(c, grid), SIM_BATCH_THREADS, smem, c->stream>>>(b, G);
     HFB_AFTER_LAUNCH(c, "simIntegrateBatch");
   } else if (k == BK_GRID_POST) {
-    if (!grid) grid = c->smCount * 8u;
+    if (!grid) {
+      int perSM = 0;
+      cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, gridPostSimBatch, GP_THREADS, 0);
+      if (e != cudaSuccess) return e;
+      grid = (uint32_t)(perSM > 0 ? perSM : 1) * c->smCount;
+    }
     gridPostSimBatch<<<batchLaunchGrid(c, grid), GP_THREADS, 0, c->stream>>>(b, G);
     HFB_AFTER_LAUNCH(c, "gridPostSimBatch");
   } else {

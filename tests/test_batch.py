@@ -139,6 +139,19 @@ def test_frame_batch_many_small_instances(groups):
     _batch_vs_alone(insts, 3, groups=groups)
 
 
+def test_frame_batch_crowded_bins():
+    """An instance whose tiles hold bins of more than 1,024 and 16,384 records
+    beside a sparse one: the batched list builder (blocks of 32 bins, the
+    larger bins queued per block, the largest one block each) links every
+    bin as the single-instance launches do."""
+    rng = np.random.Generator(np.random.PCG64(5))
+    common = dict(tile_size=32, depth_bins=4, slices=4, shading_points=8, grid_dims=32, iterations=4,
+                  avg_segments_per_tile=65536)
+    insts = [synthetic.make_instance(rng, strands=40000, points=16, width=192, height=160, **common),
+             synthetic.make_instance(rng, strands=1500, points=16, width=320, height=240, **common)]
+    _batch_vs_alone(insts, 2)
+
+
 def test_frame_batch_with_hair_depth():
     """Instances that draw the hair depth after the fine pass and shade with
     it: the batched frames equal each instance's frames alone."""

@@ -86,6 +86,21 @@ def test_tiles_pass_bit_exact(oracle, tile, bins):
     _compare_tiles(oracle, inst, fr, rb)
 
 
+def test_tiles_pass_crowded_bins_bit_exact(oracle):
+    """40,000 strands in a 192x160 viewport with 32 px tiles and 4 depth bins:
+    bins of every size class the list builder sorts differently -- up to 32
+    records (one warp's registers), up to 1,024 (a warp in shared memory),
+    more (a block), and more than 16,384 (sorted in runs, then merged)."""
+    inst = small_instance(strands=40000, width=192, height=160, tile_size=32, depth_bins=4,
+                          avg_segments_per_tile=65536)
+    fr = frame_of(inst)
+    ctx, hair, rb, _ = _raster_gpu(inst, fr)
+    ot, osg, _ = _compare_tiles(oracle, inst, fr, rb)
+    n = np.array([len(v) for v in walk_lists(ot, osg, fr.max_drawn).values()])
+    assert ((n > 8) & (n <= 32)).any() and ((n > 32) & (n <= 1024)).any(), "no small or medium bins"
+    assert (n > 1024).sum() >= 4 and (n > 16384).any(), f"largest bin {n.max()}: the test does not test"
+
+
 @pytest.mark.parametrize("entry,value", [(None, None), (2, 2e-5), (7, -2e-4), (10, 0.05), (10, 1e-12)])
 def test_tiles_pass_bins_for_any_inverse_projection(oracle, entry, value):
     """The record's depth bin, the smallest over its passing pixels, is taken
