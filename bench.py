@@ -688,7 +688,7 @@ def served_config():
 
 
 def run_served(frames_per_session, device, seed=0, rate_hz=2000.0, budget_bytes=150 << 30, session_rate_hz=2000.0,
-               lanes=2, tick_budget_ms=12.0, count=256):
+               lanes=3, tick_budget_ms=8.0, count=256):
     """The serving workload: `count` sessions arriving as a Poisson process of
     `session_rate_hz`, admitted under the memory budget; once its state is
     on the device each session asks for `frames_per_session` frames as a

@@ -267,8 +267,8 @@ class CostModel:
 class Server:
     """Sessions served on `lanes` contexts of one pass config."""
 
-    def __init__(self, cfg: HairConfig, device: int = 0, budget_bytes: int = 150 << 30, lanes: int = 2,
-                 tick_budget_ms: float = 12.0, make_instance=None, hair_depth: bool = True, groups: int = 1):
+    def __init__(self, cfg: HairConfig, device: int = 0, budget_bytes: int = 150 << 30, lanes: int = 3,
+                 tick_budget_ms: float = 8.0, make_instance=None, hair_depth: bool = True, groups: int = 1):
         """hair_depth: each session's frame draws the hair depth for its
         shading (the reference's frame); False shades with the scene depth.
         tick_budget_ms: the estimated GPU time a tick may hold (at least one
