@@ -932,7 +932,7 @@ def main():
                              if k in ("offered_frames_per_s", "frames_per_s", "steady_frames_per_s",
                                       "request_p50_ms", "request_p99_ms", "steady_request_p99_ms",
                                       "frames_per_tick", "tick_gpu_p50_ms")}
-                            for hz in (1000.0, 1200.0, 1400.0, 1600.0)]
+                            for hz in (1000.0, 1200.0, 1400.0, 1600.0, 1800.0)]
         from hairfb import replicas
         sv["wall_s"] = replicas.max_over_ranks([sv["wall_s"]], dist, "cuda")[0]
         if rank == 0:
