@@ -226,7 +226,7 @@ uint32_t batchBlocks(const HfbConfig& cfg, BatchKind k, const BatchInst& I) {
       return v < 1u ? 1u : (v > 256u ? 256u : v);
     }
     case BK_FINALIZE: return divCeil(TB, 32u);  // a warp takes 4 consecutive bins
-    case BK_LARGE: {  // one CTA per bin of more than 1,024 records, which come with the segments
+    case BK_LARGE: {  // a CTA per bin of more than 1,024 records: more segments, more such bins
       const uint32_t v = divCeil(nSeg, 32768u);
       return v < 4u ? 4u : (v > 64u ? 64u : v);
     }

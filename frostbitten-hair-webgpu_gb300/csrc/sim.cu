@@ -540,10 +540,11 @@ __device__ __forceinline__ void gridPostSimBody(const HfbSimUniforms& u, uint32_
                                                 uint32_t blk, GridPostShared& sh) {
   const uint32_t N = S * P;
   const f3 gmin = gridMin(u), gmax = gridMax(u);
-  // a thread's GP_PPT consecutive ordered points: those of one strand that fall in
-  // the same cell add their corner values in registers first (wrapping, as the
-  // table and the grid do), and the cell's sums go to the table when the cell
-  // changes or the points end -- one set of table adds per run of points
+  // a thread's GP_PPT consecutive ordered points: consecutive points that fall in
+  // the same cell (mostly neighbours on one strand) add their corner values in
+  // registers first (wrapping, as the table and the grid do), and the cell's sums
+  // go to the table when the cell changes or the points end -- one set of table
+  // adds per run of points
   uint4 acc[8];
   uint32_t c0 = 0, c1 = 0, c2 = 0, cm = GP_NO_CELL;  // the cell being summed; cm: its corner mask
   const uint32_t vb = blk * GP_POINTS + threadIdx.x * GP_PPT;
