@@ -480,8 +480,9 @@ def e2e_frames(args, batch, stream):
     """Frames through the public calls with host inputs and outputs: each
     step is hfb_frame_batch (both uniform blocks of every instance go up
     from host memory inside the call), then every instance's frame image
-    (hfb_present: the hair over a black scene, tone mapped to RGBA8, what the
-    reference presents) is copied into pinned host memory.  The copies run
+    (hfb_present_batch, one call per part of the batch: the hair over a
+    black scene, tone mapped to RGBA8, what the reference presents) is
+    copied into pinned host memory.  The copies run
     on a stream of their own while the next frame renders, into two host
     buffers used in turn; a frame's images are presented only once the
     copies that last read their device buffers are done.  Returns (seconds
@@ -489,7 +490,7 @@ def e2e_frames(args, batch, stream):
     step); the host waits for the last copy before the clock stops."""
     import torch
     from hairfb import uniforms as UN
-    from hairfb.lib import byref, ptr
+    from hairfb.lib import HfbPresentItem, ptr
     # (context, renderers, stream) of each part of the batch
     parts = [(b.ctx, b.renderers, b.ctx.stream_obj) for b in batch.batches] if hasattr(batch, "batches") \
         else [(batch.ctx, batch.renderers, stream)]
@@ -499,6 +500,14 @@ def e2e_frames(args, batch, stream):
     host_img = [[torch.empty(r.inst.height * r.inst.width * 4, dtype=torch.uint8).pin_memory() for r in rs]
                 for _ in range(2)]
     ub = {id(r): ctypes.cast(ctypes.c_char_p(r.uniforms), ctypes.c_void_p) for r in rs}
+    # each part's images of each buffer slot: one hfb_present_batch call
+    present = {}
+    for pi, (_, prs, _) in enumerate(parts):
+        for slot in range(2):
+            arr = (HfbPresentItem * len(prs))()
+            for k, r in enumerate(prs):
+                arr[k] = HfbPresentItem(ub[id(r)].value, ctypes.addressof(r.rb.rb), None, ptr(dev_img[slot][id(r)]))
+            present[(pi, slot)] = arr
     copy_stream = torch.cuda.Stream()
     copied = [None, None]
     t0 = None
@@ -508,11 +517,10 @@ def e2e_frames(args, batch, stream):
             t0 = time.perf_counter()
         slot = k & 1
         batch.frame()
-        for pctx, prs, pst in parts:
+        for pi, (pctx, prs, pst) in enumerate(parts):
             if copied[slot] is not None:  # the copies of two frames ago read these device images
                 pst.wait_event(copied[slot])
-            for r in prs:
-                pctx.call("hfb_present", ub[id(r)], byref(r.rb.rb), None, ptr(dev_img[slot][id(r)]))
+            pctx.call("hfb_present_batch", present[(pi, slot)], len(prs))
             done = torch.cuda.Event()
             done.record(pst)
             copy_stream.wait_event(done)
@@ -822,7 +830,7 @@ def report_batched(args, res, world, dist):
         "e2e": {"value": world * n * args.steps / e2e_s, "unit": "frames/s",
                 "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"],
                 "what": "hfb_frame_batch with both uniform blocks of every instance from host memory, then every "
-                        "instance's presented RGBA8 image (hfb_present) copied to pinned host memory on a copy "
+                        "instance's presented RGBA8 image (hfb_present_batch) copied to pinned host memory on a copy "
                         "stream overlapping the next frame; host clock over the steps, last copy included"},
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
                      "peak_source": peak_src, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,

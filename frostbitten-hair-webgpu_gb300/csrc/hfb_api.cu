@@ -498,6 +498,21 @@ int hfb_present(HfbCtx* c, const HfbUniforms* u, const HfbRasterBuffers* rb, con
   HFB_LAUNCH(c, hfb::launchPresent(c, *u, rb->width, rb->height, rb->rasterizerResult + 4, scene, rgba), "present");
 }
 
+int hfb_present_batch(HfbCtx* c, const HfbPresentItem* items, uint32_t n) {
+  HFB_CHECK_CTX(c);
+  HFB_REQUIRE(c, n == 0 || items, "NULL argument");
+  for (uint32_t k = 0; k < n; k++) {
+    const HfbPresentItem& it = items[k];
+    const std::string at = "item " + std::to_string(k) + ": ";
+    HFB_REQUIRE(c, it.uniforms && it.rgba, at + "NULL argument");
+    HFB_REQUIRE(c, !it.sceneColor || aligned16(it.sceneColor), at + "vec4 buffers must be 16-byte aligned");
+    std::string err = checkRaster(c, it.rb);
+    if (err.empty()) err = checkViewport(it.uniforms, it.rb);
+    HFB_REQUIRE(c, err.empty(), at + err);
+  }
+  HFB_LAUNCH(c, hfb::launchPresentBatch(c, items, n), "present_batch");
+}
+
 // Checks one instance of a frame (the union of the per-pass checks).
 static std::string checkInstance(const HfbCtx* c, const HfbInstance* in) {
   if (!in) return "instance is NULL";

@@ -362,6 +362,7 @@ cudaError_t launchGtao(HfbCtx* c, const HfbUniforms& u, const float* depth, cons
                        float* ao);
 cudaError_t launchPresent(HfbCtx* c, const HfbUniforms& u, uint32_t W, uint32_t H, const float* result,
                           const float* scene, uint8_t* rgba);
+cudaError_t launchPresentBatch(HfbCtx* c, const HfbPresentItem* items, uint32_t n);
 // The hair depth pass's list of big triangles has its own region of the
 // raster scratch, after the tiles and fine passes' working memory, so the
 // pass can run beside them: HD_LIST_ENTRIES entries + the count.

@@ -30,11 +30,10 @@ __device__ __forceinline__ uint8_t unorm8(float c) {  // float -> unorm8, round 
   return (uint8_t)__float2uint_rn(fmul(sat(c), 255.0f));
 }
 
-__global__ void __launch_bounds__(256)
-presentKernel(float gamma, float exposure, float ditherStr, uint32_t W, uint32_t H, const float4* __restrict__ result,
-              const float4* __restrict__ scene, uchar4* __restrict__ out) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= W * H) return;
+// Pixel i (row-major, row 0 at the top) of one image.
+__device__ __forceinline__ void presentPixel(float gamma, float exposure, float ditherStr, uint32_t W, uint32_t H,
+                                             const float4* __restrict__ result, const float4* __restrict__ scene,
+                                             uchar4* __restrict__ out, uint32_t i) {
   const uint32_t x = i % W, y = i / W;  // y: row from the top
   const float4 src = __ldg(HFB_G(&result[(size_t)(H - 1u - y) * W + x]));
   const float4 dst = scene ? __ldg(HFB_G(&scene[i])) : make_float4(0.f, 0.f, 0.f, 1.f);
@@ -55,6 +54,44 @@ presentKernel(float gamma, float exposure, float ditherStr, uint32_t W, uint32_t
   *HFB_G(&out[i]) = make_uchar4(o[0], o[1], o[2], 255);
 }
 
+__global__ void __launch_bounds__(256)
+presentKernel(float gamma, float exposure, float ditherStr, uint32_t W, uint32_t H, const float4* __restrict__ result,
+              const float4* __restrict__ scene, uchar4* __restrict__ out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= W * H) return;
+  presentPixel(gamma, exposure, ditherStr, W, H, result, scene, out, i);
+}
+
+// Up to PRESENT_BATCH images in one launch, passed by value (48 B each, inside
+// the 4 KB of kernel parameters every launch may carry): image k covers the
+// launch's pixels [first[k], first[k + 1]).
+constexpr uint32_t PRESENT_BATCH = 64;
+struct PresentImage {
+  float gamma, exposure, dither;
+  uint32_t W, H, first;
+  const float4* result;
+  const float4* scene;
+  uchar4* out;
+};
+struct PresentBatch {
+  uint32_t n, total;
+  PresentImage im[PRESENT_BATCH];
+};
+static_assert(sizeof(PresentBatch) <= 4000, "kernel parameters above 4 KB");
+
+__global__ void __launch_bounds__(256) presentBatchKernel(const PresentBatch pb) {
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < pb.total; g += stride) {
+    uint32_t lo = 0, hi = pb.n - 1u;  // the last image whose first pixel is at or before g
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi + 1u) >> 1;
+      if (pb.im[mid].first <= g) lo = mid; else hi = mid - 1u;
+    }
+    const PresentImage& m = pb.im[lo];
+    presentPixel(m.gamma, m.exposure, m.dither, m.W, m.H, m.result, m.scene, m.out, g - m.first);
+  }
+}
+
 }  // namespace
 
 cudaError_t launchPresent(HfbCtx* c, const HfbUniforms& u, uint32_t W, uint32_t H, const float* result,
@@ -67,6 +104,43 @@ cudaError_t launchPresent(HfbCtx* c, const HfbUniforms& u, uint32_t W, uint32_t 
   HFB_AFTER_LAUNCH(c, "presentKernel");
   c->launches += 1;
   return cudaGetLastError();
+}
+
+// Images of at most 2^32 - 1 pixels in all per launch of PRESENT_BATCH; the
+// caller has checked every item.
+cudaError_t launchPresentBatch(HfbCtx* c, const HfbPresentItem* items, uint32_t n) {
+  HFB_CHECK_BIND(c);
+  for (uint32_t k0 = 0; k0 < n; k0 += PRESENT_BATCH) {
+    PresentBatch pb{};
+    uint64_t total = 0;
+    for (uint32_t k = k0; k < n && k < k0 + PRESENT_BATCH; k++) {
+      const HfbPresentItem& it = items[k];
+      const uint32_t W = it.rb->width, H = it.rb->height;
+      if ((uint64_t)W * H == 0u) continue;
+      if (total + (uint64_t)W * H > 0xffffffffull) return cudaErrorInvalidValue;
+      PresentImage& m = pb.im[pb.n++];
+      m.gamma = it.uniforms->colorMgmt.x;
+      m.exposure = it.uniforms->colorMgmt.y;
+      m.dither = it.uniforms->colorMgmt.z;
+      m.W = W;
+      m.H = H;
+      m.first = (uint32_t)total;
+      m.result = (const float4*)(it.rb->rasterizerResult + 4);
+      m.scene = (const float4*)it.sceneColor;
+      m.out = (uchar4*)it.rgba;
+      total += (uint64_t)W * H;
+    }
+    if (pb.n == 0) continue;
+    pb.total = (uint32_t)total;
+    const uint32_t blocks = divCeil(pb.total, 256u);
+    const uint32_t cap = c->smCount * 8u;
+    presentBatchKernel<<<blocks < cap ? blocks : cap, 256, 0, c->stream>>>(pb);
+    HFB_AFTER_LAUNCH(c, "presentBatchKernel");
+    c->launches += 1;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 }  // namespace hfb

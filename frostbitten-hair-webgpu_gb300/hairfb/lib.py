@@ -42,6 +42,14 @@ class HfbRasterBuffers(ctypes.Structure):
                 ("scratch", ctypes.c_void_p), ("scratchBytes", ctypes.c_size_t)]
 
 
+class HfbPresentItem(ctypes.Structure):
+    """One hfb_present call's arguments, for hfb_present_batch (host
+    addresses of the uniforms and the raster buffers' struct, device
+    addresses of the scene colour (or NULL) and the RGBA8 image)."""
+    _fields_ = [("uniforms", ctypes.c_void_p), ("rb", ctypes.c_void_p), ("sceneColor", ctypes.c_void_p),
+                ("rgba", ctypes.c_void_p)]
+
+
 class HfbInstance(ctypes.Structure):
     """One hair instance of a frame (hfb_frame / hfb_frame_batch)."""
     _fields_ = [("uniforms", ctypes.c_void_p), ("simUniforms", ctypes.c_void_p), ("hair", HfbHairData),
@@ -101,6 +109,7 @@ SIGNATURES = {
     "hfb_tiles_pass_noalloc": (I, [P, P, P, P, P, P, U32, P]),
     "hfb_hair_depth": (I, [P, P, P, P, P, U32, P, P, P]),
     "hfb_present": (I, [P, P, P, P, P]),
+    "hfb_present_batch": (I, [P, P, U32]),
     "hfb_hair_normals": (I, [P, P, P, P, P, U32, P, P, P, P]),
     "hfb_gtao": (I, [P, P, P, P, ctypes.c_float, P]),
     "hfb_frame": (I, [P, P]),

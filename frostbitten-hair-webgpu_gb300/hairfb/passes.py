@@ -17,7 +17,7 @@ import torch
 from . import hair_object as HO
 from .config import HairConfig
 from .formats import SdfVolume
-from .lib import Context, HfbHairData, HfbRasterBuffers, byref, ptr, strand_grid_order
+from .lib import Context, HfbHairData, HfbPresentItem, HfbRasterBuffers, byref, ptr, strand_grid_order
 
 
 def _dev(a, dtype=None) -> torch.Tensor:
@@ -348,6 +348,18 @@ class PresentPass:
             out = torch.empty((rb.height, rb.width, 4), dtype=torch.uint8, device="cuda")
         self.ctx.call("hfb_present", _ub(uniforms), byref(rb.rb), ptr(scene_color), ptr(out))
         return out
+
+    def cmd_draw_batch(self, items) -> None:
+        """cmd_draw for every (uniforms, rb, scene_color or None, out) of
+        items, out given: one launch per 64 images (hfb_present_batch), each
+        image as cmd_draw makes it."""
+        arr = (HfbPresentItem * len(items))()
+        keep = []  # the uniform blocks' host pointers stay valid through the call
+        for k, (uniforms, rb, scene_color, out) in enumerate(items):
+            ub = _ub(uniforms)
+            keep.append((uniforms, ub))
+            arr[k] = HfbPresentItem(ub.value, ctypes.addressof(rb.rb), ptr(scene_color), ptr(out))
+        self.ctx.call("hfb_present_batch", arr, len(items))
 
 
 class AoPass:

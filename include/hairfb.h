@@ -361,6 +361,18 @@ typedef struct HfbInstance {
 HFB_API int hfb_present(HfbCtx* ctx, const HfbUniforms* uniforms, const HfbRasterBuffers* rb,
                         const float* sceneColor, uint8_t* rgba);
 
+/* hfb_present for the images of many instances (those of a batched frame),
+ * in one launch per 64 images: items[k] holds one hfb_present call's
+ * arguments, each checked as hfb_present checks them before any launch, and
+ * each image equals what hfb_present makes of the same arguments. */
+typedef struct HfbPresentItem {
+  const HfbUniforms* uniforms;
+  const HfbRasterBuffers* rb;
+  const float* sceneColor; /* NULL = black */
+  uint8_t* rgba;
+} HfbPresentItem;
+HFB_API int hfb_present_batch(HfbCtx* ctx, const HfbPresentItem* items, uint32_t n);
+
 /* HwHairPass.cmdDrawHair's normal output (hwHairPass.wgsl.ts:88-97): at every
  * pixel where the hair is in front (its depth equals hairDepth, as
  * hfb_hair_depth left it), the octahedron encoding of the normalised
@@ -456,12 +468,14 @@ static_assert(sizeof(HfbHairData) == 32, "HfbHairData layout");
 static_assert(sizeof(HfbUniforms) == 1184, "Uniforms layout");
 static_assert(sizeof(HfbSimUniforms) == 304, "SimulationUniforms layout");
 static_assert(sizeof(HfbInstance) == 272, "HfbInstance layout");
+static_assert(sizeof(HfbPresentItem) == 32, "HfbPresentItem layout");
 #else
 _Static_assert(sizeof(HfbConfig) == 64, "HfbConfig layout");
 _Static_assert(sizeof(HfbHairData) == 32, "HfbHairData layout");
 _Static_assert(sizeof(HfbUniforms) == 1184, "Uniforms layout");
 _Static_assert(sizeof(HfbSimUniforms) == 304, "SimulationUniforms layout");
 _Static_assert(sizeof(HfbInstance) == 272, "HfbInstance layout");
+_Static_assert(sizeof(HfbPresentItem) == 32, "HfbPresentItem layout");
 #endif
 
 #endif /* HAIRFB_H */

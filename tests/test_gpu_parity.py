@@ -695,6 +695,36 @@ def test_present_within_1_255(oracle, scene, tmp_path):
     assert png[:8] == b"\x89PNG\r\n\x1a\n"
 
 
+def test_present_batch_equals_present():
+    """hfb_present_batch: three rendered frames of different viewports, one
+    over a scene colour image, in one launch; each image equals hfb_present's
+    on the same arguments, byte for byte."""
+    from hairfb.lib import HfbError
+    from hairfb.passes import PresentPass
+    from hairfb.renderer import Renderer
+    rng = np.random.default_rng(2)
+    items = []
+    ctx = None
+    for k, (w, h, scene) in enumerate([(320, 240, False), (200, 150, True), (97, 61, False)]):
+        inst = small_instance(seed=k, strands=600, width=w, height=h)
+        r = Renderer(inst, 0, ctx=ctx)
+        ctx = r.ctx
+        r.before_first_frame()
+        r.frame()
+        sc = torch.as_tensor(rng.uniform(0.0, 2.0, (h, w, 4)).astype(np.float32)).cuda() if scene else None
+        alone = PresentPass(ctx).cmd_draw(r.uniforms, r.rb, sc)
+        items.append((r, sc, alone, torch.zeros_like(alone)))
+    PresentPass(ctx).cmd_draw_batch([(r.uniforms, r.rb, sc, out) for r, sc, _, out in items])
+    ctx.sync()
+    for k, (r, sc, alone, batched) in enumerate(items):
+        a, b = alone.cpu().numpy(), batched.cpu().numpy()
+        assert len(np.unique(a[..., :3].reshape(-1, 3), axis=0)) > 20, f"image {k} is flat: the case does not test"
+        assert np.array_equal(a, b), f"image {k}: {(a != b).any(-1).sum()} pixels differ"
+    with pytest.raises(HfbError, match="item 1"):
+        PresentPass(ctx).cmd_draw_batch([(items[0][0].uniforms, items[0][0].rb, None, items[0][3]),
+                                         (items[0][0].uniforms, items[1][0].rb, None, items[1][3])])
+
+
 @pytest.mark.parametrize("kw", [dict(), dict(strands=300, fiber_radius=0.02)])
 def test_hair_normals_and_gtao(oracle, kw):
     """HwHairPass's normals (bit-exact: the winner of each pixel, the
