@@ -65,6 +65,16 @@ def test_config_struct_matches_header():
     assert (c.sortBuckets, c.sortBucketSize, c.processorCount) == (64, 16, 512)
 
 
+def test_ctypes_structs_match_the_header_sizes():
+    """The host mirrors of the C-ABI structs have the sizes include/hairfb.h
+    static-asserts (a mismatch would shift every field the library reads)."""
+    from hairfb.lib import HfbHairData, HfbInstance, HfbPresentItem
+    txt = open(HEADER).read()
+    asserted = dict((k, int(v)) for k, v in re.findall(r"static_assert\(sizeof\((\w+)\) == (\d+)", txt))
+    for cls in (HfbConfig, HfbHairData, HfbInstance, HfbPresentItem):
+        assert ctypes.sizeof(cls) == asserted[cls.__name__], cls.__name__
+
+
 def test_max_drawn_segments_formula():
     # getLengthOfHairTileSegmentsBuffer, hairTileSegmentsBuffer.ts:81-87
     cfg = HairConfig(tile_size=16, avg_segments_per_tile=128)
