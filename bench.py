@@ -927,6 +927,7 @@ def main():
 
     if wl == "served256":
         import torch
+        from hairfb import uniforms as UN
         dev = int(os.environ.get("LOCAL_RANK", "0"))
         torch.cuda.set_device(dev)
         sv = run_served(600, dev, seed=rank)
@@ -952,7 +953,13 @@ def main():
                     "config": {"workload": wl, "describe": WORKLOADS[wl], "served": sv,
                                "step": "one tick: the oldest pending frame requests, one per session, "
                                        "within the tick's GPU-time budget (hfb_frame_batch)"},
-                    "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                    "e2e": {"value": fps, "unit": "frames/s",
+                            "h2d_bytes_per_step": round(sv["frames_per_tick"] * (UN.RENDER_UNIFORMS_BYTES +
+                                                                                UN.SIM_UNIFORMS_BYTES)),
+                            "d2h_bytes_per_step": 0,
+                            "what": "value is already end to end: the host's clock over the public calls, "
+                                    "each tick's uniform blocks going up from host memory inside "
+                                    "hfb_frame_batch; a served frame stays on the device (no readback)"},
                     "roofline": None, "cpu_baseline": None, "gpu_launches": None}
             print(json.dumps(line), flush=True)
         if dist:
