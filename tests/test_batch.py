@@ -139,6 +139,68 @@ def test_frame_batch_many_small_instances(groups):
     _batch_vs_alone(insts, 3, groups=groups)
 
 
+def _lists(tiles, segs):
+    """Every non-empty (tile, bin) list, vectorised: (bins, lengths, the
+    records in list order).  The builder stores a list of n records in n
+    consecutive slots ending at its head, each linked to the one before
+    (checked here), so a list is its slots read backwards."""
+    heads = tiles[:, 2].astype(np.int64)
+    bins = np.nonzero(heads)[0]
+    n = tiles[bins, 3].astype(np.int64)
+    assert (n > 0).all(), "a list without its length"
+    first = np.cumsum(n) - n
+    k = np.arange(int(n.sum())) - np.repeat(first, n)         # position in its list, 0 = head
+    slot = np.repeat(heads[bins] - 1, n) - k                  # head first, then backwards
+    nxt = segs[2 + 2 * slot].astype(np.int64)
+    last = k == np.repeat(n - 1, n)
+    assert (nxt[last] == 0xFFFFFFFF).all() and (nxt[~last] == slot[~last] - 1).all(), "a list is not linked backwards"
+    return bins, n, segs[1 + 2 * slot]
+
+
+def test_frame_batch_of_the_64_instance_workload():
+    """All 64 instances of the benchmark's batched workload (strands
+    U[1k, 20k], points in {16, 24, 32}, viewports 256^2-1024^2) at the
+    constants the autotuner picks for it (8 px tiles, 4 depth bins), hair
+    depth on: two batched frames equal each instance's frames alone --
+    positions, grids, counts, per-bin depth bounds, every list walked from
+    its head, tile list bit-exact, shading within 1e-6, pixels within
+    1/255; no record dropped."""
+    insts = synthetic.batched_instances(seed=0, count=64, tile_size=8, depth_bins=4, grid_dims=64, slices=4,
+                                        shading_points=8, iterations=7, avg_segments_per_tile=512)
+    alone = [Renderer(inst, 0, hair_depth=True) for inst in insts]
+    ctx = Context(insts[0].cfg.to_c(), 0)
+    batch = BatchRenderer([Renderer(inst, 0, ctx=ctx, hair_depth=True) for inst in insts])
+    for r in alone:
+        r.before_first_frame()
+    batch.before_first_frame()
+    for f in range(2):
+        for r in alone:
+            r.frame()
+        batch.frame()
+        torch.cuda.synchronize()
+        for k, (ra, rb) in enumerate(zip(alone, batch.renderers)):
+            tag = f"frame {f}, instance {k}"
+            assert torch.equal(ra.hair.positions, rb.hair.positions), f"{tag}: positions differ"
+            assert torch.equal(ra.grids.density_velocity, rb.grids.density_velocity), f"{tag}: density grid differs"
+            assert np.array_equal(ra.rb.read_segment_counts(), rb.rb.read_segment_counts()), f"{tag}: counts"
+            tla, tlb = ra.rb.read_tiles().reshape(-1, 4), rb.rb.read_tiles().reshape(-1, 4)
+            assert np.array_equal(tla[:, :2], tlb[:, :2]), f"{tag}: depth bounds differ"
+            sa, sb = ra.rb.read_tile_segments(), rb.rb.read_tile_segments()
+            assert sa[0] == sb[0], f"{tag}: drawnSegmentsCount differs"
+            la, lb = _lists(tla, sa), _lists(tlb, sb)
+            assert all(np.array_equal(x, y) for x, y in zip(la, lb)), f"{tag}: lists differ"
+            ta, tb = ra.rb.read_tile_list(), rb.rb.read_tile_list()
+            assert np.array_equal(ta[:1 + int(ta[0])], tb[:1 + int(tb[0])]), f"{tag}: tile list differs"
+            assert (ra.hair.shading - rb.hair.shading).abs().max().item() <= 1e-6, f"{tag}: shading differs"
+            err = np.abs(ra.rb.read_result()[4:] - rb.rb.read_result()[4:]).max()
+            assert err <= 1.0 / 255.0, f"{tag}: pixel error {err:.4g}"
+    assert ctx.counters()["tileRecordsDropped"] == 0, "a pool overflowed: which records drop depends on timing"
+    for r in alone:
+        r.rb.close()
+    for r in batch.renderers:
+        r.rb.close()
+
+
 def test_frame_batch_crowded_bins():
     """An instance whose tiles hold bins of more than 1,024 and 16,384 records
     beside a sparse one: the batched list builder (blocks of 32 bins, the
