@@ -176,7 +176,7 @@ class Session:
     pending: collections.deque = dataclasses.field(default_factory=collections.deque)
     busy: bool = False         # in a tick on the GPU
     finished_s: float = -1.0
-    work: float = 0.0          # frame cost units (cost model)
+    work: tuple = (0.0, 0.0)   # a frame's (points, pixels): the cost model's units
 
 
 @dataclasses.dataclass

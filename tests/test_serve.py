@@ -47,6 +47,30 @@ def test_cost_model_fits_tick_times():
     assert abs(cm.ms(1e6, 1e6) - (0.3 + 0.2 + 0.1)) < 1e-6
 
 
+def test_tick_takes_the_oldest_requests_one_per_session_within_the_budget():
+    """Server._form (host logic, no GPU): the sessions with a pending request
+    and no frame on the GPU, oldest request first, one frame each, until the
+    cost model's estimate would pass the tick budget -- and at least one."""
+    import types
+    cm = serve.CostModel(a=0.0, b=1e-3, c=0.0)  # 1 ms per 1,000 points
+    fake = types.SimpleNamespace(cost=cm, tick_budget_ms=3.0)
+
+    def session(sid, points, requests, busy=False):
+        s = serve.Session(serve.SessionSpec(sid, 0.0, points, 1, 16, 16, 10, 0))
+        s.work = (float(points), 0.0)
+        s.pending.extend(requests)
+        s.busy = busy
+        return s
+
+    ready = [session(0, 1000, [0.5, 0.6]), session(1, 1000, [0.2]), session(2, 1000, [0.1], busy=True),
+             session(3, 1000, []), session(4, 1000, [0.3]), session(5, 1000, [0.4])]
+    group = serve.Server._form(fake, ready)
+    assert [s.spec.sid for s in group] == [1, 4, 5]  # oldest first; busy and idle sessions skipped; 3 ms
+    fake.tick_budget_ms = 0.5
+    assert [s.spec.sid for s in serve.Server._form(fake, ready)] == [1]  # over budget alone: still one
+    assert serve.Server._form(fake, [ready[2], ready[3]]) == []
+
+
 @pytest.mark.gpu
 def test_steady_rate_counts_the_window_where_every_session_asks():
     """steady_frames_per_s: frames completed between the last session's first
