@@ -3,6 +3,7 @@ import ctypes
 import os
 import re
 import struct
+import time
 
 import numpy as np
 import pytest
@@ -237,3 +238,52 @@ def test_png_writer():
     raw = zlib.decompress(png[idat + 4:idat + 4 + n])
     rows = np.frombuffer(raw, np.uint8).reshape(7, 1 + 5 * 4)
     assert (rows[:, 0] == 0).all() and np.array_equal(rows[:, 1:].reshape(7, 5, 4), img)
+
+
+def test_autotuner_stages_keep_only_clear_gains(monkeypatch):
+    """The tuner's stages 1-3 (host logic, timings faked, no GPU): the fastest
+    tile size x depth bins that drops no record, the base constants kept
+    unless a candidate is 3 % faster, then slices and the persistent CTA
+    count each kept only when 3 % faster than the choice so far."""
+    from hairfb import autotune as AT
+
+    class FakeCtx:
+        def __init__(self, cfg, device):
+            self.cfg = cfg
+
+        def set_stream(self, s):
+            pass
+
+        def close(self):
+            pass
+
+    class FakeRenderer:
+        def use_config(self, cfg, ctx):
+            self.cfg = cfg
+
+    def fake_time(cfg):
+        table = {(16, 8): (10.0, 0), (8, 4): (9.0, 0), (8, 8): (9.9, 0), (32, 4): (5.0, 7)}  # 32 px drops records
+        ms, dropped = table.get((cfg.tileSize, cfg.tileDepthBins), (12.0, 0))  # the context's C config
+        if cfg.slicesPerPixel == 2:
+            ms *= 0.99  # 1 %: not kept
+        if cfg.processorCount == 512:
+            ms *= 0.9   # 10 %: kept
+        return ms, dropped
+
+    monkeypatch.setattr(AT, "Context", FakeCtx)
+    monkeypatch.setattr(AT, "time_batch", lambda rs, ctx, stream, frames, warmup: fake_time(ctx.cfg))
+    monkeypatch.setattr(AT.torch.cuda, "synchronize", lambda *a: None)
+    base = HairConfig(tile_size=16, tile_depth_bins=8, slices_per_pixel=4)
+    rs = [FakeRenderer(), FakeRenderer()]
+    trials = []
+    ms, cfg, ctx = AT._tune_config(rs, base, 0, None, (8, 16, 32), (4, 8), (2, 4, 8), (0, 512), 2, 1,
+                                   time.perf_counter() + 60.0, "all", trials)
+    assert (cfg.tile_size, cfg.tile_depth_bins, cfg.slices_per_pixel, cfg.processor_count) == (8, 4, 4, 512)
+    assert abs(ms - 9.0 * 0.9) < 1e-9 and all(r.cfg == cfg for r in rs)
+    assert len(trials) == 6 + 2 + 1  # the grid, two other slice counts, one other CTA count
+    # a winner within 3 % of the base constants leaves the base in place
+    monkeypatch.setattr(AT, "time_batch", lambda rs, ctx, stream, frames, warmup:
+                        (9.8 if (ctx.cfg.tileSize, ctx.cfg.tileDepthBins) == (8, 4) else 10.0, 0))
+    ms, cfg, ctx = AT._tune_config(rs, base, 0, None, (8, 16), (4, 8), (4,), (0,), 2, 1,
+                                   time.perf_counter() + 60.0, "all", [])
+    assert (cfg.tile_size, cfg.tile_depth_bins) == (16, 8) and ms == 10.0
