@@ -71,7 +71,6 @@ def test_tick_takes_the_oldest_requests_one_per_session_within_the_budget():
     assert serve.Server._form(fake, [ready[2], ready[3]]) == []
 
 
-@pytest.mark.gpu
 def test_steady_rate_counts_the_window_where_every_session_asks():
     """steady_frames_per_s: frames completed between the last session's first
     request and the first session's last frame, per second of that window."""
@@ -89,6 +88,7 @@ def test_steady_rate_counts_the_window_where_every_session_asks():
     assert st.steady_frames_per_s == 0.0 and st.steady_pct(0.99) == 0.0
 
 
+@pytest.mark.gpu
 def test_served_sessions_equal_sessions_alone():
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
